@@ -1,0 +1,78 @@
+/*
+ * lns3d_gb300 -- C ABI of the GB300 (sm_103a) implicit ADI line solvers.
+ *
+ * Each entry point is the drop-in for one reference Fortran solver of the
+ * LNS3D implicit step and keeps its argument order, sizes and array layouts
+ * (Fortran column-major, complex as interleaved (re, im) doubles, i.e.
+ * complex*16).  A Fortran host binds them through iso_c_binding with VALUE
+ * integer arguments and assumed-size arrays.
+ *
+ * Two forms per solver:
+ *   lns_<name>      host pointers: the arrays are staged to the GPU, solved
+ *                   and copied back; synchronous, like the Fortran call.
+ *   lns_<name>_dev  device pointers: enqueued on `stream` (a cudaStream_t,
+ *                   NULL for the legacy default stream); asynchronous.
+ *
+ * Block size: nblk must be 5 (ndof, src/global.f90).  Lines need n >= 7
+ * rows (the boundary-closure rows 1, 2, n-4..n must be distinct; the
+ * reference itself has no such check and silently mis-solves shorter lines).
+ *
+ * Return value: LNS_OK, or an LNS_ERR_* code; lns_last_error() describes the
+ * last failure of the calling thread.  The reference has no error return; it
+ * produces Inf/NaN on a zero pivot, which the GPU path reports as
+ * LNS_ERR_PIVOT (the arrays then hold the same non-finite values).
+ */
+#ifndef LNS3D_GB300_H
+#define LNS3D_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LNS_OK 0
+#define LNS_ERR_ARG 1      /* invalid size, nblk != 5, bad code or flag */
+#define LNS_ERR_CUDA 2     /* CUDA runtime failure (message in lns_last_error) */
+#define LNS_ERR_PIVOT 3    /* a pivot became zero or non-finite */
+#define LNS_ERR_NOMEM 4    /* device allocation failed */
+
+/* Last error message of the calling thread ("" if none). */
+const char* lns_last_error(void);
+/* Library version string. */
+const char* lns_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Real block-pentadiagonal solves with the 4th-order boundary-closure rows,
+ * single pass (factor + solve).  mat is scratch on return (its content is
+ * unspecified, as in the reference); rhs returns the solution.
+ */
+/* replaces src/penta2bc.f:2  penta2bc(n, nsys, nblk, mat(5,nblk,nblk,n,nsys), rhs(nblk,n,nsys)) */
+int lns_penta2bc(int32_t n, int32_t nsys, int32_t nblk, double* mat, double* rhs);
+int lns_penta2bc_dev(int32_t n, int32_t nsys, int32_t nblk, double* mat, double* rhs, void* stream);
+/* replaces src/penta1bc.f:2  penta1bc(nsys, n, nblk, mat(5,nblk,nblk,nsys,n), rhs(nblk,nsys,n)) */
+int lns_penta1bc(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs);
+int lns_penta1bc_dev(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Complex boundary-closure solves with the LU / solve split.
+ * code 0: factor mat in place (multipliers stored where entries are
+ * eliminated, as the reference); 1: solve rhs with a factored mat; 2: both.
+ * The solve phase applies the row n-3 -> n-1 update that the reference
+ * mis-indexes (src/cpenta1bc.f:675, src/cpenta2bc.f:676), i.e. it solves the
+ * factored system exactly.
+ */
+/* replaces src/cpenta2bc.f:2  cpenta2bc(n, nsys, nblk, mat, rhs, code) */
+int lns_cpenta2bc(int32_t n, int32_t nsys, int32_t nblk, double* mat, double* rhs, int32_t code);
+int lns_cpenta2bc_dev(int32_t n, int32_t nsys, int32_t nblk, double* mat, double* rhs, int32_t code,
+                      void* stream);
+/* replaces src/cpenta1bc.f:2  cpenta1bc(nsys, n, nblk, mat, rhs, code) */
+int lns_cpenta1bc(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs, int32_t code);
+int lns_cpenta1bc_dev(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs, int32_t code,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LNS3D_GB300_H */

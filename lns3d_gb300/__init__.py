@@ -1,0 +1,10 @@
+"""lns3d_gb300: GB300-native implicit ADI line solvers of LNS3D.
+
+The compute path is the sm_103a C-ABI library ``lib/liblns3d_gb300.so``
+(``include/lns3d_gb300.h``); this package is its host-side mirror with the
+reference's solver names and argument conventions.
+"""
+from ._lib import LnsError, lib, library_path
+from .penta import cpenta1bc, cpenta2bc, penta1bc, penta2bc
+
+__all__ = ["LnsError", "lib", "library_path", "penta2bc", "penta1bc", "cpenta2bc", "cpenta1bc"]

@@ -1,0 +1,64 @@
+"""ctypes binding of lib/liblns3d_gb300.so (the C ABI in include/lns3d_gb300.h).
+
+The library is the only compute path: importing this module fails loudly
+when it has not been built, and nothing here falls back to CPU code.
+"""
+import ctypes
+import os
+
+from ._build import LIBDIR, LIBNAME
+
+LNS_OK, LNS_ERR_ARG, LNS_ERR_CUDA, LNS_ERR_PIVOT, LNS_ERR_NOMEM = 0, 1, 2, 3, 4
+_NAMES = {1: "LNS_ERR_ARG", 2: "LNS_ERR_CUDA", 3: "LNS_ERR_PIVOT", 4: "LNS_ERR_NOMEM"}
+
+
+class LnsError(RuntimeError):
+    """A non-zero status returned by the C ABI."""
+
+    def __init__(self, code, where, message):
+        self.code = code
+        super().__init__("%s failed with %s: %s" % (where, _NAMES.get(code, code), message))
+
+
+def library_path():
+    return os.path.join(LIBDIR, LIBNAME)
+
+
+_lib = None
+I32, P, DP = ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p
+
+# name -> argument types (all return int)
+SIGNATURES = {
+    "lns_penta2bc": [I32, I32, I32, DP, DP],
+    "lns_penta2bc_dev": [I32, I32, I32, DP, DP, P],
+    "lns_penta1bc": [I32, I32, I32, DP, DP],
+    "lns_penta1bc_dev": [I32, I32, I32, DP, DP, P],
+    "lns_cpenta2bc": [I32, I32, I32, DP, DP, I32],
+    "lns_cpenta2bc_dev": [I32, I32, I32, DP, DP, I32, P],
+    "lns_cpenta1bc": [I32, I32, I32, DP, DP, I32],
+    "lns_cpenta1bc_dev": [I32, I32, I32, DP, DP, I32, P],
+}
+
+
+def lib():
+    """Load (once) and return the C-ABI library; raise if it is not built."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise ImportError("lns3d_gb300: %s is not built; run __graft_entry__.build() or "
+                              "python -m lns3d_gb300._build" % path)
+        L = ctypes.CDLL(path)
+        L.lns_last_error.restype = ctypes.c_char_p
+        L.lns_version.restype = ctypes.c_char_p
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def check(rc, where):
+    if rc != LNS_OK:
+        raise LnsError(rc, where, lib().lns_last_error().decode())

@@ -1,0 +1,93 @@
+"""Host-side mirror of the reference line-solver interface.
+
+The functions keep the Fortran names, argument order and array layouts of
+the LNS3D solvers (src/penta2bc.f:2, src/penta1bc.f:2, src/cpenta2bc.f:2,
+src/cpenta1bc.f:2): ``mat`` and ``rhs`` are flat buffers holding the Fortran
+column-major arrays ``mat(5,nblk,nblk,n,nsys)`` / ``rhs(nblk,n,nsys)`` (the
+"2" solvers) or ``mat(5,nblk,nblk,nsys,n)`` / ``rhs(nblk,nsys,n)`` (the "1"
+solvers), real float64 or complex128.  They are updated in place, like the
+Fortran INOUT arguments.
+
+``mat``/``rhs`` may be numpy arrays (host memory: the call stages them to the
+GPU and back, synchronously) or CUDA torch tensors (device memory: the solve
+is enqueued on torch's current stream).  Every call runs the sm_103a kernels
+of ``lib/liblns3d_gb300.so``; errors raise :class:`LnsError` (the reference
+has no error return and leaves Inf/NaN on a zero pivot).
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import LnsError, check, lib
+
+__all__ = ["penta2bc", "penta1bc", "cpenta2bc", "cpenta1bc", "LnsError"]
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _buf(a, complex_, count, name):
+    """Pointer to a contiguous buffer of `count` elements; (ptr, is_device)."""
+    if _is_torch(a):
+        import torch
+
+        want = torch.complex128 if complex_ else torch.float64
+        if a.dtype != want:
+            raise TypeError("%s must be %s, got %s" % (name, want, a.dtype))
+        if not a.is_contiguous():
+            raise ValueError("%s must be contiguous" % name)
+        if a.numel() < count:
+            raise ValueError("%s holds %d elements, needs %d" % (name, a.numel(), count))
+        return ctypes.c_void_p(a.data_ptr()), a.is_cuda
+    want = np.complex128 if complex_ else np.float64
+    if not isinstance(a, np.ndarray) or a.dtype != want:
+        raise TypeError("%s must be a numpy %s array" % (name, np.dtype(want).name))
+    if not (a.flags.c_contiguous or a.flags.f_contiguous):
+        raise ValueError("%s must be contiguous" % name)
+    if a.size < count:
+        raise ValueError("%s holds %d elements, needs %d" % (name, a.size, count))
+    if not a.flags.writeable:
+        raise ValueError("%s must be writeable" % name)
+    return ctypes.c_void_p(a.ctypes.data), False
+
+
+def _stream():
+    import torch
+
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _call(name, dims, nblk, mat, rhs, complex_, code=None):
+    n_rows = dims[0] * dims[1]
+    pm, dev_m = _buf(mat, complex_, 125 * n_rows, "mat")
+    pr, dev_r = _buf(rhs, complex_, 5 * n_rows, "rhs")
+    if dev_m != dev_r:
+        raise ValueError("mat and rhs must both be host arrays or both CUDA tensors")
+    L = lib()
+    extra = [] if code is None else [int(code)]
+    if dev_m:
+        rc = getattr(L, "lns_%s_dev" % name)(dims[0], dims[1], nblk, pm, pr, *extra, _stream())
+    else:
+        rc = getattr(L, "lns_%s" % name)(dims[0], dims[1], nblk, pm, pr, *extra)
+    check(rc, name)
+
+
+def penta2bc(n, nsys, nblk, mat, rhs):
+    """Real boundary-closure solve, lines along the first spatial index."""
+    _call("penta2bc", (n, nsys), nblk, mat, rhs, False)
+
+
+def penta1bc(nsys, n, nblk, mat, rhs):
+    """Real boundary-closure solve, lines along the second spatial index."""
+    _call("penta1bc", (nsys, n), nblk, mat, rhs, False)
+
+
+def cpenta2bc(n, nsys, nblk, mat, rhs, code):
+    """Complex boundary-closure solve; code 0 factor, 1 solve, 2 both."""
+    _call("cpenta2bc", (n, nsys), nblk, mat, rhs, True, code)
+
+
+def cpenta1bc(nsys, n, nblk, mat, rhs, code):
+    """Complex boundary-closure solve (lines batched over the first index)."""
+    _call("cpenta1bc", (nsys, n), nblk, mat, rhs, True, code)

@@ -1,0 +1,89 @@
+"""CPU tests of the C-ABI library: it loads, exports every declared entry
+point, and validates arguments before touching a GPU."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names.update(re.findall(r"\b(lns_\w+)\s*\(", src))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import lns3d_gb300
+
+    return lns3d_gb300.lib()
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for base in ("penta2bc", "penta1bc", "cpenta2bc", "cpenta1bc"):
+        assert "lns_" + base in names and "lns_" + base + "_dev" in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_header():
+    from lns3d_gb300._lib import SIGNATURES
+
+    solver_syms = [n for n in declared_symbols() if n not in ("lns_last_error", "lns_version")]
+    assert sorted(SIGNATURES) == solver_syms
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.lns_version()
+
+
+@pytest.mark.parametrize("name,args", [
+    ("lns_penta2bc", (7, 1, 4)),      # nblk must be 5
+    ("lns_penta2bc", (6, 1, 5)),      # too few rows
+    ("lns_penta1bc", (-1, 8, 5)),     # negative nsys
+    ("lns_penta1bc", (1, 3, 5)),
+])
+def test_argument_errors_real(lib, name, args):
+    a = np.zeros(125 * 64)
+    rc = getattr(lib, name)(*args, a.ctypes.data, a.ctypes.data)
+    assert rc == 1
+    assert lib.lns_last_error()
+
+
+@pytest.mark.parametrize("code", [-1, 3])
+def test_argument_errors_code(lib, code):
+    a = np.zeros(2 * 125 * 64)
+    for name in ("lns_cpenta2bc", "lns_cpenta1bc"):
+        assert getattr(lib, name)(8, 8, 5, a.ctypes.data, a.ctypes.data, code) == 1
+        assert b"code" in lib.lns_last_error()
+
+
+def test_python_mirror_type_checks():
+    import lns3d_gb300 as g
+
+    with pytest.raises(TypeError):
+        g.penta2bc(8, 1, 5, np.zeros(125 * 8, np.float32), np.zeros(40))
+    with pytest.raises(ValueError):
+        g.penta2bc(8, 1, 5, np.zeros(10), np.zeros(40))
+    with pytest.raises(g.LnsError) as e:
+        g.penta2bc(8, 1, 4, np.zeros(125 * 8), np.zeros(40))
+    assert e.value.code == 1
+
+
+def test_zero_lines_is_a_no_op():
+    import lns3d_gb300 as g
+
+    # nsys = 0 is valid and launches nothing (no GPU needed)
+    g.penta2bc(8, 0, 5, np.zeros(1), np.zeros(1))
