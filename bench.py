@@ -46,7 +46,6 @@ BYTES_PER_PT = 2 * 2000 + 2 * 80
 # algorithmic FP64 flops per grid point (complex multiply-add = 8 flops):
 # in-block LU 140, multipliers 150, Schur update 550, back substitution 60
 FLOPS_PER_PT = 8 * (140 + 150 + 550 + 60)
-FP64_PEAK_TFLOPS = 1.19  # measured DFMA rate on this GPU (profiles/fp64_peak_gb300.txt)
 
 
 def env_rank():
@@ -154,6 +153,38 @@ def time_reference_cpu(sample_reps=3):
                       % (sample_reps, t * 1e3)}
 
 
+def run_e2e(torch, dev, L, rank, world, K):
+    """Steps through the host-pointer entry point lns_cpenta2bc: each step
+    copies the step's matrix and right-hand side from pinned host memory to
+    the device, solves, and copies the factored matrix, the solution and the
+    status word back."""
+    host_mat = torch.empty(MAT_EL, dtype=torch.complex128).pin_memory()
+    host_rhs = torch.empty(RHS_EL, dtype=torch.complex128).pin_memory()
+    src = [make_batch(torch, dev, 50000 + 1000 * rank + s) for s in range(2)]
+    host_src = [(m.cpu().pin_memory(), r.cpu().pin_memory()) for m, r in src]
+    del src
+    ke = max(2, min(K, 5))
+
+    def e2e_step(s):
+        m, r = host_src[s % 2]
+        host_mat.copy_(m)
+        host_rhs.copy_(r)
+        t = time.perf_counter()
+        rc = L.lns_cpenta2bc(N_ROWS, N_LINES, 5, ctypes.c_void_p(host_mat.data_ptr()),
+                             ctypes.c_void_p(host_rhs.data_ptr()), 2)
+        if rc:
+            raise RuntimeError(L.lns_last_error().decode())
+        return time.perf_counter() - t
+
+    e2e_step(0)
+    t = [e2e_step(s) for s in range(ke)]
+    if world > 1:
+        tt = torch.tensor([max(t)], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        return world * PTS / float(tt.item())
+    return PTS / statistics.mean(t)
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -185,6 +216,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer end-to-end leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -251,29 +283,10 @@ def main():
     del batches
 
     # end to end: host-pointer C-ABI call from pinned host memory
-    host_mat = torch.empty(MAT_EL, dtype=torch.complex128).pin_memory()
-    host_rhs = torch.empty(RHS_EL, dtype=torch.complex128).pin_memory()
-    src = [make_batch(torch, dev, 50000 + 1000 * rank + s) for s in range(2)]
-    host_src = [(m.cpu().pin_memory(), r.cpu().pin_memory()) for m, r in src]
-    del src
-    KE = max(2, min(K, 5))
-
-    def e2e_step(s):
-        m, r = host_src[s % 2]
-        host_mat.copy_(m)
-        host_rhs.copy_(r)
-        t = time.perf_counter()
-        rc = L.lns_cpenta2bc(N_ROWS, N_LINES, 5, ctypes.c_void_p(host_mat.data_ptr()),
-                             ctypes.c_void_p(host_rhs.data_ptr()), 2)
-        if rc:
-            raise RuntimeError(L.lns_last_error().decode())
-        return time.perf_counter() - t
-
-    e2e_step(0)
-    e2e_t = [e2e_step(s) for s in range(KE)]
-    e2e_value = world * PTS / statistics.mean(e2e_t)
+    e2e_value = None if args.no_e2e else run_e2e(torch, dev, L, rank, world, K)
 
     hbm_peak, peak_kind = peaks()
+    fp64_peak = L.lns_probe_fp64_tflops()  # measured live on this GPU
     achieved = BYTES_PER_PT * PTS / (kern_ms / 1e3) / 1e9
     fp64_achieved = FLOPS_PER_PT * PTS / (kern_ms / 1e3) / 1e12
     cpu = None
@@ -290,16 +303,18 @@ def main():
                        "l2": "inputs larger than L2 (262 MB matrix per step, fresh batch each step)"},
             "latency_ms": {"p50": per_step[len(per_step) // 2],
                            "p99": per_step[min(len(per_step) - 1, int(round(0.99 * (len(per_step) - 1))))]},
-            "e2e": {"value": e2e_value, "unit": "grid-pt/s",
-                    "h2d_bytes_per_step": (MAT_EL + RHS_EL) * CPLX,
-                    "d2h_bytes_per_step": (MAT_EL + RHS_EL) * CPLX + 4},
+            "e2e": None if e2e_value is None else {
+                "value": e2e_value, "unit": "grid-pt/s",
+                "h2d_bytes_per_step": (MAT_EL + RHS_EL) * CPLX,
+                "d2h_bytes_per_step": (MAT_EL + RHS_EL) * CPLX + 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": None,
                          "peak_source": peak_kind, "kernel": "penta_bc_kernel<cd>",
                          "bytes_per_pt": BYTES_PER_PT},
-            "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": FP64_PEAK_TFLOPS,
-                              "unit": "TFLOP/s", "frac": fp64_achieved / FP64_PEAK_TFLOPS,
-                              "flops_per_pt": FLOPS_PER_PT, "peak_source": "measured DFMA probe"},
+            "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak,
+                              "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak,
+                              "flops_per_pt": FLOPS_PER_PT,
+                              "peak_source": "measured live: DFMA stream on every SM (lns_probe_fp64_tflops)"},
             "cpu_baseline": cpu,
             "gpu_launches": K,
             "clocks": clocks,

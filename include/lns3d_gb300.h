@@ -41,6 +41,11 @@ extern "C" {
 const char* lns_last_error(void);
 /* Library version string. */
 const char* lns_version(void);
+/* Measured FP64 fused multiply-add rate of the current device in TFLOP/s
+ * (a short DFMA stream on every SM); the denominator of the FP64 roofline
+ * that the line solvers are reported against.  No reference counterpart.
+ * Returns a negative value on failure. */
+double lns_probe_fp64_tflops(void);
 
 /* ---------------------------------------------------------------------------
  * Real block-pentadiagonal solves with the 4th-order boundary-closure rows,
@@ -70,6 +75,44 @@ int lns_cpenta2bc_dev(int32_t n, int32_t nsys, int32_t nblk, double* mat, double
 int lns_cpenta1bc(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs, int32_t code);
 int lns_cpenta1bc_dev(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs, int32_t code,
                       void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Periodic solves.  np = n + 1 rows per line, n unknowns; on return row np
+ * of rhs repeats row 1 (src/penta2p.f:749-751).  per(2,nblk,nblk,np,nsys)
+ * ("2" solvers; (2,nblk,nblk,nsys,np) for the "1" solvers) receives the fill
+ * of columns n-1, n.  Real solvers: single pass, per is scratch and per2 --
+ * the reference's (6,nblk,nblk,nsys) scratch -- is not touched.  Complex
+ * solvers: code as for the boundary solvers, and per and
+ * per2(np-2:np-1,nblk,nblk,np,nsys) (or (...,nsys,np)) hold the factored
+ * fill between a code 0 and a code 1 call, in the reference's format.
+ *
+ * By default the factorisation reproduces the reference exactly, including
+ * its placement of one fill block at row n-5 (src/penta2p.f:278,339 and the
+ * same statements in penta1p.f, cpenta1p.f, cpenta2p.f), which makes the
+ * reference solve a slightly different system whose error decays with the
+ * line length.  lns_set_periodic_exact(1) switches every later periodic
+ * factorisation of the process to the exact LU; lns_set_periodic_exact(0)
+ * restores the reference behaviour.
+ */
+int lns_set_periodic_exact(int32_t on);
+/* replaces src/penta2p.f:2  penta2p(np, nsys, nblk, mat, rhs, per, per2) */
+int lns_penta2p(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per, double* per2);
+int lns_penta2p_dev(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per,
+                    double* per2, void* stream);
+/* replaces src/penta1p.f:2  penta1p(nsys, np, nblk, mat, rhs, per, per2) */
+int lns_penta1p(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per, double* per2);
+int lns_penta1p_dev(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per,
+                    double* per2, void* stream);
+/* replaces src/cpenta2p.f:2  cpenta2p(np, nsys, nblk, mat, rhs, per, per2, code) */
+int lns_cpenta2p(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per, double* per2,
+                 int32_t code);
+int lns_cpenta2p_dev(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per,
+                     double* per2, int32_t code, void* stream);
+/* replaces src/cpenta1p.f:2  cpenta1p(nsys, np, nblk, mat, rhs, per, per2, code) */
+int lns_cpenta1p(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per, double* per2,
+                 int32_t code);
+int lns_cpenta1p_dev(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per,
+                     double* per2, int32_t code, void* stream);
 
 #ifdef __cplusplus
 }

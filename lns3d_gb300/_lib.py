@@ -37,6 +37,15 @@ SIGNATURES = {
     "lns_cpenta2bc_dev": [I32, I32, I32, DP, DP, I32, P],
     "lns_cpenta1bc": [I32, I32, I32, DP, DP, I32],
     "lns_cpenta1bc_dev": [I32, I32, I32, DP, DP, I32, P],
+    "lns_set_periodic_exact": [I32],
+    "lns_penta2p": [I32, I32, I32, DP, DP, DP, DP],
+    "lns_penta2p_dev": [I32, I32, I32, DP, DP, DP, DP, P],
+    "lns_penta1p": [I32, I32, I32, DP, DP, DP, DP],
+    "lns_penta1p_dev": [I32, I32, I32, DP, DP, DP, DP, P],
+    "lns_cpenta2p": [I32, I32, I32, DP, DP, DP, DP, I32],
+    "lns_cpenta2p_dev": [I32, I32, I32, DP, DP, DP, DP, I32, P],
+    "lns_cpenta1p": [I32, I32, I32, DP, DP, DP, DP, I32],
+    "lns_cpenta1p_dev": [I32, I32, I32, DP, DP, DP, DP, I32, P],
 }
 
 
@@ -51,6 +60,8 @@ def lib():
         L = ctypes.CDLL(path)
         L.lns_last_error.restype = ctypes.c_char_p
         L.lns_version.restype = ctypes.c_char_p
+        L.lns_probe_fp64_tflops.restype = ctypes.c_double
+        L.lns_probe_fp64_tflops.argtypes = []
         for name, args in SIGNATURES.items():
             fn = getattr(L, name)
             fn.argtypes = args

@@ -8,11 +8,16 @@
 
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
+#include <type_traits>
 
 #include "../../include/lns3d_gb300.h"
 #include "penta_direct.cuh"
+#include "penta_periodic.cuh"
+#include "mixed.cuh"
 
 namespace {
 
@@ -119,9 +124,291 @@ int host_bc(double* mat, double* rhs, int n, int nsys, long long row_stride, lon
   return LNS_OK;
 }
 
+std::atomic<int> g_periodic_exact{0};
+
+template <typename T>
+int launch_p(void* mat, void* rhs, void* per, void* per2, int np, int nsys, long long row_stride,
+             long long line_stride, int code, cudaStream_t st, int* status, int exact = -1) {
+  if (nsys == 0) return LNS_OK;
+  const bool cplx = std::is_same<T, lns::cd>::value || std::is_same<T, lns::cf>::value;
+  const int compat = exact < 0 ? (g_periodic_exact.load() ? 0 : 1) : (exact ? 0 : 1);
+  lns::PeriodicArgs a{mat, rhs, per, per2, np - 1, np, nsys, row_stride, line_stride, code,
+                      compat, cplx ? 1 : 0, status};
+  const int blocks = (nsys + lns::kPWarpsPerCta - 1) / lns::kPWarpsPerCta;
+  const size_t smem = (size_t)lns::kPWarpsPerCta * lns::kPWarpSmem * sizeof(T);
+  lns::penta_p_kernel<T><<<blocks, 32 * lns::kPWarpsPerCta, smem, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "penta_p_kernel launch");
+  return LNS_OK;
+}
+
+template <typename T>
+int host_p(double* mat, double* rhs, double* per, double* per2, int np, int nsys, long long row_stride,
+           long long line_stride, int code) {
+  if (nsys == 0) return LNS_OK;
+  const bool cplx = sizeof(T) == 16;
+  std::lock_guard<std::mutex> lock(g_stage.mu);
+  const size_t mat_b = (size_t)125 * np * nsys * sizeof(T);
+  const size_t rhs_b = (size_t)5 * np * nsys * sizeof(T);
+  const size_t per_b = (size_t)50 * np * nsys * sizeof(T);
+  void *dm, *dr, *dp, *dp2 = nullptr;
+  int rc = stage_get(0, mat_b, &dm);
+  if (!rc) rc = stage_get(1, rhs_b, &dr);
+  if (!rc) rc = stage_get(2, per_b, &dp);
+  if (!rc && cplx) rc = stage_get(3, per_b, &dp2);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(dm, mat, mat_b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && code != 0) e = cudaMemcpy(dr, rhs, rhs_b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && code == 1) e = cudaMemcpy(dp, per, per_b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && code == 1 && cplx) e = cudaMemcpy(dp2, per2, per_b, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "copy to device");
+  e = cudaMemset(g_stage.status, 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+  rc = launch_p<T>(dm, dr, dp, dp2, np, nsys, row_stride, line_stride, code, 0, g_stage.status);
+  if (rc) return rc;
+  if (cplx && code != 1) {
+    e = cudaMemcpy(mat, dm, mat_b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(per, dp, per_b, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(per2, dp2, per_b, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "copy factors to host");
+  }
+  if (code != 0) {
+    e = cudaMemcpy(rhs, dr, rhs_b, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "copy rhs to host");
+  }
+  int status = 0;
+  e = cudaMemcpy(&status, g_stage.status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "copy status to host");
+  if (status) return fail(LNS_ERR_PIVOT, "zero or non-finite pivot");
+  return LNS_OK;
+}
+
+// ---------------------------------------------------------------- mixed
+// Workspace of a mixed-precision solve of `rows` x `nsys` block rows:
+// FP32 matrix factors, FP32 periodic fill (per, per2), FP32 residual /
+// correction, FP64 iterate.
+struct MixedLayout {
+  size_t w, per, per2, r, x, total;
+};
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+MixedLayout mixed_layout(int rows, int nsys, bool cplx, bool periodic) {
+  const size_t el32 = cplx ? 8 : 4, el64 = cplx ? 16 : 8, rs = (size_t)rows * nsys;
+  MixedLayout L{};
+  size_t off = 0;
+  L.w = off; off += align256(125 * rs * el32);
+  L.per = off; off += periodic ? align256(50 * rs * el32) : 0;
+  L.per2 = off; off += periodic ? align256(50 * rs * el32) : 0;
+  L.r = off; off += align256(5 * rs * el32);
+  L.x = off; off += align256(5 * rs * el64);
+  L.total = off;
+  return L;
+}
+
+int grid_for(long long n) {
+  long long b = (n + 255) / 256;
+  return (int)std::min<long long>(std::max<long long>(b, 1), 152 * 32);
+}
+
+// code 0: factor (FP32) into work; 1: solve with `refine` FP64 refinement
+// steps; 2: both.  mat is read only.
+template <typename TH, typename TL>
+int mixed_solve(const double* mat, double* rhs, int rows, int nsys, long long row_stride, long long line_stride,
+                bool periodic, int code, int refine, void* work, cudaStream_t st) {
+  if (nsys == 0) return LNS_OK;
+  const bool cplx = std::is_same<TH, lns::cd>::value;
+  const MixedLayout Lw = mixed_layout(rows, nsys, cplx, periodic);
+  char* wb = reinterpret_cast<char*>(work);
+  TL* W = reinterpret_cast<TL*>(wb + Lw.w);
+  TL* P = reinterpret_cast<TL*>(wb + Lw.per);
+  TL* P2 = reinterpret_cast<TL*>(wb + Lw.per2);
+  TL* R = reinterpret_cast<TL*>(wb + Lw.r);
+  TH* X = reinterpret_cast<TH*>(wb + Lw.x);
+  const long long nmat = 125LL * rows * nsys, nrhs = 5LL * rows * nsys;
+  const int n = periodic ? rows - 1 : rows;
+  int rc = LNS_OK;
+  cudaError_t e;
+  if (code != 1) {
+    lns::narrow_kernel<TH, TL><<<grid_for(nmat), 256, 0, st>>>(reinterpret_cast<const TH*>(mat), W, nmat);
+    rc = periodic ? launch_p<TL>(W, R, P, P2, rows, nsys, row_stride, line_stride, 0, st, nullptr, 1)
+                  : launch_bc<TL>(W, R, rows, nsys, row_stride, line_stride, 0, st, nullptr);
+    if (rc) return rc;
+  }
+  if (code != 0) {
+    lns::narrow_kernel<TH, TL><<<grid_for(nrhs), 256, 0, st>>>(reinterpret_cast<const TH*>(rhs), R, nrhs);
+    for (int it = 0; it <= refine; ++it) {
+      if (it > 0) {
+        lns::ResidualArgs ra{mat, rhs, X, R, n, rows, nsys, row_stride, line_stride, periodic ? 1 : 0};
+        const long long th = 5LL * n * nsys;
+        lns::residual_kernel<TH, TL><<<(unsigned)((th + 255) / 256), 256, 0, st>>>(ra);
+      }
+      rc = periodic ? launch_p<TL>(W, R, P, P2, rows, nsys, row_stride, line_stride, 1, st, nullptr, 1)
+                    : launch_bc<TL>(W, R, rows, nsys, row_stride, line_stride, 1, st, nullptr);
+      if (rc) return rc;
+      lns::widen_add_kernel<TH, TL><<<grid_for(nrhs), 256, 0, st>>>(X, R, nrhs, it == 0 ? 1 : 0);
+    }
+    e = cudaMemcpyAsync(rhs, X, nrhs * sizeof(TH), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "mixed solve copy-out");
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "mixed solve launch");
+  return LNS_OK;
+}
+
+// Host-pointer form of the mixed solve (factor + solve), staged like host_bc.
+template <typename TH, typename TL>
+int host_mixed(const double* mat, double* rhs, int rows, int nsys, long long row_stride, long long line_stride,
+               bool periodic, int refine) {
+  if (nsys == 0) return LNS_OK;
+  std::lock_guard<std::mutex> lock(g_stage.mu);
+  const bool cplx = std::is_same<TH, lns::cd>::value;
+  const size_t mat_b = (size_t)125 * rows * nsys * sizeof(TH);
+  const size_t rhs_b = (size_t)5 * rows * nsys * sizeof(TH);
+  const size_t work_b = mixed_layout(rows, nsys, cplx, periodic).total;
+  void *dm, *dr, *dw;
+  int rc = stage_get(0, mat_b, &dm);
+  if (!rc) rc = stage_get(1, rhs_b, &dr);
+  if (!rc) rc = stage_get(2, work_b, &dw);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(dm, mat, mat_b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dr, rhs, rhs_b, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "copy to device");
+  rc = mixed_solve<TH, TL>(reinterpret_cast<const double*>(dm), reinterpret_cast<double*>(dr), rows, nsys,
+                           row_stride, line_stride, periodic, 2, refine, dw, 0);
+  if (rc) return rc;
+  e = cudaMemcpy(rhs, dr, rhs_b, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "copy rhs to host");
+  return LNS_OK;
+}
+
+int check_mixed(int code, int refine, const char* who) {
+  if (code < 0 || code > 2) return fail(LNS_ERR_ARG, std::string(who) + ": code must be 0, 1 or 2");
+  if (refine < 0 || refine > 16) return fail(LNS_ERR_ARG, std::string(who) + ": refine must be 0..16");
+  return LNS_OK;
+}
+
+int check_p(int np, int nsys, int nblk, const char* who) {
+  if (nblk != 5) return fail(LNS_ERR_ARG, std::string(who) + ": nblk must be 5");
+  if (np < 8) return fail(LNS_ERR_ARG, std::string(who) + ": periodic lines need np >= 8");
+  if (nsys < 0) return fail(LNS_ERR_ARG, std::string(who) + ": nsys < 0");
+  return LNS_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+size_t lns_mixed_workspace_bytes(int32_t rows, int32_t nsys, int32_t is_complex, int32_t periodic) {
+  if (rows <= 0 || nsys < 0) return 0;
+  return mixed_layout(rows, nsys, is_complex != 0, periodic != 0).total;
+}
+
+int lns_cpenta2bc_mixed_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                            int32_t refine, void* work, void* stream) {
+  int rc = check_sizes(n, nsys, nblk, "cpenta2bc_mixed");
+  if (!rc) rc = check_mixed(code, refine, "cpenta2bc_mixed");
+  if (rc) return rc;
+  return mixed_solve<lns::cd, lns::cf>(mat, rhs, n, nsys, 1, n, false, code, refine, work, (cudaStream_t)stream);
+}
+int lns_cpenta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                            int32_t refine, void* work, void* stream) {
+  int rc = check_sizes(n, nsys, nblk, "cpenta1bc_mixed");
+  if (!rc) rc = check_mixed(code, refine, "cpenta1bc_mixed");
+  if (rc) return rc;
+  return mixed_solve<lns::cd, lns::cf>(mat, rhs, n, nsys, nsys, 1, false, code, refine, work, (cudaStream_t)stream);
+}
+int lns_cpenta2p_mixed_dev(int32_t np, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                           int32_t refine, void* work, void* stream) {
+  int rc = check_p(np, nsys, nblk, "cpenta2p_mixed");
+  if (!rc) rc = check_mixed(code, refine, "cpenta2p_mixed");
+  if (rc) return rc;
+  return mixed_solve<lns::cd, lns::cf>(mat, rhs, np, nsys, 1, np, true, code, refine, work, (cudaStream_t)stream);
+}
+int lns_cpenta1p_mixed_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                           int32_t refine, void* work, void* stream) {
+  int rc = check_p(np, nsys, nblk, "cpenta1p_mixed");
+  if (!rc) rc = check_mixed(code, refine, "cpenta1p_mixed");
+  if (rc) return rc;
+  return mixed_solve<lns::cd, lns::cf>(mat, rhs, np, nsys, nsys, 1, true, code, refine, work, (cudaStream_t)stream);
+}
+int lns_cpenta2bc_mixed(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine) {
+  int rc = check_sizes(n, nsys, nblk, "cpenta2bc_mixed");
+  if (!rc) rc = check_mixed(2, refine, "cpenta2bc_mixed");
+  if (rc) return rc;
+  return host_mixed<lns::cd, lns::cf>(mat, rhs, n, nsys, 1, n, false, refine);
+}
+int lns_penta2bc_mixed_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine,
+                           void* work, void* stream) {
+  int rc = check_sizes(n, nsys, nblk, "penta2bc_mixed");
+  if (!rc) rc = check_mixed(2, refine, "penta2bc_mixed");
+  if (rc) return rc;
+  return mixed_solve<double, float>(mat, rhs, n, nsys, 1, n, false, 2, refine, work, (cudaStream_t)stream);
+}
+int lns_penta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* mat, double* rhs, int32_t refine,
+                           void* work, void* stream) {
+  int rc = check_sizes(n, nsys, nblk, "penta1bc_mixed");
+  if (!rc) rc = check_mixed(2, refine, "penta1bc_mixed");
+  if (rc) return rc;
+  return mixed_solve<double, float>(mat, rhs, n, nsys, nsys, 1, false, 2, refine, work, (cudaStream_t)stream);
+}
+
+int lns_set_periodic_exact(int32_t on) {
+  if (on != 0 && on != 1) return fail(LNS_ERR_ARG, "lns_set_periodic_exact: 0 or 1");
+  g_periodic_exact.store(on);
+  return LNS_OK;
+}
+
+int lns_penta2p(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per, double* per2) {
+  int rc = check_p(np, nsys, nblk, "penta2p");
+  if (rc) return rc;
+  (void)per2;
+  return host_p<double>(mat, rhs, per, per2, np, nsys, 1, np, 2);
+}
+int lns_penta2p_dev(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per,
+                    double* per2, void* stream) {
+  int rc = check_p(np, nsys, nblk, "penta2p");
+  if (rc) return rc;
+  return launch_p<double>(mat, rhs, per, per2, np, nsys, 1, np, 2, (cudaStream_t)stream, nullptr);
+}
+int lns_penta1p(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per, double* per2) {
+  int rc = check_p(np, nsys, nblk, "penta1p");
+  if (rc) return rc;
+  return host_p<double>(mat, rhs, per, per2, np, nsys, nsys, 1, 2);
+}
+int lns_penta1p_dev(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per,
+                    double* per2, void* stream) {
+  int rc = check_p(np, nsys, nblk, "penta1p");
+  if (rc) return rc;
+  return launch_p<double>(mat, rhs, per, per2, np, nsys, nsys, 1, 2, (cudaStream_t)stream, nullptr);
+}
+int lns_cpenta2p(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per, double* per2,
+                 int32_t code) {
+  int rc = check_p(np, nsys, nblk, "cpenta2p");
+  if (rc) return rc;
+  if (code < 0 || code > 2) return fail(LNS_ERR_ARG, "cpenta2p: code must be 0, 1 or 2");
+  return host_p<lns::cd>(mat, rhs, per, per2, np, nsys, 1, np, code);
+}
+int lns_cpenta2p_dev(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per,
+                     double* per2, int32_t code, void* stream) {
+  int rc = check_p(np, nsys, nblk, "cpenta2p");
+  if (rc) return rc;
+  if (code < 0 || code > 2) return fail(LNS_ERR_ARG, "cpenta2p: code must be 0, 1 or 2");
+  return launch_p<lns::cd>(mat, rhs, per, per2, np, nsys, 1, np, code, (cudaStream_t)stream, nullptr);
+}
+int lns_cpenta1p(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per, double* per2,
+                 int32_t code) {
+  int rc = check_p(np, nsys, nblk, "cpenta1p");
+  if (rc) return rc;
+  if (code < 0 || code > 2) return fail(LNS_ERR_ARG, "cpenta1p: code must be 0, 1 or 2");
+  return host_p<lns::cd>(mat, rhs, per, per2, np, nsys, nsys, 1, code);
+}
+int lns_cpenta1p_dev(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per,
+                     double* per2, int32_t code, void* stream) {
+  int rc = check_p(np, nsys, nblk, "cpenta1p");
+  if (rc) return rc;
+  if (code < 0 || code > 2) return fail(LNS_ERR_ARG, "cpenta1p: code must be 0, 1 or 2");
+  return launch_p<lns::cd>(mat, rhs, per, per2, np, nsys, nsys, 1, code, (cudaStream_t)stream, nullptr);
+}
+
 
 const char* lns_last_error(void) { return g_err.c_str(); }
 const char* lns_version(void) { return "lns3d_gb300 0.1 (sm_103a)"; }

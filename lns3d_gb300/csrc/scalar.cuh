@@ -107,7 +107,9 @@ __device__ __forceinline__ double to_hi(float a) { return (double)a; }
 __device__ __forceinline__ cd to_hi(cf a) { return cd{(double)a.x, (double)a.y}; }
 
 __device__ __forceinline__ bool finite_s(double a) { return isfinite(a); }
+__device__ __forceinline__ bool finite_s(float a) { return isfinite(a); }
 __device__ __forceinline__ bool finite_s(cd a) { return isfinite(a.x) && isfinite(a.y); }
+__device__ __forceinline__ bool finite_s(cf a) { return isfinite(a.x) && isfinite(a.y); }
 
 // Warp shuffles of the scalar types.
 __device__ __forceinline__ double shfl(unsigned mask, double v, int src) { return __shfl_sync(mask, v, src); }

@@ -20,7 +20,8 @@ import numpy as np
 
 from ._lib import LnsError, check, lib
 
-__all__ = ["penta2bc", "penta1bc", "cpenta2bc", "cpenta1bc", "LnsError"]
+__all__ = ["penta2bc", "penta1bc", "cpenta2bc", "cpenta1bc", "penta2p", "penta1p", "cpenta2p", "cpenta1p",
+           "set_periodic_exact", "LnsError"]
 
 
 def _is_torch(a):
@@ -58,18 +59,30 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def _call(name, dims, nblk, mat, rhs, complex_, code=None):
+def _call(name, dims, nblk, mat, rhs, complex_, code=None, per=None, per2=None):
     n_rows = dims[0] * dims[1]
     pm, dev_m = _buf(mat, complex_, 125 * n_rows, "mat")
     pr, dev_r = _buf(rhs, complex_, 5 * n_rows, "rhs")
-    if dev_m != dev_r:
-        raise ValueError("mat and rhs must both be host arrays or both CUDA tensors")
+    bufs = [pm, pr]
+    devs = {dev_m, dev_r}
+    if per is not None:
+        pp, dev_p = _buf(per, complex_, 50 * n_rows, "per")
+        bufs.append(pp)
+        devs.add(dev_p)
+        if complex_:
+            pp2, dev_p2 = _buf(per2, complex_, 50 * n_rows, "per2")
+            devs.add(dev_p2)
+        else:  # real per2 is reference scratch, unused here
+            pp2 = ctypes.c_void_p(0)
+        bufs.append(pp2)
+    if len(devs) != 1:
+        raise ValueError("arrays must all be host arrays or all CUDA tensors")
     L = lib()
     extra = [] if code is None else [int(code)]
     if dev_m:
-        rc = getattr(L, "lns_%s_dev" % name)(dims[0], dims[1], nblk, pm, pr, *extra, _stream())
+        rc = getattr(L, "lns_%s_dev" % name)(dims[0], dims[1], nblk, *bufs, *extra, _stream())
     else:
-        rc = getattr(L, "lns_%s" % name)(dims[0], dims[1], nblk, pm, pr, *extra)
+        rc = getattr(L, "lns_%s" % name)(dims[0], dims[1], nblk, *bufs, *extra)
     check(rc, name)
 
 
@@ -91,3 +104,29 @@ def cpenta2bc(n, nsys, nblk, mat, rhs, code):
 def cpenta1bc(nsys, n, nblk, mat, rhs, code):
     """Complex boundary-closure solve (lines batched over the first index)."""
     _call("cpenta1bc", (nsys, n), nblk, mat, rhs, True, code)
+
+
+def penta2p(np_, nsys, nblk, mat, rhs, per, per2=None):
+    """Real periodic solve (np_ rows, the last repeating the first)."""
+    _call("penta2p", (np_, nsys), nblk, mat, rhs, False, per=per, per2=per2)
+
+
+def penta1p(nsys, np_, nblk, mat, rhs, per, per2=None):
+    """Real periodic solve, lines batched over the first index."""
+    _call("penta1p", (nsys, np_), nblk, mat, rhs, False, per=per, per2=per2)
+
+
+def cpenta2p(np_, nsys, nblk, mat, rhs, per, per2, code):
+    """Complex periodic solve; code 0 factor, 1 solve, 2 both."""
+    _call("cpenta2p", (np_, nsys), nblk, mat, rhs, True, code, per=per, per2=per2)
+
+
+def cpenta1p(nsys, np_, nblk, mat, rhs, per, per2, code):
+    """Complex periodic solve, lines batched over the first index."""
+    _call("cpenta1p", (nsys, np_), nblk, mat, rhs, True, code, per=per, per2=per2)
+
+
+def set_periodic_exact(on):
+    """True: later periodic factorisations are the exact LU; False (default):
+    they reproduce the reference's fill placement at row n-5."""
+    check(lib().lns_set_periodic_exact(1 if on else 0), "set_periodic_exact")

@@ -110,17 +110,19 @@ def run_gpu(case, code=2, device=None):
     fn = getattr(g, case["solver"])
     d = dims(case)
     args = [out["mat"], out["rhs"]]
+    names = ["mat", "rhs"]
+    if c["periodic"]:
+        names += ["per", "per2"]
+        args += [out["per"], out["per2"]]
     if device is not None:
         import torch
 
-        args = [torch.from_numpy(a.ravel(order="F")).to(device) for a in args]
+        args = [torch.from_numpy(out[k].ravel(order="F")).to(device) for k in names]
     extra = [code] if c["complex"] else []
-    if c["periodic"]:
-        raise NotImplementedError
     fn(d[0], d[1], 5, *args, *extra)
     if device is not None:
-        out["mat"] = args[0].cpu().numpy().reshape(out["mat"].shape, order="F")
-        out["rhs"] = args[1].cpu().numpy().reshape(out["rhs"].shape, order="F")
+        for k, a in zip(names, args):
+            out[k] = a.cpu().numpy().reshape(out[k].shape, order="F")
     return out
 
 
