@@ -153,6 +153,45 @@ def time_reference_cpu(sample_reps=3):
                       % (sample_reps, t * 1e3)}
 
 
+def run_mixed(torch, dev, L, sp, stream, rank, world, W, K, fp64_x, refine=2):
+    """Times the mixed-precision solve (lns_cpenta2bc_mixed_dev, code 2) and
+    checks the first timed step's solution against the FP64 direct one."""
+    batches = [make_batch(torch, dev, 1000 * rank + s) for s in range(W + K)]
+    nbytes = L.lns_mixed_workspace_bytes(N_ROWS, N_LINES, 1, 0)
+    work = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    wp = ctypes.c_void_p(work.data_ptr())
+
+    def solve(mat, rhs):
+        rc = L.lns_cpenta2bc_mixed_dev(N_ROWS, N_LINES, 5, ctypes.c_void_p(mat.data_ptr()),
+                                       ctypes.c_void_p(rhs.data_ptr()), 2, refine, wp, sp)
+        if rc:
+            raise RuntimeError(L.lns_last_error().decode())
+
+    for s in range(W):
+        solve(*batches[s])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    for s in range(K):
+        ev[s][0].record(stream)
+        solve(*batches[W + s])
+        ev[s][1].record(stream)
+    torch.cuda.synchronize()
+    per_step = sorted(a.elapsed_time(b) for a, b in ev)
+    total_ms = sum(per_step)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    x = batches[W][1]
+    err = float((x - fp64_x).abs().max() / fp64_x.abs().max())
+    return {"value": world * PTS * K / (total_ms / 1e3), "ms_per_step": total_ms / K,
+            "latency_ms": {"p50": per_step[len(per_step) // 2], "p99": per_step[-1]},
+            "refine_steps": refine, "rel_diff_vs_fp64_direct": err,
+            "workspace_bytes": int(nbytes), "launches_per_step": 3 + 4 * refine + 3}
+
+
 def run_e2e(torch, dev, L, rank, world, K):
     """Steps through the host-pointer entry point lns_cpenta2bc: each step
     copies the step's matrix and right-hand side from pinned host memory to
@@ -217,6 +256,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer end-to-end leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -277,10 +317,15 @@ def main():
     value = world * PTS * K / (total_ms / 1e3)
     kern_ms = statistics.mean(per_step)
 
-    # parity spot check of one timed batch's first lines against nothing
-    # else than finiteness (full parity lives in tests/)
     assert torch.isfinite(torch.view_as_real(batches[W][1])).all()
+    fp64_x = batches[W][1].clone()
     del batches
+
+    # mixed precision: FP32 LU + two FP64 refinement steps, same workload;
+    # the matrix is read only, so the batches are regenerated pristine
+    mixed = None
+    if not args.no_mixed:
+        mixed = run_mixed(torch, dev, L, sp, stream, rank, world, W, K, fp64_x)
 
     # end to end: host-pointer C-ABI call from pinned host memory
     e2e_value = None if args.no_e2e else run_e2e(torch, dev, L, rank, world, K)
@@ -316,6 +361,7 @@ def main():
                               "flops_per_pt": FLOPS_PER_PT,
                               "peak_source": "measured live: DFMA stream on every SM (lns_probe_fp64_tflops)"},
             "cpu_baseline": cpu,
+            "mixed": mixed,
             "gpu_launches": K,
             "clocks": clocks,
         }

@@ -25,6 +25,7 @@
 #ifndef LNS3D_GB300_H
 #define LNS3D_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -113,6 +114,38 @@ int lns_cpenta1p(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rh
                  int32_t code);
 int lns_cpenta1p_dev(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per,
                      double* per2, int32_t code, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Mixed-precision solves (no reference counterpart: the reference solves in
+ * FP64 only).  The LU factors are computed and applied in FP32 -- the FP64
+ * rate of the GB300 is 1/64 of its FP32 rate -- and `refine` steps of
+ * iterative refinement, x += LU32^-1 (b - A x) with the residual formed in
+ * FP64 from the untouched mat, restore FP64 accuracy for well-conditioned
+ * lines (two steps reach FP64 rounding on the isolated-solve workload);
+ * refine = 0 gives the FP32 interior solve of the mixed ADI step.
+ * mat is read only.  code 0 writes the FP32 factors to `work`; code 1
+ * solves rhs in place with the factors in `work` (mat must still hold the
+ * matrix that was factored); code 2 does both.  `work` is a device buffer of
+ * lns_mixed_workspace_bytes(rows, nsys, is_complex, periodic) bytes (rows =
+ * n, or np for periodic lines), owned by the caller and kept between the
+ * code 0 and code 1 calls.  Periodic mixed solves always use the exact LU.
+ */
+size_t lns_mixed_workspace_bytes(int32_t rows, int32_t nsys, int32_t is_complex, int32_t periodic);
+int lns_cpenta2bc_mixed_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                            int32_t refine, void* work, void* stream);
+int lns_cpenta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                            int32_t refine, void* work, void* stream);
+int lns_cpenta2p_mixed_dev(int32_t np, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                           int32_t refine, void* work, void* stream);
+int lns_cpenta1p_mixed_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, double* rhs, int32_t code,
+                           int32_t refine, void* work, void* stream);
+/* real boundary solves, factor + solve in one call */
+int lns_penta2bc_mixed_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine,
+                           void* work, void* stream);
+int lns_penta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* mat, double* rhs, int32_t refine,
+                           void* work, void* stream);
+/* host-pointer form of cpenta2bc_mixed (factor + solve), staged internally */
+int lns_cpenta2bc_mixed(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine);
 
 #ifdef __cplusplus
 }

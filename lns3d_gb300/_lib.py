@@ -46,6 +46,13 @@ SIGNATURES = {
     "lns_cpenta2p_dev": [I32, I32, I32, DP, DP, DP, DP, I32, P],
     "lns_cpenta1p": [I32, I32, I32, DP, DP, DP, DP, I32],
     "lns_cpenta1p_dev": [I32, I32, I32, DP, DP, DP, DP, I32, P],
+    "lns_cpenta2bc_mixed_dev": [I32, I32, I32, DP, DP, I32, I32, P, P],
+    "lns_cpenta1bc_mixed_dev": [I32, I32, I32, DP, DP, I32, I32, P, P],
+    "lns_cpenta2p_mixed_dev": [I32, I32, I32, DP, DP, I32, I32, P, P],
+    "lns_cpenta1p_mixed_dev": [I32, I32, I32, DP, DP, I32, I32, P, P],
+    "lns_penta2bc_mixed_dev": [I32, I32, I32, DP, DP, I32, P, P],
+    "lns_penta1bc_mixed_dev": [I32, I32, I32, DP, DP, I32, P, P],
+    "lns_cpenta2bc_mixed": [I32, I32, I32, DP, DP, I32],
 }
 
 
@@ -62,6 +69,8 @@ def lib():
         L.lns_version.restype = ctypes.c_char_p
         L.lns_probe_fp64_tflops.restype = ctypes.c_double
         L.lns_probe_fp64_tflops.argtypes = []
+        L.lns_mixed_workspace_bytes.restype = ctypes.c_size_t
+        L.lns_mixed_workspace_bytes.argtypes = [I32, I32, I32, I32]
         for name, args in SIGNATURES.items():
             fn = getattr(L, name)
             fn.argtypes = args

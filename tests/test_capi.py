@@ -42,7 +42,8 @@ def test_python_signatures_cover_header():
     from lns3d_gb300._lib import SIGNATURES
 
     solver_syms = [n for n in declared_symbols()
-                   if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops")]
+                   if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops",
+                                "lns_mixed_workspace_bytes")]
     assert sorted(SIGNATURES) == solver_syms
 
 
@@ -88,3 +89,18 @@ def test_zero_lines_is_a_no_op():
 
     # nsys = 0 is valid and launches nothing (no GPU needed)
     g.penta2bc(8, 0, 5, np.zeros(1), np.zeros(1))
+
+
+def test_mixed_workspace_size(lib):
+    # FP32 factors + FP32 residual + FP64 iterate, 256-byte aligned pieces
+    b = lib.lns_mixed_workspace_bytes(256, 512, 1, 0)
+    assert b >= 256 * 512 * (125 * 8 + 5 * 8 + 5 * 16)
+    assert lib.lns_mixed_workspace_bytes(257, 512, 1, 1) > b
+    assert lib.lns_mixed_workspace_bytes(0, 1, 1, 0) == 0
+
+
+@pytest.mark.parametrize("refine", [-1, 17])
+def test_mixed_argument_errors(lib, refine):
+    a = np.zeros(2 * 125 * 64)
+    assert lib.lns_cpenta2bc_mixed_dev(8, 8, 5, a.ctypes.data, a.ctypes.data, 2, refine, None, None) == 1
+    assert lib.lns_cpenta2bc_mixed(8, 8, 5, a.ctypes.data, a.ctypes.data, refine) == 1
