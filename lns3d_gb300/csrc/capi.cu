@@ -15,21 +15,26 @@
 #include <type_traits>
 
 #include "../../include/lns3d_gb300.h"
-#include "penta_direct.cuh"
-#include "penta_periodic.cuh"
-#include "mixed.cuh"
+#include "launch.cuh"
 
-namespace {
+static thread_local std::string g_err;
+std::atomic<int> g_periodic_exact{0};
 
-thread_local std::string g_err;
-
-int fail(int code, const std::string& msg) {
+int lns_fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
-int cuda_fail(cudaError_t e, const char* where) {
-  return fail(LNS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+int lns_cuda_fail(cudaError_t e, const char* where) {
+  return lns_fail(LNS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
+
+namespace {
+
+using lns::host::launch_bc;
+using lns::host::launch_p;
+using lns::host::launch_solve;
+int fail(int code, const std::string& msg) { return lns_fail(code, msg); }
+int cuda_fail(cudaError_t e, const char* where) { return lns_cuda_fail(e, where); }
 
 // Device staging buffers of the host-pointer entry points.
 struct Staging {
@@ -73,19 +78,6 @@ int check_sizes(int n, int nsys, int nblk, const char* who) {
   return LNS_OK;
 }
 
-template <typename T>
-int launch_bc(void* mat, void* rhs, int n, int nsys, long long row_stride, long long line_stride, int code,
-              cudaStream_t st, int* status) {
-  if (nsys == 0) return LNS_OK;
-  lns::PentaArgs a{mat, rhs, n, nsys, row_stride, line_stride, code, status};
-  const int blocks = (nsys + lns::kWarpsPerCta - 1) / lns::kWarpsPerCta;
-  const size_t smem = (size_t)lns::kWarpsPerCta * (lns::kRing * lns::kRowSz + 16) * sizeof(T);
-  lns::penta_bc_kernel<T><<<blocks, 32 * lns::kWarpsPerCta, smem, st>>>(a);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "penta_bc_kernel launch");
-  return LNS_OK;
-}
-
 // Host-pointer form: stage, solve, copy back.
 template <typename T>
 int host_bc(double* mat, double* rhs, int n, int nsys, long long row_stride, long long line_stride, int code,
@@ -121,24 +113,6 @@ int host_bc(double* mat, double* rhs, int n, int nsys, long long row_stride, lon
   e = cudaMemcpy(&status, g_stage.status, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "copy status to host");
   if (status) return fail(LNS_ERR_PIVOT, "zero or non-finite pivot");
-  return LNS_OK;
-}
-
-std::atomic<int> g_periodic_exact{0};
-
-template <typename T>
-int launch_p(void* mat, void* rhs, void* per, void* per2, int np, int nsys, long long row_stride,
-             long long line_stride, int code, cudaStream_t st, int* status, int exact = -1) {
-  if (nsys == 0) return LNS_OK;
-  const bool cplx = std::is_same<T, lns::cd>::value || std::is_same<T, lns::cf>::value;
-  const int compat = exact < 0 ? (g_periodic_exact.load() ? 0 : 1) : (exact ? 0 : 1);
-  lns::PeriodicArgs a{mat, rhs, per, per2, np - 1, np, nsys, row_stride, line_stride, code,
-                      compat, cplx ? 1 : 0, status};
-  const int blocks = (nsys + lns::kPWarpsPerCta - 1) / lns::kPWarpsPerCta;
-  const size_t smem = (size_t)lns::kPWarpsPerCta * lns::kPWarpSmem * sizeof(T);
-  lns::penta_p_kernel<T><<<blocks, 32 * lns::kPWarpsPerCta, smem, st>>>(a);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "penta_p_kernel launch");
   return LNS_OK;
 }
 

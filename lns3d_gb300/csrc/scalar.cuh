@@ -105,6 +105,8 @@ __device__ __forceinline__ float to_lo(double a) { return (float)a; }
 __device__ __forceinline__ cf to_lo(cd a) { return cf{(float)a.x, (float)a.y}; }
 __device__ __forceinline__ double to_hi(float a) { return (double)a; }
 __device__ __forceinline__ cd to_hi(cf a) { return cd{(double)a.x, (double)a.y}; }
+__device__ __forceinline__ double to_hi(double a) { return a; }
+__device__ __forceinline__ cd to_hi(cd a) { return a; }
 
 __device__ __forceinline__ bool finite_s(double a) { return isfinite(a); }
 __device__ __forceinline__ bool finite_s(float a) { return isfinite(a); }
