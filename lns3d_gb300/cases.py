@@ -1,0 +1,72 @@
+"""Synthetic inputs of the linearised single-Fourier-mode ADI workloads.
+
+The reference reads its grid, metrics and mean flow from ``grid.dat``,
+``metric.dat`` and ``mean.dat`` (src/gengrid.f90:17-80, src/genmean.f90);
+these generators produce the same arrays for an analytic mesh:
+
+* grid: x uniform on [0, Lx] and periodic (point nx repeats point 1), y on
+  [-Ly, Ly] clustered at the layer as y = Ly sinh(s (2 eta - 1)) / sinh(s); the
+  computational coordinates are xi, eta in [0, 1] with d xi = 1/(nx-1),
+  d eta = 1/(ny-1) (src/gengrid.f90:36-45);
+* metrics: the ten arrays m1, m2, n1, n2, m11, m12, m22, n11, n12, n22 of the
+  reference (d xi/dx, ..., d^2 eta/dy^2), exact for the analytic mapping;
+* mean flow: a parallel compressible shear layer u = (1 + tanh(y/delta))/2,
+  v = w = 0, T from the Crocco-Busemann relation for equal free-stream
+  temperatures, T = 1 + (gamma-1)/2 Ma^2 u (1-u), rho = 1/T (uniform
+  pressure);
+* initial disturbance: seed-normal complex amplitudes times a Gaussian
+  window in x (and one in y), scaled to a maximum of `amp`.
+
+The default period Lx = 5.5 keeps every streamwise wavenumber of the
+periodic box (2 pi k / Lx >= 1.14) above the Kelvin-Helmholtz neutral
+wavenumber of the tanh layer (alpha delta = 1), so the layer is linearly
+stable and the implicit pseudo-time iteration converges to the steady
+(zero) disturbance; a longer box admits growing modes and the residual
+grows, in the reference algorithm as here.
+
+Arrays are numpy, Fortran-ordered, with the reference shapes: metrics
+(nx, ny), vm (5, nx, ny), v (5, nx, ny) complex.
+"""
+import numpy as np
+
+GAMMA = 1.4
+
+
+def shear_layer(nx=512, ny=256, Lx=5.5, Ly=10.0, stretch=3.0, delta=1.0, Ma=0.8, Re=500.0, Pr=0.72,
+                beta=0.2, omega=0.05, amp=1e-6, seed=0, window=None):
+    xi = np.linspace(0.0, 1.0, nx)
+    eta = np.linspace(0.0, 1.0, ny)
+    s = stretch
+    z = s * (2.0 * eta - 1.0)
+    y1 = Ly * np.sinh(z) / np.sinh(s)
+    dy = Ly * 2.0 * s * np.cosh(z) / np.sinh(s)            # dy/deta
+    d2y = Ly * 4.0 * s * s * np.sinh(z) / np.sinh(s)       # d2y/deta2
+    x = np.asfortranarray(np.repeat((Lx * xi)[:, None], ny, axis=1))
+    y = np.asfortranarray(np.repeat(y1[None, :], nx, axis=0))
+    ones = np.ones((nx, ny))
+    zeros = np.zeros((nx, ny))
+    metrics = {
+        "m1": ones / Lx, "m2": zeros.copy(), "n1": zeros.copy(),
+        "n2": np.repeat((1.0 / dy)[None, :], nx, axis=0),
+        "m11": zeros.copy(), "m12": zeros.copy(), "m22": zeros.copy(),
+        "n11": zeros.copy(), "n12": zeros.copy(),
+        "n22": np.repeat((-d2y / dy ** 3)[None, :], nx, axis=0),
+    }
+    metrics = {k: np.asfortranarray(v) for k, v in metrics.items()}
+    u = 0.5 * (1.0 + np.tanh(y / delta))
+    t = 1.0 + 0.5 * (GAMMA - 1.0) * Ma * Ma * u * (1.0 - u)
+    vm = np.zeros((5, nx, ny), order="F")
+    vm[0] = 1.0 / t
+    vm[1] = u
+    vm[4] = t
+    rng = np.random.default_rng(seed)
+    pert = rng.standard_normal((5, nx, ny)) + 1j * rng.standard_normal((5, nx, ny))
+    w = window if window is not None else Lx / 8.0
+    pert *= np.exp(-(((x - 0.5 * Lx) / w) ** 2))[None, :, :]
+    pert *= np.exp(-((y / (0.25 * Ly)) ** 2))[None, :, :]
+    pert *= amp / np.abs(pert).max()
+    v = np.asfortranarray(pert.astype(np.complex128))
+    params = dict(nx=nx, ny=ny, dxi=1.0 / (nx - 1), deta=1.0 / (ny - 1), Ma=Ma, Re=Re, Pr=Pr, gamma=GAMMA,
+                  gamma1=GAMMA - 1.0, omega=omega, kz=beta, alfa=1.0, xper=1, yper=0, navier=1, wall=1, wallt=1,
+                  top=0, optx=-1, opty=-1)
+    return dict(params=params, x=x, y=y, metrics=metrics, vm=vm, v=v)
