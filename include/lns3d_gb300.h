@@ -147,6 +147,103 @@ int lns_penta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* 
 /* host-pointer form of cpenta2bc_mixed (factor + solve), staged internally */
 int lns_cpenta2bc_mixed(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine);
 
+/* ---------------------------------------------------------------------------
+ * The linearised single-Fourier-mode implicit ADI step (src/impdrv3d.f90,
+ * impl = 1, iLHS = 1) as one device-resident context.
+ *
+ * The reference keeps its state in modules (src/global.f90,
+ * src/local2d.f90, src/local3d.f90) and reads it from the input deck
+ * (src/input.f90); here a context owns the metrics, the frozen operators,
+ * the time step, the factored xi and eta LHS and the scratch fields on one
+ * device.  Sequence of a run (src/lns3d.f90:140-160, src/impdrv3d.f90):
+ *   lns_ctx3d_create        deck values, device buffers
+ *   lns_upload_metrics3d    metric.dat arrays
+ *   lns_upload_mean3d       mean flow: genmtrx(vm, kz, vm) and set_time_step
+ *                           on the GPU; the next step factors the LHS again
+ *   lns_step3d / _dev       nsteps implicit steps of niter correctors
+ * Supported options: xper = 1 (periodic xi sweep, cpenta2p), yper = 0 with a
+ * viscous wall at j = 1 (navier = 1, wall 1 or 2, wallt 0 or 1) and a
+ * zero-disturbance top (top = 0); optx, opty any; constant viscosity
+ * (mattyp 0); no sponge, smoother, damper or filter.  Other options return
+ * LNS_ERR_ARG.
+ *
+ * precision LNS_FP64 follows the reference arithmetic (complex*16
+ * throughout).  LNS_MIXED keeps the RHS, the residual and the update in
+ * FP64 and forms, factors and applies both LHS in FP32 (complex*8): the
+ * sweeps compute the correction only, so the converged state is the FP64
+ * one while each step differs from the FP64 step by FP32 rounding of the
+ * correction.  No reference counterpart.
+ *
+ * All arrays are Fortran-ordered: v(5,nx,ny) complex*16 as interleaved
+ * doubles, vm(5,nx,ny), metrics(nx,ny,10).
+ */
+#define LNS_FP64 0
+#define LNS_MIXED 1
+
+typedef struct {
+  int32_t nx, ny;            /* grid points; with xper, point nx repeats point 1 */
+  double dxi, deta;          /* computational spacings (src/gengrid.f90: 1/(nx-1), 1/(ny-1)) */
+  double Ma, Re, Pr, gamma;  /* src/input.f90 namelist values; gamma1 = gamma - 1 */
+  double omega, beta;        /* temporal frequency and spanwise wavenumber kz = 2 pi / Lz */
+  double alfa;               /* implicitness, 1 for backward Euler (impl = 1) */
+  double cflmax, dtmax;      /* src/temporal.f90 time-step control */
+  int32_t loctime;           /* 0 global time step, 1 local time step */
+  int32_t xper, yper, navier, wall, wallt, top, optx, opty;
+  int32_t precision;         /* LNS_FP64 or LNS_MIXED */
+} lns_params3d;
+
+typedef struct lns_ctx3d lns_ctx3d;
+
+/* Allocates the context on the current device.  replaces the allocations of
+ * src/impdrv3d.f90:46-99 and the deck of src/input.f90 */
+int lns_ctx3d_create(const lns_params3d* params, lns_ctx3d** ctx);
+int lns_ctx3d_destroy(lns_ctx3d* ctx);
+/* Device bytes the context holds (excluding what the caller owns). */
+size_t lns_ctx3d_bytes(const lns_ctx3d* ctx);
+/* metrics(nx,ny,10) on the host: m1 m2 n1 n2 m11 m12 m22 n11 n12 n22
+ * (src/gengrid.f90:82-131, metric.dat) */
+int lns_upload_metrics3d(lns_ctx3d* ctx, const double* metrics);
+/* vm(5,nx,ny) on the host: builds the frozen operators (src/genmtrx.f90,
+ * linear = 1, called as genmtrx(vm, kz, vm) at src/lns3d.f90:149) and the
+ * time step (src/temporal.f90:12-130, called at src/impdrv3d.f90:54);
+ * *cfl (may be NULL) returns the CFL number of that time step.  Invalidates
+ * the stored LHS factors. */
+int lns_upload_mean3d(lns_ctx3d* ctx, const double* vm, double* cfl);
+/* nsteps implicit steps on the host disturbance v(5,nx,ny) (in place);
+ * totres[nsteps] (may be NULL) receives resstat3D's residual of the last
+ * corrector of each step.  replaces the body of src/impdrv3d.f90:130-356:
+ * vold = v, itrBC3D, then niter times lrhs3D, rbe3D, rhsBC3D, resstat3D,
+ * the xi sweep cpenta2p (LHS lhs1f3D + lhsbc1f3D factored at the first
+ * step of the context), the eta sweep cpenta1bc (lhs2f3D + lhsbt2f3D +
+ * lhsbc2f3D), v = v + r, itrBC3D. */
+int lns_step3d(lns_ctx3d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres);
+/* Device form: v is a device array; totres_dev (may be NULL) a device array
+ * of nsteps doubles; enqueued on `stream`.  The first call after
+ * lns_upload_mean3d factors the LHS and waits for the pivot check. */
+int lns_step3d_dev(lns_ctx3d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream);
+
+/* Inspection (device arrays, enqueued on `stream`), for parity checks.
+ * r = rhsBC3D(rbe3D(lrhs3D(v), v, vold)) (src/lrhs3d.f90:2,
+ * src/impdrv3d.f90:444, src/rhsbc3d.f90:2) in FP64, and *totres_dev =
+ * resstat3D(r) (src/resstat3d.f90:2) when totres_dev is not NULL. */
+int lns_rhs3d_dev(lns_ctx3d* ctx, const double* v, const double* vold, double* r, double* totres_dev, void* stream);
+/* The unfactored LHS of the xi (dir 1: src/lhs1f3d.f90 + src/lhsbc1f3d.f90)
+ * or eta sweep (dir 2: src/lhs2f3d.f90 + src/lhsbt2f3d.f90 +
+ * src/lhsbc2f3d.f90) into the complex*16 device array mat(5,5,5,nx,ny). */
+int lns_lhs3d_dev(lns_ctx3d* ctx, int32_t dir, double* mat, void* stream);
+/* Phase timing, no reference counterpart.  lns_ctx3d_profile(ctx, 1) makes
+ * every later corrector record CUDA events on its stream around the RHS, the
+ * xi sweep, the eta sweep and the update (and resets the record);
+ * lns_ctx3d_profile_read waits for them and returns the summed milliseconds
+ * of the four phases in ms[4] and the number of correctors in *ncorr, then
+ * clears the record. */
+int lns_ctx3d_profile(lns_ctx3d* ctx, int32_t on);
+int lns_ctx3d_profile_read(lns_ctx3d* ctx, double* ms, int32_t* ncorr);
+/* Copy of a frozen field to the host in the reference layout:
+ * 0 Ah, 1 Bh, 2 Dh, 3 Dhi (5,5,nx,ny); 4 Vh11, 5 Vh12, 6 Vh22, 7 ABhi
+ * (6,nx,ny); 8 dtl (nx,ny). */
+int lns_get_field3d(lns_ctx3d* ctx, int32_t which, double* out);
+
 #ifdef __cplusplus
 }
 #endif

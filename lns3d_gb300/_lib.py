@@ -53,7 +53,28 @@ SIGNATURES = {
     "lns_penta2bc_mixed_dev": [I32, I32, I32, DP, DP, I32, P, P],
     "lns_penta1bc_mixed_dev": [I32, I32, I32, DP, DP, I32, P, P],
     "lns_cpenta2bc_mixed": [I32, I32, I32, DP, DP, I32],
+    "lns_ctx3d_create": [P, P],
+    "lns_ctx3d_destroy": [P],
+    "lns_upload_metrics3d": [P, DP],
+    "lns_upload_mean3d": [P, DP, DP],
+    "lns_step3d": [P, DP, I32, I32, DP],
+    "lns_step3d_dev": [P, DP, I32, I32, DP, P],
+    "lns_rhs3d_dev": [P, DP, DP, DP, DP, P],
+    "lns_lhs3d_dev": [P, I32, DP, P],
+    "lns_get_field3d": [P, I32, DP],
+    "lns_ctx3d_profile": [P, I32],
+    "lns_ctx3d_profile_read": [P, DP, P],
 }
+
+
+class Params3D(ctypes.Structure):
+    """lns_params3d of include/lns3d_gb300.h."""
+    _fields_ = [("nx", I32), ("ny", I32), ("dxi", ctypes.c_double), ("deta", ctypes.c_double),
+                ("Ma", ctypes.c_double), ("Re", ctypes.c_double), ("Pr", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("omega", ctypes.c_double), ("beta", ctypes.c_double),
+                ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double), ("dtmax", ctypes.c_double),
+                ("loctime", I32), ("xper", I32), ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32),
+                ("top", I32), ("optx", I32), ("opty", I32), ("precision", I32)]
 
 
 def lib():
@@ -71,6 +92,8 @@ def lib():
         L.lns_probe_fp64_tflops.argtypes = []
         L.lns_mixed_workspace_bytes.restype = ctypes.c_size_t
         L.lns_mixed_workspace_bytes.argtypes = [I32, I32, I32, I32]
+        L.lns_ctx3d_bytes.restype = ctypes.c_size_t
+        L.lns_ctx3d_bytes.argtypes = [P]
         for name, args in SIGNATURES.items():
             fn = getattr(L, name)
             fn.argtypes = args

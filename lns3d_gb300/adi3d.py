@@ -1,0 +1,148 @@
+"""Host-side mirror of the linearised 3D implicit driver (src/impdrv3d.f90).
+
+:class:`ImpDrv3D` owns one device context of the C ABI (``lns_ctx3d_*`` in
+``include/lns3d_gb300.h``): the deck values, the metrics, the frozen
+operators built on the GPU from the mean flow (``genmtrx(vm, kz, vm)``,
+src/lns3d.f90:149), the time step (src/temporal.f90) and the LHS factors
+(formed and factored at the first step, src/impdrv3d.f90:229-319).
+
+The disturbance ``v`` is the Fortran array ``v(5,nx,ny)`` complex*16: a numpy
+complex128 array (host memory; the call stages it, like the Fortran call) or
+a CUDA torch complex128 tensor (device memory; enqueued on torch's current
+stream).  Every call runs the sm_103a kernels of ``lib/liblns3d_gb300.so``;
+there is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import Params3D, check, lib
+
+FP64, MIXED = 0, 1
+FIELDS = {"Ah": 0, "Bh": 1, "Dh": 2, "Dhi": 3, "Vh11": 4, "Vh12": 5, "Vh22": 6, "ABhi": 7, "dtl": 8}
+METRICS = ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _stream():
+    import torch
+
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class ImpDrv3D:
+    """One linearised single-mode ADI problem resident on the current GPU.
+
+    params: dict with the deck values nx, ny, dxi, deta, Ma, Re, Pr, gamma,
+    omega, kz (beta), alfa, xper, yper, navier, wall, wallt, top, optx, opty,
+    plus cflmax, dtmax, loctime; metrics: dict of the ten (nx, ny) arrays;
+    vm: (5, nx, ny) mean flow.  precision: FP64 (reference arithmetic) or
+    MIXED (FP32 LHS factors and sweeps, FP64 RHS, residual and update).
+    """
+
+    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64):
+        p = params
+        self.nx, self.ny = int(p["nx"]), int(p["ny"])
+        self.precision = precision
+        prm = Params3D(nx=self.nx, ny=self.ny, dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
+                       gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax,
+                       dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
+                       wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
+                       precision=precision)
+        self._ctx = ctypes.c_void_p()
+        check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
+        m = np.empty((self.nx, self.ny, 10), order="F")
+        for k, name in enumerate(METRICS):
+            m[:, :, k] = metrics[name]
+        check(lib().lns_upload_metrics3d(self._ctx, ctypes.c_void_p(m.ctypes.data)), "lns_upload_metrics3d")
+        self.set_mean(vm)
+
+    def set_mean(self, vm):
+        """Upload a mean flow; rebuild the operators and time step on the GPU."""
+        vm = np.asfortranarray(vm, dtype=np.float64)
+        assert vm.shape == (5, self.nx, self.ny)
+        cfl = ctypes.c_double()
+        check(lib().lns_upload_mean3d(self._ctx, ctypes.c_void_p(vm.ctypes.data), ctypes.byref(cfl)),
+              "lns_upload_mean3d")
+        self.cfl = cfl.value
+
+    @property
+    def device_bytes(self):
+        return lib().lns_ctx3d_bytes(self._ctx)
+
+    def _check_v(self, v, name="v"):
+        n = 5 * self.nx * self.ny
+        if _is_torch(v):
+            import torch
+
+            if v.dtype != torch.complex128 or not v.is_cuda or not v.is_contiguous() or v.numel() != n:
+                raise ValueError("%s must be a contiguous CUDA complex128 tensor of %d elements" % (name, n))
+            return ctypes.c_void_p(v.data_ptr()), True
+        if not isinstance(v, np.ndarray) or v.dtype != np.complex128 or v.size != n:
+            raise ValueError("%s must be a complex128 array of shape (5, nx, ny)" % name)
+        if not v.flags.f_contiguous:
+            raise ValueError("%s must be Fortran-ordered (5, nx, ny)" % name)
+        return ctypes.c_void_p(v.ctypes.data), False
+
+    def step(self, v, nsteps=1, niter=1, totres=None):
+        """Advance v in place by nsteps implicit steps of niter correctors.
+
+        Host v: returns a numpy array of the per-step residuals.  Device v:
+        `totres` may be a CUDA float64 tensor of nsteps entries that receives
+        them; returns None (asynchronous)."""
+        pv, dev = self._check_v(v)
+        if dev:
+            pt = ctypes.c_void_p(totres.data_ptr()) if totres is not None else None
+            check(lib().lns_step3d_dev(self._ctx, pv, nsteps, niter, pt, _stream()), "lns_step3d_dev")
+            return None
+        res = np.zeros(max(nsteps, 1))
+        check(lib().lns_step3d(self._ctx, pv, nsteps, niter, ctypes.c_void_p(res.ctypes.data)), "lns_step3d")
+        return res[:nsteps]
+
+    def rhs(self, v, vold, r, totres=None):
+        """r = rhsBC3D(rbe3D(lrhs3D(v))) on device tensors; totres: 1-element tensor."""
+        pv, _ = self._check_v(v)
+        po, _ = self._check_v(vold, "vold")
+        pr, _ = self._check_v(r, "r")
+        pt = ctypes.c_void_p(totres.data_ptr()) if totres is not None else None
+        check(lib().lns_rhs3d_dev(self._ctx, pv, po, pr, pt, _stream()), "lns_rhs3d_dev")
+
+    def lhs(self, direction, mat):
+        """Unfactored LHS of the xi (1) or eta (2) sweep into a device tensor of 125 nx ny complex128."""
+        if mat.numel() != 125 * self.nx * self.ny or not mat.is_cuda:
+            raise ValueError("mat must be a CUDA tensor of 125*nx*ny complex128 entries")
+        check(lib().lns_lhs3d_dev(self._ctx, direction, ctypes.c_void_p(mat.data_ptr()), _stream()), "lns_lhs3d_dev")
+
+    def field(self, name):
+        """A frozen field in the reference layout (numpy, Fortran order)."""
+        shape = {0: (5, 5), 1: (5, 5), 2: (5, 5), 3: (5, 5), 8: ()}.get(FIELDS[name], (6,))
+        out = np.zeros(shape + (self.nx, self.ny), order="F")
+        check(lib().lns_get_field3d(self._ctx, FIELDS[name], ctypes.c_void_p(out.ctypes.data)), "lns_get_field3d")
+        return out
+
+    def profile(self, on=True):
+        """Start (or stop) recording per-phase CUDA events of every corrector."""
+        check(lib().lns_ctx3d_profile(self._ctx, 1 if on else 0), "lns_ctx3d_profile")
+
+    def profile_read(self):
+        """Summed milliseconds of the phases rhs, xsweep, ysweep, update and
+        the number of correctors recorded since profiling started."""
+        ms = np.zeros(4)
+        n = ctypes.c_int32()
+        check(lib().lns_ctx3d_profile_read(self._ctx, ctypes.c_void_p(ms.ctypes.data), ctypes.byref(n)),
+              "lns_ctx3d_profile_read")
+        return dict(zip(("rhs", "xsweep", "ysweep", "update"), ms.tolist())), n.value
+
+    def close(self):
+        if self._ctx:
+            lib().lns_ctx3d_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

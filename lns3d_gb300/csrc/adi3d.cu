@@ -1,0 +1,1038 @@
+// The linearised single-Fourier-mode implicit ADI step on the GPU
+// (src/impdrv3d.f90:130-356 with impl = 1, iLHS = 1) and its C ABI
+// (lns_ctx3d_*, include/lns3d_gb300.h).
+//
+// A context owns everything the step needs on the device: the frozen
+// operators (built once from the mean flow by genmtrx_kernel, or uploaded),
+// the local time step, the two factored LHS (factored once, at the first
+// step, as the reference does), and the disturbance.  A step is
+//   c1v = d v/d xi                                     grad1_kernel
+//   r = vold - v - dtl L(v), boundary rows, residual    rhs_kernel
+//   xi sweep, eta sweep (stored factors)                penta_solve_kernel
+//   v += r, boundary values                             update_kernel
+// In the mixed-precision mode the factors and the sweeps are FP32 and the
+// RHS, residual and update stay FP64.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lns3d_gb300.h"
+#include "adi3d.cuh"
+#include "launch.cuh"
+
+namespace lns {
+namespace a3 {
+
+// Frozen operators on the device, structure-of-arrays: element (a,b)
+// (0-based) of a 5x5 operator at point p is at [(a + 5 b) * np + p], entry k
+// of a 6-vector at [k * np + p].
+struct Ops {
+  double *Ah, *Bh, *Dh, *Dhi, *V11, *V12, *V22, *AB, *dtl;
+  long long np;
+};
+
+struct Metrics {
+  const double *m1, *m2, *n1, *n2, *m11, *m12, *m22, *n11, *n12, *n22;
+};
+
+__device__ __forceinline__ double& opel(double* A, const Ops& o, int a, int b, long long p) {
+  return A[(long long)(a + 5 * b) * o.np + p];
+}
+
+// ------------------------------------------------------------------ genmtrx
+// src/genmtrx.f90 with linear = 1, general = true, mattyp = 0, idamp = 0,
+// complex_analysis = true; one thread per point.
+__global__ void genmtrx_kernel(Grid g, const double* __restrict__ vm, Metrics mt, Ops o) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y + 1;
+  if (i > g.nx) return;
+  const long long p = pix(g, i, j);
+  auto V = [&](int k, int ii, int jj) { return vm[k + 5 * pix(g, ii, jj)]; };
+  double g1v[5], g2v[5], g11v[5], g12v[5], g22v[5];
+  for (int k = 0; k < 5; ++k) {
+    g1v[k] = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, j); });
+    g2v[k] = d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return V(k, i, jj); });
+    g11v[k] = d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return V(k, ii, j); });
+    g22v[k] = d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return V(k, i, jj); });
+    g12v[k] = d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) {
+      return d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, jj); });
+    });
+  }
+  if (g.navier && !g.yper && (g.wallt == 1 || g.wallt == 2) && j == 1) g2v[4] = 0.0;  // src/gradbc.f90
+  const double m1 = mt.m1[p], m2 = mt.m2[p], n1 = mt.n1[p], n2 = mt.n2[p];
+  const double m11 = mt.m11[p], m12 = mt.m12[p], m22 = mt.m22[p], n11 = mt.n11[p], n12 = mt.n12[p], n22 = mt.n22[p];
+  const double m1m1 = m1 * m1, m1m2 = m1 * m2, m2m2 = m2 * m2, n1n1 = n1 * n1, n1n2 = n1 * n2, n2n2 = n2 * n2;
+  const double m1n1 = m1 * n1, m1n2 = m1 * n2, m2n1 = m2 * n1, m2n2 = m2 * n2;
+  double g1vl[5], g2vl[5], g11vl[5], g12vl[5], g22vl[5];
+  for (int k = 0; k < 5; ++k) {  // src/genmtrx.f90:116-136
+    g11vl[k] = g11v[k] * m1m1 + two * g12v[k] * m1n1 + g22v[k] * n1n1 + g1v[k] * m11 + g2v[k] * n11;
+    g12vl[k] = g11v[k] * m1m2 + g12v[k] * (m1n2 + m2n1) + g22v[k] * n1n2 + g1v[k] * m12 + g2v[k] * n12;
+    g22vl[k] = g11v[k] * m2m2 + two * g12v[k] * m2n2 + g22v[k] * n2n2 + g1v[k] * m22 + g2v[k] * n22;
+    g1vl[k] = g1v[k] * m1 + g2v[k] * n1;
+    g2vl[k] = g1v[k] * m2 + g2v[k] * n2;
+  }
+  const double rho = V(0, i, j), u1 = V(1, i, j), u2 = V(2, i, j), u3 = V(3, i, j), t = V(4, i, j);
+  const double rhoinv = 1.0 / rho;
+  const double grho[3] = {g1vl[0], g2vl[0], 0.0};
+  const double gu[3][3] = {{g1vl[1], g2vl[1], 0.0}, {g1vl[2], g2vl[2], 0.0}, {g1vl[3], g2vl[3], 0.0}};
+  const double gt[3] = {g1vl[4], g2vl[4], 0.0};
+  const double g1divu = g11vl[1] + g12vl[2], g2divu = g12vl[1] + g22vl[2], g3divu = 0.0;
+  const double S1jj = pt5 * (g11vl[1] + g11vl[1] + g22vl[1] + g12vl[2]);
+  const double S2jj = pt5 * (g11vl[2] + g12vl[1] + g22vl[2] + g22vl[2]);
+  const double S3jj = pt5 * (g11vl[3] + g22vl[3]);
+  const double Lapt = g11vl[4] + g22vl[4];
+  const double divu = gu[0][0] + gu[1][1] + gu[2][2];
+  double S[3][3] = {{gu[0][0], pt5 * (gu[0][1] + gu[1][0]), pt5 * gu[2][0]},
+                    {pt5 * (gu[1][0] + gu[0][1]), gu[1][1], pt5 * gu[2][1]},
+                    {pt5 * gu[2][0], pt5 * gu[2][1], 0.0}};
+  // getmat, src/getmat.f90:11-20 (mattyp 0)
+  const double mu = 1.0, dmu = 0.0, d2mu = 0.0, con = mu, dcon = dmu, d2con = d2mu;
+  const double lm = -pt66 * mu, dlm = -pt66 * dmu, d2lm = -pt66 * d2mu;
+  const double g1mu = dmu * gt[0], g2mu = dmu * gt[1], g3mu = dmu * gt[2];
+  const double g1dmu = d2mu * gt[0], g2dmu = d2mu * gt[1], g3dmu = d2mu * gt[2];
+  const double g1con = dcon * gt[0], g2con = dcon * gt[1], g3con = dcon * gt[2];
+  const double g1dcon = d2con * gt[0], g2dcon = d2con * gt[1], g3dcon = d2con * gt[2];
+  const double g1lm = dlm * gt[0], g2lm = dlm * gt[1], g3lm = dlm * gt[2];
+  const double g1dlm = d2lm * gt[0], g2dlm = d2lm * gt[1], g3dlm = d2lm * gt[2];
+  const double gamma = g.gamma, gamma1 = g.gamma1, Ma2 = g.Ma * g.Ma, Re = g.Re, Pr = g.Pr, kzl = g.kz;
+  double A[5][5] = {}, B[5][5] = {}, C[5][5] = {}, D[5][5] = {}, Vij[4];
+  double fact1 = rhoinv / Re, fact2;
+  const double gmsinv = 1.0 / (gamma * Ma2);
+  // A, src/genmtrx.f90:463-507
+  A[0][0] = u1; A[0][1] = rho;
+  A[1][0] = rhoinv * t * gmsinv;
+  A[1][1] = u1 - fact1 * g1lm - fact1 * two * g1mu;
+  A[1][2] = -(fact1 * g2mu);
+  A[1][3] = -(fact1 * g3mu);
+  A[1][4] = gmsinv - fact1 * dlm * divu - fact1 * dmu * two * S[0][0];
+  A[2][1] = -(fact1 * g2lm);
+  A[2][2] = u1 - fact1 * g1mu;
+  A[2][4] = -(fact1 * dmu * two * S[1][0]);
+  A[3][1] = -(fact1 * g3lm);
+  A[3][3] = u1 - fact1 * g1mu;
+  A[3][4] = -(fact1 * dmu * two * S[2][0]);
+  // B, src/genmtrx.f90:530-574
+  B[0][0] = u2; B[0][2] = rho;
+  B[1][1] = u2 - fact1 * g2mu;
+  B[1][2] = -(fact1 * g1lm);
+  B[1][4] = -(fact1 * dmu * two * S[0][1]);
+  B[2][0] = rhoinv * t * gmsinv;
+  B[2][1] = -(fact1 * g1mu);
+  B[2][2] = u2 - fact1 * g2lm - fact1 * two * g2mu;
+  B[2][3] = -(fact1 * g3mu);
+  B[2][4] = gmsinv - fact1 * dlm * divu - fact1 * dmu * two * S[1][1];
+  B[3][2] = -(fact1 * g3lm);
+  B[3][3] = u2 - fact1 * g2mu;
+  B[3][4] = -(fact1 * dmu * two * S[2][1]);
+  // C, src/genmtrx.f90:929-973
+  C[0][0] = u3; C[0][3] = rho;
+  C[1][1] = u3 - fact1 * g3mu;
+  C[1][3] = -(fact1 * g1lm);
+  C[1][4] = -(fact1 * dmu * two * S[0][2]);
+  C[2][2] = u3 - fact1 * g3mu;
+  C[2][3] = -(fact1 * g2lm);
+  C[2][4] = -(fact1 * dmu * two * S[1][2]);
+  C[3][0] = rhoinv * t * gmsinv;
+  C[3][1] = -(fact1 * g1mu);
+  C[3][2] = -(fact1 * g2mu);
+  C[3][3] = u3 - fact1 * g3lm - fact1 * two * g3mu;
+  C[3][4] = gmsinv - fact1 * dlm * divu - fact1 * dmu * two * S[2][2];
+  // D, src/genmtrx.f90:708-780 (linear = 1)
+  D[0][0] = divu; D[0][1] = grho[0]; D[0][2] = grho[1]; D[0][3] = grho[2];
+  D[1][0] = rhoinv * (u1 * gu[0][0] + u2 * gu[0][1] + u3 * gu[0][2] + gmsinv * gt[0]);
+  D[1][1] = gu[0][0]; D[1][2] = gu[0][1]; D[1][3] = gu[0][2];
+  D[1][4] = rhoinv * gmsinv * grho[0] - fact1 * (g1dlm * divu + dlm * g1divu) -
+            fact1 * two * (g1dmu * S[0][0] + g2dmu * S[0][1] + g3dmu * S[0][2] + dmu * S1jj);
+  D[2][0] = rhoinv * (u1 * gu[1][0] + u2 * gu[1][1] + u3 * gu[1][2] + gmsinv * gt[1]);
+  D[2][1] = gu[1][0]; D[2][2] = gu[1][1]; D[2][3] = gu[1][2];
+  D[2][4] = rhoinv * gmsinv * grho[1] - fact1 * (g2dlm * divu + dlm * g2divu) -
+            fact1 * two * (g1dmu * S[1][0] + g2dmu * S[1][1] + g3dmu * S[1][2] + dmu * S2jj);
+  D[3][0] = rhoinv * (u1 * gu[2][0] + u2 * gu[2][1] + u3 * gu[2][2] + gmsinv * gt[2]);
+  D[3][1] = gu[2][0]; D[3][2] = gu[2][1]; D[3][3] = gu[2][2];
+  D[3][4] = rhoinv * gmsinv * grho[2] - fact1 * (g3dlm * divu + dlm * g3divu) -
+            fact1 * two * (g1dmu * S[2][0] + g2dmu * S[2][1] + g3dmu * S[2][2] + dmu * S3jj);
+  fact1 = gamma * rhoinv / (Pr * Re);
+  fact2 = gamma * gamma1 * Ma2 * rhoinv / Re;
+  A[4][1] = gamma1 * t - fact2 * two * lm * divu - four * fact2 * mu * S[0][0];
+  A[4][2] = -(four * fact2 * mu * S[1][0]);
+  A[4][3] = -(four * fact2 * mu * S[2][0]);
+  A[4][4] = u1 - fact1 * (g1con + dcon * gt[0]);
+  B[4][1] = -(four * fact2 * mu * S[0][1]);
+  B[4][2] = gamma1 * t - fact2 * two * lm * divu - four * fact2 * mu * S[1][1];
+  B[4][3] = -(four * fact2 * mu * S[2][1]);
+  B[4][4] = u2 - fact1 * (g2con + dcon * gt[1]);
+  C[4][1] = -(four * fact2 * mu * S[0][2]);
+  C[4][2] = -(four * fact2 * mu * S[1][2]);
+  C[4][3] = gamma1 * t - fact2 * two * lm * divu - four * fact2 * mu * S[2][2];
+  C[4][4] = u3 - fact1 * (g3con + dcon * gt[2]);
+  D[4][0] = rhoinv * (u1 * gt[0] + u2 * gt[1] + u3 * gt[2] + gamma1 * t * divu);
+  D[4][1] = gt[0]; D[4][2] = gt[1]; D[4][3] = gt[2];
+  {
+    const double ssq = S[0][0] * S[0][0] + S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][0] * S[1][0] +
+                       S[1][1] * S[1][1] + S[1][2] * S[1][2] + S[2][0] * S[2][0] + S[2][1] * S[2][1] +
+                       S[2][2] * S[2][2];
+    D[4][4] = -(gamma1 * rhoinv * (u1 * grho[0] + u2 * grho[1] + u3 * grho[2]));
+    D[4][4] = D[4][4] - fact1 * (g1dcon * gt[0] + g2dcon * gt[1] + g3dcon * gt[2] + dcon * Lapt) -
+              fact2 * dlm * (divu * divu) - two * fact2 * dmu * ssq;
+  }
+  // Vij, src/genmtrx.f90:590-600
+  fact1 = 1.0 / Re;
+  fact2 = gamma / (Pr * Re);
+  Vij[0] = fact1 * rhoinv * (lm + two * mu);
+  Vij[1] = fact1 * rhoinv * mu;
+  Vij[2] = fact2 * rhoinv * con;
+  Vij[3] = fact1 * rhoinv * (lm + mu);
+  // \hat{A}, \hat{B}, src/genmtrx.f90:608-694
+  for (int pass = 0; pass < 2; ++pass) {
+    double* H = pass == 0 ? o.Ah : o.Bh;
+    const double e1 = pass == 0 ? m1 : n1, e2 = pass == 0 ? m2 : n2;
+    const double e11 = pass == 0 ? m11 : n11, e12 = pass == 0 ? m12 : n12, e22 = pass == 0 ? m22 : n22;
+    double h[5][5];
+    h[0][0] = A[0][0] * e1 + B[0][0] * e2; h[0][1] = A[0][1] * e1; h[0][2] = B[0][2] * e2; h[0][3] = 0.0; h[0][4] = 0.0;
+    h[1][0] = A[1][0] * e1;
+    h[1][1] = A[1][1] * e1 + B[1][1] * e2 - Vij[0] * e11 - Vij[1] * e22;
+    h[1][2] = A[1][2] * e1 + B[1][2] * e2 - Vij[3] * e12;
+    h[1][3] = A[1][3] * e1;
+    h[1][4] = A[1][4] * e1 + B[1][4] * e2;
+    h[2][0] = B[2][0] * e2;
+    h[2][1] = A[2][1] * e1 + B[2][1] * e2 - Vij[3] * e12;
+    h[2][2] = A[2][2] * e1 + B[2][2] * e2 - Vij[1] * e11 - Vij[0] * e22;
+    h[2][3] = B[2][3] * e2;
+    h[2][4] = A[2][4] * e1 + B[2][4] * e2;
+    h[3][0] = 0.0;
+    h[3][1] = A[3][1] * e1;
+    h[3][2] = B[3][2] * e2;
+    h[3][3] = A[3][3] * e1 + B[3][3] * e2 - Vij[1] * e11 - Vij[1] * e22;
+    h[3][4] = A[3][4] * e1 + B[3][4] * e2;
+    for (int b = 0; b < 4; ++b) h[4][b] = A[4][b] * e1 + B[4][b] * e2;
+    h[4][4] = A[4][4] * e1 + B[4][4] * e2 - Vij[2] * e11 - Vij[2] * e22;
+    if (pass == 1 && !g.yper && g.wallt == 2 && j == 1)
+      for (int a = 0; a < 5; ++a) h[a][4] = 0.0;
+    for (int a = 0; a < 5; ++a)
+      for (int b = 0; b < 5; ++b) opel(H, o, a, b, p) = h[a][b];
+  }
+  if (kzl != 0.0) {  // src/genmtrx.f90:843-848
+    D[1][1] = D[1][1] + (kzl * kzl) * Vij[1];
+    D[2][2] = D[2][2] + (kzl * kzl) * Vij[1];
+    D[3][3] = D[3][3] + (kzl * kzl) * Vij[0];
+    D[4][4] = D[4][4] + (kzl * kzl) * Vij[2];
+  }
+  for (int a = 0; a < 5; ++a)
+    for (int b = 0; b < 5; ++b) {
+      opel(o.Dh, o, a, b, p) = D[a][b];
+      opel(o.Dhi, o, a, b, p) = kzl * C[a][b] - (a == b ? g.omega : 0.0);
+    }
+  // \hat{V}, src/genmtrx.f90:867-913; 3D terms :919-925
+  const long long np = o.np;
+  o.V11[0 * np + p] = Vij[0] * m1m1 + Vij[1] * m2m2;
+  o.V11[1 * np + p] = Vij[1] * m1m1 + Vij[0] * m2m2;
+  o.V11[2 * np + p] = Vij[1] * m1m1 + Vij[1] * m2m2;
+  o.V11[3 * np + p] = Vij[2] * m1m1 + Vij[2] * m2m2;
+  o.V11[4 * np + p] = Vij[3] * m1m2;
+  o.V11[5 * np + p] = Vij[3] * m1m2;
+  o.V12[0 * np + p] = two * (Vij[0] * m1n1 + Vij[1] * m2n2);
+  o.V12[1 * np + p] = two * (Vij[1] * m1n1 + Vij[0] * m2n2);
+  o.V12[2 * np + p] = two * (Vij[1] * m1n1 + Vij[1] * m2n2);
+  o.V12[3 * np + p] = two * (Vij[2] * m1n1 + Vij[2] * m2n2);
+  o.V12[4 * np + p] = Vij[3] * (m1n2 + m2n1);
+  o.V12[5 * np + p] = Vij[3] * (m1n2 + m2n1);
+  o.V22[0 * np + p] = Vij[0] * n1n1 + Vij[1] * n2n2;
+  o.V22[1 * np + p] = Vij[1] * n1n1 + Vij[0] * n2n2;
+  o.V22[2 * np + p] = Vij[1] * n1n1 + Vij[1] * n2n2;
+  o.V22[3 * np + p] = Vij[2] * n1n1 + Vij[2] * n2n2;
+  o.V22[4 * np + p] = Vij[3] * n1n2;
+  o.V22[5 * np + p] = Vij[3] * n1n2;
+  o.AB[0 * np + p] = kzl * Vij[3] * m1;
+  o.AB[1 * np + p] = kzl * Vij[3] * m2;
+  o.AB[2 * np + p] = kzl * Vij[3] * n1;
+  o.AB[3 * np + p] = kzl * Vij[3] * n2;
+  o.AB[4 * np + p] = 0.0;
+  o.AB[5 * np + p] = 0.0;
+}
+
+// -------------------------------------------------------------- time step
+// src/temporal.f90:40-95: acoustic CFL per point; block maxima in part[]
+__global__ void cfl_kernel(Grid g, const double* __restrict__ vm, Metrics mt, double* dtl, double* part) {
+  __shared__ double red[256];
+  const long long np = (long long)g.nx * g.ny;
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double c = -1.0;
+  if (p < np) {
+    const double m1 = mt.m1[p], m2 = mt.m2[p], n1 = mt.n1[p], n2 = mt.n2[p];
+    double volinv = 1.0 / (m1 * n2 - m2 * n1);
+    const double sxj = n2 * g.dxi * volinv, syj = -m2 * g.dxi * volinv;
+    const double sxi = -n1 * g.deta * volinv, syi = m1 * g.deta * volinv;
+    volinv = 1.0 / (g.dxi * g.deta * volinv);
+    const double acoustic =
+        sqrt(sxi * sxi + two * sxi * syi + syi * syi + sxj * sxj + two * sxj * syj + syj * syj) / g.Ma;
+    const double u1 = vm[1 + 5 * p], u2 = vm[2 + 5 * p], t = sqrt(vm[4 + 5 * p]);
+    c = (fabs(u1 * sxi + u2 * syi) + fabs(u1 * sxj + u2 * syj) + t * acoustic) * volinv;
+    dtl[p] = c;
+  }
+  red[threadIdx.x] = c;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// maximum of the block maxima, then the local or global time step
+__global__ void dtl_kernel(long long np, int nparts, const double* part, double* dtl, double cflmax, double dtmax,
+                           int loctime, double* cfl_out) {
+  __shared__ double cfla;
+  if (threadIdx.x == 0) {
+    double m = -1.0;
+    for (int k = 0; k < nparts; ++k) m = fmax(m, part[k]);
+    cfla = m;
+  }
+  __syncthreads();
+  const double cfl = cfla;
+  const bool fixed = cfl * dtmax <= cflmax;
+  const double delt = fixed ? dtmax : cflmax / cfl;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < np; p += (long long)gridDim.x * blockDim.x)
+    dtl[p] = fixed ? dtmax : (loctime == 0 ? delt : cflmax / dtl[p]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *cfl_out = cfl * delt;
+}
+
+// -------------------------------------------------------------------- LHS
+// Entry (k, a, b) of the block row of point p (src/lhs1f3d.f90:53-122,
+// src/lhs2f3d.f90), given the first (ak) and second (bk) derivative
+// coefficient of slot k; `combined` selects the boundary-row form of
+// src/lhsbt2f3d.f90:44-50 in which the diagonal slot is formed as
+// dtl (a X + rcalcd alfa (Dh + i Dhi)).  The operations run in the order of
+// the reference's loops.
+__device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, long long p, int k, int a, int b,
+                                        double ak, double bk, bool combined) {
+  const long long np = o.np;
+  const long long e = (long long)((a - 1) + 5 * (b - 1)) * np + p;
+  const double x = (dir == 1 ? o.Ah : o.Bh)[e];
+  const double d = o.dtl[p], alfa = g.alfa;
+  const bool calcd = dir == 1;
+  const double rcalcd = calcd ? 1.0 : 0.0;
+  double re, im;
+  if (combined && k == 3) {
+    re = d * (ak * x + rcalcd * alfa * o.Dh[e]);
+    im = d * (0.0 + rcalcd * alfa * o.Dhi[e]);
+  } else {
+    re = ak * d * x;
+    im = 0.0;
+  }
+  // \hat{A}_i, \hat{B}_i: c_k = i a_k
+  const double w = ak * d;
+  if ((a == 2 && b == 4) || (a == 4 && b == 2)) im = im - w * o.AB[(dir == 1 ? 0 : 2) * np + p];
+  if ((a == 3 && b == 4) || (a == 4 && b == 3)) im = im - w * o.AB[(dir == 1 ? 1 : 3) * np + p];
+  if (calcd && !combined && k == 3) {
+    re = re + alfa * d * o.Dh[e];
+    im = im + alfa * d * o.Dhi[e];
+  }
+  // viscous terms: V(0) (2,2), V(4) (2,3), V(5) (3,2), V(1) (3,3), V(2) (4,4), V(3) (5,5)
+  int vk = -1;
+  if (a == 2 && b == 2) vk = 0;
+  else if (a == 2 && b == 3) vk = 4;
+  else if (a == 3 && b == 2) vk = 5;
+  else if (a == 3 && b == 3) vk = 1;
+  else if (a == 4 && b == 4) vk = 2;
+  else if (a == 5 && b == 5) vk = 3;
+  if (vk >= 0) re = re - (bk * d) * (dir == 1 ? o.V11 : o.V22)[vk * np + p];
+  if (k == 3 && a == b) re = re + 1.0;
+  return cd{re, im};
+}
+
+__device__ __forceinline__ void store_el(cd* m, long long q, cd v) { m[q] = v; }
+__device__ __forceinline__ void store_el(cf* m, long long q, cd v) { m[q] = cf{(float)v.x, (float)v.y}; }
+
+// The LHS of the xi (dir 1, src/lhs1f3d.f90 + src/lhsbc1f3d.f90) or eta
+// sweep (dir 2, src/lhs2f3d.f90 + src/lhsbt2f3d.f90 + src/lhsbc2f3d.f90),
+// mat(5,5,5,nx,ny).  One thread per entry, so consecutive threads store
+// consecutive entries; T = cf rounds the FP64 entry to FP32.
+template <typename T>
+__global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= 125 * o.np) return;
+  const long long p = q / 125;
+  const int e = (int)(q - 125 * p);
+  const int k = e % 5 + 1, a = (e / 5) % 5 + 1, b = e / 25 + 1;
+  const int i = (int)(p % g.nx) + 1, j = (int)(p / g.nx) + 1;
+  const cd one{1.0, 0.0}, zero{0.0, 0.0};
+  const cd ident = (k == 3 && a == b) ? one : zero;
+  // boundary conditions of the wall (j = 1) and top (j = ny) rows
+  if (!g.yper && (g.top == 0 || g.top == 1) && j == g.ny) return store_el(mat, q, ident);
+  if (!g.yper && g.navier && j == 1) {
+    if (dir == 1) return store_el(mat, q, ident);  // src/lhsbc1f3d.f90:24-45
+    // src/lhsbc2f3d.f90:24-66: continuity / temperature rows in slots 3,4,5,1,2
+    const double gcs[5] = {gc1, gc2, gc3, gc4, gc5};
+    const int tk = (k + 2) % 5;  // coefficient of slot k: slots 3,4,5,1,2 <-> 0..4
+    if (a >= 2 && a <= 4) return store_el(mat, q, ident);
+    if ((a == 1 && g.wall == 1) || (a == 5 && g.wallt == 1))
+      return store_el(mat, q, b == a ? cd{-gcs[tk], 0.0} : zero);
+    if (a == 5 && g.wallt == 0) return store_el(mat, q, ident);
+  }
+  const double h = dir == 1 ? g.dxi : g.deta, alfa = g.alfa;
+  const int per = dir == 1 ? g.xper : g.yper;
+  const int pos = dir == 1 ? i : j, n = dir == 1 ? g.nx : g.ny;
+  double ak, bk;
+  bool combined = false;
+  if (per || (pos > 2 && pos < n - 1)) {
+    const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
+    ak = alfa * gi[k - 1] / h;
+    bk = alfa * di[k - 1] / (h * h);
+  } else {
+    // boundary rows j = 1, 2, ny-1, ny (src/lhsbt2f3d.f90:36-600): coefficient t of slot k
+    const double hinv = 1.0 / h, hsinv = 1.0 / (h * h);
+    const double g1[5] = {gc1, gc2, gc3, gc4, gc5}, d1[5] = {dd1, dd2, dd3, dd4, dd5};
+    const double g2[5] = {gb1, gb2, gb3, gb4, gb5}, d2[5] = {db1, db2, db3, db4, db5};
+    combined = true;
+    if (pos == 1) {  // slots 3,4,5,1,2
+      const int t = (k + 2) % 5;
+      ak = alfa * g1[t] * hinv, bk = alfa * d1[t] * hsinv;
+    } else if (pos == 2) {  // slots 2,3,4,5,1
+      const int t = (k + 3) % 5;
+      ak = alfa * g2[t] * hinv, bk = alfa * d2[t] * hsinv;
+    } else if (pos == n - 1) {  // slots 4,3,2,1,5
+      const int t = k == 5 ? 4 : 4 - k;
+      ak = -(alfa * g2[t] * hinv), bk = alfa * d2[t] * hsinv;
+    } else {  // slots 3,2,1,5,4
+      const int t = k <= 3 ? 3 - k : 8 - k;
+      ak = -(alfa * g1[t] * hinv), bk = alfa * d1[t] * hsinv;
+    }
+  }
+  store_el(mat, q, lhs_entry(g, o, dir, p, k, a, b, ak, bk, combined));
+}
+
+// -------------------------------------------------------------------- RHS
+// c1v = d v / d xi (complex)
+__global__ void grad1_kernel(Grid g, const cd* __restrict__ v, cd* __restrict__ c1v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y + 1;
+  if (i > g.nx) return;
+  const long long p = pix(g, i, j);
+  for (int k = 0; k < 5; ++k) {
+    const double re = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return v[k + 5 * pix(g, ii, j)].x; });
+    const double im = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return v[k + 5 * pix(g, ii, j)].y; });
+    c1v[k + 5 * p] = cd{re, im};
+  }
+}
+
+// r = vold - v - dtl L(v) (src/lrhs3d.f90:33-218, rbe3D), then the boundary
+// rows (src/rhsbc3d.f90), written as FP64 (r64) and/or FP32 (r32); the
+// block sums of |r|^2 / dtl^2 (src/resstat3d.f90:37-46) go to part[].
+__global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __restrict__ v,
+                                                  const cd* __restrict__ vold, const cd* __restrict__ c1v,
+                                                  cd* r64, cf* r32, double* part) {
+  __shared__ double red[128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y + 1;
+  double resnod = 0.0;
+  if (i <= g.nx) {
+    const long long p = pix(g, i, j), np = o.np;
+    cd c1[5], c2[5], c11[5], c12[5], c22[5], vv[5], r[5];
+    #pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      auto VX = [&](int ii) -> const cd& { return v[k + 5 * pix(g, ii, j)]; };
+      auto VY = [&](int jj) -> const cd& { return v[k + 5 * pix(g, i, jj)]; };
+      auto CY = [&](int jj) -> const cd& { return c1v[k + 5 * pix(g, i, jj)]; };
+      vv[k] = v[k + 5 * p];
+      c1[k] = c1v[k + 5 * p];
+      c2[k] = cd{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).x; }),
+                 d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).y; })};
+      c11[k] = cd{d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).x; }),
+                  d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).y; })};
+      c22[k] = cd{d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).x; }),
+                  d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).y; })};
+      c12[k] = cd{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).x; }),
+                  d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).y; })};
+    }
+    if (g.navier && (g.wallt == 1 || g.wallt == 2) && j == 1) c2[4] = cd{0.0, 0.0};  // src/cgradbc.f90
+    auto OP = [&](const double* A, int a, int b) { return A[(long long)(a + 5 * b) * np + p]; };
+    #pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      cd acc{0.0, 0.0};
+      #pragma unroll
+      for (int b = 0; b < 5; ++b) acc = cd{acc.x + OP(o.Ah, m, b) * c1[b].x, acc.y + OP(o.Ah, m, b) * c1[b].y};
+      #pragma unroll
+      for (int b = 0; b < 5; ++b) acc = cd{acc.x + OP(o.Bh, m, b) * c2[b].x, acc.y + OP(o.Bh, m, b) * c2[b].y};
+      #pragma unroll
+      for (int b = 0; b < 5; ++b) acc = cd{acc.x + OP(o.Dh, m, b) * vv[b].x, acc.y + OP(o.Dh, m, b) * vv[b].y};
+      r[m] = acc;
+    }
+    auto VH = [&](const double* A, int k) { return A[(long long)k * np + p]; };
+    auto sub = [&](int m, double c, const cd& z) { r[m] = cd{r[m].x - c * z.x, r[m].y - c * z.y}; };
+    const double* Vs[3] = {o.V11, o.V12, o.V22};
+    const cd* Cs[3] = {c11, c12, c22};
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      sub(1, VH(Vs[s], 0), Cs[s][1]); sub(1, VH(Vs[s], 4), Cs[s][2]);
+      sub(2, VH(Vs[s], 5), Cs[s][1]); sub(2, VH(Vs[s], 1), Cs[s][2]);
+      sub(3, VH(Vs[s], 2), Cs[s][3]);
+      sub(4, VH(Vs[s], 3), Cs[s][4]);
+    }
+    // 3D terms, im * z = (-Im z, Re z)
+    const double a1 = VH(o.AB, 0), a2 = VH(o.AB, 1), a3 = VH(o.AB, 2), a4 = VH(o.AB, 3);
+    {
+      cd s1{a1 * c1[3].x + a3 * c2[3].x, a1 * c1[3].y + a3 * c2[3].y};
+      r[1] = cd{r[1].x + s1.y, r[1].y - s1.x};
+      cd s2{a2 * c1[3].x + a4 * c2[3].x, a2 * c1[3].y + a4 * c2[3].y};
+      r[2] = cd{r[2].x + s2.y, r[2].y - s2.x};
+      cd s3{a1 * c1[1].x + a2 * c1[2].x + a3 * c2[1].x + a4 * c2[2].x,
+            a1 * c1[1].y + a2 * c1[2].y + a3 * c2[1].y + a4 * c2[2].y};
+      r[3] = cd{r[3].x + s3.y, r[3].y - s3.x};
+    }
+    #pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      cd s{0.0, 0.0};
+      #pragma unroll
+      for (int b = 0; b < 5; ++b) s = cd{s.x + OP(o.Dhi, m, b) * vv[b].x, s.y + OP(o.Dhi, m, b) * vv[b].y};
+      r[m] = cd{r[m].x - s.y, r[m].y + s.x};
+    }
+    // rbe3D
+    const double dtl = o.dtl[p];
+    #pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const cd vo = vold[m + 5 * p];
+      r[m] = cd{vo.x - vv[m].x - dtl * r[m].x, vo.y - vv[m].y - dtl * r[m].y};
+    }
+    // boundary rows, src/rhsbc3d.f90:34-170
+    if (!g.yper) {
+      if (g.navier && j == 1) {
+        for (int m = 1; m <= 3; ++m) r[m] = cd{-(vv[m].x - 0.0), -(vv[m].y - 0.0)};
+        auto W = [&](int k, int jj) -> const cd& { return v[k + 5 * pix(g, i, jj)]; };
+        if (g.wall == 1)
+          r[0] = cd{gc1 * W(0, 1).x + gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x,
+                    gc1 * W(0, 1).y + gc2 * W(0, 2).y + gc3 * W(0, 3).y + gc4 * W(0, 4).y + gc5 * W(0, 5).y};
+        if (g.wall == 2)
+          r[0] = cd{W(0, 1).x - two * W(0, 2).x + W(0, 3).x, W(0, 1).y - two * W(0, 2).y + W(0, 3).y};
+        if (g.wallt == 0) r[4] = cd{0.0, 0.0};
+        if (g.wallt == 1)
+          r[4] = cd{gc1 * W(4, 1).x + gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x,
+                    gc1 * W(4, 1).y + gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y};
+      }
+      if (g.top == 0 && j == g.ny)
+        #pragma unroll
+        for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
+    } else if (j == g.ny) {
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
+    }
+    if (g.xper && i == g.nx)
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
+    #pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      if (r64) r64[m + 5 * p] = r[m];
+      if (r32) r32[m + 5 * p] = cf{(float)r[m].x, (float)r[m].y};
+      resnod += r[m].x * r[m].x + r[m].y * r[m].y;
+    }
+    resnod = resnod / (dtl * dtl);
+  }
+  red[threadIdx.x] = resnod;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = red[0];
+}
+
+// totres = sqrt(sum / (nx ny)) in a fixed summation order
+__global__ void resid_kernel(int nparts, const double* part, long long npts, double* out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += part[k];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sqrt(red[0] / (double)npts);
+}
+
+// ----------------------------------------------------------------- update
+// v += r (add) and the boundary values of src/itrbc3d.f90:35-205; one
+// thread per column i.  The periodic copy of column 1 to column nx is a
+// separate launch (periodic_copy_kernel).
+template <typename RT>
+__global__ void update_kernel(Grid g, cd* __restrict__ v, const RT* __restrict__ r, int add) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > g.nx) return;
+  if (add)
+    for (int j = 1; j <= g.ny; ++j)
+      for (int m = 0; m < 5; ++m) {
+        cd& x = v[m + 5 * pix(g, i, j)];
+        const cd d = to_hi(r[m + 5 * pix(g, i, j)]);
+        x = cd{x.x + d.x, x.y + d.y};
+      }
+  if (!g.yper) {
+    if (g.navier) {
+      auto W = [&](int k, int jj) -> cd& { return v[k + 5 * pix(g, i, jj)]; };
+      for (int m = 1; m <= 3; ++m) W(m, 1) = cd{0.0, 0.0};
+      if (g.wall == 1)
+        W(0, 1) = cd{-(gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x) / gc1,
+                     -(gc2 * W(0, 2).y + gc3 * W(0, 3).y + gc4 * W(0, 4).y + gc5 * W(0, 5).y) / gc1};
+      if (g.wall == 2) W(0, 1) = cd{two * W(0, 2).x - W(0, 3).x, two * W(0, 2).y - W(0, 3).y};
+      if (g.wallt == 0) W(4, 1) = cd{0.0, 0.0};
+      if (g.wallt == 1)
+        W(4, 1) = cd{-(gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x) / gc1,
+                     -(gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y) / gc1};
+    }
+    if (g.top == 0)
+      for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, i, g.ny)] = cd{0.0, 0.0};
+  } else {
+    for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, i, g.ny)] = v[m + 5 * pix(g, i, 1)];
+  }
+}
+__global__ void periodic_copy_kernel(Grid g, cd* v) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > g.ny) return;
+  for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, g.nx, j)] = v[m + 5 * pix(g, 1, j)];
+}
+
+}  // namespace a3
+}  // namespace lns
+
+// ======================================================================
+// Context and C ABI
+// ======================================================================
+using lns::cd;
+using lns::cf;
+using lns::a3::Grid;
+using lns::a3::Metrics;
+using lns::a3::Ops;
+
+struct lns_ctx3d {
+  lns_params3d prm;
+  Grid g;
+  int device = -1;
+  long long np = 0;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+  double* metrics = nullptr;  // (nx,ny,10)
+  double* vm = nullptr;       // (5,nx,ny)
+  double* opbuf = nullptr;    // Ah Bh Dh Dhi (25 np each), V11 V12 V22 AB (6 np each), dtl (np)
+  Ops ops{};
+  cd *v = nullptr, *vold = nullptr, *r64 = nullptr, *c1v = nullptr;
+  cf* r32 = nullptr;
+  void *matx = nullptr, *maty = nullptr, *perx = nullptr, *per2x = nullptr;
+  double* part = nullptr;  // block partials (residual, CFL)
+  int nparts = 0;
+  double* dscal = nullptr;  // [0] cfl, [1..] residual of the inspection call
+  double* res_dev = nullptr;  // residual history of the host-form steps
+  int res_cap = 0;
+  int* status = nullptr;
+  bool have_metrics = false, have_mean = false, factored = false;
+  // phase timing (lns_ctx3d_profile): per corrector, events before the RHS,
+  // after the RHS, after the xi sweep, after the eta sweep, after the update
+  bool profile = false;
+  std::vector<cudaEvent_t> events;
+  size_t ev_used = 0;
+};
+
+namespace {
+
+int fail3(int code, const std::string& msg) { return lns_fail(code, msg); }
+int cuda3(cudaError_t e, const char* where) { return lns_cuda_fail(e, where); }
+
+// interior stencil coefficients, src/cgrad.f90:35-75 and src/cgrad2.f90:38-100
+void coef1(int opt, double dinv, double g[6]) {
+  double c, a, b;
+  if (opt == 0) c = 1.0 / 60.0;
+  else if (opt == -1) c = 0.0;
+  else {
+    const double w = 2.0 * 3.1415926535897932385e+0 / 12.0;
+    c = (w / 2.0 - 2.0 * sin(w) / 3.0 + sin(2.0 * w) / 12.0) / (5.0 * sin(w) - 4.0 * sin(2.0 * w) + sin(3.0 * w));
+  }
+  a = (2.0 + 15.0 * c) / 3.0;
+  b = -(1.0 + 48.0 * c) / 12.0;
+  g[0] = -c * dinv; g[1] = -b * dinv; g[2] = -a * dinv;
+  g[3] = a * dinv;  g[4] = b * dinv;  g[5] = c * dinv;
+}
+void coef2(int opt, double dsinv, double d[7]) {
+  double c, a, b;
+  if (opt == 0) c = 1.0 / 90.0;
+  else if (opt == -1) c = 0.0;
+  else {
+    const double w = 2.0 * 3.1415926535897932385e+0 / 12.0;
+    const double s1 = sin(w / 2.0), s2 = sin(w), s3 = sin(3.0 * w / 2.0);
+    c = -(3.0 * (w * w) - 16.0 * (s1 * s1) + (s2 * s2)) / (12.0 * (-15.0 * (s1 * s1) + 6.0 * (s2 * s2) - (s3 * s3)));
+  }
+  a = (4.0 + 45.0 * c) / 3.0;
+  b = -(1.0 + 72.0 * c) / 12.0;
+  d[0] = c * dsinv; d[1] = b * dsinv; d[2] = a * dsinv; d[3] = -2.0 * (a + b + c) * dsinv;
+  d[4] = a * dsinv; d[5] = b * dsinv; d[6] = c * dsinv;
+}
+
+int dalloc(lns_ctx3d* c, size_t bytes, void** out) {
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  c->allocs.push_back(*out);
+  c->bytes += bytes;
+  return LNS_OK;
+}
+
+void free_all(lns_ctx3d* c) {
+  for (void* p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+  for (cudaEvent_t e : c->events) cudaEventDestroy(e);
+  c->events.clear();
+}
+
+// records the next profiling event on `st` (no-op unless profiling)
+int mark(lns_ctx3d* c, cudaStream_t st) {
+  if (!c->profile) return LNS_OK;
+  if (c->ev_used == c->events.size()) {
+    cudaEvent_t e;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return cuda3(r, "cudaEventCreate");
+    c->events.push_back(e);
+  }
+  cudaError_t r = cudaEventRecord(c->events[c->ev_used++], st);
+  return r == cudaSuccess ? LNS_OK : cuda3(r, "cudaEventRecord");
+}
+
+int check_device(const lns_ctx3d* c) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda3(e, "cudaGetDevice");
+  if (dev != c->device) return fail3(LNS_ERR_ARG, "context belongs to another device");
+  return LNS_OK;
+}
+
+Metrics metrics_of(const lns_ctx3d* c) {
+  const double* m = c->metrics;
+  const long long np = c->np;
+  return Metrics{m, m + np, m + 2 * np, m + 3 * np, m + 4 * np, m + 5 * np, m + 6 * np, m + 7 * np, m + 8 * np,
+                 m + 9 * np};
+}
+
+dim3 pt_grid(const Grid& g) { return dim3((g.nx + 127) / 128, g.ny); }
+
+// residual history buffer of at least n entries
+int res_reserve(lns_ctx3d* c, int n) {
+  if (c->res_cap >= n) return LNS_OK;
+  void* p = nullptr;
+  int rc = dalloc(c, sizeof(double) * (size_t)n, &p);
+  if (rc) return rc;
+  c->res_dev = (double*)p;
+  c->res_cap = n;
+  return LNS_OK;
+}
+
+// r = RHS of one corrector into r64 (FP64) and / or r32 (FP32); totres to *res.
+int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vold, cd* r64, cf* r32, double* res, cudaStream_t st) {
+  const Grid& g = c->g;
+  lns::a3::grad1_kernel<<<pt_grid(g), 128, 0, st>>>(g, v, c->c1v);
+  lns::a3::rhs_kernel<<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vold, c->c1v, r64, r32, c->part);
+  const int nrhs = (int)(pt_grid(g).x * pt_grid(g).y);  // rhs_kernel block partials
+  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "rhs kernels launch");
+}
+
+template <typename T>
+int launch_lhs(lns_ctx3d* c, int dir, T* mat, cudaStream_t st) {
+  const long long nq = 125 * c->np;
+  lns::a3::lhs_kernel<T><<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->g, c->ops, dir, mat);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "lhs_kernel launch");
+}
+
+// Forms and factors both LHS (code 0), then checks the pivots.
+template <typename T>
+int factor_all(lns_ctx3d* c, cudaStream_t st) {
+  const Grid& g = c->g;
+  T* mx = (T*)c->matx;
+  T* my = (T*)c->maty;
+  T* rr = c->r32 ? (T*)c->r32 : (T*)c->r64;  // right-hand side: not touched by code 0
+  cudaError_t e = cudaMemsetAsync(c->status, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda3(e, "cudaMemsetAsync");
+  int rc = launch_lhs<T>(c, 1, mx, st);
+  if (!rc) rc = lns::host::launch_p<T>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status);
+  if (!rc) rc = launch_lhs<T>(c, 2, my, st);
+  if (!rc) rc = lns::host::launch_bc<T>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
+  if (rc) return rc;
+  int status = 0;
+  e = cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda3(e, "LHS factorisation");
+  if (status) return fail3(LNS_ERR_PIVOT, "zero or non-finite pivot in the LHS factorisation");
+  c->factored = true;
+  return LNS_OK;
+}
+
+// v += r and the boundary values (itrBC3D); add = 0 applies only the latter.
+template <typename RT>
+int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
+  const Grid& g = c->g;
+  lns::a3::update_kernel<RT><<<(g.nx + 127) / 128, 128, 0, st>>>(g, v, r, add);
+  if (g.xper) lns::a3::periodic_copy_kernel<<<(g.ny + 127) / 128, 128, 0, st>>>(g, v);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "update kernels launch");
+}
+
+// nsteps steps of niter correctors on device v (src/impdrv3d.f90:130-356)
+int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cudaStream_t st) {
+  const Grid& g = c->g;
+  const bool mixed = c->prm.precision == LNS_MIXED;
+  int rc;
+  if (!c->factored) {
+    rc = mixed ? factor_all<cf>(c, st) : factor_all<cd>(c, st);
+    if (rc) return rc;
+  }
+  const size_t vbytes = sizeof(cd) * 5 * (size_t)c->np;
+  for (int s = 0; s < nsteps; ++s) {
+    cudaError_t e = cudaMemcpyAsync(c->vold, v, vbytes, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda3(e, "cudaMemcpyAsync vold");
+    rc = launch_update<cd>(c, v, (const cd*)nullptr, 0, st);
+    if (rc) return rc;
+    for (int it = 0; it < niter; ++it) {
+      double* res = (it == niter - 1 && totres_dev) ? totres_dev + s : c->dscal + 1;
+      rc = mark(c, st);
+      if (mixed) {
+        if (!rc) rc = launch_rhs(c, v, c->vold, nullptr, c->r32, res, st);
+        if (!rc) rc = mark(c, st);
+        if (!rc) rc = lns::host::launch_solve<cf, true>(c->matx, c->r32, c->perx, c->per2x, g.nx - 1, g.ny, 1, g.nx, st);
+        if (!rc) rc = mark(c, st);
+        if (!rc) rc = lns::host::launch_solve<cf, false>(c->maty, c->r32, nullptr, nullptr, g.ny, g.nx, g.nx, 1, st);
+        if (!rc) rc = mark(c, st);
+        if (!rc) rc = launch_update<cf>(c, v, c->r32, 1, st);
+      } else {
+        if (!rc) rc = launch_rhs(c, v, c->vold, c->r64, nullptr, res, st);
+        if (!rc) rc = mark(c, st);
+        if (!rc) rc = lns::host::launch_solve<cd, true>(c->matx, c->r64, c->perx, c->per2x, g.nx - 1, g.ny, 1, g.nx, st);
+        if (!rc) rc = mark(c, st);
+        if (!rc) rc = lns::host::launch_solve<cd, false>(c->maty, c->r64, nullptr, nullptr, g.ny, g.nx, g.nx, 1, st);
+        if (!rc) rc = mark(c, st);
+        if (!rc) rc = launch_update<cd>(c, v, c->r64, 1, st);
+      }
+      if (!rc) rc = mark(c, st);
+      if (rc) return rc;
+    }
+  }
+  return LNS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
+  if (!p || !out) return fail3(LNS_ERR_ARG, "ctx3d_create: null argument");
+  *out = nullptr;
+  if (p->nx < 8 || p->ny < 7) return fail3(LNS_ERR_ARG, "ctx3d_create: need nx >= 8 and ny >= 7");
+  if ((long long)p->nx * p->ny > (1LL << 31) / 125)
+    return fail3(LNS_ERR_ARG, "ctx3d_create: nx*ny too large for 32-bit launch indexing");
+  if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
+  if (p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: only a periodic xi direction (xper = 1) is supported");
+  if (p->yper != 0 || p->navier != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: need yper = 0 and navier = 1");
+  if (p->wall != 1 && p->wall != 2) return fail3(LNS_ERR_ARG, "ctx3d_create: wall must be 1 or 2");
+  if (p->wallt != 0 && p->wallt != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: wallt must be 0 or 1");
+  if (p->top != 0) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0");
+  if (p->loctime != 0 && p->loctime != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: loctime must be 0 or 1");
+  if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
+    return fail3(LNS_ERR_ARG, "ctx3d_create: precision must be LNS_FP64 or LNS_MIXED");
+  lns_ctx3d* c = new lns_ctx3d();
+  c->prm = *p;
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda3(e, "cudaGetDevice");
+  }
+  Grid& g = c->g;
+  g.nx = p->nx; g.ny = p->ny; g.dxi = p->dxi; g.deta = p->deta;
+  g.Ma = p->Ma; g.Re = p->Re; g.Pr = p->Pr; g.gamma = p->gamma; g.gamma1 = p->gamma - 1.0;
+  g.omega = p->omega; g.kz = p->beta; g.alfa = p->alfa;
+  g.xper = p->xper; g.yper = p->yper; g.navier = p->navier; g.wall = p->wall; g.wallt = p->wallt; g.top = p->top;
+  g.dxinv = 1.0 / p->dxi; g.dyinv = 1.0 / p->deta;
+  g.dxsinv = 1.0 / (p->dxi * p->dxi); g.dysinv = 1.0 / (p->deta * p->deta);
+  coef1(p->optx, g.dxinv, g.gx);
+  coef1(p->opty, g.dyinv, g.gy);
+  coef2(p->optx, g.dxsinv, g.dx2);
+  coef2(p->opty, g.dysinv, g.dy2);
+  const long long np = (long long)p->nx * p->ny;
+  c->np = np;
+  c->nparts = std::max(((p->nx + 127) / 128) * p->ny, (int)((np + 255) / 256));
+  const bool mixed = p->precision == LNS_MIXED;
+  const size_t el = mixed ? sizeof(cf) : sizeof(cd);
+  void* q = nullptr;
+  int rc = LNS_OK;
+  auto A = [&](size_t bytes, void** dst) {
+    if (!rc) rc = dalloc(c, bytes, dst);
+  };
+  A(sizeof(double) * 10 * np, &q); c->metrics = (double*)q;
+  A(sizeof(double) * 5 * np, &q); c->vm = (double*)q;
+  A(sizeof(double) * (4 * 25 + 4 * 6 + 1) * np, &q); c->opbuf = (double*)q;
+  A(sizeof(cd) * 5 * np, &q); c->v = (cd*)q;
+  A(sizeof(cd) * 5 * np, &q); c->vold = (cd*)q;
+  A(sizeof(cd) * 5 * np, &q); c->c1v = (cd*)q;
+  if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
+  else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
+  A(el * 125 * np, &c->matx);
+  A(el * 125 * np, &c->maty);
+  A(el * 50 * np, &c->perx);
+  A(el * 50 * np, &c->per2x);
+  A(sizeof(double) * c->nparts, &q); c->part = (double*)q;
+  A(sizeof(double) * 2, &q); c->dscal = (double*)q;
+  A(sizeof(int), &q); c->status = (int*)q;
+  if (!rc) rc = res_reserve(c, 64);
+  if (rc) {
+    free_all(c);
+    delete c;
+    return rc;
+  }
+  if (!mixed) c->r32 = nullptr;
+  double* o = c->opbuf;
+  c->ops.np = np;
+  c->ops.Ah = o; c->ops.Bh = o + 25 * np; c->ops.Dh = o + 50 * np; c->ops.Dhi = o + 75 * np;
+  c->ops.V11 = o + 100 * np; c->ops.V12 = o + 106 * np; c->ops.V22 = o + 112 * np; c->ops.AB = o + 118 * np;
+  c->ops.dtl = o + 124 * np;
+  *out = c;
+  return LNS_OK;
+}
+
+int lns_ctx3d_destroy(lns_ctx3d* c) {
+  if (!c) return LNS_OK;
+  free_all(c);
+  delete c;
+  return LNS_OK;
+}
+
+size_t lns_ctx3d_bytes(const lns_ctx3d* c) { return c ? c->bytes : 0; }
+
+int lns_upload_metrics3d(lns_ctx3d* c, const double* metrics) {
+  if (!c || !metrics) return fail3(LNS_ERR_ARG, "upload_metrics3d: null argument");
+  int rc = check_device(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->metrics, metrics, sizeof(double) * 10 * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload metrics");
+  c->have_metrics = true;
+  c->have_mean = false;
+  c->factored = false;
+  return LNS_OK;
+}
+
+int lns_upload_mean3d(lns_ctx3d* c, const double* vm, double* cfl) {
+  if (!c || !vm) return fail3(LNS_ERR_ARG, "upload_mean3d: null argument");
+  if (!c->have_metrics) return fail3(LNS_ERR_ARG, "upload_mean3d: upload the metrics first");
+  int rc = check_device(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->vm, vm, sizeof(double) * 5 * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload mean flow");
+  const Grid& g = c->g;
+  const Metrics mt = metrics_of(c);
+  lns::a3::genmtrx_kernel<<<pt_grid(g), 128>>>(g, c->vm, mt, c->ops);
+  const int nb = (int)((c->np + 255) / 256);
+  lns::a3::cfl_kernel<<<nb, 256>>>(g, c->vm, mt, c->ops.dtl, c->part);
+  lns::a3::dtl_kernel<<<152, 256>>>(c->np, nb, c->part, c->ops.dtl, c->prm.cflmax, c->prm.dtmax, c->prm.loctime,
+                                    c->dscal);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda3(e, "operator kernels launch");
+  double h = 0.0;
+  e = cudaMemcpy(&h, c->dscal, sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda3(e, "operator build");
+  if (cfl) *cfl = h;
+  c->have_mean = true;
+  c->factored = false;
+  return LNS_OK;
+}
+
+int lns_step3d_dev(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream) {
+  if (!c || !v) return fail3(LNS_ERR_ARG, "step3d: null argument");
+  if (nsteps < 0 || niter < 1) return fail3(LNS_ERR_ARG, "step3d: need nsteps >= 0 and niter >= 1");
+  if (!c->have_mean) return fail3(LNS_ERR_ARG, "step3d: upload the metrics and the mean flow first");
+  int rc = check_device(c);
+  if (rc) return rc;
+  return run_steps(c, (cd*)v, nsteps, niter, totres_dev, (cudaStream_t)stream);
+}
+
+int lns_step3d(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, double* totres) {
+  if (!c || !v) return fail3(LNS_ERR_ARG, "step3d: null argument");
+  if (nsteps < 0 || niter < 1) return fail3(LNS_ERR_ARG, "step3d: need nsteps >= 0 and niter >= 1");
+  if (!c->have_mean) return fail3(LNS_ERR_ARG, "step3d: upload the metrics and the mean flow first");
+  int rc = check_device(c);
+  if (rc) return rc;
+  if (totres && (rc = res_reserve(c, nsteps))) return rc;
+  const size_t vbytes = sizeof(cd) * 5 * (size_t)c->np;
+  cudaError_t e = cudaMemcpy(c->v, v, vbytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload v");
+  rc = run_steps(c, c->v, nsteps, niter, totres ? c->res_dev : nullptr, 0);
+  if (rc) return rc;
+  e = cudaMemcpy(v, c->v, vbytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda3(e, "download v");
+  if (totres && nsteps > 0) {
+    e = cudaMemcpy(totres, c->res_dev, sizeof(double) * nsteps, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda3(e, "download totres");
+  }
+  return LNS_OK;
+}
+
+int lns_rhs3d_dev(lns_ctx3d* c, const double* v, const double* vold, double* r, double* totres_dev, void* stream) {
+  if (!c || !v || !vold || !r) return fail3(LNS_ERR_ARG, "rhs3d: null argument");
+  if (!c->have_mean) return fail3(LNS_ERR_ARG, "rhs3d: upload the metrics and the mean flow first");
+  int rc = check_device(c);
+  if (rc) return rc;
+  return launch_rhs(c, (const cd*)v, (const cd*)vold, (cd*)r, nullptr, totres_dev ? totres_dev : c->dscal + 1,
+                    (cudaStream_t)stream);
+}
+
+int lns_lhs3d_dev(lns_ctx3d* c, int32_t dir, double* mat, void* stream) {
+  if (!c || !mat) return fail3(LNS_ERR_ARG, "lhs3d: null argument");
+  if (dir != 1 && dir != 2) return fail3(LNS_ERR_ARG, "lhs3d: dir must be 1 or 2");
+  if (!c->have_mean) return fail3(LNS_ERR_ARG, "lhs3d: upload the metrics and the mean flow first");
+  int rc = check_device(c);
+  if (rc) return rc;
+  return launch_lhs<cd>(c, dir, (cd*)mat, (cudaStream_t)stream);
+}
+
+int lns_ctx3d_profile(lns_ctx3d* c, int32_t on) {
+  if (!c) return fail3(LNS_ERR_ARG, "ctx3d_profile: null context");
+  c->profile = on != 0;
+  c->ev_used = 0;
+  return LNS_OK;
+}
+
+int lns_ctx3d_profile_read(lns_ctx3d* c, double* ms, int32_t* ncorr) {
+  if (!c || !ms || !ncorr) return fail3(LNS_ERR_ARG, "ctx3d_profile_read: null argument");
+  for (int k = 0; k < 4; ++k) ms[k] = 0.0;
+  *ncorr = 0;
+  const size_t n = c->ev_used / 5;
+  for (size_t q = 0; q < n; ++q) {
+    for (int k = 0; k < 4; ++k) {
+      cudaError_t e = cudaEventSynchronize(c->events[5 * q + k + 1]);
+      float t = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&t, c->events[5 * q + k], c->events[5 * q + k + 1]);
+      if (e != cudaSuccess) return cuda3(e, "profile events");
+      ms[k] += t;
+    }
+  }
+  *ncorr = (int32_t)n;
+  c->ev_used = 0;
+  return LNS_OK;
+}
+
+int lns_get_field3d(lns_ctx3d* c, int32_t which, double* out) {
+  if (!c || !out) return fail3(LNS_ERR_ARG, "get_field3d: null argument");
+  if (which < 0 || which > 8) return fail3(LNS_ERR_ARG, "get_field3d: which must be 0..8");
+  if (!c->have_mean) return fail3(LNS_ERR_ARG, "get_field3d: upload the metrics and the mean flow first");
+  int rc = check_device(c);
+  if (rc) return rc;
+  const long long np = c->np;
+  const double* src[9] = {c->ops.Ah, c->ops.Bh, c->ops.Dh, c->ops.Dhi, c->ops.V11,
+                          c->ops.V12, c->ops.V22, c->ops.AB, c->ops.dtl};
+  const int nel = which < 4 ? 25 : (which < 8 ? 6 : 1);
+  std::vector<double> h((size_t)nel * np);
+  cudaError_t e = cudaMemcpy(h.data(), src[which], sizeof(double) * h.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda3(e, "get_field3d copy");
+  for (long long p = 0; p < np; ++p)
+    for (int k = 0; k < nel; ++k) out[k + (long long)nel * p] = h[(size_t)k * np + p];
+  return LNS_OK;
+}
+
+}  // extern "C"

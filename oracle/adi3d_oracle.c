@@ -13,6 +13,15 @@
 #include "penta_oracle.h"
 
 /* src/stencil.f90:10-94 (the reference's coefficient table) */
+/* Line and row loops are independent; the timing build (-fopenmp) runs them
+   in parallel, the parity build (no -fopenmp) serially.  The residual sum
+   stays serial so its order is the same in both. */
+#ifdef _OPENMP
+#define OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define OMP_FOR
+#endif
+
 static const double ga1 = 8.333333333333333333333E-02, ga2 = -6.666666666666666666667E-01,
                     ga3 = 6.666666666666666666667E-01, ga4 = -8.333333333333333333333E-02;
 static const double gc1 = -2.083333333333333333333E+00, gc2 = 4.000000000000000000000E+00,
@@ -133,9 +142,11 @@ int a3_deriv1(const A3Grid* g, int nc, const double* v, double* g1v, double* g2v
   coef1(g->optx, one / g->dxi, gx);
   coef1(g->opty, one / g->deta, gy);
   const int nx = g->nx, ny = g->ny;
+  OMP_FOR
   for (int j = 1; j <= ny; ++j)
     for (int c = 0; c < nc; ++c)
       line_d1(nx, g->xper, &FV(v, nc, c, g, 1, j), nc, &FV(g1v, nc, c, g, 1, j), nc, gx, one / g->dxi);
+  OMP_FOR
   for (int i = 1; i <= nx; ++i)
     for (int c = 0; c < nc; ++c)
       line_d1(ny, g->yper, &FV(v, nc, c, g, i, 1), (long)nc * nx, &FV(g2v, nc, c, g, i, 1), (long)nc * nx, gy,
@@ -152,9 +163,11 @@ int a3_deriv2(const A3Grid* g, int nc, const double* v, const double* g1v, doubl
   coef2(g->opty, dysinv, dy);
   coef1(g->opty, one / g->deta, gy);
   const int nx = g->nx, ny = g->ny;
+  OMP_FOR
   for (int j = 1; j <= ny; ++j)
     for (int c = 0; c < nc; ++c)
       line_d2(nx, g->xper, &FV(v, nc, c, g, 1, j), nc, &FV(g11v, nc, c, g, 1, j), nc, dx, dxsinv);
+  OMP_FOR
   for (int i = 1; i <= nx; ++i)
     for (int c = 0; c < nc; ++c) {
       line_d2(ny, g->yper, &FV(v, nc, c, g, i, 1), (long)nc * nx, &FV(g22v, nc, c, g, i, 1), (long)nc * nx, dy,
@@ -183,6 +196,7 @@ int a3_genmtrx(const A3Grid* g, const double* vl, A3Ops* o) {
   if (g->navier && !g->yper && (g->wallt == 1 || g->wallt == 2))  /* gradbc.f90 */
     for (int i = 1; i <= nx; ++i) FV(g2v, 5, 4, g, i, 1) = zero;
   const double gamma = g->gamma, gamma1 = g->gamma1, Ma = g->Ma, Re = g->Re, Pr = g->Pr, kzl = g->kz;
+  OMP_FOR
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) {
       const long p = IX(g, i, j);
@@ -465,6 +479,7 @@ int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
   a3_deriv2(g, 10, vl, c1v, c11v, c12v, c22v);
   if (g->navier && (g->wallt == 1 || g->wallt == 2)) /* src/cgradbc.f90 */
     for (int i = 1; i <= nx; ++i) CRE(c2v, 4, g, i, 1) = zero, CIM(c2v, 4, g, i, 1) = zero;
+  OMP_FOR
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) {
       const long p = IX(g, i, j);
@@ -545,6 +560,7 @@ int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
 
 /* rbe3D, src/impdrv3d.f90:444-469: r = vold - v - dtl r */
 void a3_rbe(const A3Grid* g, double* r, const double* v, const double* vold, const double* dtl) {
+  OMP_FOR
   for (int j = 1; j <= g->ny; ++j)
     for (int i = 1; i <= g->nx; ++i)
       for (int k = 0; k < 10; ++k) {
@@ -700,6 +716,7 @@ int a3_lhs(const A3Grid* g, const A3Ops* o, const double* dtl, int dir, double* 
   /* interior rows: slots 1..5 <-> columns -2..+2 */
   const double gi[5] = {ga1, ga2, zero, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
   for (int k = 0; k < 5; ++k) ak[k] = alfa * gi[k] / h, bk[k] = alfa * di[k] / (h * h);
+  OMP_FOR
   for (int j = 1; j <= ny; ++j)
     for (int i = 1; i <= nx; ++i) lhs_row(g, o, dtl, dir, IX(g, i, j), ak, bk, 0, mat);
   if (!per) {
@@ -789,6 +806,7 @@ double a3_step(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, do
     if (g->xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 1, ORC_COMPAT_PERIODIC_SLOT);
     else orc_cpenta_bc(2, nx, ny, matx, r, 1, 0);
     orc_cpenta_bc(1, ny, nx, maty, r, 1, 0);
+    OMP_FOR
     for (long e = 0; e < n10; ++e) v[e] = v[e] + r[e];
     a3_itrbc(g, v);
   }

@@ -83,6 +83,14 @@ static const ocx cx_one = {1.0, 0.0};
 
 /* ----------------------------------------------------------------- API */
 
+/* Lines are independent: the timing build (-fopenmp) solves them in
+   parallel, the parity build serially. */
+#ifdef _OPENMP
+#define OMP_FOR _Pragma("omp parallel for schedule(static)")
+#else
+#define OMP_FOR
+#endif
+
 static int check(int layout, int n, int nsys) {
   if (layout != 1 && layout != 2) return 1;
   if (n < 7 || nsys < 0) return 2;
@@ -172,11 +180,13 @@ int orc_cpenta_bc(int layout, int n, int nsys, double* mat, double* rhs, int cod
   ocx* M = (ocx*)mat;
   ocx* R = (ocx*)rhs;
   if (code == 0 || code == 2)
+    OMP_FOR
     for (int iv = 0; iv < nsys; ++iv) {
       Line_c L = {0, layout, n, n, nsys, iv, M, R, NULL, NULL};
       factor_c(&L, 1, 0);
     }
   if (code == 1 || code == 2)
+    OMP_FOR
     for (int iv = 0; iv < nsys; ++iv) {
       Line_c L = {0, layout, n, n, nsys, iv, M, R, NULL, NULL};
       forward_c(&L, flags, R, layout);
@@ -195,12 +205,14 @@ int orc_cpenta_p(int layout, int np, int nsys, double* mat, double* rhs, double*
   ocx* M = (ocx*)mat;
   ocx* R = (ocx*)rhs;
   if (code == 0 || code == 2)
+    OMP_FOR
     for (int iv = 0; iv < nsys; ++iv) {
       Line_c L = {1, layout, n, np, nsys, iv, M, R, (ocx*)per, (ocx*)per2};
       setup_c(&L);
       factor_c(&L, 1, flags);
     }
   if (code == 1 || code == 2)
+    OMP_FOR
     for (int iv = 0; iv < nsys; ++iv) {
       Line_c L = {1, layout, n, np, nsys, iv, M, R, (ocx*)per, (ocx*)per2};
       forward_c(&L, 0, R, layout);

@@ -43,7 +43,7 @@ def test_python_signatures_cover_header():
 
     solver_syms = [n for n in declared_symbols()
                    if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops",
-                                "lns_mixed_workspace_bytes")]
+                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes")]
     assert sorted(SIGNATURES) == solver_syms
 
 
@@ -104,3 +104,38 @@ def test_mixed_argument_errors(lib, refine):
     a = np.zeros(2 * 125 * 64)
     assert lib.lns_cpenta2bc_mixed_dev(8, 8, 5, a.ctypes.data, a.ctypes.data, 2, refine, None, None) == 1
     assert lib.lns_cpenta2bc_mixed(8, 8, 5, a.ctypes.data, a.ctypes.data, refine) == 1
+
+
+def _params3d(**kw):
+    from lns3d_gb300._lib import Params3D
+
+    base = dict(nx=64, ny=32, dxi=1 / 63, deta=1 / 31, Ma=0.8, Re=500.0, Pr=0.72, gamma=1.4, omega=0.05, beta=0.2,
+                alfa=1.0, cflmax=1.0, dtmax=1e30, loctime=1, xper=1, yper=0, navier=1, wall=1, wallt=1, top=0,
+                optx=-1, opty=-1, precision=0)
+    base.update(kw)
+    return Params3D(**base)
+
+
+@pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=0), dict(wallt=2),
+                                 dict(top=1), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
+                                 dict(loctime=2)])
+def test_ctx3d_rejects_unsupported_options(lib, bad):
+    ctx = ctypes.c_void_p()
+    rc = lib.lns_ctx3d_create(ctypes.byref(_params3d(**bad)), ctypes.byref(ctx))
+    assert rc == 1 and not ctx.value
+    assert lib.lns_last_error()
+
+
+def test_ctx3d_null_arguments(lib):
+    assert lib.lns_ctx3d_create(None, None) == 1
+    assert lib.lns_upload_metrics3d(None, None) == 1
+    assert lib.lns_upload_mean3d(None, None, None) == 1
+    assert lib.lns_step3d(None, None, 1, 1, None) == 1
+    assert lib.lns_step3d_dev(None, None, 1, 1, None, None) == 1
+    assert lib.lns_rhs3d_dev(None, None, None, None, None, None) == 1
+    assert lib.lns_lhs3d_dev(None, 1, None, None) == 1
+    assert lib.lns_get_field3d(None, 0, None) == 1
+    assert lib.lns_ctx3d_destroy(None) == 0
+    assert lib.lns_ctx3d_bytes(None) == 0
+    assert lib.lns_ctx3d_profile(None, 1) == 1
+    assert lib.lns_ctx3d_profile_read(None, None, None) == 1

@@ -1,0 +1,198 @@
+"""GPU parity of the linearised 3D implicit step (lns_ctx3d_*, through the C
+ABI) against the CPU oracle (oracle/adi3d_oracle.c) on the shear-layer case.
+
+Tolerances (FP64 path; the GPU contracts a*b+c into fused multiply-adds, the
+oracle does not, so results agree to rounding, not bitwise):
+  operators, time step, LHS        1e-12 of the field's largest entry
+  RHS and residual                 1e-11 of the largest entry (the fourth-order
+                                   stencils cancel ~1e2 of the operand scale)
+  full steps                       1e-12 of max|v| per step, as the reference's
+                                   per-step comparison asks
+"""
+import numpy as np
+import pytest
+
+from adi3dcase import Oracle3D
+
+pytestmark = pytest.mark.gpu
+
+OPS_TOL, RHS_TOL, STEP_TOL = 1e-12, 1e-11, 1e-12
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def small():
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=40, ny=33, seed=3)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1)
+    return case, orc
+
+
+def make_drv(case, precision=0, cflmax=20.0, loctime=1):
+    from lns3d_gb300 import ImpDrv3D
+
+    return ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=cflmax, loctime=loctime,
+                    precision=precision)
+
+
+def test_operators_match_oracle(cuda, small):
+    case, orc = small
+    drv = make_drv(case)
+    for name in ("Ah", "Bh", "Dh", "Dhi", "Vh11", "Vh12", "Vh22", "ABhi"):
+        assert rel(drv.field(name), orc.ops[name]) < OPS_TOL, name
+    assert rel(drv.field("dtl"), orc.dtl) < OPS_TOL
+    assert abs(drv.cfl - orc.cfl) <= OPS_TOL * abs(orc.cfl)
+
+
+@pytest.mark.parametrize("loctime", [0, 1])
+def test_time_step_modes(cuda, small, loctime):
+    case, _ = small
+    orc = Oracle3D(case, cflmax=5.0, loctime=loctime)
+    drv = make_drv(case, cflmax=5.0, loctime=loctime)
+    assert rel(drv.field("dtl"), orc.dtl) < OPS_TOL
+
+
+@pytest.mark.parametrize("direction", [1, 2])
+def test_lhs_matches_oracle(cuda, small, direction):
+    import torch
+
+    case, orc = small
+    drv = make_drv(case)
+    nx, ny = orc.nx, orc.ny
+    mat = torch.zeros(125 * nx * ny, dtype=torch.complex128, device="cuda")
+    drv.lhs(direction, mat)
+    torch.cuda.synchronize()
+    got = mat.cpu().numpy().reshape((5, 5, 5, nx, ny), order="F")
+    ref = orc.lhs(direction)
+    assert rel(got, ref) < OPS_TOL
+    # the boundary-condition rows are exact
+    assert np.array_equal(got[:, :, :, :, ny - 1], ref[:, :, :, :, ny - 1])
+
+
+def test_rhs_matches_oracle(cuda, small):
+    import ctypes
+
+    import torch
+    from adi3dcase import _lib, ptr
+
+    case, orc = small
+    drv = make_drv(case)
+    rng = np.random.default_rng(11)
+    shape = (5, orc.nx, orc.ny)
+    v = np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    vold = np.asfortranarray(v + 1e-3 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    L = _lib()
+    r = orc.lrhs(v)
+    L.a3_rbe(ctypes.byref(orc.g), ptr(r), ptr(v), ptr(vold), ptr(orc.dtl))
+    L.a3_rhsbc(ctypes.byref(orc.g), ptr(r), ptr(v))
+    res = L.a3_resstat(ctypes.byref(orc.g), ptr(r), ptr(orc.dtl))
+    dev = lambda a: torch.from_numpy(a.ravel(order="F")).cuda()
+    dv, dvo = dev(v), dev(vold)
+    dr = torch.zeros_like(dv)
+    tot = torch.zeros(1, dtype=torch.float64, device="cuda")
+    drv.rhs(dv, dvo, dr, tot)
+    torch.cuda.synchronize()
+    got = dr.cpu().numpy().reshape(shape, order="F")
+    assert rel(got, r) < RHS_TOL
+    assert abs(tot.item() - res) <= RHS_TOL * res
+
+
+@pytest.mark.parametrize("niter", [1, 2])
+def test_steps_match_oracle(cuda, niter):
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=40, ny=33, seed=5)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1)
+    drv = make_drv(case)
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    for s in range(4):
+        res_ref = orc.step(v_ref, niter=niter)
+        res_gpu = drv.step(v_gpu, nsteps=1, niter=niter)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+
+
+def test_device_steps_match_host_steps(cuda, small):
+    import torch
+
+    case, _ = small
+    a, b = make_drv(case), make_drv(case)
+    v_host = case["v"].copy(order="F")
+    res_host = a.step(v_host, nsteps=6, niter=1)
+    dv = torch.from_numpy(case["v"].ravel(order="F")).cuda()
+    tot = torch.zeros(6, dtype=torch.float64, device="cuda")
+    b.step(dv, nsteps=6, niter=1, totres=tot)
+    torch.cuda.synchronize()
+    got = dv.cpu().numpy().reshape(case["v"].shape, order="F")
+    assert np.array_equal(got, v_host)
+    assert np.array_equal(tot.cpu().numpy(), res_host)
+
+
+def test_many_steps_track_oracle_and_converge(cuda):
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=48, ny=40, seed=0)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1)
+    drv = make_drv(case)
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    res_ref = np.array([orc.step(v_ref) for _ in range(300)])
+    res_gpu = drv.step(v_gpu, nsteps=300)
+    assert rel(v_gpu, v_ref) < 1e-10
+    assert np.abs(res_gpu - res_ref).max() <= 1e-9 * res_ref.max()
+    assert res_gpu[-1] < 1e-2 * res_gpu[0]
+
+
+def test_mixed_precision_converges_to_fp64_state(cuda):
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=48, ny=40, seed=0)
+    d64, d32 = make_drv(case, precision=0), make_drv(case, precision=1)
+    assert d32.device_bytes < d64.device_bytes
+    v64 = case["v"].copy(order="F")
+    v32 = case["v"].copy(order="F")
+    r64 = d64.step(v64, nsteps=300)
+    r32 = d32.step(v32, nsteps=300)
+    # every step solves for the correction only: FP32 sweeps perturb the path
+    # by FP32 rounding of the correction, and the FP64 residual drives both to
+    # the same state
+    assert np.abs(r32 - r64).max() <= 1e-4 * r64.max()
+    assert rel(v32, v64) < 1e-5
+    assert r32[-1] < 1e-2 * r32[0]
+
+
+def test_state_mutation_refactors_after_new_mean(cuda, small):
+    case, orc = small
+    drv = make_drv(case)
+    v = case["v"].copy(order="F")
+    drv.step(v, nsteps=2)
+    # a new mean flow rebuilds the operators and the factors
+    vm2 = case["vm"].copy()
+    vm2[4] *= 1.01
+    drv.set_mean(vm2)
+    case2 = dict(case, vm=vm2)
+    orc2 = Oracle3D(case2, cflmax=20.0, loctime=1)
+    v_ref = v.copy(order="F")
+    orc2.step(v_ref)
+    drv.step(v)
+    assert rel(v, v_ref) < STEP_TOL
+
+
+def test_rejects_bad_arguments(cuda, small):
+    import torch
+    from lns3d_gb300 import LnsError
+
+    case, _ = small
+    drv = make_drv(case)
+    with pytest.raises(LnsError):
+        drv.step(case["v"].copy(order="F"), nsteps=1, niter=0)
+    with pytest.raises(ValueError):
+        drv.step(np.zeros((5, 3, 3), np.complex128, order="F"))
+    with pytest.raises(LnsError):
+        drv.lhs(3, torch.zeros(125 * 40 * 33, dtype=torch.complex128, device="cuda"))
