@@ -1,27 +1,36 @@
 #!/usr/bin/env python3
-"""Benchmark of the batched block-pentadiagonal line solve.
+"""Benchmark of the implicit ADI step of the linearised single-Fourier-mode
+solver (src/impdrv3d.f90) on one GB300.
 
-Workload (the isolated batched solve): 512 independent complex lines of 256
-block rows with 5x5 blocks, boundary-closure rows (cpenta2bc semantics),
-factor + solve (code 2) per step.  Block entries have real and imaginary
-parts uniform in [-1, 1] with +10*I on the diagonal blocks; right-hand sides
-are standard normal.  Inputs are synthetic and seeded; every timed step
-solves its own pristine batch resident in HBM (262 MB of matrix per batch,
-larger than L2, so no flush is needed).
+Headline workload: a parallel compressible shear layer on a 512 x 256 grid
+(x periodic, y stretched; u = (1 + tanh y)/2, T by Crocco-Busemann, Ma 0.8,
+Re 500), spanwise wavenumber beta 0.2, frequency omega 0.05, local time
+stepping at CFL 20, seeded 1e-6 disturbance in a Gaussian window.  A step is
+one implicit step with one corrector (impl 1, niter 1): RHS, xi sweep, eta
+sweep, update, on factors formed at the first step.  Inputs are synthetic
+(lns3d_gb300.cases.shear_layer); the working set of a step (operators 131 MB,
+two factored LHS of 262 MB each) is larger than L2.
 
 One JSON line on stdout (rank 0):
-  value        grid points solved per second (rows x lines / step time), all GPUs
-  e2e          the same through the host-pointer C-ABI call with pinned host
-               buffers, host<->device copies inside the timed region
-  roofline     HBM roofline of the solver kernel (algorithmic bytes / kernel
-               time vs the measured copy bandwidth) and, beside it, the FP64
-               roofline that binds it
-  cpu_baseline the reference's own solver sources (translated to C, OpenMP
-               over all host cores) on the same workload
+  value        FP64 grid-point-steps per second of the drop-in step, all GPUs
+  mixed        the same with FP32 LHS factors and sweeps (FP64 RHS, residual
+               and update)
+  converge     steps and time to a 1e-10 residual from the initial
+               disturbance, FP64 and mixed, and the final state difference
+  e2e          the FP64 step through the host-pointer C-ABI call
+               (lns_step3d): disturbance copied from pinned host memory and
+               back every step, inside the timed region
+  roofline     the dominant kernel (a sweep) against the measured HBM copy
+               bandwidth, and beside it against the measured FP64 rate
+  cpu_baseline the oracle restatement of the step (OpenMP over all host
+               cores) on a bounded sample of the same workload
+  isolated_solve  the batched complex block-penta solve on its own (512
+               lines x 256 rows, cpenta2bc factor + solve)
 
---impl reference runs only the reference CPU path and prints its line.
-Multi-GPU (torchrun): independent replicas, one per GPU; no collective on the
-data path.
+--impl reference times only the CPU path (the reference's Fortran cannot be
+built without a Fortran compiler; its restatement stands in) and prints its
+line.  Multi-GPU (torchrun): independent replicas, one per GPU; no
+collective on the data path.
 """
 import argparse
 import ctypes
@@ -35,6 +44,25 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# ---- headline: the 3D step
+NX, NY = 512, 256
+PTS3 = NX * NY
+CFL3 = 20.0
+# algorithmic HBM bytes per grid point of each phase (FP64):
+#   RHS     v, vold 160 B + operators 984 B (Ah Bh Dh Dhi 100 doubles, V 18,
+#           the 4 used 3D terms, dtl) + r write 80 B            = 1224 B
+#   xi sweep (periodic) factors 2000 B + fill per, per2 1600 B + r read and
+#           write 160 B                                           = 3760 B
+#   eta sweep factors 2000 B + r read and write 160 B            = 2160 B
+#   update  v read and write 160 B + r read 80 B                 =  240 B
+PHASE_BYTES = {"rhs": 1224, "xsweep": 3760, "ysweep": 2160, "update": 240}
+# complex multiply-adds per point of a sweep (8 flops each): lower blocks 50,
+# in-block lower 10, upper blocks 50, in-block upper 10 and 5 divisions
+# (counted 5), periodic fill columns and rows +100
+PHASE_FLOPS = {"xsweep": 8 * 225, "ysweep": 8 * 125}
+KERNELS_PER_STEP = 8   # bc (predictor), grad1, rhs, resid, xi sweep, eta sweep, add, bc
+
+# ---- secondary: the isolated batched solve
 N_ROWS, N_LINES = 256, 512
 PTS = N_ROWS * N_LINES
 MAT_EL = 125 * PTS           # complex elements
@@ -224,46 +252,168 @@ def run_e2e(torch, dev, L, rank, world, K):
     return PTS / statistics.mean(t)
 
 
+def step3d_cpu(steps, warm=1):
+    """The oracle restatement of the step built with OpenMP over grid rows and
+    lines (oracle/liborc_omp.so), all host cores, on the headline workload;
+    returns seconds per step over `steps` steps after `warm` steps (the first
+    of which forms and factors the LHS)."""
+    import numpy as np
+
+    import oracle
+    from lns3d_gb300.cases import shear_layer
+
+    from oracle.adi3d import Oracle3D
+
+    lib = oracle.orc_omp()
+    case = shear_layer(nx=NX, ny=NY, seed=0)
+    orc = Oracle3D(case, cflmax=CFL3, loctime=1, lib=lib)
+    v = np.asfortranarray(case["v"].copy())
+    for _ in range(warm):
+        orc.step(v)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.step(v)
+    return (time.perf_counter() - t0) / steps
+
+
+def cpu_baseline3d(steps):
+    t = step3d_cpu(steps)
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": PTS3 / t, "unit": "grid-pt-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d implicit steps (niter 1) of the 512x256 shear-layer case after the factoring step, "
+                      "%.1f ms/step; restatement of impdrv3d + cpenta2p/cpenta1bc, -O3 -fopenmp" % (steps, t * 1e3)}
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    reps = max(1, args.steps)
-    for _ in range(args.warmup):
-        time_reference_cpu(1)
+    steps = max(1, args.steps)
     t0 = time.perf_counter()
-    cb = time_reference_cpu(reps)
+    t = step3d_cpu(steps, warm=max(1, min(args.warmup, 2)))
     wall = time.perf_counter() - t0
-    line = {"impl": "reference", "metric": "ADI grid-pt-steps/s (isolated batched complex block-penta solve)",
-            "value": cb["value"], "unit": "grid-pt/s", "n_gpus": args.gpus, "steps": reps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * PTS / cb["value"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": "cpenta2bc-512lines-256rows-complex-factor+solve", "lines": N_LINES,
-                       "rows": N_ROWS, "nblk": 5, "code": 2},
-            "cpu_baseline": {"value": cb["value"], "unit": "grid-pt/s", "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"]},
-            "e2e": {"value": cb["value"], "unit": "grid-pt/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    value = PTS3 / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "grid-pt-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": config3(world),
+            "cpu_baseline": {"value": value, "unit": "grid-pt-steps/s", "cores": cores, "kind": "port",
+                             "sample": "%d implicit steps of the 512x256 case on %d host threads (the reference's "
+                                       "Fortran has no compiler here; its C restatement, -O3 -fopenmp)"
+                                       % (steps, cores)},
+            "e2e": {"value": value, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
     print(json.dumps(line))
     return 0
 
 
+METRIC = "ADI grid-pt-steps/s (linearised 3D implicit step, FP64 drop-in; mixed beside)"
+
+
+def config3(world):
+    return {"workload": "impdrv3d-shear-layer-512x256-beta0.2-omega0.05-niter1", "nx": NX, "ny": NY,
+            "beta": 0.2, "omega": 0.05, "cfl": CFL3, "loctime": 1, "niter": 1,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "working set larger than L2 (operators 131 MB + two factored LHS 262 MB each per step)"}
+
+
+def time_steps(torch, drv, v, K, stream, totres=None):
+    """K steps of one step each, CUDA events around every step; returns
+    (total ms, sorted per-step ms)."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(K):
+        ev[s][0].record(stream)
+        drv.step(v, nsteps=1, niter=1, totres=None if totres is None else totres[s:])
+        ev[s][1].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), sorted(a.elapsed_time(b) for a, b in ev)
+
+
+def converge(torch, drv, v0, tol=1e-10, max_steps=2000, chunk=100):
+    """Steps from v0 until the residual is <= tol (or max_steps); returns
+    (steps, ms, residual history, final v)."""
+    v = v0.clone()
+    res = torch.zeros(max_steps, dtype=torch.float64, device=v.device)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    done = 0
+    hit = None
+    while done < max_steps and hit is None:
+        n = min(chunk, max_steps - done)
+        drv.step(v, nsteps=n, niter=1, totres=res[done:])
+        done += n
+        r = res[:done].cpu()
+        below = (r <= tol).nonzero()
+        if below.numel():
+            hit = int(below[0]) + 1
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return (hit if hit is not None else -1), ms, done, res[:done].cpu().numpy(), v
+
+
+def percentile(xs, q):
+    return xs[min(len(xs) - 1, int(round(q * (len(xs) - 1))))]
+
+
+def run_isolated(torch, dev, L, sp, stream, rank, world, W, K):
+    """The isolated batched solve (cpenta2bc code 2, FP64) and its mixed
+    form; each step solves its own pristine batch resident in HBM."""
+    batches = [make_batch(torch, dev, 1000 * rank + s) for s in range(W + K)]
+    torch.cuda.synchronize()
+
+    def solve(mat, rhs):
+        rc = L.lns_cpenta2bc_dev(N_ROWS, N_LINES, 5, ctypes.c_void_p(mat.data_ptr()),
+                                 ctypes.c_void_p(rhs.data_ptr()), 2, sp)
+        if rc:
+            raise RuntimeError(L.lns_last_error().decode())
+
+    for s in range(W):
+        solve(*batches[s])
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    for s in range(K):
+        ev[s][0].record(stream)
+        solve(*batches[W + s])
+        ev[s][1].record(stream)
+    torch.cuda.synchronize()
+    per_step = sorted(a.elapsed_time(b) for a, b in ev)
+    assert torch.isfinite(torch.view_as_real(batches[W][1])).all()
+    fp64_x = batches[W][1].clone()
+    del batches
+    mixed = run_mixed(torch, dev, L, sp, stream, rank, world, W, K, fp64_x)
+    ms = statistics.mean(per_step)
+    return {"workload": "cpenta2bc-512lines-256rows-complex-factor+solve", "value": PTS / (ms / 1e3),
+            "unit": "grid-pt/s", "ms_per_step": ms,
+            "latency_ms": {"p50": percentile(per_step, 0.5), "p99": percentile(per_step, 0.99)},
+            "bytes_per_pt": BYTES_PER_PT, "flops_per_pt": FLOPS_PER_PT,
+            "hbm_gbs": BYTES_PER_PT * PTS / (ms / 1e3) / 1e9,
+            "fp64_tflops": FLOPS_PER_PT * PTS / (ms / 1e3) / 1e12, "mixed": mixed}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer end-to-end leg")
-    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--no-converge", action="store_true", help="skip the runs to a 1e-10 residual")
+    ap.add_argument("--no-isolated", action="store_true", help="skip the isolated batched-solve leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
 
+    import numpy as np
     import torch
 
     import lns3d_gb300 as g
+    from lns3d_gb300.cases import shear_layer
 
     rank, world, local = env_rank()
     dev = torch.device("cuda", local)
@@ -277,92 +427,132 @@ def main():
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
 
-    # pristine batches: one per warm-up and timed step
-    batches = [make_batch(torch, dev, 1000 * rank + s) for s in range(W + K)]
-    torch.cuda.synchronize()
+    case = shear_layer(nx=NX, ny=NY, seed=rank)
+    v0 = torch.from_numpy(case["v"].ravel(order="F")).to(dev)
 
-    def solve(mat, rhs):
-        rc = L.lns_cpenta2bc_dev(N_ROWS, N_LINES, 5, ctypes.c_void_p(mat.data_ptr()),
-                                 ctypes.c_void_p(rhs.data_ptr()), 2, sp)
-        if rc:
-            raise RuntimeError(L.lns_last_error().decode())
+    def make(precision):
+        t0 = time.perf_counter()
+        d = g.ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=CFL3, loctime=1, precision=precision)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        v = v0.clone()
+        d.step(v, nsteps=1)   # forms and factors both LHS
+        torch.cuda.synchronize()
+        return d, v, {"operators_ms": (t1 - t0) * 1e3, "first_step_ms": (time.perf_counter() - t1) * 1e3}
 
-    for s in range(W):
-        solve(*batches[s])
+    # ---- FP64 drop-in step
+    d64, v64, setup64 = make(g.adi3d.FP64)
+    for _ in range(W):
+        d64.step(v64, nsteps=1)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clk = Clocks(local)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e_all0 = torch.cuda.Event(enable_timing=True)
-    e_all1 = torch.cuda.Event(enable_timing=True)
-    e_all0.record(stream)
-    for s in range(K):
-        ev[s][0].record(stream)
-        solve(*batches[W + s])
-        ev[s][1].record(stream)
-    e_all1.record(stream)
-    torch.cuda.synchronize()
+    total_ms, per_step = time_steps(torch, d64, v64, K, stream)
     clocks = clk.stop()
-    total_ms = e_all0.elapsed_time(e_all1)
-    per_step = sorted(a.elapsed_time(b) for a, b in ev)
     if world > 1:
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
         torch.distributed.barrier()
-    ms_per_step = total_ms / K
-    value = world * PTS * K / (total_ms / 1e3)
-    kern_ms = statistics.mean(per_step)
+    value = world * PTS3 * K / (total_ms / 1e3)
 
-    assert torch.isfinite(torch.view_as_real(batches[W][1])).all()
-    fp64_x = batches[W][1].clone()
-    del batches
+    # per-phase kernel times (events on the launching stream, separate pass)
+    d64.profile(True)
+    time_steps(torch, d64, v64, K, stream)
+    phases64, ncorr = d64.profile_read()
+    d64.profile(False)
+    ph64 = {k: v / ncorr for k, v in phases64.items()}
 
-    # mixed precision: FP32 LU + two FP64 refinement steps, same workload;
-    # the matrix is read only, so the batches are regenerated pristine
-    mixed = None
-    if not args.no_mixed:
-        mixed = run_mixed(torch, dev, L, sp, stream, rank, world, W, K, fp64_x)
+    # ---- mixed step
+    d32, v32, setup32 = make(g.adi3d.MIXED)
+    for _ in range(W):
+        d32.step(v32, nsteps=1)
+    torch.cuda.synchronize()
+    total32, per32 = time_steps(torch, d32, v32, K, stream)
+    d32.profile(True)
+    time_steps(torch, d32, v32, K, stream)
+    phases32, n32 = d32.profile_read()
+    d32.profile(False)
+    ph32 = {k: v / n32 for k, v in phases32.items()}
+    if world > 1:
+        t = torch.tensor([total32], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total32 = float(t.item())
+    mixed = {"value": world * PTS3 * K / (total32 / 1e3), "ms_per_step": total32 / K,
+             "latency_ms": {"p50": percentile(per32, 0.5), "p99": percentile(per32, 0.99)},
+             "phase_ms": ph32, "setup": setup32, "device_bytes": int(d32.device_bytes)}
 
-    # end to end: host-pointer C-ABI call from pinned host memory
-    e2e_value = None if args.no_e2e else run_e2e(torch, dev, L, rank, world, K)
+    # ---- to a 1e-10 residual from the initial disturbance
+    conv = None
+    if not args.no_converge:
+        a = converge(torch, g.ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=CFL3, loctime=1,
+                                       precision=g.adi3d.FP64), v0)
+        b = converge(torch, g.ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=CFL3, loctime=1,
+                                       precision=g.adi3d.MIXED), v0)
+        n = min(len(a[3]), len(b[3]))
+        diff = float((a[4] - b[4]).abs().max() / a[4].abs().max())
+        conv = {"tol": 1e-10, "max_steps": 2000,
+                "fp64": {"steps": a[0], "ms": a[1], "steps_run": a[2], "final_res": float(a[3][-1]),
+                         "pt_steps_per_s": PTS3 * a[2] / (a[1] / 1e3)},
+                "mixed": {"steps": b[0], "ms": b[1], "steps_run": b[2], "final_res": float(b[3][-1]),
+                          "pt_steps_per_s": PTS3 * b[2] / (b[1] / 1e3)},
+                "mixed_vs_fp64_state_rel_diff": diff,
+                "mixed_vs_fp64_res_rel_diff_max": float(np.max(np.abs(a[3][:n] - b[3][:n]) / a[3][:n])),
+                "time_to_tol_speedup": (a[1] / b[1]) if a[0] > 0 and b[0] > 0 else None}
+
+    # ---- end to end through the host-pointer C ABI
+    e2e = None
+    if not args.no_e2e:
+        host_v = torch.from_numpy(case["v"].ravel(order="F")).pin_memory()
+        hv = host_v.numpy()
+        d64.step(hv, nsteps=1)
+        ke = max(3, min(K, 10))
+        t = []
+        for _ in range(ke):
+            t0 = time.perf_counter()
+            d64.step(hv, nsteps=1)
+            t.append(time.perf_counter() - t0)
+        tm = statistics.mean(t)
+        if world > 1:
+            tt = torch.tensor([tm], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            tm = float(tt.item())
+        e2e = {"value": world * PTS3 / tm, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": 5 * PTS3 * 16,
+               "d2h_bytes_per_step": 5 * PTS3 * 16 + 8, "ms_per_step": tm * 1e3}
+
+    # ---- the isolated batched solve
+    iso = None
+    if not args.no_isolated:
+        del d32
+        iso = run_isolated(torch, dev, L, sp, stream, rank, world, 3, max(3, min(K, 10)))
 
     hbm_peak, peak_kind = peaks()
-    fp64_peak = L.lns_probe_fp64_tflops()  # measured live on this GPU
-    achieved = BYTES_PER_PT * PTS / (kern_ms / 1e3) / 1e9
-    fp64_achieved = FLOPS_PER_PT * PTS / (kern_ms / 1e3) / 1e12
+    fp64_peak = L.lns_probe_fp64_tflops()
+    dom = max(("xsweep", "ysweep"), key=lambda k: ph64[k])
+    achieved = PHASE_BYTES[dom] * PTS3 / (ph64[dom] / 1e3) / 1e9
+    fp64_achieved = PHASE_FLOPS[dom] * PTS3 / (ph64[dom] / 1e3) / 1e12
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = time_reference_cpu(3)
+        cpu = cpu_baseline3d(8)
     if rank == 0:
         line = {
-            "metric": "ADI grid-pt-steps/s (isolated batched complex block-penta solve)",
-            "value": value, "unit": "grid-pt/s", "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": "cpenta2bc-512lines-256rows-complex-factor+solve", "lines": N_LINES,
-                       "rows": N_ROWS, "nblk": 5, "code": 2, "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (262 MB matrix per step, fresh batch each step)"},
-            "latency_ms": {"p50": per_step[len(per_step) // 2],
-                           "p99": per_step[min(len(per_step) - 1, int(round(0.99 * (len(per_step) - 1))))]},
-            "e2e": None if e2e_value is None else {
-                "value": e2e_value, "unit": "grid-pt/s",
-                "h2d_bytes_per_step": (MAT_EL + RHS_EL) * CPLX,
-                "d2h_bytes_per_step": (MAT_EL + RHS_EL) * CPLX + 4},
+            "metric": METRIC, "value": value, "unit": "grid-pt-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic", "config": config3(world),
+            "latency_ms": {"p50": percentile(per_step, 0.5), "p99": percentile(per_step, 0.99)},
+            "phase_ms": ph64, "setup": setup64, "device_bytes": int(d64.device_bytes),
+            "mixed": mixed, "converge": conv, "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None,
-                         "peak_source": peak_kind, "kernel": "penta_bc_kernel<cd>",
-                         "bytes_per_pt": BYTES_PER_PT},
-            "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak,
-                              "unit": "TFLOP/s", "frac": fp64_achieved / fp64_peak,
-                              "flops_per_pt": FLOPS_PER_PT,
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "penta_solve_kernel<cd,%d> (%s)" % (dom == "xsweep", dom),
+                         "bytes_per_pt": PHASE_BYTES[dom]},
+            "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                              "frac": fp64_achieved / fp64_peak, "flops_per_pt": PHASE_FLOPS[dom],
                               "peak_source": "measured live: DFMA stream on every SM (lns_probe_fp64_tflops)"},
             "cpu_baseline": cpu,
-            "mixed": mixed,
-            "gpu_launches": K,
+            "isolated_solve": iso,
+            "gpu_launches": KERNELS_PER_STEP * K,
             "clocks": clocks,
         }
         print(json.dumps(line))

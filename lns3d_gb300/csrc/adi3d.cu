@@ -9,7 +9,7 @@
 //   c1v = d v/d xi                                     grad1_kernel
 //   r = vold - v - dtl L(v), boundary rows, residual    rhs_kernel
 //   xi sweep, eta sweep (stored factors)                penta_solve_kernel
-//   v += r, boundary values                             update_kernel
+//   v += r, boundary values                             add_kernel, bc_kernel
 // In the mixed-precision mode the factors and the sweeps are FP32 and the
 // RHS, residual and update stay FP64.
 #include <cuda_runtime.h>
@@ -553,43 +553,53 @@ __global__ void resid_kernel(int nparts, const double* part, long long npts, dou
 }
 
 // ----------------------------------------------------------------- update
-// v += r (add) and the boundary values of src/itrbc3d.f90:35-205; one
-// thread per column i.  The periodic copy of column 1 to column nx is a
-// separate launch (periodic_copy_kernel).
+// v += r over every entry (src/impdrv3d.f90:339-347)
 template <typename RT>
-__global__ void update_kernel(Grid g, cd* __restrict__ v, const RT* __restrict__ r, int add) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (i > g.nx) return;
-  if (add)
-    for (int j = 1; j <= g.ny; ++j)
-      for (int m = 0; m < 5; ++m) {
-        cd& x = v[m + 5 * pix(g, i, j)];
-        const cd d = to_hi(r[m + 5 * pix(g, i, j)]);
-        x = cd{x.x + d.x, x.y + d.y};
-      }
-  if (!g.yper) {
-    if (g.navier) {
-      auto W = [&](int k, int jj) -> cd& { return v[k + 5 * pix(g, i, jj)]; };
-      for (int m = 1; m <= 3; ++m) W(m, 1) = cd{0.0, 0.0};
-      if (g.wall == 1)
-        W(0, 1) = cd{-(gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x) / gc1,
-                     -(gc2 * W(0, 2).y + gc3 * W(0, 3).y + gc4 * W(0, 4).y + gc5 * W(0, 5).y) / gc1};
-      if (g.wall == 2) W(0, 1) = cd{two * W(0, 2).x - W(0, 3).x, two * W(0, 2).y - W(0, 3).y};
-      if (g.wallt == 0) W(4, 1) = cd{0.0, 0.0};
-      if (g.wallt == 1)
-        W(4, 1) = cd{-(gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x) / gc1,
-                     -(gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y) / gc1};
-    }
-    if (g.top == 0)
-      for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, i, g.ny)] = cd{0.0, 0.0};
-  } else {
-    for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, i, g.ny)] = v[m + 5 * pix(g, i, 1)];
-  }
+__global__ void add_kernel(long long n, cd* __restrict__ v, const RT* __restrict__ r) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const cd d = to_hi(r[e]);
+  const cd x = v[e];
+  v[e] = cd{x.x + d.x, x.y + d.y};
 }
-__global__ void periodic_copy_kernel(Grid g, cd* v) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (j > g.ny) return;
-  for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, g.nx, j)] = v[m + 5 * pix(g, 1, j)];
+
+// The boundary values of src/itrbc3d.f90:35-205: threads 0..ncol-1 own a
+// column i (wall row j = 1 from rows 2..5, top row j = ny); with a periodic
+// x direction the remaining threads copy the interior rows of column 1 to
+// column nx, and the thread of column 1 copies its boundary rows.
+__global__ void bc_kernel(Grid g, cd* __restrict__ v) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncol = g.xper ? g.nx - 1 : g.nx;
+  if (t < ncol) {
+    const int i = t + 1;
+    auto W = [&](int k, int jj) -> cd& { return v[k + 5 * pix(g, i, jj)]; };
+    if (!g.yper) {
+      if (g.navier) {
+        for (int m = 1; m <= 3; ++m) W(m, 1) = cd{0.0, 0.0};
+        if (g.wall == 1)
+          W(0, 1) = cd{-(gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x) / gc1,
+                       -(gc2 * W(0, 2).y + gc3 * W(0, 3).y + gc4 * W(0, 4).y + gc5 * W(0, 5).y) / gc1};
+        if (g.wall == 2) W(0, 1) = cd{two * W(0, 2).x - W(0, 3).x, two * W(0, 2).y - W(0, 3).y};
+        if (g.wallt == 0) W(4, 1) = cd{0.0, 0.0};
+        if (g.wallt == 1)
+          W(4, 1) = cd{-(gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x) / gc1,
+                       -(gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y) / gc1};
+      }
+      if (g.top == 0)
+        for (int m = 0; m < 5; ++m) W(m, g.ny) = cd{0.0, 0.0};
+    } else {
+      for (int m = 0; m < 5; ++m) W(m, g.ny) = W(m, 1);
+    }
+    if (g.xper && i == 1)
+      for (int m = 0; m < 5; ++m) {
+        v[m + 5 * pix(g, g.nx, 1)] = W(m, 1);
+        v[m + 5 * pix(g, g.nx, g.ny)] = W(m, g.ny);
+      }
+  } else if (g.xper) {
+    const int j = t - ncol + 2;
+    if (j <= g.ny - 1)
+      for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, g.nx, j)] = v[m + 5 * pix(g, 1, j)];
+  }
 }
 
 }  // namespace a3
@@ -771,8 +781,10 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
 template <typename RT>
 int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
   const Grid& g = c->g;
-  lns::a3::update_kernel<RT><<<(g.nx + 127) / 128, 128, 0, st>>>(g, v, r, add);
-  if (g.xper) lns::a3::periodic_copy_kernel<<<(g.ny + 127) / 128, 128, 0, st>>>(g, v);
+  const long long n = 5 * c->np;
+  if (add) lns::a3::add_kernel<RT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, r);
+  const int nt = g.nx + g.ny;
+  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "update kernels launch");
 }

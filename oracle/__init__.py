@@ -2,7 +2,8 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
 this package.  It loads ``liborc_penta.so`` (the restatement of the
-reference line solvers) and, where built, ``_ref/libref_penta.so`` (the
+reference line solvers and of the linear 3D step), ``liborc_omp.so`` (the
+same sources built for speed with OpenMP) and, where built, ``_ref/libref_penta.so`` (the
 reference's own solver sources translated by f77sub2c.py).
 """
 import ctypes
@@ -10,30 +11,40 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORC_PATH = os.path.join(HERE, "liborc_penta.so")
+ORC_OMP_PATH = os.path.join(HERE, "liborc_omp.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref_penta.so")
 REF_FAST_PATH = os.path.join(HERE, "_ref", "libref_penta_fast.so")
 
 COMPAT_PERIODIC_SLOT = 1
 COMPAT_CBC_RHS = 2
 
-_orc = None
+_orc = {}
 _ref = {}
 
 
-def orc():
-    global _orc
-    if _orc is None:
-        if not os.path.exists(ORC_PATH):
+def _load(path):
+    if path not in _orc:
+        if not os.path.exists(path):
             raise ImportError("oracle not built: make -C oracle")
-        L = ctypes.CDLL(ORC_PATH)
+        L = ctypes.CDLL(path)
         i, p = ctypes.c_int, ctypes.c_void_p
         L.orc_penta_bc.argtypes = [i, i, i, p, p]
         L.orc_penta_p.argtypes = [i, i, i, p, p, p, i]
         L.orc_cpenta_bc.argtypes = [i, i, i, p, p, i, i]
         L.orc_cpenta_p.argtypes = [i, i, i, p, p, p, p, i, i]
         L.orc_oob_count.restype = ctypes.c_long
-        _orc = L
-    return _orc
+        _orc[path] = L
+    return _orc[path]
+
+
+def orc():
+    """The parity build of the restatement (serial, no contraction)."""
+    return _load(ORC_PATH)
+
+
+def orc_omp():
+    """The same restatement built -O3 -fopenmp: the timed CPU baseline."""
+    return _load(ORC_OMP_PATH)
 
 
 def ref(fast=False):

@@ -1,92 +1,2 @@
-"""ctypes harness of the linear ADI step oracle (oracle/adi3d_oracle.c)."""
-import ctypes
-
-import numpy as np
-
-import oracle
-
-D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
-
-
-class A3Grid(ctypes.Structure):
-    _fields_ = [("nx", I), ("ny", I), ("dxi", D), ("deta", D), ("Ma", D), ("Re", D), ("Pr", D), ("gamma", D),
-                ("gamma1", D), ("omega", D), ("kz", D), ("alfa", D), ("cflmax", D), ("dtmax", D),
-                ("loctime", I), ("xper", I), ("yper", I), ("navier", I), ("wall", I), ("wallt", I), ("top", I),
-                ("optx", I), ("opty", I)] + [(k, P) for k in
-                                             ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")]
-
-
-class A3Ops(ctypes.Structure):
-    _fields_ = [(k, P) for k in ("Ah", "Bh", "Dh", "Dhi", "Vh11", "Vh12", "Vh22", "ABhi")]
-
-
-def _lib():
-    L = oracle.orc()
-    if not hasattr(L, "_a3_setup"):
-        L.a3_genmtrx.argtypes = [ctypes.POINTER(A3Grid), P, ctypes.POINTER(A3Ops)]
-        L.a3_set_time_step.argtypes = [ctypes.POINTER(A3Grid), P, P]
-        L.a3_set_time_step.restype = D
-        L.a3_deriv1.argtypes = [ctypes.POINTER(A3Grid), I, P, P, P]
-        L.a3_deriv2.argtypes = [ctypes.POINTER(A3Grid), I, P, P, P, P, P]
-        L.a3_lrhs.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, P]
-        L.a3_rbe.argtypes = [ctypes.POINTER(A3Grid), P, P, P, P]
-        L.a3_rhsbc.argtypes = [ctypes.POINTER(A3Grid), P, P]
-        L.a3_resstat.argtypes = [ctypes.POINTER(A3Grid), P, P]
-        L.a3_resstat.restype = D
-        L.a3_itrbc.argtypes = [ctypes.POINTER(A3Grid), P]
-        L.a3_lhs.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, P]
-        L.a3_step.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, P, P, P, P, P, P, P,
-                              ctypes.POINTER(I)]
-        L.a3_step.restype = D
-        L._a3_setup = True
-    return L
-
-
-def ptr(a):
-    return ctypes.c_void_p(a.ctypes.data)
-
-
-class Oracle3D:
-    """Holds the oracle's grid struct, operators and factor arrays for one case."""
-
-    def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30):
-        self.case = case
-        p = case["params"]
-        self.nx, self.ny = p["nx"], p["ny"]
-        self.keep = {k: np.asfortranarray(v, dtype=np.float64) for k, v in case["metrics"].items()}
-        self.g = A3Grid(cflmax=cflmax, dtmax=dtmax, loctime=loctime,
-                        **{k: p[k] for k in ("nx", "ny", "dxi", "deta", "Ma", "Re", "Pr", "gamma", "gamma1",
-                                             "omega", "kz", "alfa", "xper", "yper", "navier", "wall", "wallt",
-                                             "top", "optx", "opty")},
-                        **{k: ptr(v).value for k, v in self.keep.items()})
-        nx, ny = self.nx, self.ny
-        self.ops = {k: np.zeros((5, 5, nx, ny), order="F") for k in ("Ah", "Bh", "Dh", "Dhi")}
-        self.ops.update({k: np.zeros((6, nx, ny), order="F") for k in ("Vh11", "Vh12", "Vh22", "ABhi")})
-        self.o = A3Ops(**{k: ptr(v).value for k, v in self.ops.items()})
-        self.vm = np.asfortranarray(case["vm"], dtype=np.float64)
-        L = _lib()
-        assert L.a3_genmtrx(ctypes.byref(self.g), ptr(self.vm), ctypes.byref(self.o)) == 0
-        self.dtl = np.zeros((nx, ny), order="F")
-        self.cfl = L.a3_set_time_step(ctypes.byref(self.g), ptr(self.vm), ptr(self.dtl))
-        self.matx = np.zeros((5, 5, 5, nx, ny), np.complex128, order="F")
-        self.maty = np.zeros((5, 5, 5, nx, ny), np.complex128, order="F")
-        self.perx = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
-        self.per2x = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
-        self.r = np.zeros((5, nx, ny), np.complex128, order="F")
-        self.factored = I(0)
-
-    def step(self, v, niter=1):
-        vold = np.zeros_like(v)
-        return _lib().a3_step(ctypes.byref(self.g), ctypes.byref(self.o), ptr(self.dtl), niter, ptr(v), ptr(vold),
-                              ptr(self.r), ptr(self.matx), ptr(self.maty), ptr(self.perx), ptr(self.per2x),
-                              ctypes.byref(self.factored))
-
-    def lrhs(self, v):
-        r = np.zeros_like(v)
-        assert _lib().a3_lrhs(ctypes.byref(self.g), ctypes.byref(self.o), ptr(v), ptr(r)) == 0
-        return r
-
-    def lhs(self, direction):
-        mat = np.zeros((5, 5, 5, self.nx, self.ny), np.complex128, order="F")
-        assert _lib().a3_lhs(ctypes.byref(self.g), ctypes.byref(self.o), ptr(self.dtl), direction, ptr(mat)) == 0
-        return mat
+"""The 3D-step oracle harness, re-exported for the tests."""
+from oracle.adi3d import A3Grid, A3Ops, Oracle3D, _lib, ptr  # noqa: F401

@@ -196,3 +196,39 @@ def test_rejects_bad_arguments(cuda, small):
         drv.step(np.zeros((5, 3, 3), np.complex128, order="F"))
     with pytest.raises(LnsError):
         drv.lhs(3, torch.zeros(125 * 40 * 33, dtype=torch.complex128, device="cuda"))
+
+
+def test_full_size_steps_match_oracle(cuda):
+    # the 512 x 256 benchmark workload itself, three steps
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=512, ny=256, seed=0)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1)
+    drv = make_drv(case)
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    res_ref = [orc.step(v_ref) for _ in range(3)]
+    res_gpu = drv.step(v_gpu, nsteps=3)
+    assert rel(v_gpu, v_ref) < STEP_TOL
+    assert np.abs(np.array(res_gpu) - res_ref).max() <= 1e-10 * max(res_ref)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_full_size_step_is_linear(cuda, precision):
+    # size-independent property at the benchmark size: step(2a - 3b) equals
+    # 2 step(a) - 3 step(b) to rounding (the step is linear in v)
+    import torch
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=512, ny=256, seed=0)
+    drv = make_drv(case, precision=precision)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    n = 5 * 512 * 256
+    a = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
+    b = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
+    c = 2.0 * a - 3.0 * b
+    for v in (a, b, c):
+        drv.step(v, nsteps=2)
+    torch.cuda.synchronize()
+    err = float((c - (2.0 * a - 3.0 * b)).abs().max() / c.abs().max())
+    assert err < (1e-12 if precision == 0 else 1e-5), err
