@@ -28,13 +28,12 @@ int launch_solve(const void* mat, void* rhs, const void* per, const void* per2, 
                  long long row_stride, long long line_stride, cudaStream_t st) {
   if (nsys == 0) return LNS_OK;
   const size_t smem = lns::solve_smem_bytes<T>(PER);
-  static bool attr_set = false;  // per instantiation
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(lns::penta_solve_kernel<T, PER>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return lns_cuda_fail(e, "cudaFuncSetAttribute");
-    attr_set = true;
-  }
+  // Set on every launch: the kernel template is instantiated in more than
+  // one translation unit, each registering its own copy, so a once-only
+  // flag could leave the copy that a launch resolves to without the limit.
+  cudaError_t ea = cudaFuncSetAttribute(lns::penta_solve_kernel<T, PER>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (ea != cudaSuccess) return lns_cuda_fail(ea, "cudaFuncSetAttribute");
   lns::SolveArgs a{mat, rhs, per, per2, n, nsys, row_stride, line_stride, PER ? 1 : 0};
   const int lpw = lns::SolveCfg<T>::kLpw;
   lns::penta_solve_kernel<T, PER><<<(nsys + lpw - 1) / lpw, 32, smem, st>>>(a);
