@@ -147,6 +147,27 @@ int lns_penta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* 
 /* host-pointer form of cpenta2bc_mixed (factor + solve), staged internally */
 int lns_cpenta2bc_mixed(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine);
 
+/* lns_cpenta2bc_mixed_dev with code 2 (factor + solve) that allocates no
+ * device memory and takes no workspace.  No counterpart in the reference.
+ * It is for callers that hold no device buffer to lend as scratch and must
+ * not have the library call cudaMalloc during a solve -- for example a host
+ * whose device memory is handed out by its own pool allocator (a library
+ * allocation would fail or fragment the pool), or one that keeps cudaMalloc,
+ * which may wait for work already queued on the device, out of its
+ * time-critical loop.
+ * Scratch is one fixed array of LNS_STATIC_WORKSPACE_BYTES in the library's
+ * device image.  Problems whose scratch, lns_mixed_workspace_bytes(n, nsys,
+ * 1, 0), exceeds it (about 29 900 rows x lines) are rejected with
+ * LNS_ERR_ARG and a message giving both sizes.  Nothing in the scratch needs
+ * to start at zero.  The first call on a device looks up the array's address
+ * (once per device); make that first call before any stream capture.  All
+ * calls on a device share the one array, so calls that overlap in time -- on
+ * different streams or from different host threads -- race and corrupt each
+ * other's results: keep them ordered (one stream, or events). */
+#define LNS_STATIC_WORKSPACE_BYTES (32u << 20)
+int lns_cpenta2bc_mixed_static_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs,
+                                   int32_t refine, void* stream);
+
 /* ---------------------------------------------------------------------------
  * The linearised single-Fourier-mode implicit ADI step (src/impdrv3d.f90,
  * impl = 1, iLHS = 1) as one device-resident context.

@@ -53,6 +53,7 @@ SIGNATURES = {
     "lns_penta2bc_mixed_dev": [I32, I32, I32, DP, DP, I32, P, P],
     "lns_penta1bc_mixed_dev": [I32, I32, I32, DP, DP, I32, P, P],
     "lns_cpenta2bc_mixed": [I32, I32, I32, DP, DP, I32],
+    "lns_cpenta2bc_mixed_static_dev": [I32, I32, I32, DP, DP, I32, P],
     "lns_ctx3d_create": [P, P],
     "lns_ctx3d_destroy": [P],
     "lns_upload_metrics3d": [P, DP],

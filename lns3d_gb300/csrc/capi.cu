@@ -269,6 +269,39 @@ int check_p(int np, int nsys, int nblk, const char* who) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Fixed scratch of lns_cpenta2bc_mixed_static_dev.  A file-scope device
+// array, so the entry point never allocates: its address is looked up once
+// per device (cudaGetSymbolAddress, with that device current) and cached.
+// Nothing in it needs to start at zero: every call writes each scratch
+// entry it reads.  All calls on a device share it.
+namespace {
+
+constexpr size_t kStaticWorkBytes = size_t(LNS_STATIC_WORKSPACE_BYTES);
+__device__ __align__(256) unsigned char g_static_work[kStaticWorkBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kMaxDevices] = {};
+
+int static_work(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(LNS_ERR_ARG, "static workspace: device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_work);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static workspace)");
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return LNS_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 size_t lns_mixed_workspace_bytes(int32_t rows, int32_t nsys, int32_t is_complex, int32_t periodic) {
@@ -433,6 +466,23 @@ int lns_cpenta1bc_dev(int32_t nsys, int32_t n, int32_t nblk, double* mat, double
   if (rc) return rc;
   if (code < 0 || code > 2) return fail(LNS_ERR_ARG, "cpenta1bc: code must be 0, 1 or 2");
   return launch_bc<lns::cd>(mat, rhs, n, nsys, nsys, 1, code, (cudaStream_t)stream, nullptr);
+}
+
+int lns_cpenta2bc_mixed_static_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs,
+                                   int32_t refine, void* stream) {
+  int rc = check_sizes(n, nsys, nblk, "cpenta2bc_mixed_static");
+  if (!rc) rc = check_mixed(2, refine, "cpenta2bc_mixed_static");
+  if (rc) return rc;
+  const size_t need = mixed_layout(n, nsys, true, false).total;
+  if (need > kStaticWorkBytes)
+    return fail(LNS_ERR_ARG, "cpenta2bc_mixed_static: n = " + std::to_string(n) + ", nsys = " +
+                                 std::to_string(nsys) + " needs " + std::to_string(need) +
+                                 " bytes of scratch, more than the fixed " + std::to_string(kStaticWorkBytes) +
+                                 "-byte static workspace; use lns_cpenta2bc_mixed_dev with a caller workspace");
+  void* w = nullptr;
+  rc = static_work(&w);
+  if (rc) return rc;
+  return mixed_solve<lns::cd, lns::cf>(mat, rhs, n, nsys, 1, n, false, 2, refine, w, (cudaStream_t)stream);
 }
 
 }  // extern "C"
