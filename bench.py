@@ -545,7 +545,7 @@ def main():
             "mixed": mixed, "converge": conv, "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
-                         "kernel": "penta_solve_kernel<cd,%d> (%s)" % (dom == "xsweep", dom),
+                         "kernel": "chain sweep kernels of the %s phase (scale, recurrences%s)" % (dom, ", tail, fill" if dom == "xsweep" else ""),
                          "bytes_per_pt": PHASE_BYTES[dom]},
             "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                               "frac": fp64_achieved / fp64_peak, "flops_per_pt": PHASE_FLOPS[dom],

@@ -211,6 +211,12 @@ typedef struct {
   int32_t loctime;           /* 0 global time step, 1 local time step */
   int32_t xper, yper, navier, wall, wallt, top, optx, opty;
   int32_t precision;         /* LNS_FP64 or LNS_MIXED */
+  int32_t res_compat;        /* 0: totres of each corrector is the residual of
+                                that corrector.  1: the reference's reported
+                                value, whose sum keeps the previous result
+                                (its totres is saved between calls,
+                                src/resstat3d.f90:18), so that it levels off
+                                near 1/(nx*ny).  The step itself is the same. */
 } lns_params3d;
 
 typedef struct lns_ctx3d lns_ctx3d;

@@ -40,10 +40,13 @@ class ImpDrv3D:
     omega, kz (beta), alfa, xper, yper, navier, wall, wallt, top, optx, opty,
     plus cflmax, dtmax, loctime; metrics: dict of the ten (nx, ny) arrays;
     vm: (5, nx, ny) mean flow.  precision: FP64 (reference arithmetic) or
-    MIXED (FP32 LHS factors and sweeps, FP64 RHS, residual and update).
+    MIXED (FP32 scaled LHS factors and sweeps, FP64 RHS, residual and
+    update).  res_compat: report the reference's running residual
+    (src/resstat3d.f90:18 keeps totres between calls) instead of each
+    corrector's own.
     """
 
-    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64):
+    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -51,7 +54,7 @@ class ImpDrv3D:
                        gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax,
                        dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
                        wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
-                       precision=precision)
+                       precision=precision, res_compat=1 if res_compat else 0)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")

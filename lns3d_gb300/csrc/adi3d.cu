@@ -22,6 +22,7 @@
 #include "../../include/lns3d_gb300.h"
 #include "adi3d.cuh"
 #include "launch.cuh"
+#include "penta_chain.cuh"
 
 namespace lns {
 namespace a3 {
@@ -538,8 +539,10 @@ __global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __res
   if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = red[0];
 }
 
-// totres = sqrt(sum / (nx ny)) in a fixed summation order
-__global__ void resid_kernel(int nparts, const double* part, long long npts, double* out) {
+// totres = sqrt(sum / (nx ny)) in a fixed summation order; with acc the sum
+// starts from *acc and the result is stored back into it (the reference's
+// saved totres, src/resstat3d.f90:18)
+__global__ void resid_kernel(int nparts, const double* part, long long npts, double* out, double* acc) {
   __shared__ double red[256];
   double s = 0.0;
   for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += part[k];
@@ -549,7 +552,12 @@ __global__ void resid_kernel(int nparts, const double* part, long long npts, dou
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = sqrt(red[0] / (double)npts);
+  if (threadIdx.x == 0) {
+    const double tot = acc ? *acc + red[0] : red[0];
+    const double r = sqrt(tot / (double)npts);
+    *out = r;
+    if (acc) *acc = r;
+  }
 }
 
 // ----------------------------------------------------------------- update
@@ -627,7 +635,11 @@ struct lns_ctx3d {
   Ops ops{};
   cd *v = nullptr, *vold = nullptr, *r64 = nullptr, *c1v = nullptr;
   cf* r32 = nullptr;
+  // FP64 factors in the reference storage (both modes), and the same
+  // factors in the scaled block form of penta_chain.cuh in the precision of
+  // the sweeps (fillE/fillK alias perx/per2x in the FP64 mode)
   void *matx = nullptr, *maty = nullptr, *perx = nullptr, *per2x = nullptr;
+  void *chnx = nullptr, *chny = nullptr, *fillE = nullptr, *fillK = nullptr;
   double* part = nullptr;  // block partials (residual, CFL)
   int nparts = 0;
   double* dscal = nullptr;  // [0] cfl, [1..] residual of the inspection call
@@ -736,12 +748,13 @@ int res_reserve(lns_ctx3d* c, int n) {
 }
 
 // r = RHS of one corrector into r64 (FP64) and / or r32 (FP32); totres to *res.
-int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vold, cd* r64, cf* r32, double* res, cudaStream_t st) {
+int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vold, cd* r64, cf* r32, double* res, double* acc,
+               cudaStream_t st) {
   const Grid& g = c->g;
   lns::a3::grad1_kernel<<<pt_grid(g), 128, 0, st>>>(g, v, c->c1v);
   lns::a3::rhs_kernel<<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vold, c->c1v, r64, r32, c->part);
   const int nrhs = (int)(pt_grid(g).x * pt_grid(g).y);  // rhs_kernel block partials
-  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res);
+  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res, acc);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "rhs kernels launch");
 }
@@ -754,20 +767,75 @@ int launch_lhs(lns_ctx3d* c, int dir, T* mat, cudaStream_t st) {
   return e == cudaSuccess ? LNS_OK : cuda3(e, "lhs_kernel launch");
 }
 
-// Forms and factors both LHS (code 0), then checks the pivots.
+// Arguments of the xi sweep (periodic lines along i, one per j: np = nx,
+// n = nx - 1 unknowns) and of the eta sweep (lines along j, one per i).
+lns::chain::Args xargs(lns_ctx3d* c, void* rhs) {
+  const Grid& g = c->g;
+  return lns::chain::Args{c->matx, c->chnx, c->perx, c->per2x, c->fillE, c->fillK, rhs, g.nx - 1, g.ny, 1, g.nx};
+}
+lns::chain::Args yargs(lns_ctx3d* c, void* rhs) {
+  const Grid& g = c->g;
+  return lns::chain::Args{c->maty, c->chny, nullptr, nullptr, nullptr, nullptr, rhs, g.ny, g.nx, g.nx, 1};
+}
+
+// The xi sweep: s = D^-1 r, forward recurrence, rows n-1 and n with the
+// periodic fill, the fill correction, backward recurrence.
 template <typename T>
+int sweep_x(lns_ctx3d* c, T* r, cudaStream_t st) {
+  namespace ch = lns::chain;
+  const ch::Args a = xargs(c, r);
+  const long long pts = (long long)a.n * a.nsys, fill = (long long)(a.n - 3) * a.nsys;
+  const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
+  const size_t sm = ch::chain_smem_bytes<T>();
+  ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
+  ch::chain_fwd_kernel<T, true><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  ch::tail_kernel<T><<<a.nsys, 32 * ch::kTailWarps, 0, st>>>(a);
+  ch::fill_kernel<T><<<(unsigned)((fill + 255) / 256), 256, 0, st>>>(a);
+  ch::chain_bwd_kernel<T, true><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "xi sweep launch");
+}
+
+// The eta sweep: s = D^-1 r, forward and backward recurrences.
+template <typename T>
+int sweep_y(lns_ctx3d* c, T* r, cudaStream_t st) {
+  namespace ch = lns::chain;
+  const ch::Args a = yargs(c, r);
+  const long long pts = (long long)a.n * a.nsys;
+  const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
+  const size_t sm = ch::chain_smem_bytes<T>();
+  ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
+  ch::chain_fwd_kernel<T, false><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  ch::chain_bwd_kernel<T, false><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "eta sweep launch");
+}
+
+// Forms both LHS and factors them in FP64 (code 0), checks the pivots, and
+// writes the scaled block form in the precision TC of the sweeps.
+template <typename TC>
 int factor_all(lns_ctx3d* c, cudaStream_t st) {
   const Grid& g = c->g;
-  T* mx = (T*)c->matx;
-  T* my = (T*)c->maty;
-  T* rr = c->r32 ? (T*)c->r32 : (T*)c->r64;  // right-hand side: not touched by code 0
+  cd* mx = (cd*)c->matx;
+  cd* my = (cd*)c->maty;
+  cd* rr = c->c1v;  // a right-hand-side argument; code 0 does not touch it
   cudaError_t e = cudaMemsetAsync(c->status, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda3(e, "cudaMemsetAsync");
-  int rc = launch_lhs<T>(c, 1, mx, st);
-  if (!rc) rc = lns::host::launch_p<T>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status);
-  if (!rc) rc = launch_lhs<T>(c, 2, my, st);
-  if (!rc) rc = lns::host::launch_bc<T>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
+  int rc = launch_lhs<cd>(c, 1, mx, st);
+  if (!rc) rc = lns::host::launch_p<cd>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status);
+  if (!rc) rc = launch_lhs<cd>(c, 2, my, st);
+  if (!rc) rc = lns::host::launch_bc<cd>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
   if (rc) return rc;
+  namespace ch = lns::chain;
+  const ch::Args ax = xargs(c, nullptr), ay = yargs(c, nullptr);
+  const long long tx = (long long)ax.n * ax.nsys, ty = (long long)ay.n * ay.nsys;
+  const unsigned bx = (unsigned)((tx + ch::kPrepWarps - 1) / ch::kPrepWarps);
+  const unsigned by = (unsigned)((ty + ch::kPrepWarps - 1) / ch::kPrepWarps);
+  ch::prep_kernel<cd, TC, true><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+  ch::prep_fill_kernel<cd, TC><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+  ch::prep_kernel<cd, TC, false><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda3(e, "prep kernels launch");
   int status = 0;
   e = cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -799,6 +867,7 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
     if (rc) return rc;
   }
   const size_t vbytes = sizeof(cd) * 5 * (size_t)c->np;
+  double* acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
   for (int s = 0; s < nsteps; ++s) {
     cudaError_t e = cudaMemcpyAsync(c->vold, v, vbytes, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return cuda3(e, "cudaMemcpyAsync vold");
@@ -808,19 +877,19 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
       double* res = (it == niter - 1 && totres_dev) ? totres_dev + s : c->dscal + 1;
       rc = mark(c, st);
       if (mixed) {
-        if (!rc) rc = launch_rhs(c, v, c->vold, nullptr, c->r32, res, st);
+        if (!rc) rc = launch_rhs(c, v, c->vold, nullptr, c->r32, res, acc, st);
         if (!rc) rc = mark(c, st);
-        if (!rc) rc = lns::host::launch_solve<cf, true>(c->matx, c->r32, c->perx, c->per2x, g.nx - 1, g.ny, 1, g.nx, st);
+        if (!rc) rc = sweep_x<cf>(c, c->r32, st);
         if (!rc) rc = mark(c, st);
-        if (!rc) rc = lns::host::launch_solve<cf, false>(c->maty, c->r32, nullptr, nullptr, g.ny, g.nx, g.nx, 1, st);
+        if (!rc) rc = sweep_y<cf>(c, c->r32, st);
         if (!rc) rc = mark(c, st);
         if (!rc) rc = launch_update<cf>(c, v, c->r32, 1, st);
       } else {
-        if (!rc) rc = launch_rhs(c, v, c->vold, c->r64, nullptr, res, st);
+        if (!rc) rc = launch_rhs(c, v, c->vold, c->r64, nullptr, res, acc, st);
         if (!rc) rc = mark(c, st);
-        if (!rc) rc = lns::host::launch_solve<cd, true>(c->matx, c->r64, c->perx, c->per2x, g.nx - 1, g.ny, 1, g.nx, st);
+        if (!rc) rc = sweep_x<cd>(c, c->r64, st);
         if (!rc) rc = mark(c, st);
-        if (!rc) rc = lns::host::launch_solve<cd, false>(c->maty, c->r64, nullptr, nullptr, g.ny, g.nx, g.nx, 1, st);
+        if (!rc) rc = sweep_y<cd>(c, c->r64, st);
         if (!rc) rc = mark(c, st);
         if (!rc) rc = launch_update<cd>(c, v, c->r64, 1, st);
       }
@@ -848,6 +917,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->wallt != 0 && p->wallt != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: wallt must be 0 or 1");
   if (p->top != 0) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0");
   if (p->loctime != 0 && p->loctime != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: loctime must be 0 or 1");
+  if (p->res_compat != 0 && p->res_compat != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: res_compat must be 0 or 1");
   if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
     return fail3(LNS_ERR_ARG, "ctx3d_create: precision must be LNS_FP64 or LNS_MIXED");
   lns_ctx3d* c = new lns_ctx3d();
@@ -886,12 +956,21 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   A(sizeof(cd) * 5 * np, &q); c->c1v = (cd*)q;
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
-  A(el * 125 * np, &c->matx);
-  A(el * 125 * np, &c->maty);
-  A(el * 50 * np, &c->perx);
-  A(el * 50 * np, &c->per2x);
+  A(sizeof(cd) * 125 * np, &c->matx);
+  A(sizeof(cd) * 125 * np, &c->maty);
+  A(sizeof(cd) * 50 * np, &c->perx);
+  A(sizeof(cd) * 50 * np, &c->per2x);
+  A(el * 125 * np, &c->chnx);
+  A(el * 125 * np, &c->chny);
+  if (mixed) {
+    A(el * 50 * np, &c->fillE);
+    A(el * 50 * np, &c->fillK);
+  } else {
+    c->fillE = c->perx;
+    c->fillK = c->per2x;
+  }
   A(sizeof(double) * c->nparts, &q); c->part = (double*)q;
-  A(sizeof(double) * 2, &q); c->dscal = (double*)q;
+  A(sizeof(double) * 3, &q); c->dscal = (double*)q;  // cfl, scratch residual, running residual
   A(sizeof(int), &q); c->status = (int*)q;
   if (!rc) rc = res_reserve(c, 64);
   if (rc) {
@@ -900,6 +979,12 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
     return rc;
   }
   if (!mixed) c->r32 = nullptr;
+  cudaError_t ez = cudaMemset(c->dscal, 0, sizeof(double) * 3);
+  if (ez != cudaSuccess) {
+    free_all(c);
+    delete c;
+    return cuda3(ez, "cudaMemset");
+  }
   double* o = c->opbuf;
   c->ops.np = np;
   c->ops.Ah = o; c->ops.Bh = o + 25 * np; c->ops.Dh = o + 50 * np; c->ops.Dhi = o + 75 * np;
@@ -991,7 +1076,7 @@ int lns_rhs3d_dev(lns_ctx3d* c, const double* v, const double* vold, double* r, 
   int rc = check_device(c);
   if (rc) return rc;
   return launch_rhs(c, (const cd*)v, (const cd*)vold, (cd*)r, nullptr, totres_dev ? totres_dev : c->dscal + 1,
-                    (cudaStream_t)stream);
+                    nullptr, (cudaStream_t)stream);
 }
 
 int lns_lhs3d_dev(lns_ctx3d* c, int32_t dir, double* mat, void* stream) {

@@ -1,0 +1,514 @@
+// Sweeps of the 3D step on factors kept in a scaled block form.
+//
+// The line solvers factor A = L U in the reference's storage
+// (src/cpenta1bc.f:52-498, src/cpenta2p.f): per row i the stored lower
+// blocks S_ic (applied as y_i += S_ic y_c), the in-block LU of the diagonal
+// block D_i = L_ii U_ii, and the upper blocks T_ic (x_i -= T_ic x_c).  With
+//     yh_i = U_ii^-1 y_i,   s_i = D_i^-1 r_i,
+//     F_ic = -D_i^-1 S_ic U_cc,   B_ic = U_ii^-1 T_ic,
+// the two triangular solves become
+//     forward   yh_i = s_i - sum_c F_ic yh_c
+//     backward  x_i  = yh_i - sum_c B_ic x_c
+// so a row of either recurrence is two (at the boundary rows up to four)
+// dense 5x5 block-vector products and nothing else: no in-block
+// substitution, no division.  The products of a row are spread over 25
+// lanes of a warp, lane l = m + 5 q owning entry (m, q); the sum over q is a
+// gather of five shuffles.  s_i = D_i^-1 r_i and, for periodic lines, the
+// fill of rows n-1, n (columns n-1, n) are independent of the recurrence and
+// run as point-parallel kernels around it.
+//
+// Internal record of row i (125 entries, block-major, entry (m, q) of a
+// block at m + 5 q):
+//   block 0  D_i^-1
+//   blocks 1..4 by row type (F_d: column i-d, B_d: column i+d)
+//     rows 3..n-2     F1 F2 B1 B2          row 1    B3 B4 B1 B2
+//     row 2           F1 B3 B1 B2          row n-1  F1 F2 B1 F3
+//     row n           F1 F2 F3 F4          periodic lines: F1 F2 B1 B2 on
+//                                          every row, absent blocks zero
+// Periodic fill, 50 entries per record (may overwrite the per / per2
+// records they come from):
+//   E(i)   E1 = U_ii^-1 per(1,i) (column n-1, rows <= n-4) at [0,25),
+//          E0 = U_ii^-1 per(2,i) (column n,   rows <= n-3) at [25,50)
+//   K(c)   K1 = -D_{n-1}^-1 per2(n-1,c) U_cc (c <= n-4) at [0,25),
+//          K0 = -D_n^-1 per2(n,c) U_cc       (c <= n-3) at [25,50)
+// The prep kernels read the factors in one precision (TM) and write the
+// internal form in the precision of the sweeps (TC), computing in FP64.
+#pragma once
+#include "penta_direct.cuh"
+
+namespace lns {
+namespace chain {
+
+struct Args {
+  const void* mat;   // factored records, reference storage (prep only)
+  void* chn;         // internal records
+  const void* per;   // periodic fill in the reference storage (prep only)
+  const void* per2;
+  void* fillE;       // periodic fill E, K in the internal form (may alias per, per2)
+  void* fillK;
+  void* rhs;
+  int n;             // unknowns per line (periodic: np - 1)
+  int nsys;
+  long long row_stride, line_stride;
+};
+
+__device__ __forceinline__ long long rec_of(const Args& a, int r, int iv) {
+  return a.row_stride * (r - 1) + a.line_stride * iv;
+}
+
+// ------------------------------------------------------------------- prep
+// Warp-per-record helpers (FP64 arithmetic whatever the storage type).
+__device__ __forceinline__ cd ld_cd(const cd* p) { return *p; }
+__device__ __forceinline__ cd ld_cd(const cf* p) { return cd{(double)p->x, (double)p->y}; }
+__device__ __forceinline__ void st_t(cd* p, cd v) { *p = v; }
+__device__ __forceinline__ void st_t(cf* p, cd v) { *p = cf{(float)v.x, (float)v.y}; }
+
+// C = A * B for 5x5 blocks in shared memory (entry (m,q) at m + 5 q), lane
+// l < 25 computes entry l.  `upperB` skips the zero lower part of B.
+__device__ __forceinline__ cd mm5(const cd* A, const cd* B, int m, int q, bool upperB) {
+  cd acc{0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+    if (!upperB || k <= q) acc = fmac(acc, A[m + 5 * k], B[k + 5 * q]);
+  return acc;
+}
+
+constexpr int kPrepWarps = 4;
+// per-warp shared memory of the prep kernels, in cd units
+constexpr int kPrepSm = 7 * 25;
+
+// Position of the block of column offset d (-4..4, d != 0) in the internal
+// record of row i, or -1 when the row holds no such block.
+__device__ __forceinline__ int pos_bc(int i, int n, int d) {
+  if (i == 1) return d == 1 ? 3 : d == 2 ? 4 : d == 3 ? 1 : d == 4 ? 2 : -1;
+  if (i == 2) return d == -1 ? 1 : d == 1 ? 3 : d == 2 ? 4 : d == 3 ? 2 : -1;
+  if (i == n) return d == -1 ? 1 : d == -2 ? 2 : d == -3 ? 3 : d == -4 ? 4 : -1;
+  if (i == n - 1) return d == -1 ? 1 : d == -2 ? 2 : d == 1 ? 3 : d == -3 ? 4 : -1;
+  return d == -1 ? 1 : d == -2 ? 2 : d == 1 ? 3 : d == 2 ? 4 : -1;
+}
+__device__ __forceinline__ bool has_bc(int i, int n, int d) {
+  const int c = i + d;
+  if (c < 1 || c > n) return false;
+  if (d < 0) return c >= (i >= n - 1 ? n - 4 : i - 2);
+  return c <= (i <= 2 ? 5 : min(i + 2, n));
+}
+__device__ __forceinline__ int pos_p(int d) { return d == -1 ? 1 : d == -2 ? 2 : d == 1 ? 3 : d == 2 ? 4 : -1; }
+__device__ __forceinline__ bool has_p(int i, int n, int d) {
+  // periodic band after the fill set-up (src/cpenta2p.f:52-77): lower blocks
+  // from column 1, upper blocks up to column n
+  const int c = i + d;
+  return c >= 1 && c <= n && d >= -2 && d <= 2 && d != 0;
+}
+
+// One warp per record (row i of line iv): writes the internal record and,
+// for periodic lines, E into the per record.
+template <typename TM, typename TC, bool PER>
+__global__ void __launch_bounds__(32 * kPrepWarps) prep_kernel(Args a) {
+  __shared__ cd sm[kPrepWarps][kPrepSm];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const long long task = (long long)blockIdx.x * kPrepWarps + warp;
+  if (task >= (long long)a.n * a.nsys) return;
+  const int iv = (int)(task / a.n), i = (int)(task % a.n) + 1;
+  const int n = a.n;
+  cd* Dg = sm[warp];       // factored diagonal block of row i
+  cd* Li = Dg + 25;        // L_ii^-1
+  cd* Ui = Dg + 50;        // U_ii^-1
+  cd* Di = Dg + 75;        // D_i^-1
+  cd* S = Dg + 100;        // a stored off-diagonal block
+  cd* Uc = Dg + 125;       // U_cc of its column
+  cd* Tm = Dg + 150;       // S U_cc
+  const TM* mat = reinterpret_cast<const TM*>(a.mat);
+  TC* chn = reinterpret_cast<TC*>(a.chn);
+  const long long rc = rec_of(a, i, iv);
+  const TM* rec = mat + 125 * rc;
+  const int m = lane % 5, q = lane / 5;
+  if (lane < 25) Dg[m + 5 * q] = ld_cd(rec + 2 + 5 * m + 25 * q);
+  __syncwarp();
+  if (lane < 5) {
+    const int j = lane;
+    // column j of L_ii^-1: L = I - strict lower part of the stored block
+    cd z[5];
+#pragma unroll
+    for (int mm = 0; mm < 5; ++mm) {
+      cd v = cd{mm == j ? 1.0 : 0.0, 0.0};
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        if (k < mm && k >= j) v = fmac(v, Dg[mm + 5 * k], z[k]);
+      z[mm] = mm < j ? cd{0.0, 0.0} : v;
+    }
+#pragma unroll
+    for (int mm = 0; mm < 5; ++mm) Li[mm + 5 * j] = z[mm];
+    // column j of U_ii^-1: U = upper part with the diagonal
+#pragma unroll
+    for (int mm = 4; mm >= 0; --mm) {
+      cd v = cd{mm == j ? 1.0 : 0.0, 0.0};
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        if (k > mm) v = fmsc(v, Dg[mm + 5 * k], z[k]);
+      z[mm] = mm > j ? cd{0.0, 0.0} : mul(v, rcp(Dg[mm + 5 * mm]));
+    }
+#pragma unroll
+    for (int mm = 0; mm < 5; ++mm) Ui[mm + 5 * j] = z[mm];
+  }
+  __syncwarp();
+  const bool act = lane < 25;  // lanes 25..31 idle in the block products
+  if (act) Di[lane] = mm5(Ui, Li, m, q, false);
+  __syncwarp();
+  TC* out = chn + 125 * rc;
+  if (lane < 25) st_t(out + lane, Di[lane]);
+  bool written[5] = {true, false, false, false, false};
+  for (int d = -4; d <= 4; ++d) {
+    if (d == 0) continue;
+    const bool has = PER ? has_p(i, n, d) : has_bc(i, n, d);
+    if (!has) continue;
+    const int pos = PER ? pos_p(d) : pos_bc(i, n, d);
+    const int c = i + d;
+    if (lane < 25) S[lane] = ld_cd(rec + (slot_bc(i, c) - 1) + 5 * m + 25 * q);
+    if (d < 0 && lane < 25)
+      Uc[lane] = m <= q ? ld_cd(mat + 125 * rec_of(a, c, iv) + 2 + 5 * m + 25 * q) : cd{0.0, 0.0};
+    __syncwarp();
+    cd v{0.0, 0.0};
+    if (d < 0) {
+      if (act) Tm[lane] = mm5(S, Uc, m, q, true);
+      __syncwarp();
+      if (act) v = mm5(Di, Tm, m, q, false);
+      v = cd{-v.x, -v.y};
+    } else if (act) {
+      v = mm5(Ui, S, m, q, false);
+    }
+    if (lane < 25) st_t(out + 25 * pos + lane, v);
+    written[pos] = true;
+    __syncwarp();
+  }
+  for (int p = 1; p < 5; ++p)
+    if (!written[p] && lane < 25) st_t(out + 25 * p + lane, cd{0.0, 0.0});
+  if (PER) {
+    // E1, E0 from per(1,i), per(2,i) (reference order j + 2m + 10q)
+    const TM* pr = reinterpret_cast<const TM*>(a.per) + 50 * rc;
+    TC* pe = reinterpret_cast<TC*>(a.fillE) + 50 * rc;
+    cd p1 = cd{0.0, 0.0}, p0 = cd{0.0, 0.0};
+    if (lane < 25) {
+      p1 = ld_cd(pr + 0 + 2 * m + 10 * q);
+      p0 = ld_cd(pr + 1 + 2 * m + 10 * q);
+    }
+    __syncwarp();
+    if (lane < 25) S[lane] = p1, Tm[lane] = p0;
+    __syncwarp();
+    const cd e1 = (act && i <= n - 4) ? mm5(Ui, S, m, q, false) : cd{0.0, 0.0};
+    const cd e0 = (act && i <= n - 3) ? mm5(Ui, Tm, m, q, false) : cd{0.0, 0.0};
+    if (lane < 25) {
+      st_t(pe + lane, e1);
+      st_t(pe + 25 + lane, e0);
+    }
+  }
+}
+
+// Periodic lines: K1, K0 of column c from its per2 record (one warp per
+// record; needs D_{n-1}^-1, D_n^-1 from prep_kernel).
+template <typename TM, typename TC>
+__global__ void __launch_bounds__(32 * kPrepWarps) prep_fill_kernel(Args a) {
+  __shared__ cd sm[kPrepWarps][4 * 25];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const long long task = (long long)blockIdx.x * kPrepWarps + warp;
+  if (task >= (long long)a.n * a.nsys) return;
+  const int iv = (int)(task / a.n), c = (int)(task % a.n) + 1;
+  const int n = a.n;
+  const int m = lane % 5, q = lane / 5;
+  const TM* p2 = reinterpret_cast<const TM*>(a.per2) + 50 * rec_of(a, c, iv);
+  TC* pk = reinterpret_cast<TC*>(a.fillK) + 50 * rec_of(a, c, iv);
+  if (c > n - 3) {
+    if (lane < 25) st_t(pk + lane, cd{0.0, 0.0}), st_t(pk + 25 + lane, cd{0.0, 0.0});
+    return;
+  }
+  const TM* mat = reinterpret_cast<const TM*>(a.mat);
+  const TC* chn = reinterpret_cast<const TC*>(a.chn);
+  cd* Uc = sm[warp];
+  cd* P = Uc + 25;
+  cd* Tm = Uc + 50;
+  cd* Dn = Uc + 75;
+  if (lane < 25) Uc[lane] = m <= q ? ld_cd(mat + 125 * rec_of(a, c, iv) + 2 + 5 * m + 25 * q) : cd{0.0, 0.0};
+  cd k1 = cd{0.0, 0.0}, k0 = cd{0.0, 0.0};
+  for (int t = 0; t < 2; ++t) {
+    const int row = t == 0 ? n - 1 : n;
+    if (t == 0 && c > n - 4) continue;
+    __syncwarp();
+    if (lane < 25) {
+      P[lane] = ld_cd(p2 + t + 2 * m + 10 * q);
+      Dn[lane] = ld_cd(chn + 125 * rec_of(a, row, iv) + lane);
+    }
+    __syncwarp();
+    if (lane < 25) Tm[lane] = mm5(P, Uc, m, q, true);
+    __syncwarp();
+    cd v{0.0, 0.0};
+    if (lane < 25) v = mm5(Dn, Tm, m, q, false);
+    v = cd{-v.x, -v.y};
+    if (t == 0) k1 = v; else k0 = v;
+  }
+  __syncwarp();
+  if (lane < 25) {
+    st_t(pk + lane, k1);
+    st_t(pk + 25 + lane, k0);
+  }
+}
+
+// ------------------------------------------------------------ the sweeps
+// s = D^-1 r in place, one thread per record of rows 1..n.
+template <typename T>
+__global__ void scale_kernel(Args a) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)a.n * a.nsys) return;
+  int i, iv;
+  if (a.row_stride == 1) i = (int)(t % a.n) + 1, iv = (int)(t / a.n);
+  else iv = (int)(t % a.nsys), i = (int)(t / a.nsys) + 1;
+  const long long rc = rec_of(a, i, iv);
+  const T* D = reinterpret_cast<const T*>(a.chn) + 125 * rc;
+  T* r = reinterpret_cast<T*>(a.rhs) + 5 * rc;
+  T x[5], s[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) x[k] = r[k];
+#pragma unroll
+  for (int mm = 0; mm < 5; ++mm) {
+    T acc = zero<T>();
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc = fmac(acc, D[mm + 5 * k], x[k]);
+    s[mm] = acc;
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[k] = s[k];
+}
+
+template <typename T> struct ChainCfg;
+template <> struct ChainCfg<cd> { static constexpr int kAhead = 12; };
+template <> struct ChainCfg<cf> { static constexpr int kAhead = 24; };
+constexpr int kChainWarps = 2;                 // lines per CTA
+constexpr int kStage = 55;                     // 50 block entries + 5 right-hand-side entries
+
+template <typename T>
+constexpr size_t chain_smem_bytes() {
+  return (size_t)kChainWarps * (ChainCfg<T>::kAhead + 1) * kStage * sizeof(T);
+}
+
+// sum over q of lane (m,q)'s partial, for m = this lane's q
+template <typename T>
+__device__ __forceinline__ T gather5(T p, int qq) {
+  const unsigned full = 0xffffffffu;
+  T s = shfl(full, p, qq);
+  s = add(s, shfl(full, p, qq + 5));
+  s = add(s, shfl(full, p, qq + 10));
+  s = add(s, shfl(full, p, qq + 15));
+  s = add(s, shfl(full, p, qq + 20));
+  return s;
+}
+
+// Stage row r: entries [off, off+50) of its internal record and its 5
+// right-hand-side entries.
+template <typename T>
+__device__ __forceinline__ void chain_stage(T* slot, const Args& a, int r, int iv, int off, int lane) {
+  const long long rc = rec_of(a, r, iv);
+  const T* src = reinterpret_cast<const T*>(a.chn) + 125 * rc + off;
+  const T* rhs = reinterpret_cast<const T*>(a.rhs) + 5 * rc;
+  cp_async_el(slot + lane, src + lane);
+  const int e = lane + 32;
+  if (e < 50) cp_async_el(slot + e, src + e);
+  else if (e < 55) cp_async_el(slot + e, rhs + (e - 50));
+}
+
+// Forward recurrence yh_i = s_i - sum_c F_ic yh_c over rows 1..top (top = n,
+// or n-2 for periodic lines whose rows n-1, n follow in tail_kernel).
+template <typename T, bool PER>
+__global__ void __launch_bounds__(32 * kChainWarps) chain_fwd_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int kAhead = ChainCfg<T>::kAhead, kRing = kAhead + 1;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int iv = blockIdx.x * kChainWarps + warp;
+  if (iv >= a.nsys) return;
+  T* ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
+  const int n = a.n, top = PER ? n - 2 : n;
+  const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
+  T* grhs = reinterpret_cast<T*>(a.rhs);
+  const T* gchn = reinterpret_cast<const T*>(a.chn);
+  for (int r = 1; r <= kAhead; ++r) {
+    if (r <= top) chain_stage(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, lane);
+    cp_async_commit();
+  }
+  T z1 = zero<T>(), z2 = zero<T>(), z3 = zero<T>(), z4 = zero<T>();  // yh of rows i-1..i-4, component qq
+  for (int i = 1; i <= top; ++i) {
+    __syncwarp();  // every lane is done with the slot about to be refilled
+    const int r = i + kAhead;
+    if (r <= top) chain_stage(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, lane);
+    cp_async_commit();
+    cp_async_wait<kAhead>();
+    __syncwarp();
+    const T* st = ring + ((i - 1) % kRing) * kStage;
+    T p;
+    if (PER || (i >= 3 && i <= n - 2)) {
+      p = fmac(mul(st[l], z1), st[25 + l], z2);
+    } else if (i == 1) {
+      p = zero<T>();
+    } else if (i == 2) {
+      p = mul(st[l], z1);
+    } else {
+      const T* g = gchn + 125 * rec_of(a, i, iv);
+      p = fmac(mul(st[l], z1), st[25 + l], z2);
+      if (i == n - 1) {
+        p = fmac(p, g[100 + l], z3);
+      } else {
+        p = fmac(p, g[75 + l], z3);
+        p = fmac(p, g[100 + l], z4);
+      }
+    }
+    const T yv = sub(st[50 + qq], gather5(p, qq));
+    z4 = z3; z3 = z2; z2 = z1; z1 = yv;
+    if (lane < 25 && m == 0) grhs[5 * rec_of(a, i, iv) + qq] = yv;
+  }
+  cp_async_wait<0>();
+}
+
+// Backward recurrence x_i = c_i - sum_c B_ic x_c from row top down to 1
+// (top = n; periodic: n-2, with x_{n-1}, x_n from tail_kernel and c_i from
+// fill_kernel; row np then repeats row 1).
+template <typename T, bool PER>
+__global__ void __launch_bounds__(32 * kChainWarps) chain_bwd_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int kAhead = ChainCfg<T>::kAhead, kRing = kAhead + 1;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int iv = blockIdx.x * kChainWarps + warp;
+  if (iv >= a.nsys) return;
+  T* ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
+  const int n = a.n, top = PER ? n - 2 : n;
+  const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
+  T* grhs = reinterpret_cast<T*>(a.rhs);
+  const T* gchn = reinterpret_cast<const T*>(a.chn);
+  // ring slot k holds the k-th row processed (row top - k)
+  for (int k = 0; k < kAhead; ++k) {
+    const int r = top - k;
+    if (r >= 1) chain_stage(ring + (k % kRing) * kStage, a, r, iv, 75, lane);
+    cp_async_commit();
+  }
+  T x1 = zero<T>(), x2 = zero<T>(), x3 = zero<T>(), x4 = zero<T>();  // x of rows i+1..i+4, component qq
+  if (PER) {
+    x1 = grhs[5 * rec_of(a, n - 1, iv) + qq];
+    x2 = grhs[5 * rec_of(a, n, iv) + qq];
+  }
+  for (int k = 0; k < top; ++k) {
+    __syncwarp();  // every lane is done with the slot about to be refilled
+    const int i = top - k;
+    const int kn = k + kAhead, rn = top - kn;
+    if (rn >= 1) chain_stage(ring + (kn % kRing) * kStage, a, rn, iv, 75, lane);
+    cp_async_commit();
+    cp_async_wait<kAhead>();
+    __syncwarp();
+    const T* st = ring + (k % kRing) * kStage;
+    T p;
+    if (PER || (i >= 3 && i <= n - 2)) {
+      p = fmac(mul(st[l], x1), st[25 + l], x2);
+    } else if (i == n) {
+      p = zero<T>();
+    } else if (i == n - 1) {
+      p = mul(st[l], x1);
+    } else {
+      const T* g = gchn + 125 * rec_of(a, i, iv);
+      p = fmac(mul(st[l], x1), st[25 + l], x2);
+      if (i == 2) {
+        p = fmac(p, g[50 + l], x3);
+      } else {
+        p = fmac(p, g[25 + l], x3);
+        p = fmac(p, g[50 + l], x4);
+      }
+    }
+    const T xv = sub(st[50 + qq], gather5(p, qq));
+    x4 = x3; x3 = x2; x2 = x1; x1 = xv;
+    if (lane < 25 && m == 0) {
+      grhs[5 * rec_of(a, i, iv) + qq] = xv;
+      if (PER && i == 1) grhs[5 * rec_of(a, n + 1, iv) + qq] = xv;  // row np = row 1
+    }
+  }
+  cp_async_wait<0>();
+}
+
+// Periodic lines, after the forward recurrence: the fill sums
+// t1 = sum_{c<=n-4} K1_c yh_c, t0 = sum_{c<=n-3} K0_c yh_c, rows n-1 and n of
+// both recurrences, and x_{n-1}, x_n into the right-hand side.  One CTA of
+// kTailWarps warps per line.
+constexpr int kTailWarps = 8;
+template <typename T>
+__global__ void __launch_bounds__(32 * kTailWarps) tail_kernel(Args a) {
+  __shared__ T red[2][kTailWarps][25];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int iv = blockIdx.x;
+  const int n = a.n;
+  const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
+  T* grhs = reinterpret_cast<T*>(a.rhs);
+  const T* gchn = reinterpret_cast<const T*>(a.chn);
+  const T* gp2 = reinterpret_cast<const T*>(a.fillK);
+  T acc1 = zero<T>(), acc0 = zero<T>();
+  for (int c = 1 + warp; c <= n - 3; c += kTailWarps) {
+    const long long rc = rec_of(a, c, iv);
+    const T y = grhs[5 * rc + qq];
+    acc1 = fmac(acc1, gp2[50 * rc + l], y);       // K1 (zero for c = n-3)
+    acc0 = fmac(acc0, gp2[50 * rc + 25 + l], y);  // K0
+  }
+  if (lane < 25) {
+    red[0][warp][lane] = acc1;
+    red[1][warp][lane] = acc0;
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  T s1 = zero<T>(), s0 = zero<T>();
+#pragma unroll
+  for (int w = 0; w < kTailWarps; ++w) {
+    s1 = add(s1, red[0][w][l]);
+    s0 = add(s0, red[1][w][l]);
+  }
+  const T t1 = gather5(s1, qq), t0 = gather5(s0, qq);
+  const long long r1 = rec_of(a, n - 1, iv), r0 = rec_of(a, n, iv);
+  const T ym2 = grhs[5 * rec_of(a, n - 2, iv) + qq], ym3 = grhs[5 * rec_of(a, n - 3, iv) + qq];
+  // row n-1: band columns n-2 (F1), n-3 (F2)
+  const T* c1 = gchn + 125 * r1;
+  T p = fmac(mul(c1[25 + l], ym2), c1[50 + l], ym3);
+  const T yn1 = sub(sub(grhs[5 * r1 + qq], t1), gather5(p, qq));
+  // row n: band columns n-1 (F1), n-2 (F2)
+  const T* c0 = gchn + 125 * r0;
+  p = fmac(mul(c0[25 + l], yn1), c0[50 + l], ym2);
+  const T yn0 = sub(sub(grhs[5 * r0 + qq], t0), gather5(p, qq));
+  // backward: x_n = yh_n, x_{n-1} = yh_{n-1} - B1 x_n
+  p = mul(c1[75 + l], yn0);
+  const T xn1 = sub(yn1, gather5(p, qq));
+  if (lane < 25 && m == 0) {
+    grhs[5 * r1 + qq] = xn1;
+    grhs[5 * r0 + qq] = yn0;
+  }
+}
+
+// Periodic lines: c_i = yh_i - E1_i x_{n-1} - E0_i x_n for rows 1..n-3, one
+// thread per record.
+template <typename T>
+__global__ void fill_kernel(Args a) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int rows = a.n - 3;
+  if (t >= (long long)rows * a.nsys) return;
+  int i, iv;
+  if (a.row_stride == 1) i = (int)(t % rows) + 1, iv = (int)(t / rows);
+  else iv = (int)(t % a.nsys), i = (int)(t / a.nsys) + 1;
+  T* grhs = reinterpret_cast<T*>(a.rhs);
+  const long long rc = rec_of(a, i, iv);
+  const T* E = reinterpret_cast<const T*>(a.fillE) + 50 * rc;
+  const T* xa = grhs + 5 * rec_of(a, a.n - 1, iv);
+  const T* xb = grhs + 5 * rec_of(a, a.n, iv);
+  T xn1[5], xn0[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) xn1[k] = xa[k], xn0[k] = xb[k];
+  T* r = grhs + 5 * rc;
+#pragma unroll
+  for (int mm = 0; mm < 5; ++mm) {
+    T acc = r[mm];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[mm + 5 * k], xn1[k]);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[25 + mm + 5 * k], xn0[k]);
+    r[mm] = acc;
+  }
+}
+
+}  // namespace chain
+}  // namespace lns

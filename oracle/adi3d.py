@@ -16,7 +16,8 @@ class A3Grid(ctypes.Structure):
                 ("gamma1", D), ("omega", D), ("kz", D), ("alfa", D), ("cflmax", D), ("dtmax", D),
                 ("loctime", I), ("xper", I), ("yper", I), ("navier", I), ("wall", I), ("wallt", I), ("top", I),
                 ("optx", I), ("opty", I)] + [(k, P) for k in
-                                             ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")]
+                                             ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")] + \
+        [("resacc", P)]
 
 
 class A3Ops(ctypes.Structure):
@@ -52,7 +53,7 @@ def ptr(a):
 class Oracle3D:
     """Holds the oracle's grid struct, operators and factor arrays for one case."""
 
-    def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None):
+    def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, res_compat=False):
         self.L = _lib(lib)
         self.case = case
         p = case["params"]
@@ -63,6 +64,10 @@ class Oracle3D:
                                              "omega", "kz", "alfa", "xper", "yper", "navier", "wall", "wallt",
                                              "top", "optx", "opty")},
                         **{k: ptr(v).value for k, v in self.keep.items()})
+        # the reference's running residual sum (its saved totres), when asked for
+        self.resacc = ctypes.c_double(0.0)
+        if res_compat:
+            self.g.resacc = ctypes.cast(ctypes.byref(self.resacc), P).value
         nx, ny = self.nx, self.ny
         self.ops = {k: np.zeros((5, 5, nx, ny), order="F") for k in ("Ah", "Bh", "Dh", "Dhi")}
         self.ops.update({k: np.zeros((6, nx, ny), order="F") for k in ("Vh11", "Vh12", "Vh22", "ABhi")})

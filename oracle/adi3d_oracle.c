@@ -12,39 +12,8 @@
 
 #include "penta_oracle.h"
 
-/* src/stencil.f90:10-94 (the reference's coefficient table) */
-/* Line and row loops are independent; the timing build (-fopenmp) runs them
-   in parallel, the parity build (no -fopenmp) serially.  The residual sum
-   stays serial so its order is the same in both. */
-#ifdef _OPENMP
-#define OMP_FOR _Pragma("omp parallel for schedule(static)")
-#else
-#define OMP_FOR
-#endif
+#include "oracle_common.h"
 
-static const double ga1 = 8.333333333333333333333E-02, ga2 = -6.666666666666666666667E-01,
-                    ga3 = 6.666666666666666666667E-01, ga4 = -8.333333333333333333333E-02;
-static const double gc1 = -2.083333333333333333333E+00, gc2 = 4.000000000000000000000E+00,
-                    gc3 = -3.000000000000000000000E+00, gc4 = 1.333333333333333333333E+00,
-                    gc5 = -2.500000000000000000000E-01;
-static const double gb1 = -2.500000000000000000000E-01, gb2 = -8.333333333333333333333E-01,
-                    gb3 = 1.500000000000000000000E+00, gb4 = -5.000000000000000000000E-01,
-                    gb5 = 8.333333333333333333333E-02;
-static const double da1 = -8.333333333333333333333E-02, da2 = 1.333333333333333333333E+00,
-                    da3 = -2.500000000000000000000E+00, da4 = 1.333333333333333333333E+00,
-                    da5 = -8.333333333333333333333E-02;
-static const double db1 = 9.166666666666666666667E-01, db2 = -1.666666666666666666667E+00,
-                    db3 = 5.000000000000000000000E-01, db4 = 3.333333333333333333333E-01,
-                    db5 = -8.333333333333333333333E-02;
-static const double dd1 = 2.916666666666666666667E+00, dd2 = -8.666666666666666666667E+00,
-                    dd3 = 9.500000000000000000000E+00, dd4 = -4.666666666666666666667E+00,
-                    dd5 = 9.166666666666666666667E-01;
-/* src/global.f90:2-15 */
-static const double zero = 0.0, pt5 = 5.0000000000000000000e-1, pt66 = 6.6666666666666666666e-1,
-                    one = 1.0, two = 2.0, four = 4.0;
-
-#define IX(g, i, j) ((long)((i) - 1) + (long)(g)->nx * ((j) - 1))
-#define FV(v, nc, c, g, i, j) (v)[(long)(c) + (long)(nc) * IX(g, i, j)]
 
 /* ------------------------------------------------------------------ stencils */
 
@@ -599,9 +568,11 @@ void a3_rhsbc(const A3Grid* g, double* rl, const double* vl) {
       for (int k = 0; k < 5; ++k) CRE(rl, k, g, nx, j) = zero, CIM(rl, k, g, nx, j) = zero;
 }
 
-/* src/resstat3d.f90:37-60: sqrt(sum |r|^2 / dtl^2 / (nx ny)) */
+/* src/resstat3d.f90:37-60: sqrt(sum |r|^2 / dtl^2 / (nx ny)); with
+   g->resacc the sum starts from the previous result, as the reference's
+   saved totres does (src/resstat3d.f90:18) */
 double a3_resstat(const A3Grid* g, const double* res, const double* dtl) {
-  double totres = 0.0;
+  double totres = g->resacc ? *g->resacc : 0.0;
   for (int j = 1; j <= g->ny; ++j)
     for (int i = 1; i <= g->nx; ++i) {
       double s = 0.0;
@@ -612,7 +583,9 @@ double a3_resstat(const A3Grid* g, const double* res, const double* dtl) {
       const double d = dtl[IX(g, i, j)];
       totres = totres + s / (d * d);
     }
-  return sqrt(totres / (double)((long)g->nx * g->ny));
+  totres = sqrt(totres / (double)((long)g->nx * g->ny));
+  if (g->resacc) *g->resacc = totres;
+  return totres;
 }
 
 /* src/itrbc3d.f90:35-205 for the supported boundary conditions */

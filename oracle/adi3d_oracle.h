@@ -41,6 +41,11 @@ typedef struct {
   int xper, yper, navier, wall, wallt, top, optx, opty;
   /* metrics (nx,ny): m1 m2 n1 n2 m11 m12 m22 n11 n12 n22 */
   const double *m1, *m2, *n1, *n2, *m11, *m12, *m22, *n11, *n12, *n22;
+  /* NULL: resstat3D returns the residual of its own call.  Otherwise the
+     running sum of the reference (its totres keeps its value between calls,
+     src/resstat3d.f90:18): the sum starts from *resacc, and the result is
+     stored back into it. */
+  double* resacc;
 } A3Grid;
 
 /* Frozen operators of the linear step (outputs of genmtrx(vm, kz, vm)). */

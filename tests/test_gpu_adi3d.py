@@ -150,21 +150,25 @@ def test_many_steps_track_oracle_and_converge(cuda):
 
 
 def test_mixed_precision_converges_to_fp64_state(cuda):
+    # A mixed step is the FP64 step with the correction solved by FP32 sweeps:
+    # one step from the same state differs from the FP64 step by FP32 rounding
+    # of the correction (bound 1e-4 of the correction: FP32 precision times
+    # the growth along a 48-row line), and the FP64 residual drives both runs
+    # down at the same rate.
     from lns3d_gb300.cases import shear_layer
 
     case = shear_layer(nx=48, ny=40, seed=0)
     d64, d32 = make_drv(case, precision=0), make_drv(case, precision=1)
     assert d32.device_bytes < d64.device_bytes
-    v64 = case["v"].copy(order="F")
-    v32 = case["v"].copy(order="F")
-    r64 = d64.step(v64, nsteps=300)
-    r32 = d32.step(v32, nsteps=300)
-    # every step solves for the correction only: FP32 sweeps perturb the path
-    # by FP32 rounding of the correction, and the FP64 residual drives both to
-    # the same state
-    assert np.abs(r32 - r64).max() <= 1e-4 * r64.max()
-    assert rel(v32, v64) < 1e-5
-    assert r32[-1] < 1e-2 * r32[0]
+    v0 = case["v"].copy(order="F")
+    a, b = v0.copy(order="F"), v0.copy(order="F")
+    d64.step(a)
+    d32.step(b)
+    assert np.abs(b - a).max() <= 1e-4 * np.abs(a - v0).max()
+    r64 = d64.step(a, nsteps=600)
+    r32 = d32.step(b, nsteps=600)
+    assert np.abs(r32 / r64 - 1.0).max() < 1e-2
+    assert r32[-1] < 1e-3 * r32[0]
 
 
 def test_state_mutation_refactors_after_new_mean(cuda, small):
@@ -231,4 +235,26 @@ def test_full_size_step_is_linear(cuda, precision):
         drv.step(v, nsteps=2)
     torch.cuda.synchronize()
     err = float((c - (2.0 * a - 3.0 * b)).abs().max() / c.abs().max())
-    assert err < (1e-12 if precision == 0 else 1e-5), err
+    # FP64: rounding of the FP64 step; mixed: FP32 rounding of the correction
+    assert err < (1e-12 if precision == 0 else 1e-4), err
+
+
+def test_reference_residual_history_mode(cuda):
+    # res_compat reproduces the reference's reported residual, whose sum keeps
+    # the previous result (src/resstat3d.f90:18); the states are unaffected
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=40, ny=33, seed=6)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1, res_compat=True)
+    drv = make_drv(case)
+    from lns3d_gb300 import ImpDrv3D
+
+    drv_c = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, res_compat=True)
+    v_ref, v_a, v_b = (case["v"].copy(order="F") for _ in range(3))
+    res_ref = np.array([orc.step(v_ref, niter=2) for _ in range(30)])
+    res_c = drv_c.step(v_a, nsteps=30, niter=2)
+    drv.step(v_b, nsteps=30, niter=2)
+    assert np.abs(res_c - res_ref).max() <= 1e-10 * res_ref.max()
+    assert np.array_equal(v_a, v_b)
+    # the reported value levels off near 1 / (nx ny)
+    assert abs(res_ref[-1] - 1.0 / (40 * 33)) < 0.05 / (40 * 33)
