@@ -395,6 +395,47 @@ def run_isolated(torch, dev, L, sp, stream, rank, world, W, K):
             "fp64_tflops": FLOPS_PER_PT * PTS / (ms / 1e3) / 1e12, "mixed": mixed}
 
 
+def run_impdrv2d(torch, dev, steps, with_cpu):
+    """The nonlinear 2D step (src/impdrv.f90) on its benchmark case: an Oseen
+    vortex in a uniform stream, 128 x 128, Ma 0.5, Re 1000, global time step
+    at CFL 1 (lns3d_gb300.cases.vortex2d).  Each step forms and factors both
+    LHS, as the reference does; FP64 throughout."""
+    import lns3d_gb300 as g
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=128, ny=128, seed=0)
+    drv = g.ImpDrv2D(c["params"], c["metrics"], c["bnt"], c["pot"], cflmax=1.0, loctime=0)
+    v = torch.from_numpy(c["v"].ravel(order="F")).to(dev)
+    drv.itrbc(v)
+    drv.step(v, nsteps=3)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    total, per = time_steps(torch, drv, v, steps, stream)
+    pts = 128 * 128
+    out = {"workload": "impdrv-oseen-vortex-128x128-Ma0.5-Re1000-cfl1", "value": pts * steps / (total / 1e3),
+           "unit": "grid-pt-steps/s", "ms_per_step": total / steps, "dtype": "f64",
+           "latency_ms": {"p50": percentile(per, 0.5), "p99": percentile(per, 0.99)},
+           "launches_per_step": 12, "cpu_baseline": None}
+    if with_cpu:
+        from oracle.impdrv2d import Oracle2D
+        import oracle
+
+        o = Oracle2D(c, cflmax=1.0, loctime=0, lib=oracle.orc_omp())
+        vh = c["v"].copy(order="F")
+        o.itrbc(vh)
+        o.step(vh)
+        n = 10
+        t0 = time.perf_counter()
+        for _ in range(n):
+            o.step(vh)
+        t = (time.perf_counter() - t0) / n
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        out["cpu_baseline"] = {"value": pts / t, "unit": "grid-pt-steps/s", "cores": cores, "kind": "port",
+                               "sample": "%d steps of the 128x128 vortex case, %.1f ms/step; restatement of "
+                                         "impdrv + penta2p/penta1bc, -O3 -fopenmp" % (n, t * 1e3)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -405,6 +446,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-pointer end-to-end leg")
     ap.add_argument("--no-converge", action="store_true", help="skip the runs to a 1e-10 residual")
     ap.add_argument("--no-isolated", action="store_true", help="skip the isolated batched-solve leg")
+    ap.add_argument("--no-2d", action="store_true", help="skip the nonlinear 2D step leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -527,6 +569,10 @@ def main():
         del d32
         iso = run_isolated(torch, dev, L, sp, stream, rank, world, 3, max(3, min(K, 10)))
 
+    leg2d = None
+    if not args.no_2d:
+        leg2d = run_impdrv2d(torch, dev, max(10, K), rank == 0 and not args.no_cpu_baseline)
+
     hbm_peak, peak_kind = peaks()
     fp64_peak = L.lns_probe_fp64_tflops()
     dom = max(("xsweep", "ysweep"), key=lambda k: ph64[k])
@@ -552,6 +598,7 @@ def main():
                               "peak_source": "measured live: DFMA stream on every SM (lns_probe_fp64_tflops)"},
             "cpu_baseline": cpu,
             "isolated_solve": iso,
+            "impdrv2d": leg2d,
             "gpu_launches": KERNELS_PER_STEP * K,
             "clocks": clocks,
         }

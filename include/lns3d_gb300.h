@@ -147,6 +147,62 @@ int lns_penta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* 
 /* host-pointer form of cpenta2bc_mixed (factor + solve), staged internally */
 int lns_cpenta2bc_mixed(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine);
 
+/* ---------------------------------------------------------------------------
+ * The nonlinear two-dimensional implicit ADI step (src/impdrv.f90:171-400
+ * with linear = 0, impl = 1, iLHS = 1) as one device-resident context, FP64
+ * throughout.  Per step: set_time_step on the state, vold = v, itrBC; per
+ * corrector genmtrx(v, 0, r) (the nonlinear RHS and the operators), rbe,
+ * rhsBC, resstat, lhs1f + lhsbc1f and penta2p (xi), lhs2f + lhsbt2f +
+ * lhsbc2f and penta1bc (eta), v = v + r, itrBC.  The LHS is formed and
+ * factored every corrector, as the reference does for the nonlinear
+ * equations.
+ * Supported options: xper = 1, yper = 0, a viscous wall at j = 1 (navier 1,
+ * wall 0, 1 or 3, wallt 0 or 1) and the Riemann far field at j = ny (top 0;
+ * held free stream when Ma > 1); constant viscosity; no sponge, damper or
+ * smoother.  Arrays are Fortran-ordered: v(5,nx,ny), metrics(nx,ny,10),
+ * bnt(nx,2) (src/gengrid.f90:141-142), pot(5,nx) = the rho u v w T rows of
+ * top.pot (src/potential.f90:22-26).
+ */
+typedef struct {
+  int32_t nx, ny;
+  double dxi, deta;
+  double Ma, Re, Pr, gamma;
+  double alfa, cflmax, dtmax;
+  double theta;              /* isothermal-wall recovery angle (wallt 0, src/itrbc.f90:683-686) */
+  int32_t loctime, xper, yper, navier, wall, wallt, top, optx, opty;
+  int32_t res_compat;        /* as in lns_params3d (src/resstat.f90:17) */
+} lns_params2d;
+
+typedef struct lns_ctx2d lns_ctx2d;
+
+/* replaces the allocations of src/impdrv.f90:30-138 */
+int lns_ctx2d_create(const lns_params2d* params, lns_ctx2d** ctx);
+int lns_ctx2d_destroy(lns_ctx2d* ctx);
+size_t lns_ctx2d_bytes(const lns_ctx2d* ctx);
+/* metrics(nx,ny,10): m1 m2 n1 n2 m11 m12 m22 n11 n12 n22 (metric.dat) */
+int lns_upload_metrics2d(lns_ctx2d* ctx, const double* metrics);
+/* far field of the top boundary: unit normal bnt(nx,2) and top.pot (5,nx) */
+int lns_upload_top2d(lns_ctx2d* ctx, const double* bnt, const double* pot);
+/* itrBC on a device state (the call before the step loop, src/impdrv.f90:160) */
+int lns_itrbc2d_dev(lns_ctx2d* ctx, double* v, void* stream);
+/* nsteps steps on the host state v(5,nx,ny) in place; totres[nsteps] (may be
+ * NULL) gets resstat's value of the last corrector of each step */
+int lns_step2d(lns_ctx2d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres);
+int lns_step2d_dev(lns_ctx2d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream);
+/* Inspection (device arrays): set_time_step(v), then
+ * r = rhsBC(rbe(genmtrx(v, 0, r))) (src/genmtrx.f90, src/impdrv.f90:482,
+ * src/rhsbc.f90) with *totres_dev = resstat(r); the operators stay in the
+ * context for lns_lhs2d_dev and lns_get_field2d. */
+int lns_rhs2d_dev(lns_ctx2d* ctx, const double* v, const double* vold, double* r, double* totres_dev, void* stream);
+/* LHS of the xi (dir 1: src/lhsf.f90:7 + src/lhsbc1f.f90) or eta sweep
+ * (dir 2: src/lhsf.f90:164 + src/lhsbt2f.f90 + src/lhsbc2f.f90 with
+ * ReimannLHS, src/reimann.f90:238) from the context's operators, into the
+ * device array mat(5,5,5,nx,ny) */
+int lns_lhs2d_dev(lns_ctx2d* ctx, int32_t dir, const double* v, double* mat, void* stream);
+/* host copy of 0 Ah, 1 Bh, 2 Dh (5,5,nx,ny), 3 Vh11, 4 Vh12, 5 Vh22
+ * (6,nx,ny), 6 dtl (nx,ny) */
+int lns_get_field2d(lns_ctx2d* ctx, int32_t which, double* out);
+
 /* lns_cpenta2bc_mixed_dev with code 2 (factor + solve) that allocates no
  * device memory and takes no workspace.  No counterpart in the reference.
  * It is for callers that hold no device buffer to lend as scratch and must

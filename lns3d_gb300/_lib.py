@@ -65,7 +65,27 @@ SIGNATURES = {
     "lns_get_field3d": [P, I32, DP],
     "lns_ctx3d_profile": [P, I32],
     "lns_ctx3d_profile_read": [P, DP, P],
+    "lns_ctx2d_create": [P, P],
+    "lns_ctx2d_destroy": [P],
+    "lns_upload_metrics2d": [P, DP],
+    "lns_upload_top2d": [P, DP, DP],
+    "lns_itrbc2d_dev": [P, DP, P],
+    "lns_step2d": [P, DP, I32, I32, DP],
+    "lns_step2d_dev": [P, DP, I32, I32, DP, P],
+    "lns_rhs2d_dev": [P, DP, DP, DP, DP, P],
+    "lns_lhs2d_dev": [P, I32, DP, DP, P],
+    "lns_get_field2d": [P, I32, DP],
 }
+
+
+class Params2D(ctypes.Structure):
+    """lns_params2d of include/lns3d_gb300.h."""
+    _fields_ = [("nx", I32), ("ny", I32), ("dxi", ctypes.c_double), ("deta", ctypes.c_double),
+                ("Ma", ctypes.c_double), ("Re", ctypes.c_double), ("Pr", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double),
+                ("dtmax", ctypes.c_double), ("theta", ctypes.c_double), ("loctime", I32), ("xper", I32),
+                ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32), ("top", I32), ("optx", I32),
+                ("opty", I32), ("res_compat", I32)]
 
 
 class Params3D(ctypes.Structure):
@@ -95,6 +115,8 @@ def lib():
         L.lns_mixed_workspace_bytes.argtypes = [I32, I32, I32, I32]
         L.lns_ctx3d_bytes.restype = ctypes.c_size_t
         L.lns_ctx3d_bytes.argtypes = [P]
+        L.lns_ctx2d_bytes.restype = ctypes.c_size_t
+        L.lns_ctx2d_bytes.argtypes = [P]
         for name, args in SIGNATURES.items():
             fn = getattr(L, name)
             fn.argtypes = args

@@ -70,3 +70,82 @@ def shear_layer(nx=512, ny=256, Lx=5.5, Ly=10.0, stretch=3.0, delta=1.0, Ma=0.8,
                   gamma1=GAMMA - 1.0, omega=omega, kz=beta, alfa=1.0, xper=1, yper=0, navier=1, wall=1, wallt=1,
                   top=0, optx=-1, opty=-1)
     return dict(params=params, x=x, y=y, metrics=metrics, vm=vm, v=v)
+
+
+def _oseen_f(x):
+    """f(x) of the Oseen vortex pressure (util/mkvortex.f90:238-249):
+    1/2 - e^-x + e^-2x / 2 + x Ei(-2x) - x Ei(-x), and 1/2 beyond x = sqrt(200)."""
+    from scipy.special import expi
+
+    x = np.asarray(x, dtype=np.float64)
+    out = np.full_like(x, 0.5)
+    m = x <= np.sqrt(200.0)
+    xm = x[m]
+    out[m] = 0.5 - np.exp(-xm) + 0.5 * np.exp(-2.0 * xm) + xm * expi(-2.0 * xm) - xm * expi(-xm)
+    return out
+
+
+def vortex2d(nx=128, ny=128, L=10.0, stretch=2.0, Ma=0.5, Re=1000.0, Pr=0.72, circulation=1.0, seed=0,
+             jitter=0.1):
+    """The nonlinear two-dimensional case: an Oseen vortex in a uniform stream.
+
+    * grid: [-L, L]^2, x uniform and periodic (point nx repeats point 1), y
+      = L tanh(s (2 eta - 1)) / tanh(s); metrics exact for the mapping;
+    * state: uniform flow rho = u = T = 1 plus an Oseen vortex of core radius 1
+      (alpha = 1.2564312086261697, util/mkvortex.f90:36) with the given
+      circulation, its centre jittered uniformly by +-jitter from the origin
+      by seed; the vortex pressure follows radial equilibrium with the
+      isentropic relation (rho = (p/p_inf)^(1/gamma), T = p/(p_inf rho));
+    * far field: the top.pot values are the state's top row, as the
+      reference's vortex generator writes them (util/mkvortex.f90:183-188);
+    * deck: Ma 0.5, Re 1000, Pr 0.72, viscous no-slip adiabatic wall at j = 1
+      (wall 0, wallt 1), Riemann far field at j = ny (top 0), global time
+      step at CFL 1.
+    """
+    xi = np.linspace(0.0, 1.0, nx)
+    eta = np.linspace(0.0, 1.0, ny)
+    s = stretch
+    z = s * (2.0 * eta - 1.0)
+    y1 = L * np.tanh(z) / np.tanh(s)
+    dy = L * 2.0 * s / np.cosh(z) ** 2 / np.tanh(s)                      # dy/deta
+    d2y = -L * 8.0 * s * s * np.tanh(z) / np.cosh(z) ** 2 / np.tanh(s)  # d2y/deta2
+    x = np.asfortranarray(np.repeat((-L + 2.0 * L * xi)[:, None], ny, axis=1))
+    y = np.asfortranarray(np.repeat(y1[None, :], nx, axis=0))
+    ones = np.ones((nx, ny))
+    zeros = np.zeros((nx, ny))
+    metrics = {
+        "m1": ones / (2.0 * L), "m2": zeros.copy(), "n1": zeros.copy(),
+        "n2": np.repeat((1.0 / dy)[None, :], nx, axis=0),
+        "m11": zeros.copy(), "m12": zeros.copy(), "m22": zeros.copy(),
+        "n11": zeros.copy(), "n12": zeros.copy(),
+        "n22": np.repeat((-d2y / dy ** 3)[None, :], nx, axis=0),
+    }
+    metrics = {k: np.asfortranarray(v) for k, v in metrics.items()}
+    rng = np.random.default_rng(seed)
+    x0, y0 = rng.uniform(-jitter, jitter, 2)
+    alpha = 1.2564312086261697
+    xiv = 1.0 - np.exp(-alpha)
+    amp = circulation * xiv / (2.0 * np.pi)        # v_theta(r) -> circulation / (2 pi r) far away
+    gamma = GAMMA
+    fact = 1.0 / (gamma * Ma * Ma)
+    r = np.sqrt((x - x0) ** 2 + (y - y0) ** 2)
+    th = np.arctan2(y - y0, x - x0)
+    rs = np.where(r > 0.0, r, 1.0)
+    vth = np.where(r > 0.0, amp * (1.0 - np.exp(-alpha * rs ** 2)) / (rs * xiv), 0.0)
+    pr = np.where(r > 0.0, fact * (1.0 - (gamma - 1.0) * Ma ** 2 * amp ** 2 / (xiv * rs) ** 2
+                                   * _oseen_f(alpha * rs ** 2)) ** (gamma / (gamma - 1.0)), fact)
+    rho = (pr / fact) ** (1.0 / gamma)
+    t = pr / (fact * rho)
+    v = np.zeros((5, nx, ny), order="F")
+    v[0] = rho
+    v[1] = 1.0 - np.sin(th) * vth
+    v[2] = np.cos(th) * vth
+    v[4] = t
+    v[:, -1, :] = v[:, 0, :]        # periodic point
+    pot = np.asfortranarray(v[:, :, -1].copy())   # rho, u, v, w, T on the top row
+    params = dict(nx=nx, ny=ny, dxi=1.0 / (nx - 1), deta=1.0 / (ny - 1), Ma=Ma, Re=Re, Pr=Pr, gamma=GAMMA,
+                  gamma1=GAMMA - 1.0, omega=0.0, kz=0.0, alfa=1.0, xper=1, yper=0, navier=1, wall=0, wallt=1,
+                  top=0, optx=-1, opty=-1)
+    bnt = np.zeros((nx, 2), order="F")
+    bnt[:, 1] = 1.0        # (n1, n2) / |n| at j = ny (src/gengrid.f90:141-142)
+    return dict(params=params, x=x, y=y, metrics=metrics, v=np.asfortranarray(v), pot=pot, bnt=bnt, theta=0.0)

@@ -27,18 +27,6 @@
 namespace lns {
 namespace a3 {
 
-// Frozen operators on the device, structure-of-arrays: element (a,b)
-// (0-based) of a 5x5 operator at point p is at [(a + 5 b) * np + p], entry k
-// of a 6-vector at [k * np + p].
-struct Ops {
-  double *Ah, *Bh, *Dh, *Dhi, *V11, *V12, *V22, *AB, *dtl;
-  long long np;
-};
-
-struct Metrics {
-  const double *m1, *m2, *n1, *n2, *m11, *m12, *m22, *n11, *n12, *n22;
-};
-
 __device__ __forceinline__ double& opel(double* A, const Ops& o, int a, int b, long long p) {
   return A[(long long)(a + 5 * b) * o.np + p];
 }
@@ -252,52 +240,6 @@ __global__ void genmtrx_kernel(Grid g, const double* __restrict__ vm, Metrics mt
   o.AB[3 * np + p] = kzl * Vij[3] * n2;
   o.AB[4 * np + p] = 0.0;
   o.AB[5 * np + p] = 0.0;
-}
-
-// -------------------------------------------------------------- time step
-// src/temporal.f90:40-95: acoustic CFL per point; block maxima in part[]
-__global__ void cfl_kernel(Grid g, const double* __restrict__ vm, Metrics mt, double* dtl, double* part) {
-  __shared__ double red[256];
-  const long long np = (long long)g.nx * g.ny;
-  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  double c = -1.0;
-  if (p < np) {
-    const double m1 = mt.m1[p], m2 = mt.m2[p], n1 = mt.n1[p], n2 = mt.n2[p];
-    double volinv = 1.0 / (m1 * n2 - m2 * n1);
-    const double sxj = n2 * g.dxi * volinv, syj = -m2 * g.dxi * volinv;
-    const double sxi = -n1 * g.deta * volinv, syi = m1 * g.deta * volinv;
-    volinv = 1.0 / (g.dxi * g.deta * volinv);
-    const double acoustic =
-        sqrt(sxi * sxi + two * sxi * syi + syi * syi + sxj * sxj + two * sxj * syj + syj * syj) / g.Ma;
-    const double u1 = vm[1 + 5 * p], u2 = vm[2 + 5 * p], t = sqrt(vm[4 + 5 * p]);
-    c = (fabs(u1 * sxi + u2 * syi) + fabs(u1 * sxj + u2 * syj) + t * acoustic) * volinv;
-    dtl[p] = c;
-  }
-  red[threadIdx.x] = c;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
-}
-
-// maximum of the block maxima, then the local or global time step
-__global__ void dtl_kernel(long long np, int nparts, const double* part, double* dtl, double cflmax, double dtmax,
-                           int loctime, double* cfl_out) {
-  __shared__ double cfla;
-  if (threadIdx.x == 0) {
-    double m = -1.0;
-    for (int k = 0; k < nparts; ++k) m = fmax(m, part[k]);
-    cfla = m;
-  }
-  __syncthreads();
-  const double cfl = cfla;
-  const bool fixed = cfl * dtmax <= cflmax;
-  const double delt = fixed ? dtmax : cflmax / cfl;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < np; p += (long long)gridDim.x * blockDim.x)
-    dtl[p] = fixed ? dtmax : (loctime == 0 ? delt : cflmax / dtl[p]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) *cfl_out = cfl * delt;
 }
 
 // -------------------------------------------------------------------- LHS
@@ -539,38 +481,7 @@ __global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __res
   if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = red[0];
 }
 
-// totres = sqrt(sum / (nx ny)) in a fixed summation order; with acc the sum
-// starts from *acc and the result is stored back into it (the reference's
-// saved totres, src/resstat3d.f90:18)
-__global__ void resid_kernel(int nparts, const double* part, long long npts, double* out, double* acc) {
-  __shared__ double red[256];
-  double s = 0.0;
-  for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += part[k];
-  red[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const double tot = acc ? *acc + red[0] : red[0];
-    const double r = sqrt(tot / (double)npts);
-    *out = r;
-    if (acc) *acc = r;
-  }
-}
-
 // ----------------------------------------------------------------- update
-// v += r over every entry (src/impdrv3d.f90:339-347)
-template <typename RT>
-__global__ void add_kernel(long long n, cd* __restrict__ v, const RT* __restrict__ r) {
-  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  const cd d = to_hi(r[e]);
-  const cd x = v[e];
-  v[e] = cd{x.x + d.x, x.y + d.y};
-}
-
 // The boundary values of src/itrbc3d.f90:35-205: threads 0..ncol-1 own a
 // column i (wall row j = 1 from rows 2..5, top row j = ny); with a periodic
 // x direction the remaining threads copy the interior rows of column 1 to
@@ -850,7 +761,7 @@ template <typename RT>
 int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
   const Grid& g = c->g;
   const long long n = 5 * c->np;
-  if (add) lns::a3::add_kernel<RT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, r);
+  if (add) lns::a3::add_kernel<cd, RT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, r);
   const int nt = g.nx + g.ny;
   lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v);
   cudaError_t e = cudaGetLastError();

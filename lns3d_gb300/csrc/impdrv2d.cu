@@ -1,0 +1,890 @@
+// The nonlinear two-dimensional implicit ADI step on the GPU
+// (src/impdrv.f90:171-400 with linear = 0, impl = 1, iLHS = 1) and its C
+// ABI (lns_ctx2d_*, include/lns3d_gb300.h).
+//
+// Per step: set_time_step on the state (cfl_kernel, dtl_kernel), vold = v,
+// itrBC (bc2d_kernel); per corrector: the nonlinear RHS with rbe, rhsBC and
+// the residual partials and the operators of the LHS (rhs2d_kernel), the xi
+// LHS (lhs2d_kernel) and its periodic solve (penta2p), the eta LHS and its
+// boundary solve (penta1bc), v += r, itrBC.  Everything is FP64, as the
+// reference; the LHS is formed and factored every corrector, as the
+// reference does for the nonlinear equations.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/lns3d_gb300.h"
+#include "adi3d.cuh"
+#include "launch.cuh"
+
+namespace lns {
+namespace a2 {
+
+using a3::d1_at;
+using a3::d2_at;
+using a3::Grid;
+using a3::Metrics;
+using a3::Ops;
+using a3::pix;
+using namespace a3;  // stencil constants
+
+// Far field of the top boundary (src/gengrid.f90:141-142, src/potential.f90).
+struct Top {
+  const double* bnt;  // (nx,2)
+  const double* pot;  // (5,nx): rho, u, v, w, T of top.pot
+  double theta;       // wall recovery-temperature angle (wallt 0)
+};
+
+// ------------------------------------------------------- Riemann far field
+// src/reimann.f90:60-72: invariants of top-boundary node i from the node and
+// the two nodes below it.
+struct RmState {
+  double vn, vint[5], R1, R2, rho, p, vt;
+  bool inflow;
+};
+
+__device__ inline RmState rm_state(const Grid& g, const Top& tp, int i, const double* vb, const double* vb1,
+                                   const double* vb2) {
+  const double bn1 = tp.bnt[i - 1], bn2 = tp.bnt[g.nx + i - 1];
+  const double* pt = tp.pot + 5 * (i - 1);
+  RmState s;
+  s.vn = bn1 * vb[1] + bn2 * vb[2];
+  for (int k = 0; k < 5; ++k) s.vint[k] = two * vb1[k] - vb2[k];
+  const double cb = sqrt(pt[4]) / g.Ma;
+  s.R1 = bn1 * pt[1] + bn2 * pt[2] - two * cb / g.gamma1;
+  const double c = sqrt(s.vint[4]) / g.Ma;
+  s.R2 = bn1 * s.vint[1] + bn2 * s.vint[2] + two * c / g.gamma1;
+  s.inflow = s.vn <= 0.0;
+  if (s.inflow) {
+    s.rho = pt[0];
+    s.p = pt[0] * pt[4] / (g.gamma * (g.Ma * g.Ma));
+    s.vt = bn2 * pt[1] - bn1 * pt[2];
+  } else {
+    s.rho = s.vint[0];
+    s.p = s.vint[0] * s.vint[4] / (g.gamma * (g.Ma * g.Ma));
+    s.vt = bn2 * s.vint[1] - bn1 * s.vint[2];
+  }
+  return s;
+}
+
+// the boundary state the invariants give, src/reimann.f90:104-150
+__device__ inline void rm_values(const Grid& g, const Top& tp, int i, const RmState& s, double out[5]) {
+  const double bn1 = tp.bnt[i - 1], bn2 = tp.bnt[g.nx + i - 1];
+  const double gamma = g.gamma, gamma1 = g.gamma1;
+  const double vn = pt5 * (s.R1 + s.R2);
+  const double gq = gamma1 / four, dR = s.R2 - s.R1;
+  out[0] = pow(pow(s.rho, gamma) / (gamma * s.p) * (gq * gq) * (dR * dR), 1.0 / gamma1);
+  out[1] = (-(bn1 * vn) - bn2 * s.vt) / (-(bn1 * bn1) - bn2 * bn2);
+  out[2] = (-(bn2 * vn) + bn1 * s.vt) / (-(bn1 * bn1) - bn2 * bn2);
+  out[3] = s.inflow ? tp.pot[5 * (i - 1) + 3] : s.vint[3];
+  const double q = g.Ma * gamma1 / four * dR;
+  out[4] = q * q;
+}
+
+// Coefficient F(a,b) of ReimannLHS (src/reimann.f90:238-401): row ny holds
+// -I in slot 3, 2F in slot 2 and -F in slot 1.
+__device__ inline double rm_coef(const Grid& g, const Top& tp, int i, const RmState& s, int a, int b) {
+  const double bn1 = tp.bnt[i - 1], bn2 = tp.bnt[g.nx + i - 1];
+  const double gamma = g.gamma, gamma1 = g.gamma1, Ma = g.Ma;
+  const double dR = s.R2 - s.R1, gq = gamma1 / four, sq = sqrt(s.vint[4]);
+  const double bb = bn1 * bn1 + bn2 * bn2;
+  if (s.inflow) {
+    if (a == 1) {
+      const double f = pow(pow(s.rho, gamma) / (gamma * s.p) * (gq * gq), 1.0 / gamma1) * two / gamma1 *
+                       pow(dR, (two - gamma1) / gamma1);
+      return b == 2 ? f * bn1 : b == 3 ? f * bn2 : b == 5 ? f / (gamma1 * Ma * sq) : 0.0;
+    }
+    if (a == 2 || a == 3) {
+      const double f = pt5 * (a == 2 ? bn1 : bn2) / bb;
+      return b == 2 ? f * bn1 : b == 3 ? f * bn2 : b == 5 ? f / (gamma1 * Ma * sq) : 0.0;
+    }
+    if (a == 5) {
+      const double f = (Ma * gamma1 / four) * (Ma * gamma1 / four) * two * dR;
+      return b == 2 ? f * bn1 : b == 3 ? f * bn2 : b == 5 ? f / (gamma1 * Ma * sq) : 0.0;
+    }
+    return 0.0;
+  }
+  if (a == 1) {
+    const double rg = pow(s.rho, gamma) / (gamma * s.p);
+    const double f1 =
+        pow(rg, 1.0 / gamma1) * pow(gq, two / gamma1) * (two / gamma1) * pow(dR, (two - gamma1) / gamma1);
+    if (b == 2) return f1 * bn1 + gamma1 * pow(s.rho, gamma1) / s.p;
+    if (b == 3) return f1 * bn2;
+    if (b == 5) {
+      const double f2 = pow(gq * dR, two / gamma1) * 1.0 / (gamma * gamma1) * pow(rg, (two - gamma) / gamma1);
+      return f1 / (gamma1 * Ma * sq) - f2 * pow(s.rho, gamma + 1) / (gamma * (Ma * Ma) * (s.p * s.p));
+    }
+    return 0.0;
+  }
+  if (a == 2 || a == 3) {
+    const double f1 = pt5 * (a == 2 ? bn1 : bn2) / bb, f2 = (a == 2 ? bn2 : bn1) / bb;
+    if (b == 2) return a == 2 ? f1 * bn1 + f2 * bn2 : f1 * bn1 - f2 * bn2;
+    if (b == 3) return a == 2 ? f1 * bn2 - f2 * bn1 : f1 * bn2 + f2 * bn1;
+    if (b == 5) return f1 / (gamma1 * Ma * sq);
+    return 0.0;
+  }
+  if (a == 4) return b == 4 ? 1.0 : 0.0;  // outflow: 2 in slot 2, -1 in slot 1
+  const double f = (Ma * gamma1 / four) * (Ma * gamma1 / four) * two * dR;
+  return b == 2 ? f * bn1 : b == 3 ? f * bn2 : b == 5 ? f / (gamma1 * Ma * sq) : 0.0;
+}
+
+__device__ __forceinline__ double tw_wall(const Grid& g, double theta) {
+  const double tt = tan(theta);
+  return 1.0 + pt5 * g.gamma1 * (g.Ma * g.Ma) * (1.0 + tt * tt) * sqrt(g.Pr);
+}
+
+// -------------------------------------------------------------------- RHS
+// The nonlinear RHS and the operators (src/genmtrx.f90 with linear = 0,
+// general = true, mattyp = 0, kzl = 0), rbe (src/impdrv.f90:482-505), the
+// boundary rows (src/rhsbc.f90:256-370) and the block sums of resstat
+// (src/resstat.f90:37-50).  One thread per point; r may be null (operators
+// only, when vold is null too).
+__global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, Top tp, const double* __restrict__ v,
+                                                    const double* __restrict__ vold, double* __restrict__ r,
+                                                    double* part) {
+  __shared__ double red[128];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y + 1;
+  double resnod = 0.0;
+  if (i <= g.nx) {
+    const long long p = pix(g, i, j), np = o.np;
+    auto V = [&](int k, int ii, int jj) { return v[k + 5 * pix(g, ii, jj)]; };
+    double g1v[5], g2v[5], g11v[5], g12v[5], g22v[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      g1v[k] = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, j); });
+      g2v[k] = d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return V(k, i, jj); });
+      g11v[k] = d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return V(k, ii, j); });
+      g22v[k] = d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return V(k, i, jj); });
+      g12v[k] = d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) {
+        return d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, jj); });
+      });
+    }
+    if (g.navier && (g.wallt == 1 || g.wallt == 2) && j == 1) g2v[4] = 0.0;  // src/gradbc.f90:15
+    const double m1 = mt.m1[p], m2 = mt.m2[p], n1 = mt.n1[p], n2 = mt.n2[p];
+    const double m11 = mt.m11[p], m12 = mt.m12[p], m22 = mt.m22[p], n11 = mt.n11[p], n12 = mt.n12[p],
+                 n22 = mt.n22[p];
+    const double m1m1 = m1 * m1, m1m2 = m1 * m2, m2m2 = m2 * m2, n1n1 = n1 * n1, n1n2 = n1 * n2, n2n2 = n2 * n2;
+    const double m1n1 = m1 * n1, m1n2 = m1 * n2, m2n1 = m2 * n1, m2n2 = m2 * n2;
+    double g1vl[5], g2vl[5], g11vl[5], g12vl[5], g22vl[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {  // src/genmtrx.f90:116-136
+      g11vl[k] = g11v[k] * m1m1 + two * g12v[k] * m1n1 + g22v[k] * n1n1 + g1v[k] * m11 + g2v[k] * n11;
+      g12vl[k] = g11v[k] * m1m2 + g12v[k] * (m1n2 + m2n1) + g22v[k] * n1n2 + g1v[k] * m12 + g2v[k] * n12;
+      g22vl[k] = g11v[k] * m2m2 + two * g12v[k] * m2n2 + g22v[k] * n2n2 + g1v[k] * m22 + g2v[k] * n22;
+      g1vl[k] = g1v[k] * m1 + g2v[k] * n1;
+      g2vl[k] = g1v[k] * m2 + g2v[k] * n2;
+    }
+    const double gamma = g.gamma, gamma1 = g.gamma1, Ma2 = g.Ma * g.Ma, Re = g.Re, Pr = g.Pr;
+    const double fact = 1.0 / (gamma * Ma2);
+    double fact1 = 1.0 / Re, fact2 = gamma / (Pr * Re);
+    const double fact3 = gamma * gamma1 * Ma2 / Re;
+    const double rho = V(0, i, j), u1 = V(1, i, j), u2 = V(2, i, j), t = V(4, i, j);
+    const double rhoinv = 1.0 / rho;
+    const double grho[3] = {g1vl[0], g2vl[0], 0.0};
+    const double gu[3][3] = {{g1vl[1], g2vl[1], 0.0}, {g1vl[2], g2vl[2], 0.0}, {g1vl[3], g2vl[3], 0.0}};
+    const double gt[3] = {g1vl[4], g2vl[4], 0.0};
+    const double g1divu = g11vl[1] + g12vl[2], g2divu = g12vl[1] + g22vl[2], g3divu = 0.0;
+    const double S1jj = pt5 * (g11vl[1] + g11vl[1] + g22vl[1] + g12vl[2]);
+    const double S2jj = pt5 * (g11vl[2] + g12vl[1] + g22vl[2] + g22vl[2]);
+    const double S3jj = pt5 * (g11vl[3] + g22vl[3]);
+    const double Lapt = g11vl[4] + g22vl[4];
+    const double divu = gu[0][0] + gu[1][1] + gu[2][2];
+    const double gp[3] = {fact * (grho[0] * t + rho * gt[0]), fact * (grho[1] * t + rho * gt[1]),
+                          fact * (grho[2] * t + rho * gt[2])};
+    const double S[3][3] = {{gu[0][0], pt5 * (gu[0][1] + gu[1][0]), pt5 * gu[2][0]},
+                            {pt5 * (gu[1][0] + gu[0][1]), gu[1][1], pt5 * gu[2][1]},
+                            {pt5 * gu[2][0], pt5 * gu[2][1], 0.0}};
+    const double mu = 1.0, dmu = 0.0, d2mu = 0.0, con = mu, dcon = dmu, d2con = d2mu;
+    const double lm = -pt66 * mu, dlm = -pt66 * dmu, d2lm = -pt66 * d2mu;
+    const double g1mu = dmu * gt[0], g2mu = dmu * gt[1], g3mu = dmu * gt[2];
+    const double g1dmu = d2mu * gt[0], g2dmu = d2mu * gt[1], g3dmu = d2mu * gt[2];
+    const double g1con = dcon * gt[0], g2con = dcon * gt[1], g3con = dcon * gt[2];
+    const double g1dcon = d2con * gt[0], g2dcon = d2con * gt[1], g3dcon = d2con * gt[2];
+    const double g1lm = dlm * gt[0], g2lm = dlm * gt[1], g3lm = dlm * gt[2];
+    const double g1dlm = d2lm * gt[0], g2dlm = d2lm * gt[1], g3dlm = d2lm * gt[2];
+    double rr[5];
+    // nonlinear RHS, src/genmtrx.f90:282-312
+    rr[0] = rho * divu + grho[0] * u1 + grho[1] * u2;
+    rr[1] = u1 * gu[0][0] + u2 * gu[0][1] + rhoinv * gp[0] -
+            fact1 * (g1lm * divu + lm * g1divu + two * (g1mu * S[0][0] + g2mu * S[0][1] + mu * S1jj)) * rhoinv;
+    rr[2] = u1 * gu[1][0] + u2 * gu[1][1] + rhoinv * gp[1] -
+            fact1 * (g2lm * divu + lm * g2divu + two * (g1mu * S[1][0] + g2mu * S[1][1] + mu * S2jj)) * rhoinv;
+    rr[3] = u1 * gu[2][0] + u2 * gu[2][1] - fact1 * (two * (g1mu * S[2][0] + g2mu * S[2][1] + mu * S3jj)) * rhoinv;
+    {
+      const double s8 = S[0][0] * S[0][0] + S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][0] * S[1][0] +
+                        S[1][1] * S[1][1] + S[1][2] * S[1][2] + S[2][0] * S[2][0] + S[2][1] * S[2][1];
+      rr[4] = u1 * gt[0] + u2 * gt[1] + gamma1 * t * divu -
+              rhoinv * (fact2 * (g1con * gt[0] + g2con * gt[1] + con * Lapt) +
+                        fact3 * (lm * (divu * divu) + two * mu * s8));
+    }
+    double A[5][5] = {}, B[5][5] = {}, D[5][5] = {}, Vij[4];
+    const double gmsinv = 1.0 / (gamma * Ma2);
+    fact1 = rhoinv / Re;
+    // A, src/genmtrx.f90:458-503; B, :525-575
+    A[0][0] = u1; A[0][1] = rho;
+    A[1][0] = rhoinv * t * gmsinv;
+    A[1][1] = u1 - fact1 * g1lm - fact1 * two * g1mu;
+    A[1][2] = -(fact1 * g2mu);
+    A[1][3] = -(fact1 * g3mu);
+    A[1][4] = gmsinv - fact1 * dlm * divu - fact1 * dmu * two * S[0][0];
+    A[2][1] = -(fact1 * g2lm);
+    A[2][2] = u1 - fact1 * g1mu;
+    A[2][4] = -(fact1 * dmu * two * S[1][0]);
+    A[3][1] = -(fact1 * g3lm);
+    A[3][3] = u1 - fact1 * g1mu;
+    A[3][4] = -(fact1 * dmu * two * S[2][0]);
+    B[0][0] = u2; B[0][2] = rho;
+    B[1][1] = u2 - fact1 * g2mu;
+    B[1][2] = -(fact1 * g1lm);
+    B[1][4] = -(fact1 * dmu * two * S[0][1]);
+    B[2][0] = rhoinv * t * gmsinv;
+    B[2][1] = -(fact1 * g1mu);
+    B[2][2] = u2 - fact1 * g2lm - fact1 * two * g2mu;
+    B[2][3] = -(fact1 * g3mu);
+    B[2][4] = gmsinv - fact1 * dlm * divu - fact1 * dmu * two * S[1][1];
+    B[3][2] = -(fact1 * g3lm);
+    B[3][3] = u2 - fact1 * g2mu;
+    B[3][4] = -(fact1 * dmu * two * S[2][1]);
+    // D, src/genmtrx.f90:702-782 (linear = 0)
+    D[0][0] = divu; D[0][1] = grho[0]; D[0][2] = grho[1]; D[0][3] = grho[2];
+    D[1][0] = rhoinv * (gmsinv * gt[0] - rhoinv * gp[0] + fact1 * (g1lm * divu + lm * g1divu) +
+                        fact1 * two * (g1mu * S[0][0] + g2mu * S[0][1] + g3mu * S[0][2] + mu * S1jj));
+    D[1][1] = gu[0][0]; D[1][2] = gu[0][1]; D[1][3] = gu[0][2];
+    D[1][4] = rhoinv * gmsinv * grho[0] - fact1 * (g1dlm * divu + dlm * g1divu) -
+              fact1 * two * (g1dmu * S[0][0] + g2dmu * S[0][1] + g3dmu * S[0][2] + dmu * S1jj);
+    D[2][0] = rhoinv * (gmsinv * gt[1] - rhoinv * gp[1] + fact1 * (g2lm * divu + lm * g2divu) +
+                        fact1 * two * (g1mu * S[1][0] + g2mu * S[1][1] + g3mu * S[1][2] + mu * S2jj));
+    D[2][1] = gu[1][0]; D[2][2] = gu[1][1]; D[2][3] = gu[1][2];
+    D[2][4] = rhoinv * gmsinv * grho[1] - fact1 * (g2dlm * divu + dlm * g2divu) -
+              fact1 * two * (g1dmu * S[1][0] + g2dmu * S[1][1] + g3dmu * S[1][2] + dmu * S2jj);
+    D[3][0] = rhoinv * (gmsinv * gt[2] - rhoinv * gp[2] + fact1 * (g3lm * divu + lm * g3divu) +
+                        fact1 * two * (g1mu * S[2][0] + g2mu * S[2][1] + g3mu * S[2][2] + mu * S3jj));
+    D[3][1] = gu[2][0]; D[3][2] = gu[2][1]; D[3][3] = gu[2][2];
+    D[3][4] = rhoinv * gmsinv * grho[2] - fact1 * (g3dlm * divu + dlm * g3divu) -
+              fact1 * two * (g1dmu * S[2][0] + g2dmu * S[2][1] + g3dmu * S[2][2] + dmu * S3jj);
+    fact1 = gamma * rhoinv / (Pr * Re);
+    fact2 = gamma * gamma1 * Ma2 * rhoinv / Re;
+    A[4][1] = gamma1 * t - fact2 * two * lm * divu - four * fact2 * mu * S[0][0];
+    A[4][2] = -(four * fact2 * mu * S[1][0]);
+    A[4][3] = -(four * fact2 * mu * S[2][0]);
+    A[4][4] = u1 - fact1 * (g1con + dcon * gt[0]);
+    B[4][1] = -(four * fact2 * mu * S[0][1]);
+    B[4][2] = gamma1 * t - fact2 * two * lm * divu - four * fact2 * mu * S[1][1];
+    B[4][3] = -(four * fact2 * mu * S[2][1]);
+    B[4][4] = u2 - fact1 * (g2con + dcon * gt[1]);
+    {
+      const double ssq = S[0][0] * S[0][0] + S[0][1] * S[0][1] + S[0][2] * S[0][2] + S[1][0] * S[1][0] +
+                         S[1][1] * S[1][1] + S[1][2] * S[1][2] + S[2][0] * S[2][0] + S[2][1] * S[2][1] +
+                         S[2][2] * S[2][2];
+      D[4][0] = fact1 * rhoinv * (g1con * gt[0] + g2con * gt[1] + g3con * gt[2] + con * Lapt) +
+                fact2 * rhoinv * lm * (divu * divu) + two * fact2 * rhoinv * mu * ssq;
+      D[4][1] = gt[0]; D[4][2] = gt[1]; D[4][3] = gt[2];
+      D[4][4] = gamma1 * divu;
+      D[4][4] = D[4][4] - fact1 * (g1dcon * gt[0] + g2dcon * gt[1] + g3dcon * gt[2] + dcon * Lapt) -
+                fact2 * dlm * (divu * divu) - two * fact2 * dmu * ssq;
+    }
+    // Vij, src/genmtrx.f90:586-600
+    fact1 = 1.0 / Re;
+    fact2 = gamma / (Pr * Re);
+    Vij[0] = fact1 * rhoinv * (lm + two * mu);
+    Vij[1] = fact1 * rhoinv * mu;
+    Vij[2] = fact2 * rhoinv * con;
+    Vij[3] = fact1 * rhoinv * (lm + mu);
+    // \hat{A}, \hat{B}, src/genmtrx.f90:602-700
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+      double* H = pass == 0 ? o.Ah : o.Bh;
+      const double e1 = pass == 0 ? m1 : n1, e2 = pass == 0 ? m2 : n2;
+      const double e11 = pass == 0 ? m11 : n11, e12 = pass == 0 ? m12 : n12, e22 = pass == 0 ? m22 : n22;
+      double h[5][5];
+      h[0][0] = A[0][0] * e1 + B[0][0] * e2; h[0][1] = A[0][1] * e1; h[0][2] = B[0][2] * e2; h[0][3] = 0.0; h[0][4] = 0.0;
+      h[1][0] = A[1][0] * e1;
+      h[1][1] = A[1][1] * e1 + B[1][1] * e2 - Vij[0] * e11 - Vij[1] * e22;
+      h[1][2] = A[1][2] * e1 + B[1][2] * e2 - Vij[3] * e12;
+      h[1][3] = A[1][3] * e1;
+      h[1][4] = A[1][4] * e1 + B[1][4] * e2;
+      h[2][0] = B[2][0] * e2;
+      h[2][1] = A[2][1] * e1 + B[2][1] * e2 - Vij[3] * e12;
+      h[2][2] = A[2][2] * e1 + B[2][2] * e2 - Vij[1] * e11 - Vij[0] * e22;
+      h[2][3] = B[2][3] * e2;
+      h[2][4] = A[2][4] * e1 + B[2][4] * e2;
+      h[3][0] = 0.0;
+      h[3][1] = A[3][1] * e1;
+      h[3][2] = B[3][2] * e2;
+      h[3][3] = A[3][3] * e1 + B[3][3] * e2 - Vij[1] * e11 - Vij[1] * e22;
+      h[3][4] = A[3][4] * e1 + B[3][4] * e2;
+      for (int b = 0; b < 4; ++b) h[4][b] = A[4][b] * e1 + B[4][b] * e2;
+      h[4][4] = A[4][4] * e1 + B[4][4] * e2 - Vij[2] * e11 - Vij[2] * e22;
+      if (pass == 1 && !g.yper && g.wallt == 2 && j == 1)
+        for (int a = 0; a < 5; ++a) h[a][4] = 0.0;
+      for (int a = 0; a < 5; ++a)
+        for (int b = 0; b < 5; ++b) H[(long long)(a + 5 * b) * np + p] = h[a][b];
+    }
+    for (int a = 0; a < 5; ++a)
+      for (int b = 0; b < 5; ++b) o.Dh[(long long)(a + 5 * b) * np + p] = D[a][b];
+    o.V11[0 * np + p] = Vij[0] * m1m1 + Vij[1] * m2m2;
+    o.V11[1 * np + p] = Vij[1] * m1m1 + Vij[0] * m2m2;
+    o.V11[2 * np + p] = Vij[1] * m1m1 + Vij[1] * m2m2;
+    o.V11[3 * np + p] = Vij[2] * m1m1 + Vij[2] * m2m2;
+    o.V11[4 * np + p] = Vij[3] * m1m2;
+    o.V11[5 * np + p] = Vij[3] * m1m2;
+    o.V12[0 * np + p] = two * (Vij[0] * m1n1 + Vij[1] * m2n2);
+    o.V12[1 * np + p] = two * (Vij[1] * m1n1 + Vij[0] * m2n2);
+    o.V12[2 * np + p] = two * (Vij[1] * m1n1 + Vij[1] * m2n2);
+    o.V12[3 * np + p] = two * (Vij[2] * m1n1 + Vij[2] * m2n2);
+    o.V12[4 * np + p] = Vij[3] * (m1n2 + m2n1);
+    o.V12[5 * np + p] = Vij[3] * (m1n2 + m2n1);
+    o.V22[0 * np + p] = Vij[0] * n1n1 + Vij[1] * n2n2;
+    o.V22[1 * np + p] = Vij[1] * n1n1 + Vij[0] * n2n2;
+    o.V22[2 * np + p] = Vij[1] * n1n1 + Vij[1] * n2n2;
+    o.V22[3 * np + p] = Vij[2] * n1n1 + Vij[2] * n2n2;
+    o.V22[4 * np + p] = Vij[3] * n1n2;
+    o.V22[5 * np + p] = Vij[3] * n1n2;
+    if (r) {
+      // rbe
+      const double dtl = o.dtl[p];
+      for (int m = 0; m < 5; ++m) rr[m] = vold[m + 5 * p] - V(m, i, j) - dtl * rr[m];
+      // boundary rows, src/rhsbc.f90:258-362
+      if (!g.yper) {
+        if (g.navier && j == 1) {
+          for (int m = 1; m <= 3; ++m) rr[m] = 0.0;
+          if (g.wall == 1)
+            rr[0] = gc1 * V(0, i, 1) + gc2 * V(0, i, 2) + gc3 * V(0, i, 3) + gc4 * V(0, i, 4) + gc5 * V(0, i, 5);
+          if (g.wall == 3)
+            rr[0] = V(0, i, 1) - (4.0 * V(0, i, 2) - 6.0 * V(0, i, 3) + 4.0 * V(0, i, 4) - V(0, i, 5));
+          if (g.wallt == 0) rr[4] = V(4, i, 1) - tw_wall(g, tp.theta);
+          if (g.wallt == 1)
+            rr[4] = gc1 * V(4, i, 1) + gc2 * V(4, i, 2) + gc3 * V(4, i, 3) + gc4 * V(4, i, 4) + gc5 * V(4, i, 5);
+        }
+        if (j == g.ny) {
+          if (g.Ma > 1.0) {
+            for (int m = 0; m < 5; ++m) rr[m] = 0.0;
+          } else if (g.top == 0) {
+            const RmState s = rm_state(g, tp, i, v + 5 * pix(g, i, g.ny), v + 5 * pix(g, i, g.ny - 1),
+                                       v + 5 * pix(g, i, g.ny - 2));
+            double b[5];
+            rm_values(g, tp, i, s, b);
+            for (int m = 0; m < 5; ++m) rr[m] = V(m, i, j) - b[m];
+          }
+        }
+      } else if (j == g.ny) {
+        for (int m = 0; m < 5; ++m) rr[m] = 0.0;
+      }
+      if (g.xper && i == g.nx)
+        for (int m = 0; m < 5; ++m) rr[m] = 0.0;
+      for (int m = 0; m < 5; ++m) r[m + 5 * p] = rr[m];
+      resnod = (rr[0] * rr[0] + rr[1] * rr[1] + rr[2] * rr[2] + rr[3] * rr[3] + rr[4] * rr[4]) / (dtl * dtl);
+    }
+  }
+  if (!part) return;
+  red[threadIdx.x] = resnod;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = red[0];
+}
+
+// -------------------------------------------------------------------- LHS
+// Entry (k, a, b) of the LHS of point (i, j): lhs1f / lhs2f
+// (src/lhsf.f90:42-110, 198-247), the eta boundary rows (src/lhsbt2f.f90)
+// and the boundary conditions (src/lhsbc1f.f90:232-605,
+// src/lhsbc2f.f90:195-291).  One thread per entry.
+__global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v, int dir, double* __restrict__ mat) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= 125 * o.np) return;
+  const long long p = q / 125;
+  const int e = (int)(q - 125 * p);
+  const int k = e % 5 + 1, a = (e / 5) % 5 + 1, b = e / 25 + 1;
+  const int i = (int)(p % g.nx) + 1, j = (int)(p / g.nx) + 1;
+  const double ident = (k == 3 && a == b) ? 1.0 : 0.0;
+  const long long np = o.np;
+  const double d = o.dtl[p], alfa = g.alfa;
+  // boundary conditions of the wall row j = 1
+  if (!g.yper && g.navier && j == 1) {
+    if (dir == 1) {
+      if (a >= 2 && a <= 4) { mat[q] = ident; return; }
+      if (a == 1 && g.wall >= 1 && g.wall <= 3) { mat[q] = ident; return; }
+      if (a == 5 && (g.wallt == 0 || g.wallt == 1)) { mat[q] = ident; return; }
+    } else {
+      const int tk = (k + 2) % 5;  // coefficient of slot k: slots 3,4,5,1,2 <-> 0..4
+      const double gcs[5] = {gc1, gc2, gc3, gc4, gc5}, ex3[5] = {-1.0, 4.0, -6.0, 4.0, -1.0};
+      if (a >= 2 && a <= 4) { mat[q] = ident; return; }
+      if (a == 1 && (g.wall == 1 || g.wall == 3)) {
+        mat[q] = b == 1 ? (g.wall == 1 ? -gcs[tk] : ex3[tk]) : 0.0;
+        return;
+      }
+      if (a == 5 && g.wallt == 0) { mat[q] = -ident; return; }
+      if (a == 5 && g.wallt == 1) { mat[q] = b == 5 ? -gcs[tk] : 0.0; return; }
+    }
+  }
+  // the far-field row j = ny
+  if (!g.yper && j == g.ny) {
+    if (dir == 1 && g.top == 0) { mat[q] = ident; return; }
+    if (dir == 2 && g.Ma < 1.0 && g.top == 0) {
+      const RmState s = rm_state(g, tp, i, v + 5 * pix(g, i, g.ny), v + 5 * pix(g, i, g.ny - 1),
+                                 v + 5 * pix(g, i, g.ny - 2));
+      double val = 0.0;
+      if (k == 3) val = a == b ? -1.0 : 0.0;
+      else if (k == 2) val = two * rm_coef(g, tp, i, s, a, b);
+      else if (k == 1) val = -rm_coef(g, tp, i, s, a, b);
+      if (a == 4 && s.inflow && k != 3) val = 0.0;
+      mat[q] = val;
+      return;
+    }
+  }
+  const long long eab = (long long)((a - 1) + 5 * (b - 1)) * np + p;
+  const double* V = dir == 1 ? o.V11 : o.V22;
+  int vk = -1;
+  if (a == 2 && b == 2) vk = 0;
+  else if (a == 2 && b == 3) vk = 4;
+  else if (a == 3 && b == 2) vk = 5;
+  else if (a == 3 && b == 3) vk = 1;
+  else if (a == 4 && b == 4) vk = 2;
+  else if (a == 5 && b == 5) vk = 3;
+  double val;
+  const bool edge = dir == 2 && !g.yper && (j <= 2 || j >= g.ny - 1);
+  if (!edge) {
+    const double h = dir == 1 ? g.dxi : g.deta;
+    const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
+    const double ak = alfa * gi[k - 1] / h, bk = alfa * di[k - 1] / (h * h);
+    val = ak * d * (dir == 1 ? o.Ah : o.Bh)[eab];
+    if (dir == 1 && k == 3) val = val + alfa * d * o.Dh[eab];
+    if (vk >= 0) val = val - bk * d * V[vk * np + p];
+  } else {
+    // rows 1, 2, ny-1, ny: coefficient t of slot k (src/lhsbt2f.f90)
+    const double detainv = 1.0 / g.deta, detasinv = 1.0 / (g.deta * g.deta);
+    const double g1[5] = {gc1, gc2, gc3, gc4, gc5}, d1[5] = {dd1, dd2, dd3, dd4, dd5};
+    const double g2[5] = {gb1, gb2, gb3, gb4, gb5}, d2[5] = {db1, db2, db3, db4, db5};
+    double gcf, dcf;
+    bool neg = false;
+    if (j == 1) { const int t = (k + 2) % 5; gcf = g1[t]; dcf = d1[t]; }
+    else if (j == 2) { const int t = (k + 3) % 5; gcf = g2[t]; dcf = d2[t]; }
+    else if (j == g.ny - 1) { const int t = k == 5 ? 4 : 4 - k; gcf = g2[t]; dcf = d2[t]; neg = true; }
+    else { const int t = k <= 3 ? 3 - k : 8 - k; gcf = g1[t]; dcf = d1[t]; neg = true; }
+    val = alfa * d * gcf * detainv * o.Bh[eab];
+    if (neg) val = -val;
+    if (vk >= 0) val = val - alfa * d * dcf * detasinv * V[vk * np + p];
+  }
+  val = val + ident;
+  mat[q] = val;
+}
+
+// ----------------------------------------------------------------- update
+// The boundary values of src/itrbc.f90:629-760 (nonlinear branch): threads
+// 0..ncol-1 own a column (wall row from rows 2..5, far-field row from rows
+// ny-1, ny-2); with a periodic x direction the remaining threads copy the
+// interior rows of column 1 to column nx, and the thread of column 1 copies
+// its boundary rows.
+__global__ void bc2d_kernel(Grid g, Top tp, double* __restrict__ v) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncol = g.xper ? g.nx - 1 : g.nx;
+  if (t < ncol) {
+    const int i = t + 1;
+    auto W = [&](int k, int jj) -> double& { return v[k + 5 * pix(g, i, jj)]; };
+    if (g.yper) {
+      for (int m = 0; m < 5; ++m) W(m, g.ny) = W(m, 1);
+    } else {
+      if (g.navier) {
+        for (int m = 1; m <= 3; ++m) W(m, 1) = 0.0;
+        if (g.wall == 1) W(0, 1) = -(gc2 * W(0, 2) + gc3 * W(0, 3) + gc4 * W(0, 4) + gc5 * W(0, 5)) / gc1;
+        if (g.wall == 3) W(0, 1) = 4.0 * W(0, 2) - 6.0 * W(0, 3) + 4.0 * W(0, 4) - W(0, 5);
+        if (g.wallt == 0) W(4, 1) = tw_wall(g, tp.theta);
+        if (g.wallt == 1) W(4, 1) = -(gc2 * W(4, 2) + gc3 * W(4, 3) + gc4 * W(4, 4) + gc5 * W(4, 5)) / gc1;
+      }
+      if (g.Ma > 1.0) {
+        W(0, g.ny) = 1.0; W(1, g.ny) = 1.0; W(2, g.ny) = 0.0; W(3, g.ny) = 0.0; W(4, g.ny) = 1.0;
+      } else if (g.top == 0) {
+        const RmState s = rm_state(g, tp, i, &W(0, g.ny), &W(0, g.ny - 1), &W(0, g.ny - 2));
+        double b[5];
+        rm_values(g, tp, i, s, b);
+        for (int m = 0; m < 5; ++m) W(m, g.ny) = b[m];
+      }
+    }
+    if (g.xper && i == 1)
+      for (int m = 0; m < 5; ++m) {
+        v[m + 5 * pix(g, g.nx, 1)] = W(m, 1);
+        v[m + 5 * pix(g, g.nx, g.ny)] = W(m, g.ny);
+      }
+  } else if (g.xper) {
+    const int j = t - ncol + 2;
+    if (j <= g.ny - 1)
+      for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, g.nx, j)] = v[m + 5 * pix(g, 1, j)];
+  }
+}
+
+}  // namespace a2
+}  // namespace lns
+
+// ======================================================================
+// Context and C ABI
+// ======================================================================
+using lns::a3::Grid;
+using lns::a3::Metrics;
+using lns::a3::Ops;
+
+struct lns_ctx2d {
+  lns_params2d prm;
+  Grid g;
+  int device = -1;
+  long long np = 0;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+  double* metrics = nullptr;  // (nx,ny,10)
+  double* opbuf = nullptr;    // Ah Bh Dh (25 np each), V11 V12 V22 (6 np each), dtl (np)
+  Ops ops{};
+  double *bnt = nullptr, *pot = nullptr;  // far field of the top boundary
+  double *v = nullptr, *vold = nullptr, *r = nullptr, *mat = nullptr, *per = nullptr, *per2 = nullptr;
+  double* part = nullptr;
+  int nparts = 0;
+  double* dscal = nullptr;  // [0] cfl, [1] scratch residual, [2] running residual
+  double* res_dev = nullptr;
+  int res_cap = 0;
+  int* status = nullptr;
+  bool have_metrics = false, have_top = false;
+};
+
+namespace {
+
+int fail2(int code, const std::string& msg) { return lns_fail(code, msg); }
+int cuda2(cudaError_t e, const char* where) { return lns_cuda_fail(e, where); }
+
+// interior stencil coefficients, src/grad.f90 and src/grad2.f90 (as cgrad)
+void coef1(int opt, double dinv, double g[6]) {
+  double c, a, b;
+  if (opt == 0) c = 1.0 / 60.0;
+  else if (opt == -1) c = 0.0;
+  else {
+    const double w = 2.0 * 3.1415926535897932385e+0 / 12.0;
+    c = (w / 2.0 - 2.0 * sin(w) / 3.0 + sin(2.0 * w) / 12.0) / (5.0 * sin(w) - 4.0 * sin(2.0 * w) + sin(3.0 * w));
+  }
+  a = (2.0 + 15.0 * c) / 3.0;
+  b = -(1.0 + 48.0 * c) / 12.0;
+  g[0] = -c * dinv; g[1] = -b * dinv; g[2] = -a * dinv;
+  g[3] = a * dinv;  g[4] = b * dinv;  g[5] = c * dinv;
+}
+void coef2(int opt, double dsinv, double d[7]) {
+  double c, a, b;
+  if (opt == 0) c = 1.0 / 90.0;
+  else if (opt == -1) c = 0.0;
+  else {
+    const double w = 2.0 * 3.1415926535897932385e+0 / 12.0;
+    const double s1 = sin(w / 2.0), s2 = sin(w), s3 = sin(3.0 * w / 2.0);
+    c = -(3.0 * (w * w) - 16.0 * (s1 * s1) + (s2 * s2)) / (12.0 * (-15.0 * (s1 * s1) + 6.0 * (s2 * s2) - (s3 * s3)));
+  }
+  a = (4.0 + 45.0 * c) / 3.0;
+  b = -(1.0 + 72.0 * c) / 12.0;
+  d[0] = c * dsinv; d[1] = b * dsinv; d[2] = a * dsinv; d[3] = -2.0 * (a + b + c) * dsinv;
+  d[4] = a * dsinv; d[5] = b * dsinv; d[6] = c * dsinv;
+}
+
+int dalloc2(lns_ctx2d* c, size_t bytes, void** out) {
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return fail2(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  c->allocs.push_back(*out);
+  c->bytes += bytes;
+  return LNS_OK;
+}
+
+void free2(lns_ctx2d* c) {
+  for (void* p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+}
+
+int check_dev2(const lns_ctx2d* c) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda2(e, "cudaGetDevice");
+  if (dev != c->device) return fail2(LNS_ERR_ARG, "context belongs to another device");
+  return LNS_OK;
+}
+
+Metrics metrics2(const lns_ctx2d* c) {
+  const double* m = c->metrics;
+  const long long np = c->np;
+  return Metrics{m, m + np, m + 2 * np, m + 3 * np, m + 4 * np, m + 5 * np, m + 6 * np, m + 7 * np, m + 8 * np,
+                 m + 9 * np};
+}
+
+lns::a2::Top top2(const lns_ctx2d* c) { return lns::a2::Top{c->bnt, c->pot, c->prm.theta}; }
+
+dim3 pgrid(const Grid& g) { return dim3((g.nx + 127) / 128, g.ny); }
+
+// set_time_step on the state v (src/temporal.f90:12-162)
+int time_step(lns_ctx2d* c, const double* v, cudaStream_t st) {
+  const int nb = (int)((c->np + 255) / 256);
+  const Metrics mt = metrics2(c);
+  lns::a3::cfl_kernel<<<nb, 256, 0, st>>>(c->g, v, mt, c->ops.dtl, c->part);
+  lns::a3::dtl_kernel<<<152, 256, 0, st>>>(c->np, nb, c->part, c->ops.dtl, c->prm.cflmax, c->prm.dtmax,
+                                           c->prm.loctime, c->dscal);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda2(e, "time-step kernels launch");
+}
+
+int rhs2(lns_ctx2d* c, const double* v, const double* vold, double* r, double* res, double* acc, cudaStream_t st) {
+  const Grid& g = c->g;
+  lns::a2::rhs2d_kernel<<<pgrid(g), 128, 0, st>>>(g, c->ops, metrics2(c), top2(c), v, vold, r, c->part);
+  const int nrhs = (int)(pgrid(g).x * pgrid(g).y);
+  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res, acc);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda2(e, "rhs kernels launch");
+}
+
+int lhs2(lns_ctx2d* c, const double* v, int dir, double* mat, cudaStream_t st) {
+  const long long nq = 125 * c->np;
+  lns::a2::lhs2d_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->g, c->ops, top2(c), v, dir, mat);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda2(e, "lhs2d_kernel launch");
+}
+
+int bc2(lns_ctx2d* c, double* v, cudaStream_t st) {
+  const int nt = c->g.nx + c->g.ny;
+  lns::a2::bc2d_kernel<<<(nt + 127) / 128, 128, 0, st>>>(c->g, top2(c), v);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda2(e, "bc2d_kernel launch");
+}
+
+// nsteps steps of niter correctors (src/impdrv.f90:171-400)
+int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cudaStream_t st) {
+  const Grid& g = c->g;
+  const size_t vbytes = sizeof(double) * 5 * (size_t)c->np;
+  double* acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
+  cudaError_t e = cudaMemsetAsync(c->status, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda2(e, "cudaMemsetAsync");
+  int rc = LNS_OK;
+  for (int s = 0; s < nsteps && !rc; ++s) {
+    rc = time_step(c, v, st);
+    if (!rc) {
+      e = cudaMemcpyAsync(c->vold, v, vbytes, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) rc = cuda2(e, "cudaMemcpyAsync vold");
+    }
+    if (!rc) rc = bc2(c, v, st);
+    for (int it = 0; it < niter && !rc; ++it) {
+      double* res = (it == niter - 1 && totres_dev) ? totres_dev + s : c->dscal + 1;
+      rc = rhs2(c, v, c->vold, c->r, res, acc, st);
+      if (!rc) rc = lhs2(c, v, 1, c->mat, st);
+      if (!rc) rc = lns::host::launch_p<double>(c->mat, c->r, c->per, c->per2, g.nx, g.ny, 1, g.nx, 2, st, c->status);
+      if (!rc) rc = lhs2(c, v, 2, c->mat, st);
+      if (!rc) rc = lns::host::launch_bc<double>(c->mat, c->r, g.ny, g.nx, g.nx, 1, 2, st, c->status);
+      if (!rc) {
+        const long long n = 5 * c->np;
+        lns::a3::add_kernel<double, double><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, c->r);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda2(e, "add_kernel launch");
+      }
+      if (!rc) rc = bc2(c, v, st);
+    }
+  }
+  return rc;
+}
+
+int check_pivots2(lns_ctx2d* c, cudaStream_t st) {
+  int status = 0;
+  cudaError_t e = cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda2(e, "2D step");
+  if (status) return fail2(LNS_ERR_PIVOT, "zero or non-finite pivot in an LHS factorisation");
+  return LNS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
+  if (!p || !out) return fail2(LNS_ERR_ARG, "ctx2d_create: null argument");
+  *out = nullptr;
+  if (p->nx < 8 || p->ny < 7) return fail2(LNS_ERR_ARG, "ctx2d_create: need nx >= 8 and ny >= 7");
+  if ((long long)p->nx * p->ny > (1LL << 31) / 125)
+    return fail2(LNS_ERR_ARG, "ctx2d_create: nx*ny too large for 32-bit launch indexing");
+  if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail2(LNS_ERR_ARG, "ctx2d_create: dxi and deta must be > 0");
+  if (p->xper != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: only a periodic xi direction (xper = 1) is supported");
+  if (p->yper != 0 || p->navier != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: need yper = 0 and navier = 1");
+  if (p->wall != 0 && p->wall != 1 && p->wall != 3) return fail2(LNS_ERR_ARG, "ctx2d_create: wall must be 0, 1 or 3");
+  if (p->wallt != 0 && p->wallt != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: wallt must be 0 or 1");
+  if (p->top != 0) return fail2(LNS_ERR_ARG, "ctx2d_create: top must be 0");
+  if (!(p->Ma > 0.0) || p->Ma == 1.0) return fail2(LNS_ERR_ARG, "ctx2d_create: need Ma > 0 and Ma != 1");
+  if (p->loctime != 0 && p->loctime != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: loctime must be 0 or 1");
+  if (p->res_compat != 0 && p->res_compat != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: res_compat must be 0 or 1");
+  lns_ctx2d* c = new lns_ctx2d();
+  c->prm = *p;
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda2(e, "cudaGetDevice");
+  }
+  Grid& g = c->g;
+  g.nx = p->nx; g.ny = p->ny; g.dxi = p->dxi; g.deta = p->deta;
+  g.Ma = p->Ma; g.Re = p->Re; g.Pr = p->Pr; g.gamma = p->gamma; g.gamma1 = p->gamma - 1.0;
+  g.omega = 0.0; g.kz = 0.0; g.alfa = p->alfa;
+  g.xper = p->xper; g.yper = p->yper; g.navier = p->navier; g.wall = p->wall; g.wallt = p->wallt; g.top = p->top;
+  g.dxinv = 1.0 / p->dxi; g.dyinv = 1.0 / p->deta;
+  g.dxsinv = 1.0 / (p->dxi * p->dxi); g.dysinv = 1.0 / (p->deta * p->deta);
+  coef1(p->optx, g.dxinv, g.gx);
+  coef1(p->opty, g.dyinv, g.gy);
+  coef2(p->optx, g.dxsinv, g.dx2);
+  coef2(p->opty, g.dysinv, g.dy2);
+  const long long np = (long long)p->nx * p->ny;
+  c->np = np;
+  c->nparts = std::max(((p->nx + 127) / 128) * p->ny, (int)((np + 255) / 256));
+  void* q = nullptr;
+  int rc = LNS_OK;
+  auto A = [&](size_t bytes, void** dst) {
+    if (!rc) rc = dalloc2(c, bytes, dst);
+  };
+  A(sizeof(double) * 10 * np, &q); c->metrics = (double*)q;
+  A(sizeof(double) * (3 * 25 + 3 * 6 + 1) * np, &q); c->opbuf = (double*)q;
+  A(sizeof(double) * 2 * p->nx, &q); c->bnt = (double*)q;
+  A(sizeof(double) * 5 * p->nx, &q); c->pot = (double*)q;
+  A(sizeof(double) * 5 * np, &q); c->v = (double*)q;
+  A(sizeof(double) * 5 * np, &q); c->vold = (double*)q;
+  A(sizeof(double) * 5 * np, &q); c->r = (double*)q;
+  A(sizeof(double) * 125 * np, &q); c->mat = (double*)q;
+  A(sizeof(double) * 50 * np, &q); c->per = (double*)q;
+  A(sizeof(double) * 150 * p->ny, &q); c->per2 = (double*)q;
+  A(sizeof(double) * c->nparts, &q); c->part = (double*)q;
+  A(sizeof(double) * 3, &q); c->dscal = (double*)q;
+  A(sizeof(int), &q); c->status = (int*)q;
+  A(sizeof(double) * 64, &q); c->res_dev = (double*)q;
+  if (!rc) {
+    c->res_cap = 64;
+    e = cudaMemset(c->dscal, 0, sizeof(double) * 3);
+    if (e != cudaSuccess) rc = cuda2(e, "cudaMemset");
+  }
+  if (rc) {
+    free2(c);
+    delete c;
+    return rc;
+  }
+  double* o = c->opbuf;
+  c->ops.np = np;
+  c->ops.Ah = o; c->ops.Bh = o + 25 * np; c->ops.Dh = o + 50 * np;
+  c->ops.Dhi = nullptr;
+  c->ops.V11 = o + 75 * np; c->ops.V12 = o + 81 * np; c->ops.V22 = o + 87 * np;
+  c->ops.AB = nullptr;
+  c->ops.dtl = o + 93 * np;
+  *out = c;
+  return LNS_OK;
+}
+
+int lns_ctx2d_destroy(lns_ctx2d* c) {
+  if (!c) return LNS_OK;
+  free2(c);
+  delete c;
+  return LNS_OK;
+}
+
+size_t lns_ctx2d_bytes(const lns_ctx2d* c) { return c ? c->bytes : 0; }
+
+int lns_upload_metrics2d(lns_ctx2d* c, const double* metrics) {
+  if (!c || !metrics) return fail2(LNS_ERR_ARG, "upload_metrics2d: null argument");
+  int rc = check_dev2(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->metrics, metrics, sizeof(double) * 10 * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda2(e, "upload metrics");
+  c->have_metrics = true;
+  return LNS_OK;
+}
+
+int lns_upload_top2d(lns_ctx2d* c, const double* bnt, const double* pot) {
+  if (!c || !bnt || !pot) return fail2(LNS_ERR_ARG, "upload_top2d: null argument");
+  int rc = check_dev2(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->bnt, bnt, sizeof(double) * 2 * c->g.nx, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c->pot, pot, sizeof(double) * 5 * c->g.nx, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda2(e, "upload far field");
+  c->have_top = true;
+  return LNS_OK;
+}
+
+static int ready2(lns_ctx2d* c, const char* who) {
+  if (!c->have_metrics || !c->have_top)
+    return fail2(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the far field first");
+  return check_dev2(c);
+}
+
+int lns_itrbc2d_dev(lns_ctx2d* c, double* v, void* stream) {
+  if (!c || !v) return fail2(LNS_ERR_ARG, "itrbc2d: null argument");
+  int rc = ready2(c, "itrbc2d");
+  if (rc) return rc;
+  return bc2(c, v, (cudaStream_t)stream);
+}
+
+int lns_step2d_dev(lns_ctx2d* c, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream) {
+  if (!c || !v) return fail2(LNS_ERR_ARG, "step2d: null argument");
+  if (nsteps < 0 || niter < 1) return fail2(LNS_ERR_ARG, "step2d: need nsteps >= 0 and niter >= 1");
+  int rc = ready2(c, "step2d");
+  if (rc) return rc;
+  return run2(c, v, nsteps, niter, totres_dev, (cudaStream_t)stream);
+}
+
+int lns_step2d(lns_ctx2d* c, double* v, int32_t nsteps, int32_t niter, double* totres) {
+  if (!c || !v) return fail2(LNS_ERR_ARG, "step2d: null argument");
+  if (nsteps < 0 || niter < 1) return fail2(LNS_ERR_ARG, "step2d: need nsteps >= 0 and niter >= 1");
+  int rc = ready2(c, "step2d");
+  if (rc) return rc;
+  if (totres && nsteps > c->res_cap) {
+    void* q = nullptr;
+    rc = dalloc2(c, sizeof(double) * nsteps, &q);
+    if (rc) return rc;
+    c->res_dev = (double*)q;
+    c->res_cap = nsteps;
+  }
+  const size_t vbytes = sizeof(double) * 5 * (size_t)c->np;
+  cudaError_t e = cudaMemcpy(c->v, v, vbytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda2(e, "upload v");
+  rc = run2(c, c->v, nsteps, niter, totres ? c->res_dev : nullptr, 0);
+  if (!rc) rc = check_pivots2(c, 0);
+  if (rc) return rc;
+  e = cudaMemcpy(v, c->v, vbytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda2(e, "download v");
+  if (totres && nsteps > 0) {
+    e = cudaMemcpy(totres, c->res_dev, sizeof(double) * nsteps, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda2(e, "download totres");
+  }
+  return LNS_OK;
+}
+
+int lns_rhs2d_dev(lns_ctx2d* c, const double* v, const double* vold, double* r, double* totres_dev, void* stream) {
+  if (!c || !v || !vold || !r) return fail2(LNS_ERR_ARG, "rhs2d: null argument");
+  int rc = ready2(c, "rhs2d");
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = time_step(c, v, st);
+  if (!rc) rc = rhs2(c, v, vold, r, totres_dev ? totres_dev : c->dscal + 1, nullptr, st);
+  return rc;
+}
+
+int lns_lhs2d_dev(lns_ctx2d* c, int32_t dir, const double* v, double* mat, void* stream) {
+  if (!c || !v || !mat) return fail2(LNS_ERR_ARG, "lhs2d: null argument");
+  if (dir != 1 && dir != 2) return fail2(LNS_ERR_ARG, "lhs2d: dir must be 1 or 2");
+  int rc = ready2(c, "lhs2d");
+  if (rc) return rc;
+  return lhs2(c, v, dir, mat, (cudaStream_t)stream);
+}
+
+int lns_get_field2d(lns_ctx2d* c, int32_t which, double* out) {
+  if (!c || !out) return fail2(LNS_ERR_ARG, "get_field2d: null argument");
+  if (which < 0 || which > 6) return fail2(LNS_ERR_ARG, "get_field2d: which must be 0..6");
+  int rc = check_dev2(c);
+  if (rc) return rc;
+  const long long np = c->np;
+  const double* src[7] = {c->ops.Ah, c->ops.Bh, c->ops.Dh, c->ops.V11, c->ops.V12, c->ops.V22, c->ops.dtl};
+  const int nel = which < 3 ? 25 : (which < 6 ? 6 : 1);
+  std::vector<double> h((size_t)nel * np);
+  cudaError_t e = cudaMemcpy(h.data(), src[which], sizeof(double) * h.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda2(e, "get_field2d copy");
+  for (long long p = 0; p < np; ++p)
+    for (int k = 0; k < nel; ++k) out[k + (long long)nel * p] = h[(size_t)k * np + p];
+  return LNS_OK;
+}
+
+}  // extern "C"

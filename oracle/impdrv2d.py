@@ -1,0 +1,95 @@
+"""ctypes harness of the nonlinear 2D step oracle (oracle/impdrv2d_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/ as the checker and by bench.py's
+CPU-baseline leg (with the OpenMP build, liborc_omp.so)."""
+import ctypes
+
+import numpy as np
+
+from . import orc
+from .adi3d import A3Grid, A3Ops, _lib as _lib3
+
+D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+
+
+class A2Grid(ctypes.Structure):
+    _fields_ = [("g", A3Grid), ("theta", D), ("bnt", P), ("rhobt", P), ("ubt", P), ("vbt", P), ("wbt", P),
+                ("tbt", P)]
+
+
+def _lib(L=None):
+    L = _lib3(L if L is not None else orc())
+    if not hasattr(L, "_a2_setup"):
+        G = ctypes.POINTER(A2Grid)
+        L.a2_genmtrx.argtypes = [G, P, ctypes.POINTER(A3Ops), P]
+        L.a2_rbe.argtypes = [G, P, P, P, P]
+        L.a2_rhsbc.argtypes = [G, P, P]
+        L.a2_itrbc.argtypes = [G, P]
+        L.a2_resstat.argtypes = [G, P, P]
+        L.a2_resstat.restype = D
+        L.a2_lhs.argtypes = [G, ctypes.POINTER(A3Ops), P, P, I, P]
+        L.a2_step.argtypes = [G, I, P, P, P, ctypes.POINTER(A3Ops), P, P, P, P]
+        L.a2_step.restype = D
+        L._a2_setup = True
+    return L
+
+
+def ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Oracle2D:
+    """Grid struct, operator storage and scratch of the oracle for one case."""
+
+    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False):
+        self.L = _lib(lib)
+        p = case["params"]
+        self.nx, self.ny = nx, ny = p["nx"], p["ny"]
+        self.keep = {k: np.asfortranarray(v, dtype=np.float64) for k, v in case["metrics"].items()}
+        pot = np.asfortranarray(case["pot"], dtype=np.float64)
+        self.pot = {k: np.ascontiguousarray(pot[i]) for i, k in enumerate(("rhobt", "ubt", "vbt", "wbt", "tbt"))}
+        self.bnt = np.asfortranarray(case["bnt"], dtype=np.float64)
+        g3 = A3Grid(cflmax=cflmax, dtmax=dtmax, loctime=loctime,
+                    **{k: p[k] for k in ("nx", "ny", "dxi", "deta", "Ma", "Re", "Pr", "gamma", "gamma1", "omega",
+                                         "kz", "alfa", "xper", "yper", "navier", "wall", "wallt", "top", "optx",
+                                         "opty")},
+                    **{k: ptr(v).value for k, v in self.keep.items()})
+        self.resacc = ctypes.c_double(0.0)
+        if res_compat:
+            g3.resacc = ctypes.cast(ctypes.byref(self.resacc), P).value
+        self.g = A2Grid(g=g3, theta=case.get("theta", 0.0), bnt=ptr(self.bnt).value,
+                        **{k: ptr(v).value for k, v in self.pot.items()})
+        self.ops = {k: np.zeros((5, 5, nx, ny), order="F") for k in ("Ah", "Bh", "Dh", "Dhi")}
+        self.ops.update({k: np.zeros((6, nx, ny), order="F") for k in ("Vh11", "Vh12", "Vh22", "ABhi")})
+        self.o = A3Ops(**{k: ptr(v).value for k, v in self.ops.items()})
+        self.dtl = np.zeros((nx, ny), order="F")
+        self.r = np.zeros((5, nx, ny), order="F")
+        self.vold = np.zeros((5, nx, ny), order="F")
+        self.mat = np.zeros((5, 5, 5, nx, ny), order="F")
+        self.per = np.zeros((2, 5, 5, nx, ny), order="F")
+        self.cfl = ctypes.c_double(0.0)
+
+    def itrbc(self, v):
+        self.L.a2_itrbc(ctypes.byref(self.g), ptr(v))
+
+    def step(self, v, niter=1):
+        return self.L.a2_step(ctypes.byref(self.g), niter, ptr(v), ptr(self.vold), ptr(self.r), ctypes.byref(self.o),
+                              ptr(self.dtl), ptr(self.mat), ptr(self.per), ctypes.byref(self.cfl))
+
+    def genmtrx(self, v):
+        r = np.zeros_like(v)
+        assert self.L.a2_genmtrx(ctypes.byref(self.g), ptr(v), ctypes.byref(self.o), ptr(r)) == 0
+        return r
+
+    def rhs(self, v, vold, dtl):
+        """r = rhsBC(rbe(genmtrx(v))) and its resstat value."""
+        r = self.genmtrx(v)
+        self.L.a2_rbe(ctypes.byref(self.g), ptr(r), ptr(v), ptr(vold), ptr(dtl))
+        self.L.a2_rhsbc(ctypes.byref(self.g), ptr(r), ptr(v))
+        return r, self.L.a2_resstat(ctypes.byref(self.g), ptr(r), ptr(dtl))
+
+    def lhs(self, v, dtl, direction):
+        """LHS of a sweep for the operators of the last genmtrx call."""
+        mat = np.zeros((5, 5, 5, self.nx, self.ny), order="F")
+        assert self.L.a2_lhs(ctypes.byref(self.g), ctypes.byref(self.o), ptr(dtl), ptr(v), direction, ptr(mat)) == 0
+        return mat

@@ -43,7 +43,7 @@ def test_python_signatures_cover_header():
 
     solver_syms = [n for n in declared_symbols()
                    if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops",
-                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes")]
+                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes")]
     assert sorted(SIGNATURES) == solver_syms
 
 
@@ -139,3 +139,37 @@ def test_ctx3d_null_arguments(lib):
     assert lib.lns_ctx3d_bytes(None) == 0
     assert lib.lns_ctx3d_profile(None, 1) == 1
     assert lib.lns_ctx3d_profile_read(None, None, None) == 1
+
+
+def _params2d(**kw):
+    from lns3d_gb300._lib import Params2D
+
+    base = dict(nx=32, ny=24, dxi=1 / 31, deta=1 / 23, Ma=0.5, Re=1000.0, Pr=0.72, gamma=1.4, alfa=1.0, cflmax=1.0,
+                dtmax=1e30, theta=0.0, loctime=0, xper=1, yper=0, navier=1, wall=0, wallt=1, top=0, optx=-1, opty=-1,
+                res_compat=0)
+    base.update(kw)
+    return Params2D(**base)
+
+
+@pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=2), dict(wallt=2),
+                                 dict(top=1), dict(nx=7), dict(ny=6), dict(Ma=1.0), dict(deta=0.0),
+                                 dict(res_compat=3)])
+def test_ctx2d_rejects_unsupported_options(lib, bad):
+    ctx = ctypes.c_void_p()
+    rc = lib.lns_ctx2d_create(ctypes.byref(_params2d(**bad)), ctypes.byref(ctx))
+    assert rc == 1 and not ctx.value
+    assert lib.lns_last_error()
+
+
+def test_ctx2d_null_arguments(lib):
+    assert lib.lns_ctx2d_create(None, None) == 1
+    assert lib.lns_upload_metrics2d(None, None) == 1
+    assert lib.lns_upload_top2d(None, None, None) == 1
+    assert lib.lns_itrbc2d_dev(None, None, None) == 1
+    assert lib.lns_step2d(None, None, 1, 1, None) == 1
+    assert lib.lns_step2d_dev(None, None, 1, 1, None, None) == 1
+    assert lib.lns_rhs2d_dev(None, None, None, None, None, None) == 1
+    assert lib.lns_lhs2d_dev(None, 1, None, None, None) == 1
+    assert lib.lns_get_field2d(None, 0, None) == 1
+    assert lib.lns_ctx2d_destroy(None) == 0
+    assert lib.lns_ctx2d_bytes(None) == 0

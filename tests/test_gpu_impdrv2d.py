@@ -1,0 +1,169 @@
+"""GPU parity of the nonlinear 2D implicit step (lns_ctx2d_*, through the C
+ABI) against the CPU oracle (oracle/impdrv2d_oracle.c) on the vortex case.
+
+Tolerances (FP64; the GPU fuses multiply-adds, the oracle does not):
+  operators, time step, LHS        1e-12 of the field's largest entry
+  RHS and residual                 1e-11 of the largest entry
+  steps                            1e-12 of max|v| per step over the
+                                   reference's 100-step comparison
+"""
+import numpy as np
+import pytest
+
+from oracle.impdrv2d import Oracle2D
+
+pytestmark = pytest.mark.gpu
+
+OPS_TOL, RHS_TOL, STEP_TOL = 1e-12, 1e-11, 1e-12
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def make(case, **kw):
+    from lns3d_gb300 import ImpDrv2D
+
+    return ImpDrv2D(case["params"], case["metrics"], case["bnt"], case["pot"], cflmax=1.0, loctime=0, **kw)
+
+
+@pytest.fixture(scope="module")
+def small():
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=40, ny=33, seed=2)
+    # a state off the initial condition: the oracle's own first steps
+    o = Oracle2D(c, cflmax=1.0, loctime=0)
+    v = c["v"].copy(order="F")
+    o.itrbc(v)
+    for _ in range(3):
+        o.step(v)
+    return c, v
+
+
+def dev(a):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+
+
+def host(t, shape):
+    return t.cpu().numpy().reshape(shape, order="F")
+
+
+def test_rhs_operators_and_time_step_match_oracle(cuda, small):
+    import ctypes
+
+    import torch
+
+    c, v = small
+    o = Oracle2D(c, cflmax=1.0, loctime=0)
+    vold = np.asfortranarray(v * (1.0 + 1e-3 * np.random.default_rng(1).standard_normal(v.shape)))
+    L = o.L
+    cfl = L.a3_set_time_step(ctypes.byref(o.g.g), ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(o.dtl.ctypes.data))
+    r_ref, res_ref = o.rhs(v, vold, o.dtl)
+    drv = make(c)
+    dv, dvo = dev(v), dev(vold)
+    dr = torch.zeros_like(dv)
+    tot = torch.zeros(1, dtype=torch.float64, device="cuda")
+    drv.rhs(dv, dvo, dr, tot)
+    torch.cuda.synchronize()
+    assert rel(drv.field("dtl"), o.dtl) < OPS_TOL
+    for name in ("Ah", "Bh", "Dh", "Vh11", "Vh12", "Vh22"):
+        assert rel(drv.field(name), o.ops[name]) < OPS_TOL, name
+    assert rel(host(dr, v.shape), r_ref) < RHS_TOL
+    assert abs(tot.item() - res_ref) <= RHS_TOL * res_ref
+    assert cfl > 0
+
+
+@pytest.mark.parametrize("direction", [1, 2])
+def test_lhs_matches_oracle(cuda, small, direction):
+    import torch
+
+    c, v = small
+    o = Oracle2D(c, cflmax=1.0, loctime=0)
+    import ctypes
+
+    o.L.a3_set_time_step(ctypes.byref(o.g.g), ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(o.dtl.ctypes.data))
+    o.rhs(v, v, o.dtl)
+    ref = o.lhs(v, o.dtl, direction)
+    drv = make(c)
+    dv = dev(v)
+    drv.rhs(dv, dv, torch.zeros_like(dv))
+    mat = torch.zeros(125 * c["params"]["nx"] * c["params"]["ny"], dtype=torch.float64, device="cuda")
+    drv.lhs(direction, dv, mat)
+    torch.cuda.synchronize()
+    got = host(mat, ref.shape)
+    assert rel(got, ref) < OPS_TOL
+    # rows set by the boundary conditions agree to rounding of their own scale
+    assert rel(got[:, :, :, :, -1], ref[:, :, :, :, -1]) < OPS_TOL
+
+
+def test_itrbc_matches_oracle(cuda, small):
+    c, v = small
+    o = Oracle2D(c, cflmax=1.0, loctime=0)
+    w = np.asfortranarray(v * (1.0 + 1e-2 * np.random.default_rng(3).standard_normal(v.shape)))
+    want = w.copy(order="F")
+    o.itrbc(want)
+    drv = make(c)
+    dw = dev(w)
+    drv.itrbc(dw)
+    assert rel(host(dw, w.shape), want) < 1e-14
+
+
+@pytest.mark.parametrize("niter", [1, 2])
+def test_steps_match_oracle(cuda, niter):
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=40, ny=33, seed=4)
+    o = Oracle2D(c, cflmax=1.0, loctime=0)
+    drv = make(c)
+    v_ref = c["v"].copy(order="F")
+    o.itrbc(v_ref)
+    v_gpu = v_ref.copy(order="F")
+    for s in range(5):
+        res_ref = o.step(v_ref, niter=niter)
+        res_gpu = drv.step(v_gpu, nsteps=1, niter=niter)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+
+
+def test_config1_100_step_history(cuda):
+    # the reference's comparison: 128 x 128, 100 steps, every step's state and
+    # residual against the oracle
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=128, ny=128, seed=0)
+    o = Oracle2D(c, cflmax=1.0, loctime=0)
+    drv = make(c)
+    v_ref = c["v"].copy(order="F")
+    o.itrbc(v_ref)
+    v_gpu = v_ref.copy(order="F")
+    worst, worst_res = 0.0, 0.0
+    for s in range(100):
+        res_ref = o.step(v_ref)
+        res_gpu = drv.step(v_gpu)[0]
+        worst = max(worst, rel(v_gpu, v_ref))
+        worst_res = max(worst_res, abs(res_gpu - res_ref) / res_ref)
+    assert worst < STEP_TOL, worst
+    assert worst_res < 1e-10, worst_res
+
+
+def test_device_steps_and_reference_residual_mode(cuda, small):
+    import torch
+
+    c, v = small
+    a, b = make(c), make(c, res_compat=True)
+    o = Oracle2D(c, cflmax=1.0, loctime=0, res_compat=True)
+    vh = v.copy(order="F")
+    res_h = a.step(vh, nsteps=4)
+    dv = dev(v)
+    tot = torch.zeros(4, dtype=torch.float64, device="cuda")
+    b.step(dv, nsteps=4, totres=tot)
+    torch.cuda.synchronize()
+    assert np.array_equal(host(dv, v.shape), vh)
+    vo = v.copy(order="F")
+    res_o = np.array([o.step(vo) for _ in range(4)])
+    assert np.abs(tot.cpu().numpy() - res_o).max() <= 1e-10 * res_o.max()
+    assert abs(res_h[0] - res_o[0]) <= 1e-10 * res_o[0]   # the first call has no previous value
