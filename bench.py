@@ -60,7 +60,26 @@ PHASE_BYTES = {"rhs": 1224, "xsweep": 3760, "ysweep": 2160, "update": 240}
 # in-block lower 10, upper blocks 50, in-block upper 10 and 5 divisions
 # (counted 5), periodic fill columns and rows +100
 PHASE_FLOPS = {"xsweep": 8 * 225, "ysweep": 8 * 125}
-KERNELS_PER_STEP = 8   # bc (predictor), grad1, rhs, resid, xi sweep, eta sweep, add, bc
+# per kernel segment (lns_ctx3d_profile): algorithmic bytes and flops per
+# grid point of one launch, FP64
+#   rhs      grad1 + rhs + resid: v, vold, dv/dxi 240 B + operators 984 B + r 80 B
+#   x_scale  D^-1 400 B + r read and write 160 B            (25 complex FMA)
+#   x_fwd    F1, F2 800 B + s read 80 B + yh write 80 B     (50 complex FMA)
+#   x_fill   K 800 B + E 800 B + yh read, write 160 B       (100 complex FMA)
+#   x_bwd    B1, B2 800 B + c read 80 B + x write 80 B      (50 complex FMA)
+#   y_*      as x without the fill
+#   update   v read, write 160 B + r 80 B
+KERNEL_BYTES = {"rhs": 1304, "x_scale": 560, "x_fwd": 960, "x_fill": 1760, "x_bwd": 960, "y_scale": 560,
+                "y_fwd": 960, "y_bwd": 960, "update": 240}
+KERNEL_FLOPS = {"x_scale": 200, "x_fwd": 400, "x_fill": 800, "x_bwd": 400, "y_scale": 200, "y_fwd": 400,
+                "y_bwd": 400}
+KERNEL_NAMES = {"x_fwd": "chain_fwd_kernel<cd, periodic> (xi forward recurrence)",
+                "x_bwd": "chain_bwd_kernel<cd, periodic> (xi backward recurrence)",
+                "rhs": "grad1_kernel + rhs_kernel + resid_kernel"}
+# DRAM bytes per launch from the ncu capture of the same kernel on this
+# workload (profiles/chain_kernels_cd_xsweep_512x256.md)
+KERNEL_TRAFFIC = {"x_fwd": 129.283840e6 + 6.081792e6, "x_bwd": 129.350144e6 + 6.129152e6}
+KERNELS_PER_STEP = 14  # bc (predictor), grad1, rhs, resid, xi sweep (5), eta sweep (3), add, bc
 
 # ---- secondary: the isolated batched solve
 N_ROWS, N_LINES = 256, 512
@@ -436,6 +455,75 @@ def run_impdrv2d(torch, dev, steps, with_cpu):
     return out
 
 
+def batch_problems(P=64, seed=4):
+    """The batched workload: 64 linearised shear-layer problems, beta on a
+    uniform grid of [0, 0.4] and omega on [0.01, 0.1] (8 x 8), grid sizes
+    drawn by seed from nx in {128, 192, 256, 384, 512}, ny in {64, 96, 128,
+    192, 256}."""
+    import numpy as np
+
+    from lns3d_gb300.cases import shear_layer
+
+    rng = np.random.default_rng(seed)
+    side = int(round(P ** 0.5))
+    betas = np.linspace(0.0, 0.4, side)
+    omegas = np.linspace(0.01, 0.1, side)
+    out = []
+    for k in range(P):
+        nx = int(rng.choice([128, 192, 256, 384, 512]))
+        ny = int(rng.choice([64, 96, 128, 192, 256]))
+        out.append(shear_layer(nx=nx, ny=ny, beta=float(betas[k // side]), omega=float(omegas[k % side]), seed=k))
+    return out
+
+
+def run_batch(torch, with_cpu, max_steps=2000, tol=1e-10):
+    """All 64 problems to a 1e-10 residual in one batch (mixed precision:
+    FP64 residual, FP32 scaled factors and sweeps), lines per CTA autotuned."""
+    import numpy as np
+
+    import lns3d_gb300 as g
+
+    probs = batch_problems()
+    pts = np.array([c["params"]["nx"] * c["params"]["ny"] for c in probs])
+    t0 = time.perf_counter()
+    batch = g.Batch3D(probs, cflmax=CFL3, loctime=1, precision=g.adi3d.MIXED)
+    w = batch.tune()
+    setup = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps, res = batch.run(max_steps=max_steps, tol=tol, check_every=25)
+    wall = time.perf_counter() - t0
+    conv = steps > 0
+    done_pts = float((pts * np.where(conv, steps, max_steps)).sum())
+    out = {"workload": "batch-64-shear-layers-beta0-0.4-omega0.01-0.1-uneven-grids-mixed-to-1e-10",
+           "problems": len(probs), "grid_points": int(pts.sum()), "converged": int(conv.sum()),
+           "steps_min": int(steps[conv].min()) if conv.any() else None,
+           "steps_max": int(steps[conv].max()) if conv.any() else None,
+           "wall_s": wall, "setup_s": setup, "value": done_pts / wall, "unit": "grid-pt-steps/s",
+           "lines_per_cta": w, "device_bytes": int(batch.device_bytes), "cpu_baseline": None}
+    batch.close()
+    if with_cpu:
+        import oracle
+        from oracle.adi3d import Oracle3D
+
+        lib = oracle.orc_omp()
+        t = 0.0
+        n = 0
+        for c in probs[:8]:
+            o = Oracle3D(c, cflmax=CFL3, loctime=1, lib=lib)
+            v = np.asfortranarray(c["v"].copy())
+            o.step(v)
+            t0 = time.perf_counter()
+            o.step(v)
+            o.step(v)
+            t += time.perf_counter() - t0
+            n += 2 * c["params"]["nx"] * c["params"]["ny"]
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        out["cpu_baseline"] = {"value": n / t, "unit": "grid-pt-steps/s", "cores": cores, "kind": "port",
+                               "sample": "2 steps of each of the first 8 problems, serially, OpenMP inside each"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -447,6 +535,7 @@ def main():
     ap.add_argument("--no-converge", action="store_true", help="skip the runs to a 1e-10 residual")
     ap.add_argument("--no-isolated", action="store_true", help="skip the isolated batched-solve leg")
     ap.add_argument("--no-2d", action="store_true", help="skip the nonlinear 2D step leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-problem leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -502,9 +591,10 @@ def main():
     # per-phase kernel times (events on the launching stream, separate pass)
     d64.profile(True)
     time_steps(torch, d64, v64, K, stream)
-    phases64, ncorr = d64.profile_read()
+    phases64, ncorr, seg64 = d64.profile_read()
     d64.profile(False)
     ph64 = {k: v / ncorr for k, v in phases64.items()}
+    kern64 = {k: v / ncorr for k, v in seg64.items()}
 
     # ---- mixed step
     d32, v32, setup32 = make(g.adi3d.MIXED)
@@ -514,16 +604,17 @@ def main():
     total32, per32 = time_steps(torch, d32, v32, K, stream)
     d32.profile(True)
     time_steps(torch, d32, v32, K, stream)
-    phases32, n32 = d32.profile_read()
+    phases32, n32, seg32 = d32.profile_read()
     d32.profile(False)
     ph32 = {k: v / n32 for k, v in phases32.items()}
+    kern32 = {k: v / n32 for k, v in seg32.items()}
     if world > 1:
         t = torch.tensor([total32], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total32 = float(t.item())
     mixed = {"value": world * PTS3 * K / (total32 / 1e3), "ms_per_step": total32 / K,
              "latency_ms": {"p50": percentile(per32, 0.5), "p99": percentile(per32, 0.99)},
-             "phase_ms": ph32, "setup": setup32, "device_bytes": int(d32.device_bytes)}
+             "phase_ms": ph32, "kernel_ms": kern32, "setup": setup32, "device_bytes": int(d32.device_bytes)}
 
     # ---- to a 1e-10 residual from the initial disturbance
     conv = None
@@ -569,15 +660,20 @@ def main():
         del d32
         iso = run_isolated(torch, dev, L, sp, stream, rank, world, 3, max(3, min(K, 10)))
 
+    legb = None
+    if not args.no_batch:
+        legb = run_batch(torch, rank == 0 and not args.no_cpu_baseline)
+
     leg2d = None
     if not args.no_2d:
         leg2d = run_impdrv2d(torch, dev, max(10, K), rank == 0 and not args.no_cpu_baseline)
 
     hbm_peak, peak_kind = peaks()
     fp64_peak = L.lns_probe_fp64_tflops()
-    dom = max(("xsweep", "ysweep"), key=lambda k: ph64[k])
-    achieved = PHASE_BYTES[dom] * PTS3 / (ph64[dom] / 1e3) / 1e9
-    fp64_achieved = PHASE_FLOPS[dom] * PTS3 / (ph64[dom] / 1e3) / 1e12
+    # the dominant kernel: the xi forward recurrence (chain_fwd_kernel<cd, 1>)
+    dom = max(kern64, key=lambda k: kern64[k])
+    achieved = KERNEL_BYTES[dom] * PTS3 / (kern64[dom] / 1e3) / 1e9
+    fp64_achieved = KERNEL_FLOPS.get(dom, 0) * PTS3 / (kern64[dom] / 1e3) / 1e12
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline3d(8)
@@ -587,18 +683,19 @@ def main():
             "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c128", "data": "synthetic", "config": config3(world),
             "latency_ms": {"p50": percentile(per_step, 0.5), "p99": percentile(per_step, 0.99)},
-            "phase_ms": ph64, "setup": setup64, "device_bytes": int(d64.device_bytes),
+            "phase_ms": ph64, "kernel_ms": kern64, "setup": setup64, "device_bytes": int(d64.device_bytes),
             "mixed": mixed, "converge": conv, "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
-                         "kernel": "chain sweep kernels of the %s phase (scale, recurrences%s)" % (dom, ", tail, fill" if dom == "xsweep" else ""),
-                         "bytes_per_pt": PHASE_BYTES[dom]},
+                         "frac": achieved / hbm_peak, "traffic": KERNEL_TRAFFIC.get(dom), "peak_source": peak_kind,
+                         "kernel": KERNEL_NAMES.get(dom, dom), "kernel_ms": kern64[dom],
+                         "bytes_per_pt": KERNEL_BYTES[dom]},
             "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                              "frac": fp64_achieved / fp64_peak, "flops_per_pt": PHASE_FLOPS[dom],
+                              "frac": fp64_achieved / fp64_peak, "flops_per_pt": KERNEL_FLOPS.get(dom, 0),
                               "peak_source": "measured live: DFMA stream on every SM (lns_probe_fp64_tflops)"},
             "cpu_baseline": cpu,
             "isolated_solve": iso,
             "impdrv2d": leg2d,
+            "batch": legb,
             "gpu_launches": KERNELS_PER_STEP * K,
             "clocks": clocks,
         }

@@ -315,17 +315,50 @@ int lns_rhs3d_dev(lns_ctx3d* ctx, const double* v, const double* vold, double* r
  * src/lhsbc2f3d.f90) into the complex*16 device array mat(5,5,5,nx,ny). */
 int lns_lhs3d_dev(lns_ctx3d* ctx, int32_t dir, double* mat, void* stream);
 /* Phase timing, no reference counterpart.  lns_ctx3d_profile(ctx, 1) makes
- * every later corrector record CUDA events on its stream around the RHS, the
- * xi sweep, the eta sweep and the update (and resets the record);
- * lns_ctx3d_profile_read waits for them and returns the summed milliseconds
- * of the four phases in ms[4] and the number of correctors in *ncorr, then
- * clears the record. */
+ * every later corrector record CUDA events on its stream (and resets the
+ * record); lns_ctx3d_profile_read waits for them and returns the summed
+ * milliseconds of LNS_PROFILE_SEGMENTS segments in ms[]: 0 RHS, 1 xi
+ * scaling, 2 xi forward recurrence, 3 xi fill (tail and correction), 4 xi
+ * backward recurrence, 5 eta scaling, 6 eta forward, 7 eta backward,
+ * 8 update; and the number of correctors in *ncorr.  Clears the record. */
+#define LNS_PROFILE_SEGMENTS 9
 int lns_ctx3d_profile(lns_ctx3d* ctx, int32_t on);
 int lns_ctx3d_profile_read(lns_ctx3d* ctx, double* ms, int32_t* ncorr);
 /* Copy of a frozen field to the host in the reference layout:
  * 0 Ah, 1 Bh, 2 Dh, 3 Dhi (5,5,nx,ny); 4 Vh11, 5 Vh12, 6 Vh22, 7 ABhi
  * (6,nx,ny); 8 dtl (nx,ny). */
 int lns_get_field3d(lns_ctx3d* ctx, int32_t which, double* out);
+
+/* ---------------------------------------------------------------------------
+ * Batches of linearised problems (no reference counterpart: the reference
+ * runs one problem per process).  A batch holds nprob independent problems
+ * -- each with its own deck (grid size, beta, omega, ...), metrics, mean
+ * flow and disturbance -- and advances all of them together: every phase of
+ * the step (RHS, scaling, recurrences, fill, update) is one launch for all
+ * problems, whose blocks look up their problem and local block in a work
+ * table, and the whole step is captured once as a CUDA graph and replayed.
+ * Each problem's result is identical to a lns_ctx3d run of the same problem
+ * (the same kernels on the same data).  All problems share the precision.
+ */
+typedef struct lns_batch3d lns_batch3d;
+/* params[nprob]: the deck of each problem */
+int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** batch);
+int lns_batch3d_destroy(lns_batch3d* batch);
+size_t lns_batch3d_bytes(const lns_batch3d* batch);
+/* metrics (nx,ny,10), mean flow vm(5,nx,ny) and disturbance v(5,nx,ny)
+ * complex of problem prob (host arrays) */
+int lns_batch3d_upload(lns_batch3d* batch, int32_t prob, const double* metrics, const double* vm, const double* v);
+/* Picks the lines per CTA of the recurrences (1, 2 or 4) by timing a few
+ * steps of each; the problems' states are restored afterwards. */
+int lns_batch3d_tune(lns_batch3d* batch, int32_t niter, int32_t* lines_per_cta);
+/* Steps every problem until its residual (resstat3D, the last corrector of
+ * a step) is <= tol, or max_steps steps.  Residuals are checked every
+ * check_every steps; a converged problem stops stepping at that check.
+ * steps[prob] = the first step whose residual was <= tol (-1 if none),
+ * final_res[prob] = its residual at the stop. */
+int lns_batch3d_run(lns_batch3d* batch, int32_t max_steps, int32_t niter, double tol, int32_t check_every,
+                    int32_t* steps, double* final_res);
+int lns_batch3d_get_state(lns_batch3d* batch, int32_t prob, double* v);
 
 #ifdef __cplusplus
 }

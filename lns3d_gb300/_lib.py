@@ -65,6 +65,12 @@ SIGNATURES = {
     "lns_get_field3d": [P, I32, DP],
     "lns_ctx3d_profile": [P, I32],
     "lns_ctx3d_profile_read": [P, DP, P],
+    "lns_batch3d_create": [I32, P, P],
+    "lns_batch3d_destroy": [P],
+    "lns_batch3d_upload": [P, I32, DP, DP, DP],
+    "lns_batch3d_tune": [P, I32, P],
+    "lns_batch3d_run": [P, I32, I32, ctypes.c_double, I32, P, P],
+    "lns_batch3d_get_state": [P, I32, DP],
     "lns_ctx2d_create": [P, P],
     "lns_ctx2d_destroy": [P],
     "lns_upload_metrics2d": [P, DP],
@@ -115,6 +121,8 @@ def lib():
         L.lns_mixed_workspace_bytes.argtypes = [I32, I32, I32, I32]
         L.lns_ctx3d_bytes.restype = ctypes.c_size_t
         L.lns_ctx3d_bytes.argtypes = [P]
+        L.lns_batch3d_bytes.restype = ctypes.c_size_t
+        L.lns_batch3d_bytes.argtypes = [P]
         L.lns_ctx2d_bytes.restype = ctypes.c_size_t
         L.lns_ctx2d_bytes.argtypes = [P]
         for name, args in SIGNATURES.items():

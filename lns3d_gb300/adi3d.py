@@ -130,19 +130,93 @@ class ImpDrv3D:
         """Start (or stop) recording per-phase CUDA events of every corrector."""
         check(lib().lns_ctx3d_profile(self._ctx, 1 if on else 0), "lns_ctx3d_profile")
 
+    SEGMENTS = ("rhs", "x_scale", "x_fwd", "x_fill", "x_bwd", "y_scale", "y_fwd", "y_bwd", "update")
+
     def profile_read(self):
-        """Summed milliseconds of the phases rhs, xsweep, ysweep, update and
-        the number of correctors recorded since profiling started."""
-        ms = np.zeros(4)
+        """Summed milliseconds per kernel segment (SEGMENTS) and per phase
+        (rhs, xsweep, ysweep, update), and the number of correctors recorded
+        since profiling started."""
+        ms = np.zeros(len(self.SEGMENTS))
         n = ctypes.c_int32()
         check(lib().lns_ctx3d_profile_read(self._ctx, ctypes.c_void_p(ms.ctypes.data), ctypes.byref(n)),
               "lns_ctx3d_profile_read")
-        return dict(zip(("rhs", "xsweep", "ysweep", "update"), ms.tolist())), n.value
+        seg = dict(zip(self.SEGMENTS, ms.tolist()))
+        phases = {"rhs": seg["rhs"], "xsweep": sum(seg[k] for k in ("x_scale", "x_fwd", "x_fill", "x_bwd")),
+                  "ysweep": sum(seg[k] for k in ("y_scale", "y_fwd", "y_bwd")), "update": seg["update"]}
+        return phases, n.value, seg
 
     def close(self):
         if self._ctx:
             lib().lns_ctx3d_destroy(self._ctx)
             self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch3D:
+    """Many linearised problems advanced together (lns_batch3d_* of the C ABI).
+
+    problems: list of dicts with keys params, metrics, vm, v (as for
+    ImpDrv3D / lns3d_gb300.cases.shear_layer).  Every phase of a step is one
+    launch for all problems and the step is replayed as a CUDA graph; each
+    problem's result equals its own ImpDrv3D run.
+    """
+
+    def __init__(self, problems, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False):
+        self.P = len(problems)
+        self.shapes = []
+        arr = (Params3D * self.P)()
+        for k, pr in enumerate(problems):
+            p = pr["params"]
+            arr[k] = Params3D(nx=p["nx"], ny=p["ny"], dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"],
+                              Pr=p["Pr"], gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"],
+                              cflmax=cflmax, dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"],
+                              navier=p["navier"], wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"],
+                              opty=p["opty"], precision=precision, res_compat=1 if res_compat else 0)
+            self.shapes.append((5, int(p["nx"]), int(p["ny"])))
+        self._b = ctypes.c_void_p()
+        check(lib().lns_batch3d_create(self.P, arr, ctypes.byref(self._b)), "lns_batch3d_create")
+        for k, pr in enumerate(problems):
+            nx, ny = self.shapes[k][1:]
+            m = np.empty((nx, ny, 10), order="F")
+            for i, name in enumerate(METRICS):
+                m[:, :, i] = pr["metrics"][name]
+            vm = np.asfortranarray(pr["vm"], dtype=np.float64)
+            v = np.asfortranarray(pr["v"], dtype=np.complex128)
+            check(lib().lns_batch3d_upload(self._b, k, ctypes.c_void_p(m.ctypes.data), ctypes.c_void_p(vm.ctypes.data),
+                                           ctypes.c_void_p(v.ctypes.data)), "lns_batch3d_upload")
+
+    @property
+    def device_bytes(self):
+        return lib().lns_batch3d_bytes(self._b)
+
+    def tune(self, niter=1):
+        w = ctypes.c_int32()
+        check(lib().lns_batch3d_tune(self._b, niter, ctypes.byref(w)), "lns_batch3d_tune")
+        return w.value
+
+    def run(self, max_steps, tol=0.0, niter=1, check_every=25):
+        """Steps every problem until its residual <= tol (or max_steps);
+        returns (steps to tol per problem, -1 if not reached; final residuals)."""
+        steps = np.zeros(self.P, dtype=np.int32)
+        res = np.zeros(self.P)
+        check(lib().lns_batch3d_run(self._b, max_steps, niter, tol, check_every, ctypes.c_void_p(steps.ctypes.data),
+                                    ctypes.c_void_p(res.ctypes.data)), "lns_batch3d_run")
+        return steps, res
+
+    def state(self, k):
+        v = np.zeros(self.shapes[k], np.complex128, order="F")
+        check(lib().lns_batch3d_get_state(self._b, k, ctypes.c_void_p(v.ctypes.data)), "lns_batch3d_get_state")
+        return v
+
+    def close(self):
+        if self._b:
+            lib().lns_batch3d_destroy(self._b)
+            self._b = ctypes.c_void_p()
 
     def __del__(self):
         try:

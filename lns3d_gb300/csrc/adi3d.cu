@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/lns3d_gb300.h"
@@ -348,10 +349,11 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
 }
 
 // -------------------------------------------------------------------- RHS
-// c1v = d v / d xi (complex)
-__global__ void grad1_kernel(Grid g, const cd* __restrict__ v, cd* __restrict__ c1v) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int j = blockIdx.y + 1;
+// c1v = d v / d xi (complex); (bx, by) is the block within the problem
+__device__ __forceinline__ void grad1_body(const Grid& g, const cd* __restrict__ v, cd* __restrict__ c1v, int bx,
+                                           int by) {
+  const int i = bx * blockDim.x + threadIdx.x + 1;
+  const int j = by + 1;
   if (i > g.nx) return;
   const long long p = pix(g, i, j);
   for (int k = 0; k < 5; ++k) {
@@ -361,15 +363,19 @@ __global__ void grad1_kernel(Grid g, const cd* __restrict__ v, cd* __restrict__ 
   }
 }
 
+__global__ void grad1_kernel(Grid g, const cd* __restrict__ v, cd* __restrict__ c1v) {
+  grad1_body(g, v, c1v, blockIdx.x, blockIdx.y);
+}
+
 // r = vold - v - dtl L(v) (src/lrhs3d.f90:33-218, rbe3D), then the boundary
 // rows (src/rhsbc3d.f90), written as FP64 (r64) and/or FP32 (r32); the
-// block sums of |r|^2 / dtl^2 (src/resstat3d.f90:37-46) go to part[].
-__global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __restrict__ v,
-                                                  const cd* __restrict__ vold, const cd* __restrict__ c1v,
-                                                  cd* r64, cf* r32, double* part) {
+// block sums of |r|^2 / dtl^2 (src/resstat3d.f90:37-46) go to part[bx + nbx by].
+__device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* __restrict__ v,
+                                         const cd* __restrict__ vold, const cd* __restrict__ c1v, cd* r64, cf* r32,
+                                         double* part, int bx, int by, int nbx) {
   __shared__ double red[128];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int j = blockIdx.y + 1;
+  const int i = bx * blockDim.x + threadIdx.x + 1;
+  const int j = by + 1;
   double resnod = 0.0;
   if (i <= g.nx) {
     const long long p = pix(g, i, j), np = o.np;
@@ -478,7 +484,12 @@ __global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __res
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * blockIdx.y] = red[0];
+  if (threadIdx.x == 0) part[bx + nbx * by] = red[0];
+}
+__global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __restrict__ v,
+                                                  const cd* __restrict__ vold, const cd* __restrict__ c1v,
+                                                  cd* r64, cf* r32, double* part) {
+  rhs_body(g, o, v, vold, c1v, r64, r32, part, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 // ----------------------------------------------------------------- update
@@ -486,8 +497,8 @@ __global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __res
 // column i (wall row j = 1 from rows 2..5, top row j = ny); with a periodic
 // x direction the remaining threads copy the interior rows of column 1 to
 // column nx, and the thread of column 1 copies its boundary rows.
-__global__ void bc_kernel(Grid g, cd* __restrict__ v) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, int bx) {
+  const int t = bx * blockDim.x + threadIdx.x;
   const int ncol = g.xper ? g.nx - 1 : g.nx;
   if (t < ncol) {
     const int i = t + 1;
@@ -520,6 +531,87 @@ __global__ void bc_kernel(Grid g, cd* __restrict__ v) {
       for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, g.nx, j)] = v[m + 5 * pix(g, 1, j)];
   }
 }
+
+__global__ void bc_kernel(Grid g, cd* __restrict__ v) { bc_body(g, v, blockIdx.x); }
+
+// ------------------------------------------------------------- batching
+// Per-problem arguments of the per-step kernels of a batch (lns_batch3d):
+// one launch of a batched kernel runs one phase of every problem, block b
+// doing block table[b].y (and .z) of problem table[b].x; problems whose
+// active flag is zero are skipped.
+struct StepArgs {
+  Grid g;
+  Ops o;
+  cd *v, *vold, *c1v, *r64;
+  cf* r32;
+  double* part;  // RHS block partials
+  int nbx, nrhs;  // RHS blocks along x, partial count
+  double* acc;   // running residual of the reference mode, or null
+};
+
+__global__ void copy_batch_kernel(const StepArgs* __restrict__ list, const int2* __restrict__ table,
+                                  const int* __restrict__ active) {
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  const StepArgs& a = list[w.x];
+  const long long e = (long long)w.y * blockDim.x + threadIdx.x;
+  if (e < 5 * a.o.np) a.vold[e] = a.v[e];
+}
+__global__ void bc_batch_kernel(const StepArgs* __restrict__ list, const int2* __restrict__ table,
+                                const int* __restrict__ active) {
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  bc_body(list[w.x].g, list[w.x].v, w.y);
+}
+__global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4* __restrict__ table,
+                                   const int* __restrict__ active) {
+  const int4 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  const StepArgs& a = list[w.x];
+  grad1_body(a.g, a.v, a.c1v, w.y, w.z);
+}
+__global__ void __launch_bounds__(128) rhs_batch_kernel(const StepArgs* __restrict__ list,
+                                                        const int4* __restrict__ table,
+                                                        const int* __restrict__ active, int mixed) {
+  const int4 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  const StepArgs& a = list[w.x];
+  rhs_body(a.g, a.o, a.v, a.vold, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr, a.part, w.y, w.z, a.nbx);
+}
+// residual of each problem into hist[step * P + p] (src/resstat3d.f90:37-60)
+__global__ void resid_batch_kernel(const StepArgs* __restrict__ list, const int* __restrict__ active,
+                                   double* __restrict__ hist, const int* __restrict__ step, int P) {
+  __shared__ double red[256];
+  const int p = blockIdx.x;
+  if (!active[p]) return;
+  const StepArgs& a = list[p];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < a.nrhs; k += blockDim.x) s += a.part[k];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double tot = a.acc ? *a.acc + red[0] : red[0];
+    const double r = sqrt(tot / (double)a.o.np);
+    hist[(long long)(*step) * P + p] = r;
+    if (a.acc) *a.acc = r;
+  }
+}
+template <typename RT>
+__global__ void add_batch_kernel(const StepArgs* __restrict__ list, const int2* __restrict__ table,
+                                 const int* __restrict__ active) {
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  const StepArgs& a = list[w.x];
+  const long long e = (long long)w.y * blockDim.x + threadIdx.x;
+  if (e >= 5 * a.o.np) return;
+  const RT* r = reinterpret_cast<const RT*>(std::is_same<RT, cd>::value ? (const void*)a.r64 : (const void*)a.r32);
+  a.v[e] = add(a.v[e], to_hi(r[e]));
+}
+__global__ void step_incr_kernel(int* step) { *step += 1; }
 
 }  // namespace a3
 }  // namespace lns
@@ -558,8 +650,9 @@ struct lns_ctx3d {
   int res_cap = 0;
   int* status = nullptr;
   bool have_metrics = false, have_mean = false, factored = false;
-  // phase timing (lns_ctx3d_profile): per corrector, events before the RHS,
-  // after the RHS, after the xi sweep, after the eta sweep, after the update
+  // phase timing (lns_ctx3d_profile): per corrector, events around the RHS,
+  // the scaling, recurrences, tail and fill kernels of both sweeps, and the
+  // update (LNS_PROFILE_SEGMENTS segments)
   bool profile = false;
   std::vector<cudaEvent_t> events;
   size_t ev_used = 0;
@@ -699,10 +792,14 @@ int sweep_x(lns_ctx3d* c, T* r, cudaStream_t st) {
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
   ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
+  int rc = mark(c, st);
   ch::chain_fwd_kernel<T, true><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  if (!rc) rc = mark(c, st);
   ch::tail_kernel<T><<<a.nsys, 32 * ch::kTailWarps, 0, st>>>(a);
   ch::fill_kernel<T><<<(unsigned)((fill + 255) / 256), 256, 0, st>>>(a);
+  if (!rc) rc = mark(c, st);
   ch::chain_bwd_kernel<T, true><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "xi sweep launch");
 }
@@ -716,8 +813,11 @@ int sweep_y(lns_ctx3d* c, T* r, cudaStream_t st) {
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
   ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
+  int rc = mark(c, st);
   ch::chain_fwd_kernel<T, false><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  if (!rc) rc = mark(c, st);
   ch::chain_bwd_kernel<T, false><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "eta sweep launch");
 }
@@ -1008,14 +1108,16 @@ int lns_ctx3d_profile(lns_ctx3d* c, int32_t on) {
 
 int lns_ctx3d_profile_read(lns_ctx3d* c, double* ms, int32_t* ncorr) {
   if (!c || !ms || !ncorr) return fail3(LNS_ERR_ARG, "ctx3d_profile_read: null argument");
-  for (int k = 0; k < 4; ++k) ms[k] = 0.0;
+  constexpr int kSeg = LNS_PROFILE_SEGMENTS;
+  for (int k = 0; k < kSeg; ++k) ms[k] = 0.0;
   *ncorr = 0;
-  const size_t n = c->ev_used / 5;
+  const size_t n = c->ev_used / (kSeg + 1);
   for (size_t q = 0; q < n; ++q) {
-    for (int k = 0; k < 4; ++k) {
-      cudaError_t e = cudaEventSynchronize(c->events[5 * q + k + 1]);
+    for (int k = 0; k < kSeg; ++k) {
+      cudaError_t e = cudaEventSynchronize(c->events[(kSeg + 1) * q + k + 1]);
       float t = 0.f;
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&t, c->events[5 * q + k], c->events[5 * q + k + 1]);
+      if (e == cudaSuccess)
+        e = cudaEventElapsedTime(&t, c->events[(kSeg + 1) * q + k], c->events[(kSeg + 1) * q + k + 1]);
       if (e != cudaSuccess) return cuda3(e, "profile events");
       ms[k] += t;
     }
@@ -1041,6 +1143,419 @@ int lns_get_field3d(lns_ctx3d* c, int32_t which, double* out) {
   for (long long p = 0; p < np; ++p)
     for (int k = 0; k < nel; ++k) out[k + (long long)nel * p] = h[(size_t)k * np + p];
   return LNS_OK;
+}
+
+}  // extern "C"
+
+// ======================================================================
+// Batches of problems (lns_batch3d_*): one launch per phase for all
+// problems, the step captured once as a CUDA graph
+// ======================================================================
+struct lns_batch3d {
+  int P = 0;
+  bool mixed = false;
+  int device = -1;
+  int W = lns::chain::kChainWarps;  // lines per CTA of the recurrences
+  std::vector<lns_ctx3d*> ctx;
+  std::vector<void*> allocs;
+  size_t bytes = 0;
+  cudaStream_t st = nullptr;
+  lns::a3::StepArgs* d_args = nullptr;
+  lns::chain::Args *d_ax = nullptr, *d_ay = nullptr;
+  int* d_active = nullptr;
+  int* d_step = nullptr;
+  double* d_hist = nullptr;
+  long long hist_cap = 0;  // steps
+  int2 *t_elem = nullptr, *t_col = nullptr, *t_sx = nullptr, *t_fx = nullptr, *t_tx = nullptr, *t_lx = nullptr,
+       *t_sy = nullptr, *t_fy = nullptr;
+  int4* t_pts = nullptr;
+  int n_elem = 0, n_col = 0, n_sx = 0, n_fx = 0, n_tx = 0, n_lx = 0, n_sy = 0, n_fy = 0, n_pts = 0;
+  cudaGraphExec_t exec = nullptr;
+  int exec_W = 0, exec_niter = 0;
+  std::vector<int> active;
+  std::vector<bool> uploaded;
+};
+
+namespace {
+
+int balloc(lns_batch3d* b, size_t bytes, void** out) {
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  b->allocs.push_back(*out);
+  b->bytes += bytes;
+  return LNS_OK;
+}
+
+template <typename E>
+int upload_table(lns_batch3d* b, const std::vector<E>& h, E** d, int* n) {
+  void* q = nullptr;
+  int rc = balloc(b, sizeof(E) * std::max<size_t>(h.size(), 1), &q);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(q, h.data(), sizeof(E) * h.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload work table");
+  *d = (E*)q;
+  *n = (int)h.size();
+  return LNS_OK;
+}
+
+// The work tables of every phase, from the problems' sizes and the
+// recurrences' lines per CTA W.
+int build_tables(lns_batch3d* b) {
+  std::vector<int2> te, tc, tsx, tfx, ttx, tlx, tsy, tfy;
+  std::vector<int4> tp;
+  for (int p = 0; p < b->P; ++p) {
+    const Grid& g = b->ctx[p]->g;
+    const long long np = b->ctx[p]->np;
+    for (long long k = 0; k < (5 * np + 255) / 256; ++k) te.push_back(make_int2(p, (int)k));
+    for (int k = 0; k < (g.nx + g.ny + 127) / 128; ++k) tc.push_back(make_int2(p, k));
+    const int nbx = (g.nx + 127) / 128;
+    for (int by = 0; by < g.ny; ++by)
+      for (int bx = 0; bx < nbx; ++bx) tp.push_back(make_int4(p, bx, by, 0));
+    const long long nxp = (long long)(g.nx - 1) * g.ny, nyp = (long long)g.ny * g.nx;
+    for (long long k = 0; k < (nxp + 255) / 256; ++k) tsx.push_back(make_int2(p, (int)k));
+    for (int k = 0; k < (g.ny + b->W - 1) / b->W; ++k) tfx.push_back(make_int2(p, k));
+    for (int k = 0; k < g.ny; ++k) ttx.push_back(make_int2(p, k));
+    for (long long k = 0; k < ((long long)(g.nx - 1 - 3) * g.ny + 255) / 256; ++k) tlx.push_back(make_int2(p, (int)k));
+    for (long long k = 0; k < (nyp + 255) / 256; ++k) tsy.push_back(make_int2(p, (int)k));
+    for (int k = 0; k < (g.nx + b->W - 1) / b->W; ++k) tfy.push_back(make_int2(p, k));
+  }
+  int rc = upload_table(b, te, &b->t_elem, &b->n_elem);
+  if (!rc) rc = upload_table(b, tc, &b->t_col, &b->n_col);
+  if (!rc) rc = upload_table(b, tp, &b->t_pts, &b->n_pts);
+  if (!rc) rc = upload_table(b, tsx, &b->t_sx, &b->n_sx);
+  if (!rc) rc = upload_table(b, tfx, &b->t_fx, &b->n_fx);
+  if (!rc) rc = upload_table(b, ttx, &b->t_tx, &b->n_tx);
+  if (!rc) rc = upload_table(b, tlx, &b->t_lx, &b->n_lx);
+  if (!rc) rc = upload_table(b, tsy, &b->t_sy, &b->n_sy);
+  if (!rc) rc = upload_table(b, tfy, &b->t_fy, &b->n_fy);
+  return rc;
+}
+
+// One step of niter correctors of every active problem, enqueued on b->st.
+template <typename T, int W>
+int enqueue_step(lns_batch3d* b, int niter) {
+  namespace a3 = lns::a3;
+  namespace ch = lns::chain;
+  cudaStream_t st = b->st;
+  const size_t sm = ch::chain_smem_bytes<T>(W);
+  a3::copy_batch_kernel<<<b->n_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active);
+  a3::bc_batch_kernel<<<b->n_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active);
+  for (int it = 0; it < niter; ++it) {
+    a3::grad1_batch_kernel<<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active);
+    a3::rhs_batch_kernel<<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, b->mixed ? 1 : 0);
+    a3::resid_batch_kernel<<<b->P, 256, 0, st>>>(b->d_args, b->d_active, b->d_hist, b->d_step, b->P);
+    ch::scale_batch_kernel<T><<<b->n_sx, 256, 0, st>>>(b->d_ax, b->t_sx, b->d_active);
+    ch::chain_fwd_batch_kernel<T, true, W><<<b->n_fx, 32 * W, sm, st>>>(b->d_ax, b->t_fx, b->d_active);
+    ch::tail_batch_kernel<T><<<b->n_tx, 32 * ch::kTailWarps, 0, st>>>(b->d_ax, b->t_tx, b->d_active);
+    ch::fill_batch_kernel<T><<<b->n_lx, 256, 0, st>>>(b->d_ax, b->t_lx, b->d_active);
+    ch::chain_bwd_batch_kernel<T, true, W><<<b->n_fx, 32 * W, sm, st>>>(b->d_ax, b->t_fx, b->d_active);
+    ch::scale_batch_kernel<T><<<b->n_sy, 256, 0, st>>>(b->d_ay, b->t_sy, b->d_active);
+    ch::chain_fwd_batch_kernel<T, false, W><<<b->n_fy, 32 * W, sm, st>>>(b->d_ay, b->t_fy, b->d_active);
+    ch::chain_bwd_batch_kernel<T, false, W><<<b->n_fy, 32 * W, sm, st>>>(b->d_ay, b->t_fy, b->d_active);
+    a3::add_batch_kernel<T><<<b->n_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active);
+    a3::bc_batch_kernel<<<b->n_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active);
+  }
+  a3::step_incr_kernel<<<1, 1, 0, st>>>(b->d_step);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "batched step launch");
+}
+
+template <typename T>
+int enqueue_step_w(lns_batch3d* b, int niter) {
+  switch (b->W) {
+    case 1: return enqueue_step<T, 1>(b, niter);
+    case 2: return enqueue_step<T, 2>(b, niter);
+    case 4: return enqueue_step<T, 4>(b, niter);
+    default: return fail3(LNS_ERR_ARG, "batch: lines per CTA must be 1, 2 or 4");
+  }
+}
+
+// (Re)captures the step as a graph for the current W and niter.
+int capture(lns_batch3d* b, int niter) {
+  if (b->exec && b->exec_W == b->W && b->exec_niter == niter) return LNS_OK;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda3(e, "cudaStreamBeginCapture");
+  int rc = b->mixed ? enqueue_step_w<cf>(b, niter) : enqueue_step_w<cd>(b, niter);
+  e = cudaStreamEndCapture(b->st, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda3(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&b->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda3(e, "cudaGraphInstantiate");
+  b->exec_W = b->W;
+  b->exec_niter = niter;
+  return LNS_OK;
+}
+
+// Forms and factors the LHS of every problem not yet factored, and writes
+// the per-problem argument tables.
+int prepare(lns_batch3d* b) {
+  std::vector<lns::a3::StepArgs> args(b->P);
+  std::vector<lns::chain::Args> ax(b->P), ay(b->P);
+  for (int p = 0; p < b->P; ++p) {
+    lns_ctx3d* c = b->ctx[p];
+    if (!b->uploaded[p]) return fail3(LNS_ERR_ARG, "batch: problem " + std::to_string(p) + " not uploaded");
+    if (!c->factored) {
+      int rc = b->mixed ? factor_all<cf>(c, b->st) : factor_all<cd>(c, b->st);
+      if (rc) return rc;
+    }
+    lns::a3::StepArgs& a = args[p];
+    a.g = c->g;
+    a.o = c->ops;
+    a.v = c->v;
+    a.vold = c->vold;
+    a.c1v = c->c1v;
+    a.r64 = c->r64;
+    a.r32 = c->r32;
+    a.part = c->part;
+    a.nbx = (c->g.nx + 127) / 128;
+    a.nrhs = a.nbx * c->g.ny;
+    a.acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
+    void* r = b->mixed ? (void*)c->r32 : (void*)c->r64;
+    ax[p] = xargs(c, r);
+    ay[p] = yargs(c, r);
+  }
+  cudaError_t e = cudaMemcpy(b->d_args, args.data(), sizeof(args[0]) * b->P, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_ax, ax.data(), sizeof(ax[0]) * b->P, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_ay, ay.data(), sizeof(ay[0]) * b->P, cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "upload batch arguments");
+}
+
+int set_active(lns_batch3d* b) {
+  cudaError_t e = cudaMemcpyAsync(b->d_active, b->active.data(), sizeof(int) * b->P, cudaMemcpyHostToDevice, b->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "upload active flags");
+}
+
+int reserve_hist(lns_batch3d* b, long long steps) {
+  if (steps <= b->hist_cap) return LNS_OK;
+  void* q = nullptr;
+  int rc = balloc(b, sizeof(double) * (size_t)steps * b->P, &q);
+  if (rc) return rc;
+  b->d_hist = (double*)q;
+  b->hist_cap = steps;
+  if (b->exec) {  // the graph holds the old history pointer
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return LNS_OK;
+}
+
+void destroy_batch(lns_batch3d* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (void* p : b->allocs) cudaFree(p);
+  for (lns_ctx3d* c : b->ctx) lns_ctx3d_destroy(c);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** out) {
+  if (!params || !out || nprob < 1) return fail3(LNS_ERR_ARG, "batch3d_create: need nprob >= 1 and parameters");
+  *out = nullptr;
+  for (int p = 1; p < nprob; ++p)
+    if (params[p].precision != params[0].precision)
+      return fail3(LNS_ERR_ARG, "batch3d_create: every problem must use the same precision");
+  lns_batch3d* b = new lns_batch3d();
+  b->P = nprob;
+  b->mixed = params[0].precision == LNS_MIXED;
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda3(e, "cudaGetDevice");
+  }
+  int rc = LNS_OK;
+  for (int p = 0; p < nprob && !rc; ++p) {
+    lns_ctx3d* c = nullptr;
+    rc = lns_ctx3d_create(&params[p], &c);
+    if (!rc) {
+      b->ctx.push_back(c);
+      b->bytes += lns_ctx3d_bytes(c);
+    }
+  }
+  void* q = nullptr;
+  if (!rc) {
+    e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda3(e, "cudaStreamCreate");
+  }
+  if (!rc) rc = balloc(b, sizeof(lns::a3::StepArgs) * nprob, &q), b->d_args = (lns::a3::StepArgs*)q;
+  if (!rc) rc = balloc(b, sizeof(lns::chain::Args) * nprob, &q), b->d_ax = (lns::chain::Args*)q;
+  if (!rc) rc = balloc(b, sizeof(lns::chain::Args) * nprob, &q), b->d_ay = (lns::chain::Args*)q;
+  if (!rc) rc = balloc(b, sizeof(int) * nprob, &q), b->d_active = (int*)q;
+  if (!rc) rc = balloc(b, sizeof(int), &q), b->d_step = (int*)q;
+  if (!rc) rc = reserve_hist(b, 64);
+  if (!rc) rc = build_tables(b);
+  if (rc) {
+    destroy_batch(b);
+    return rc;
+  }
+  b->active.assign(nprob, 1);
+  b->uploaded.assign(nprob, false);
+  *out = b;
+  return LNS_OK;
+}
+
+int lns_batch3d_destroy(lns_batch3d* b) {
+  if (b) destroy_batch(b);
+  return LNS_OK;
+}
+
+size_t lns_batch3d_bytes(const lns_batch3d* b) { return b ? b->bytes : 0; }
+
+int lns_batch3d_upload(lns_batch3d* b, int32_t prob, const double* metrics, const double* vm, const double* v) {
+  if (!b || !metrics || !vm || !v) return fail3(LNS_ERR_ARG, "batch3d_upload: null argument");
+  if (prob < 0 || prob >= b->P) return fail3(LNS_ERR_ARG, "batch3d_upload: problem index out of range");
+  lns_ctx3d* c = b->ctx[prob];
+  int rc = lns_upload_metrics3d(c, metrics);
+  if (!rc) rc = lns_upload_mean3d(c, vm, nullptr);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->v, v, sizeof(cd) * 5 * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload v");
+  b->uploaded[prob] = true;
+  return LNS_OK;
+}
+
+int lns_batch3d_get_state(lns_batch3d* b, int32_t prob, double* v) {
+  if (!b || !v) return fail3(LNS_ERR_ARG, "batch3d_get_state: null argument");
+  if (prob < 0 || prob >= b->P) return fail3(LNS_ERR_ARG, "batch3d_get_state: problem index out of range");
+  lns_ctx3d* c = b->ctx[prob];
+  cudaError_t e = cudaStreamSynchronize(b->st);
+  if (e == cudaSuccess) e = cudaMemcpy(v, c->v, sizeof(cd) * 5 * c->np, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "download v");
+}
+
+int lns_batch3d_run(lns_batch3d* b, int32_t max_steps, int32_t niter, double tol, int32_t check_every,
+                    int32_t* steps, double* final_res) {
+  if (!b || !steps || !final_res) return fail3(LNS_ERR_ARG, "batch3d_run: null argument");
+  if (max_steps < 0 || niter < 1 || check_every < 1) return fail3(LNS_ERR_ARG, "batch3d_run: bad step counts");
+  int rc = check_device(b->ctx[0]);
+  if (!rc) rc = prepare(b);
+  if (!rc) rc = reserve_hist(b, max_steps);
+  if (!rc) rc = capture(b, niter);
+  if (rc) return rc;
+  for (int p = 0; p < b->P; ++p) {
+    b->active[p] = 1;
+    steps[p] = -1;
+    final_res[p] = -1.0;
+  }
+  rc = set_active(b);
+  if (rc) return rc;
+  cudaError_t e = cudaMemsetAsync(b->d_step, 0, sizeof(int), b->st);
+  if (e != cudaSuccess) return cuda3(e, "cudaMemsetAsync");
+  std::vector<double> hist;
+  int done = 0;
+  while (done < max_steps) {
+    const int n = std::min(check_every, max_steps - done);
+    for (int s = 0; s < n; ++s) {
+      e = cudaGraphLaunch(b->exec, b->st);
+      if (e != cudaSuccess) return cuda3(e, "cudaGraphLaunch");
+    }
+    hist.resize((size_t)n * b->P);
+    e = cudaMemcpyAsync(hist.data(), b->d_hist + (size_t)done * b->P, sizeof(double) * hist.size(),
+                        cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) return cuda3(e, "batched steps");
+    int left = 0;
+    for (int p = 0; p < b->P; ++p) {
+      if (!b->active[p]) continue;
+      for (int s = 0; s < n; ++s) {
+        final_res[p] = hist[(size_t)s * b->P + p];
+        if (final_res[p] <= tol) {
+          // converged at step done + s + 1; later steps of this check ran
+          // before the flag changed, so keep the first crossing
+          steps[p] = done + s + 1;
+          b->active[p] = 0;
+          break;
+        }
+      }
+      left += b->active[p];
+    }
+    done += n;
+    if (!left) break;
+    rc = set_active(b);
+    if (rc) return rc;
+  }
+  return LNS_OK;
+}
+
+int lns_batch3d_tune(lns_batch3d* b, int32_t niter, int32_t* lines_per_cta) {
+  if (!b || !lines_per_cta || niter < 1) return fail3(LNS_ERR_ARG, "batch3d_tune: bad argument");
+  int rc = check_device(b->ctx[0]);
+  if (!rc) rc = prepare(b);
+  if (rc) return rc;
+  // keep the states: tuning steps run on copies that are restored after
+  std::vector<void*> save(b->P, nullptr);
+  for (int p = 0; p < b->P && !rc; ++p) {
+    cudaError_t e = cudaMalloc(&save[p], sizeof(cd) * 5 * b->ctx[p]->np + 3 * sizeof(double));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(save[p], b->ctx[p]->v, sizeof(cd) * 5 * b->ctx[p]->np, cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy((char*)save[p] + sizeof(cd) * 5 * b->ctx[p]->np, b->ctx[p]->dscal, 3 * sizeof(double),
+                     cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) rc = cuda3(e, "tune: save states");
+  }
+  int best = b->W;
+  float best_ms = 1e30f;
+  const int cands[3] = {1, 2, 4};
+  if (!rc) rc = reserve_hist(b, 16);
+  for (int k = 0; k < 3 && !rc; ++k) {
+    b->W = cands[k];
+    rc = build_tables(b);
+    if (!rc) rc = capture(b, niter);
+    if (rc) break;
+    b->active.assign(b->P, 1);
+    rc = set_active(b);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int rep = 0; rep < 2 && !rc; ++rep) {  // warm-up, then timed
+      cudaMemsetAsync(b->d_step, 0, sizeof(int), b->st);
+      cudaEventRecord(e0, b->st);
+      for (int s = 0; s < 4; ++s) cudaGraphLaunch(b->exec, b->st);
+      cudaEventRecord(e1, b->st);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) rc = cuda3(e, "tune: timed steps");
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc && ms < best_ms) best_ms = ms, best = cands[k];
+  }
+  for (int p = 0; p < b->P; ++p) {
+    if (!save[p]) continue;
+    if (!rc) {
+      cudaError_t e = cudaMemcpy(b->ctx[p]->v, save[p], sizeof(cd) * 5 * b->ctx[p]->np, cudaMemcpyDeviceToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(b->ctx[p]->dscal, (char*)save[p] + sizeof(cd) * 5 * b->ctx[p]->np, 3 * sizeof(double),
+                       cudaMemcpyDeviceToDevice);
+      if (e != cudaSuccess) rc = cuda3(e, "tune: restore states");
+    }
+    cudaFree(save[p]);
+  }
+  if (rc) return rc;
+  b->W = best;
+  rc = build_tables(b);
+  if (!rc && b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  *lines_per_cta = best;
+  return rc;
 }
 
 }  // extern "C"

@@ -252,10 +252,11 @@ __global__ void __launch_bounds__(32 * kPrepWarps) prep_fill_kernel(Args a) {
 }
 
 // ------------------------------------------------------------ the sweeps
-// s = D^-1 r in place, one thread per record of rows 1..n.
+// s = D^-1 r in place, one thread per record of rows 1..n; bx is the block
+// index within the problem.
 template <typename T>
-__global__ void scale_kernel(Args a) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void scale_body(const Args& a, long long bx) {
+  const long long t = bx * blockDim.x + threadIdx.x;
   if (t >= (long long)a.n * a.nsys) return;
   int i, iv;
   if (a.row_stride == 1) i = (int)(t % a.n) + 1, iv = (int)(t / a.n);
@@ -276,16 +277,28 @@ __global__ void scale_kernel(Args a) {
 #pragma unroll
   for (int k = 0; k < 5; ++k) r[k] = s[k];
 }
+template <typename T>
+__global__ void scale_kernel(Args a) { scale_body<T>(a, blockIdx.x); }
+
+// Work tables of the batched launches: block b of a batched launch runs
+// block y of problem x (several problems in one launch, one ADI phase).
+template <typename T>
+__global__ void scale_batch_kernel(const Args* __restrict__ list, const int2* __restrict__ table,
+                                   const int* __restrict__ active) {
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  scale_body<T>(list[w.x], w.y);
+}
 
 template <typename T> struct ChainCfg;
 template <> struct ChainCfg<cd> { static constexpr int kAhead = 12; };
 template <> struct ChainCfg<cf> { static constexpr int kAhead = 24; };
-constexpr int kChainWarps = 2;                 // lines per CTA
+constexpr int kChainWarps = 2;                 // lines per CTA of the single-problem launches
 constexpr int kStage = 55;                     // 50 block entries + 5 right-hand-side entries
 
 template <typename T>
-constexpr size_t chain_smem_bytes() {
-  return (size_t)kChainWarps * (ChainCfg<T>::kAhead + 1) * kStage * sizeof(T);
+constexpr size_t chain_smem_bytes(int lines_per_cta = kChainWarps) {
+  return (size_t)lines_per_cta * (ChainCfg<T>::kAhead + 1) * kStage * sizeof(T);
 }
 
 // sum over q of lane (m,q)'s partial, for m = this lane's q
@@ -315,12 +328,11 @@ __device__ __forceinline__ void chain_stage(T* slot, const Args& a, int r, int i
 
 // Forward recurrence yh_i = s_i - sum_c F_ic yh_c over rows 1..top (top = n,
 // or n-2 for periodic lines whose rows n-1, n follow in tail_kernel).
-template <typename T, bool PER>
-__global__ void __launch_bounds__(32 * kChainWarps) chain_fwd_kernel(Args a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+template <typename T, bool PER, int W>
+__device__ __forceinline__ void chain_fwd_body(const Args& a, int bx, unsigned char* smem_raw) {
   constexpr int kAhead = ChainCfg<T>::kAhead, kRing = kAhead + 1;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int iv = blockIdx.x * kChainWarps + warp;
+  const int iv = bx * W + warp;
   if (iv >= a.nsys) return;
   T* ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
   const int n = a.n, top = PER ? n - 2 : n;
@@ -367,12 +379,11 @@ __global__ void __launch_bounds__(32 * kChainWarps) chain_fwd_kernel(Args a) {
 // Backward recurrence x_i = c_i - sum_c B_ic x_c from row top down to 1
 // (top = n; periodic: n-2, with x_{n-1}, x_n from tail_kernel and c_i from
 // fill_kernel; row np then repeats row 1).
-template <typename T, bool PER>
-__global__ void __launch_bounds__(32 * kChainWarps) chain_bwd_kernel(Args a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+template <typename T, bool PER, int W>
+__device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned char* smem_raw) {
   constexpr int kAhead = ChainCfg<T>::kAhead, kRing = kAhead + 1;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int iv = blockIdx.x * kChainWarps + warp;
+  const int iv = bx * W + warp;
   if (iv >= a.nsys) return;
   T* ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
   const int n = a.n, top = PER ? n - 2 : n;
@@ -426,16 +437,44 @@ __global__ void __launch_bounds__(32 * kChainWarps) chain_bwd_kernel(Args a) {
   cp_async_wait<0>();
 }
 
+template <typename T, bool PER, int W = kChainWarps>
+__global__ void __launch_bounds__(32 * W) chain_fwd_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  chain_fwd_body<T, PER, W>(a, blockIdx.x, smem_raw);
+}
+template <typename T, bool PER, int W = kChainWarps>
+__global__ void __launch_bounds__(32 * W) chain_bwd_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  chain_bwd_body<T, PER, W>(a, blockIdx.x, smem_raw);
+}
+template <typename T, bool PER, int W>
+__global__ void __launch_bounds__(32 * W) chain_fwd_batch_kernel(const Args* __restrict__ list,
+                                                                 const int2* __restrict__ table,
+                                                                 const int* __restrict__ active) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  chain_fwd_body<T, PER, W>(list[w.x], w.y, smem_raw);
+}
+template <typename T, bool PER, int W>
+__global__ void __launch_bounds__(32 * W) chain_bwd_batch_kernel(const Args* __restrict__ list,
+                                                                 const int2* __restrict__ table,
+                                                                 const int* __restrict__ active) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  chain_bwd_body<T, PER, W>(list[w.x], w.y, smem_raw);
+}
+
 // Periodic lines, after the forward recurrence: the fill sums
 // t1 = sum_{c<=n-4} K1_c yh_c, t0 = sum_{c<=n-3} K0_c yh_c, rows n-1 and n of
 // both recurrences, and x_{n-1}, x_n into the right-hand side.  One CTA of
 // kTailWarps warps per line.
 constexpr int kTailWarps = 8;
 template <typename T>
-__global__ void __launch_bounds__(32 * kTailWarps) tail_kernel(Args a) {
+__device__ __forceinline__ void tail_body(const Args& a, int iv) {
   __shared__ T red[2][kTailWarps][25];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int iv = blockIdx.x;
   const int n = a.n;
   const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
   T* grhs = reinterpret_cast<T*>(a.rhs);
@@ -480,11 +519,22 @@ __global__ void __launch_bounds__(32 * kTailWarps) tail_kernel(Args a) {
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(32 * kTailWarps) tail_kernel(Args a) { tail_body<T>(a, blockIdx.x); }
+template <typename T>
+__global__ void __launch_bounds__(32 * kTailWarps) tail_batch_kernel(const Args* __restrict__ list,
+                                                                    const int2* __restrict__ table,
+                                                                    const int* __restrict__ active) {
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  tail_body<T>(list[w.x], w.y);
+}
+
 // Periodic lines: c_i = yh_i - E1_i x_{n-1} - E0_i x_n for rows 1..n-3, one
 // thread per record.
 template <typename T>
-__global__ void fill_kernel(Args a) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void fill_body(const Args& a, long long bx) {
+  const long long t = bx * blockDim.x + threadIdx.x;
   const int rows = a.n - 3;
   if (t >= (long long)rows * a.nsys) return;
   int i, iv;
@@ -508,6 +558,16 @@ __global__ void fill_kernel(Args a) {
     for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[25 + mm + 5 * k], xn0[k]);
     r[mm] = acc;
   }
+}
+
+template <typename T>
+__global__ void fill_kernel(Args a) { fill_body<T>(a, blockIdx.x); }
+template <typename T>
+__global__ void fill_batch_kernel(const Args* __restrict__ list, const int2* __restrict__ table,
+                                  const int* __restrict__ active) {
+  const int2 w = table[blockIdx.x];
+  if (!active[w.x]) return;
+  fill_body<T>(list[w.x], w.y);
 }
 
 }  // namespace chain

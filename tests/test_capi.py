@@ -43,7 +43,7 @@ def test_python_signatures_cover_header():
 
     solver_syms = [n for n in declared_symbols()
                    if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops",
-                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes")]
+                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes", "lns_batch3d_bytes")]
     assert sorted(SIGNATURES) == solver_syms
 
 
@@ -173,3 +173,16 @@ def test_ctx2d_null_arguments(lib):
     assert lib.lns_get_field2d(None, 0, None) == 1
     assert lib.lns_ctx2d_destroy(None) == 0
     assert lib.lns_ctx2d_bytes(None) == 0
+
+
+def test_batch3d_argument_errors(lib):
+    assert lib.lns_batch3d_create(0, None, None) == 1
+    bad = (type(_params3d()) * 2)(_params3d(), _params3d(precision=1))
+    b = ctypes.c_void_p()
+    assert lib.lns_batch3d_create(2, bad, ctypes.byref(b)) == 1 and not b.value
+    assert lib.lns_batch3d_upload(None, 0, None, None, None) == 1
+    assert lib.lns_batch3d_tune(None, 1, None) == 1
+    assert lib.lns_batch3d_run(None, 1, 1, 1e-10, 1, None, None) == 1
+    assert lib.lns_batch3d_get_state(None, 0, None) == 1
+    assert lib.lns_batch3d_destroy(None) == 0
+    assert lib.lns_batch3d_bytes(None) == 0
