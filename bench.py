@@ -524,6 +524,75 @@ def run_batch(torch, with_cpu, max_steps=2000, tol=1e-10):
     return out
 
 
+def serve_stream(n, rate=50.0, seed=5):
+    """The served stream: n linearised solve requests with Poisson arrivals
+    at `rate` per second, beta ~ U[0, 0.5], omega ~ U[0.01, 0.15], nx and ny
+    log-uniform in [64, 1024] x [64, 512] (multiples of 16), tolerance 1e-10;
+    the shear-layer mean flow of the other legs on each request's grid."""
+    import numpy as np
+
+    from lns3d_gb300.cases import shear_layer
+
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for k in range(n):
+        nx = int(np.clip(16 * round(np.exp(rng.uniform(np.log(64), np.log(1024))) / 16), 64, 1024))
+        ny = int(np.clip(16 * round(np.exp(rng.uniform(np.log(64), np.log(512))) / 16), 64, 512))
+        reqs.append((float(t[k]), nx, ny, float(rng.uniform(0.0, 0.5)), float(rng.uniform(0.01, 0.15)), k))
+    return reqs
+
+
+def run_serve(torch, n_requests=100, rate=50.0, tol=1e-10, max_steps=2000, serial_sample=3):
+    """The serving leg: a prefix of the stream through lns_server3d (mixed
+    precision, continuous batching, 64 slots, 64 GiB budget) in real time,
+    and a sample of the same requests solved one at a time by the FP64
+    drop-in step, for the serial comparison."""
+    import numpy as np
+
+    import lns3d_gb300 as g
+    from lns3d_gb300.cases import shear_layer
+
+    reqs = serve_stream(n_requests, rate)
+    cases = [shear_layer(nx=nx, ny=ny, beta=beta, omega=omega, seed=k) for _, nx, ny, beta, omega, k in reqs]
+    srv = g.Server3D(64 << 30, max_slots=64, precision=g.adi3d.MIXED)
+    pending = [(r[0], c) for r, c in zip(reqs, cases)]
+    ids = []
+    t0 = time.perf_counter()
+    while pending or any(srv.poll(i)["state"] in ("queued", "running") for i in ids):
+        now = time.perf_counter() - t0
+        while pending and pending[0][0] <= now:
+            ids.append(srv.submit(pending.pop(0)[1], tol=tol, max_steps=max_steps, cflmax=CFL3))
+        running, queued = srv.tick(25)
+        if not running and not queued and pending:
+            time.sleep(max(0.0, pending[0][0] - (time.perf_counter() - t0)))
+    wall = time.perf_counter() - t0
+    polls = [srv.poll(i) for i in ids]
+    lat = np.array(sorted(p["latency_s"] for p in polls))
+    done = sum(p["state"] == "done" for p in polls)
+    srv.close()
+    # serial FP64 drop-in solves of the first requests of the stream
+    ser = []
+    for c in cases[:serial_sample]:
+        d = g.ImpDrv3D(c["params"], c["metrics"], c["vm"], cflmax=CFL3, loctime=1, precision=g.adi3d.FP64)
+        v = torch.from_numpy(c["v"].ravel(order="F")).cuda()
+        res = torch.zeros(max_steps, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        steps = 0
+        while steps < max_steps:
+            d.step(v, nsteps=25, totres=res[steps:])
+            steps += 25
+            if float(res[steps - 1].item()) <= tol:
+                break
+        ser.append(time.perf_counter() - ts)
+    return {"workload": "serve-%d-of-1000-requests-poisson-%g-per-s-mixed-to-1e-10" % (n_requests, rate),
+            "requests": n_requests, "converged": int(done), "wall_s": wall, "solves_per_s": n_requests / wall,
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "serial_fp64": {"sample": serial_sample, "mean_solve_s": float(np.mean(ser)),
+                            "solves_per_s": 1.0 / float(np.mean(ser))}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -536,6 +605,8 @@ def main():
     ap.add_argument("--no-isolated", action="store_true", help="skip the isolated batched-solve leg")
     ap.add_argument("--no-2d", action="store_true", help="skip the nonlinear 2D step leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-problem leg")
+    ap.add_argument("--serve-requests", type=int, default=100,
+                    help="requests of the served stream to run (the stream has 1000); 0 skips the leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -664,6 +735,10 @@ def main():
     if not args.no_batch:
         legb = run_batch(torch, rank == 0 and not args.no_cpu_baseline)
 
+    legs = None
+    if args.serve_requests > 0:
+        legs = run_serve(torch, n_requests=args.serve_requests)
+
     leg2d = None
     if not args.no_2d:
         leg2d = run_impdrv2d(torch, dev, max(10, K), rank == 0 and not args.no_cpu_baseline)
@@ -696,6 +771,7 @@ def main():
             "isolated_solve": iso,
             "impdrv2d": leg2d,
             "batch": legb,
+            "serve": legs,
             "gpu_launches": KERNELS_PER_STEP * K,
             "clocks": clocks,
         }

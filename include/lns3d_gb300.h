@@ -352,13 +352,47 @@ int lns_batch3d_upload(lns_batch3d* batch, int32_t prob, const double* metrics, 
  * steps of each; the problems' states are restored afterwards. */
 int lns_batch3d_tune(lns_batch3d* batch, int32_t niter, int32_t* lines_per_cta);
 /* Steps every problem until its residual (resstat3D, the last corrector of
- * a step) is <= tol, or max_steps steps.  Residuals are checked every
- * check_every steps; a converged problem stops stepping at that check.
- * steps[prob] = the first step whose residual was <= tol (-1 if none),
- * final_res[prob] = its residual at the stop. */
+ * a step) is <= tol (tol > 0), or max_steps steps.  A problem stops on the
+ * device in the step whose residual reaches tol: its state stays the one
+ * whose residual met the tolerance, whatever check_every (how often the host
+ * reads the residuals) and the other problems are.  steps[prob] = that step
+ * (-1 if none), final_res[prob] = the last residual measured. */
 int lns_batch3d_run(lns_batch3d* batch, int32_t max_steps, int32_t niter, double tol, int32_t check_every,
                     int32_t* steps, double* final_res);
 int lns_batch3d_get_state(lns_batch3d* batch, int32_t prob, double* v);
+
+/* ---------------------------------------------------------------------------
+ * Serving (no reference counterpart).  A server keeps every admitted
+ * request's operators, factors and state resident on the device and
+ * advances all of them as one batch; requests that arrive while others are
+ * running are admitted at the next tick when a slot and device memory
+ * (budget_bytes) are free, and leave the batch when their residual reaches
+ * their tolerance (the state is then the one that met it, as in
+ * lns_batch3d_run) or after max_steps steps.  A request's result is
+ * independent of the other requests in the batch.  Not thread-safe: one
+ * host thread drives a server.
+ */
+#define LNS_REQ_QUEUED 1
+#define LNS_REQ_RUNNING 2
+#define LNS_REQ_DONE 3      /* converged: residual <= tol */
+#define LNS_REQ_STOPPED 4   /* max_steps reached first */
+#define LNS_REQ_FAILED 5    /* could not be admitted (allocation or upload failed) */
+typedef struct lns_server3d lns_server3d;
+int lns_server3d_create(size_t budget_bytes, int32_t max_slots, int32_t precision, int32_t niter,
+                        lns_server3d** server);
+int lns_server3d_destroy(lns_server3d* server);
+/* copies the request's host arrays (as lns_batch3d_upload); *id names it */
+int lns_server3d_submit(lns_server3d* server, const lns_params3d* params, const double* metrics, const double* vm,
+                        const double* v, double tol, int32_t max_steps, int64_t* id);
+/* admits what fits, runs nsteps batched steps, retires finished requests */
+int lns_server3d_tick(lns_server3d* server, int32_t nsteps, int32_t* running, int32_t* queued);
+/* state LNS_REQ_*, the step that met tol (or steps run), the last residual,
+ * and the seconds from submission to completion (-1 while unfinished) */
+int lns_server3d_poll(lns_server3d* server, int64_t id, int32_t* state, int32_t* steps, double* res,
+                      double* latency_s);
+/* the finished request's state v(5,nx,ny) complex; forgets the request */
+int lns_server3d_fetch(lns_server3d* server, int64_t id, double* v);
+size_t lns_server3d_bytes_in_use(const lns_server3d* server);
 
 #ifdef __cplusplus
 }

@@ -71,6 +71,12 @@ SIGNATURES = {
     "lns_batch3d_tune": [P, I32, P],
     "lns_batch3d_run": [P, I32, I32, ctypes.c_double, I32, P, P],
     "lns_batch3d_get_state": [P, I32, DP],
+    "lns_server3d_create": [ctypes.c_size_t, I32, I32, I32, P],
+    "lns_server3d_destroy": [P],
+    "lns_server3d_submit": [P, P, DP, DP, DP, ctypes.c_double, I32, P],
+    "lns_server3d_tick": [P, I32, P, P],
+    "lns_server3d_poll": [P, ctypes.c_int64, P, P, P, P],
+    "lns_server3d_fetch": [P, ctypes.c_int64, DP],
     "lns_ctx2d_create": [P, P],
     "lns_ctx2d_destroy": [P],
     "lns_upload_metrics2d": [P, DP],
@@ -121,6 +127,8 @@ def lib():
         L.lns_mixed_workspace_bytes.argtypes = [I32, I32, I32, I32]
         L.lns_ctx3d_bytes.restype = ctypes.c_size_t
         L.lns_ctx3d_bytes.argtypes = [P]
+        L.lns_server3d_bytes_in_use.restype = ctypes.c_size_t
+        L.lns_server3d_bytes_in_use.argtypes = [P]
         L.lns_batch3d_bytes.restype = ctypes.c_size_t
         L.lns_batch3d_bytes.argtypes = [P]
         L.lns_ctx2d_bytes.restype = ctypes.c_size_t

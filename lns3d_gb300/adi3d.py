@@ -223,3 +223,76 @@ class Batch3D:
             self.close()
         except Exception:
             pass
+
+
+REQ_STATES = {1: "queued", 2: "running", 3: "done", 4: "stopped", 5: "failed"}
+
+
+class Server3D:
+    """Continuous batching of linearised solves (lns_server3d_* of the C ABI).
+
+    Requests are submitted at any time; each tick admits what fits in the
+    device-memory budget and the free slots, advances every running request
+    by nsteps batched steps, and retires the ones whose residual reached
+    their tolerance (their state is the one that met it) or that ran out of
+    steps.  A request's result does not depend on the other requests.
+    """
+
+    def __init__(self, budget_bytes, max_slots=64, precision=MIXED, niter=1):
+        self.precision = precision
+        self._s = ctypes.c_void_p()
+        check(lib().lns_server3d_create(ctypes.c_size_t(int(budget_bytes)), max_slots, precision, niter,
+                                        ctypes.byref(self._s)), "lns_server3d_create")
+        self._shape = {}
+
+    def submit(self, problem, tol=1e-10, max_steps=2000, cflmax=1.0, dtmax=1e30, loctime=1, res_compat=False):
+        p = problem["params"]
+        prm = Params3D(nx=p["nx"], ny=p["ny"], dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
+                       gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax,
+                       loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"], wall=p["wall"],
+                       wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"], precision=self.precision,
+                       res_compat=1 if res_compat else 0)
+        nx, ny = int(p["nx"]), int(p["ny"])
+        m = np.empty((nx, ny, 10), order="F")
+        for i, name in enumerate(METRICS):
+            m[:, :, i] = problem["metrics"][name]
+        vm = np.asfortranarray(problem["vm"], dtype=np.float64)
+        v = np.asfortranarray(problem["v"], dtype=np.complex128)
+        rid = ctypes.c_int64()
+        check(lib().lns_server3d_submit(self._s, ctypes.byref(prm), ctypes.c_void_p(m.ctypes.data),
+                                        ctypes.c_void_p(vm.ctypes.data), ctypes.c_void_p(v.ctypes.data), tol,
+                                        max_steps, ctypes.byref(rid)), "lns_server3d_submit")
+        self._shape[rid.value] = (5, nx, ny)
+        return rid.value
+
+    def tick(self, nsteps=25):
+        run, que = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().lns_server3d_tick(self._s, nsteps, ctypes.byref(run), ctypes.byref(que)), "lns_server3d_tick")
+        return run.value, que.value
+
+    def poll(self, rid):
+        st, steps, res, lat = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double(), ctypes.c_double()
+        check(lib().lns_server3d_poll(self._s, rid, ctypes.byref(st), ctypes.byref(steps), ctypes.byref(res),
+                                      ctypes.byref(lat)), "lns_server3d_poll")
+        return {"state": REQ_STATES.get(st.value, st.value), "steps": steps.value, "res": res.value,
+                "latency_s": lat.value}
+
+    def fetch(self, rid):
+        v = np.zeros(self._shape.pop(rid), np.complex128, order="F")
+        check(lib().lns_server3d_fetch(self._s, rid, ctypes.c_void_p(v.ctypes.data)), "lns_server3d_fetch")
+        return v
+
+    @property
+    def bytes_in_use(self):
+        return lib().lns_server3d_bytes_in_use(self._s)
+
+    def close(self):
+        if self._s:
+            lib().lns_server3d_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -14,7 +14,10 @@
 // RHS, residual and update stay FP64.
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cmath>
+#include <deque>
+#include <map>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -547,6 +550,7 @@ struct StepArgs {
   double* part;  // RHS block partials
   int nbx, nrhs;  // RHS blocks along x, partial count
   double* acc;   // running residual of the reference mode, or null
+  double tol;    // the problem stops (active = 0) at the first residual <= tol; 0: never
 };
 
 __global__ void copy_batch_kernel(const StepArgs* __restrict__ list, const int2* __restrict__ table,
@@ -579,8 +583,11 @@ __global__ void __launch_bounds__(128) rhs_batch_kernel(const StepArgs* __restri
   rhs_body(a.g, a.o, a.v, a.vold, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr, a.part, w.y, w.z, a.nbx);
 }
 // residual of each problem into hist[step * P + p] (src/resstat3d.f90:37-60)
-__global__ void resid_batch_kernel(const StepArgs* __restrict__ list, const int* __restrict__ active,
-                                   double* __restrict__ hist, const int* __restrict__ step, int P) {
+// A problem whose residual reaches its tolerance is switched off here, so
+// the rest of this step and later steps leave its state as it was when the
+// residual was measured.
+__global__ void resid_batch_kernel(const StepArgs* __restrict__ list, int* active, double* __restrict__ hist,
+                                   const int* __restrict__ step, int P) {
   __shared__ double red[256];
   const int p = blockIdx.x;
   if (!active[p]) return;
@@ -598,6 +605,7 @@ __global__ void resid_batch_kernel(const StepArgs* __restrict__ list, const int*
     const double r = sqrt(tot / (double)a.o.np);
     hist[(long long)(*step) * P + p] = r;
     if (a.acc) *a.acc = r;
+    if (a.tol > 0.0 && r <= a.tol) active[p] = 0;
   }
 }
 template <typename RT>
@@ -1153,6 +1161,8 @@ int lns_get_field3d(lns_ctx3d* c, int32_t which, double* out) {
 // ======================================================================
 struct lns_batch3d {
   int P = 0;
+  int cap = 0;            // problems the per-problem device arrays hold
+  bool owns_ctx = true;   // a server's batch borrows its requests' contexts
   bool mixed = false;
   int device = -1;
   int W = lns::chain::kChainWarps;  // lines per CTA of the recurrences
@@ -1165,13 +1175,14 @@ struct lns_batch3d {
   int* d_active = nullptr;
   int* d_step = nullptr;
   double* d_hist = nullptr;
-  long long hist_cap = 0;  // steps
+  long long hist_cap = 0;  // entries (steps x problems)
   int2 *t_elem = nullptr, *t_col = nullptr, *t_sx = nullptr, *t_fx = nullptr, *t_tx = nullptr, *t_lx = nullptr,
        *t_sy = nullptr, *t_fy = nullptr;
   int4* t_pts = nullptr;
   int n_elem = 0, n_col = 0, n_sx = 0, n_fx = 0, n_tx = 0, n_lx = 0, n_sy = 0, n_fy = 0, n_pts = 0;
   cudaGraphExec_t exec = nullptr;
   int exec_W = 0, exec_niter = 0;
+  std::vector<void*> table_allocs;  // freed when the tables are rebuilt
   std::vector<int> active;
   std::vector<bool> uploaded;
 };
@@ -1192,8 +1203,9 @@ int balloc(lns_batch3d* b, size_t bytes, void** out) {
 template <typename E>
 int upload_table(lns_batch3d* b, const std::vector<E>& h, E** d, int* n) {
   void* q = nullptr;
-  int rc = balloc(b, sizeof(E) * std::max<size_t>(h.size(), 1), &q);
-  if (rc) return rc;
+  cudaError_t ea = cudaMalloc(&q, sizeof(E) * std::max<size_t>(h.size(), 1));
+  if (ea != cudaSuccess) return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(ea));
+  b->table_allocs.push_back(q);
   cudaError_t e = cudaMemcpy(q, h.data(), sizeof(E) * h.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda3(e, "upload work table");
   *d = (E*)q;
@@ -1204,6 +1216,12 @@ int upload_table(lns_batch3d* b, const std::vector<E>& h, E** d, int* n) {
 // The work tables of every phase, from the problems' sizes and the
 // recurrences' lines per CTA W.
 int build_tables(lns_batch3d* b) {
+  if (b->exec) {  // the captured step refers to the tables being replaced
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  for (void* q : b->table_allocs) cudaFree(q);
+  b->table_allocs.clear();
   std::vector<int2> te, tc, tsx, tfx, ttx, tlx, tsy, tfy;
   std::vector<int4> tp;
   for (int p = 0; p < b->P; ++p) {
@@ -1300,7 +1318,7 @@ int capture(lns_batch3d* b, int niter) {
 
 // Forms and factors the LHS of every problem not yet factored, and writes
 // the per-problem argument tables.
-int prepare(lns_batch3d* b) {
+int prepare(lns_batch3d* b, double tol) {
   std::vector<lns::a3::StepArgs> args(b->P);
   std::vector<lns::chain::Args> ax(b->P), ay(b->P);
   for (int p = 0; p < b->P; ++p) {
@@ -1322,6 +1340,7 @@ int prepare(lns_batch3d* b) {
     a.nbx = (c->g.nx + 127) / 128;
     a.nrhs = a.nbx * c->g.ny;
     a.acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
+    a.tol = tol;
     void* r = b->mixed ? (void*)c->r32 : (void*)c->r64;
     ax[p] = xargs(c, r);
     ay[p] = yargs(c, r);
@@ -1332,19 +1351,46 @@ int prepare(lns_batch3d* b) {
   return e == cudaSuccess ? LNS_OK : cuda3(e, "upload batch arguments");
 }
 
+// Per-problem device arrays for at least n problems.
+int reserve_problems(lns_batch3d* b, int n) {
+  if (n <= b->cap) return LNS_OK;
+  void* q = nullptr;
+  int rc = balloc(b, sizeof(lns::a3::StepArgs) * n, &q);
+  if (!rc) b->d_args = (lns::a3::StepArgs*)q, rc = balloc(b, sizeof(lns::chain::Args) * n, &q);
+  if (!rc) b->d_ax = (lns::chain::Args*)q, rc = balloc(b, sizeof(lns::chain::Args) * n, &q);
+  if (!rc) b->d_ay = (lns::chain::Args*)q, rc = balloc(b, sizeof(int) * n, &q);
+  if (!rc) b->d_active = (int*)q, b->cap = n;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return rc;
+}
+
 int set_active(lns_batch3d* b) {
   cudaError_t e = cudaMemcpyAsync(b->d_active, b->active.data(), sizeof(int) * b->P, cudaMemcpyHostToDevice, b->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
   return e == cudaSuccess ? LNS_OK : cuda3(e, "upload active flags");
 }
 
+// Residual history for `steps` steps of the current problems: the step
+// kernels write hist[step * P + p], so the capacity is counted in entries and
+// grows with the number of problems as well as with the steps.
 int reserve_hist(lns_batch3d* b, long long steps) {
-  if (steps <= b->hist_cap) return LNS_OK;
+  const long long need = steps * (long long)b->P;
+  if (need <= b->hist_cap) return LNS_OK;
   void* q = nullptr;
-  int rc = balloc(b, sizeof(double) * (size_t)steps * b->P, &q);
-  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(b->st);  // no step in flight writes the old buffer
+  if (e != cudaSuccess) return cuda3(e, "history: synchronize");
+  e = cudaMalloc(&q, sizeof(double) * (size_t)need);
+  if (e != cudaSuccess) return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  if (b->d_hist) {
+    cudaFree(b->d_hist);
+    b->bytes -= sizeof(double) * (size_t)b->hist_cap;
+  }
   b->d_hist = (double*)q;
-  b->hist_cap = steps;
+  b->hist_cap = need;
+  b->bytes += sizeof(double) * (size_t)need;
   if (b->exec) {  // the graph holds the old history pointer
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
@@ -1354,8 +1400,11 @@ int reserve_hist(lns_batch3d* b, long long steps) {
 
 void destroy_batch(lns_batch3d* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->d_hist) cudaFree(b->d_hist);
   for (void* p : b->allocs) cudaFree(p);
-  for (lns_ctx3d* c : b->ctx) lns_ctx3d_destroy(c);
+  for (void* p : b->table_allocs) cudaFree(p);
+  if (b->owns_ctx)
+    for (lns_ctx3d* c : b->ctx) lns_ctx3d_destroy(c);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
@@ -1392,10 +1441,7 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
     e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) rc = cuda3(e, "cudaStreamCreate");
   }
-  if (!rc) rc = balloc(b, sizeof(lns::a3::StepArgs) * nprob, &q), b->d_args = (lns::a3::StepArgs*)q;
-  if (!rc) rc = balloc(b, sizeof(lns::chain::Args) * nprob, &q), b->d_ax = (lns::chain::Args*)q;
-  if (!rc) rc = balloc(b, sizeof(lns::chain::Args) * nprob, &q), b->d_ay = (lns::chain::Args*)q;
-  if (!rc) rc = balloc(b, sizeof(int) * nprob, &q), b->d_active = (int*)q;
+  if (!rc) rc = reserve_problems(b, nprob);
   if (!rc) rc = balloc(b, sizeof(int), &q), b->d_step = (int*)q;
   if (!rc) rc = reserve_hist(b, 64);
   if (!rc) rc = build_tables(b);
@@ -1443,10 +1489,11 @@ int lns_batch3d_run(lns_batch3d* b, int32_t max_steps, int32_t niter, double tol
   if (!b || !steps || !final_res) return fail3(LNS_ERR_ARG, "batch3d_run: null argument");
   if (max_steps < 0 || niter < 1 || check_every < 1) return fail3(LNS_ERR_ARG, "batch3d_run: bad step counts");
   int rc = check_device(b->ctx[0]);
-  if (!rc) rc = prepare(b);
+  if (!rc) rc = prepare(b, tol);
   if (!rc) rc = reserve_hist(b, max_steps);
   if (!rc) rc = capture(b, niter);
   if (rc) return rc;
+  if ((long long)max_steps * b->P > b->hist_cap) return fail3(LNS_ERR_ARG, "batch3d_run: residual history too small");
   for (int p = 0; p < b->P; ++p) {
     b->active[p] = 1;
     steps[p] = -1;
@@ -1457,6 +1504,7 @@ int lns_batch3d_run(lns_batch3d* b, int32_t max_steps, int32_t niter, double tol
   cudaError_t e = cudaMemsetAsync(b->d_step, 0, sizeof(int), b->st);
   if (e != cudaSuccess) return cuda3(e, "cudaMemsetAsync");
   std::vector<double> hist;
+  std::vector<int> act(b->P);
   int done = 0;
   while (done < max_steps) {
     const int n = std::min(check_every, max_steps - done);
@@ -1467,27 +1515,26 @@ int lns_batch3d_run(lns_batch3d* b, int32_t max_steps, int32_t niter, double tol
     hist.resize((size_t)n * b->P);
     e = cudaMemcpyAsync(hist.data(), b->d_hist + (size_t)done * b->P, sizeof(double) * hist.size(),
                         cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(act.data(), b->d_active, sizeof(int) * b->P, cudaMemcpyDeviceToHost, b->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
     if (e != cudaSuccess) return cuda3(e, "batched steps");
     int left = 0;
     for (int p = 0; p < b->P; ++p) {
       if (!b->active[p]) continue;
       for (int s = 0; s < n; ++s) {
-        final_res[p] = hist[(size_t)s * b->P + p];
-        if (final_res[p] <= tol) {
-          // converged at step done + s + 1; later steps of this check ran
-          // before the flag changed, so keep the first crossing
+        const double r = hist[(size_t)s * b->P + p];
+        final_res[p] = r;
+        if (!act[p] && r <= tol) {  // the device stopped the problem at this step
           steps[p] = done + s + 1;
-          b->active[p] = 0;
           break;
         }
       }
-      left += b->active[p];
+      b->active[p] = act[p];
+      left += act[p];
     }
     done += n;
     if (!left) break;
-    rc = set_active(b);
-    if (rc) return rc;
   }
   return LNS_OK;
 }
@@ -1495,7 +1542,7 @@ int lns_batch3d_run(lns_batch3d* b, int32_t max_steps, int32_t niter, double tol
 int lns_batch3d_tune(lns_batch3d* b, int32_t niter, int32_t* lines_per_cta) {
   if (!b || !lines_per_cta || niter < 1) return fail3(LNS_ERR_ARG, "batch3d_tune: bad argument");
   int rc = check_device(b->ctx[0]);
-  if (!rc) rc = prepare(b);
+  if (!rc) rc = prepare(b, 0.0);
   if (rc) return rc;
   // keep the states: tuning steps run on copies that are restored after
   std::vector<void*> save(b->P, nullptr);
@@ -1557,5 +1604,282 @@ int lns_batch3d_tune(lns_batch3d* b, int32_t niter, int32_t* lines_per_cta) {
   *lines_per_cta = best;
   return rc;
 }
+
+}  // extern "C"
+
+// ======================================================================
+// Serving (lns_server3d_*): requests admitted by device-memory footprint
+// into a running batch that is re-formed whenever requests join or leave
+// ======================================================================
+namespace {
+
+struct SrvReq {
+  int64_t id = 0;
+  lns_params3d prm{};
+  std::vector<double> metrics, vm, v;  // host inputs until admission; v holds the result at completion
+  double tol = 0.0;
+  int max_steps = 0;
+  lns_ctx3d* ctx = nullptr;
+  int state = 0;  // LNS_REQ_*
+  int steps = 0, conv = -1;
+  double res = -1.0;
+  double t_submit = 0.0, t_admit = 0.0, t_done = 0.0;
+};
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// device bytes lns_ctx3d_create allocates for these parameters
+size_t ctx_bytes_for(const lns_params3d& p) {
+  const size_t np = (size_t)p.nx * p.ny;
+  const bool mixed = p.precision == LNS_MIXED;
+  const size_t el = mixed ? sizeof(cf) : sizeof(cd);
+  size_t b = sizeof(double) * (10 + 5 + 125) * np + sizeof(cd) * 15 * np;
+  b += mixed ? sizeof(cf) * 5 * np : sizeof(cd) * 5 * np;
+  b += sizeof(cd) * (250 + 100) * np + el * 250 * np;
+  if (mixed) b += el * 100 * np;
+  b += sizeof(double) * (((size_t)p.nx + 127) / 128 * p.ny + np / 256 + 2) + 1024;
+  return b;
+}
+
+}  // namespace
+
+struct lns_server3d {
+  lns_batch3d* b = nullptr;
+  size_t budget = 0, used = 0;
+  int max_slots = 0, niter = 1;
+  int precision = LNS_MIXED;
+  std::deque<SrvReq*> queue;
+  std::vector<SrvReq*> running;
+  std::map<int64_t, SrvReq*> all;
+  int64_t next_id = 1;
+  bool dirty = true;
+};
+
+namespace {
+
+// Forms the batch of the running requests: per-problem arguments (factoring
+// new ones), work tables and the captured step.
+int reform(lns_server3d* s) {
+  lns_batch3d* b = s->b;
+  b->ctx.clear();
+  for (SrvReq* r : s->running) b->ctx.push_back(r->ctx);
+  b->P = (int)b->ctx.size();
+  b->uploaded.assign(b->P, true);
+  b->active.assign(b->P, 1);
+  if (!b->P) return LNS_OK;
+  int rc = reserve_problems(b, b->P);
+  if (!rc) rc = prepare(b, 0.0);
+  if (rc) return rc;
+  // per-request tolerances
+  std::vector<lns::a3::StepArgs> args(b->P);
+  cudaError_t e = cudaMemcpy(args.data(), b->d_args, sizeof(args[0]) * b->P, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda3(e, "read batch arguments");
+  for (int p = 0; p < b->P; ++p) args[p].tol = s->running[p]->tol;
+  e = cudaMemcpy(b->d_args, args.data(), sizeof(args[0]) * b->P, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload batch arguments");
+  rc = build_tables(b);
+  if (!rc && b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (!rc) rc = set_active(b);
+  s->dirty = false;
+  return rc;
+}
+
+int admit(lns_server3d* s) {
+  while (!s->queue.empty() && (int)s->running.size() < s->max_slots) {
+    SrvReq* r = s->queue.front();
+    const size_t need = ctx_bytes_for(r->prm);
+    if (s->used + need > s->budget && !s->running.empty()) break;  // wait for memory
+    lns_ctx3d* c = nullptr;
+    int rc = lns_ctx3d_create(&r->prm, &c);
+    if (!rc) rc = lns_upload_metrics3d(c, r->metrics.data());
+    if (!rc) rc = lns_upload_mean3d(c, r->vm.data(), nullptr);
+    if (!rc) {
+      cudaError_t e = cudaMemcpy(c->v, r->v.data(), sizeof(cd) * 5 * c->np, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) rc = cuda3(e, "upload v");
+    }
+    s->queue.pop_front();
+    if (rc) {
+      if (c) lns_ctx3d_destroy(c);
+      r->state = LNS_REQ_FAILED;
+      r->t_done = now_s();
+      continue;
+    }
+    r->ctx = c;
+    r->state = LNS_REQ_RUNNING;
+    r->t_admit = now_s();
+    r->metrics.clear();
+    r->metrics.shrink_to_fit();
+    r->vm.clear();
+    r->vm.shrink_to_fit();
+    s->used += lns_ctx3d_bytes(c);
+    s->running.push_back(r);
+    s->dirty = true;
+  }
+  return LNS_OK;
+}
+
+void retire(lns_server3d* s, SrvReq* r, int state) {
+  cudaMemcpy(r->v.data(), r->ctx->v, sizeof(cd) * 5 * r->ctx->np, cudaMemcpyDeviceToHost);
+  s->used -= lns_ctx3d_bytes(r->ctx);
+  lns_ctx3d_destroy(r->ctx);
+  r->ctx = nullptr;
+  r->state = state;
+  r->t_done = now_s();
+  s->dirty = true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lns_server3d_create(size_t budget_bytes, int32_t max_slots, int32_t precision, int32_t niter,
+                        lns_server3d** out) {
+  if (!out || max_slots < 1 || niter < 1) return fail3(LNS_ERR_ARG, "server3d_create: bad argument");
+  if (precision != LNS_FP64 && precision != LNS_MIXED)
+    return fail3(LNS_ERR_ARG, "server3d_create: precision must be LNS_FP64 or LNS_MIXED");
+  *out = nullptr;
+  lns_server3d* s = new lns_server3d();
+  s->budget = budget_bytes;
+  s->max_slots = max_slots;
+  s->precision = precision;
+  s->niter = niter;
+  lns_batch3d* b = new lns_batch3d();
+  b->owns_ctx = false;
+  b->mixed = precision == LNS_MIXED;
+  int rc = LNS_OK;
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e != cudaSuccess) rc = cuda3(e, "cudaGetDevice");
+  void* q = nullptr;
+  if (!rc) {
+    e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda3(e, "cudaStreamCreate");
+  }
+  if (!rc) rc = reserve_problems(b, std::min(max_slots, 64));
+  if (!rc) rc = balloc(b, sizeof(int), &q), b->d_step = (int*)q;
+  if (rc) {
+    destroy_batch(b);
+    delete s;
+    return rc;
+  }
+  s->b = b;
+  *out = s;
+  return LNS_OK;
+}
+
+int lns_server3d_destroy(lns_server3d* s) {
+  if (!s) return LNS_OK;
+  for (auto& kv : s->all) {
+    if (kv.second->ctx) lns_ctx3d_destroy(kv.second->ctx);
+    delete kv.second;
+  }
+  destroy_batch(s->b);
+  delete s;
+  return LNS_OK;
+}
+
+int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* metrics, const double* vm,
+                        const double* v, double tol, int32_t max_steps, int64_t* id) {
+  if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
+  if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
+  if (!(tol > 0.0) || max_steps < 1) return fail3(LNS_ERR_ARG, "server3d_submit: need tol > 0 and max_steps >= 1");
+  if (ctx_bytes_for(*prm) > s->budget) return fail3(LNS_ERR_ARG, "server3d_submit: request larger than the budget");
+  SrvReq* r = new SrvReq();
+  r->id = s->next_id++;
+  r->prm = *prm;
+  const size_t np = (size_t)prm->nx * prm->ny;
+  r->metrics.assign(metrics, metrics + 10 * np);
+  r->vm.assign(vm, vm + 5 * np);
+  r->v.assign(v, v + 10 * np);
+  r->tol = tol;
+  r->max_steps = max_steps;
+  r->state = LNS_REQ_QUEUED;
+  r->t_submit = now_s();
+  s->queue.push_back(r);
+  s->all[r->id] = r;
+  *id = r->id;
+  return LNS_OK;
+}
+
+int lns_server3d_tick(lns_server3d* s, int32_t nsteps, int32_t* running, int32_t* queued) {
+  if (!s || nsteps < 1) return fail3(LNS_ERR_ARG, "server3d_tick: bad argument");
+  int rc = admit(s);
+  if (!rc && s->dirty) rc = reform(s);
+  if (rc) return rc;
+  lns_batch3d* b = s->b;
+  if (b->P) {
+    rc = reserve_hist(b, nsteps);
+    if (!rc) rc = capture(b, s->niter);
+    if (rc) return rc;
+    if ((long long)nsteps * b->P > b->hist_cap) return fail3(LNS_ERR_ARG, "server3d_tick: residual history too small");
+    cudaError_t e = cudaMemsetAsync(b->d_step, 0, sizeof(int), b->st);
+    for (int k = 0; k < nsteps && e == cudaSuccess; ++k) e = cudaGraphLaunch(b->exec, b->st);
+    std::vector<double> hist((size_t)nsteps * b->P);
+    std::vector<int> act(b->P);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hist.data(), b->d_hist, sizeof(double) * hist.size(), cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(act.data(), b->d_active, sizeof(int) * b->P, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    if (e != cudaSuccess) return cuda3(e, "served steps");
+    std::vector<SrvReq*> keep;
+    for (int p = 0; p < b->P; ++p) {
+      SrvReq* r = s->running[p];
+      int st = 0;
+      for (int k = 0; k < nsteps; ++k) {
+        r->steps += 1;
+        r->res = hist[(size_t)k * b->P + p];
+        if (!act[p] && r->res <= r->tol) {
+          r->conv = r->steps;
+          st = LNS_REQ_DONE;
+          break;
+        }
+        if (r->steps >= r->max_steps) {
+          st = LNS_REQ_STOPPED;
+          break;
+        }
+      }
+      if (st) retire(s, r, st);
+      else keep.push_back(r);
+    }
+    // a request that reached max_steps mid-tick ran past it; the ones kept
+    // continue in the next batch
+    s->running.swap(keep);
+  }
+  if (running) *running = (int32_t)s->running.size();
+  if (queued) *queued = (int32_t)s->queue.size();
+  return LNS_OK;
+}
+
+int lns_server3d_poll(lns_server3d* s, int64_t id, int32_t* state, int32_t* steps, double* res, double* latency_s) {
+  if (!s || !state) return fail3(LNS_ERR_ARG, "server3d_poll: null argument");
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return fail3(LNS_ERR_ARG, "server3d_poll: unknown request");
+  const SrvReq* r = it->second;
+  *state = r->state;
+  if (steps) *steps = r->conv >= 0 ? r->conv : r->steps;
+  if (res) *res = r->res;
+  if (latency_s) *latency_s = r->t_done > 0.0 ? r->t_done - r->t_submit : -1.0;
+  return LNS_OK;
+}
+
+int lns_server3d_fetch(lns_server3d* s, int64_t id, double* v) {
+  if (!s || !v) return fail3(LNS_ERR_ARG, "server3d_fetch: null argument");
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return fail3(LNS_ERR_ARG, "server3d_fetch: unknown request");
+  SrvReq* r = it->second;
+  if (r->state != LNS_REQ_DONE && r->state != LNS_REQ_STOPPED)
+    return fail3(LNS_ERR_ARG, "server3d_fetch: request not finished");
+  std::copy(r->v.begin(), r->v.end(), v);
+  s->all.erase(it);
+  delete r;
+  return LNS_OK;
+}
+
+size_t lns_server3d_bytes_in_use(const lns_server3d* s) { return s ? s->used : 0; }
 
 }  // extern "C"

@@ -43,7 +43,8 @@ def test_python_signatures_cover_header():
 
     solver_syms = [n for n in declared_symbols()
                    if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops",
-                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes", "lns_batch3d_bytes")]
+                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes", "lns_batch3d_bytes",
+                                "lns_server3d_bytes_in_use")]
     assert sorted(SIGNATURES) == solver_syms
 
 
@@ -186,3 +187,15 @@ def test_batch3d_argument_errors(lib):
     assert lib.lns_batch3d_get_state(None, 0, None) == 1
     assert lib.lns_batch3d_destroy(None) == 0
     assert lib.lns_batch3d_bytes(None) == 0
+
+
+def test_server3d_argument_errors(lib):
+    s = ctypes.c_void_p()
+    assert lib.lns_server3d_create(1 << 30, 0, 1, 1, ctypes.byref(s)) == 1
+    assert lib.lns_server3d_create(1 << 30, 4, 7, 1, ctypes.byref(s)) == 1
+    assert lib.lns_server3d_submit(None, None, None, None, None, 1e-10, 10, None) == 1
+    assert lib.lns_server3d_tick(None, 1, None, None) == 1
+    assert lib.lns_server3d_poll(None, 1, None, None, None, None) == 1
+    assert lib.lns_server3d_fetch(None, 1, None) == 1
+    assert lib.lns_server3d_destroy(None) == 0
+    assert lib.lns_server3d_bytes_in_use(None) == 0
