@@ -801,12 +801,12 @@ int sweep_x(lns_ctx3d* c, T* r, cudaStream_t st) {
   const size_t sm = ch::chain_smem_bytes<T>();
   ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
   int rc = mark(c, st);
-  ch::chain_fwd_kernel<T, true><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  ch::chain_fwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (!rc) rc = mark(c, st);
   ch::tail_kernel<T><<<a.nsys, 32 * ch::kTailWarps, 0, st>>>(a);
   ch::fill_kernel<T><<<(unsigned)((fill + 255) / 256), 256, 0, st>>>(a);
   if (!rc) rc = mark(c, st);
-  ch::chain_bwd_kernel<T, true><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  ch::chain_bwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "xi sweep launch");
@@ -822,9 +822,9 @@ int sweep_y(lns_ctx3d* c, T* r, cudaStream_t st) {
   const size_t sm = ch::chain_smem_bytes<T>();
   ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
   int rc = mark(c, st);
-  ch::chain_fwd_kernel<T, false><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  ch::chain_fwd_kernel<T, false><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (!rc) rc = mark(c, st);
-  ch::chain_bwd_kernel<T, false><<<cta, 32 * ch::kChainWarps, sm, st>>>(a);
+  ch::chain_bwd_kernel<T, false><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "eta sweep launch");
@@ -1266,13 +1266,13 @@ int enqueue_step(lns_batch3d* b, int niter) {
     a3::rhs_batch_kernel<<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, b->mixed ? 1 : 0);
     a3::resid_batch_kernel<<<b->P, 256, 0, st>>>(b->d_args, b->d_active, b->d_hist, b->d_step, b->P);
     ch::scale_batch_kernel<T><<<b->n_sx, 256, 0, st>>>(b->d_ax, b->t_sx, b->d_active);
-    ch::chain_fwd_batch_kernel<T, true, W><<<b->n_fx, 32 * W, sm, st>>>(b->d_ax, b->t_fx, b->d_active);
+    ch::chain_fwd_batch_kernel<T, true, W><<<b->n_fx, ch::chain_threads<T>(W), sm, st>>>(b->d_ax, b->t_fx, b->d_active);
     ch::tail_batch_kernel<T><<<b->n_tx, 32 * ch::kTailWarps, 0, st>>>(b->d_ax, b->t_tx, b->d_active);
     ch::fill_batch_kernel<T><<<b->n_lx, 256, 0, st>>>(b->d_ax, b->t_lx, b->d_active);
-    ch::chain_bwd_batch_kernel<T, true, W><<<b->n_fx, 32 * W, sm, st>>>(b->d_ax, b->t_fx, b->d_active);
+    ch::chain_bwd_batch_kernel<T, true, W><<<b->n_fx, ch::chain_threads<T>(W), sm, st>>>(b->d_ax, b->t_fx, b->d_active);
     ch::scale_batch_kernel<T><<<b->n_sy, 256, 0, st>>>(b->d_ay, b->t_sy, b->d_active);
-    ch::chain_fwd_batch_kernel<T, false, W><<<b->n_fy, 32 * W, sm, st>>>(b->d_ay, b->t_fy, b->d_active);
-    ch::chain_bwd_batch_kernel<T, false, W><<<b->n_fy, 32 * W, sm, st>>>(b->d_ay, b->t_fy, b->d_active);
+    ch::chain_fwd_batch_kernel<T, false, W><<<b->n_fy, ch::chain_threads<T>(W), sm, st>>>(b->d_ay, b->t_fy, b->d_active);
+    ch::chain_bwd_batch_kernel<T, false, W><<<b->n_fy, ch::chain_threads<T>(W), sm, st>>>(b->d_ay, b->t_fy, b->d_active);
     a3::add_batch_kernel<T><<<b->n_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active);
     a3::bc_batch_kernel<<<b->n_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active);
   }

@@ -290,15 +290,25 @@ __global__ void scale_batch_kernel(const Args* __restrict__ list, const int2* __
   scale_body<T>(list[w.x], w.y);
 }
 
+// kAhead: rows staged ahead of the recurrence.  kSplit: warps per line; the
+// FP64 recurrences give the real and the imaginary part of a row to two warps
+// (on two SM sub-partitions), which halves the dependent FP64 instructions
+// each warp issues per row and doubles the sub-partitions a sweep uses.
 template <typename T> struct ChainCfg;
-template <> struct ChainCfg<cd> { static constexpr int kAhead = 12; };
-template <> struct ChainCfg<cf> { static constexpr int kAhead = 24; };
+template <> struct ChainCfg<cd> { static constexpr int kAhead = 12, kSplit = 2; };
+template <> struct ChainCfg<cf> { static constexpr int kAhead = 24, kSplit = 1; };
 constexpr int kChainWarps = 2;                 // lines per CTA of the single-problem launches
 constexpr int kStage = 55;                     // 50 block entries + 5 right-hand-side entries
+constexpr int kXchg = 20;                      // split lines: 2 parities x 2 parts x 5 components (doubles)
 
 template <typename T>
+constexpr int chain_threads(int lines_per_cta = kChainWarps) {
+  return 32 * ChainCfg<T>::kSplit * lines_per_cta;
+}
+template <typename T>
 constexpr size_t chain_smem_bytes(int lines_per_cta = kChainWarps) {
-  return (size_t)lines_per_cta * (ChainCfg<T>::kAhead + 1) * kStage * sizeof(T);
+  return (size_t)lines_per_cta *
+         ((ChainCfg<T>::kAhead + 1) * kStage * sizeof(T) + (ChainCfg<T>::kSplit > 1 ? kXchg * sizeof(double) : 0));
 }
 
 // sum over q of lane (m,q)'s partial, for m = this lane's q
@@ -437,33 +447,220 @@ __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned c
   cp_async_wait<0>();
 }
 
-template <typename T, bool PER, int W = kChainWarps>
-__global__ void __launch_bounds__(32 * W) chain_fwd_kernel(Args a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  chain_fwd_body<T, PER, W>(a, blockIdx.x, smem_raw);
+// ---------------------------------------------- FP64 recurrences, split lines
+// Two warps per line: warp part c = 0 computes the real parts of a row, c = 1
+// the imaginary parts.  Lane l = m + 5 q holds component q of the previous
+// rows (both parts) and accumulates part c of block entry (m, q) times it;
+// the sum over q is a three-level tree that leaves output component m in lane
+// m, and a shuffle hands component qq back to lane group qq.  Each row, both
+// warps post their part of the new row to a shared exchange slot and meet at
+// a named barrier of the pair, which also publishes the rows the two warps
+// staged: each warp stages half of every row into the line's ring and waits
+// for its own copies one row before the barrier that precedes their use.
+
+__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;\n" ::"r"(id) : "memory"); }
+
+// Stage half c of row r (entries [off, off+50) of its record, then its five
+// right-hand-side entries) into a ring slot shared by the pair.
+__device__ __forceinline__ void chain_stage_half(cd* slot, const Args& a, int r, int iv, int off, int t) {
+  const long long rc = rec_of(a, r, iv);
+  const cd* src = reinterpret_cast<const cd*>(a.chn) + 125 * rc + off;
+  const cd* rhs = reinterpret_cast<const cd*>(a.rhs) + 5 * rc;
+  if (t < 50) cp_async_el(slot + t, src + t);
+  else if (t < 55) cp_async_el(slot + t, rhs + (t - 50));
 }
-template <typename T, bool PER, int W = kChainWarps>
-__global__ void __launch_bounds__(32 * W) chain_bwd_kernel(Args a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  chain_bwd_body<T, PER, W>(a, blockIdx.x, smem_raw);
+
+// acc + part C of -(F z): re -(F.x z.x - F.y z.y), im -(F.x z.y + F.y z.x)
+template <int C>
+__device__ __forceinline__ double part_msub(double acc, cd f, cd z) {
+  if constexpr (C == 0) return fma(f.y, z.y, fma(-f.x, z.x, acc));
+  else return fma(-f.y, z.x, fma(-f.x, z.y, acc));
+}
+
+// sum over q of lane (m, q)'s partial into lane m, then component qq to
+// every lane of group qq
+__device__ __forceinline__ double tree5(double p, int qq) {
+  const unsigned full = 0xffffffffu;
+  const double t4 = __shfl_down_sync(full, p, 20);
+  const double a = p + __shfl_down_sync(full, p, 10);
+  const double b = a + __shfl_down_sync(full, a, 5);
+  return __shfl_sync(full, b + t4, qq);
+}
+
+template <bool PER, int W, int C>
+__device__ __forceinline__ void chain2_fwd_body(const Args& a, int bx, unsigned char* smem_raw) {
+  constexpr int kAhead = ChainCfg<cd>::kAhead, kRing = kAhead + 1;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int ln = warp >> 1, t = C * 32 + lane;  // warp & 1 == C
+  const int iv = bx * W + ln;
+  if (iv >= a.nsys) return;  // both warps of the pair leave together
+  const int bar = 1 + ln;
+  cd* ring = reinterpret_cast<cd*>(smem_raw) + ln * kRing * kStage;
+  double* xch = reinterpret_cast<double*>(reinterpret_cast<cd*>(smem_raw) + W * kRing * kStage) + ln * kXchg;
+  const int n = a.n, top = PER ? n - 2 : n;
+  const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
+  double* grhs = reinterpret_cast<double*>(a.rhs);
+  const cd* gchn = reinterpret_cast<const cd*>(a.chn);
+  for (int r = 1; r <= kAhead; ++r) {
+    if (r <= top) chain_stage_half(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, t);
+    cp_async_commit();
+  }
+  cp_async_wait<kAhead - 1>();
+  pair_sync(bar);
+  cd z1{0.0, 0.0}, z2{0.0, 0.0}, z3{0.0, 0.0}, z4{0.0, 0.0};  // yh of rows i-1..i-4, component qq
+  for (int i = 1; i <= top; ++i) {
+    const int r = i + kAhead;  // refills the slot of row i-1, which both warps finished
+    if (r <= top) chain_stage_half(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, t);
+    cp_async_commit();
+    const cd* st = ring + ((i - 1) % kRing) * kStage;
+    double p = 0.0;
+    if (lane < 5) p = C ? st[50 + lane].y : st[50 + lane].x;
+    if (PER || (i >= 3 && i <= n - 2)) {
+      p = part_msub<C>(p, st[25 + l], z2);
+      p = part_msub<C>(p, st[l], z1);
+    } else if (i == 2) {
+      p = part_msub<C>(p, st[l], z1);
+    } else if (i > 2) {
+      const cd* g = gchn + 125 * rec_of(a, i, iv);
+      if (i == n - 1) {
+        p = part_msub<C>(p, g[100 + l], z3);
+      } else {
+        p = part_msub<C>(p, g[75 + l], z3);
+        p = part_msub<C>(p, g[100 + l], z4);
+      }
+      p = part_msub<C>(p, st[25 + l], z2);
+      p = part_msub<C>(p, st[l], z1);
+    }
+    const double yc = tree5(p, qq);
+    const int par = i & 1;
+    if (lane < 25 && m == 0) {
+      xch[par * 10 + C * 5 + qq] = yc;
+      grhs[2 * (5 * rec_of(a, i, iv) + qq) + C] = yc;
+    }
+    cp_async_wait<kAhead - 1>();  // this thread's half of row i+1
+    pair_sync(bar);
+    const double yo = xch[par * 10 + (1 - C) * 5 + qq];
+    z4 = z3; z3 = z2; z2 = z1;
+    z1 = C ? cd{yo, yc} : cd{yc, yo};
+  }
+  cp_async_wait<0>();
+}
+
+template <bool PER, int W, int C>
+__device__ __forceinline__ void chain2_bwd_body(const Args& a, int bx, unsigned char* smem_raw) {
+  constexpr int kAhead = ChainCfg<cd>::kAhead, kRing = kAhead + 1;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int ln = warp >> 1, t = C * 32 + lane;  // warp & 1 == C
+  const int iv = bx * W + ln;
+  if (iv >= a.nsys) return;
+  const int bar = 1 + ln;
+  cd* ring = reinterpret_cast<cd*>(smem_raw) + ln * kRing * kStage;
+  double* xch = reinterpret_cast<double*>(reinterpret_cast<cd*>(smem_raw) + W * kRing * kStage) + ln * kXchg;
+  const int n = a.n, top = PER ? n - 2 : n;
+  const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
+  double* grhs = reinterpret_cast<double*>(a.rhs);
+  const cd* grc = reinterpret_cast<const cd*>(a.rhs);
+  const cd* gchn = reinterpret_cast<const cd*>(a.chn);
+  // ring slot k holds the k-th row processed (row top - k)
+  for (int k = 0; k < kAhead; ++k) {
+    const int r = top - k;
+    if (r >= 1) chain_stage_half(ring + (k % kRing) * kStage, a, r, iv, 75, t);
+    cp_async_commit();
+  }
+  cd x1{0.0, 0.0}, x2{0.0, 0.0}, x3{0.0, 0.0}, x4{0.0, 0.0};  // x of rows i+1..i+4, component qq
+  if (PER) {
+    x1 = grc[5 * rec_of(a, n - 1, iv) + qq];
+    x2 = grc[5 * rec_of(a, n, iv) + qq];
+  }
+  cp_async_wait<kAhead - 1>();
+  pair_sync(bar);
+  for (int k = 0; k < top; ++k) {
+    const int i = top - k;
+    const int kn = k + kAhead, rn = top - kn;
+    if (rn >= 1) chain_stage_half(ring + (kn % kRing) * kStage, a, rn, iv, 75, t);
+    cp_async_commit();
+    const cd* st = ring + (k % kRing) * kStage;
+    double p = 0.0;
+    if (lane < 5) p = C ? st[50 + lane].y : st[50 + lane].x;
+    if (PER || (i >= 3 && i <= n - 2)) {
+      p = part_msub<C>(p, st[25 + l], x2);
+      p = part_msub<C>(p, st[l], x1);
+    } else if (i == n - 1) {
+      p = part_msub<C>(p, st[l], x1);
+    } else if (i < n - 1) {
+      const cd* g = gchn + 125 * rec_of(a, i, iv);
+      if (i == 2) {
+        p = part_msub<C>(p, g[50 + l], x3);
+      } else {
+        p = part_msub<C>(p, g[25 + l], x3);
+        p = part_msub<C>(p, g[50 + l], x4);
+      }
+      p = part_msub<C>(p, st[25 + l], x2);
+      p = part_msub<C>(p, st[l], x1);
+    }
+    const double xc = tree5(p, qq);
+    const int par = k & 1;
+    if (lane < 25 && m == 0) {
+      xch[par * 10 + C * 5 + qq] = xc;
+      grhs[2 * (5 * rec_of(a, i, iv) + qq) + C] = xc;
+      if (PER && i == 1) grhs[2 * (5 * rec_of(a, n + 1, iv) + qq) + C] = xc;  // row np = row 1
+    }
+    cp_async_wait<kAhead - 1>();
+    pair_sync(bar);
+    const double xo = xch[par * 10 + (1 - C) * 5 + qq];
+    x4 = x3; x3 = x2; x2 = x1;
+    x1 = C ? cd{xo, xc} : cd{xc, xo};
+  }
+  cp_async_wait<0>();
+}
+
+template <typename T, bool PER, int W>
+__device__ __forceinline__ void chain_fwd_any(const Args& a, int bx, unsigned char* smem_raw) {
+  if constexpr (ChainCfg<T>::kSplit > 1) {
+    if ((threadIdx.x / 32) & 1) chain2_fwd_body<PER, W, 1>(a, bx, smem_raw);
+    else chain2_fwd_body<PER, W, 0>(a, bx, smem_raw);
+  } else {
+    chain_fwd_body<T, PER, W>(a, bx, smem_raw);
+  }
 }
 template <typename T, bool PER, int W>
-__global__ void __launch_bounds__(32 * W) chain_fwd_batch_kernel(const Args* __restrict__ list,
-                                                                 const int2* __restrict__ table,
-                                                                 const int* __restrict__ active) {
+__device__ __forceinline__ void chain_bwd_any(const Args& a, int bx, unsigned char* smem_raw) {
+  if constexpr (ChainCfg<T>::kSplit > 1) {
+    if ((threadIdx.x / 32) & 1) chain2_bwd_body<PER, W, 1>(a, bx, smem_raw);
+    else chain2_bwd_body<PER, W, 0>(a, bx, smem_raw);
+  } else {
+    chain_bwd_body<T, PER, W>(a, bx, smem_raw);
+  }
+}
+
+// Launch with chain_threads<T>(W) threads and chain_smem_bytes<T>(W) bytes.
+template <typename T, bool PER, int W = kChainWarps>
+__global__ void __launch_bounds__(chain_threads<T>(W)) chain_fwd_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  chain_fwd_any<T, PER, W>(a, blockIdx.x, smem_raw);
+}
+template <typename T, bool PER, int W = kChainWarps>
+__global__ void __launch_bounds__(chain_threads<T>(W)) chain_bwd_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  chain_bwd_any<T, PER, W>(a, blockIdx.x, smem_raw);
+}
+template <typename T, bool PER, int W>
+__global__ void __launch_bounds__(chain_threads<T>(W)) chain_fwd_batch_kernel(const Args* __restrict__ list,
+                                                                             const int2* __restrict__ table,
+                                                                             const int* __restrict__ active) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int2 w = table[blockIdx.x];
   if (!active[w.x]) return;
-  chain_fwd_body<T, PER, W>(list[w.x], w.y, smem_raw);
+  chain_fwd_any<T, PER, W>(list[w.x], w.y, smem_raw);
 }
 template <typename T, bool PER, int W>
-__global__ void __launch_bounds__(32 * W) chain_bwd_batch_kernel(const Args* __restrict__ list,
-                                                                 const int2* __restrict__ table,
-                                                                 const int* __restrict__ active) {
+__global__ void __launch_bounds__(chain_threads<T>(W)) chain_bwd_batch_kernel(const Args* __restrict__ list,
+                                                                             const int2* __restrict__ table,
+                                                                             const int* __restrict__ active) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int2 w = table[blockIdx.x];
   if (!active[w.x]) return;
-  chain_bwd_body<T, PER, W>(list[w.x], w.y, smem_raw);
+  chain_bwd_any<T, PER, W>(list[w.x], w.y, smem_raw);
 }
 
 // Periodic lines, after the forward recurrence: the fill sums
