@@ -382,77 +382,69 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
   double resnod = 0.0;
   if (i <= g.nx) {
     const long long p = pix(g, i, j), np = o.np;
-    cd c1[5], c2[5], c11[5], c12[5], c22[5], vv[5], r[5];
-    #pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      auto VX = [&](int ii) -> const cd& { return v[k + 5 * pix(g, ii, j)]; };
-      auto VY = [&](int jj) -> const cd& { return v[k + 5 * pix(g, i, jj)]; };
-      auto CY = [&](int jj) -> const cd& { return c1v[k + 5 * pix(g, i, jj)]; };
-      vv[k] = v[k + 5 * p];
-      c1[k] = c1v[k + 5 * p];
-      c2[k] = cd{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).x; }),
-                 d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).y; })};
-      c11[k] = cd{d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).x; }),
-                  d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).y; })};
-      c22[k] = cd{d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).x; }),
-                  d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).y; })};
-      c12[k] = cd{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).x; }),
-                  d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).y; })};
-    }
-    if (g.navier && (g.wallt == 1 || g.wallt == 2) && j == 1) c2[4] = cd{0.0, 0.0};  // src/cgradbc.f90
     auto OP = [&](const double* A, int a, int b) { return A[(long long)(a + 5 * b) * np + p]; };
-    #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      cd acc{0.0, 0.0};
-      #pragma unroll
-      for (int b = 0; b < 5; ++b) acc = cd{acc.x + OP(o.Ah, m, b) * c1[b].x, acc.y + OP(o.Ah, m, b) * c1[b].y};
-      #pragma unroll
-      for (int b = 0; b < 5; ++b) acc = cd{acc.x + OP(o.Bh, m, b) * c2[b].x, acc.y + OP(o.Bh, m, b) * c2[b].y};
-      #pragma unroll
-      for (int b = 0; b < 5; ++b) acc = cd{acc.x + OP(o.Dh, m, b) * vv[b].x, acc.y + OP(o.Dh, m, b) * vv[b].y};
-      r[m] = acc;
-    }
     auto VH = [&](const double* A, int k) { return A[(long long)k * np + p]; };
-    auto sub = [&](int m, double c, const cd& z) { r[m] = cd{r[m].x - c * z.x, r[m].y - c * z.y}; };
-    const double* Vs[3] = {o.V11, o.V12, o.V22};
-    const cd* Cs[3] = {c11, c12, c22};
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      sub(1, VH(Vs[s], 0), Cs[s][1]); sub(1, VH(Vs[s], 4), Cs[s][2]);
-      sub(2, VH(Vs[s], 5), Cs[s][1]); sub(2, VH(Vs[s], 1), Cs[s][2]);
-      sub(3, VH(Vs[s], 2), Cs[s][3]);
-      sub(4, VH(Vs[s], 3), Cs[s][4]);
-    }
-    // 3D terms, im * z = (-Im z, Re z)
+    // i z = (-Im z, Re z); r -= i s  <=>  r += (Im s, -Re s)
+    auto subi = [](cd& rr, double sx, double sy) { rr = cd{rr.x + sy, rr.y - sx}; };
     const double a1 = VH(o.AB, 0), a2 = VH(o.AB, 1), a3 = VH(o.AB, 2), a4 = VH(o.AB, 3);
-    {
-      cd s1{a1 * c1[3].x + a3 * c2[3].x, a1 * c1[3].y + a3 * c2[3].y};
-      r[1] = cd{r[1].x + s1.y, r[1].y - s1.x};
-      cd s2{a2 * c1[3].x + a4 * c2[3].x, a2 * c1[3].y + a4 * c2[3].y};
-      r[2] = cd{r[2].x + s2.y, r[2].y - s2.x};
-      cd s3{a1 * c1[1].x + a2 * c1[2].x + a3 * c2[1].x + a4 * c2[2].x,
-            a1 * c1[1].y + a2 * c1[2].y + a3 * c2[1].y + a4 * c2[2].y};
-      r[3] = cd{r[3].x + s3.y, r[3].y - s3.x};
-    }
+    const double* Vs[3] = {o.V11, o.V12, o.V22};
+    cd r[5];
     #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      cd s{0.0, 0.0};
+    for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
+    // One input component b at a time: its derivatives, then its terms in
+    // every output row, so that only r and one component's derivatives are
+    // live.
+    #pragma unroll 1
+    for (int b = 0; b < 5; ++b) {
+      auto VX = [&](int ii) -> const cd& { return v[b + 5 * pix(g, ii, j)]; };
+      auto VY = [&](int jj) -> const cd& { return v[b + 5 * pix(g, i, jj)]; };
+      auto CY = [&](int jj) -> const cd& { return c1v[b + 5 * pix(g, i, jj)]; };
+      const cd vb = v[b + 5 * p], c1b = c1v[b + 5 * p];
+      cd c2b{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).x; }),
+             d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).y; })};
+      if (b == 4 && g.navier && (g.wallt == 1 || g.wallt == 2) && j == 1) c2b = cd{0.0, 0.0};  // src/cgradbc.f90
       #pragma unroll
-      for (int b = 0; b < 5; ++b) s = cd{s.x + OP(o.Dhi, m, b) * vv[b].x, s.y + OP(o.Dhi, m, b) * vv[b].y};
-      r[m] = cd{r[m].x - s.y, r[m].y + s.x};
+      for (int m = 0; m < 5; ++m) {
+        const double A = OP(o.Ah, m, b), B = OP(o.Bh, m, b), D = OP(o.Dh, m, b), Di = OP(o.Dhi, m, b);
+        r[m].x += A * c1b.x + B * c2b.x + D * vb.x - Di * vb.y;
+        r[m].y += A * c1b.y + B * c2b.y + D * vb.y + Di * vb.x;
+      }
+      if (b == 0) continue;
+      const cd c11b{d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).x; }),
+                    d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).y; })};
+      const cd c22b{d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).x; }),
+                    d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).y; })};
+      const cd c12b{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).x; }),
+                    d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).y; })};
+      const cd Cs[3] = {c11b, c12b, c22b};
+      // viscous terms (entries of Vh11, Vh12, Vh22) and the 3D terms of ABhi
+      #pragma unroll
+      for (int s3 = 0; s3 < 3; ++s3) {
+        auto sub = [&](int m, int k) { const double c = VH(Vs[s3], k); r[m] = cd{r[m].x - c * Cs[s3].x, r[m].y - c * Cs[s3].y}; };
+        if (b == 1) { sub(1, 0); sub(2, 5); }
+        if (b == 2) { sub(1, 4); sub(2, 1); }
+        if (b == 3) sub(3, 2);
+        if (b == 4) sub(4, 3);
+      }
+      if (b == 1) subi(r[3], a1 * c1b.x + a3 * c2b.x, a1 * c1b.y + a3 * c2b.y);
+      if (b == 2) subi(r[3], a2 * c1b.x + a4 * c2b.x, a2 * c1b.y + a4 * c2b.y);
+      if (b == 3) {
+        subi(r[1], a1 * c1b.x + a3 * c2b.x, a1 * c1b.y + a3 * c2b.y);
+        subi(r[2], a2 * c1b.x + a4 * c2b.x, a2 * c1b.y + a4 * c2b.y);
+      }
     }
     // rbe3D
     const double dtl = o.dtl[p];
     #pragma unroll
     for (int m = 0; m < 5; ++m) {
-      const cd vo = vold[m + 5 * p];
-      r[m] = cd{vo.x - vv[m].x - dtl * r[m].x, vo.y - vv[m].y - dtl * r[m].y};
+      const cd vo = vold[m + 5 * p], vm = v[m + 5 * p];
+      r[m] = cd{vo.x - vm.x - dtl * r[m].x, vo.y - vm.y - dtl * r[m].y};
     }
     // boundary rows, src/rhsbc3d.f90:34-170
     if (!g.yper) {
       if (g.navier && j == 1) {
-        for (int m = 1; m <= 3; ++m) r[m] = cd{-(vv[m].x - 0.0), -(vv[m].y - 0.0)};
         auto W = [&](int k, int jj) -> const cd& { return v[k + 5 * pix(g, i, jj)]; };
+        for (int m = 1; m <= 3; ++m) r[m] = cd{-(W(m, 1).x - 0.0), -(W(m, 1).y - 0.0)};
         if (g.wall == 1)
           r[0] = cd{gc1 * W(0, 1).x + gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x,
                     gc1 * W(0, 1).y + gc2 * W(0, 2).y + gc3 * W(0, 3).y + gc4 * W(0, 4).y + gc5 * W(0, 5).y};
@@ -489,7 +481,7 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
   }
   if (threadIdx.x == 0) part[bx + nbx * by] = red[0];
 }
-__global__ void __launch_bounds__(128) rhs_kernel(Grid g, Ops o, const cd* __restrict__ v,
+__global__ void __launch_bounds__(128, 4) rhs_kernel(Grid g, Ops o, const cd* __restrict__ v,
                                                   const cd* __restrict__ vold, const cd* __restrict__ c1v,
                                                   cd* r64, cf* r32, double* part) {
   rhs_body(g, o, v, vold, c1v, r64, r32, part, blockIdx.x, blockIdx.y, gridDim.x);
@@ -574,7 +566,7 @@ __global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4
   const StepArgs& a = list[w.x];
   grad1_body(a.g, a.v, a.c1v, w.y, w.z);
 }
-__global__ void __launch_bounds__(128) rhs_batch_kernel(const StepArgs* __restrict__ list,
+__global__ void __launch_bounds__(128, 4) rhs_batch_kernel(const StepArgs* __restrict__ list,
                                                         const int4* __restrict__ table,
                                                         const int* __restrict__ active, int mixed) {
   const int4 w = table[blockIdx.x];
