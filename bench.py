@@ -76,9 +76,10 @@ KERNEL_FLOPS = {"x_scale": 200, "x_fwd": 400, "x_fill": 800, "x_bwd": 400, "y_sc
 KERNEL_NAMES = {"x_fwd": "chain_fwd_kernel<cd, periodic> (xi forward recurrence)",
                 "x_bwd": "chain_bwd_kernel<cd, periodic> (xi backward recurrence)",
                 "rhs": "grad1_kernel + rhs_kernel + resid_kernel"}
-# DRAM bytes per launch from the ncu capture of the same kernel on this
-# workload (profiles/chain_kernels_cd_xsweep_512x256.md)
-KERNEL_TRAFFIC = {"x_fwd": 129.283840e6 + 6.081792e6, "x_bwd": 129.350144e6 + 6.129152e6}
+# DRAM bytes per launch from ncu captures on this workload: the forward
+# recurrence from profiles/chain_kernels_cd_xsweep_512x256.md, the backward
+# one from an earlier capture of the same records read by one warp per line
+KERNEL_TRAFFIC = {"x_fwd": 129.294080e6 + 5.967104e6, "x_bwd": 129.350144e6 + 6.129152e6}
 KERNELS_PER_STEP = 14  # bc (predictor), grad1, rhs, resid, xi sweep (5), eta sweep (3), add, bc
 
 # ---- secondary: the isolated batched solve
