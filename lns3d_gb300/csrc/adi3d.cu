@@ -373,6 +373,7 @@ __global__ void grad1_kernel(Grid g, const cd* __restrict__ v, cd* __restrict__ 
 // r = vold - v - dtl L(v) (src/lrhs3d.f90:33-218, rbe3D), then the boundary
 // rows (src/rhsbc3d.f90), written as FP64 (r64) and/or FP32 (r32); the
 // block sums of |r|^2 / dtl^2 (src/resstat3d.f90:37-46) go to part[bx + nbx by].
+template <bool NARROW>
 __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* __restrict__ v,
                                          const cd* __restrict__ vold, const cd* __restrict__ c1v, cd* r64, cf* r32,
                                          double* part, int bx, int by, int nbx) {
@@ -400,8 +401,8 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
       auto VY = [&](int jj) -> const cd& { return v[b + 5 * pix(g, i, jj)]; };
       auto CY = [&](int jj) -> const cd& { return c1v[b + 5 * pix(g, i, jj)]; };
       const cd vb = v[b + 5 * p], c1b = c1v[b + 5 * p];
-      cd c2b{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).x; }),
-             d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).y; })};
+      cd c2b{d1_at<NARROW>(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).x; }),
+             d1_at<NARROW>(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return VY(jj).y; })};
       if (b == 4 && g.navier && (g.wallt == 1 || g.wallt == 2) && j == 1) c2b = cd{0.0, 0.0};  // src/cgradbc.f90
       #pragma unroll
       for (int m = 0; m < 5; ++m) {
@@ -410,12 +411,12 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
         r[m].y += A * c1b.y + B * c2b.y + D * vb.y + Di * vb.x;
       }
       if (b == 0) continue;
-      const cd c11b{d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).x; }),
-                    d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).y; })};
-      const cd c22b{d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).x; }),
-                    d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).y; })};
-      const cd c12b{d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).x; }),
-                    d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).y; })};
+      const cd c11b{d2_at<NARROW>(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).x; }),
+                    d2_at<NARROW>(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).y; })};
+      const cd c22b{d2_at<NARROW>(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).x; }),
+                    d2_at<NARROW>(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).y; })};
+      const cd c12b{d1_at<NARROW>(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).x; }),
+                    d1_at<NARROW>(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).y; })};
       const cd Cs[3] = {c11b, c12b, c22b};
       // viscous terms (entries of Vh11, Vh12, Vh22) and the 3D terms of ABhi
       #pragma unroll
@@ -481,10 +482,11 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
   }
   if (threadIdx.x == 0) part[bx + nbx * by] = red[0];
 }
+template <bool NARROW>
 __global__ void __launch_bounds__(128, 4) rhs_kernel(Grid g, Ops o, const cd* __restrict__ v,
                                                   const cd* __restrict__ vold, const cd* __restrict__ c1v,
                                                   cd* r64, cf* r32, double* part) {
-  rhs_body(g, o, v, vold, c1v, r64, r32, part, blockIdx.x, blockIdx.y, gridDim.x);
+  rhs_body<NARROW>(g, o, v, vold, c1v, r64, r32, part, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 // ----------------------------------------------------------------- update
@@ -566,13 +568,15 @@ __global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4
   const StepArgs& a = list[w.x];
   grad1_body(a.g, a.v, a.c1v, w.y, w.z);
 }
+template <bool NARROW>
 __global__ void __launch_bounds__(128, 4) rhs_batch_kernel(const StepArgs* __restrict__ list,
                                                         const int4* __restrict__ table,
                                                         const int* __restrict__ active, int mixed) {
   const int4 w = table[blockIdx.x];
   if (!active[w.x]) return;
   const StepArgs& a = list[w.x];
-  rhs_body(a.g, a.o, a.v, a.vold, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr, a.part, w.y, w.z, a.nbx);
+  rhs_body<NARROW>(a.g, a.o, a.v, a.vold, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr, a.part, w.y, w.z,
+                   a.nbx);
 }
 // residual of each problem into hist[step * P + p] (src/resstat3d.f90:37-60)
 // A problem whose residual reaches its tolerance is switched off here, so
@@ -756,7 +760,10 @@ int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vold, cd* r64, cf* r32, doub
                cudaStream_t st) {
   const Grid& g = c->g;
   lns::a3::grad1_kernel<<<pt_grid(g), 128, 0, st>>>(g, v, c->c1v);
-  lns::a3::rhs_kernel<<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vold, c->c1v, r64, r32, c->part);
+  if (lns::a3::narrow_stencils(g))
+    lns::a3::rhs_kernel<true><<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vold, c->c1v, r64, r32, c->part);
+  else
+    lns::a3::rhs_kernel<false><<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vold, c->c1v, r64, r32, c->part);
   const int nrhs = (int)(pt_grid(g).x * pt_grid(g).y);  // rhs_kernel block partials
   lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res, acc);
   cudaError_t e = cudaGetLastError();
@@ -1251,11 +1258,16 @@ int enqueue_step(lns_batch3d* b, int niter) {
   namespace ch = lns::chain;
   cudaStream_t st = b->st;
   const size_t sm = ch::chain_smem_bytes<T>(W);
+  bool narrow = true;  // every problem's stencils are five-point
+  for (int p = 0; p < b->P; ++p) narrow = narrow && a3::narrow_stencils(b->ctx[p]->g);
   a3::copy_batch_kernel<<<b->n_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active);
   a3::bc_batch_kernel<<<b->n_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active);
   for (int it = 0; it < niter; ++it) {
     a3::grad1_batch_kernel<<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active);
-    a3::rhs_batch_kernel<<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, b->mixed ? 1 : 0);
+    if (narrow)
+      a3::rhs_batch_kernel<true><<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, b->mixed ? 1 : 0);
+    else
+      a3::rhs_batch_kernel<false><<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, b->mixed ? 1 : 0);
     a3::resid_batch_kernel<<<b->P, 256, 0, st>>>(b->d_args, b->d_active, b->d_hist, b->d_step, b->P);
     ch::scale_batch_kernel<T><<<b->n_sx, 256, 0, st>>>(b->d_ax, b->t_sx, b->d_active);
     ch::chain_fwd_batch_kernel<T, true, W><<<b->n_fx, ch::chain_threads<T>(W), sm, st>>>(b->d_ax, b->t_fx, b->d_active);

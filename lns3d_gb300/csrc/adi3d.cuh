@@ -45,6 +45,12 @@ struct Grid {
   double dxinv, dyinv, dxsinv, dysinv;
 };
 
+// true when every interior stencil of g has zero outermost coefficients
+inline bool narrow_stencils(const Grid& g) {
+  return g.gx[0] == 0.0 && g.gx[5] == 0.0 && g.gy[0] == 0.0 && g.gy[5] == 0.0 && g.dx2[0] == 0.0 &&
+         g.dx2[6] == 0.0 && g.dy2[0] == 0.0 && g.dy2[6] == 0.0;
+}
+
 // Frozen operators on the device, structure-of-arrays: element (a,b)
 // (0-based) of a 5x5 operator at point p is at [(a + 5 b) * np + p], entry k
 // of a 6-vector at [k * np + p].
@@ -63,11 +69,16 @@ __device__ __forceinline__ long long pix(const Grid& g, int i, int j) {
 
 // First derivative along a line of n points at point i (1-based), from the
 // values u(k); periodic lines have period n-1 (point n repeats point 1).
-template <class U>
+// NARROW: the interior stencil's outermost coefficients (offsets +-3) are zero,
+// as for the fourth-order scheme (optx, opty = -1); their terms are skipped,
+// and the sum is an explicit left-to-right chain of fused multiply-adds so
+// that every kernel using it rounds the same way.
+template <bool NARROW = false, class U>
 __device__ __forceinline__ double d1_at(int i, int n, int periodic, const double* c, double dinv, U u) {
   if (periodic) {
     if (i == n) i = 1;
     auto w = [&](int k) { return k < 1 ? k + n - 1 : (k > n - 1 ? k - (n - 1) : k); };
+    if constexpr (NARROW) return fma(c[4], u(w(i + 2)), fma(c[3], u(w(i + 1)), fma(c[2], u(w(i - 1)), c[1] * u(w(i - 2)))));
     return c[0] * u(w(i - 3)) + c[1] * u(w(i - 2)) + c[2] * u(w(i - 1)) + c[3] * u(w(i + 1)) + c[4] * u(w(i + 2)) +
            c[5] * u(w(i + 3));
   }
@@ -77,14 +88,17 @@ __device__ __forceinline__ double d1_at(int i, int n, int periodic, const double
   if (i == n - 2) return (ga1 * u(n - 4) + ga2 * u(n - 3) + ga3 * u(n - 1) + ga4 * u(n)) * dinv;
   if (i == n - 1) return -((gb1 * u(n) + gb2 * u(n - 1) + gb3 * u(n - 2) + gb4 * u(n - 3) + gb5 * u(n - 4)) * dinv);
   if (i == n) return -((gc1 * u(n) + gc2 * u(n - 1) + gc3 * u(n - 2) + gc4 * u(n - 3) + gc5 * u(n - 4)) * dinv);
+  if constexpr (NARROW) return fma(c[4], u(i + 2), fma(c[3], u(i + 1), fma(c[2], u(i - 1), c[1] * u(i - 2))));
   return c[0] * u(i - 3) + c[1] * u(i - 2) + c[2] * u(i - 1) + c[3] * u(i + 1) + c[4] * u(i + 2) + c[5] * u(i + 3);
 }
 
-template <class U>
+template <bool NARROW = false, class U>
 __device__ __forceinline__ double d2_at(int i, int n, int periodic, const double* c, double dsinv, U u) {
   if (periodic) {
     if (i == n) i = 1;
     auto w = [&](int k) { return k < 1 ? k + n - 1 : (k > n - 1 ? k - (n - 1) : k); };
+    if constexpr (NARROW)
+      return fma(c[5], u(w(i + 2)), fma(c[4], u(w(i + 1)), fma(c[3], u(i), fma(c[2], u(w(i - 1)), c[1] * u(w(i - 2))))));
     return c[0] * u(w(i - 3)) + c[1] * u(w(i - 2)) + c[2] * u(w(i - 1)) + c[3] * u(i) + c[4] * u(w(i + 1)) +
            c[5] * u(w(i + 2)) + c[6] * u(w(i + 3));
   }
@@ -94,6 +108,7 @@ __device__ __forceinline__ double d2_at(int i, int n, int periodic, const double
   if (i == n - 2) return (da1 * u(n - 4) + da2 * u(n - 3) + da3 * u(n - 2) + da4 * u(n - 1) + da5 * u(n)) * dsinv;
   if (i == n - 1) return (db1 * u(n) + db2 * u(n - 1) + db3 * u(n - 2) + db4 * u(n - 3) + db5 * u(n - 4)) * dsinv;
   if (i == n) return (dd1 * u(n) + dd2 * u(n - 1) + dd3 * u(n - 2) + dd4 * u(n - 3) + dd5 * u(n - 4)) * dsinv;
+  if constexpr (NARROW) return fma(c[5], u(i + 2), fma(c[4], u(i + 1), fma(c[3], u(i), fma(c[2], u(i - 1), c[1] * u(i - 2)))));
   return c[0] * u(i - 3) + c[1] * u(i - 2) + c[2] * u(i - 1) + c[3] * u(i) + c[4] * u(i + 1) + c[5] * u(i + 2) +
          c[6] * u(i + 3);
 }
