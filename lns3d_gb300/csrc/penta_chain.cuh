@@ -323,13 +323,10 @@ __device__ __forceinline__ T gather5(T p, int qq) {
   return s;
 }
 
-// Stage row r: entries [off, off+50) of its internal record and its 5
-// right-hand-side entries.
+// Stage one row into a ring slot: the 50 block entries at src (its record
+// plus the sweep's offset) and the 5 right-hand-side entries at rhs.
 template <typename T>
-__device__ __forceinline__ void chain_stage(T* slot, const Args& a, int r, int iv, int off, int lane) {
-  const long long rc = rec_of(a, r, iv);
-  const T* src = reinterpret_cast<const T*>(a.chn) + 125 * rc + off;
-  const T* rhs = reinterpret_cast<const T*>(a.rhs) + 5 * rc;
+__device__ __forceinline__ void chain_stage(T* slot, const T* src, const T* rhs, int lane) {
   cp_async_el(slot + lane, src + lane);
   const int e = lane + 32;
   if (e < 50) cp_async_el(slot + e, src + e);
@@ -337,31 +334,40 @@ __device__ __forceinline__ void chain_stage(T* slot, const Args& a, int r, int i
 }
 
 // Forward recurrence yh_i = s_i - sum_c F_ic yh_c over rows 1..top (top = n,
-// or n-2 for periodic lines whose rows n-1, n follow in tail_kernel).
+// or n-2 for periodic lines whose rows n-1, n follow in tail_kernel).  The
+// staging, ring and output positions advance by pointer increments.
 template <typename T, bool PER, int W>
 __device__ __forceinline__ void chain_fwd_body(const Args& a, int bx, unsigned char* smem_raw) {
   constexpr int kAhead = ChainCfg<T>::kAhead, kRing = kAhead + 1;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int iv = bx * W + warp;
   if (iv >= a.nsys) return;
-  T* ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
+  T* const ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
+  T* const rend = ring + kRing * kStage;
   const int n = a.n, top = PER ? n - 2 : n;
   const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
   T* grhs = reinterpret_cast<T*>(a.rhs);
   const T* gchn = reinterpret_cast<const T*>(a.chn);
+  const long long rs = a.row_stride, rec1 = a.line_stride * (long long)iv;
+  const T* sp = gchn + 125 * rec1 + 25;  // staging cursor: record of the next row to stage
+  const T* rp = grhs + 5 * rec1;         // and its right-hand side
+  T* ws = ring;                          // slot of the next row to stage
   for (int r = 1; r <= kAhead; ++r) {
-    if (r <= top) chain_stage(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, lane);
+    if (r <= top) chain_stage(ws, sp, rp, lane);
     cp_async_commit();
+    sp += 125 * rs, rp += 5 * rs, ws += kStage;
   }
+  const T* st = ring;                // slot of row i
+  T* out = grhs + 5 * rec1 + qq;     // component qq of row i
   T z1 = zero<T>(), z2 = zero<T>(), z3 = zero<T>(), z4 = zero<T>();  // yh of rows i-1..i-4, component qq
   for (int i = 1; i <= top; ++i) {
     __syncwarp();  // every lane is done with the slot about to be refilled
-    const int r = i + kAhead;
-    if (r <= top) chain_stage(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, lane);
+    if (i + kAhead <= top) chain_stage(ws, sp, rp, lane);
     cp_async_commit();
+    sp += 125 * rs, rp += 5 * rs, ws += kStage;
+    if (ws == rend) ws = ring;
     cp_async_wait<kAhead>();
     __syncwarp();
-    const T* st = ring + ((i - 1) % kRing) * kStage;
     T p;
     if (PER || (i >= 3 && i <= n - 2)) {
       p = fmac(mul(st[l], z1), st[25 + l], z2);
@@ -381,7 +387,10 @@ __device__ __forceinline__ void chain_fwd_body(const Args& a, int bx, unsigned c
     }
     const T yv = sub(st[50 + qq], gather5(p, qq));
     z4 = z3; z3 = z2; z2 = z1; z1 = yv;
-    if (lane < 25 && m == 0) grhs[5 * rec_of(a, i, iv) + qq] = yv;
+    if (lane < 25 && m == 0) *out = yv;
+    out += 5 * rs;
+    st += kStage;
+    if (st == rend) st = ring;
   }
   cp_async_wait<0>();
 }
@@ -395,17 +404,23 @@ __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned c
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int iv = bx * W + warp;
   if (iv >= a.nsys) return;
-  T* ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
+  T* const ring = reinterpret_cast<T*>(smem_raw) + warp * kRing * kStage;
+  T* const rend = ring + kRing * kStage;
   const int n = a.n, top = PER ? n - 2 : n;
   const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
   T* grhs = reinterpret_cast<T*>(a.rhs);
   const T* gchn = reinterpret_cast<const T*>(a.chn);
-  // ring slot k holds the k-th row processed (row top - k)
+  const long long rs = a.row_stride, rect = a.line_stride * (long long)iv + rs * (top - 1);  // record of row top
+  const T* sp = gchn + 125 * rect + 75;
+  const T* rp = grhs + 5 * rect;
+  T* ws = ring;  // ring slot k holds the k-th row processed (row top - k)
   for (int k = 0; k < kAhead; ++k) {
-    const int r = top - k;
-    if (r >= 1) chain_stage(ring + (k % kRing) * kStage, a, r, iv, 75, lane);
+    if (top - k >= 1) chain_stage(ws, sp, rp, lane);
     cp_async_commit();
+    sp -= 125 * rs, rp -= 5 * rs, ws += kStage;
   }
+  const T* st = ring;
+  T* out = grhs + 5 * rect + qq;
   T x1 = zero<T>(), x2 = zero<T>(), x3 = zero<T>(), x4 = zero<T>();  // x of rows i+1..i+4, component qq
   if (PER) {
     x1 = grhs[5 * rec_of(a, n - 1, iv) + qq];
@@ -414,12 +429,12 @@ __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned c
   for (int k = 0; k < top; ++k) {
     __syncwarp();  // every lane is done with the slot about to be refilled
     const int i = top - k;
-    const int kn = k + kAhead, rn = top - kn;
-    if (rn >= 1) chain_stage(ring + (kn % kRing) * kStage, a, rn, iv, 75, lane);
+    if (top - (k + kAhead) >= 1) chain_stage(ws, sp, rp, lane);
     cp_async_commit();
+    sp -= 125 * rs, rp -= 5 * rs, ws += kStage;
+    if (ws == rend) ws = ring;
     cp_async_wait<kAhead>();
     __syncwarp();
-    const T* st = ring + (k % kRing) * kStage;
     T p;
     if (PER || (i >= 3 && i <= n - 2)) {
       p = fmac(mul(st[l], x1), st[25 + l], x2);
@@ -440,9 +455,12 @@ __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned c
     const T xv = sub(st[50 + qq], gather5(p, qq));
     x4 = x3; x3 = x2; x2 = x1; x1 = xv;
     if (lane < 25 && m == 0) {
-      grhs[5 * rec_of(a, i, iv) + qq] = xv;
+      *out = xv;
       if (PER && i == 1) grhs[5 * rec_of(a, n + 1, iv) + qq] = xv;  // row np = row 1
     }
+    out -= 5 * rs;
+    st += kStage;
+    if (st == rend) st = ring;
   }
   cp_async_wait<0>();
 }
@@ -460,12 +478,9 @@ __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned c
 
 __device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;\n" ::"r"(id) : "memory"); }
 
-// Stage half c of row r (entries [off, off+50) of its record, then its five
-// right-hand-side entries) into a ring slot shared by the pair.
-__device__ __forceinline__ void chain_stage_half(cd* slot, const Args& a, int r, int iv, int off, int t) {
-  const long long rc = rec_of(a, r, iv);
-  const cd* src = reinterpret_cast<const cd*>(a.chn) + 125 * rc + off;
-  const cd* rhs = reinterpret_cast<const cd*>(a.rhs) + 5 * rc;
+// Stage thread t's part of one row (the 50 block entries at src, the 5
+// right-hand-side entries at rhs) into a ring slot shared by the pair.
+__device__ __forceinline__ void chain_stage_half(cd* slot, const cd* src, const cd* rhs, int t) {
   if (t < 50) cp_async_el(slot + t, src + t);
   else if (t < 55) cp_async_el(slot + t, rhs + (t - 50));
 }
@@ -501,18 +516,27 @@ __device__ __forceinline__ void chain2_fwd_body(const Args& a, int bx, unsigned 
   const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
   double* grhs = reinterpret_cast<double*>(a.rhs);
   const cd* gchn = reinterpret_cast<const cd*>(a.chn);
+  cd* const rend = ring + kRing * kStage;
+  const long long rs = a.row_stride, rec1 = a.line_stride * (long long)iv;
+  const cd* sp = gchn + 125 * rec1 + 25;                       // staging cursor (record, rhs)
+  const cd* rp = reinterpret_cast<const cd*>(a.rhs) + 5 * rec1;
+  cd* ws = ring;
   for (int r = 1; r <= kAhead; ++r) {
-    if (r <= top) chain_stage_half(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, t);
+    if (r <= top) chain_stage_half(ws, sp, rp, t);
     cp_async_commit();
+    sp += 125 * rs, rp += 5 * rs, ws += kStage;
   }
   cp_async_wait<kAhead - 1>();
   pair_sync(bar);
+  const cd* st = ring;                          // slot of row i
+  double* out = grhs + 2 * (5 * rec1 + qq) + C;  // part C of component qq of row i
   cd z1{0.0, 0.0}, z2{0.0, 0.0}, z3{0.0, 0.0}, z4{0.0, 0.0};  // yh of rows i-1..i-4, component qq
   for (int i = 1; i <= top; ++i) {
-    const int r = i + kAhead;  // refills the slot of row i-1, which both warps finished
-    if (r <= top) chain_stage_half(ring + ((r - 1) % kRing) * kStage, a, r, iv, 25, t);
+    // refills the slot of row i-1, which both warps finished
+    if (i + kAhead <= top) chain_stage_half(ws, sp, rp, t);
     cp_async_commit();
-    const cd* st = ring + ((i - 1) % kRing) * kStage;
+    sp += 125 * rs, rp += 5 * rs, ws += kStage;
+    if (ws == rend) ws = ring;
     double p = 0.0;
     if (lane < 5) p = C ? st[50 + lane].y : st[50 + lane].x;
     if (PER || (i >= 3 && i <= n - 2)) {
@@ -535,8 +559,11 @@ __device__ __forceinline__ void chain2_fwd_body(const Args& a, int bx, unsigned 
     const int par = i & 1;
     if (lane < 25 && m == 0) {
       xch[par * 10 + C * 5 + qq] = yc;
-      grhs[2 * (5 * rec_of(a, i, iv) + qq) + C] = yc;
+      *out = yc;
     }
+    out += 10 * rs;
+    st += kStage;
+    if (st == rend) st = ring;
     cp_async_wait<kAhead - 1>();  // this thread's half of row i+1
     pair_sync(bar);
     const double yo = xch[par * 10 + (1 - C) * 5 + qq];
@@ -561,12 +588,18 @@ __device__ __forceinline__ void chain2_bwd_body(const Args& a, int bx, unsigned 
   double* grhs = reinterpret_cast<double*>(a.rhs);
   const cd* grc = reinterpret_cast<const cd*>(a.rhs);
   const cd* gchn = reinterpret_cast<const cd*>(a.chn);
-  // ring slot k holds the k-th row processed (row top - k)
+  cd* const rend = ring + kRing * kStage;
+  const long long rs = a.row_stride, rect = a.line_stride * (long long)iv + rs * (top - 1);  // record of row top
+  const cd* sp = gchn + 125 * rect + 75;
+  const cd* rp = grc + 5 * rect;
+  cd* ws = ring;  // ring slot k holds the k-th row processed (row top - k)
   for (int k = 0; k < kAhead; ++k) {
-    const int r = top - k;
-    if (r >= 1) chain_stage_half(ring + (k % kRing) * kStage, a, r, iv, 75, t);
+    if (top - k >= 1) chain_stage_half(ws, sp, rp, t);
     cp_async_commit();
+    sp -= 125 * rs, rp -= 5 * rs, ws += kStage;
   }
+  const cd* st = ring;
+  double* out = grhs + 2 * (5 * rect + qq) + C;
   cd x1{0.0, 0.0}, x2{0.0, 0.0}, x3{0.0, 0.0}, x4{0.0, 0.0};  // x of rows i+1..i+4, component qq
   if (PER) {
     x1 = grc[5 * rec_of(a, n - 1, iv) + qq];
@@ -576,10 +609,10 @@ __device__ __forceinline__ void chain2_bwd_body(const Args& a, int bx, unsigned 
   pair_sync(bar);
   for (int k = 0; k < top; ++k) {
     const int i = top - k;
-    const int kn = k + kAhead, rn = top - kn;
-    if (rn >= 1) chain_stage_half(ring + (kn % kRing) * kStage, a, rn, iv, 75, t);
+    if (top - (k + kAhead) >= 1) chain_stage_half(ws, sp, rp, t);
     cp_async_commit();
-    const cd* st = ring + (k % kRing) * kStage;
+    sp -= 125 * rs, rp -= 5 * rs, ws += kStage;
+    if (ws == rend) ws = ring;
     double p = 0.0;
     if (lane < 5) p = C ? st[50 + lane].y : st[50 + lane].x;
     if (PER || (i >= 3 && i <= n - 2)) {
@@ -602,9 +635,12 @@ __device__ __forceinline__ void chain2_bwd_body(const Args& a, int bx, unsigned 
     const int par = k & 1;
     if (lane < 25 && m == 0) {
       xch[par * 10 + C * 5 + qq] = xc;
-      grhs[2 * (5 * rec_of(a, i, iv) + qq) + C] = xc;
+      *out = xc;
       if (PER && i == 1) grhs[2 * (5 * rec_of(a, n + 1, iv) + qq) + C] = xc;  // row np = row 1
     }
+    out -= 10 * rs;
+    st += kStage;
+    if (st == rend) st = ring;
     cp_async_wait<kAhead - 1>();
     pair_sync(bar);
     const double xo = xch[par * 10 + (1 - C) * 5 + qq];
