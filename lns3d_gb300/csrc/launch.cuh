@@ -42,6 +42,47 @@ int launch_solve(const void* mat, void* rhs, const void* per, const void* per2, 
   return LNS_OK;
 }
 
+// Threads per line of the factor kernels: a warp when the lines alone fill
+// the GPU (several per SM sub-partition), else a CTA per line so that each
+// pivot's elimination and Schur update spread over more sub-partitions.
+// The periodic pivot touches about four times the elements of a boundary
+// one.  Results do not depend on the choice.
+inline int bc_team(int nsys) { return nsys <= 304 ? 128 : 32; }
+inline int p_team(int nsys) { return nsys <= 160 ? 256 : nsys <= 640 ? 128 : 32; }
+
+template <typename T, int TEAM>
+void launch_bc_team(const lns::PentaArgs& a, cudaStream_t st) {
+  if constexpr (TEAM == 32) {
+    const int blocks = (a.nsys + lns::kWarpsPerCta - 1) / lns::kWarpsPerCta;
+    const size_t smem = (size_t)lns::kWarpsPerCta * (lns::kRing * lns::kRowSz + 16) * sizeof(T);
+    lns::penta_bc_kernel<T, 32><<<blocks, 32 * lns::kWarpsPerCta, smem, st>>>(a);
+  } else {
+    const size_t smem = (size_t)(lns::kRing * lns::kRowSz + 16) * sizeof(T);
+    lns::penta_bc_kernel<T, TEAM><<<a.nsys, TEAM, smem, st>>>(a);
+  }
+}
+
+template <typename T, int TEAM>
+void launch_p_team(const lns::PeriodicArgs& a, cudaStream_t st) {
+  if constexpr (TEAM == 32) {
+    const int blocks = (a.nsys + lns::kPWarpsPerCta - 1) / lns::kPWarpsPerCta;
+    const size_t smem = (size_t)lns::kPWarpsPerCta * lns::kPWarpSmem * sizeof(T);
+    lns::penta_p_kernel<T, 32><<<blocks, 32 * lns::kPWarpsPerCta, smem, st>>>(a);
+  } else {
+    const size_t smem = (size_t)lns::kPWarpSmem * sizeof(T);
+    lns::penta_p_kernel<T, TEAM><<<a.nsys, TEAM, smem, st>>>(a);
+  }
+}
+
+template <typename T>
+void launch_p_any(const lns::PeriodicArgs& a, cudaStream_t st) {
+  switch (p_team(a.nsys)) {
+    case 256: launch_p_team<T, 256>(a, st); break;
+    case 128: launch_p_team<T, 128>(a, st); break;
+    default: launch_p_team<T, 32>(a, st); break;
+  }
+}
+
 // code 0: factor; 1: solve; 2: factor then solve.
 template <typename T>
 int launch_bc(void* mat, void* rhs, int n, int nsys, long long row_stride, long long line_stride, int code,
@@ -49,9 +90,8 @@ int launch_bc(void* mat, void* rhs, int n, int nsys, long long row_stride, long 
   if (nsys == 0) return LNS_OK;
   if (code != 1) {
     lns::PentaArgs a{mat, rhs, n, nsys, row_stride, line_stride, 0, status};
-    const int blocks = (nsys + lns::kWarpsPerCta - 1) / lns::kWarpsPerCta;
-    const size_t smem = (size_t)lns::kWarpsPerCta * (lns::kRing * lns::kRowSz + 16) * sizeof(T);
-    lns::penta_bc_kernel<T><<<blocks, 32 * lns::kWarpsPerCta, smem, st>>>(a);
+    if (bc_team(nsys) == 128) launch_bc_team<T, 128>(a, st);
+    else launch_bc_team<T, 32>(a, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lns_cuda_fail(e, "penta_bc_kernel launch");
   }
@@ -72,9 +112,7 @@ int launch_p(void* mat, void* rhs, void* per, void* per2, int np, int nsys, long
     // n to a separate solve phase, so the right-hand side is eliminated
     // during the factorisation.
     lns::PeriodicArgs a{mat, rhs, per, per2, np - 1, np, nsys, row_stride, line_stride, 2, compat, 0, status};
-    const int blocks = (nsys + lns::kPWarpsPerCta - 1) / lns::kPWarpsPerCta;
-    const size_t smem = (size_t)lns::kPWarpsPerCta * lns::kPWarpSmem * sizeof(T);
-    lns::penta_p_kernel<T><<<blocks, 32 * lns::kPWarpsPerCta, smem, st>>>(a);
+    launch_p_any<T>(a, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lns_cuda_fail(e, "penta_p_kernel launch");
     return LNS_OK;
@@ -82,9 +120,7 @@ int launch_p(void* mat, void* rhs, void* per, void* per2, int np, int nsys, long
   if (code != 1) {
     lns::PeriodicArgs a{mat, rhs, per, per2, np - 1, np, nsys, row_stride, line_stride, 0,
                         compat, 1, status};
-    const int blocks = (nsys + lns::kPWarpsPerCta - 1) / lns::kPWarpsPerCta;
-    const size_t smem = (size_t)lns::kPWarpsPerCta * lns::kPWarpSmem * sizeof(T);
-    lns::penta_p_kernel<T><<<blocks, 32 * lns::kPWarpsPerCta, smem, st>>>(a);
+    launch_p_any<T>(a, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lns_cuda_fail(e, "penta_p_kernel launch");
   }

@@ -1,7 +1,9 @@
 // Direct FP64 block-pentadiagonal line solver, boundary-closure rows
 // (penta1bc / penta2bc / cpenta1bc / cpenta2bc semantics).
 //
-// One warp owns one line.  The line's block rows stream through a five-row
+// A team of TEAM threads owns one line: one warp (TEAM = 32, several lines
+// per CTA) when there are lines enough to fill the GPU, else a whole CTA of
+// 64..256 threads per line.  The line's block rows stream through a five-row
 // ring in shared memory (cp.async prefetch of the row three ahead), so the
 // elimination of pivot row i sees rows i..i+2 (i..n near the end of the
 // line) resident.  Each pivot row runs
@@ -60,12 +62,16 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-template <typename T>
+template <typename T, int TEAM = 32>
 struct LineCtx {
   T* ring;              // kRing * kRowSz
   T* scratch;           // 16 entries: [0,5) multipliers, [5,10) pivot reciprocals
   const PentaArgs* a;
-  int iv, lane, n;
+  int iv, lane, n;      // lane: thread index within the team
+  __device__ void sync() const {
+    if constexpr (TEAM == 32) __syncwarp();
+    else __syncthreads();
+  }
 
   __device__ T* row(int r) const { return ring + ((r - 1) % kRing) * kRowSz; }
   __device__ T* blk(int r, int k) const { return row(r) + 25 * (k - 1); }
@@ -77,7 +83,7 @@ struct LineCtx {
   __device__ void load_row(int r, bool with_rhs) const {
     const T* gm = reinterpret_cast<const T*>(a->mat) + 125 * rec(r);
     T* s = row(r);
-    for (int e = lane; e < 125; e += 32) {
+    for (int e = lane; e < 125; e += TEAM) {
       int k = e % 5, m = (e / 5) % 5, q = e / 25;
       cp_async_el(s + k * 25 + m * 5 + q, gm + e);
     }
@@ -87,7 +93,7 @@ struct LineCtx {
     T* s = row(r);
     if (with_mat) {
       T* gm = reinterpret_cast<T*>(a->mat) + 125 * rec(r);
-      for (int e = lane; e < 125; e += 32) {
+      for (int e = lane; e < 125; e += TEAM) {
         int k = e % 5, m = (e / 5) % 5, q = e / 25;
         gm[e] = s[k * 25 + m * 5 + q];
       }
@@ -97,8 +103,8 @@ struct LineCtx {
 };
 
 // Factor (and with_rhs: forward-eliminate the right-hand side) pivot row i.
-template <typename T>
-__device__ void pivot_bc(const LineCtx<T>& L, int i, bool factor, bool with_rhs) {
+template <typename T, int TEAM>
+__device__ void pivot_bc(const LineCtx<T, TEAM>& L, int i, bool factor, bool with_rhs) {
   const int n = L.n, lane = L.lane;
   T* D = L.blk(i, 3);
   T* ri = L.rhs(i);
@@ -115,7 +121,7 @@ __device__ void pivot_bc(const LineCtx<T>& L, int i, bool factor, bool with_rhs)
       const int w = 4 - nc;
       const int ncol = w + 5 * nr + (with_rhs ? 1 : 0);
       const int total = w * ncol;
-      for (int idx = lane; idx < total; idx += 32) {
+      for (int idx = lane; idx < total; idx += TEAM) {
         const int l = nc + 1 + idx / ncol, j = idx % ncol;
         const T mult = negmul(D[l * 5 + nc], r);
         T *X, *Xp;
@@ -134,12 +140,12 @@ __device__ void pivot_bc(const LineCtx<T>& L, int i, bool factor, bool with_rhs)
         *X = fmac(*X, mult, *Xp);
         if (j == 0) mults[l] = mult;
       }
-      __syncwarp();
+      L.sync();
       if (lane < w) D[(nc + 1 + lane) * 5 + nc] = mults[nc + 1 + lane];
-      __syncwarp();
+      L.sync();
     }
     if (lane == 0) facts[4] = rcp(D[24]);
-    __syncwarp();
+    L.sync();
     // B: multipliers of the rows below (src/cpenta1bc.f:75-83), in place.
     if (lane < 5 * nt) {
       const int t = i + 1 + lane / 5, m = lane % 5;
@@ -155,7 +161,7 @@ __device__ void pivot_bc(const LineCtx<T>& L, int i, bool factor, bool with_rhs)
         for (int q = nc + 1; q < 5; ++q) acc[q] = fmac(acc[q], M, D[nc * 5 + q]);
       }
     }
-    __syncwarp();
+    L.sync();
   } else if (with_rhs) {
     // forward elimination with stored multipliers (src/cpenta1bc.f:505-512)
     if (lane < 5) {
@@ -166,12 +172,12 @@ __device__ void pivot_bc(const LineCtx<T>& L, int i, bool factor, bool with_rhs)
       }
       ri[lane] = acc;
     }
-    __syncwarp();
+    L.sync();
   }
 
   // C: Schur update of the rows below (src/cpenta1bc.f:84-101)
   const int per = (factor ? 25 * nr : 0) + (with_rhs ? 5 : 0);
-  for (int idx = lane; idx < nt * per; idx += 32) {
+  for (int idx = lane; idx < nt * per; idx += TEAM) {
     const int a = idx / per, j = idx % per, t = i + 1 + a;
     const T* M = L.blk(t, slot_bc(t, i));
     if (factor && j < 25 * nr) {
@@ -191,13 +197,13 @@ __device__ void pivot_bc(const LineCtx<T>& L, int i, bool factor, bool with_rhs)
       rt[m] = acc;
     }
   }
-  __syncwarp();
+  L.sync();
 }
 
 // Back substitution of row i (src/cpenta1bc.f:760-847); x of the rows to
 // the right are the already solved right-hand sides in the ring.
-template <typename T>
-__device__ void backsub_bc(const LineCtx<T>& L, int i) {
+template <typename T, int TEAM>
+__device__ void backsub_bc(const LineCtx<T, TEAM>& L, int i) {
   const int n = L.n, lane = L.lane;
   const T* D = L.blk(i, 3);
   T* ri = L.rhs(i);
@@ -219,17 +225,28 @@ __device__ void backsub_bc(const LineCtx<T>& L, int i) {
     }
     ri[m] = acc;
   }
-  __syncwarp();
+  L.sync();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(32 * kWarpsPerCta) penta_bc_kernel(PentaArgs args) {
+// TEAM = 32: kWarpsPerCta lines per CTA, one per warp; TEAM > 32: one line
+// per CTA of TEAM threads.
+template <typename T, int TEAM = 32>
+__global__ void __launch_bounds__(TEAM == 32 ? 32 * kWarpsPerCta : TEAM) penta_bc_kernel(PentaArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int iv = blockIdx.x * kWarpsPerCta + warp;
-  if (iv >= args.nsys) return;  // whole warps exit; only __syncwarp is used below
-  T* base = reinterpret_cast<T*>(smem_raw) + warp * (kRing * kRowSz + 16);
-  LineCtx<T> L{base, base + kRing * kRowSz, &args, iv, lane, args.n};
+  int iv, lane;
+  T* base;
+  if constexpr (TEAM == 32) {
+    const int warp = threadIdx.x / 32;
+    lane = threadIdx.x % 32;
+    iv = blockIdx.x * kWarpsPerCta + warp;
+    base = reinterpret_cast<T*>(smem_raw) + warp * (kRing * kRowSz + 16);
+  } else {
+    lane = threadIdx.x;
+    iv = blockIdx.x;
+    base = reinterpret_cast<T*>(smem_raw);
+  }
+  if (iv >= args.nsys) return;  // whole teams exit; only team barriers are used below
+  LineCtx<T, TEAM> L{base, base + kRing * kRowSz, &args, iv, lane, args.n};
   const int n = args.n;
   const bool factor = args.code != 1, solve = args.code != 0;
 
@@ -247,19 +264,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) penta_bc_kernel(PentaArgs a
       cp_async_commit();
       cp_async_wait<1>();
     }
-    __syncwarp();
+    L.sync();
     pivot_bc(L, i, factor, solve);
     if (args.status && lane == 0 && factor && !finite_s(L.blk(i, 3)[24])) atomicExch(args.status, 1);
     // rows n-4..n stay resident for the back substitution
     if (i < n - 4 || !solve) L.store_row(i, factor, solve);
-    __syncwarp();
+    L.sync();
   }
   if (!solve) return;
   // backward sweep
   for (int i = n; i >= 1; --i) {
     if (i < n - 4) {
       cp_async_wait<0>();
-      __syncwarp();
+      L.sync();
     }
     if (i - 1 >= 1 && i - 1 < n - 4) {
       L.load_row(i - 1, true);

@@ -8,7 +8,9 @@
 //   per(1|2, row)      columns n-1 | n of rows 1..n-3 (row n-3's column n-1
 //                      is its slot 5);
 //   per2(n-1|n, col)   rows n-1 | n at the columns left of their band.
-// One warp owns a line.  Band rows 1..n-2 stream through a shared-memory
+// A team of TEAM threads owns a line (one warp, or a CTA of 64..256 threads
+// when there are few lines; results do not depend on TEAM).  Band rows
+// 1..n-2 stream through a shared-memory
 // ring (with their per blocks); rows n-1 and n stay resident for the whole
 // elimination, with their fill held in a three-column window.  Each pivot
 // row has up to four blocks right of the diagonal (i+1, i+2, n-1, n) and up
@@ -38,14 +40,18 @@ struct PeriodicArgs {
   int* status;
 };
 
-template <typename T>
+template <typename T, int TEAM = 32>
 struct PLine {
   T* ring;     // kRing rows of kPRowSz: [0,125) slots, [125,175) per(1), per(2), [175,180) rhs
   T* res;      // rows n-1, n: 125 slots + 5 rhs each
   T* fw;       // fill windows of rows n-1, n: 3 blocks each, column c at (c-1)%3
   T* scratch;
   const PeriodicArgs* a;
-  int iv, lane, n;
+  int iv, lane, n;  // lane: thread index within the team
+  __device__ void sync() const {
+    if constexpr (TEAM == 32) __syncwarp();
+    else __syncthreads();
+  }
 
   __device__ T* ringrow(int r) const { return ring + ((r - 1) % kRing) * kPRowSz; }
   __device__ long long rec(int r) const { return a->row_stride * (r - 1) + a->line_stride * iv; }
@@ -74,13 +80,13 @@ struct PLine {
   __device__ void load_band_row(int r, bool factor, bool with_rhs) const {
     const T* gm = reinterpret_cast<const T*>(a->mat) + 125 * rec(r);
     T* s = ringrow(r);
-    for (int e = lane; e < 125; e += 32) {
+    for (int e = lane; e < 125; e += TEAM) {
       const int k = e % 5, m = (e / 5) % 5, q = e / 25;
       cp_async_el(s + k * 25 + m * 5 + q, gm + e);
     }
     if (!factor) {  // factored per blocks from the earlier factorisation
       const T* gp = reinterpret_cast<const T*>(a->per) + 50 * rec(r);
-      for (int e = lane; e < 50; e += 32) {
+      for (int e = lane; e < 50; e += TEAM) {
         const int j = e % 2, m = (e / 2) % 5, q = e / 10;
         cp_async_el(s + 125 + 25 * j + m * 5 + q, gp + e);
       }
@@ -90,7 +96,7 @@ struct PLine {
   // Fill set-up of a freshly landed band row, src/penta2p.f:44-51.
   __device__ void setup_band_row(int r) const {
     T* s = ringrow(r);
-    for (int e = lane; e < 50; e += 32) {
+    for (int e = lane; e < 50; e += TEAM) {
       const int j = e / 25, mq = e % 25;
       T v = zero<T>();
       if (r == 1) v = s[25 * j + mq];          // per(1) = slot 1, per(2) = slot 2
@@ -102,12 +108,12 @@ struct PLine {
     T* s = ringrow(r);
     if (with_mat) {
       T* gm = reinterpret_cast<T*>(a->mat) + 125 * rec(r);
-      for (int e = lane; e < 125; e += 32) {
+      for (int e = lane; e < 125; e += TEAM) {
         const int k = e % 5, m = (e / 5) % 5, q = e / 25;
         gm[e] = s[k * 25 + m * 5 + q];
       }
       T* gp = reinterpret_cast<T*>(a->per) + 50 * rec(r);
-      for (int e = lane; e < 50; e += 32) {
+      for (int e = lane; e < 50; e += TEAM) {
         const int j = e % 2, m = (e / 2) % 5, q = e / 10;
         gp[e] = s[125 + 25 * j + m * 5 + q];
       }
@@ -118,7 +124,7 @@ struct PLine {
     for (int rr = 0; rr < 2; ++rr) {
       const T* gm = reinterpret_cast<const T*>(a->mat) + 125 * rec(n - 1 + rr);
       T* s = res + rr * 130;
-      for (int e = lane; e < 125; e += 32) {
+      for (int e = lane; e < 125; e += TEAM) {
         const int k = e % 5, m = (e / 5) % 5, q = e / 25;
         cp_async_el(s + k * 25 + m * 5 + q, gm + e);
       }
@@ -131,7 +137,7 @@ struct PLine {
       T* s = res + rr * 130;
       if (with_mat) {
         T* gm = reinterpret_cast<T*>(a->mat) + 125 * rec(n - 1 + rr);
-        for (int e = lane; e < 125; e += 32) {
+        for (int e = lane; e < 125; e += TEAM) {
           const int k = e % 5, m = (e / 5) % 5, q = e / 25;
           gm[e] = s[k * 25 + m * 5 + q];
         }
@@ -143,7 +149,7 @@ struct PLine {
   __device__ void store_fill(int col) const {
     if (!a->store_per2) return;
     T* gp = reinterpret_cast<T*>(a->per2) + 50 * rec(col);
-    for (int e = lane; e < 50; e += 32) {
+    for (int e = lane; e < 50; e += TEAM) {
       const int j = e % 2, m = (e / 2) % 5, q = e / 10;
       const int lim = j == 0 ? n - 4 : n - 3;
       if (col <= lim) gp[e] = fw[75 * j + 25 * ((col - 1) % 3) + m * 5 + q];
@@ -151,7 +157,7 @@ struct PLine {
   }
   __device__ void load_fill(int col) const {
     const T* gp = reinterpret_cast<const T*>(a->per2) + 50 * rec(col);
-    for (int e = lane; e < 50; e += 32) {
+    for (int e = lane; e < 50; e += TEAM) {
       const int j = e % 2, m = (e / 2) % 5, q = e / 10;
       const int lim = j == 0 ? n - 4 : n - 3;
       if (col <= lim) fw[75 * j + 25 * ((col - 1) % 3) + m * 5 + q] = gp[e];
@@ -162,19 +168,19 @@ struct PLine {
   __device__ void clear_unused_fill() const {
     for (int r = n - 1; r <= n + 1; ++r) {
       T* gp = reinterpret_cast<T*>(a->per) + 50 * rec(r);
-      for (int e = lane; e < 50; e += 32) gp[e] = zero<T>();
+      for (int e = lane; e < 50; e += TEAM) gp[e] = zero<T>();
     }
     if (!a->store_per2) return;
     for (int c = n - 3; c <= n + 1; ++c) {
       T* gp = reinterpret_cast<T*>(a->per2) + 50 * rec(c);
-      for (int e = lane; e < 50; e += 32) {
+      for (int e = lane; e < 50; e += TEAM) {
         const int lim = (e % 2) == 0 ? n - 4 : n - 3;
         if (c > lim) gp[e] = zero<T>();
       }
     }
   }
   __device__ void zero_fill(int col) const {
-    for (int e = lane; e < 50; e += 32) fw[75 * (e / 25) + 25 * ((col - 1) % 3) + e % 25] = zero<T>();
+    for (int e = lane; e < 50; e += TEAM) fw[75 * (e / 25) + 25 * ((col - 1) % 3) + e % 25] = zero<T>();
   }
 };
 
@@ -191,8 +197,8 @@ __device__ __forceinline__ int p_cols(int i, int n, int* c) {
   return cnt;  // ascending by construction
 }
 
-template <typename T>
-__device__ void pivot_p(const PLine<T>& L, int i, bool factor, bool with_rhs) {
+template <typename T, int TEAM>
+__device__ void pivot_p(const PLine<T, TEAM>& L, int i, bool factor, bool with_rhs) {
   const int n = L.n, lane = L.lane;
   T* D = L.get(i, i);
   T* ri = L.rhs(i);
@@ -208,7 +214,7 @@ __device__ void pivot_p(const PLine<T>& L, int i, bool factor, bool with_rhs) {
       if (lane == 0) facts[nc] = r;
       const int w = 4 - nc;
       const int ncol = w + 5 * nr + (with_rhs ? 1 : 0);
-      for (int idx = lane; idx < w * ncol; idx += 32) {
+      for (int idx = lane; idx < w * ncol; idx += TEAM) {
         const int l = nc + 1 + idx / ncol, j = idx % ncol;
         const T mult = negmul(D[l * 5 + nc], r);
         T *X, *Xp;
@@ -227,12 +233,12 @@ __device__ void pivot_p(const PLine<T>& L, int i, bool factor, bool with_rhs) {
         *X = fmac(*X, mult, *Xp);
         if (j == 0) mults[l] = mult;
       }
-      __syncwarp();
+      L.sync();
       if (lane < w) D[(nc + 1 + lane) * 5 + nc] = mults[nc + 1 + lane];
-      __syncwarp();
+      L.sync();
     }
     if (lane == 0) facts[4] = rcp(D[24]);
-    __syncwarp();
+    L.sync();
     if (lane < 5 * nt) {
       const int t = tg[lane / 5], m = lane % 5;
       T* B = L.get(t, i);
@@ -247,7 +253,7 @@ __device__ void pivot_p(const PLine<T>& L, int i, bool factor, bool with_rhs) {
         for (int q = nc + 1; q < 5; ++q) acc[q] = fmac(acc[q], M, D[nc * 5 + q]);
       }
     }
-    __syncwarp();
+    L.sync();
   } else if (with_rhs) {
     if (lane < 5) {
       T acc = ri[lane];
@@ -257,11 +263,11 @@ __device__ void pivot_p(const PLine<T>& L, int i, bool factor, bool with_rhs) {
       }
       ri[lane] = acc;
     }
-    __syncwarp();
+    L.sync();
   }
 
   const int per = (factor ? 25 * nr : 0) + (with_rhs ? 5 : 0);
-  for (int idx = lane; idx < nt * per; idx += 32) {
+  for (int idx = lane; idx < nt * per; idx += TEAM) {
     const int t = tg[idx / per], j = idx % per;
     const T* M = L.get(t, i);
     if (factor && j < 25 * nr) {
@@ -283,12 +289,12 @@ __device__ void pivot_p(const PLine<T>& L, int i, bool factor, bool with_rhs) {
       rt[m] = acc;
     }
   }
-  __syncwarp();
+  L.sync();
 }
 
 // x of rows n-1, n live in the resident rows; x of i+1, i+2 in the ring.
-template <typename T>
-__device__ void backsub_p(const PLine<T>& L, int i) {
+template <typename T, int TEAM>
+__device__ void backsub_p(const PLine<T, TEAM>& L, int i) {
   const int n = L.n, lane = L.lane;
   const T* D = L.get(i, i);
   T* ri = L.rhs(i);
@@ -308,18 +314,29 @@ __device__ void backsub_p(const PLine<T>& L, int i) {
     }
     ri[m] = acc;
   }
-  __syncwarp();
+  L.sync();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(32 * kPWarpsPerCta) penta_p_kernel(PeriodicArgs args) {
+// TEAM = 32: kPWarpsPerCta lines per CTA, one per warp; TEAM > 32: one line
+// per CTA of TEAM threads.
+template <typename T, int TEAM = 32>
+__global__ void __launch_bounds__(TEAM == 32 ? 32 * kPWarpsPerCta : TEAM) penta_p_kernel(PeriodicArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int iv = blockIdx.x * kPWarpsPerCta + warp;
-  if (iv >= args.nsys) return;
-  T* base = reinterpret_cast<T*>(smem_raw) + warp * kPWarpSmem;
-  PLine<T> L{base, base + kRing * kPRowSz, base + kRing * kPRowSz + 260, base + kRing * kPRowSz + 410,
-             &args, iv, lane, args.n};
+  int iv, lane;
+  T* base;
+  if constexpr (TEAM == 32) {
+    const int warp = threadIdx.x / 32;
+    lane = threadIdx.x % 32;
+    iv = blockIdx.x * kPWarpsPerCta + warp;
+    base = reinterpret_cast<T*>(smem_raw) + warp * kPWarpSmem;
+  } else {
+    lane = threadIdx.x;
+    iv = blockIdx.x;
+    base = reinterpret_cast<T*>(smem_raw);
+  }
+  if (iv >= args.nsys) return;  // whole teams exit; only team barriers are used below
+  PLine<T, TEAM> L{base, base + kRing * kPRowSz, base + kRing * kPRowSz + 260, base + kRing * kPRowSz + 410,
+                   &args, iv, lane, args.n};
   const int n = args.n;
   const bool factor = args.code != 1, solve = args.code != 0;
 
@@ -329,13 +346,13 @@ __global__ void __launch_bounds__(32 * kPWarpsPerCta) penta_p_kernel(PeriodicArg
   cp_async_commit();
   int loaded = 3;
   cp_async_wait<0>();
-  __syncwarp();
+  L.sync();
   if (factor) {
     // fill set-up, src/penta2p.f:44-57
     for (int r = 1; r <= 3; ++r) L.setup_band_row(r);
-    for (int e = lane; e < 150; e += 32) L.fw[e] = zero<T>();
-    __syncwarp();
-    for (int e = lane; e < 25; e += 32) {
+    for (int e = lane; e < 150; e += TEAM) L.fw[e] = zero<T>();
+    L.sync();
+    for (int e = lane; e < 25; e += TEAM) {
       L.fw[e] = L.slot(n - 1, 5)[e];            // row n-1, column 1
       L.fw[75 + e] = L.slot(n, 4)[e];           // row n, column 1
       L.fw[75 + 25 + e] = L.slot(n, 5)[e];      // row n, column 2
@@ -344,7 +361,7 @@ __global__ void __launch_bounds__(32 * kPWarpsPerCta) penta_p_kernel(PeriodicArg
     L.load_fill(1);
     L.load_fill(2);
   }
-  __syncwarp();
+  L.sync();
 
   for (int i = 1; i <= n; ++i) {
     // band rows up to min(i+2, n-2) must be resident; prefetch one more
@@ -353,20 +370,20 @@ __global__ void __launch_bounds__(32 * kPWarpsPerCta) penta_p_kernel(PeriodicArg
     while (loaded < want) L.load_band_row(++loaded, factor, solve);
     cp_async_commit();
     if (loaded > need) cp_async_wait<1>(); else cp_async_wait<0>();
-    __syncwarp();
+    L.sync();
     // row i+2 lands for this pivot: initialise its fill (rows 1..3 above)
     if (factor && i >= 2 && i + 2 <= n - 2) L.setup_band_row(i + 2);
     if (!factor && solve && i + 2 <= n - 3) L.load_fill(i + 2);
-    __syncwarp();
+    L.sync();
     pivot_p(L, i, factor, solve);
     if (args.status && lane == 0 && factor && !finite_s(L.get(i, i)[24])) atomicExch(args.status, 1);
     if (factor) {
       L.store_fill(i);
-      __syncwarp();
+      L.sync();
       if (i + 3 <= n - 3) L.zero_fill(i + 3);
     }
     if (i <= n - 2 && (i < n - 6 || !solve)) L.store_band_row(i, factor, solve);
-    __syncwarp();
+    L.sync();
   }
   if (factor) L.clear_unused_fill();
   if (!solve) {
@@ -376,7 +393,7 @@ __global__ void __launch_bounds__(32 * kPWarpsPerCta) penta_p_kernel(PeriodicArg
   for (int i = n; i >= 1; --i) {
     if (i <= n - 2 && i < n - 6) {
       cp_async_wait<0>();
-      __syncwarp();
+      L.sync();
     }
     if (i - 1 >= 1 && i - 1 < n - 6) {
       L.load_band_row(i - 1, false, true);
