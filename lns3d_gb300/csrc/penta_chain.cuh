@@ -34,6 +34,8 @@
 // The prep kernels read the factors in one precision (TM) and write the
 // internal form in the precision of the sweeps (TC), computing in FP64.
 #pragma once
+#include <type_traits>
+
 #include "penta_direct.cuh"
 
 namespace lns {
@@ -782,14 +784,33 @@ __device__ __forceinline__ void fill_body(const Args& a, long long bx) {
 #pragma unroll
   for (int k = 0; k < 5; ++k) xn1[k] = xa[k], xn0[k] = xb[k];
   T* r = grhs + 5 * rc;
+  if constexpr (std::is_same<T, cf>::value) {
+    // FP32 records are 400 B and 16-byte aligned: read them as 25 16-byte
+    // loads, entry e = m + 5 q (+ 25 for E0) in storage order, which is also
+    // each output's order of accumulation below.
+    const float4* E4 = reinterpret_cast<const float4*>(E);
+    T acc[5];
 #pragma unroll
-  for (int mm = 0; mm < 5; ++mm) {
-    T acc = r[mm];
+    for (int mm = 0; mm < 5; ++mm) acc[mm] = r[mm];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[mm + 5 * k], xn1[k]);
+    for (int k = 0; k < 25; ++k) {
+      const float4 w = E4[k];
+      const int e0 = 2 * k, e1 = 2 * k + 1;
+      acc[e0 % 5] = fmsc(acc[e0 % 5], cf{w.x, w.y}, e0 < 25 ? xn1[e0 / 5] : xn0[(e0 - 25) / 5]);
+      acc[e1 % 5] = fmsc(acc[e1 % 5], cf{w.z, w.w}, e1 < 25 ? xn1[e1 / 5] : xn0[(e1 - 25) / 5]);
+    }
 #pragma unroll
-    for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[25 + mm + 5 * k], xn0[k]);
-    r[mm] = acc;
+    for (int mm = 0; mm < 5; ++mm) r[mm] = acc[mm];
+  } else {
+#pragma unroll
+    for (int mm = 0; mm < 5; ++mm) {
+      T acc = r[mm];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[mm + 5 * k], xn1[k]);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[25 + mm + 5 * k], xn0[k]);
+      r[mm] = acc;
+    }
   }
 }
 
