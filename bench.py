@@ -544,11 +544,12 @@ def serve_stream(n, rate=50.0, seed=5):
     return reqs
 
 
-def run_serve(torch, n_requests=100, rate=50.0, tol=1e-10, max_steps=2000, serial_sample=3):
+def run_serve(torch, n_requests=100, rate=50.0, tol=1e-10, max_steps=2000, serial_every=10):
     """The serving leg: a prefix of the stream through lns_server3d (mixed
     precision, continuous batching, 64 slots, 64 GiB budget) in real time,
-    and a sample of the same requests solved one at a time by the FP64
-    drop-in step, for the serial comparison."""
+    and every serial_every-th request of the same prefix solved one at a time
+    by the FP64 drop-in step, for the serial comparison (solves per second of
+    the sample, the same tolerance and step limit)."""
     import numpy as np
 
     import lns3d_gb300 as g
@@ -571,10 +572,13 @@ def run_serve(torch, n_requests=100, rate=50.0, tol=1e-10, max_steps=2000, seria
     polls = [srv.poll(i) for i in ids]
     lat = np.array(sorted(p["latency_s"] for p in polls))
     done = sum(p["state"] == "done" for p in polls)
+    pts = np.array([c["params"]["nx"] * c["params"]["ny"] for c in cases], dtype=np.float64)
+    served_pt_steps = float(sum(p["steps"] * n for p, n in zip(polls, pts)))
     srv.close()
-    # serial FP64 drop-in solves of the first requests of the stream
-    ser = []
-    for c in cases[:serial_sample]:
+    # serial FP64 drop-in solves of every serial_every-th request
+    ser, ser_pt_steps = [], 0.0
+    for k in range(0, n_requests, serial_every):
+        c = cases[k]
         d = g.ImpDrv3D(c["params"], c["metrics"], c["vm"], cflmax=CFL3, loctime=1, precision=g.adi3d.FP64)
         v = torch.from_numpy(c["v"].ravel(order="F")).cuda()
         res = torch.zeros(max_steps, dtype=torch.float64, device="cuda")
@@ -587,11 +591,15 @@ def run_serve(torch, n_requests=100, rate=50.0, tol=1e-10, max_steps=2000, seria
             if float(res[steps - 1].item()) <= tol:
                 break
         ser.append(time.perf_counter() - ts)
+        ser_pt_steps += steps * pts[k]
+        d.close()
     return {"workload": "serve-%d-of-1000-requests-poisson-%g-per-s-mixed-to-1e-10" % (n_requests, rate),
             "requests": n_requests, "converged": int(done), "wall_s": wall, "solves_per_s": n_requests / wall,
+            "pt_steps_per_s": served_pt_steps / wall,
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-            "serial_fp64": {"sample": serial_sample, "mean_solve_s": float(np.mean(ser)),
-                            "solves_per_s": 1.0 / float(np.mean(ser))}}
+            "serial_fp64": {"sample": "every %dth request (%d solves)" % (serial_every, len(ser)),
+                            "mean_solve_s": float(np.mean(ser)), "solves_per_s": len(ser) / float(np.sum(ser)),
+                            "pt_steps_per_s": ser_pt_steps / float(np.sum(ser))}}
 
 
 def main():
