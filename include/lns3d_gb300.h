@@ -148,6 +148,39 @@ int lns_penta1bc_mixed_dev(int32_t nsys, int32_t n, int32_t nblk, const double* 
 int lns_cpenta2bc_mixed(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, int32_t refine);
 
 /* ---------------------------------------------------------------------------
+ * Block-tridiagonal line solves of the second-order implicit path (iLHS = 0
+ * of src/impdrv.f90:307-344), real FP64, factor and right-hand side in one
+ * pass as the reference does:
+ *   lns_solve2bc  replaces solve2bc(n,nsys,nblk,mat,rhs,bc),   src/nsolve2bc.f90:2
+ *   lns_solve1bc  replaces solve1bc(nsys,n,nblk,mat,rhs,bc),   src/nsolve1bc.f90:2
+ *   lns_solve2p   replaces solve2p(np,nsys,nblk,mat,rhs,per,per2), src/nsolve2p.f90:2
+ *   lns_solve1p   replaces solve1p(nsys,np,nblk,mat,rhs,per,per2), src/nsolve1p.f90:2
+ * mat(3,nblk,nblk,n,nsys) ("2") or (3,nblk,nblk,nsys,n) ("1"): slot 1, 2, 3
+ * = columns i-1, i, i+1; bc(14,nblk,nblk,nsys): the blocks the second-order
+ * boundary rows add (rows 1..3 and n-2..n reach five columns,
+ * src/nsolve2bc.f90:40-420); periodic lines have np = n+1 rows, row np
+ * repeats row 1, and per, per2 are the reference's fill scratch (not used:
+ * the GPU keeps its fill in the workspace).  nblk must be 5; n >= 8 (np >= 9).
+ * The solution replaces rhs; mat and bc are read only.  The host forms
+ * stage through library-owned device buffers; the _dev forms take device
+ * pointers and a device workspace of lns_tri_workspace_bytes(rows, nsys,
+ * periodic) bytes (rows = n, or np for periodic lines).
+ */
+size_t lns_tri_workspace_bytes(int32_t rows, int32_t nsys, int32_t periodic);
+int lns_solve2bc(int32_t n, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* bc);
+int lns_solve1bc(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs, double* bc);
+int lns_solve2p(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per, double* per2);
+int lns_solve1p(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per, double* per2);
+int lns_solve2bc_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, const double* bc,
+                     void* work, void* stream);
+int lns_solve1bc_dev(int32_t nsys, int32_t n, int32_t nblk, const double* mat, double* rhs, const double* bc,
+                     void* work, void* stream);
+int lns_solve2p_dev(int32_t np, int32_t nsys, int32_t nblk, const double* mat, double* rhs, void* work,
+                    void* stream);
+int lns_solve1p_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, double* rhs, void* work,
+                    void* stream);
+
+/* ---------------------------------------------------------------------------
  * The nonlinear two-dimensional implicit ADI step (src/impdrv.f90:171-400
  * with linear = 0, impl = 1, iLHS = 1) as one device-resident context, FP64
  * throughout.  Per step: set_time_step on the state, vold = v, itrBC; per

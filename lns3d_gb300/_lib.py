@@ -38,6 +38,14 @@ SIGNATURES = {
     "lns_cpenta1bc": [I32, I32, I32, DP, DP, I32],
     "lns_cpenta1bc_dev": [I32, I32, I32, DP, DP, I32, P],
     "lns_set_periodic_exact": [I32],
+    "lns_solve2bc": [I32, I32, I32, DP, DP, DP],
+    "lns_solve1bc": [I32, I32, I32, DP, DP, DP],
+    "lns_solve2p": [I32, I32, I32, DP, DP, DP, DP],
+    "lns_solve1p": [I32, I32, I32, DP, DP, DP, DP],
+    "lns_solve2bc_dev": [I32, I32, I32, DP, DP, DP, P, P],
+    "lns_solve1bc_dev": [I32, I32, I32, DP, DP, DP, P, P],
+    "lns_solve2p_dev": [I32, I32, I32, DP, DP, P, P],
+    "lns_solve1p_dev": [I32, I32, I32, DP, DP, P, P],
     "lns_penta2p": [I32, I32, I32, DP, DP, DP, DP],
     "lns_penta2p_dev": [I32, I32, I32, DP, DP, DP, DP, P],
     "lns_penta1p": [I32, I32, I32, DP, DP, DP, DP],
@@ -125,6 +133,8 @@ def lib():
         L.lns_probe_fp64_tflops.argtypes = []
         L.lns_mixed_workspace_bytes.restype = ctypes.c_size_t
         L.lns_mixed_workspace_bytes.argtypes = [I32, I32, I32, I32]
+        L.lns_tri_workspace_bytes.restype = ctypes.c_size_t
+        L.lns_tri_workspace_bytes.argtypes = [I32, I32, I32]
         L.lns_ctx3d_bytes.restype = ctypes.c_size_t
         L.lns_ctx3d_bytes.argtypes = [P]
         L.lns_server3d_bytes_in_use.restype = ctypes.c_size_t

@@ -486,3 +486,182 @@ int lns_cpenta2bc_mixed_static_dev(int32_t n, int32_t nsys, int32_t nblk, const 
 }
 
 }  // extern "C"
+
+// ======================================================================
+// Block-tridiagonal solvers of the second-order implicit path (iLHS = 0):
+// solve1bc / solve2bc (src/nsolve1bc.f90:2, src/nsolve2bc.f90:2) and
+// solve1p / solve2p (src/nsolve1p.f90:2, src/nsolve2p.f90:2)
+// ======================================================================
+// A block-tridiagonal line, with the blocks that its second-order boundary
+// rows add (bc(14,5,5,nsys)), is a block-pentadiagonal line whose other
+// blocks are zero, and the reference eliminates it in the pentadiagonal
+// solvers' order; each line is copied into pentadiagonal records in a
+// workspace and solved (factor and right-hand side in one pass) by the
+// pentadiagonal kernels.  Updates by the zero blocks add exact zeros.
+namespace {
+
+// Source of the block of row t at column c of a boundary-closure line:
+// > 0 the mat slot, < 0 minus the bc index, 0 none (src/nsolve2bc.f90:40-420).
+__device__ __forceinline__ int tri_src_bc(int t, int c, int n) {
+  const int tab[6][5] = {{2, 3, -1, -2, -3},      // row 1, columns 1..5
+                         {1, 2, 3, -4, -5},       // row 2
+                         {-7, 1, 2, 3, -6},       // row 3
+                         {-8, 1, 2, 3, -9},       // row n-2, columns n-4..n
+                         {-10, -11, 1, 2, 3},     // row n-1
+                         {-12, -13, -14, 1, 2}};  // row n
+  int r = -1, c0 = 1;
+  if (t <= 3) r = t - 1;
+  else if (t >= n - 2) r = t - (n - 2) + 3, c0 = n - 4;
+  if (r >= 0) {
+    const int a = c - c0;
+    return a >= 0 && a < 5 ? tab[r][a] : 0;
+  }
+  const int k = c - t + 2;
+  return k >= 1 && k <= 3 ? k : 0;
+}
+
+// Column held by slot k (1..5) of row t of a pentadiagonal boundary-closure
+// line (the inverse of lns::slot_bc).
+__device__ __forceinline__ int col_of_slot_bc(int t, int k, int n) {
+  const int r1[5] = {4, 5, 1, 2, 3}, r2[5] = {5, 1, 2, 3, 4};
+  const int o1[5] = {-3, -2, -1, 0, -4}, o0[5] = {-2, -1, 0, -4, -3};
+  if (t == 1) return r1[k - 1];
+  if (t == 2) return r2[k - 1];
+  if (t == n - 1) return n + o1[k - 1];
+  if (t == n) return n + o0[k - 1];
+  return t + k - 3;
+}
+
+// One thread per entry of the pentadiagonal records of rows 1..rows.
+__global__ void tri_to_penta_kernel(const double* __restrict__ tmat, const double* __restrict__ bc,
+                                    double* __restrict__ pmat, int rows, int n, int nsys, long long rs,
+                                    long long ls, int periodic) {
+  const long long task = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (task >= (long long)rows * nsys * 125) return;
+  const int e = (int)(task % 25), k = (int)((task / 25) % 5) + 1;
+  const long long rr = task / 125;
+  const int t = (int)(rr % rows) + 1, iv = (int)(rr / rows);
+  const long long rec = rs * (t - 1) + ls * iv;
+  const int mq = e;  // m + 5 q
+  double v = 0.0;
+  if (periodic) {
+    if (t <= n && k >= 2 && k <= 4) v = tmat[(k - 2) + 3 * mq + 75 * rec];
+  } else {
+    const int s = tri_src_bc(t, col_of_slot_bc(t, k, n), n);
+    if (s > 0) v = tmat[(s - 1) + 3 * mq + 75 * rec];
+    else if (s < 0) v = bc[(-s - 1) + 14 * mq + 350LL * iv];
+  }
+  pmat[(k - 1) + 5 * mq + 125 * rec] = v;
+}
+
+size_t tri_work_bytes(int rows, int nsys, bool periodic) {
+  return sizeof(double) * (size_t)rows * nsys * (125 + (periodic ? 50 : 0));
+}
+
+int check_tri(int rows, int nsys, int nblk, bool periodic, const char* who) {
+  if (nblk != 5) return fail(LNS_ERR_ARG, std::string(who) + ": nblk must be 5");
+  if (nsys < 0) return fail(LNS_ERR_ARG, std::string(who) + ": nsys < 0");
+  if (rows < (periodic ? 9 : 8))
+    return fail(LNS_ERR_ARG, std::string(who) + (periodic ? ": lines need np >= 9 rows" : ": lines need n >= 8 rows") +
+                                 " (the reference's boundary rows would overlap)");
+  return LNS_OK;
+}
+
+// Device form: convert into the workspace, then factor and solve.
+int tri_dev(int layout, bool periodic, int rows, int nsys, const double* tmat, double* rhs, const double* bc,
+            void* work, cudaStream_t st, int* status) {
+  if (nsys == 0) return LNS_OK;
+  if (!tmat || !rhs || !work || (!periodic && !bc)) return fail(LNS_ERR_ARG, "tridiagonal solve: null argument");
+  const int n = periodic ? rows - 1 : rows;
+  const long long rs = layout == 2 ? 1 : nsys, ls = layout == 2 ? rows : 1;
+  double* pmat = reinterpret_cast<double*>(work);
+  double* per = pmat + (size_t)125 * rows * nsys;
+  const long long total = (long long)rows * nsys * 125;
+  tri_to_penta_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(tmat, bc, pmat, rows, n, nsys, rs, ls,
+                                                                      periodic ? 1 : 0);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "tri_to_penta_kernel launch");
+  if (periodic) return launch_p<double>(pmat, rhs, per, nullptr, rows, nsys, rs, ls, 2, st, status, 1);
+  return launch_bc<double>(pmat, rhs, rows, nsys, rs, ls, 2, st, status);
+}
+
+// Host form: stage, solve, copy the solution back (mat and bc are left as
+// they were; the reference's copies are scratch on return).
+int tri_host(int layout, bool periodic, int rows, int nsys, const double* tmat, double* rhs, const double* bc) {
+  if (nsys == 0) return LNS_OK;
+  if (!tmat || !rhs || (!periodic && !bc)) return fail(LNS_ERR_ARG, "tridiagonal solve: null argument");
+  std::lock_guard<std::mutex> lock(g_stage.mu);
+  const size_t mat_b = sizeof(double) * 75 * (size_t)rows * nsys, rhs_b = sizeof(double) * 5 * (size_t)rows * nsys;
+  const size_t bc_b = sizeof(double) * 350 * (size_t)nsys;
+  void *dm = nullptr, *dr = nullptr, *db = nullptr, *dw = nullptr;
+  int rc = stage_get(0, mat_b, &dm);
+  if (!rc) rc = stage_get(1, rhs_b, &dr);
+  if (!rc && !periodic) rc = stage_get(2, bc_b, &db);
+  if (!rc) rc = stage_get(3, tri_work_bytes(rows, nsys, periodic), &dw);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(dm, tmat, mat_b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dr, rhs, rhs_b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !periodic) e = cudaMemcpy(db, bc, bc_b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(g_stage.status, 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_fail(e, "stage tridiagonal line");
+  rc = tri_dev(layout, periodic, rows, nsys, (const double*)dm, (double*)dr, (const double*)db, dw, 0,
+               g_stage.status);
+  if (rc) return rc;
+  e = cudaMemcpy(rhs, dr, rhs_b, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "copy rhs to host");
+  int status = 0;
+  e = cudaMemcpy(&status, g_stage.status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "copy status to host");
+  if (status) return fail(LNS_ERR_PIVOT, "zero or non-finite pivot");
+  return LNS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t lns_tri_workspace_bytes(int32_t rows, int32_t nsys, int32_t periodic) {
+  if (rows < 1 || nsys < 0) return 0;
+  return tri_work_bytes(rows, nsys, periodic != 0);
+}
+
+int lns_solve2bc(int32_t n, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* bc) {
+  int rc = check_tri(n, nsys, nblk, false, "solve2bc");
+  return rc ? rc : tri_host(2, false, n, nsys, mat, rhs, bc);
+}
+int lns_solve1bc(int32_t nsys, int32_t n, int32_t nblk, double* mat, double* rhs, double* bc) {
+  int rc = check_tri(n, nsys, nblk, false, "solve1bc");
+  return rc ? rc : tri_host(1, false, n, nsys, mat, rhs, bc);
+}
+int lns_solve2p(int32_t np, int32_t nsys, int32_t nblk, double* mat, double* rhs, double* per, double* per2) {
+  (void)per, (void)per2;  // the reference's fill scratch; the GPU keeps its fill in the workspace
+  int rc = check_tri(np, nsys, nblk, true, "solve2p");
+  return rc ? rc : tri_host(2, true, np, nsys, mat, rhs, nullptr);
+}
+int lns_solve1p(int32_t nsys, int32_t np, int32_t nblk, double* mat, double* rhs, double* per, double* per2) {
+  (void)per, (void)per2;
+  int rc = check_tri(np, nsys, nblk, true, "solve1p");
+  return rc ? rc : tri_host(1, true, np, nsys, mat, rhs, nullptr);
+}
+int lns_solve2bc_dev(int32_t n, int32_t nsys, int32_t nblk, const double* mat, double* rhs, const double* bc,
+                     void* work, void* stream) {
+  int rc = check_tri(n, nsys, nblk, false, "solve2bc");
+  return rc ? rc : tri_dev(2, false, n, nsys, mat, rhs, bc, work, (cudaStream_t)stream, nullptr);
+}
+int lns_solve1bc_dev(int32_t nsys, int32_t n, int32_t nblk, const double* mat, double* rhs, const double* bc,
+                     void* work, void* stream) {
+  int rc = check_tri(n, nsys, nblk, false, "solve1bc");
+  return rc ? rc : tri_dev(1, false, n, nsys, mat, rhs, bc, work, (cudaStream_t)stream, nullptr);
+}
+int lns_solve2p_dev(int32_t np, int32_t nsys, int32_t nblk, const double* mat, double* rhs, void* work,
+                    void* stream) {
+  int rc = check_tri(np, nsys, nblk, true, "solve2p");
+  return rc ? rc : tri_dev(2, true, np, nsys, mat, rhs, nullptr, work, (cudaStream_t)stream, nullptr);
+}
+int lns_solve1p_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, double* rhs, void* work,
+                    void* stream) {
+  int rc = check_tri(np, nsys, nblk, true, "solve1p");
+  return rc ? rc : tri_dev(1, true, np, nsys, mat, rhs, nullptr, work, (cudaStream_t)stream, nullptr);
+}
+
+}  // extern "C"

@@ -130,3 +130,57 @@ def set_periodic_exact(on):
     """True: later periodic factorisations are the exact LU; False (default):
     they reproduce the reference's fill placement at row n-5."""
     check(lib().lns_set_periodic_exact(1 if on else 0), "set_periodic_exact")
+
+
+# ---------------------------------------------------------------------------
+# Block-tridiagonal solves of the second-order implicit path (iLHS = 0):
+# src/nsolve{1,2}{bc,p}.f90, same argument order.  Host numpy arrays or
+# CUDA torch tensors (float64); the device form allocates its workspace
+# with torch.
+
+
+def _tri(name, dims, rows, nsys, nblk, mat, rhs, bc=None):
+    n_rows = rows * nsys
+    pm, dev_m = _buf(mat, False, 75 * n_rows, "mat")
+    pr, dev_r = _buf(rhs, False, 5 * n_rows, "rhs")
+    bufs, devs = [pm, pr], {dev_m, dev_r}
+    if bc is not None:
+        pb, dev_b = _buf(bc, False, 350 * nsys, "bc")
+        bufs.append(pb)
+        devs.add(dev_b)
+    if len(devs) != 1:
+        raise ValueError("arrays must all be host arrays or all CUDA tensors")
+    L = lib()
+    if dev_m:
+        import torch
+
+        wb = L.lns_tri_workspace_bytes(rows, nsys, 0 if bc is not None else 1)
+        work = torch.empty(max(wb, 8), dtype=torch.uint8, device=mat.device)
+        rc = getattr(L, "lns_%s_dev" % name)(dims[0], dims[1], nblk, *bufs, ctypes.c_void_p(work.data_ptr()),
+                                             _stream())
+    else:
+        if bc is None:
+            bufs += [ctypes.c_void_p(0), ctypes.c_void_p(0)]
+        rc = getattr(L, "lns_%s" % name)(dims[0], dims[1], nblk, *bufs)
+    check(rc, name)
+
+
+def solve2bc(n, nsys, nblk, mat, rhs, bc):
+    """Block-tridiagonal boundary-closure solve, lines along the first index."""
+    _tri("solve2bc", (n, nsys), n, nsys, nblk, mat, rhs, bc)
+
+
+def solve1bc(nsys, n, nblk, mat, rhs, bc):
+    """Block-tridiagonal boundary-closure solve, lines batched over the first index."""
+    _tri("solve1bc", (nsys, n), n, nsys, nblk, mat, rhs, bc)
+
+
+def solve2p(np_, nsys, nblk, mat, rhs):
+    """Periodic block-tridiagonal solve (np_ rows, the last repeating the first)."""
+    _tri("solve2p", (np_, nsys), np_, nsys, nblk, mat, rhs)
+
+
+def solve1p(nsys, np_, nblk, mat, rhs):
+    """Periodic block-tridiagonal solve, lines batched over the first index."""
+    _tri("solve1p", (nsys, np_), np_, nsys, nblk, mat, rhs)
+

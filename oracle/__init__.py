@@ -33,6 +33,8 @@ def _load(path):
         L.orc_cpenta_bc.argtypes = [i, i, i, p, p, i, i]
         L.orc_cpenta_p.argtypes = [i, i, i, p, p, p, p, i, i]
         L.orc_oob_count.restype = ctypes.c_long
+        L.orc_tri_bc.argtypes = [i, i, i, p, p, p]
+        L.orc_tri_p.argtypes = [i, i, i, p, p]
         _orc[path] = L
     return _orc[path]
 
@@ -64,6 +66,11 @@ def ref(fast=False):
                 getattr(L, "ref_" + nm).argtypes = [i, i, i, p, p, i]
             for nm in ("cpenta1p", "cpenta2p"):
                 getattr(L, "ref_" + nm).argtypes = [i, i, i, p, p, p, p, i]
+            if hasattr(L, "ref_solve2bc"):  # the block-tridiagonal solvers
+                for nm in ("solve1bc", "solve2bc"):
+                    getattr(L, "ref_" + nm).argtypes = [i, i, i, p, p, p]
+                for nm in ("solve1p", "solve2p"):
+                    getattr(L, "ref_" + nm).argtypes = [i, i, i, p, p, p, p]
             _ref[path] = L
     return _ref[path]
 

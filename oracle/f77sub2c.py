@@ -10,13 +10,17 @@ bit-for-bit on the same inputs.  The generated C is a build product, written
 only under ``oracle/_ref/`` (git-ignored); no reference source is copied into
 the repository.
 
-Supported subset (exactly what the eight solver files use):
+Supported subset (exactly what the translated solver files use):
   subroutine header, ``implicit none``, ``integer``/``real``/``complex``
   declarations with explicit-shape (optionally ``lo:hi``) dimensions,
   ``parameter``, ``do v = a, b[, s]`` / ``end do``, ``if (...) then`` /
   ``else`` / ``end if``, assignment, ``return``, ``end``, and the
   ``!$omp parallel do`` directive (translated to ``#pragma omp parallel for``
-  with every scalar assigned inside the loop made private).
+  with every scalar assigned inside the loop made private).  Free-form
+  sources (``.f90``: the block-tridiagonal solvers src/nsolve{1,2}{p,bc}.f90)
+  add ``&`` continuation lines, ``type[, intent(...)|, parameter] :: list``
+  declarations and array-section assignments (``a(:, 1:k, 1, iv) = b(1, :,
+  1:k, 1, iv)``), expanded into loops over the section subscripts in order.
 
 Semantics follow a gfortran build with ``-fdefault-real-8``: ``real`` is
 double, ``complex`` is a pair of doubles, complex multiply is
@@ -255,8 +259,64 @@ def expr_c(text, unit):
     return e
 
 
+def section_loops(lhs_text, rhs_text, unit, pad):
+    """Loops for an array-section assignment: the i-th section subscript of
+    the left side pairs with the i-th of the right side."""
+    def parts(text):
+        m = re.match(r"([a-z_][a-z_0-9]*)\s*\((.*)\)$", text.strip())
+        return m.group(1), split_top(m.group(2))
+    ln, lsub = parts(lhs_text)
+    rn, rsub = parts(rhs_text)
+    def ranges(nm, subs):
+        out = []
+        for k, sb in enumerate(subs):
+            if ":" in sb:
+                lo, hi = sb.split(":")
+                dlo, dhi = unit.dims[nm][k]
+                out.append((k, lo.strip() or dlo, hi.strip() or dhi))
+        return out
+    lr, rr = ranges(ln, lsub), ranges(rn, rsub)
+    if len(lr) != len(rr):
+        raise SyntaxError("non-conforming sections: %s = %s" % (lhs_text, rhs_text))
+    lines, lidx, ridx = [], list(lsub), list(rsub)
+    for a, ((kl, lo, hi), (kr, rlo, _rhi)) in enumerate(zip(lr, rr)):
+        v = "sec_%d" % a
+        lines.append(pad + "  " * a + "for (long %s = 0; %s <= (long)(%s) - (long)(%s); ++%s) {" % (
+            v, v, expr_c(hi, unit)[0], expr_c(lo, unit)[0], v))
+        lidx[kl] = "__SEC%d_L__" % a
+        ridx[kr] = "__SEC%d_R__" % a
+    subs = {}
+    for a, ((kl, lo, _), (kr, rlo, _)) in enumerate(zip(lr, rr)):
+        subs["__sec%d_l__" % a] = "((long)(%s) + sec_%d)" % (expr_c(lo, unit)[0], a)
+        subs["__sec%d_r__" % a] = "((long)(%s) + sec_%d)" % (expr_c(rlo, unit)[0], a)
+    unit.params.update({k: "0" for k in subs})
+    lhs = expr_c("%s(%s)" % (ln, ",".join(lidx)), unit)
+    rhs = expr_c("%s(%s)" % (rn, ",".join(ridx)), unit)
+    for k in subs:
+        del unit.params[k]
+    stmt = "%s = %s;" % (lhs[0], promote(rhs, lhs[1]))
+    for k, v in subs.items():
+        stmt = stmt.replace(k, v)
+    lines.append(pad + "  " * len(lr) + stmt)
+    lines.append(pad + "}" * len(lr))
+    return lines
+
+
 def translate(path):
+    free = path.endswith(".f90")
     src = open(path).read().lower().splitlines()
+    if free:  # join '&' continuation lines
+        joined, cur = [], ""
+        for raw in src:
+            s = raw.split("!")[0].rstrip() if not raw.strip().startswith("!$omp") else raw.rstrip()
+            if cur:
+                s = cur + " " + s.strip().lstrip("&")
+                cur = ""
+            if s.endswith("&") and not s.strip().startswith("!"):
+                cur = s[:-1]
+                continue
+            joined.append(s if s.strip() else raw)
+        src = joined
     stmts = []  # (kind, payload)
     for raw in src:
         s = raw.strip()
@@ -265,7 +325,7 @@ def translate(path):
         if s.startswith("!$omp"):
             stmts.append(("omp", s))
             continue
-        if s.startswith("!") or raw[:1] in ("c", "*") and not raw.startswith(" "):
+        if s.startswith("!") or (not free and raw[:1] in ("c", "*") and not raw.startswith(" ")):
             continue
         s = s.split("!")[0].strip()
         if s:
@@ -280,7 +340,7 @@ def translate(path):
     omp_assigned = set()
     for kind, s in stmts:
         if kind == "omp":
-            if "parallel do" in s:
+            if "parallel do" in s and not re.search(r"end\s+parallel", s):
                 pending_omp = True
             continue
         m = re.match(r"subroutine\s+([a-z_0-9]+)\s*\((.*)\)$", s)
@@ -288,6 +348,17 @@ def translate(path):
             unit = Unit(m.group(1), [a.strip() for a in m.group(2).split(",")])
             continue
         if s == "implicit none":
+            continue
+        m = re.match(r"(integer|real|complex)\s*((?:,\s*[a-z]+(?:\([a-z]+\))?\s*)*)::\s*(.*)$", s)
+        if m:  # free-form declaration: type[, intent(...)][, parameter] :: list
+            typ = {"integer": "int", "real": "real", "complex": "complex"}[m.group(1)]
+            if "parameter" in m.group(2):
+                for it in split_top(m.group(3)):
+                    nm, val = [x.strip() for x in it.split("=")]
+                    unit.params[nm] = val
+                    unit.types[nm] = typ
+            else:
+                unit.declare(typ, parse_decl_items(m.group(3)))
             continue
         m = re.match(r"(integer|real|complex)\s+(.*)$", s)
         if m:
@@ -347,9 +418,12 @@ def translate(path):
         if s == "return":
             body.append("    " * indent + "return;")
             continue
-        if s == "end":
+        if s == "end" or s.startswith("end subroutine"):
             continue
         m = re.match(r"(.*?)=(.*)$", s)
+        if m and ":" in m.group(1):  # array-section assignment
+            body.extend(section_loops(m.group(1).strip(), m.group(2).strip(), unit, "    " * indent))
+            continue
         if m:
             lhs = expr_c(m.group(1).strip(), unit)
             rhs = expr_c(m.group(2).strip(), unit)

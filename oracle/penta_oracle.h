@@ -56,6 +56,13 @@ int orc_cpenta_bc(int layout, int n, int nsys, double* mat, double* rhs, int cod
 int orc_cpenta_p(int layout, int np, int nsys, double* mat, double* rhs,
                  double* per, double* per2, int code, int flags);
 
+/* Block-tridiagonal solves of the second-order path (tri_oracle.c):
+ * solve1bc / solve2bc (src/nsolve{1,2}bc.f90) with the boundary blocks
+ * bc(14,5,5,nsys), n >= 8; solve1p / solve2p (src/nsolve{1,2}p.f90) on
+ * np = n+1 rows, row np = row 1.  mat(3,5,5,...) is read only. */
+int orc_tri_bc(int layout, int n, int nsys, const double* mat, double* rhs, const double* bc);
+int orc_tri_p(int layout, int np, int nsys, const double* mat, double* rhs);
+
 #ifdef __cplusplus
 }
 #endif

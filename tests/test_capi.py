@@ -29,7 +29,8 @@ def lib():
 
 def test_header_declares_entry_points():
     names = declared_symbols()
-    for base in ("penta2bc", "penta1bc", "cpenta2bc", "cpenta1bc", "penta2p", "penta1p", "cpenta2p", "cpenta1p"):
+    for base in ("penta2bc", "penta1bc", "cpenta2bc", "cpenta1bc", "penta2p", "penta1p", "cpenta2p", "cpenta1p",
+                 "solve2bc", "solve1bc", "solve2p", "solve1p"):
         assert "lns_" + base in names and "lns_" + base + "_dev" in names
 
 
@@ -44,7 +45,7 @@ def test_python_signatures_cover_header():
     solver_syms = [n for n in declared_symbols()
                    if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops",
                                 "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes", "lns_batch3d_bytes",
-                                "lns_server3d_bytes_in_use")]
+                                "lns_server3d_bytes_in_use", "lns_tri_workspace_bytes")]
     assert sorted(SIGNATURES) == solver_syms
 
 
