@@ -46,8 +46,12 @@ int launch_solve(const void* mat, void* rhs, const void* per, const void* per2, 
 // the GPU (several per SM sub-partition), else a CTA per line so that each
 // pivot's elimination and Schur update spread over more sub-partitions.
 // The periodic pivot touches about four times the elements of a boundary
-// one.  Results do not depend on the choice.
-inline int bc_team(int nsys) { return nsys <= 304 ? 128 : 32; }
+// one; FP64 lines fill the FP64 pipes sooner than FP32 ones.  Results do
+// not depend on the choice.
+template <typename T>
+inline int bc_team(int nsys) {
+  return nsys <= (sizeof(typename lns::real_of<T>::type) == 8 ? 304 : 640) ? 128 : 32;
+}
 inline int p_team(int nsys) { return nsys <= 160 ? 256 : nsys <= 640 ? 128 : 32; }
 
 template <typename T, int TEAM>
@@ -90,7 +94,7 @@ int launch_bc(void* mat, void* rhs, int n, int nsys, long long row_stride, long 
   if (nsys == 0) return LNS_OK;
   if (code != 1) {
     lns::PentaArgs a{mat, rhs, n, nsys, row_stride, line_stride, 0, status};
-    if (bc_team(nsys) == 128) launch_bc_team<T, 128>(a, st);
+    if (bc_team<T>(nsys) == 128) launch_bc_team<T, 128>(a, st);
     else launch_bc_team<T, 32>(a, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lns_cuda_fail(e, "penta_bc_kernel launch");
