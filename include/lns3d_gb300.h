@@ -306,6 +306,13 @@ typedef struct {
                                 (its totres is saved between calls,
                                 src/resstat3d.f90:18), so that it levels off
                                 near 1/(nx*ny).  The step itself is the same. */
+  int32_t impl;              /* time scheme (src/impdrv3d.f90:130-199): 1 (or 0)
+                                backward Euler with alfa; 2 two-step backward,
+                                backward Euler for the context's first step and
+                                rtb3D with alfa = 2/3 after it; 3 midpoint, the
+                                operator at (v + vold)/2 with alfa = 1/2.  Steps
+                                are counted from the context's creation (a fresh
+                                run, lstep = 0).  Batches and servers take 1. */
 } lns_params3d;
 
 typedef struct lns_ctx3d lns_ctx3d;

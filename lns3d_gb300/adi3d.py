@@ -41,12 +41,15 @@ class ImpDrv3D:
     plus cflmax, dtmax, loctime; metrics: dict of the ten (nx, ny) arrays;
     vm: (5, nx, ny) mean flow.  precision: FP64 (reference arithmetic) or
     MIXED (FP32 scaled LHS factors and sweeps, FP64 RHS, residual and
-    update).  res_compat: report the reference's running residual
+    update).  impl: time scheme, 1 backward Euler, 2 two-step backward
+    (backward Euler for the context's first step), 3 midpoint
+    (src/impdrv3d.f90:130-199).  res_compat: report the reference's running residual
     (src/resstat3d.f90:18 keeps totres between calls) instead of each
     corrector's own.
     """
 
-    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False):
+    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False,
+                 impl=1):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -54,7 +57,7 @@ class ImpDrv3D:
                        gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax,
                        dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
                        wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
-                       precision=precision, res_compat=1 if res_compat else 0)
+                       precision=precision, res_compat=1 if res_compat else 0, impl=impl)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")

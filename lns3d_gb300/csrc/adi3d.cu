@@ -370,12 +370,17 @@ __global__ void grad1_kernel(Grid g, const cd* __restrict__ v, cd* __restrict__ 
   grad1_body(g, v, c1v, blockIdx.x, blockIdx.y);
 }
 
-// r = vold - v - dtl L(v) (src/lrhs3d.f90:33-218, rbe3D), then the boundary
-// rows (src/rhsbc3d.f90), written as FP64 (r64) and/or FP32 (r32); the
-// block sums of |r|^2 / dtl^2 (src/resstat3d.f90:37-46) go to part[bx + nbx by].
+// r = vold - vs - dtl L(v) (src/lrhs3d.f90:33-218, rbe3D), or with v2old
+// the two-step backward r = 4/3 vold - 1/3 v2old - vs - 2/3 dtl L(v)
+// (rtb3D, src/impdrv3d.f90:471-501), then the boundary rows of the state vs
+// (src/rhsbc3d.f90), written as FP64 (r64) and/or FP32 (r32); the block sums
+// of |r|^2 / dtl^2 (src/resstat3d.f90:37-46) go to part[bx + nbx by].  v is
+// the field the operator is applied to: the state, or (v + vold)/2 for the
+// midpoint rule.
 template <bool NARROW>
 __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* __restrict__ v,
-                                         const cd* __restrict__ vold, const cd* __restrict__ c1v, cd* r64, cf* r32,
+                                         const cd* __restrict__ vs, const cd* __restrict__ vold,
+                                         const cd* __restrict__ v2old, const cd* __restrict__ c1v, cd* r64, cf* r32,
                                          double* part, int bx, int by, int nbx) {
   __shared__ double red[128];
   const int i = bx * blockDim.x + threadIdx.x + 1;
@@ -436,15 +441,26 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
     }
     // rbe3D
     const double dtl = o.dtl[p];
-    #pragma unroll
-    for (int m = 0; m < 5; ++m) {
-      const cd vo = vold[m + 5 * p], vm = v[m + 5 * p];
-      r[m] = cd{vo.x - vm.x - dtl * r[m].x, vo.y - vm.y - dtl * r[m].y};
+    if (v2old) {
+      const double onept33 = 1.3333333333333333333e+0, pt33 = 3.3333333333333333333e-1,
+                   pt66 = 6.6666666666666666666e-1;  // src/global.f90:13-18
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const cd vo = vold[m + 5 * p], v2 = v2old[m + 5 * p], vm = vs[m + 5 * p];
+        r[m] = cd{onept33 * vo.x - pt33 * v2.x - vm.x - pt66 * dtl * r[m].x,
+                  onept33 * vo.y - pt33 * v2.y - vm.y - pt66 * dtl * r[m].y};
+      }
+    } else {
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const cd vo = vold[m + 5 * p], vm = vs[m + 5 * p];
+        r[m] = cd{vo.x - vm.x - dtl * r[m].x, vo.y - vm.y - dtl * r[m].y};
+      }
     }
     // boundary rows, src/rhsbc3d.f90:34-170
     if (!g.yper) {
       if (g.navier && j == 1) {
-        auto W = [&](int k, int jj) -> const cd& { return v[k + 5 * pix(g, i, jj)]; };
+        auto W = [&](int k, int jj) -> const cd& { return vs[k + 5 * pix(g, i, jj)]; };
         for (int m = 1; m <= 3; ++m) r[m] = cd{-(W(m, 1).x - 0.0), -(W(m, 1).y - 0.0)};
         if (g.wall == 1)
           r[0] = cd{gc1 * W(0, 1).x + gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x,
@@ -484,9 +500,10 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
 }
 template <bool NARROW>
 __global__ void __launch_bounds__(128, 4) rhs_kernel(Grid g, Ops o, const cd* __restrict__ v,
-                                                  const cd* __restrict__ vold, const cd* __restrict__ c1v,
+                                                  const cd* __restrict__ vs, const cd* __restrict__ vold,
+                                                  const cd* __restrict__ v2old, const cd* __restrict__ c1v,
                                                   cd* r64, cf* r32, double* part) {
-  rhs_body<NARROW>(g, o, v, vold, c1v, r64, r32, part, blockIdx.x, blockIdx.y, gridDim.x);
+  rhs_body<NARROW>(g, o, v, vs, vold, v2old, c1v, r64, r32, part, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 // ----------------------------------------------------------------- update
@@ -575,8 +592,8 @@ __global__ void __launch_bounds__(128, 4) rhs_batch_kernel(const StepArgs* __res
   const int4 w = table[blockIdx.x];
   if (!active[w.x]) return;
   const StepArgs& a = list[w.x];
-  rhs_body<NARROW>(a.g, a.o, a.v, a.vold, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr, a.part, w.y, w.z,
-                   a.nbx);
+  rhs_body<NARROW>(a.g, a.o, a.v, a.v, a.vold, nullptr, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr,
+                   a.part, w.y, w.z, a.nbx);
 }
 // residual of each problem into hist[step * P + p] (src/resstat3d.f90:37-60)
 // A problem whose residual reaches its tolerance is switched off here, so
@@ -654,6 +671,11 @@ struct lns_ctx3d {
   int res_cap = 0;
   int* status = nullptr;
   bool have_metrics = false, have_mean = false, factored = false;
+  // time scheme (src/impdrv3d.f90:130-199): the previous-previous state
+  // (impl 2), the averaged field (impl 3), steps taken, alfa of the factors
+  cd *v2old = nullptr, *wavg = nullptr;
+  long long lstep = 0;
+  double alfa_fac = -1.0;
   // phase timing (lns_ctx3d_profile): per corrector, events around the RHS,
   // the scaling, recurrences, tail and fill kernels of both sweeps, and the
   // update (LNS_PROFILE_SEGMENTS segments)
@@ -756,14 +778,17 @@ int res_reserve(lns_ctx3d* c, int n) {
 }
 
 // r = RHS of one corrector into r64 (FP64) and / or r32 (FP32); totres to *res.
-int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vold, cd* r64, cf* r32, double* res, double* acc,
-               cudaStream_t st) {
+// The operator acts on the field v; vs is the state (rbe3D / rtb3D and the
+// boundary rows); v2old selects rtb3D.
+int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vs, const cd* vold, const cd* v2old, cd* r64, cf* r32,
+               double* res, double* acc, cudaStream_t st) {
   const Grid& g = c->g;
   lns::a3::grad1_kernel<<<pt_grid(g), 128, 0, st>>>(g, v, c->c1v);
   if (lns::a3::narrow_stencils(g))
-    lns::a3::rhs_kernel<true><<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vold, c->c1v, r64, r32, c->part);
+    lns::a3::rhs_kernel<true><<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vs, vold, v2old, c->c1v, r64, r32, c->part);
   else
-    lns::a3::rhs_kernel<false><<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vold, c->c1v, r64, r32, c->part);
+    lns::a3::rhs_kernel<false><<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vs, vold, v2old, c->c1v, r64, r32,
+                                                           c->part);
   const int nrhs = (int)(pt_grid(g).x * pt_grid(g).y);  // rhs_kernel block partials
   lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res, acc);
   cudaError_t e = cudaGetLastError();
@@ -876,26 +901,49 @@ int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
 }
 
 // nsteps steps of niter correctors on device v (src/impdrv3d.f90:130-356)
+__global__ void avg_kernel(long long n, const cd* __restrict__ a, const cd* __restrict__ b, cd* __restrict__ w) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k < n) w[k] = cd{0.5 * (a[k].x + b[k].x), 0.5 * (a[k].y + b[k].y)};
+}
+
+// nsteps steps of the time scheme impl (src/impdrv3d.f90:130-356): 1
+// backward Euler with the deck's alfa; 2 two-step backward, backward Euler
+// for the first step of the context and rtb3D with alfa = 2/3 after it
+// (the LHS formed and factored again once); 3 the midpoint rule, the
+// operator applied to (v + vold)/2 with alfa = 1/2.
 int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cudaStream_t st) {
-  const Grid& g = c->g;
   const bool mixed = c->prm.precision == LNS_MIXED;
+  const int impl = c->prm.impl == 0 ? 1 : c->prm.impl;
   int rc;
-  if (!c->factored) {
-    rc = mixed ? factor_all<cf>(c, st) : factor_all<cd>(c, st);
-    if (rc) return rc;
-  }
   const size_t vbytes = sizeof(cd) * 5 * (size_t)c->np;
   double* acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
   for (int s = 0; s < nsteps; ++s) {
-    cudaError_t e = cudaMemcpyAsync(c->vold, v, vbytes, cudaMemcpyDeviceToDevice, st);
+    const bool rtb = impl == 2 && c->lstep > 0;
+    const double alfa = impl == 3 ? 0.5 : rtb ? 6.6666666666666666666e-1 : (impl == 2 ? 1.0 : c->prm.alfa);
+    if (!c->factored || c->alfa_fac != alfa) {
+      c->g.alfa = alfa;
+      rc = mixed ? factor_all<cf>(c, st) : factor_all<cd>(c, st);
+      if (rc) return rc;
+      c->alfa_fac = alfa;
+    }
+    cudaError_t e = cudaSuccess;
+    if (rtb) e = cudaMemcpyAsync(c->v2old, c->vold, vbytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->vold, v, vbytes, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return cuda3(e, "cudaMemcpyAsync vold");
     rc = launch_update<cd>(c, v, (const cd*)nullptr, 0, st);
     if (rc) return rc;
     for (int it = 0; it < niter; ++it) {
       double* res = (it == niter - 1 && totres_dev) ? totres_dev + s : c->dscal + 1;
       rc = mark(c, st);
+      const cd* field = v;
+      if (impl == 3) {
+        const long long n = 5 * c->np;
+        avg_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, c->vold, c->wavg);
+        field = c->wavg;
+      }
+      const cd* v2 = rtb ? c->v2old : nullptr;
       if (mixed) {
-        if (!rc) rc = launch_rhs(c, v, c->vold, nullptr, c->r32, res, acc, st);
+        if (!rc) rc = launch_rhs(c, field, v, c->vold, v2, nullptr, c->r32, res, acc, st);
         if (!rc) rc = mark(c, st);
         if (!rc) rc = sweep_x<cf>(c, c->r32, st);
         if (!rc) rc = mark(c, st);
@@ -903,7 +951,7 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
         if (!rc) rc = mark(c, st);
         if (!rc) rc = launch_update<cf>(c, v, c->r32, 1, st);
       } else {
-        if (!rc) rc = launch_rhs(c, v, c->vold, c->r64, nullptr, res, acc, st);
+        if (!rc) rc = launch_rhs(c, field, v, c->vold, v2, c->r64, nullptr, res, acc, st);
         if (!rc) rc = mark(c, st);
         if (!rc) rc = sweep_x<cd>(c, c->r64, st);
         if (!rc) rc = mark(c, st);
@@ -914,6 +962,7 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
       if (!rc) rc = mark(c, st);
       if (rc) return rc;
     }
+    c->lstep += 1;
   }
   return LNS_OK;
 }
@@ -938,6 +987,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->res_compat != 0 && p->res_compat != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: res_compat must be 0 or 1");
   if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
     return fail3(LNS_ERR_ARG, "ctx3d_create: precision must be LNS_FP64 or LNS_MIXED");
+  if (p->impl < 0 || p->impl > 3) return fail3(LNS_ERR_ARG, "ctx3d_create: impl must be 1, 2 or 3 (0 means 1)");
   lns_ctx3d* c = new lns_ctx3d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);
@@ -972,6 +1022,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   A(sizeof(cd) * 5 * np, &q); c->v = (cd*)q;
   A(sizeof(cd) * 5 * np, &q); c->vold = (cd*)q;
   A(sizeof(cd) * 5 * np, &q); c->c1v = (cd*)q;
+  if (p->impl == 2) { A(sizeof(cd) * 5 * np, &q); c->v2old = (cd*)q; }
+  if (p->impl == 3) { A(sizeof(cd) * 5 * np, &q); c->wavg = (cd*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
   A(sizeof(cd) * 125 * np, &c->matx);
@@ -1093,7 +1145,8 @@ int lns_rhs3d_dev(lns_ctx3d* c, const double* v, const double* vold, double* r, 
   if (!c->have_mean) return fail3(LNS_ERR_ARG, "rhs3d: upload the metrics and the mean flow first");
   int rc = check_device(c);
   if (rc) return rc;
-  return launch_rhs(c, (const cd*)v, (const cd*)vold, (cd*)r, nullptr, totres_dev ? totres_dev : c->dscal + 1,
+  return launch_rhs(c, (const cd*)v, (const cd*)v, (const cd*)vold, nullptr, (cd*)r, nullptr,
+                    totres_dev ? totres_dev : c->dscal + 1,
                     nullptr, (cudaStream_t)stream);
 }
 
@@ -1423,6 +1476,8 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
   for (int p = 1; p < nprob; ++p)
     if (params[p].precision != params[0].precision)
       return fail3(LNS_ERR_ARG, "batch3d_create: every problem must use the same precision");
+  for (int p = 0; p < nprob; ++p)
+    if (params[p].impl > 1) return fail3(LNS_ERR_ARG, "batch3d_create: batches run impl = 1 (backward Euler)");
   lns_batch3d* b = new lns_batch3d();
   b->P = nprob;
   b->mixed = params[0].precision == LNS_MIXED;
@@ -1790,6 +1845,7 @@ int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* 
                         const double* v, double tol, int32_t max_steps, int64_t* id) {
   if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
   if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
+  if (prm->impl > 1) return fail3(LNS_ERR_ARG, "server3d_submit: servers run impl = 1 (backward Euler)");
   if (!(tol > 0.0) || max_steps < 1) return fail3(LNS_ERR_ARG, "server3d_submit: need tol > 0 and max_steps >= 1");
   if (ctx_bytes_for(*prm) > s->budget) return fail3(LNS_ERR_ARG, "server3d_submit: request larger than the budget");
   SrvReq* r = new SrvReq();

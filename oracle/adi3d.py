@@ -42,6 +42,9 @@ def _lib(L=None):
         L.a3_step.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, P, P, P, P, P, P, P,
                               ctypes.POINTER(I)]
         L.a3_step.restype = D
+        L.a3_step_impl.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, I, I, P, P, P, P, P, P, P, P,
+                                   P, ctypes.POINTER(D)]
+        L.a3_step_impl.restype = D
         L._a3_setup = True
     return L
 
@@ -83,6 +86,22 @@ class Oracle3D:
         self.per2x = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
         self.r = np.zeros((5, nx, ny), np.complex128, order="F")
         self.factored = I(0)
+
+    def step_impl(self, v, impl, niter=1):
+        """One step of time scheme impl (1, 2, 3) on v in place; vold,
+        v2old and the step count carry over between calls (src/impdrv3d.f90)"""
+        if not hasattr(self, "_lstep"):
+            self._lstep = 0
+            self._vold = np.zeros_like(v)
+            self._v2old = np.zeros_like(v)
+            self._w = np.zeros_like(v)
+            self._alfa_fac = D(-1.0)
+        res = self.L.a3_step_impl(ctypes.byref(self.g), ctypes.byref(self.o), ptr(self.dtl), niter, impl,
+                                  self._lstep, ptr(v), ptr(self._vold), ptr(self._v2old), ptr(self._w), ptr(self.r),
+                                  ptr(self.matx), ptr(self.maty), ptr(self.perx), ptr(self.per2x),
+                                  ctypes.byref(self._alfa_fac))
+        self._lstep += 1
+        return res
 
     def step(self, v, niter=1):
         vold = np.zeros_like(v)

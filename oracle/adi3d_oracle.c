@@ -752,6 +752,19 @@ int a3_lhs(const A3Grid* g, const A3Ops* o, const double* dtl, int dir, double* 
   return 0;
 }
 
+/* rtb3D, src/impdrv3d.f90:471-501: r = 4/3 vold - 1/3 v2old - v - 2/3 dtl r */
+void a3_rtb(const A3Grid* g, double* r, const double* v, const double* vold, const double* v2old, const double* dtl) {
+  const double onept33 = 1.3333333333333333333e+0, pt33 = 3.3333333333333333333e-1,
+               pt66 = 6.6666666666666666666e-1;  /* src/global.f90:13-18 */
+  OMP_FOR
+  for (int j = 1; j <= g->ny; ++j)
+    for (int i = 1; i <= g->nx; ++i)
+      for (int k = 0; k < 10; ++k) {
+        const long e = k + 10 * IX(g, i, j);
+        r[e] = onept33 * vold[e] - pt33 * v2old[e] - v[e] - pt66 * dtl[IX(g, i, j)] * r[e];
+      }
+}
+
 /* -------------------------------------------------------------------- step */
 
 /* src/impdrv3d.f90:130-356 with impl = 1, iLHS = 1, USE_CPENTA1BC semantics
@@ -777,6 +790,57 @@ double a3_step(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, do
       *factored = 1;
     }
     if (g->xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 1, ORC_COMPAT_PERIODIC_SLOT);
+    else orc_cpenta_bc(2, nx, ny, matx, r, 1, 0);
+    orc_cpenta_bc(1, ny, nx, maty, r, 1, 0);
+    OMP_FOR
+    for (long e = 0; e < n10; ++e) v[e] = v[e] + r[e];
+    a3_itrbc(g, v);
+  }
+  return totres;
+}
+
+/* One step of the time schemes of src/impdrv3d.f90:130-356 (iLHS = 1):
+   impl 1 backward Euler (alfa = g->alfa); impl 2 two-step backward, which is
+   backward Euler while lstep = 0 and then rtb3D with alfa = 2/3, the LHS
+   factored again at the first step with lstep = 1 (:134-143,179-193,228-231);
+   impl 3 midpoint, the RHS operator at (v + vold)/2 with rbe3D and alfa =
+   1/2 (:195-199).  vold and v2old carry over between steps; w is scratch;
+   *alfa_fac is the alfa of the current factors (any value outside
+   {1, 2/3, 1/2, g->alfa} before the first step). */
+double a3_step_impl(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, int impl, int lstep, double* v,
+                    double* vold, double* v2old, double* w, double* r, double* matx, double* maty, double* perx,
+                    double* per2x, double* alfa_fac) {
+  const int nx = g->nx, ny = g->ny;
+  const long n10 = 10L * nx * ny;
+  const double pt66 = 6.6666666666666666666e-1, pt5 = 0.5;
+  A3Grid gl = *g;
+  double totres = 0.0;
+  if (impl == 2 && lstep > 0) memcpy(v2old, vold, n10 * sizeof(double));
+  memcpy(vold, v, n10 * sizeof(double));
+  a3_itrbc(g, v);
+  for (int iter = 1; iter <= niter; ++iter) {
+    const int rtb = impl == 2 && lstep > 0;
+    gl.alfa = impl == 3 ? pt5 : rtb ? pt66 : (impl == 2 ? 1.0 : g->alfa);
+    if (impl == 3) {
+      OMP_FOR
+      for (long e = 0; e < n10; ++e) w[e] = pt5 * (v[e] + vold[e]);
+      a3_lrhs(&gl, o, w, r);
+    } else {
+      a3_lrhs(&gl, o, v, r);
+    }
+    if (rtb) a3_rtb(&gl, r, v, vold, v2old, dtl);
+    else a3_rbe(&gl, r, v, vold, dtl);
+    a3_rhsbc(&gl, r, v);
+    totres = a3_resstat(&gl, r, dtl);
+    if (*alfa_fac != gl.alfa) {
+      a3_lhs(&gl, o, dtl, 1, matx);
+      if (gl.xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 0, ORC_COMPAT_PERIODIC_SLOT);
+      else orc_cpenta_bc(2, nx, ny, matx, r, 0, 0);
+      a3_lhs(&gl, o, dtl, 2, maty);
+      orc_cpenta_bc(1, ny, nx, maty, r, 0, 0);
+      *alfa_fac = gl.alfa;
+    }
+    if (gl.xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 1, ORC_COMPAT_PERIODIC_SLOT);
     else orc_cpenta_bc(2, nx, ny, matx, r, 1, 0);
     orc_cpenta_bc(1, ny, nx, maty, r, 1, 0);
     OMP_FOR

@@ -258,3 +258,47 @@ def test_reference_residual_history_mode(cuda):
     assert np.array_equal(v_a, v_b)
     # the reported value levels off near 1 / (nx ny)
     assert abs(res_ref[-1] - 1.0 / (40 * 33)) < 0.05 / (40 * 33)
+
+
+@pytest.mark.parametrize("impl,niter", [(2, 1), (3, 1), (2, 2)])
+def test_time_schemes_match_oracle(cuda, impl, niter):
+    """impl 2 (two-step backward: backward Euler, then rtb3D with the LHS
+    refactored at alfa = 2/3) and impl 3 (midpoint), src/impdrv3d.f90:130-199,
+    against the oracle step by step; the device form splits the same steps
+    over two calls."""
+    import torch
+
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=40, ny=33, seed=9)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1)
+    drv = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, impl=impl)
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    for s in range(4):
+        res_ref = orc.step_impl(v_ref, impl, niter=niter)
+        res_gpu = drv.step(v_gpu, nsteps=1, niter=niter)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+    dev = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, impl=impl)
+    dv = torch.from_numpy(case["v"].ravel(order="F")).cuda()
+    dev.step(dv, nsteps=1, niter=niter)
+    dev.step(dv, nsteps=3, niter=niter)
+    torch.cuda.synchronize()
+    assert rel(dv.cpu().numpy().reshape(v_ref.shape, order="F"), v_ref) < STEP_TOL
+
+
+def test_time_schemes_differ_and_reject_bad_impl(cuda, small):
+    from lns3d_gb300 import ImpDrv3D, LnsError
+
+    case, _ = small
+    out = {}
+    for impl in (1, 2, 3):
+        d = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, impl=impl)
+        v = case["v"].copy(order="F")
+        d.step(v, nsteps=3)
+        out[impl] = v
+    assert rel(out[1], out[2]) > 1e-8 and rel(out[1], out[3]) > 1e-8
+    with pytest.raises(LnsError):
+        ImpDrv3D(case["params"], case["metrics"], case["vm"], impl=4)

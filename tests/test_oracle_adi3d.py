@@ -114,3 +114,25 @@ def test_zero_disturbance_is_a_fixed_point():
     v = np.zeros_like(case["v"], order="F")
     res = o.step(v, niter=2)
     assert res == 0.0 and not v.any()
+
+
+def test_time_scheme_steps_are_consistent():
+    """The oracle's scheme step: impl 1 equals the backward Euler step bit for
+    bit; impl 2's first step (lstep = 0) is backward Euler; the midpoint step
+    keeps the zero state at zero (src/impdrv3d.f90:130-199)."""
+    import numpy as np
+
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=24, ny=20, seed=4)
+    a, b, c = (Oracle3D(case, cflmax=20.0, loctime=1) for _ in range(3))
+    va, vb, vc = (case["v"].copy(order="F") for _ in range(3))
+    ra = a.step(va)
+    rb = b.step_impl(vb, 1)
+    rc = c.step_impl(vc, 2)
+    assert np.array_equal(va, vb) and ra == rb
+    assert np.array_equal(va, vc) and ra == rc
+    z = Oracle3D(case, cflmax=20.0, loctime=1)
+    v0 = np.zeros_like(case["v"], order="F")
+    z.step_impl(v0, 3)
+    assert np.abs(v0).max() == 0.0
