@@ -30,6 +30,9 @@ def _lib(L=None):
         L.a2_lhs.argtypes = [G, ctypes.POINTER(A3Ops), P, P, I, P]
         L.a2_step.argtypes = [G, I, P, P, P, ctypes.POINTER(A3Ops), P, P, P, P]
         L.a2_step.restype = D
+        L.a2_lhs2.argtypes = [G, ctypes.POINTER(A3Ops), P, P, I, P, P]
+        L.a2_step2.argtypes = [G, I, P, P, P, ctypes.POINTER(A3Ops), P, P, P, P]
+        L.a2_step2.restype = D
         L._a2_setup = True
     return L
 
@@ -41,8 +44,11 @@ def ptr(a):
 class Oracle2D:
     """Grid struct, operator storage and scratch of the oracle for one case."""
 
-    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False):
+    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False, ilhs=1):
+        """ilhs = 1: fourth-order LHS, pentadiagonal solves; ilhs = 0:
+        second-order LHS, block-tridiagonal solves (src/impdrv.f90:307-344)."""
         self.L = _lib(lib)
+        self.ilhs = ilhs
         p = case["params"]
         self.nx, self.ny = nx, ny = p["nx"], p["ny"]
         self.keep = {k: np.asfortranarray(v, dtype=np.float64) for k, v in case["metrics"].items()}
@@ -67,12 +73,18 @@ class Oracle2D:
         self.vold = np.zeros((5, nx, ny), order="F")
         self.mat = np.zeros((5, 5, 5, nx, ny), order="F")
         self.per = np.zeros((2, 5, 5, nx, ny), order="F")
+        self.mat3 = np.zeros((3, 5, 5, nx, ny), order="F")
+        self.bc = np.zeros((14, 5, 5, nx), order="F")
         self.cfl = ctypes.c_double(0.0)
 
     def itrbc(self, v):
         self.L.a2_itrbc(ctypes.byref(self.g), ptr(v))
 
     def step(self, v, niter=1):
+        if self.ilhs == 0:
+            return self.L.a2_step2(ctypes.byref(self.g), niter, ptr(v), ptr(self.vold), ptr(self.r),
+                                   ctypes.byref(self.o), ptr(self.dtl), ptr(self.mat3), ptr(self.bc),
+                                   ctypes.byref(self.cfl))
         return self.L.a2_step(ctypes.byref(self.g), niter, ptr(v), ptr(self.vold), ptr(self.r), ctypes.byref(self.o),
                               ptr(self.dtl), ptr(self.mat), ptr(self.per), ctypes.byref(self.cfl))
 
@@ -93,3 +105,11 @@ class Oracle2D:
         mat = np.zeros((5, 5, 5, self.nx, self.ny), order="F")
         assert self.L.a2_lhs(ctypes.byref(self.g), ctypes.byref(self.o), ptr(dtl), ptr(v), direction, ptr(mat)) == 0
         return mat
+
+    def lhs2(self, v, dtl, direction):
+        """Second-order LHS of a sweep: (mat(3,5,5,nx,ny), bc(14,5,5,nlines))."""
+        mat = np.zeros((3, 5, 5, self.nx, self.ny), order="F")
+        bc = np.zeros((14, 5, 5, self.ny if direction == 1 else self.nx), order="F")
+        assert self.L.a2_lhs2(ctypes.byref(self.g), ctypes.byref(self.o), ptr(dtl), ptr(v), direction, ptr(mat),
+                              ptr(bc)) == 0
+        return mat, bc

@@ -428,10 +428,14 @@ double a2_resstat(const A2Grid* a2, const double* res, const double* dtl) {
 
 #define MT(k, a, b, p) mat[(long)(k - 1) + 5 * (a - 1) + 25 * (b - 1) + 125 * (p)]
 
-/* ReimannLHS, src/reimann.f90:238-401: slots 3, 2, 1 (columns ny, ny-1,
-   ny-2) of row ny */
-static void rm_lhs(const A2Grid* a2, int i, const double* vb, const double* vb1, const double* vb2, double* mat,
-                   long p) {
+/* A 5x5 block in some storage: entry (a, b) at p[(a-1) sa + (b-1) sb]. */
+typedef struct { double* p; long sa, sb; } Blk;
+#define RB(k, a, b) (rb[(k) - 1].p[(long)((a) - 1) * rb[(k) - 1].sa + (long)((b) - 1) * rb[(k) - 1].sb])
+
+/* ReimannLHS, src/reimann.f90:238-401: the blocks of row ny at columns
+   ny-2, ny-1, ny (rb[0], rb[1], rb[2]); entries not set are left as they are */
+static void rm_lhs_blk(const A2Grid* a2, int i, const double* vb, const double* vb1, const double* vb2,
+                       const Blk rb[3]) {
   const A3Grid* g = G(a2);
   const int nx = g->nx;
   const double bn1 = a2->bnt[i - 1], bn2 = a2->bnt[nx + i - 1];
@@ -442,27 +446,27 @@ static void rm_lhs(const A2Grid* a2, int i, const double* vb, const double* vb1,
   const double bb = bn1 * bn1 + bn2 * bn2;
   double fact, fact1, fact2;
   /* m2 = 2 F (slot 2), m3 = -F (slot 1) for the row's coefficients F */
-#define PUT(a, b, F) (MT(2, a, b, p) = two * (F), MT(1, a, b, p) = -(F))
+#define PUT(a, b, F) (RB(2, a, b) = two * (F), RB(1, a, b) = -(F))
   if (s.inflow) {
     fact = pow(pow(s.rho, gamma) / (gamma * s.p) * (gq * gq), one / gamma1) * two / gamma1 *
            pow(dR, (two - gamma1) / gamma1);
-    MT(3, 1, 1, p) = -one;
+    RB(3, 1, 1) = -one;
     PUT(1, 2, fact * bn1);
     PUT(1, 3, fact * bn2);
     PUT(1, 5, fact / (gamma1 * Ma * sq));
     fact = pt5 * bn1 / bb;
-    MT(3, 2, 2, p) = -one;
+    RB(3, 2, 2) = -one;
     PUT(2, 2, fact * bn1);
     PUT(2, 3, fact * bn2);
     PUT(2, 5, fact / (gamma1 * Ma * sq));
     fact = pt5 * bn2 / bb;
-    MT(3, 3, 3, p) = -one;
+    RB(3, 3, 3) = -one;
     PUT(3, 2, fact * bn1);
     PUT(3, 3, fact * bn2);
     PUT(3, 5, fact / (gamma1 * Ma * sq));
-    MT(3, 4, 4, p) = -one;
+    RB(3, 4, 4) = -one;
     fact = (Ma * gamma1 / four) * (Ma * gamma1 / four) * two * dR;
-    MT(3, 5, 5, p) = -one;
+    RB(3, 5, 5) = -one;
     PUT(5, 2, fact * bn1);
     PUT(5, 3, fact * bn2);
     PUT(5, 5, fact / (gamma1 * Ma * sq));
@@ -471,32 +475,40 @@ static void rm_lhs(const A2Grid* a2, int i, const double* vb, const double* vb1,
     fact1 = pow(rg, one / gamma1) * pow(gq, two / gamma1) * (two / gamma1) * pow(dR, (two - gamma1) / gamma1);
     fact2 = pow(gq * dR, two / gamma1) * one / (gamma * gamma1) * pow(rg, (two - gamma) / gamma1);
     const double fr = fact2 * pow(s.rho, gamma + 1) / (gamma * (Ma * Ma) * (s.p * s.p));
-    MT(3, 1, 1, p) = -one;
+    RB(3, 1, 1) = -one;
     PUT(1, 2, fact1 * bn1 + gamma1 * pow(s.rho, gamma1) / s.p);
     PUT(1, 3, fact1 * bn2);
     PUT(1, 5, fact1 / (gamma1 * Ma * sq) - fr);
     fact1 = pt5 * bn1 / bb;
     fact2 = bn2 / bb;
-    MT(3, 2, 2, p) = -one;
+    RB(3, 2, 2) = -one;
     PUT(2, 2, fact1 * bn1 + fact2 * bn2);
     PUT(2, 3, fact1 * bn2 - fact2 * bn1);
     PUT(2, 5, fact1 / (gamma1 * Ma * sq));
     fact1 = pt5 * bn2 / bb;
     fact2 = bn1 / bb;
-    MT(3, 3, 3, p) = -one;
+    RB(3, 3, 3) = -one;
     PUT(3, 2, fact1 * bn1 - fact2 * bn2);
     PUT(3, 3, fact1 * bn2 + fact2 * bn1);
     PUT(3, 5, fact1 / (gamma1 * Ma * sq));
-    MT(3, 4, 4, p) = -one;
-    MT(2, 4, 4, p) = two;
-    MT(1, 4, 4, p) = -one;
+    RB(3, 4, 4) = -one;
+    RB(2, 4, 4) = two;
+    RB(1, 4, 4) = -one;
     fact = (Ma * gamma1 / four) * (Ma * gamma1 / four) * two * dR;
-    MT(3, 5, 5, p) = -one;
+    RB(3, 5, 5) = -one;
     PUT(5, 2, fact * bn1);
     PUT(5, 3, fact * bn2);
     PUT(5, 5, fact / (gamma1 * Ma * sq));
   }
 #undef PUT
+}
+
+/* the same into slots 3, 2, 1 (columns ny, ny-1, ny-2) of row ny's
+   pentadiagonal record */
+static void rm_lhs(const A2Grid* a2, int i, const double* vb, const double* vb1, const double* vb2, double* mat,
+                   long p) {
+  const Blk rb[3] = {{&MT(1, 1, 1, p), 5, 25}, {&MT(2, 1, 1, p), 5, 25}, {&MT(3, 1, 1, p), 5, 25}};
+  rm_lhs_blk(a2, i, vb, vb1, vb2, rb);
 }
 
 /* lhs1f / lhs2f (src/lhsf.f90:7-162, 164-329), the eta boundary rows
@@ -660,6 +672,258 @@ double a2_step(const A2Grid* a2, int niter, double* v, double* vold, double* r, 
     orc_penta_p(2, nx, ny, mat, r, per, ORC_COMPAT_PERIODIC_SLOT);
     a2_lhs(a2, ops, dtl, v, 2, mat);
     orc_penta_bc(1, ny, nx, mat, r);
+    OMP_FOR
+    for (long e = 0; e < n5; ++e) v[e] = v[e] + r[e];
+    a2_itrbc(a2, v);
+  }
+  return totres;
+}
+
+/* ----------------------------------------------- second-order LHS (iLHS = 0) */
+
+/* Block of row t (1..n) at column c of line iv in the block-tridiagonal
+   storage: mat(3,5,5,...) slot c-t+2 or one of the boundary blocks
+   bc(14,5,5,nlines), in the block table of src/nsolve2bc.f90:40-420 (the
+   same table as oracle/tri_oracle.c). */
+static Blk tri_blk(double* mat3, double* bc, long rec, int iv, int t, int c, int n) {
+  static const int tab[6][5] = {{2, 3, -1, -2, -3}, {1, 2, 3, -4, -5}, {-7, 1, 2, 3, -6},
+                                {-8, 1, 2, 3, -9}, {-10, -11, 1, 2, 3}, {-12, -13, -14, 1, 2}};
+  int src = 0;
+  if (t <= 3) src = tab[t - 1][c - 1];
+  else if (t >= n - 2) src = tab[t - (n - 2) + 3][c - (n - 4)];
+  else src = c - t + 2;
+  Blk b;
+  if (src > 0) b.p = mat3 + (src - 1) + 75 * rec, b.sa = 3, b.sb = 15;
+  else b.p = bc + (-src - 1) + 350L * iv, b.sa = 14, b.sb = 70;
+  return b;
+}
+#define EB(B, a, b) ((B).p[(long)((a) - 1) * (B).sa + (long)((b) - 1) * (B).sb])
+
+/* The second-order LHS of the xi (dir 1: lhs1, src/lhs.f90:7-137, with the
+   nonlinear lhsbc1 rows, src/lhsbc1.f90) or eta direction (dir 2: lhs2,
+   src/lhs.f90:140-277, lhsbt2, src/lhsbt2.f90, and the nonlinear lhsbc2
+   rows, src/lhsbc2.f90) in the reference's block-tridiagonal storage:
+   dir 1 mat3(3,5,5,nx,ny) (lines over j; a periodic xi leaves bc zero,
+   src/lhsbt1.f90), dir 2 mat3(3,5,5,nx,ny) with bc(14,5,5,nx) (lines over
+   i).  Expression order follows the reference (Fortran left to right). */
+int a2_lhs2(const A2Grid* a2, const A3Ops* o, const double* dtl, const double* vl, int dir, double* mat3,
+            double* bc) {
+  const A3Grid* g = G(a2);
+  const int nx = g->nx, ny = g->ny;
+  const double alfa = g->alfa;
+  if ((dir == 1 && !g->xper) || g->yper || ny < 8) return 1;
+  const double h = dir == 1 ? g->dxi : g->deta;
+  const double a1 = -alfa * pt5 / h, a2c = alfa * zero, a3 = alfa * pt5 / h;
+  const double b1 = alfa / (h * h), b2 = -alfa * two / (h * h), b3 = alfa / (h * h);
+  const double ak[3] = {a1, a2c, a3}, bk[3] = {b1, b2, b3};
+  memset(bc, 0, sizeof(double) * 350 * (size_t)(dir == 1 ? ny : nx));
+  /* band, src/lhs.f90:44-104 (lhs1) and :180-240 (lhs2) */
+  OMP_FOR
+  for (int j = 1; j <= ny; ++j)
+    for (int i = 1; i <= nx; ++i) {
+      const long p = IX(g, i, j);
+      const double d = dtl[p];
+      const double* X = (dir == 1 ? o->Ah : o->Bh) + 25 * p;
+      const double* V = (dir == 1 ? o->Vh11 : o->Vh22) + 6 * p;
+      double* m = mat3 + 75 * p;
+#define M3(k, a, b) m[(k - 1) + 3 * (a - 1) + 15 * (b - 1)]
+      for (int a = 1; a <= 5; ++a)
+        for (int b = 1; b <= 5; ++b)
+          for (int k = 1; k <= 3; ++k) M3(k, a, b) = ak[k - 1] * d * X[(a - 1) + 5 * (b - 1)];
+      if (dir == 1)
+        for (int a = 1; a <= 5; ++a)
+          for (int b = 1; b <= 5; ++b) M3(2, a, b) = M3(2, a, b) + alfa * d * o->Dh[(a - 1) + 5 * (b - 1) + 25 * p];
+      for (int k = 1; k <= 3; ++k) {
+        M3(k, 2, 2) = M3(k, 2, 2) - bk[k - 1] * d * V[0];
+        M3(k, 2, 3) = M3(k, 2, 3) - bk[k - 1] * d * V[4];
+        M3(k, 3, 2) = M3(k, 3, 2) - bk[k - 1] * d * V[5];
+        M3(k, 3, 3) = M3(k, 3, 3) - bk[k - 1] * d * V[1];
+        M3(k, 4, 4) = M3(k, 4, 4) - bk[k - 1] * d * V[2];
+        M3(k, 5, 5) = M3(k, 5, 5) - bk[k - 1] * d * V[3];
+      }
+      for (int a = 1; a <= 5; ++a) M3(2, a, a) = M3(2, a, a) + one;
+#undef M3
+    }
+  if (dir == 2) {
+    /* boundary rows, src/lhsbt2.f90:28-520: row j, the stencil over columns
+       c0..c0+4, first (g) and second (d) derivative coefficients, sign */
+    const double detainv = one / g->deta, detasinv = one / (g->deta * g->deta);
+    const double gcs[5] = {gc1, gc2, gc3, gc4, gc5}, gbs[5] = {gb1, gb2, gb3, gb4, gb5};
+    const double gas[5] = {ga1, ga2, zero, ga3, ga4};
+    const double dds[5] = {dd1, dd2, dd3, dd4, dd5}, dbs[5] = {db1, db2, db3, db4, db5};
+    const double das[5] = {da1, da2, da3, da4, da5};
+    for (int i = 1; i <= nx; ++i)
+      for (int r = 0; r < 6; ++r) {
+        const int j = r < 3 ? r + 1 : ny - 5 + r;
+        const int c0 = r < 3 ? 1 : ny - 4;
+        /* coefficient of column c0 + t */
+        double gk[5], dk[5];
+        double sg = one;
+        for (int t = 0; t < 5; ++t) {
+          if (r == 0) gk[t] = gcs[t], dk[t] = dds[t];
+          else if (r == 1) gk[t] = gbs[t], dk[t] = dbs[t];
+          else if (r == 2 || r == 3) gk[t] = gas[t], dk[t] = das[t];
+          else if (r == 4) gk[t] = gbs[4 - t], dk[t] = dbs[4 - t], sg = -one;
+          else gk[t] = gcs[4 - t], dk[t] = dds[4 - t], sg = -one;
+        }
+        const long p = IX(g, i, j);
+        const double d = dtl[p];
+        const double* X = o->Bh + 25 * p;
+        const double* V = o->Vh22 + 6 * p;
+        const long rec = (long)(i - 1) + (long)nx * (j - 1);
+        for (int t = 0; t < 5; ++t) {
+          const int c = c0 + t;
+          const Blk B = tri_blk(mat3, bc, rec, i - 1, j, c, ny);
+          for (int a = 1; a <= 5; ++a)
+            for (int b = 1; b <= 5; ++b) {
+              /* the central rows 3 and ny-2 set their diagonal block to a
+                 literal zero before the viscous terms */
+              const double v = alfa * d * gk[t] * detainv * X[(a - 1) + 5 * (b - 1)];
+              EB(B, a, b) = (r == 2 || r == 3) && t == 2 ? zero : sg < zero ? -v : v;
+            }
+          const double w = alfa * d * dk[t] * detasinv;
+          EB(B, 2, 2) = EB(B, 2, 2) - w * V[0];
+          EB(B, 2, 3) = EB(B, 2, 3) - w * V[4];
+          EB(B, 3, 2) = EB(B, 3, 2) - w * V[5];
+          EB(B, 3, 3) = EB(B, 3, 3) - w * V[1];
+          EB(B, 4, 4) = EB(B, 4, 4) - w * V[2];
+          EB(B, 5, 5) = EB(B, 5, 5) - w * V[3];
+        }
+        /* the far-end rows have no block at column j+1 beyond ny; rows 1
+           and ny keep mat(1) / mat(3) of the band zero */
+        if (r == 0)
+          for (int a = 1; a <= 5; ++a)
+            for (int b = 1; b <= 5; ++b) mat3[0 + 3 * (a - 1) + 15 * (b - 1) + 75 * rec] = zero;
+        if (r == 5)
+          for (int a = 1; a <= 5; ++a)
+            for (int b = 1; b <= 5; ++b) mat3[2 + 3 * (a - 1) + 15 * (b - 1) + 75 * rec] = zero;
+        for (int a = 1; a <= 5; ++a) mat3[1 + 3 * (a - 1) + 15 * (a - 1) + 75 * rec] += one;
+      }
+  }
+  /* boundary conditions (nonlinear branches) */
+  for (int i = 1; i <= nx; ++i) {
+    const long rw = (long)(i - 1), rt = (long)(i - 1) + (long)nx * (ny - 1);
+    double* mw = mat3 + 75 * rw;
+    double* mt = mat3 + 75 * rt;
+#define MW(k, a, b) mw[(k - 1) + 3 * (a - 1) + 15 * (b - 1)]
+#define MTT(k, a, b) mt[(k - 1) + 3 * (a - 1) + 15 * (b - 1)]
+#define BCI(jb, a, b) bc[(jb - 1) + 14 * (a - 1) + 70 * (b - 1) + 350L * (i - 1)]
+    if (g->navier) {
+      if (dir == 1) {
+        /* src/lhsbc1.f90 (nonlinear): identity rows at the wall */
+        if (g->wall == 1 || g->wall == 2 || g->wall == 3) {
+          for (int k = 1; k <= 3; ++k)
+            for (int b = 1; b <= 5; ++b) MW(k, 1, b) = zero;
+          MW(2, 1, 1) = one;
+        }
+        for (int a = 2; a <= 4; ++a) {
+          for (int k = 1; k <= 3; ++k)
+            for (int b = 1; b <= 5; ++b) MW(k, a, b) = zero;
+          MW(2, a, a) = one;
+        }
+        if (g->wallt == 0 || g->wallt == 1) {
+          for (int k = 1; k <= 3; ++k)
+            for (int b = 1; b <= 5; ++b) MW(k, 5, b) = zero;
+          MW(2, 5, 5) = one;
+        }
+      } else {
+        /* src/lhsbc2.f90 (nonlinear) */
+        if (g->wall == 1) {
+          for (int k = 1; k <= 3; ++k)
+            for (int b = 1; b <= 5; ++b) MW(k, 1, b) = zero;
+          for (int jb = 1; jb <= 3; ++jb)
+            for (int b = 1; b <= 5; ++b) BCI(jb, 1, b) = zero;
+          MW(2, 1, 1) = -gc1;
+          MW(3, 1, 1) = -gc2;
+          BCI(1, 1, 1) = -gc3;
+          BCI(2, 1, 1) = -gc4;
+          BCI(3, 1, 1) = -gc5;
+        }
+        if (g->wall == 3) {  /* bc(1:3,1,:,:) is not cleared, src/lhsbc2.f90 */
+          for (int k = 1; k <= 3; ++k)
+            for (int b = 1; b <= 5; ++b) MW(k, 1, b) = zero;
+          MW(2, 1, 1) = -one;
+          MW(3, 1, 1) = 4.0;
+          BCI(1, 1, 1) = -6.0;
+          BCI(2, 1, 1) = 4.0;
+          BCI(3, 1, 1) = -one;
+        }
+        for (int a = 2; a <= 4; ++a) {
+          for (int k = 1; k <= 3; ++k)
+            for (int b = 1; b <= 5; ++b) MW(k, a, b) = zero;
+          for (int jb = 1; jb <= 3; ++jb)
+            for (int b = 1; b <= 5; ++b) BCI(jb, a, b) = zero;
+          MW(2, a, a) = one;
+        }
+        if (g->wallt == 0 || g->wallt == 1) {
+          for (int k = 1; k <= 3; ++k)
+            for (int b = 1; b <= 5; ++b) MW(k, 5, b) = zero;
+          for (int jb = 1; jb <= 3; ++jb)
+            for (int b = 1; b <= 5; ++b) BCI(jb, 5, b) = zero;
+        }
+        if (g->wallt == 0) MW(2, 5, 5) = -one;
+        if (g->wallt == 1) {
+          MW(2, 5, 5) = -gc1;
+          MW(3, 5, 5) = -gc2;
+          BCI(1, 5, 5) = -gc3;
+          BCI(2, 5, 5) = -gc4;
+          BCI(3, 5, 5) = -gc5;
+        }
+      }
+    }
+    if (dir == 1) {
+      if (g->top == 0) {  /* src/lhsbc1.f90 (nonlinear), top identity rows */
+        for (int k = 1; k <= 3; ++k)
+          for (int a = 1; a <= 5; ++a)
+            for (int b = 1; b <= 5; ++b) MTT(k, a, b) = zero;
+        for (int a = 1; a <= 5; ++a) MTT(2, a, a) = one;
+      }
+    } else if (g->Ma >= one || g->top == 0) {
+      for (int k = 1; k <= 3; ++k)
+        for (int a = 1; a <= 5; ++a)
+          for (int b = 1; b <= 5; ++b) MTT(k, a, b) = zero;
+      for (int jb = 12; jb <= 14; ++jb)
+        for (int a = 1; a <= 5; ++a)
+          for (int b = 1; b <= 5; ++b) BCI(jb, a, b) = zero;
+      if (g->Ma < one) {
+        /* ReimannLHS on (mat(2), mat(1), bc(14)) of row ny */
+        const Blk rb[3] = {{&BCI(14, 1, 1), 14, 70}, {&MTT(1, 1, 1), 3, 15}, {&MTT(2, 1, 1), 3, 15}};
+        rm_lhs_blk(a2, i, vl + 5 * IX(g, i, ny), vl + 5 * IX(g, i, ny - 1), vl + 5 * IX(g, i, ny - 2), rb);
+      } else {
+        for (int a = 1; a <= 5; ++a) MTT(2, a, a) = one;
+      }
+    }
+#undef MW
+#undef MTT
+#undef BCI
+  }
+  return 0;
+}
+#undef EB
+
+/* src/impdrv.f90:171-400 with linear = 0, impl = 1, iLHS = 0: the
+   second-order LHS and the block-tridiagonal solves solve2p (xi) and
+   solve1bc (eta), src/impdrv.f90:307-344.  mat3 (3,5,5,nx,ny) and bc
+   (14,5,5,nx) are scratch. */
+double a2_step2(const A2Grid* a2, int niter, double* v, double* vold, double* r, A3Ops* ops, double* dtl,
+                double* mat3, double* bc, double* cfl) {
+  const A3Grid* g = G(a2);
+  const int nx = g->nx, ny = g->ny;
+  const long n5 = 5L * nx * ny;
+  double totres = 0.0;
+  const double c = a3_set_time_step(g, v, dtl);
+  if (cfl) *cfl = c;
+  memcpy(vold, v, n5 * sizeof(double));
+  a2_itrbc(a2, v);
+  for (int iter = 1; iter <= niter; ++iter) {
+    a2_genmtrx(a2, v, ops, r);
+    a2_rbe(a2, r, v, vold, dtl);
+    a2_rhsbc(a2, r, v);
+    totres = a2_resstat(a2, r, dtl);
+    a2_lhs2(a2, ops, dtl, v, 1, mat3, bc);
+    orc_tri_p(2, nx, ny, mat3, r);
+    a2_lhs2(a2, ops, dtl, v, 2, mat3, bc);
+    orc_tri_bc(1, ny, nx, mat3, r, bc);
     OMP_FOR
     for (long e = 0; e < n5; ++e) v[e] = v[e] + r[e];
     a2_itrbc(a2, v);

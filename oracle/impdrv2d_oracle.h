@@ -58,6 +58,12 @@ int a2_lhs(const A2Grid* g, const A3Ops* ops, const double* dtl, const double* v
    corrector; *cfl the step's CFL number. */
 double a2_step(const A2Grid* g, int niter, double* v, double* vold, double* r, A3Ops* ops, double* dtl,
                double* mat, double* per, double* cfl);
+/* The second-order path (iLHS = 0): LHS in the block-tridiagonal storage
+   mat3(3,5,5,nx,ny) + bc(14,5,5,nx) (src/lhs.f90, src/lhsbt2.f90,
+   src/lhsbc1.f90, src/lhsbc2.f90), and its step with solve2p / solve1bc. */
+int a2_lhs2(const A2Grid* g, const A3Ops* ops, const double* dtl, const double* v, int dir, double* mat3, double* bc);
+double a2_step2(const A2Grid* g, int niter, double* v, double* vold, double* r, A3Ops* ops, double* dtl,
+                double* mat3, double* bc, double* cfl);
 
 #ifdef __cplusplus
 }

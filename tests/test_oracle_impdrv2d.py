@@ -58,3 +58,59 @@ def test_vortex_steps_stay_finite_and_periodic():
     assert np.isfinite(v).all() and all(r > 0 for r in res)
     assert np.array_equal(v[:, -1, :], v[:, 0, :])
     assert not v[1:4, :, 0].any()      # no-slip wall
+
+
+def test_second_order_lhs_rest_fixed_point_and_vortex():
+    """iLHS = 0 (second-order LHS, block-tridiagonal solves): the rest state
+    stays fixed, and on the vortex the update stays close to the
+    fourth-order path's (both approximate the same implicit operator, so a
+    sign or slot error shows as an O(1) difference)."""
+    from lns3d_gb300.cases import vortex2d
+
+    c = rest_case()
+    o = Oracle2D(c, cflmax=1.0, loctime=0, ilhs=0)
+    v = c["v"].copy(order="F")
+    o.itrbc(v)
+    for _ in range(3):
+        assert o.step(v) < 1e-13
+    assert np.abs(v - c["v"]).max() < 1e-13
+
+    c = vortex2d(nx=32, ny=28)
+    out = []
+    for ilhs in (1, 0):
+        o = Oracle2D(c, cflmax=1.0, loctime=0, ilhs=ilhs)
+        v = c["v"].copy(order="F")
+        o.itrbc(v)
+        v0 = v.copy()
+        o.step(v)
+        out.append(v - v0)
+        assert np.isfinite(v).all() and np.array_equal(v[:, -1, :], v[:, 0, :])
+        assert not v[1:4, :, 0].any()
+    d4, d2 = out
+    assert not np.array_equal(d4, d2)
+    assert np.linalg.norm(d2 - d4) < 0.2 * np.linalg.norm(d4)
+
+
+def test_second_order_lhs_structure():
+    """Band and boundary blocks of the second-order eta LHS: rows 3 and ny-2
+    keep a zero first-derivative part on the diagonal (identity plus the
+    viscous term), the top row carries the far-field blocks, and the eta
+    boundary array is filled only in the rows that use it."""
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=16, ny=12)
+    o = Oracle2D(c, cflmax=1.0, loctime=0, ilhs=0)
+    v = c["v"].copy(order="F")
+    o.itrbc(v)
+    o.rhs(v, v, o.dtl)
+    dtl = np.full((16, 12), 0.01, order="F")
+    mat, bc = o.lhs2(v, dtl, 2)
+    d = mat[1, :, :, :, 2]
+    assert np.array_equal(d[0, 0], np.ones(16))          # continuity row: identity only
+    assert not d[0, 1:].any()
+    assert not mat[0, :, :, :, 0].any()                  # row 1 has no west block
+    assert not mat[2, :, :, :, -1].any()                 # row ny has no east block
+    assert bc[:11].any() and bc[13].any()                # rows 1..3, ny-2..ny; bc(14) holds the far-field block
+    m1, b1 = o.lhs2(v, dtl, 1)
+    assert not b1.any()                                  # periodic xi: no boundary blocks
+    assert np.array_equal(m1[1, 1:4, :, :, 0], np.broadcast_to(np.eye(5)[1:4, :, None], (3, 5, 16)))
