@@ -182,7 +182,7 @@ int lns_solve1p_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, d
 
 /* ---------------------------------------------------------------------------
  * The nonlinear two-dimensional implicit ADI step (src/impdrv.f90:171-400
- * with linear = 0, impl = 1, iLHS = 1) as one device-resident context, FP64
+ * with linear = 0, impl = 1, iLHS = 1 or 0) as one device-resident context, FP64
  * throughout.  Per step: set_time_step on the state, vold = v, itrBC; per
  * corrector genmtrx(v, 0, r) (the nonlinear RHS and the operators), rbe,
  * rhsBC, resstat, lhs1f + lhsbc1f and penta2p (xi), lhs2f + lhsbt2f +
@@ -204,6 +204,10 @@ typedef struct {
   double theta;              /* isothermal-wall recovery angle (wallt 0, src/itrbc.f90:683-686) */
   int32_t loctime, xper, yper, navier, wall, wallt, top, optx, opty;
   int32_t res_compat;        /* as in lns_params3d (src/resstat.f90:17) */
+  int32_t lhs_order;         /* 0 or 4: the fourth-order LHS with pentadiagonal solves (iLHS = 1);
+                                2: the second-order LHS (src/lhs.f90, src/lhsbt2.f90, src/lhsbc1.f90,
+                                src/lhsbc2.f90) with the block-tridiagonal solves solve2p (xi) and
+                                solve1bc (eta) (iLHS = 0, src/impdrv.f90:307-344); needs ny >= 8 */
 } lns_params2d;
 
 typedef struct lns_ctx2d lns_ctx2d;
@@ -230,7 +234,10 @@ int lns_rhs2d_dev(lns_ctx2d* ctx, const double* v, const double* vold, double* r
 /* LHS of the xi (dir 1: src/lhsf.f90:7 + src/lhsbc1f.f90) or eta sweep
  * (dir 2: src/lhsf.f90:164 + src/lhsbt2f.f90 + src/lhsbc2f.f90 with
  * ReimannLHS, src/reimann.f90:238) from the context's operators, into the
- * device array mat(5,5,5,nx,ny) */
+ * device array mat(5,5,5,nx,ny).  With lhs_order = 2 the second-order LHS
+ * (src/lhs.f90, src/lhsbt2.f90, src/lhsbc{1,2}.f90): its mat(3,5,5,..) and
+ * bc(14,5,5,..) blocks placed in the pentadiagonal slots of their columns,
+ * zero blocks elsewhere */
 int lns_lhs2d_dev(lns_ctx2d* ctx, int32_t dir, const double* v, double* mat, void* stream);
 /* host copy of 0 Ah, 1 Bh, 2 Dh (5,5,nx,ny), 3 Vh11, 4 Vh12, 5 Vh22
  * (6,nx,ny), 6 dtl (nx,ny) */

@@ -395,7 +395,16 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
 // (src/lhsf.f90:42-110, 198-247), the eta boundary rows (src/lhsbt2f.f90)
 // and the boundary conditions (src/lhsbc1f.f90:232-605,
 // src/lhsbc2f.f90:195-291).  One thread per entry.
-__global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v, int dir, double* __restrict__ mat) {
+//
+// order2 selects the second-order LHS of the iLHS = 0 path: lhs1 / lhs2
+// (src/lhs.f90:7-137, 140-277), lhsbt2 (src/lhsbt2.f90) and the nonlinear
+// lhsbc1 / lhsbc2 rows (src/lhsbc1.f90, src/lhsbc2.f90).  Its block-
+// tridiagonal rows are written in the same pentadiagonal slots (the outer
+// slots of a band row hold zero blocks, the boundary rows' bc(1..14)
+// blocks sit in the slots of their columns), so one set of line solvers
+// serves both orders: zero blocks add exact zeros to the elimination.
+__global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v, int dir, int order2,
+                             double* __restrict__ mat) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 125 * o.np) return;
   const long long p = q / 125;
@@ -415,7 +424,11 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
       const int tk = (k + 2) % 5;  // coefficient of slot k: slots 3,4,5,1,2 <-> 0..4
       const double gcs[5] = {gc1, gc2, gc3, gc4, gc5}, ex3[5] = {-1.0, 4.0, -6.0, 4.0, -1.0};
       if (a >= 2 && a <= 4) { mat[q] = ident; return; }
-      if (a == 1 && (g.wall == 1 || g.wall == 3)) {
+      // the second-order wall-3 row clears only mat(:,1,:,:,1) (columns 1
+      // and 2): the blocks of columns 3..5 keep their closure entries off
+      // the first column (src/lhsbc2.f90, wall = 3)
+      const bool keep = order2 && g.wall == 3 && b != 1 && (k == 5 || k == 1 || k == 2);
+      if (a == 1 && (g.wall == 1 || g.wall == 3) && !keep) {
         mat[q] = b == 1 ? (g.wall == 1 ? -gcs[tk] : ex3[tk]) : 0.0;
         return;
       }
@@ -449,7 +462,23 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   else if (a == 5 && b == 5) vk = 3;
   double val;
   const bool edge = dir == 2 && !g.yper && (j <= 2 || j >= g.ny - 1);
-  if (!edge) {
+  if (order2 && !edge && (dir == 1 || j > 3 && j < g.ny - 2)) {
+    // three-point band in slots 2..4 (src/lhs.f90:28-104, 176-240)
+    if (k == 1 || k == 5) { mat[q] = 0.0; return; }
+    const double h = dir == 1 ? g.dxi : g.deta;
+    const double ak = k == 2 ? -alfa * 0.5 / h : k == 3 ? alfa * 0.0 : alfa * 0.5 / h;
+    const double bk = k == 3 ? -alfa * 2.0 / (h * h) : alfa / (h * h);
+    val = ak * d * (dir == 1 ? o.Ah : o.Bh)[eab];
+    if (dir == 1 && k == 3) val = val + alfa * d * o.Dh[eab];
+    if (vk >= 0) val = val - bk * d * V[vk * np + p];
+  } else if (order2 && !edge) {
+    // rows 3 and ny-2: the central five-point stencil of lhsbt2 with a
+    // literal zero diagonal block (src/lhsbt2.f90, rows 3 and ny-2)
+    const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
+    const double detainv = 1.0 / g.deta, detasinv = 1.0 / (g.deta * g.deta);
+    val = k == 3 ? 0.0 : alfa * d * gi[k - 1] * detainv * o.Bh[eab];
+    if (vk >= 0) val = val - alfa * d * di[k - 1] * detasinv * V[vk * np + p];
+  } else if (!edge) {
     const double h = dir == 1 ? g.dxi : g.deta;
     const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
     const double ak = alfa * gi[k - 1] / h, bk = alfa * di[k - 1] / (h * h);
@@ -640,7 +669,8 @@ int rhs2(lns_ctx2d* c, const double* v, const double* vold, double* r, double* r
 
 int lhs2(lns_ctx2d* c, const double* v, int dir, double* mat, cudaStream_t st) {
   const long long nq = 125 * c->np;
-  lns::a2::lhs2d_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->g, c->ops, top2(c), v, dir, mat);
+  const int order2 = c->prm.lhs_order == 2 ? 1 : 0;
+  lns::a2::lhs2d_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->g, c->ops, top2(c), v, dir, order2, mat);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda2(e, "lhs2d_kernel launch");
 }
@@ -671,7 +701,12 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
       double* res = (it == niter - 1 && totres_dev) ? totres_dev + s : c->dscal + 1;
       rc = rhs2(c, v, c->vold, c->r, res, acc, st);
       if (!rc) rc = lhs2(c, v, 1, c->mat, st);
-      if (!rc) rc = lns::host::launch_p<double>(c->mat, c->r, c->per, c->per2, g.nx, g.ny, 1, g.nx, 2, st, c->status);
+      // the fourth-order path solves with penta2p (its periodic fill-slot
+      // quirk kept unless the exact mode is on), the second-order path with
+      // solve2p, which has no such quirk (src/nsolve2p.f90)
+      if (!rc)
+        rc = lns::host::launch_p<double>(c->mat, c->r, c->per, c->per2, g.nx, g.ny, 1, g.nx, 2, st, c->status,
+                                         c->prm.lhs_order == 2 ? 1 : -1);
       if (!rc) rc = lhs2(c, v, 2, c->mat, st);
       if (!rc) rc = lns::host::launch_bc<double>(c->mat, c->r, g.ny, g.nx, g.nx, 1, 2, st, c->status);
       if (!rc) {
@@ -714,6 +749,9 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   if (!(p->Ma > 0.0) || p->Ma == 1.0) return fail2(LNS_ERR_ARG, "ctx2d_create: need Ma > 0 and Ma != 1");
   if (p->loctime != 0 && p->loctime != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: loctime must be 0 or 1");
   if (p->res_compat != 0 && p->res_compat != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: res_compat must be 0 or 1");
+  if (p->lhs_order != 0 && p->lhs_order != 2 && p->lhs_order != 4)
+    return fail2(LNS_ERR_ARG, "ctx2d_create: lhs_order must be 0 (fourth order), 2 or 4");
+  if (p->lhs_order == 2 && p->ny < 8) return fail2(LNS_ERR_ARG, "ctx2d_create: the second-order LHS needs ny >= 8");
   lns_ctx2d* c = new lns_ctx2d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);

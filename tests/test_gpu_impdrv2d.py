@@ -167,3 +167,80 @@ def test_device_steps_and_reference_residual_mode(cuda, small):
     res_o = np.array([o.step(vo) for _ in range(4)])
     assert np.abs(tot.cpu().numpy() - res_o).max() <= 1e-10 * res_o.max()
     assert abs(res_h[0] - res_o[0]) <= 1e-10 * res_o[0]   # the first call has no previous value
+
+
+# ---------------------------------------------------------------- iLHS = 0
+# The second-order LHS (src/lhs.f90, src/lhsbt2.f90, src/lhsbc{1,2}.f90)
+# with the block-tridiagonal solves (src/nsolve2p.f90, src/nsolve1bc.f90).
+# The device writes it in the pentadiagonal slots; both sides are compared
+# as the dense matrices of their lines.
+
+
+def _dense_lines(direction, nx, ny, tri=None, penta=None):
+    import tricase
+    from test_oracle import dense as penta_dense
+
+    out = []
+    nsys = ny if direction == 1 else nx
+    for iv in range(nsys):
+        if tri is not None:
+            mat3, bc = tri
+            case = ({"solver": "solve2p", "rows": nx, "mat": mat3} if direction == 1 else
+                    {"solver": "solve1bc", "rows": ny, "mat": mat3, "bc": bc})
+            out.append(tricase.dense_line(case, iv))
+        else:
+            case = ({"solver": "penta2p", "rows": nx, "mat": penta} if direction == 1 else
+                    {"solver": "penta1bc", "rows": ny, "mat": penta})
+            out.append(penta_dense(case, iv)[0])
+    return np.array(out)
+
+
+@pytest.mark.parametrize("direction,wall,wallt", [(1, 0, 1), (2, 0, 1), (2, 1, 0), (2, 3, 1)])
+def test_second_order_lhs_matches_oracle(cuda, small, direction, wall, wallt):
+    import ctypes
+
+    import torch
+
+    c, v = small
+    c = dict(c, params=dict(c["params"], wall=wall, wallt=wallt))
+    o = Oracle2D(c, cflmax=1.0, loctime=0, ilhs=0)
+    o.L.a3_set_time_step(ctypes.byref(o.g.g), ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(o.dtl.ctypes.data))
+    o.rhs(v, v, o.dtl)
+    nx, ny = c["params"]["nx"], c["params"]["ny"]
+    ref = _dense_lines(direction, nx, ny, tri=o.lhs2(v, o.dtl, direction))
+    drv = make(c, ilhs=0)
+    dv = dev(v)
+    drv.rhs(dv, dv, torch.zeros_like(dv))
+    mat = torch.zeros(125 * nx * ny, dtype=torch.float64, device="cuda")
+    drv.lhs(direction, dv, mat)
+    torch.cuda.synchronize()
+    got = _dense_lines(direction, nx, ny, penta=host(mat, (5, 5, 5, nx, ny)))
+    assert rel(got, ref) < OPS_TOL
+    # the fourth-order LHS of the same context type differs (a wrong switch
+    # would pass the comparison above only by accident)
+    drv4 = make(c)
+    drv4.rhs(dv, dv, torch.zeros_like(dv))
+    drv4.lhs(direction, dv, mat)
+    torch.cuda.synchronize()
+    assert rel(_dense_lines(direction, nx, ny, penta=host(mat, (5, 5, 5, nx, ny))), ref) > 1e-3
+
+
+@pytest.mark.parametrize("niter,wall", [(1, 0), (2, 0), (1, 3)])
+def test_second_order_steps_match_oracle(cuda, niter, wall):
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=40, ny=33, seed=5)
+    c["params"]["wall"] = wall
+    o = Oracle2D(c, cflmax=1.0, loctime=0, ilhs=0)
+    drv = make(c, ilhs=0)
+    v_ref = c["v"].copy(order="F")
+    o.itrbc(v_ref)
+    v_gpu = v_ref.copy(order="F")
+    v4 = v_ref.copy(order="F")
+    for s in range(5):
+        res_ref = o.step(v_ref, niter=niter)
+        res_gpu = drv.step(v_gpu, nsteps=1, niter=niter)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+    make(c).step(v4, nsteps=5, niter=niter)
+    assert rel(v4, v_ref) > 1e-9
