@@ -182,7 +182,7 @@ int lns_solve1p_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, d
 
 /* ---------------------------------------------------------------------------
  * The nonlinear two-dimensional implicit ADI step (src/impdrv.f90:171-400
- * with linear = 0, impl = 1, iLHS = 1 or 0) as one device-resident context, FP64
+ * with linear = 0, impl = 1, 2 or 3, iLHS = 1 or 0) as one device-resident context, FP64
  * throughout.  Per step: set_time_step on the state, vold = v, itrBC; per
  * corrector genmtrx(v, 0, r) (the nonlinear RHS and the operators), rbe,
  * rhsBC, resstat, lhs1f + lhsbc1f and penta2p (xi), lhs2f + lhsbt2f +
@@ -208,6 +208,11 @@ typedef struct {
                                 2: the second-order LHS (src/lhs.f90, src/lhsbt2.f90, src/lhsbc1.f90,
                                 src/lhsbc2.f90) with the block-tridiagonal solves solve2p (xi) and
                                 solve1bc (eta) (iLHS = 0, src/impdrv.f90:307-344); needs ny >= 8 */
+  int32_t impl;              /* time scheme (src/impdrv.f90:186-279): 1 (or 0) backward Euler with
+                                alfa; 2 two-step backward, backward Euler at alfa = 1 for the
+                                context's first step and rtb at alfa = 2/3 after it; 3 midpoint,
+                                genmtrx on (v + vold)/2 with alfa = 1/2.  Steps are counted from
+                                the context's creation (a fresh run, lstep = 0). */
 } lns_params2d;
 
 typedef struct lns_ctx2d lns_ctx2d;

@@ -105,7 +105,7 @@ class Params2D(ctypes.Structure):
                 ("gamma", ctypes.c_double), ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double),
                 ("dtmax", ctypes.c_double), ("theta", ctypes.c_double), ("loctime", I32), ("xper", I32),
                 ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32), ("top", I32), ("optx", I32),
-                ("opty", I32), ("res_compat", I32), ("lhs_order", I32)]
+                ("opty", I32), ("res_compat", I32), ("lhs_order", I32), ("impl", I32)]
 
 
 class Params3D(ctypes.Structure):

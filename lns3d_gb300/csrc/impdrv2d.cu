@@ -141,9 +141,13 @@ __device__ __forceinline__ double tw_wall(const Grid& g, double theta) {
 // general = true, mattyp = 0, kzl = 0), rbe (src/impdrv.f90:482-505), the
 // boundary rows (src/rhsbc.f90:256-370) and the block sums of resstat
 // (src/resstat.f90:37-50).  One thread per point; r may be null (operators
-// only, when vold is null too).
-__global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, Top tp, const double* __restrict__ v,
-                                                    const double* __restrict__ vold, double* __restrict__ r,
+// only, when vold is null too).  genmtrx acts on the state vs (v itself, or
+// pt5 (v + vold) for the midpoint rule, src/impdrv.f90:271-279); rbe and the
+// boundary rows use v; a non-null v2old selects rtb (src/impdrv.f90:511-539)
+// in place of rbe.
+__global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, Top tp, const double* __restrict__ vs,
+                                                    const double* __restrict__ v, const double* __restrict__ vold,
+                                                    const double* __restrict__ v2old, double* __restrict__ r,
                                                     double* part) {
   __shared__ double red[128];
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -151,7 +155,8 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
   double resnod = 0.0;
   if (i <= g.nx) {
     const long long p = pix(g, i, j), np = o.np;
-    auto V = [&](int k, int ii, int jj) { return v[k + 5 * pix(g, ii, jj)]; };
+    auto V = [&](int k, int ii, int jj) { return vs[k + 5 * pix(g, ii, jj)]; };
+    auto VF = [&](int k, int ii, int jj) { return v[k + 5 * pix(g, ii, jj)]; };
     double g1v[5], g2v[5], g11v[5], g12v[5], g22v[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
@@ -347,18 +352,25 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
     if (r) {
       // rbe
       const double dtl = o.dtl[p];
-      for (int m = 0; m < 5; ++m) rr[m] = vold[m + 5 * p] - V(m, i, j) - dtl * rr[m];
+      if (v2old) {
+        const double onept33 = 1.3333333333333333333e+0, pt33 = 3.3333333333333333333e-1,
+                     pt66 = 6.6666666666666666666e-1;
+        for (int m = 0; m < 5; ++m)
+          rr[m] = onept33 * vold[m + 5 * p] - pt33 * v2old[m + 5 * p] - VF(m, i, j) - pt66 * dtl * rr[m];
+      } else {
+        for (int m = 0; m < 5; ++m) rr[m] = vold[m + 5 * p] - VF(m, i, j) - dtl * rr[m];
+      }
       // boundary rows, src/rhsbc.f90:258-362
       if (!g.yper) {
         if (g.navier && j == 1) {
           for (int m = 1; m <= 3; ++m) rr[m] = 0.0;
           if (g.wall == 1)
-            rr[0] = gc1 * V(0, i, 1) + gc2 * V(0, i, 2) + gc3 * V(0, i, 3) + gc4 * V(0, i, 4) + gc5 * V(0, i, 5);
+            rr[0] = gc1 * VF(0, i, 1) + gc2 * VF(0, i, 2) + gc3 * VF(0, i, 3) + gc4 * VF(0, i, 4) + gc5 * VF(0, i, 5);
           if (g.wall == 3)
-            rr[0] = V(0, i, 1) - (4.0 * V(0, i, 2) - 6.0 * V(0, i, 3) + 4.0 * V(0, i, 4) - V(0, i, 5));
-          if (g.wallt == 0) rr[4] = V(4, i, 1) - tw_wall(g, tp.theta);
+            rr[0] = VF(0, i, 1) - (4.0 * VF(0, i, 2) - 6.0 * VF(0, i, 3) + 4.0 * VF(0, i, 4) - VF(0, i, 5));
+          if (g.wallt == 0) rr[4] = VF(4, i, 1) - tw_wall(g, tp.theta);
           if (g.wallt == 1)
-            rr[4] = gc1 * V(4, i, 1) + gc2 * V(4, i, 2) + gc3 * V(4, i, 3) + gc4 * V(4, i, 4) + gc5 * V(4, i, 5);
+            rr[4] = gc1 * VF(4, i, 1) + gc2 * VF(4, i, 2) + gc3 * VF(4, i, 3) + gc4 * VF(4, i, 4) + gc5 * VF(4, i, 5);
         }
         if (j == g.ny) {
           if (g.Ma > 1.0) {
@@ -368,7 +380,7 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
                                        v + 5 * pix(g, i, g.ny - 2));
             double b[5];
             rm_values(g, tp, i, s, b);
-            for (int m = 0; m < 5; ++m) rr[m] = V(m, i, j) - b[m];
+            for (int m = 0; m < 5; ++m) rr[m] = VF(m, i, j) - b[m];
           }
         }
       } else if (j == g.ny) {
@@ -547,6 +559,13 @@ __global__ void bc2d_kernel(Grid g, Top tp, double* __restrict__ v) {
   }
 }
 
+// w = pt5 (v + vold), the midpoint state (src/impdrv.f90:273)
+__global__ void avg2d_kernel(long long n, const double* __restrict__ v, const double* __restrict__ vold,
+                             double* __restrict__ w) {
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (e < n) w[e] = 0.5 * (v[e] + vold[e]);
+}
+
 }  // namespace a2
 }  // namespace lns
 
@@ -569,6 +588,8 @@ struct lns_ctx2d {
   Ops ops{};
   double *bnt = nullptr, *pot = nullptr;  // far field of the top boundary
   double *v = nullptr, *vold = nullptr, *r = nullptr, *mat = nullptr, *per = nullptr, *per2 = nullptr;
+  double *v2old = nullptr, *wavg = nullptr;  // impl 2 / impl 3 state
+  long long lstep = 0;                       // steps taken since creation
   double* part = nullptr;
   int nparts = 0;
   double* dscal = nullptr;  // [0] cfl, [1] scratch residual, [2] running residual
@@ -658,19 +679,22 @@ int time_step(lns_ctx2d* c, const double* v, cudaStream_t st) {
   return e == cudaSuccess ? LNS_OK : cuda2(e, "time-step kernels launch");
 }
 
-int rhs2(lns_ctx2d* c, const double* v, const double* vold, double* r, double* res, double* acc, cudaStream_t st) {
+int rhs2(lns_ctx2d* c, const double* vs, const double* v, const double* vold, const double* v2old, double* r,
+         double* res, double* acc, cudaStream_t st) {
   const Grid& g = c->g;
-  lns::a2::rhs2d_kernel<<<pgrid(g), 128, 0, st>>>(g, c->ops, metrics2(c), top2(c), v, vold, r, c->part);
+  lns::a2::rhs2d_kernel<<<pgrid(g), 128, 0, st>>>(g, c->ops, metrics2(c), top2(c), vs, v, vold, v2old, r, c->part);
   const int nrhs = (int)(pgrid(g).x * pgrid(g).y);
   lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res, acc);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda2(e, "rhs kernels launch");
 }
 
-int lhs2(lns_ctx2d* c, const double* v, int dir, double* mat, cudaStream_t st) {
+int lhs2(lns_ctx2d* c, const double* v, int dir, double* mat, double alfa, cudaStream_t st) {
   const long long nq = 125 * c->np;
   const int order2 = c->prm.lhs_order == 2 ? 1 : 0;
-  lns::a2::lhs2d_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->g, c->ops, top2(c), v, dir, order2, mat);
+  Grid g = c->g;
+  g.alfa = alfa;
+  lns::a2::lhs2d_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(g, c->ops, top2(c), v, dir, order2, mat);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda2(e, "lhs2d_kernel launch");
 }
@@ -682,16 +706,28 @@ int bc2(lns_ctx2d* c, double* v, cudaStream_t st) {
   return e == cudaSuccess ? LNS_OK : cuda2(e, "bc2d_kernel launch");
 }
 
-// nsteps steps of niter correctors (src/impdrv.f90:171-400)
+// nsteps steps of niter correctors (src/impdrv.f90:171-400) with the time
+// scheme of the context (src/impdrv.f90:186-279): impl 1 backward Euler
+// with the deck's alfa; impl 2 backward Euler at alfa = 1 for the
+// context's first step, then v2old = vold and rtb at alfa = pt66; impl 3
+// genmtrx on pt5 (v + vold) with rbe at alfa = pt5
 int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cudaStream_t st) {
   const Grid& g = c->g;
   const size_t vbytes = sizeof(double) * 5 * (size_t)c->np;
+  const long long n5 = 5 * c->np;
+  const int impl = c->prm.impl == 0 ? 1 : c->prm.impl;
   double* acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
   cudaError_t e = cudaMemsetAsync(c->status, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda2(e, "cudaMemsetAsync");
   int rc = LNS_OK;
   for (int s = 0; s < nsteps && !rc; ++s) {
+    const bool rtb = impl == 2 && c->lstep > 0;
+    const double alfa = impl == 3 ? 0.5 : rtb ? 6.6666666666666666666e-1 : (impl == 2 ? 1.0 : c->prm.alfa);
     rc = time_step(c, v, st);
+    if (!rc && rtb) {
+      e = cudaMemcpyAsync(c->v2old, c->vold, vbytes, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) rc = cuda2(e, "cudaMemcpyAsync v2old");
+    }
     if (!rc) {
       e = cudaMemcpyAsync(c->vold, v, vbytes, cudaMemcpyDeviceToDevice, st);
       if (e != cudaSuccess) rc = cuda2(e, "cudaMemcpyAsync vold");
@@ -699,15 +735,22 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
     if (!rc) rc = bc2(c, v, st);
     for (int it = 0; it < niter && !rc; ++it) {
       double* res = (it == niter - 1 && totres_dev) ? totres_dev + s : c->dscal + 1;
-      rc = rhs2(c, v, c->vold, c->r, res, acc, st);
-      if (!rc) rc = lhs2(c, v, 1, c->mat, st);
+      const double* vs = v;
+      if (impl == 3) {
+        lns::a2::avg2d_kernel<<<(unsigned)((n5 + 255) / 256), 256, 0, st>>>(n5, v, c->vold, c->wavg);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda2(e, "avg2d_kernel launch");
+        vs = c->wavg;
+      }
+      if (!rc) rc = rhs2(c, vs, v, c->vold, rtb ? c->v2old : nullptr, c->r, res, acc, st);
+      if (!rc) rc = lhs2(c, v, 1, c->mat, alfa, st);
       // the fourth-order path solves with penta2p (its periodic fill-slot
       // quirk kept unless the exact mode is on), the second-order path with
       // solve2p, which has no such quirk (src/nsolve2p.f90)
       if (!rc)
         rc = lns::host::launch_p<double>(c->mat, c->r, c->per, c->per2, g.nx, g.ny, 1, g.nx, 2, st, c->status,
                                          c->prm.lhs_order == 2 ? 1 : -1);
-      if (!rc) rc = lhs2(c, v, 2, c->mat, st);
+      if (!rc) rc = lhs2(c, v, 2, c->mat, alfa, st);
       if (!rc) rc = lns::host::launch_bc<double>(c->mat, c->r, g.ny, g.nx, g.nx, 1, 2, st, c->status);
       if (!rc) {
         const long long n = 5 * c->np;
@@ -717,6 +760,7 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
       }
       if (!rc) rc = bc2(c, v, st);
     }
+    if (!rc) c->lstep += 1;
   }
   return rc;
 }
@@ -752,6 +796,7 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   if (p->lhs_order != 0 && p->lhs_order != 2 && p->lhs_order != 4)
     return fail2(LNS_ERR_ARG, "ctx2d_create: lhs_order must be 0 (fourth order), 2 or 4");
   if (p->lhs_order == 2 && p->ny < 8) return fail2(LNS_ERR_ARG, "ctx2d_create: the second-order LHS needs ny >= 8");
+  if (p->impl < 0 || p->impl > 3) return fail2(LNS_ERR_ARG, "ctx2d_create: impl must be 0 or 1 (backward Euler), 2 or 3");
   lns_ctx2d* c = new lns_ctx2d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);
@@ -792,6 +837,8 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   A(sizeof(double) * 3, &q); c->dscal = (double*)q;
   A(sizeof(int), &q); c->status = (int*)q;
   A(sizeof(double) * 64, &q); c->res_dev = (double*)q;
+  if (p->impl == 2) { A(sizeof(double) * 5 * np, &q); c->v2old = (double*)q; }
+  if (p->impl == 3) { A(sizeof(double) * 5 * np, &q); c->wavg = (double*)q; }
   if (!rc) {
     c->res_cap = 64;
     e = cudaMemset(c->dscal, 0, sizeof(double) * 3);
@@ -897,7 +944,7 @@ int lns_rhs2d_dev(lns_ctx2d* c, const double* v, const double* vold, double* r, 
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   rc = time_step(c, v, st);
-  if (!rc) rc = rhs2(c, v, vold, r, totres_dev ? totres_dev : c->dscal + 1, nullptr, st);
+  if (!rc) rc = rhs2(c, v, v, vold, nullptr, r, totres_dev ? totres_dev : c->dscal + 1, nullptr, st);
   return rc;
 }
 
@@ -906,7 +953,7 @@ int lns_lhs2d_dev(lns_ctx2d* c, int32_t dir, const double* v, double* mat, void*
   if (dir != 1 && dir != 2) return fail2(LNS_ERR_ARG, "lhs2d: dir must be 1 or 2");
   int rc = ready2(c, "lhs2d");
   if (rc) return rc;
-  return lhs2(c, v, dir, mat, (cudaStream_t)stream);
+  return lhs2(c, v, dir, mat, c->prm.alfa, (cudaStream_t)stream);
 }
 
 int lns_get_field2d(lns_ctx2d* c, int32_t which, double* out) {

@@ -37,19 +37,22 @@ class ImpDrv2D:
     """
 
     def __init__(self, params, metrics, bnt, pot, cflmax=1.0, dtmax=1e30, loctime=0, theta=0.0, res_compat=False,
-                 ilhs=1):
+                 ilhs=1, impl=1):
         """ilhs: the reference's iLHS switch, 1 = fourth-order LHS with
         pentadiagonal solves, 0 = second-order LHS with block-tridiagonal
-        solves (src/impdrv.f90:307-344)."""
+        solves (src/impdrv.f90:307-344).  impl: time scheme, 1 backward
+        Euler, 2 two-step backward, 3 midpoint (src/impdrv.f90:186-279)."""
         if ilhs not in (0, 1):
             raise ValueError("ilhs must be 0 or 1")
+        if impl not in (1, 2, 3):
+            raise ValueError("impl must be 1, 2 or 3")
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         prm = Params2D(nx=self.nx, ny=self.ny, dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
                        gamma=p["gamma"], alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax, theta=theta, loctime=loctime,
                        xper=p["xper"], yper=p["yper"], navier=p["navier"], wall=p["wall"], wallt=p["wallt"],
                        top=p["top"], optx=p["optx"], opty=p["opty"], res_compat=1 if res_compat else 0,
-                       lhs_order=2 if ilhs == 0 else 4)
+                       lhs_order=2 if ilhs == 0 else 4, impl=impl)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx2d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx2d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")

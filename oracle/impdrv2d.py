@@ -33,6 +33,9 @@ def _lib(L=None):
         L.a2_lhs2.argtypes = [G, ctypes.POINTER(A3Ops), P, P, I, P, P]
         L.a2_step2.argtypes = [G, I, P, P, P, ctypes.POINTER(A3Ops), P, P, P, P]
         L.a2_step2.restype = D
+        L.a2_step_impl.argtypes = [G, I, I, ctypes.c_long, I, P, P, P, P, P, ctypes.POINTER(A3Ops), P, P, P, P, P,
+                                   P]
+        L.a2_step_impl.restype = D
         L._a2_setup = True
     return L
 
@@ -44,11 +47,13 @@ def ptr(a):
 class Oracle2D:
     """Grid struct, operator storage and scratch of the oracle for one case."""
 
-    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False, ilhs=1):
+    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False, ilhs=1, impl=1):
         """ilhs = 1: fourth-order LHS, pentadiagonal solves; ilhs = 0:
-        second-order LHS, block-tridiagonal solves (src/impdrv.f90:307-344)."""
+        second-order LHS, block-tridiagonal solves (src/impdrv.f90:307-344).
+        impl: time scheme 1 (backward Euler), 2 (two-step backward), 3
+        (midpoint), src/impdrv.f90:186-279; steps are counted from creation."""
         self.L = _lib(lib)
-        self.ilhs = ilhs
+        self.ilhs, self.impl, self.lstep = ilhs, impl, 0
         p = case["params"]
         self.nx, self.ny = nx, ny = p["nx"], p["ny"]
         self.keep = {k: np.asfortranarray(v, dtype=np.float64) for k, v in case["metrics"].items()}
@@ -73,6 +78,8 @@ class Oracle2D:
         self.vold = np.zeros((5, nx, ny), order="F")
         self.mat = np.zeros((5, 5, 5, nx, ny), order="F")
         self.per = np.zeros((2, 5, 5, nx, ny), order="F")
+        self.v2old = np.zeros((5, nx, ny), order="F")
+        self.w = np.zeros((5, nx, ny), order="F")
         self.mat3 = np.zeros((3, 5, 5, nx, ny), order="F")
         self.bc = np.zeros((14, 5, 5, nx), order="F")
         self.cfl = ctypes.c_double(0.0)
@@ -81,6 +88,13 @@ class Oracle2D:
         self.L.a2_itrbc(ctypes.byref(self.g), ptr(v))
 
     def step(self, v, niter=1):
+        if self.impl != 1:
+            res = self.L.a2_step_impl(ctypes.byref(self.g), self.ilhs, self.impl, self.lstep, niter, ptr(v),
+                                      ptr(self.vold), ptr(self.v2old), ptr(self.w), ptr(self.r),
+                                      ctypes.byref(self.o), ptr(self.dtl), ptr(self.mat), ptr(self.per),
+                                      ptr(self.mat3), ptr(self.bc), ctypes.byref(self.cfl))
+            self.lstep += 1
+            return res
         if self.ilhs == 0:
             return self.L.a2_step2(ctypes.byref(self.g), niter, ptr(v), ptr(self.vold), ptr(self.r),
                                    ctypes.byref(self.o), ptr(self.dtl), ptr(self.mat3), ptr(self.bc),

@@ -930,3 +930,76 @@ double a2_step2(const A2Grid* a2, int niter, double* v, double* vold, double* r,
   }
   return totres;
 }
+
+/* ------------------------------------------------------------ time schemes */
+
+/* rtb, src/impdrv.f90:511-539: the two-step backward right-hand side
+   r = onept33 vold - pt33 v2old - v - pt66 dtl r */
+void a2_rtb(const A2Grid* a2, double* r, const double* v, const double* vold, const double* v2old,
+            const double* dtl) {
+  const A3Grid* g = G(a2);
+  const double onept33 = 1.3333333333333333333, pt33 = 3.3333333333333333333e-1, pt66 = 6.6666666666666666666e-1;
+  for (int j = 1; j <= g->ny; ++j)
+    for (int i = 1; i <= g->nx; ++i)
+      for (int k = 0; k < 5; ++k) {
+        const long e = k + 5 * IX(g, i, j);
+        r[e] = onept33 * vold[e] - pt33 * v2old[e] - v[e] - pt66 * dtl[IX(g, i, j)] * r[e];
+      }
+}
+
+/* One step of src/impdrv.f90:172-402 (linear = 0) with the time scheme impl
+   (src/impdrv.f90:186-198, 245-279) and the LHS order ilhs
+   (src/impdrv.f90:307-332):
+     impl 1  backward Euler with the grid's alfa;
+     impl 2  two-step backward: backward Euler (alfa = 1) while lstep = 0,
+             afterwards v2old = vold and rtb with alfa = pt66;
+     impl 3  midpoint: genmtrx on pt5 (v + vold) (the operators of the LHS
+             too), rbe, alfa = pt5.
+   ilhs 1 uses the fourth-order LHS and the pentadiagonal solvers, 0 the
+   second-order LHS and the block-tridiagonal solvers.  v2old and w
+   (5,nx,ny) are needed for impl 2 and 3; mat(5,5,5,nx,ny) + per for ilhs 1,
+   mat3(3,5,5,nx,ny) + bc(14,5,5,nx) for ilhs 0. */
+double a2_step_impl(const A2Grid* a2, int ilhs, int impl, long lstep, int niter, double* v, double* vold,
+                    double* v2old, double* w, double* r, A3Ops* ops, double* dtl, double* mat, double* per,
+                    double* mat3, double* bc, double* cfl) {
+  const A3Grid* g = G(a2);
+  const int nx = g->nx, ny = g->ny;
+  const long n5 = 5L * nx * ny;
+  const int rtb = impl == 2 && lstep > 0;
+  A2Grid al = *a2;
+  al.g.alfa = impl == 3 ? pt5 : rtb ? 6.6666666666666666666e-1 : (impl == 2 ? one : g->alfa);
+  double totres = 0.0;
+  const double c = a3_set_time_step(g, v, dtl);
+  if (cfl) *cfl = c;
+  if (rtb) memcpy(v2old, vold, n5 * sizeof(double));
+  memcpy(vold, v, n5 * sizeof(double));
+  a2_itrbc(a2, v);
+  for (int iter = 1; iter <= niter; ++iter) {
+    if (impl == 3) {
+      OMP_FOR
+      for (long e = 0; e < n5; ++e) w[e] = pt5 * (v[e] + vold[e]);
+      a2_genmtrx(&al, w, ops, r);
+    } else {
+      a2_genmtrx(&al, v, ops, r);
+    }
+    if (rtb) a2_rtb(&al, r, v, vold, v2old, dtl);
+    else a2_rbe(&al, r, v, vold, dtl);
+    a2_rhsbc(&al, r, v);
+    totres = a2_resstat(&al, r, dtl);
+    if (ilhs == 0) {
+      a2_lhs2(&al, ops, dtl, v, 1, mat3, bc);
+      orc_tri_p(2, nx, ny, mat3, r);
+      a2_lhs2(&al, ops, dtl, v, 2, mat3, bc);
+      orc_tri_bc(1, ny, nx, mat3, r, bc);
+    } else {
+      a2_lhs(&al, ops, dtl, v, 1, mat);
+      orc_penta_p(2, nx, ny, mat, r, per, ORC_COMPAT_PERIODIC_SLOT);
+      a2_lhs(&al, ops, dtl, v, 2, mat);
+      orc_penta_bc(1, ny, nx, mat, r);
+    }
+    OMP_FOR
+    for (long e = 0; e < n5; ++e) v[e] = v[e] + r[e];
+    a2_itrbc(a2, v);
+  }
+  return totres;
+}

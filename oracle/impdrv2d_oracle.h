@@ -64,6 +64,13 @@ double a2_step(const A2Grid* g, int niter, double* v, double* vold, double* r, A
 int a2_lhs2(const A2Grid* g, const A3Ops* ops, const double* dtl, const double* v, int dir, double* mat3, double* bc);
 double a2_step2(const A2Grid* g, int niter, double* v, double* vold, double* r, A3Ops* ops, double* dtl,
                 double* mat3, double* bc, double* cfl);
+/* rtb (src/impdrv.f90:511-539) and one step with the time scheme impl 1/2/3
+   (src/impdrv.f90:186-279) and the LHS order ilhs 1/0; lstep counts the
+   steps before this one. */
+void a2_rtb(const A2Grid* g, double* r, const double* v, const double* vold, const double* v2old, const double* dtl);
+double a2_step_impl(const A2Grid* g, int ilhs, int impl, long lstep, int niter, double* v, double* vold,
+                    double* v2old, double* w, double* r, A3Ops* ops, double* dtl, double* mat, double* per,
+                    double* mat3, double* bc, double* cfl);
 
 #ifdef __cplusplus
 }

@@ -244,3 +244,36 @@ def test_second_order_steps_match_oracle(cuda, niter, wall):
         assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
     make(c).step(v4, nsteps=5, niter=niter)
     assert rel(v4, v_ref) > 1e-9
+
+
+@pytest.mark.parametrize("impl,ilhs", [(2, 1), (3, 1), (2, 0), (3, 0)])
+def test_time_schemes_match_oracle(cuda, impl, ilhs):
+    """impl 2 (two-step backward: backward Euler first, then rtb at alfa =
+    2/3) and impl 3 (midpoint: genmtrx on (v + vold)/2, alfa = 1/2),
+    src/impdrv.f90:186-279, per step against the oracle, with both LHS
+    orders; the first step of impl 2 is the backward Euler step."""
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=40, ny=33, seed=6)
+    o = Oracle2D(c, cflmax=1.0, loctime=0, ilhs=ilhs, impl=impl)
+    drv = make(c, ilhs=ilhs, impl=impl)
+    v_ref = c["v"].copy(order="F")
+    o.itrbc(v_ref)
+    v_gpu = v_ref.copy(order="F")
+    v_be = v_ref.copy(order="F")
+    for s in range(4):
+        res_ref = o.step(v_ref)
+        res_gpu = drv.step(v_gpu, nsteps=1)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+        if s == 0:
+            make(c, ilhs=ilhs).step(v_be, nsteps=1)
+            assert (rel(v_gpu, v_be) < STEP_TOL) == (impl == 2)
+
+
+def test_time_scheme_argument_checks():
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=16, ny=12)
+    with pytest.raises(ValueError):
+        make(c, impl=4)

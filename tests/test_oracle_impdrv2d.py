@@ -114,3 +114,41 @@ def test_second_order_lhs_structure():
     m1, b1 = o.lhs2(v, dtl, 1)
     assert not b1.any()                                  # periodic xi: no boundary blocks
     assert np.array_equal(m1[1, 1:4, :, :, 0], np.broadcast_to(np.eye(5)[1:4, :, None], (3, 5, 16)))
+
+
+def test_time_schemes_rest_fixed_point_and_consistency():
+    """impl 2 and 3 (src/impdrv.f90:186-279): the rest state stays fixed;
+    impl 2's first step is the backward Euler step at alfa = 1 (the
+    fourth- and second-order paths alike); the schemes then differ from
+    backward Euler but stay close to it on the vortex (all approximate the
+    same steady operator)."""
+    from lns3d_gb300.cases import vortex2d
+
+    c = rest_case()
+    for impl in (2, 3):
+        o = Oracle2D(c, cflmax=1.0, loctime=0, impl=impl)
+        v = c["v"].copy(order="F")
+        o.itrbc(v)
+        for _ in range(3):
+            assert o.step(v) < 1e-13
+        assert np.abs(v - c["v"]).max() < 1e-13
+
+    c = vortex2d(nx=32, ny=28)
+    for ilhs in (1, 0):
+        runs = {}
+        for impl in (1, 2, 3):
+            o = Oracle2D(c, cflmax=1.0, loctime=0, ilhs=ilhs, impl=impl)
+            v = c["v"].copy(order="F")
+            o.itrbc(v)
+            res = [o.step(v)]
+            first = v.copy(order="F")
+            res += [o.step(v) for _ in range(3)]
+            runs[impl] = (first, v, res)
+            assert np.isfinite(v).all() and np.array_equal(v[:, -1, :], v[:, 0, :])
+        assert np.array_equal(runs[2][0], runs[1][0])            # BE first step (alfa = 1 here)
+        assert runs[2][2][0] == runs[1][2][0]
+        assert not np.array_equal(runs[2][1], runs[1][1])
+        assert not np.array_equal(runs[3][0], runs[1][0])
+        for impl in (2, 3):
+            d = np.linalg.norm(runs[impl][1] - c["v"]) / np.linalg.norm(c["v"])
+            assert np.linalg.norm(runs[impl][1] - runs[1][1]) < 0.5 * np.linalg.norm(runs[1][1] - c["v"]) + 1e-3 * d
