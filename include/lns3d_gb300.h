@@ -325,6 +325,12 @@ typedef struct {
                                 operator at (v + vold)/2 with alfa = 1/2.  Steps
                                 are counted from the context's creation (a fresh
                                 run, lstep = 0).  Batches and servers take 1. */
+  int32_t ispg;              /* sponge (src/lrhs3d.f90:220-240, src/lhs2f3d.f90:207-224,
+                                src/lhsbt2f3d.f90:147-167): 0 none; 1 r += spg v and
+                                alfa dtl spg on the diagonal of the eta LHS; > 4 the same
+                                with spg + spg2.  The inflow sponges 2, 3 and the
+                                iterated sponge 4 are not supported.  Batches and servers
+                                take 0. */
 } lns_params3d;
 
 typedef struct lns_ctx3d lns_ctx3d;
@@ -338,6 +344,10 @@ size_t lns_ctx3d_bytes(const lns_ctx3d* ctx);
 /* metrics(nx,ny,10) on the host: m1 m2 n1 n2 m11 m12 m22 n11 n12 n22
  * (src/gengrid.f90:82-131, metric.dat) */
 int lns_upload_metrics3d(lns_ctx3d* ctx, const double* metrics);
+/* The sponge coefficients spg(nx,ny) and, for ispg > 4, spg2(nx,ny), as the
+ * host's sponge setup (src/sponge.f90) leaves them; needed before the first
+ * step when ispg != 0; invalidates the factored LHS. */
+int lns_upload_sponge3d(lns_ctx3d* ctx, const double* spg, const double* spg2);
 /* vm(5,nx,ny) on the host: builds the frozen operators (src/genmtrx.f90,
  * linear = 1, called as genmtrx(vm, kz, vm) at src/lns3d.f90:149) and the
  * time step (src/temporal.f90:12-130, called at src/impdrv3d.f90:54);

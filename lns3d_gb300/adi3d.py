@@ -45,11 +45,12 @@ class ImpDrv3D:
     (backward Euler for the context's first step), 3 midpoint
     (src/impdrv3d.f90:130-199).  res_compat: report the reference's running residual
     (src/resstat3d.f90:18 keeps totres between calls) instead of each
-    corrector's own.
+    corrector's own.  ispg, spg, spg2: the sponge (0 none, 1 spg, > 4
+    spg + spg2; src/lrhs3d.f90:220-240), spg and spg2 (nx, ny) arrays.
     """
 
     def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False,
-                 impl=1):
+                 impl=1, ispg=0, spg=None, spg2=None):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -57,13 +58,19 @@ class ImpDrv3D:
                        gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax,
                        dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
                        wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
-                       precision=precision, res_compat=1 if res_compat else 0, impl=impl)
+                       precision=precision, res_compat=1 if res_compat else 0, impl=impl, ispg=ispg)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")
         for k, name in enumerate(METRICS):
             m[:, :, k] = metrics[name]
         check(lib().lns_upload_metrics3d(self._ctx, ctypes.c_void_p(m.ctypes.data)), "lns_upload_metrics3d")
+        if ispg:
+            s1 = np.asfortranarray(spg, dtype=np.float64)
+            s2 = np.asfortranarray(spg2, dtype=np.float64) if spg2 is not None else None
+            check(lib().lns_upload_sponge3d(self._ctx, ctypes.c_void_p(s1.ctypes.data),
+                                            ctypes.c_void_p(s2.ctypes.data) if s2 is not None else None),
+                  "lns_upload_sponge3d")
         self.set_mean(vm)
 
     def set_mean(self, vm):

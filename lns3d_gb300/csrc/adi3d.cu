@@ -287,6 +287,9 @@ __device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, lo
   else if (a == 5 && b == 5) vk = 3;
   if (vk >= 0) re = re - (bk * d) * (dir == 1 ? o.V11 : o.V22)[vk * np + p];
   if (k == 3 && a == b) re = re + 1.0;
+  // sponge of the eta LHS (src/lhs2f3d.f90:207-224, src/lhsbt2f3d.f90:147-167;
+  // the xi LHS has calcd = true and no sponge)
+  if (dir == 2 && o.spg && k == 3 && a == b) re = re + g.alfa * d * o.spg[p];
   return cd{re, im};
 }
 
@@ -437,6 +440,15 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
       if (b == 3) {
         subi(r[1], a1 * c1b.x + a3 * c2b.x, a1 * c1b.y + a3 * c2b.y);
         subi(r[2], a2 * c1b.x + a4 * c2b.x, a2 * c1b.y + a4 * c2b.y);
+      }
+    }
+    // sponge, src/lrhs3d.f90:222-240: r = r + spg v on the operator's field
+    if (o.spg) {
+      const double sp = o.spg[p];
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const cd vm = v[m + 5 * p];
+        r[m] = cd{r[m].x + sp * vm.x, r[m].y + sp * vm.y};
       }
     }
     // rbe3D
@@ -671,6 +683,8 @@ struct lns_ctx3d {
   int res_cap = 0;
   int* status = nullptr;
   bool have_metrics = false, have_mean = false, factored = false;
+  bool have_sponge = false;   // ispg != 0: lns_upload_sponge3d called
+  double* spg = nullptr;      // spg, or spg + spg2 (ispg > 4)
   // time scheme (src/impdrv3d.f90:130-199): the previous-previous state
   // (impl 2), the averaged field (impl 3), steps taken, alfa of the factors
   cd *v2old = nullptr, *wavg = nullptr;
@@ -823,12 +837,12 @@ int sweep_x(lns_ctx3d* c, T* r, cudaStream_t st) {
   const long long pts = (long long)a.n * a.nsys, fill = (long long)(a.n - 3) * a.nsys;
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
-  ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
+  ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
   int rc = mark(c, st);
   ch::chain_fwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (!rc) rc = mark(c, st);
   ch::tail_kernel<T><<<a.nsys, 32 * ch::kTailWarps, 0, st>>>(a);
-  ch::fill_kernel<T><<<(unsigned)((fill + 255) / 256), 256, 0, st>>>(a);
+  ch::fill_kernel<T><<<(unsigned)ch::fill_blocks(fill), 256, 0, st>>>(a);
   if (!rc) rc = mark(c, st);
   ch::chain_bwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (rc) return rc;
@@ -844,7 +858,7 @@ int sweep_y(lns_ctx3d* c, T* r, cudaStream_t st) {
   const long long pts = (long long)a.n * a.nsys;
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
-  ch::scale_kernel<T><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(a);
+  ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
   int rc = mark(c, st);
   ch::chain_fwd_kernel<T, false><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (!rc) rc = mark(c, st);
@@ -988,6 +1002,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
     return fail3(LNS_ERR_ARG, "ctx3d_create: precision must be LNS_FP64 or LNS_MIXED");
   if (p->impl < 0 || p->impl > 3) return fail3(LNS_ERR_ARG, "ctx3d_create: impl must be 1, 2 or 3 (0 means 1)");
+  if (p->ispg < 0 || (p->ispg >= 2 && p->ispg <= 4))
+    return fail3(LNS_ERR_ARG, "ctx3d_create: ispg must be 0, 1 or > 4 (the inflow sponges 2-4 are not supported)");
   lns_ctx3d* c = new lns_ctx3d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);
@@ -1024,6 +1040,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   A(sizeof(cd) * 5 * np, &q); c->c1v = (cd*)q;
   if (p->impl == 2) { A(sizeof(cd) * 5 * np, &q); c->v2old = (cd*)q; }
   if (p->impl == 3) { A(sizeof(cd) * 5 * np, &q); c->wavg = (cd*)q; }
+  if (p->ispg != 0) { A(sizeof(double) * np, &q); c->spg = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
   A(sizeof(cd) * 125 * np, &c->matx);
@@ -1073,6 +1090,38 @@ int lns_ctx3d_destroy(lns_ctx3d* c) {
 
 size_t lns_ctx3d_bytes(const lns_ctx3d* c) { return c ? c->bytes : 0; }
 
+}  // extern "C"
+
+namespace {
+int need_data(const lns_ctx3d* c, const char* who) {
+  if (!c->have_mean) return fail3(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the mean flow first");
+  if (c->prm.ispg != 0 && !c->have_sponge)
+    return fail3(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
+  return LNS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int lns_upload_sponge3d(lns_ctx3d* c, const double* spg, const double* spg2) {
+  if (!c || !spg) return fail3(LNS_ERR_ARG, "upload_sponge3d: null argument");
+  if (c->prm.ispg == 0) return fail3(LNS_ERR_ARG, "upload_sponge3d: the context was created with ispg = 0");
+  if (c->prm.ispg > 4 && !spg2) return fail3(LNS_ERR_ARG, "upload_sponge3d: ispg > 4 needs spg2");
+  int rc = check_device(c);
+  if (rc) return rc;
+  // the double sponge enters the RHS and the LHS only as spg + spg2
+  // (src/lrhs3d.f90:232-240, src/lhs2f3d.f90:217-224): add once here
+  std::vector<double> h(spg, spg + c->np);
+  if (c->prm.ispg > 4)
+    for (long long k = 0; k < c->np; ++k) h[k] = spg[k] + spg2[k];
+  cudaError_t e = cudaMemcpy(c->spg, h.data(), sizeof(double) * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload sponge");
+  c->ops.spg = c->spg;
+  c->have_sponge = true;
+  c->factored = false;
+  return LNS_OK;
+}
+
 int lns_upload_metrics3d(lns_ctx3d* c, const double* metrics) {
   if (!c || !metrics) return fail3(LNS_ERR_ARG, "upload_metrics3d: null argument");
   int rc = check_device(c);
@@ -1113,7 +1162,7 @@ int lns_upload_mean3d(lns_ctx3d* c, const double* vm, double* cfl) {
 int lns_step3d_dev(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream) {
   if (!c || !v) return fail3(LNS_ERR_ARG, "step3d: null argument");
   if (nsteps < 0 || niter < 1) return fail3(LNS_ERR_ARG, "step3d: need nsteps >= 0 and niter >= 1");
-  if (!c->have_mean) return fail3(LNS_ERR_ARG, "step3d: upload the metrics and the mean flow first");
+  if (int rn = need_data(c, "step3d")) return rn;
   int rc = check_device(c);
   if (rc) return rc;
   return run_steps(c, (cd*)v, nsteps, niter, totres_dev, (cudaStream_t)stream);
@@ -1122,7 +1171,7 @@ int lns_step3d_dev(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, doubl
 int lns_step3d(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, double* totres) {
   if (!c || !v) return fail3(LNS_ERR_ARG, "step3d: null argument");
   if (nsteps < 0 || niter < 1) return fail3(LNS_ERR_ARG, "step3d: need nsteps >= 0 and niter >= 1");
-  if (!c->have_mean) return fail3(LNS_ERR_ARG, "step3d: upload the metrics and the mean flow first");
+  if (int rn = need_data(c, "step3d")) return rn;
   int rc = check_device(c);
   if (rc) return rc;
   if (totres && (rc = res_reserve(c, nsteps))) return rc;
@@ -1142,7 +1191,7 @@ int lns_step3d(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, double* t
 
 int lns_rhs3d_dev(lns_ctx3d* c, const double* v, const double* vold, double* r, double* totres_dev, void* stream) {
   if (!c || !v || !vold || !r) return fail3(LNS_ERR_ARG, "rhs3d: null argument");
-  if (!c->have_mean) return fail3(LNS_ERR_ARG, "rhs3d: upload the metrics and the mean flow first");
+  if (int rn = need_data(c, "rhs3d")) return rn;
   int rc = check_device(c);
   if (rc) return rc;
   return launch_rhs(c, (const cd*)v, (const cd*)v, (const cd*)vold, nullptr, (cd*)r, nullptr,
@@ -1153,7 +1202,7 @@ int lns_rhs3d_dev(lns_ctx3d* c, const double* v, const double* vold, double* r, 
 int lns_lhs3d_dev(lns_ctx3d* c, int32_t dir, double* mat, void* stream) {
   if (!c || !mat) return fail3(LNS_ERR_ARG, "lhs3d: null argument");
   if (dir != 1 && dir != 2) return fail3(LNS_ERR_ARG, "lhs3d: dir must be 1 or 2");
-  if (!c->have_mean) return fail3(LNS_ERR_ARG, "lhs3d: upload the metrics and the mean flow first");
+  if (int rn = need_data(c, "lhs3d")) return rn;
   int rc = check_device(c);
   if (rc) return rc;
   return launch_lhs<cd>(c, dir, (cd*)mat, (cudaStream_t)stream);
@@ -1190,7 +1239,7 @@ int lns_ctx3d_profile_read(lns_ctx3d* c, double* ms, int32_t* ncorr) {
 int lns_get_field3d(lns_ctx3d* c, int32_t which, double* out) {
   if (!c || !out) return fail3(LNS_ERR_ARG, "get_field3d: null argument");
   if (which < 0 || which > 8) return fail3(LNS_ERR_ARG, "get_field3d: which must be 0..8");
-  if (!c->have_mean) return fail3(LNS_ERR_ARG, "get_field3d: upload the metrics and the mean flow first");
+  if (int rn = need_data(c, "get_field3d")) return rn;
   int rc = check_device(c);
   if (rc) return rc;
   const long long np = c->np;
@@ -1285,11 +1334,11 @@ int build_tables(lns_batch3d* b) {
     for (int by = 0; by < g.ny; ++by)
       for (int bx = 0; bx < nbx; ++bx) tp.push_back(make_int4(p, bx, by, 0));
     const long long nxp = (long long)(g.nx - 1) * g.ny, nyp = (long long)g.ny * g.nx;
-    for (long long k = 0; k < (nxp + 255) / 256; ++k) tsx.push_back(make_int2(p, (int)k));
+    for (long long k = 0; k < lns::chain::scale_blocks(nxp); ++k) tsx.push_back(make_int2(p, (int)k));
     for (int k = 0; k < (g.ny + b->W - 1) / b->W; ++k) tfx.push_back(make_int2(p, k));
     for (int k = 0; k < g.ny; ++k) ttx.push_back(make_int2(p, k));
-    for (long long k = 0; k < ((long long)(g.nx - 1 - 3) * g.ny + 255) / 256; ++k) tlx.push_back(make_int2(p, (int)k));
-    for (long long k = 0; k < (nyp + 255) / 256; ++k) tsy.push_back(make_int2(p, (int)k));
+    for (long long k = 0; k < lns::chain::fill_blocks((long long)(g.nx - 1 - 3) * g.ny); ++k) tlx.push_back(make_int2(p, (int)k));
+    for (long long k = 0; k < lns::chain::scale_blocks(nyp); ++k) tsy.push_back(make_int2(p, (int)k));
     for (int k = 0; k < (g.nx + b->W - 1) / b->W; ++k) tfy.push_back(make_int2(p, k));
   }
   int rc = upload_table(b, te, &b->t_elem, &b->n_elem);
@@ -1478,6 +1527,8 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
       return fail3(LNS_ERR_ARG, "batch3d_create: every problem must use the same precision");
   for (int p = 0; p < nprob; ++p)
     if (params[p].impl > 1) return fail3(LNS_ERR_ARG, "batch3d_create: batches run impl = 1 (backward Euler)");
+  for (int p = 0; p < nprob; ++p)
+    if (params[p].ispg != 0) return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge (ispg = 0)");
   lns_batch3d* b = new lns_batch3d();
   b->P = nprob;
   b->mixed = params[0].precision == LNS_MIXED;
@@ -1846,6 +1897,7 @@ int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* 
   if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
   if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
   if (prm->impl > 1) return fail3(LNS_ERR_ARG, "server3d_submit: servers run impl = 1 (backward Euler)");
+  if (prm->ispg != 0) return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge (ispg = 0)");
   if (!(tol > 0.0) || max_steps < 1) return fail3(LNS_ERR_ARG, "server3d_submit: need tol > 0 and max_steps >= 1");
   if (ctx_bytes_for(*prm) > s->budget) return fail3(LNS_ERR_ARG, "server3d_submit: request larger than the budget");
   SrvReq* r = new SrvReq();

@@ -57,6 +57,9 @@ inline bool narrow_stencils(const Grid& g) {
 struct Ops {
   double *Ah, *Bh, *Dh, *Dhi, *V11, *V12, *V22, *AB, *dtl;
   long long np;
+  // the sponge coefficient (nx,ny): spg, or spg + spg2 for the double
+  // sponge; null without a sponge
+  const double* spg = nullptr;
 };
 
 struct Metrics {

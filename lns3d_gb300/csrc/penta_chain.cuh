@@ -254,30 +254,41 @@ __global__ void __launch_bounds__(32 * kPrepWarps) prep_fill_kernel(Args a) {
 }
 
 // ------------------------------------------------------------ the sweeps
-// s = D^-1 r in place, one thread per record of rows 1..n; bx is the block
-// index within the problem.
+// s = D^-1 r in place for the records of rows 1..n; bx is the block index
+// within the problem.  Five lanes per record (lane m forms s_m), six records
+// per warp: a load instruction of the warp reads six 5-entry column runs of
+// D instead of 32 scattered records, and each output keeps the order of
+// accumulation of a per-record loop.  The record's r is read by all five
+// lanes before any of them writes (the __syncwarp between).
+constexpr int kScaleRecsPerWarp = 6;
+__host__ __device__ constexpr long long scale_blocks(long long recs, int threads = 256) {
+  return (recs + (long long)(threads / 32) * kScaleRecsPerWarp - 1) / ((long long)(threads / 32) * kScaleRecsPerWarp);
+}
 template <typename T>
 __device__ __forceinline__ void scale_body(const Args& a, long long bx) {
-  const long long t = bx * blockDim.x + threadIdx.x;
-  if (t >= (long long)a.n * a.nsys) return;
-  int i, iv;
-  if (a.row_stride == 1) i = (int)(t % a.n) + 1, iv = (int)(t / a.n);
-  else iv = (int)(t % a.nsys), i = (int)(t / a.nsys) + 1;
-  const long long rc = rec_of(a, i, iv);
-  const T* D = reinterpret_cast<const T*>(a.chn) + 125 * rc;
-  T* r = reinterpret_cast<T*>(a.rhs) + 5 * rc;
-  T x[5], s[5];
+  const int lane = threadIdx.x % 32, mm = lane % 5;
+  const long long t = (bx * blockDim.x + threadIdx.x) / 32 * kScaleRecsPerWarp + lane / 5;
+  const bool on = lane < 5 * kScaleRecsPerWarp && t < (long long)a.n * a.nsys;
+  const T* D = nullptr;
+  T* r = nullptr;
+  T x[5];
+  if (on) {
+    int i, iv;
+    if (a.row_stride == 1) i = (int)(t % a.n) + 1, iv = (int)(t / a.n);
+    else iv = (int)(t % a.nsys), i = (int)(t / a.nsys) + 1;
+    const long long rc = rec_of(a, i, iv);
+    D = reinterpret_cast<const T*>(a.chn) + 125 * rc;
+    r = reinterpret_cast<T*>(a.rhs) + 5 * rc;
 #pragma unroll
-  for (int k = 0; k < 5; ++k) x[k] = r[k];
-#pragma unroll
-  for (int mm = 0; mm < 5; ++mm) {
+    for (int k = 0; k < 5; ++k) x[k] = r[k];
+  }
+  __syncwarp();
+  if (on) {
     T acc = zero<T>();
 #pragma unroll
     for (int k = 0; k < 5; ++k) acc = fmac(acc, D[mm + 5 * k], x[k]);
-    s[mm] = acc;
+    r[mm] = acc;
   }
-#pragma unroll
-  for (int k = 0; k < 5; ++k) r[k] = s[k];
 }
 template <typename T>
 __global__ void scale_kernel(Args a) { scale_body<T>(a, blockIdx.x); }
@@ -716,6 +727,9 @@ __device__ __forceinline__ void tail_body(const Args& a, int iv) {
   const T* gchn = reinterpret_cast<const T*>(a.chn);
   const T* gp2 = reinterpret_cast<const T*>(a.fillK);
   T acc1 = zero<T>(), acc0 = zero<T>();
+  // unrolled so that several rows' loads are in flight per warp (the sums
+  // keep their order)
+#pragma unroll 4
   for (int c = 1 + warp; c <= n - 3; c += kTailWarps) {
     const long long rc = rec_of(a, c, iv);
     const T y = grhs[5 * rc + qq];
@@ -766,10 +780,17 @@ __global__ void __launch_bounds__(32 * kTailWarps) tail_batch_kernel(const Args*
 }
 
 // Periodic lines: c_i = yh_i - E1_i x_{n-1} - E0_i x_n for rows 1..n-3, one
-// thread per record.
+// thread per entry of c_i (thread 5 t + m forms entry m of record t), so a
+// warp's loads cover a few consecutive records' E runs; each entry keeps
+// the order of accumulation of a per-record loop (E1 columns, then E0).
+__host__ __device__ constexpr long long fill_blocks(long long recs, int threads = 256) {
+  return (5 * recs + threads - 1) / threads;
+}
 template <typename T>
 __device__ __forceinline__ void fill_body(const Args& a, long long bx) {
-  const long long t = bx * blockDim.x + threadIdx.x;
+  const long long t5 = bx * blockDim.x + threadIdx.x;
+  const long long t = t5 / 5;
+  const int mm = (int)(t5 - 5 * t);
   const int rows = a.n - 3;
   if (t >= (long long)rows * a.nsys) return;
   int i, iv;
@@ -777,41 +798,15 @@ __device__ __forceinline__ void fill_body(const Args& a, long long bx) {
   else iv = (int)(t % a.nsys), i = (int)(t / a.nsys) + 1;
   T* grhs = reinterpret_cast<T*>(a.rhs);
   const long long rc = rec_of(a, i, iv);
-  const T* E = reinterpret_cast<const T*>(a.fillE) + 50 * rc;
+  const T* E = reinterpret_cast<const T*>(a.fillE) + 50 * rc + mm;
   const T* xa = grhs + 5 * rec_of(a, a.n - 1, iv);
   const T* xb = grhs + 5 * rec_of(a, a.n, iv);
-  T xn1[5], xn0[5];
+  T acc = grhs[5 * rc + mm];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) xn1[k] = xa[k], xn0[k] = xb[k];
-  T* r = grhs + 5 * rc;
-  if constexpr (std::is_same<T, cf>::value) {
-    // FP32 records are 400 B and 16-byte aligned: read them as 25 16-byte
-    // loads, entry e = m + 5 q (+ 25 for E0) in storage order, which is also
-    // each output's order of accumulation below.
-    const float4* E4 = reinterpret_cast<const float4*>(E);
-    T acc[5];
+  for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[5 * k], xa[k]);
 #pragma unroll
-    for (int mm = 0; mm < 5; ++mm) acc[mm] = r[mm];
-#pragma unroll
-    for (int k = 0; k < 25; ++k) {
-      const float4 w = E4[k];
-      const int e0 = 2 * k, e1 = 2 * k + 1;
-      acc[e0 % 5] = fmsc(acc[e0 % 5], cf{w.x, w.y}, e0 < 25 ? xn1[e0 / 5] : xn0[(e0 - 25) / 5]);
-      acc[e1 % 5] = fmsc(acc[e1 % 5], cf{w.z, w.w}, e1 < 25 ? xn1[e1 / 5] : xn0[(e1 - 25) / 5]);
-    }
-#pragma unroll
-    for (int mm = 0; mm < 5; ++mm) r[mm] = acc[mm];
-  } else {
-#pragma unroll
-    for (int mm = 0; mm < 5; ++mm) {
-      T acc = r[mm];
-#pragma unroll
-      for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[mm + 5 * k], xn1[k]);
-#pragma unroll
-      for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[25 + mm + 5 * k], xn0[k]);
-      r[mm] = acc;
-    }
-  }
+  for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[25 + 5 * k], xb[k]);
+  grhs[5 * rc + mm] = acc;
 }
 
 template <typename T>

@@ -17,7 +17,7 @@ class A3Grid(ctypes.Structure):
                 ("loctime", I), ("xper", I), ("yper", I), ("navier", I), ("wall", I), ("wallt", I), ("top", I),
                 ("optx", I), ("opty", I)] + [(k, P) for k in
                                              ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")] + \
-        [("resacc", P)]
+        [("resacc", P), ("ispg", I), ("spg", P), ("spg2", P)]
 
 
 class A3Ops(ctypes.Structure):
@@ -56,7 +56,10 @@ def ptr(a):
 class Oracle3D:
     """Holds the oracle's grid struct, operators and factor arrays for one case."""
 
-    def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, res_compat=False):
+    def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, res_compat=False, ispg=0, spg=None,
+                 spg2=None):
+        """ispg, spg, spg2: the sponge (0 none, 1 spg, > 4 spg + spg2), spg
+        and spg2 (nx, ny) as the reference's sponge setup leaves them."""
         self.L = _lib(lib)
         self.case = case
         p = case["params"]
@@ -72,6 +75,11 @@ class Oracle3D:
         if res_compat:
             self.g.resacc = ctypes.cast(ctypes.byref(self.resacc), P).value
         nx, ny = self.nx, self.ny
+        if ispg:
+            self.spg = np.asfortranarray(spg, dtype=np.float64).reshape((nx, ny), order="F")
+            self.spg2 = np.asfortranarray(spg2 if spg2 is not None else np.zeros((nx, ny)),
+                                          dtype=np.float64).reshape((nx, ny), order="F")
+            self.g.ispg, self.g.spg, self.g.spg2 = ispg, ptr(self.spg).value, ptr(self.spg2).value
         self.ops = {k: np.zeros((5, 5, nx, ny), order="F") for k in ("Ah", "Bh", "Dh", "Dhi")}
         self.ops.update({k: np.zeros((6, nx, ny), order="F") for k in ("Vh11", "Vh12", "Vh22", "ABhi")})
         self.o = A3Ops(**{k: ptr(v).value for k, v in self.ops.items()})

@@ -438,6 +438,7 @@ double a3_set_time_step(const A3Grid* g, const double* vl, double* dtl) {
 int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
   const int nx = g->nx, ny = g->ny;
   const long n10 = 10L * nx * ny;
+  if (g->ispg >= 2 && g->ispg <= 4) return 1; /* inflow sponges and cspg_it: not restated */
   double* c1v = (double*)calloc(n10, sizeof(double));
   double* c2v = (double*)calloc(n10, sizeof(double));
   double* c11v = (double*)calloc(n10, sizeof(double));
@@ -517,6 +518,12 @@ int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
 #undef Z2
 #undef ZV
 #undef RR
+      }
+      /* sponge, src/lrhs3d.f90:222-240: rl = rl + spg vl (ispg 1) or
+         rl = rl + (spg + spg2) vl (ispg > 4) */
+      if (g->ispg == 1 || g->ispg > 4) {
+        const double sp = g->ispg == 1 ? g->spg[p] : g->spg[p] + g->spg2[p];
+        for (int k = 0; k < 10; ++k) rl[k + 10 * p] = rl[k + 10 * p] + sp * vl[k + 10 * p];
       }
 #undef C1
 #undef C2
@@ -675,6 +682,13 @@ static void lhs_row(const A3Grid* g, const A3Ops* o, const double* dtl, int dir,
     MRE(k, 5, 5, p) = MRE(k, 5, 5, p) - w * V[3];
   }
   for (int a = 1; a <= 5; ++a) MRE(3, a, a, p) = MRE(3, a, a, p) + one;
+  /* sponge of the eta LHS (calcd false there; src/lhs2f3d.f90:207-224,
+     src/lhsbt2f3d.f90:147-167): mat(3,a,a) + alfa dtl spg, or
+     alfa dtl (spg + spg2) for ispg >= 2 */
+  if (!calcd && g->ispg >= 1) {
+    const double sp = g->ispg == 1 ? g->spg[p] : g->spg[p] + g->spg2[p];
+    for (int a = 1; a <= 5; ++a) MRE(3, a, a, p) = MRE(3, a, a, p) + alfa * d * sp;
+  }
 }
 
 /* src/lhs1f3d.f90 / src/lhs2f3d.f90, then the boundary rows of

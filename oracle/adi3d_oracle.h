@@ -46,6 +46,10 @@ typedef struct {
      src/resstat3d.f90:18): the sum starts from *resacc, and the result is
      stored back into it. */
   double* resacc;
+  /* sponge (src/lrhs3d.f90:220-240, src/lhs2f3d.f90:207-224): ispg 0 none,
+     1 spg, > 4 spg + spg2 (2..4 not restated); spg, spg2 (nx,ny) */
+  int ispg;
+  const double *spg, *spg2;
 } A3Grid;
 
 /* Frozen operators of the linear step (outputs of genmtrx(vm, kz, vm)). */

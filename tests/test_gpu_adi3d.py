@@ -302,3 +302,93 @@ def test_time_schemes_differ_and_reject_bad_impl(cuda, small):
     assert rel(out[1], out[2]) > 1e-8 and rel(out[1], out[3]) > 1e-8
     with pytest.raises(LnsError):
         ImpDrv3D(case["params"], case["metrics"], case["vm"], impl=4)
+
+
+@pytest.mark.parametrize("ispg", [1, 5])
+def test_sponge_matches_oracle(cuda, ispg):
+    """The sponge (ispg 1: spg; ispg 5: spg + spg2) in the RHS
+    (src/lrhs3d.f90:220-240) and the eta LHS (src/lhs2f3d.f90:207-224,
+    src/lhsbt2f3d.f90:147-167): RHS, both LHS and steps against the oracle."""
+    import ctypes
+
+    import torch
+    from adi3dcase import _lib, ptr, sponge
+
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=40, ny=33, seed=8)
+    spg, spg2 = sponge(40, 33, amp=1.0)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1, ispg=ispg, spg=spg, spg2=spg2)
+    mk = lambda: ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, ispg=ispg,
+                          spg=spg, spg2=spg2)
+    drv = mk()
+    nx, ny = 40, 33
+    for direction in (1, 2):
+        mat = torch.zeros(125 * nx * ny, dtype=torch.complex128, device="cuda")
+        drv.lhs(direction, mat)
+        torch.cuda.synchronize()
+        got = mat.cpu().numpy().reshape((5, 5, 5, nx, ny), order="F")
+        assert rel(got, orc.lhs(direction)) < OPS_TOL, direction
+    rng = np.random.default_rng(12)
+    shape = (5, nx, ny)
+    v = np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    vold = np.asfortranarray(v + 1e-3 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    L = _lib()
+    r = orc.lrhs(v)
+    L.a3_rbe(ctypes.byref(orc.g), ptr(r), ptr(v), ptr(vold), ptr(orc.dtl))
+    L.a3_rhsbc(ctypes.byref(orc.g), ptr(r), ptr(v))
+    dev = lambda a: torch.from_numpy(a.ravel(order="F")).cuda()
+    dv, dvo = dev(v), dev(vold)
+    dr = torch.zeros_like(dv)
+    drv.rhs(dv, dvo, dr, torch.zeros(1, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    assert rel(dr.cpu().numpy().reshape(shape, order="F"), r) < RHS_TOL
+    drv = mk()
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    for s in range(4):
+        res_ref = orc.step(v_ref)
+        res_gpu = drv.step(v_gpu, nsteps=1)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+
+
+def test_sponge_needs_upload(cuda):
+    """ispg != 0: stepping before lns_upload_sponge3d is an argument error;
+    ispg > 4 needs spg2."""
+    import ctypes
+
+    from lns3d_gb300._lib import Params3D, lib
+    from lns3d_gb300.adi3d import METRICS
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 16, 12
+    case = shear_layer(nx=nx, ny=ny, seed=1)
+    p = case["params"]
+    L = lib()
+    P = lambda a: ctypes.c_void_p(a.ctypes.data)
+    m = np.empty((nx, ny, 10), order="F")
+    for k, name in enumerate(METRICS):
+        m[:, :, k] = case["metrics"][name]
+    vm = np.asfortranarray(case["vm"])
+    v = np.zeros(10 * nx * ny)
+    sp = np.full(nx * ny, 0.1)
+    for ispg in (1, 5):
+        prm = Params3D(nx=nx, ny=ny, dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
+                       gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=1.0, cflmax=1.0, dtmax=1e30,
+                       loctime=1, xper=1, yper=0, navier=1, wall=p["wall"], wallt=p["wallt"], top=0, optx=-1,
+                       opty=-1, ispg=ispg)
+        ctx = ctypes.c_void_p()
+        assert L.lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(ctx)) == 0
+        try:
+            assert L.lns_upload_metrics3d(ctx, P(m)) == 0
+            assert L.lns_upload_mean3d(ctx, P(vm), None) == 0
+            assert L.lns_step3d(ctx, P(v), 1, 1, None) == 1
+            assert b"sponge" in L.lns_last_error()
+            if ispg == 5:
+                assert L.lns_upload_sponge3d(ctx, P(sp), None) == 1
+            assert L.lns_upload_sponge3d(ctx, P(sp), P(sp)) == 0
+            assert L.lns_step3d(ctx, P(v), 1, 1, None) == 0
+        finally:
+            L.lns_ctx3d_destroy(ctx)

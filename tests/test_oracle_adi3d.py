@@ -136,3 +136,53 @@ def test_time_scheme_steps_are_consistent():
     v0 = np.zeros_like(case["v"], order="F")
     z.step_impl(v0, 3)
     assert np.abs(v0).max() == 0.0
+
+
+@pytest.mark.parametrize("ispg", [1, 5])
+def test_sponge_terms_known_answer(ispg):
+    """The sponge (src/lrhs3d.f90:220-240; eta LHS src/lhs2f3d.f90:207-224
+    and src/lhsbt2f3d.f90:147-167): the RHS gains sp v and the eta LHS
+    alfa dtl sp on the diagonal of every row the boundary conditions leave,
+    sp = spg (ispg 1) or spg + spg2 (ispg > 4); the xi LHS is unchanged."""
+    from adi3dcase import sponge
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=24, ny=20, seed=1)
+    spg, spg2 = sponge(24, 20)
+    plain = Oracle3D(case, cflmax=20.0, loctime=1)
+    o = Oracle3D(case, cflmax=20.0, loctime=1, ispg=ispg, spg=spg, spg2=spg2)
+    sp = spg if ispg == 1 else spg + spg2
+    rng = np.random.default_rng(2)
+    v = np.asfortranarray(rng.standard_normal((5, 24, 20)) + 1j * rng.standard_normal((5, 24, 20)))
+    assert np.array_equal(o.lrhs(v), plain.lrhs(v) + sp[None] * v)
+    assert np.array_equal(o.lhs(1), plain.lhs(1))
+    m_s, m_p = o.lhs(2), plain.lhs(2)
+    d = m_s - m_p
+    want = case["params"]["alfa"] * o.dtl * sp
+    for a in range(5):
+        # rows 2..ny-1 keep every block row; the wall row keeps its continuity
+        # row only when wall = 2 (the case's wall 1 replaces it)
+        # (m + x) - m recovers x to the rounding of m's scale
+        tol = 4e-16 * (np.abs(m_p[2, a, a, :, 1:-1]) + np.abs(want[:, 1:-1]))
+        assert (np.abs(d[2, a, a, :, 1:-1] - want[:, 1:-1]) <= tol).all()
+    mask = np.ones(d.shape, bool)
+    for a in range(5):
+        mask[2, a, a, :, 1:-1] = False
+    assert not d[mask].any()
+
+
+def test_sponge_damps_the_perturbation():
+    from adi3dcase import sponge
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=24, ny=20, seed=4)
+    spg, spg2 = sponge(24, 20, amp=2.0)
+    norms = []
+    for kw in ({}, dict(ispg=1, spg=spg, spg2=spg2), dict(ispg=5, spg=spg, spg2=spg2)):
+        o = Oracle3D(case, cflmax=20.0, loctime=1, **kw)
+        v = case["v"].copy(order="F")
+        for _ in range(6):
+            o.step(v)
+        assert np.isfinite(v).all()
+        norms.append(np.linalg.norm(v[:, :, 12:]))
+    assert norms[1] < norms[0] and norms[2] < norms[0]
