@@ -17,7 +17,7 @@ class A3Grid(ctypes.Structure):
                 ("loctime", I), ("xper", I), ("yper", I), ("navier", I), ("wall", I), ("wallt", I), ("top", I),
                 ("optx", I), ("opty", I)] + [(k, P) for k in
                                              ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")] + \
-        [("resacc", P), ("ispg", I), ("spg", P), ("spg2", P)]
+        [("resacc", P), ("ispg", I), ("spg", P), ("spg2", P), ("eps_e", D), ("buff", P)]
 
 
 class A3Ops(ctypes.Structure):
@@ -57,9 +57,11 @@ class Oracle3D:
     """Holds the oracle's grid struct, operators and factor arrays for one case."""
 
     def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, res_compat=False, ispg=0, spg=None,
-                 spg2=None):
+                 spg2=None, eps_e=0.0, buff=None):
         """ispg, spg, spg2: the sponge (0 none, 1 spg, > 4 spg + spg2), spg
-        and spg2 (nx, ny) as the reference's sponge setup leaves them."""
+        and spg2 (nx, ny) as the reference's sponge setup leaves them.
+        eps_e, buff: the explicit smoother and implicit damping, buff (nx, ny)
+        (ones, the reference's ibuff = 0, when None)."""
         self.L = _lib(lib)
         self.case = case
         p = case["params"]
@@ -80,6 +82,10 @@ class Oracle3D:
             self.spg2 = np.asfortranarray(spg2 if spg2 is not None else np.zeros((nx, ny)),
                                           dtype=np.float64).reshape((nx, ny), order="F")
             self.g.ispg, self.g.spg, self.g.spg2 = ispg, ptr(self.spg).value, ptr(self.spg2).value
+        if eps_e:
+            self.buff = np.asfortranarray(buff if buff is not None else np.ones((nx, ny)),
+                                          dtype=np.float64).reshape((nx, ny), order="F")
+            self.g.eps_e, self.g.buff = eps_e, ptr(self.buff).value
         self.ops = {k: np.zeros((5, 5, nx, ny), order="F") for k in ("Ah", "Bh", "Dh", "Dhi")}
         self.ops.update({k: np.zeros((6, nx, ny), order="F") for k in ("Vh11", "Vh12", "Vh22", "ABhi")})
         self.o = A3Ops(**{k: ptr(v).value for k, v in self.ops.items()})

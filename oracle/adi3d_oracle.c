@@ -435,6 +435,38 @@ double a3_set_time_step(const A3Grid* g, const double* vl, double* dtl) {
 #define CIM(a, k, g, i, j) (a)[2 * ((long)(k) + 5 * IX(g, i, j)) + 1]
 
 /* src/lrhs3d.f90:33-218 (ispg 0, eps_e 0) */
+/* smoother3D, src/smoother3d.f90:1-200 without symmetry planes (lsym and
+   rsym false): rl += eps_e buff D(vl), the eta pass first (rows 2 and ny-1
+   second order, 3 and ny-2 fourth order, 4..ny-3 sixth order), then the xi
+   pass with the same pattern over i (no periodic wrap, as the reference). */
+static void a3_smoother(const A3Grid* g, double* rl, const double* vl) {
+  const int nx = g->nx, ny = g->ny;
+  const double fa1 = -1.666666666666667E-01, fa2 = 2.000000000000000E+00, fa3 = -6.500000000000000E+00,
+               fa4 = 9.333333333333333E+00, fa5 = -6.500000000000000E+00, fa6 = 2.000000000000000E+00,
+               fa7 = -1.666666666666667E-01; /* src/stencil.f90:145-151 */
+  for (int pass = 0; pass < 2; ++pass) {
+    const int n = pass == 0 ? ny : nx;
+    OMP_FOR
+    for (int l = 1; l <= (pass == 0 ? nx : ny); ++l)
+      for (int c = 2; c <= n - 1; ++c) {
+        const int i = pass == 0 ? l : c, j = pass == 0 ? c : l;
+        const long st = pass == 0 ? 10L * nx : 10L;
+        const long p = IX(g, i, j);
+        const double eb = g->eps_e * g->buff[p];
+        for (int k = 0; k < 10; ++k) {
+          const double* V = vl + k + 10 * p;
+#define VS(d) V[(long)(d) * st]
+          double s;
+          if (c == 2 || c == n - 1) s = -1.0 * VS(-1) + 2.0 * VS(0) - 1.0 * VS(1);
+          else if (c == 3 || c == n - 2) s = VS(-2) - 4.0 * VS(-1) + 6.0 * VS(0) - 4.0 * VS(1) + 1.0 * VS(2);
+          else s = fa1 * VS(-3) + fa2 * VS(-2) + fa3 * VS(-1) + fa4 * VS(0) + fa5 * VS(1) + fa6 * VS(2) + fa7 * VS(3);
+#undef VS
+          rl[k + 10 * p] = rl[k + 10 * p] + eb * s;
+        }
+      }
+  }
+}
+
 int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
   const int nx = g->nx, ny = g->ny;
   const long n10 = 10L * nx * ny;
@@ -531,6 +563,7 @@ int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
 #undef R
     }
   free(c1v); free(c2v); free(c11v); free(c12v); free(c22v);
+  if (g->eps_e != zero) a3_smoother(g, rl, vl); /* src/lrhs3d.f90:294 */
   return 0;
 }
 
@@ -635,7 +668,7 @@ void a3_itrbc(const A3Grid* g, double* vl) {
    (src/lhsbt2f3d.f90:44-50) instead of adding the D terms afterwards
    (src/lhs1f3d.f90:60-124). */
 static void lhs_row(const A3Grid* g, const A3Ops* o, const double* dtl, int dir, long p, const double ak[5],
-                    const double bk[5], int combined, double* mat) {
+                    const double bk[5], int combined, int damp, double* mat) {
   const double* X = (dir == 1 ? o->Ah : o->Bh) + 25 * p;
   const double* V = (dir == 1 ? o->Vh11 : o->Vh22) + 6 * p;
   const double* AB = o->ABhi + 6 * p;
@@ -682,6 +715,20 @@ static void lhs_row(const A3Grid* g, const A3Ops* o, const double* dtl, int dir,
     MRE(k, 5, 5, p) = MRE(k, 5, 5, p) - w * V[3];
   }
   for (int a = 1; a <= 5; ++a) MRE(3, a, a, p) = MRE(3, a, a, p) + one;
+  /* implicit damping: damp 0 the fourth-order band fb1..fb5
+     (src/lhs1f3d.f90:168-200, src/lhs2f3d.f90:171-203), 2 the second-order
+     rows 2 and ny-1 of lhsbt2f3D in slots 2..4 (src/lhsbt2f3d.f90:277-298),
+     1 none (rows 1 and ny) */
+  if (g->eps_e != zero && damp != 1) {
+    const double fb[5] = {1.000000000000000E+00, -4.000000000000000E+00, 6.000000000000000E+00,
+                          -4.000000000000000E+00, 1.000000000000000E+00}; /* src/stencil.f90:137-141 */
+    const double sb[5] = {zero, -one, two, -one, zero};
+    for (int k = 1; k <= 5; ++k) {
+      if (damp == 2 && (k == 1 || k == 5)) continue;
+      const double c = damp == 0 ? fb[k - 1] : sb[k - 1];
+      for (int a = 1; a <= 5; ++a) MRE(k, a, a, p) = MRE(k, a, a, p) + alfa * d * g->eps_e * g->buff[p] * c;
+    }
+  }
   /* sponge of the eta LHS (calcd false there; src/lhs2f3d.f90:207-224,
      src/lhsbt2f3d.f90:147-167): mat(3,a,a) + alfa dtl spg, or
      alfa dtl (spg + spg2) for ispg >= 2 */
@@ -705,7 +752,7 @@ int a3_lhs(const A3Grid* g, const A3Ops* o, const double* dtl, int dir, double* 
   for (int k = 0; k < 5; ++k) ak[k] = alfa * gi[k] / h, bk[k] = alfa * di[k] / (h * h);
   OMP_FOR
   for (int j = 1; j <= ny; ++j)
-    for (int i = 1; i <= nx; ++i) lhs_row(g, o, dtl, dir, IX(g, i, j), ak, bk, 0, mat);
+    for (int i = 1; i <= nx; ++i) lhs_row(g, o, dtl, dir, IX(g, i, j), ak, bk, 0, 0, mat);
   if (!per) {
     if (dir == 1) return 1; /* non-periodic xi sweep: not supported by this oracle */
     /* boundary rows j = 1, 2, ny-1, ny (src/lhsbt2f3d.f90:36-600) */
@@ -715,13 +762,13 @@ int a3_lhs(const A3Grid* g, const A3Ops* o, const double* dtl, int dir, double* 
     const int sN1[5] = {4, 3, 2, 1, 5}, sN[5] = {3, 2, 1, 5, 4}; /* slot of coefficient t (1..5) */
     for (int i = 1; i <= nx; ++i) {
       for (int t = 0; t < 5; ++t) ak[s1[t] - 1] = alfa * g1[t] * hinv, bk[s1[t] - 1] = alfa * d1[t] * hsinv;
-      lhs_row(g, o, dtl, dir, IX(g, i, 1), ak, bk, 1, mat);
+      lhs_row(g, o, dtl, dir, IX(g, i, 1), ak, bk, 1, 1, mat);
       for (int t = 0; t < 5; ++t) ak[s2[t] - 1] = alfa * g2[t] * hinv, bk[s2[t] - 1] = alfa * d2[t] * hsinv;
-      lhs_row(g, o, dtl, dir, IX(g, i, 2), ak, bk, 1, mat);
+      lhs_row(g, o, dtl, dir, IX(g, i, 2), ak, bk, 1, 2, mat);
       for (int t = 0; t < 5; ++t) ak[sN1[t] - 1] = -(alfa * g2[t] * hinv), bk[sN1[t] - 1] = alfa * d2[t] * hsinv;
-      lhs_row(g, o, dtl, dir, IX(g, i, ny - 1), ak, bk, 1, mat);
+      lhs_row(g, o, dtl, dir, IX(g, i, ny - 1), ak, bk, 1, 2, mat);
       for (int t = 0; t < 5; ++t) ak[sN[t] - 1] = -(alfa * g1[t] * hinv), bk[sN[t] - 1] = alfa * d1[t] * hsinv;
-      lhs_row(g, o, dtl, dir, IX(g, i, ny), ak, bk, 1, mat);
+      lhs_row(g, o, dtl, dir, IX(g, i, ny), ak, bk, 1, 1, mat);
     }
   }
   /* boundary conditions of the wall (j = 1) and top (j = ny) rows */

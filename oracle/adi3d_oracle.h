@@ -50,6 +50,11 @@ typedef struct {
      1 spg, > 4 spg + spg2 (2..4 not restated); spg, spg2 (nx,ny) */
   int ispg;
   const double *spg, *spg2;
+  /* explicit smoother and implicit damping (src/smoother3d.f90,
+     src/lhs1f3d.f90:168-200, src/lhs2f3d.f90:171-203, src/lhsbt2f3d.f90:
+     277-298, 431-452): eps_e and buff(nx,ny); eps_e = 0 turns both off */
+  double eps_e;
+  const double* buff;
 } A3Grid;
 
 /* Frozen operators of the linear step (outputs of genmtrx(vm, kz, vm)). */

@@ -186,3 +186,66 @@ def test_sponge_damps_the_perturbation():
         assert np.isfinite(v).all()
         norms.append(np.linalg.norm(v[:, :, 12:]))
     assert norms[1] < norms[0] and norms[2] < norms[0]
+
+
+def test_smoother_and_damping_known_answer():
+    """The explicit smoother (src/smoother3d.f90, added at the end of
+    lrhs3D) and the implicit damping of the LHS (src/lhs1f3d.f90:168-200,
+    src/lhs2f3d.f90:171-203, src/lhsbt2f3d.f90:277-298): an impulse at an
+    interior point spreads with the sixth-order coefficients fa1..fa7 along
+    both directions, scaled by eps_e buff; the LHS gains alfa dtl eps_e buff
+    times fb1..fb5 on the diagonals of the band, and (-1, 2, -1) in slots 2..4
+    of the eta rows 2 and ny-1."""
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 24, 20
+    case = shear_layer(nx=nx, ny=ny, seed=1)
+    rng = np.random.default_rng(5)
+    buff = np.asfortranarray(0.5 + rng.uniform(size=(nx, ny)))
+    eps = 0.02
+    plain = Oracle3D(case, cflmax=20.0, loctime=1)
+    o = Oracle3D(case, cflmax=20.0, loctime=1, eps_e=eps, buff=buff)
+    v = np.zeros((5, nx, ny), np.complex128, order="F")
+    i0, j0 = 10, 9          # 0-based interior point
+    v[2, i0, j0] = 1.0 + 2.0j
+    d = o.lrhs(v) - plain.lrhs(v)
+    fa = [-1.666666666666667E-01, 2.0, -6.5, 9.333333333333333, -6.5, 2.0, -1.666666666666667E-01]
+    want = np.zeros_like(d)
+    for s in range(-3, 4):
+        want[2, i0, j0 - s] += eps * buff[i0, j0 - s] * fa[3 + s] * v[2, i0, j0]
+        want[2, i0 - s, j0] += eps * buff[i0 - s, j0] * fa[3 + s] * v[2, i0, j0]
+    scale = np.abs(plain.lrhs(v)).max()
+    assert np.abs(d - want).max() <= 1e-15 * scale
+    assert not d[[0, 1, 3, 4]].any()
+    alfa = case["params"]["alfa"]
+    fb = [1.0, -4.0, 6.0, -4.0, 1.0]
+    w = alfa * o.dtl * eps * buff
+    for direction in (1, 2):
+        dm = o.lhs(direction) - plain.lhs(direction)
+        scale = np.abs(plain.lhs(direction)).max()
+        rows = range(1, ny - 1) if direction == 1 else range(2, ny - 2)
+        for k in range(5):
+            for a in range(5):
+                got = dm[k, a, a][:, list(rows)]
+                assert np.abs(got - w[:, list(rows)] * fb[k]).max() <= 4e-16 * scale
+        if direction == 2:
+            for jj in (1, ny - 2):
+                for k, c in ((1, -1.0), (2, 2.0), (3, -1.0)):
+                    for a in range(5):
+                        assert np.abs(dm[k, a, a, :, jj] - w[:, jj] * c).max() <= 4e-16 * scale
+                assert not dm[0, :, :, :, jj].any() and not dm[4, :, :, :, jj].any()
+            assert not dm[:, :, :, :, 0].any() and not dm[:, :, :, :, ny - 1].any()
+        off = dm.copy()
+        for a in range(5):
+            off[:, a, a] = 0.0
+        assert not off.any()
+
+
+def test_smoother_keeps_steps_stable():
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=24, ny=20, seed=4)
+    o = Oracle3D(case, cflmax=20.0, loctime=1, eps_e=0.01)
+    v = case["v"].copy(order="F")
+    res = [o.step(v) for _ in range(6)]
+    assert np.isfinite(v).all() and all(np.isfinite(res))
