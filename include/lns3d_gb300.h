@@ -331,6 +331,13 @@ typedef struct {
                                 with spg + spg2.  The inflow sponges 2, 3 and the
                                 iterated sponge 4 are not supported.  Batches and servers
                                 take 0. */
+  double eps_e;              /* explicit smoother (src/smoother3d.f90, at the end of lrhs3D)
+                                and implicit damping of both LHS (src/lhs1f3d.f90:168-200,
+                                src/lhs2f3d.f90:171-203, src/lhsbt2f3d.f90:277-298,
+                                431-452) with the weight buff(nx,ny): ones (the reference's
+                                ibuff = 0) until lns_upload_buffer3d.  0 turns both off.
+                                Symmetry planes (lsym, rsym) are not supported.  Batches and
+                                servers take 0. */
 } lns_params3d;
 
 typedef struct lns_ctx3d lns_ctx3d;
@@ -348,6 +355,9 @@ int lns_upload_metrics3d(lns_ctx3d* ctx, const double* metrics);
  * host's sponge setup (src/sponge.f90) leaves them; needed before the first
  * step when ispg != 0; invalidates the factored LHS. */
 int lns_upload_sponge3d(lns_ctx3d* ctx, const double* spg, const double* spg2);
+/* The smoother weight buff(nx,ny) of the host's buffer setup (src/buffer.f90,
+ * ibuff > 0); only for eps_e != 0; invalidates the factored LHS. */
+int lns_upload_buffer3d(lns_ctx3d* ctx, const double* buff);
 /* vm(5,nx,ny) on the host: builds the frozen operators (src/genmtrx.f90,
  * linear = 1, called as genmtrx(vm, kz, vm) at src/lns3d.f90:149) and the
  * time step (src/temporal.f90:12-130, called at src/impdrv3d.f90:54);

@@ -66,6 +66,7 @@ SIGNATURES = {
     "lns_ctx3d_destroy": [P],
     "lns_upload_metrics3d": [P, DP],
     "lns_upload_sponge3d": [P, DP, DP],
+    "lns_upload_buffer3d": [P, DP],
     "lns_upload_mean3d": [P, DP, DP],
     "lns_step3d": [P, DP, I32, I32, DP],
     "lns_step3d_dev": [P, DP, I32, I32, DP, P],
@@ -117,7 +118,7 @@ class Params3D(ctypes.Structure):
                 ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double), ("dtmax", ctypes.c_double),
                 ("loctime", I32), ("xper", I32), ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32),
                 ("top", I32), ("optx", I32), ("opty", I32), ("precision", I32), ("res_compat", I32),
-                ("impl", I32), ("ispg", I32)]
+                ("impl", I32), ("ispg", I32), ("eps_e", ctypes.c_double)]
 
 
 def lib():

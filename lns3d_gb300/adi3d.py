@@ -47,10 +47,12 @@ class ImpDrv3D:
     (src/resstat3d.f90:18 keeps totres between calls) instead of each
     corrector's own.  ispg, spg, spg2: the sponge (0 none, 1 spg, > 4
     spg + spg2; src/lrhs3d.f90:220-240), spg and spg2 (nx, ny) arrays.
+    eps_e, buff: explicit smoother and implicit damping (src/smoother3d.f90),
+    buff (nx, ny) or None for the reference's default of ones.
     """
 
     def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False,
-                 impl=1, ispg=0, spg=None, spg2=None):
+                 impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -58,7 +60,8 @@ class ImpDrv3D:
                        gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax,
                        dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
                        wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
-                       precision=precision, res_compat=1 if res_compat else 0, impl=impl, ispg=ispg)
+                       precision=precision, res_compat=1 if res_compat else 0, impl=impl, ispg=ispg,
+                       eps_e=eps_e)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")
@@ -71,6 +74,9 @@ class ImpDrv3D:
             check(lib().lns_upload_sponge3d(self._ctx, ctypes.c_void_p(s1.ctypes.data),
                                             ctypes.c_void_p(s2.ctypes.data) if s2 is not None else None),
                   "lns_upload_sponge3d")
+        if eps_e and buff is not None:
+            b = np.asfortranarray(buff, dtype=np.float64)
+            check(lib().lns_upload_buffer3d(self._ctx, ctypes.c_void_p(b.ctypes.data)), "lns_upload_buffer3d")
         self.set_mean(vm)
 
     def set_mean(self, vm):

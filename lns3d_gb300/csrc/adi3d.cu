@@ -254,7 +254,7 @@ __global__ void genmtrx_kernel(Grid g, const double* __restrict__ vm, Metrics mt
 // dtl (a X + rcalcd alfa (Dh + i Dhi)).  The operations run in the order of
 // the reference's loops.
 __device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, long long p, int k, int a, int b,
-                                        double ak, double bk, bool combined) {
+                                        double ak, double bk, bool combined, int damp) {
   const long long np = o.np;
   const long long e = (long long)((a - 1) + 5 * (b - 1)) * np + p;
   const double x = (dir == 1 ? o.Ah : o.Bh)[e];
@@ -287,6 +287,14 @@ __device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, lo
   else if (a == 5 && b == 5) vk = 3;
   if (vk >= 0) re = re - (bk * d) * (dir == 1 ? o.V11 : o.V22)[vk * np + p];
   if (k == 3 && a == b) re = re + 1.0;
+  // implicit damping: damp 0 the band fb1..fb5 (src/lhs1f3d.f90:168-200,
+  // src/lhs2f3d.f90:171-203), 2 the eta rows 2 and ny-1, (-1, 2, -1) in
+  // slots 2..4 (src/lhsbt2f3d.f90:277-298, 431-452), 1 none (rows 1, ny)
+  if (o.buff && a == b && damp != 1) {
+    const double fb[5] = {1.0, -4.0, 6.0, -4.0, 1.0}, sb[5] = {0.0, -1.0, 2.0, -1.0, 0.0};
+    const double c = damp == 0 ? fb[k - 1] : sb[k - 1];
+    if (c != 0.0) re = re + g.alfa * d * o.eps_e * o.buff[p] * c;
+  }
   // sponge of the eta LHS (src/lhs2f3d.f90:207-224, src/lhsbt2f3d.f90:147-167;
   // the xi LHS has calcd = true and no sponge)
   if (dir == 2 && o.spg && k == 3 && a == b) re = re + g.alfa * d * o.spg[p];
@@ -351,7 +359,8 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
       ak = -(alfa * g1[t] * hinv), bk = alfa * d1[t] * hsinv;
     }
   }
-  store_el(mat, q, lhs_entry(g, o, dir, p, k, a, b, ak, bk, combined));
+  const int damp = !combined ? 0 : (pos == 2 || pos == n - 1) ? 2 : 1;
+  store_el(mat, q, lhs_entry(g, o, dir, p, k, a, b, ak, bk, combined, damp));
 }
 
 // -------------------------------------------------------------------- RHS
@@ -449,6 +458,38 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
       for (int m = 0; m < 5; ++m) {
         const cd vm = v[m + 5 * p];
         r[m] = cd{r[m].x + sp * vm.x, r[m].y + sp * vm.y};
+      }
+    }
+    // smoother3D (src/smoother3d.f90, lsym = rsym = false), the eta pass
+    // then the xi pass: rows/columns 2 and n-1 second order, 3 and n-2
+    // fourth order, the rest sixth order; no periodic wrap
+    if (o.buff) {
+      const double eb = o.eps_e * o.buff[p];
+      const double fa[7] = {-1.666666666666667E-01, 2.0, -6.5, 9.333333333333333, -6.5, 2.0, -1.666666666666667E-01};
+      #pragma unroll 1
+      for (int pass = 0; pass < 2; ++pass) {
+        const int c = pass == 0 ? j : i, n = pass == 0 ? g.ny : g.nx;
+        if (c < 2 || c > n - 1) continue;
+        const long long st = pass == 0 ? 5LL * g.nx : 5LL;
+        #pragma unroll
+        for (int m = 0; m < 5; ++m) {
+          const cd* V = v + m + 5 * p;
+          auto S = [&](int dd) -> const cd& { return V[dd * st]; };
+          double sx, sy;
+          if (c == 2 || c == n - 1) {
+            sx = -1.0 * S(-1).x + 2.0 * S(0).x - 1.0 * S(1).x;
+            sy = -1.0 * S(-1).y + 2.0 * S(0).y - 1.0 * S(1).y;
+          } else if (c == 3 || c == n - 2) {
+            sx = S(-2).x - 4.0 * S(-1).x + 6.0 * S(0).x - 4.0 * S(1).x + 1.0 * S(2).x;
+            sy = S(-2).y - 4.0 * S(-1).y + 6.0 * S(0).y - 4.0 * S(1).y + 1.0 * S(2).y;
+          } else {
+            sx = fa[0] * S(-3).x + fa[1] * S(-2).x + fa[2] * S(-1).x + fa[3] * S(0).x + fa[4] * S(1).x +
+                 fa[5] * S(2).x + fa[6] * S(3).x;
+            sy = fa[0] * S(-3).y + fa[1] * S(-2).y + fa[2] * S(-1).y + fa[3] * S(0).y + fa[4] * S(1).y +
+                 fa[5] * S(2).y + fa[6] * S(3).y;
+          }
+          r[m] = cd{r[m].x + eb * sx, r[m].y + eb * sy};
+        }
       }
     }
     // rbe3D
@@ -685,6 +726,7 @@ struct lns_ctx3d {
   bool have_metrics = false, have_mean = false, factored = false;
   bool have_sponge = false;   // ispg != 0: lns_upload_sponge3d called
   double* spg = nullptr;      // spg, or spg + spg2 (ispg > 4)
+  double* buff = nullptr;     // eps_e != 0: buff(nx,ny), ones until uploaded
   // time scheme (src/impdrv3d.f90:130-199): the previous-previous state
   // (impl 2), the averaged field (impl 3), steps taken, alfa of the factors
   cd *v2old = nullptr, *wavg = nullptr;
@@ -1002,6 +1044,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
     return fail3(LNS_ERR_ARG, "ctx3d_create: precision must be LNS_FP64 or LNS_MIXED");
   if (p->impl < 0 || p->impl > 3) return fail3(LNS_ERR_ARG, "ctx3d_create: impl must be 1, 2 or 3 (0 means 1)");
+  if (!(p->eps_e >= 0.0) || !std::isfinite(p->eps_e))
+    return fail3(LNS_ERR_ARG, "ctx3d_create: eps_e must be finite and >= 0");
   if (p->ispg < 0 || (p->ispg >= 2 && p->ispg <= 4))
     return fail3(LNS_ERR_ARG, "ctx3d_create: ispg must be 0, 1 or > 4 (the inflow sponges 2-4 are not supported)");
   lns_ctx3d* c = new lns_ctx3d();
@@ -1041,6 +1085,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->impl == 2) { A(sizeof(cd) * 5 * np, &q); c->v2old = (cd*)q; }
   if (p->impl == 3) { A(sizeof(cd) * 5 * np, &q); c->wavg = (cd*)q; }
   if (p->ispg != 0) { A(sizeof(double) * np, &q); c->spg = (double*)q; }
+  if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
   A(sizeof(cd) * 125 * np, &c->matx);
@@ -1077,6 +1122,18 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   c->ops.Ah = o; c->ops.Bh = o + 25 * np; c->ops.Dh = o + 50 * np; c->ops.Dhi = o + 75 * np;
   c->ops.V11 = o + 100 * np; c->ops.V12 = o + 106 * np; c->ops.V22 = o + 112 * np; c->ops.AB = o + 118 * np;
   c->ops.dtl = o + 124 * np;
+  if (c->buff) {
+    // the reference's default buffer (ibuff = 0, src/buffer.f90): ones
+    std::vector<double> ones((size_t)np, 1.0);
+    ez = cudaMemcpy(c->buff, ones.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
+    if (ez != cudaSuccess) {
+      free_all(c);
+      delete c;
+      return cuda3(ez, "buffer init");
+    }
+    c->ops.buff = c->buff;
+    c->ops.eps_e = p->eps_e;
+  }
   *out = c;
   return LNS_OK;
 }
@@ -1118,6 +1175,17 @@ int lns_upload_sponge3d(lns_ctx3d* c, const double* spg, const double* spg2) {
   if (e != cudaSuccess) return cuda3(e, "upload sponge");
   c->ops.spg = c->spg;
   c->have_sponge = true;
+  c->factored = false;
+  return LNS_OK;
+}
+
+int lns_upload_buffer3d(lns_ctx3d* c, const double* buff) {
+  if (!c || !buff) return fail3(LNS_ERR_ARG, "upload_buffer3d: null argument");
+  if (!c->buff) return fail3(LNS_ERR_ARG, "upload_buffer3d: the context was created with eps_e = 0");
+  int rc = check_device(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->buff, buff, sizeof(double) * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload buffer");
   c->factored = false;
   return LNS_OK;
 }
@@ -1528,7 +1596,8 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
   for (int p = 0; p < nprob; ++p)
     if (params[p].impl > 1) return fail3(LNS_ERR_ARG, "batch3d_create: batches run impl = 1 (backward Euler)");
   for (int p = 0; p < nprob; ++p)
-    if (params[p].ispg != 0) return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge (ispg = 0)");
+    if (params[p].ispg != 0 || params[p].eps_e != 0.0)
+      return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge or smoother (ispg = 0, eps_e = 0)");
   lns_batch3d* b = new lns_batch3d();
   b->P = nprob;
   b->mixed = params[0].precision == LNS_MIXED;
@@ -1897,7 +1966,8 @@ int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* 
   if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
   if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
   if (prm->impl > 1) return fail3(LNS_ERR_ARG, "server3d_submit: servers run impl = 1 (backward Euler)");
-  if (prm->ispg != 0) return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge (ispg = 0)");
+  if (prm->ispg != 0 || prm->eps_e != 0.0)
+    return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge or smoother (ispg = 0, eps_e = 0)");
   if (!(tol > 0.0) || max_steps < 1) return fail3(LNS_ERR_ARG, "server3d_submit: need tol > 0 and max_steps >= 1");
   if (ctx_bytes_for(*prm) > s->budget) return fail3(LNS_ERR_ARG, "server3d_submit: request larger than the budget");
   SrvReq* r = new SrvReq();

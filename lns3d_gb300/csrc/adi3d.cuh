@@ -60,6 +60,9 @@ struct Ops {
   // the sponge coefficient (nx,ny): spg, or spg + spg2 for the double
   // sponge; null without a sponge
   const double* spg = nullptr;
+  // explicit smoother / implicit damping: eps_e buff(nx,ny); null when eps_e = 0
+  const double* buff = nullptr;
+  double eps_e = 0.0;
 };
 
 struct Metrics {

@@ -120,7 +120,8 @@ def _params3d(**kw):
 
 @pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=0), dict(wallt=2),
                                  dict(top=1), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
-                                 dict(loctime=2), dict(ispg=2), dict(ispg=4), dict(ispg=-1)])
+                                 dict(loctime=2), dict(ispg=2), dict(ispg=4), dict(ispg=-1),
+                                 dict(eps_e=-1.0), dict(eps_e=float("nan"))])
 def test_ctx3d_rejects_unsupported_options(lib, bad):
     ctx = ctypes.c_void_p()
     rc = lib.lns_ctx3d_create(ctypes.byref(_params3d(**bad)), ctypes.byref(ctx))
@@ -142,6 +143,7 @@ def test_ctx3d_null_arguments(lib):
     assert lib.lns_ctx3d_profile(None, 1) == 1
     assert lib.lns_ctx3d_profile_read(None, None, None) == 1
     assert lib.lns_upload_sponge3d(None, None, None) == 1
+    assert lib.lns_upload_buffer3d(None, None) == 1
 
 
 def _params2d(**kw):

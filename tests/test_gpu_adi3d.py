@@ -392,3 +392,72 @@ def test_sponge_needs_upload(cuda):
             assert L.lns_step3d(ctx, P(v), 1, 1, None) == 0
         finally:
             L.lns_ctx3d_destroy(ctx)
+
+
+@pytest.mark.parametrize("with_sponge", [False, True])
+def test_smoother_matches_oracle(cuda, with_sponge):
+    """The explicit smoother (src/smoother3d.f90) and the implicit damping of
+    both LHS (src/lhs1f3d.f90:168-200, src/lhs2f3d.f90:171-203,
+    src/lhsbt2f3d.f90:277-298) with a non-uniform buff, alone and with the
+    sponge: RHS, both LHS and steps against the oracle."""
+    import ctypes
+
+    import torch
+    from adi3dcase import _lib, ptr, sponge
+
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 40, 33
+    case = shear_layer(nx=nx, ny=ny, seed=10)
+    buff = np.asfortranarray(0.5 + np.random.default_rng(3).uniform(size=(nx, ny)))
+    kw = dict(eps_e=0.02, buff=buff)
+    if with_sponge:
+        spg, spg2 = sponge(nx, ny)
+        kw.update(ispg=1, spg=spg, spg2=spg2)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1, **kw)
+    mk = lambda: ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, **kw)
+    drv = mk()
+    for direction in (1, 2):
+        mat = torch.zeros(125 * nx * ny, dtype=torch.complex128, device="cuda")
+        drv.lhs(direction, mat)
+        torch.cuda.synchronize()
+        got = mat.cpu().numpy().reshape((5, 5, 5, nx, ny), order="F")
+        assert rel(got, orc.lhs(direction)) < OPS_TOL, direction
+    rng = np.random.default_rng(13)
+    shape = (5, nx, ny)
+    v = np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    vold = np.asfortranarray(v + 1e-3 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    L = _lib()
+    r = orc.lrhs(v)
+    L.a3_rbe(ctypes.byref(orc.g), ptr(r), ptr(v), ptr(vold), ptr(orc.dtl))
+    L.a3_rhsbc(ctypes.byref(orc.g), ptr(r), ptr(v))
+    dev = lambda a: torch.from_numpy(a.ravel(order="F")).cuda()
+    dv, dvo = dev(v), dev(vold)
+    dr = torch.zeros_like(dv)
+    drv.rhs(dv, dvo, dr, torch.zeros(1, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    assert rel(dr.cpu().numpy().reshape(shape, order="F"), r) < RHS_TOL
+    drv = mk()
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    for s in range(4):
+        res_ref = orc.step(v_ref)
+        res_gpu = drv.step(v_gpu, nsteps=1)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+
+
+def test_smoother_default_buffer_is_ones(cuda):
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 24, 20
+    case = shear_layer(nx=nx, ny=ny, seed=2)
+    a = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, eps_e=0.01)
+    b = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, eps_e=0.01,
+                 buff=np.ones((nx, ny)))
+    va, vb = case["v"].copy(order="F"), case["v"].copy(order="F")
+    a.step(va, nsteps=3)
+    b.step(vb, nsteps=3)
+    assert np.array_equal(va, vb)
