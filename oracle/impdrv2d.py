@@ -47,11 +47,19 @@ def ptr(a):
 class Oracle2D:
     """Grid struct, operator storage and scratch of the oracle for one case."""
 
-    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False, ilhs=1, impl=1):
+    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False, ilhs=1, impl=1,
+                 ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None):
         """ilhs = 1: fourth-order LHS, pentadiagonal solves; ilhs = 0:
         second-order LHS, block-tridiagonal solves (src/impdrv.f90:307-344).
         impl: time scheme 1 (backward Euler), 2 (two-step backward), 3
-        (midpoint), src/impdrv.f90:186-279; steps are counted from creation."""
+        (midpoint), src/impdrv.f90:186-279; steps are counted from creation.
+        ispg = 2, spg, spg2: the sponge towards the free stream
+        (src/genmtrx.f90:436-446); eps_e, buff: the explicit smoother and
+        implicit damping (buff ones when None).  Both with ilhs = 1 only."""
+        if (ispg or eps_e) and ilhs == 0:
+            raise ValueError("the sponge and smoother are restated for ilhs = 1 only")
+        if ispg not in (0, 2):
+            raise ValueError("the nonlinear 2D step supports ispg 0 or 2")
         self.L = _lib(lib)
         self.ilhs, self.impl, self.lstep = ilhs, impl, 0
         p = case["params"]
@@ -68,6 +76,14 @@ class Oracle2D:
         self.resacc = ctypes.c_double(0.0)
         if res_compat:
             g3.resacc = ctypes.cast(ctypes.byref(self.resacc), P).value
+        if ispg:
+            self.spg = np.asfortranarray(spg, dtype=np.float64).reshape((nx, ny), order="F")
+            self.spg2 = np.asfortranarray(spg2, dtype=np.float64).reshape((nx, ny), order="F")
+            g3.ispg, g3.spg, g3.spg2 = ispg, ptr(self.spg).value, ptr(self.spg2).value
+        if eps_e:
+            self.buff = np.asfortranarray(buff if buff is not None else np.ones((nx, ny)),
+                                          dtype=np.float64).reshape((nx, ny), order="F")
+            g3.eps_e, g3.buff = eps_e, ptr(self.buff).value
         self.g = A2Grid(g=g3, theta=case.get("theta", 0.0), bnt=ptr(self.bnt).value,
                         **{k: ptr(v).value for k, v in self.pot.items()})
         self.ops = {k: np.zeros((5, 5, nx, ny), order="F") for k in ("Ah", "Bh", "Dh", "Dhi")}

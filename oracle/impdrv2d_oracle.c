@@ -20,6 +20,37 @@
 
 /* src/genmtrx.f90 with linear = 0, general = true, mattyp = 0, idamp = 0,
    kzl = 0: the nonlinear RHS and the operators of the LHS. */
+/* smoother, src/smoother.f90 without symmetry planes: rl += eps_e buff D(vl)
+   over the nc interleaved components of each point, the eta pass first (rows
+   2 and ny-1 second order, 3 and ny-2 fourth order, 4..ny-3 sixth order),
+   then the xi pass with the same pattern over i (no periodic wrap). */
+static void a2_smoother(const A3Grid* g, int nc, double* rl, const double* vl) {
+  const int nx = g->nx, ny = g->ny;
+  const double fa1 = -1.666666666666667E-01, fa2 = 2.000000000000000E+00, fa3 = -6.500000000000000E+00,
+               fa4 = 9.333333333333333E+00, fa5 = -6.500000000000000E+00, fa6 = 2.000000000000000E+00,
+               fa7 = -1.666666666666667E-01; /* src/stencil.f90:145-151 */
+  for (int pass = 0; pass < 2; ++pass) {
+    const int n = pass == 0 ? ny : nx;
+    for (int l = 1; l <= (pass == 0 ? nx : ny); ++l)
+      for (int c = 2; c <= n - 1; ++c) {
+        const int i = pass == 0 ? l : c, j = pass == 0 ? c : l;
+        const long st = pass == 0 ? (long)nc * nx : nc;
+        const long p = IX(g, i, j);
+        const double eb = g->eps_e * g->buff[p];
+        for (int k = 0; k < nc; ++k) {
+          const double* V = vl + k + nc * p;
+#define VS(d) V[(long)(d) * st]
+          double s;
+          if (c == 2 || c == n - 1) s = -1.0 * VS(-1) + 2.0 * VS(0) - 1.0 * VS(1);
+          else if (c == 3 || c == n - 2) s = VS(-2) - 4.0 * VS(-1) + 6.0 * VS(0) - 4.0 * VS(1) + 1.0 * VS(2);
+          else s = fa1 * VS(-3) + fa2 * VS(-2) + fa3 * VS(-1) + fa4 * VS(0) + fa5 * VS(1) + fa6 * VS(2) + fa7 * VS(3);
+#undef VS
+          rl[k + nc * p] = rl[k + nc * p] + eb * s;
+        }
+      }
+  }
+}
+
 int a2_genmtrx(const A2Grid* a2, const double* vl, A3Ops* o, double* rl) {
   const A3Grid* g = G(a2);
   const int nx = g->nx, ny = g->ny;
@@ -254,6 +285,14 @@ int a2_genmtrx(const A2Grid* a2, const double* vl, A3Ops* o, double* rl) {
       V22[5] = Vij[3] * n1n2;
     }
   free(g1v); free(g2v); free(g11v); free(g12v); free(g22v);
+  if (rl && g->ispg == 2) /* the sponge towards the free stream, genmtrx.f90:436-446 */
+    for (long p = 0; p < np; ++p) {
+      const double sp = g->spg[p] + g->spg2[p];
+      rl[0 + 5 * p] = rl[0 + 5 * p] + sp * (vl[0 + 5 * p] - one);
+      for (int k = 1; k <= 3; ++k) rl[k + 5 * p] = rl[k + 5 * p] + sp * (vl[k + 5 * p]);
+      rl[4 + 5 * p] = rl[4 + 5 * p] + sp * (vl[4 + 5 * p] - one);
+    }
+  if (rl && g->eps_e != zero) a2_smoother(g, 5, rl, vl); /* genmtrx.f90:1008 */
   return 0;
 }
 
@@ -547,6 +586,16 @@ int a2_lhs(const A2Grid* a2, const A3Ops* o, const double* dtl, const double* vl
         MT(k, 5, 5, p) = MT(k, 5, 5, p) - bk[k - 1] * d * V[3];
       }
       for (int a = 1; a <= 5; ++a) MT(3, a, a, p) = MT(3, a, a, p) + one;
+      /* implicit damping (src/lhsf.f90:113-145, 262-294) and, in the eta
+         LHS, the sponge (src/lhsf.f90:296-312) */
+      if (g->eps_e != zero) {
+        const double fb[5] = {1.000000000000000E+00, -4.000000000000000E+00, 6.000000000000000E+00,
+                              -4.000000000000000E+00, 1.000000000000000E+00};
+        for (int k = 1; k <= 5; ++k)
+          for (int a = 1; a <= 5; ++a) MT(k, a, a, p) = MT(k, a, a, p) + alfa * d * g->eps_e * g->buff[p] * fb[k - 1];
+      }
+      if (dir == 2 && g->ispg == 2)
+        for (int a = 1; a <= 5; ++a) MT(3, a, a, p) = MT(3, a, a, p) + alfa * d * (g->spg[p] + g->spg2[p]);
     }
   if (dir == 2) {
     /* rows 1, 2, ny-1, ny: coefficient t at slot s[t], src/lhsbt2f.f90 */
@@ -582,6 +631,20 @@ int a2_lhs(const A2Grid* a2, const A3Ops* o, const double* dtl, const double* vl
           MT(k, 5, 5, p) = MT(k, 5, 5, p) - w * V[3];
         }
         for (int a = 1; a <= 5; ++a) MT(3, a, a, p) = MT(3, a, a, p) + one;
+        /* sponge: lhsbt2f declares spgl(ny,nx) for the (nx,ny) array it is
+           given, so row j of line i reads element (j-1) + (i-1) ny of it
+           (src/lhsbt2f.f90:18,94-108) */
+        if (g->ispg == 2) {
+          const long q = (long)(j - 1) + (long)(i - 1) * ny;
+          for (int a = 1; a <= 5; ++a) MT(3, a, a, p) = MT(3, a, a, p) + alfa * d * (g->spg[q] + g->spg2[q]);
+        }
+        /* damping of rows 2 and ny-1 in slots 2..4 (src/lhsbt2f.f90:193-213) */
+        if (g->eps_e != zero && (r == 1 || r == 2)) {
+          const double sb[3] = {-one, two, -one};
+          for (int k = 2; k <= 4; ++k)
+            for (int a = 1; a <= 5; ++a)
+              MT(k, a, a, p) = MT(k, a, a, p) + alfa * d * g->eps_e * g->buff[p] * sb[k - 2];
+        }
       }
   }
   /* boundary conditions */

@@ -11,6 +11,7 @@ restatement is checked against properties of its algorithm:
   * the vortex case stays finite and its periodic column repeats column 1.
 """
 import numpy as np
+import pytest
 
 from oracle.impdrv2d import Oracle2D
 
@@ -152,3 +153,83 @@ def test_time_schemes_rest_fixed_point_and_consistency():
         for impl in (2, 3):
             d = np.linalg.norm(runs[impl][1] - c["v"]) / np.linalg.norm(c["v"])
             assert np.linalg.norm(runs[impl][1] - runs[1][1]) < 0.5 * np.linalg.norm(runs[1][1] - c["v"]) + 1e-3 * d
+
+
+def test_sponge_and_smoother_known_answers():
+    """The nonlinear sponge (ispg 2, src/genmtrx.f90:436-446: rl += (spg +
+    spg2) (v - v_inf) with v_inf = (1, 0, 0, 0, 1)), the smoother at the end
+    of genmtrx (src/smoother.f90) and the LHS terms: damping on the band
+    diagonals of both LHS, the sponge on the eta LHS diagonal, and in the
+    eta boundary rows the sponge read through the transposed spgl(ny,nx)
+    view (src/lhsbt2f.f90:18,94-108) with the (-1, 2, -1) damping of rows 2
+    and ny-1."""
+    from lns3d_gb300.cases import vortex2d
+
+    nx, ny = 24, 20
+    c = vortex2d(nx=nx, ny=ny)
+    rng = np.random.default_rng(7)
+    spg = np.asfortranarray(rng.uniform(size=(nx, ny)))
+    spg2 = np.asfortranarray(0.5 * rng.uniform(size=(nx, ny)))
+    buff = np.asfortranarray(0.5 + rng.uniform(size=(nx, ny)))
+    v = c["v"].copy(order="F")
+    plain = Oracle2D(c)
+    o = Oracle2D(c, ispg=2, spg=spg, spg2=spg2, eps_e=0.02, buff=buff)
+    sp = spg + spg2
+    ref = np.zeros_like(v)
+    ref[0] = ref[4] = 1.0
+    d = o.genmtrx(v) - plain.genmtrx(v)
+    # the smoother's part: the sponge removed leaves eps_e buff times the
+    # second/fourth/sixth differences; check one interior point exactly
+    i0, j0 = 10, 9
+    fa = [-1.666666666666667E-01, 2.0, -6.5, 9.333333333333333, -6.5, 2.0, -1.666666666666667E-01]
+    sy = sum(fa[t] * v[:, i0, j0 - 3 + t] for t in range(7))
+    sx = sum(fa[t] * v[:, i0 - 3 + t, j0] for t in range(7))
+    want = sp[i0, j0] * (v[:, i0, j0] - ref[:, i0, j0]) + 0.02 * buff[i0, j0] * sy + 0.02 * buff[i0, j0] * sx
+    assert np.abs(d[:, i0, j0] - want).max() <= 1e-14 * np.abs(plain.genmtrx(v)).max()
+    # LHS
+    import ctypes
+
+    o.L.a3_set_time_step(ctypes.byref(o.g.g), ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(o.dtl.ctypes.data))
+    dtl = o.dtl.copy(order="F")
+    for orc in (plain, o):
+        orc.genmtrx(v)
+    alfa = c["params"]["alfa"]
+    w = alfa * dtl * 0.02 * buff
+    fb = [1.0, -4.0, 6.0, -4.0, 1.0]
+    flat_sp = sp.ravel(order="F")
+    for direction in (1, 2):
+        dm = o.lhs(v, dtl, direction) - plain.lhs(v, dtl, direction)
+        scale = np.abs(plain.lhs(v, dtl, direction)).max()
+        rows = range(1, ny - 1) if direction == 1 else range(2, ny - 2)
+        for k in range(5):
+            for a in range(5):
+                want = w[:, list(rows)] * fb[k]
+                if direction == 2 and k == 2:
+                    want = want + alfa * dtl[:, list(rows)] * sp[:, list(rows)]
+                assert np.abs(dm[k, a, a][:, list(rows)] - want).max() <= 1e-15 * scale
+        if direction == 2:
+            for jj in (1, ny - 2):
+                quirk = np.array([flat_sp[jj + iv * ny] for iv in range(nx)])
+                for k, cc in ((1, -1.0), (2, 2.0), (3, -1.0)):
+                    for a in range(5):
+                        want = w[:, jj] * cc + (alfa * dtl[:, jj] * quirk if k == 2 else 0.0)
+                        assert np.abs(dm[k, a, a, :, jj] - want).max() <= 1e-15 * scale
+        off = dm.copy()
+        for a in range(5):
+            off[:, a, a] = 0.0
+        assert not off.any()
+
+
+def test_sponge_and_smoother_steps():
+    from lns3d_gb300.cases import vortex2d
+
+    nx, ny = 32, 28
+    c = vortex2d(nx=nx, ny=ny)
+    spg = np.asfortranarray(np.outer(np.ones(nx), np.linspace(0.0, 1.0, ny) ** 3))
+    o = Oracle2D(c, ispg=2, spg=spg, spg2=np.zeros((nx, ny)), eps_e=0.01)
+    v = c["v"].copy(order="F")
+    o.itrbc(v)
+    res = [o.step(v) for _ in range(5)]
+    assert np.isfinite(v).all() and all(r > 0 for r in res)
+    with pytest.raises(ValueError):
+        Oracle2D(c, ilhs=0, eps_e=0.01)
