@@ -213,6 +213,15 @@ typedef struct {
                                 context's first step and rtb at alfa = 2/3 after it; 3 midpoint,
                                 genmtrx on (v + vold)/2 with alfa = 1/2.  Steps are counted from
                                 the context's creation (a fresh run, lstep = 0). */
+  int32_t ispg;              /* 0, or 2: the sponge towards the free stream, r += (spg + spg2)
+                                (v - (1,0,0,0,1)) (src/genmtrx.f90:436-446) and alfa dtl
+                                (spg + spg2) on the eta LHS diagonal (src/lhsf.f90:296-312,
+                                src/lhsbt2f.f90, whose boundary rows read the array through a
+                                transposed (ny,nx) view, kept here); lns_upload_sponge2d */
+  double eps_e;              /* explicit smoother at the end of genmtrx (src/smoother.f90) and
+                                implicit damping of both LHS (src/lhsf.f90:113-145, 262-294,
+                                src/lhsbt2f.f90:193-213) weighted by buff (ones until
+                                lns_upload_buffer2d).  ispg and eps_e need lhs_order 0 or 4. */
 } lns_params2d;
 
 typedef struct lns_ctx2d lns_ctx2d;
@@ -225,6 +234,11 @@ size_t lns_ctx2d_bytes(const lns_ctx2d* ctx);
 int lns_upload_metrics2d(lns_ctx2d* ctx, const double* metrics);
 /* far field of the top boundary: unit normal bnt(nx,2) and top.pot (5,nx) */
 int lns_upload_top2d(lns_ctx2d* ctx, const double* bnt, const double* pot);
+/* The sponge arrays spg(nx,ny), spg2(nx,ny) (src/sponge.f90) when ispg = 2;
+ * needed before the first step. */
+int lns_upload_sponge2d(lns_ctx2d* ctx, const double* spg, const double* spg2);
+/* The smoother weight buff(nx,ny) (src/buffer.f90, ibuff > 0) when eps_e != 0. */
+int lns_upload_buffer2d(lns_ctx2d* ctx, const double* buff);
 /* itrBC on a device state (the call before the step loop, src/impdrv.f90:160) */
 int lns_itrbc2d_dev(lns_ctx2d* ctx, double* v, void* stream);
 /* nsteps steps on the host state v(5,nx,ny) in place; totres[nsteps] (may be

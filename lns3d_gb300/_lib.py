@@ -67,6 +67,8 @@ SIGNATURES = {
     "lns_upload_metrics3d": [P, DP],
     "lns_upload_sponge3d": [P, DP, DP],
     "lns_upload_buffer3d": [P, DP],
+    "lns_upload_sponge2d": [P, DP, DP],
+    "lns_upload_buffer2d": [P, DP],
     "lns_upload_mean3d": [P, DP, DP],
     "lns_step3d": [P, DP, I32, I32, DP],
     "lns_step3d_dev": [P, DP, I32, I32, DP, P],
@@ -107,7 +109,8 @@ class Params2D(ctypes.Structure):
                 ("gamma", ctypes.c_double), ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double),
                 ("dtmax", ctypes.c_double), ("theta", ctypes.c_double), ("loctime", I32), ("xper", I32),
                 ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32), ("top", I32), ("optx", I32),
-                ("opty", I32), ("res_compat", I32), ("lhs_order", I32), ("impl", I32)]
+                ("opty", I32), ("res_compat", I32), ("lhs_order", I32), ("impl", I32), ("ispg", I32),
+                ("eps_e", ctypes.c_double)]
 
 
 class Params3D(ctypes.Structure):

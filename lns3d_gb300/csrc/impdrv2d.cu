@@ -350,6 +350,34 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
     o.V22[4 * np + p] = Vij[3] * n1n2;
     o.V22[5 * np + p] = Vij[3] * n1n2;
     if (r) {
+      // the sponge towards the free stream (ispg 2, src/genmtrx.f90:436-446)
+      // and the explicit smoother at the end of genmtrx (src/smoother.f90,
+      // without symmetry planes; no periodic wrap), both on genmtrx's state
+      if (o.spg) {
+        const double sp = o.spg[p];
+        rr[0] = rr[0] + sp * (V(0, i, j) - 1.0);
+        for (int m = 1; m <= 3; ++m) rr[m] = rr[m] + sp * (V(m, i, j));
+        rr[4] = rr[4] + sp * (V(4, i, j) - 1.0);
+      }
+      if (o.buff) {
+        const double eb = o.eps_e * o.buff[p];
+        const double fa[7] = {-1.666666666666667E-01, 2.0, -6.5, 9.333333333333333, -6.5, 2.0,
+                              -1.666666666666667E-01};
+        for (int pass = 0; pass < 2; ++pass) {
+          const int c = pass == 0 ? j : i, n = pass == 0 ? g.ny : g.nx;
+          if (c < 2 || c > n - 1) continue;
+          for (int m = 0; m < 5; ++m) {
+            auto S = [&](int dd) { return pass == 0 ? V(m, i, j + dd) : V(m, i + dd, j); };
+            double sm;
+            if (c == 2 || c == n - 1) sm = -1.0 * S(-1) + 2.0 * S(0) - 1.0 * S(1);
+            else if (c == 3 || c == n - 2) sm = S(-2) - 4.0 * S(-1) + 6.0 * S(0) - 4.0 * S(1) + 1.0 * S(2);
+            else
+              sm = fa[0] * S(-3) + fa[1] * S(-2) + fa[2] * S(-1) + fa[3] * S(0) + fa[4] * S(1) + fa[5] * S(2) +
+                   fa[6] * S(3);
+            rr[m] = rr[m] + eb * sm;
+          }
+        }
+      }
       // rbe
       const double dtl = o.dtl[p];
       if (v2old) {
@@ -513,6 +541,22 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
     if (vk >= 0) val = val - alfa * d * dcf * detasinv * V[vk * np + p];
   }
   val = val + ident;
+  // implicit damping and sponge of the fourth-order LHS, after the I term:
+  // band rows damping then sponge (src/lhsf.f90:113-145, 262-312); the eta
+  // boundary rows the sponge through lhsbt2f's transposed spgl(ny,nx) view
+  // of the (nx,ny) array, then the damping of rows 2 and ny-1 in slots 2..4
+  // (src/lhsbt2f.f90:18, 84-108, 163-213, 266-316)
+  if (!order2 && a == b && (o.buff || o.spg)) {
+    const double wd = o.buff ? alfa * d * o.eps_e * o.buff[p] : 0.0;
+    if (!edge) {
+      const double fb[5] = {1.0, -4.0, 6.0, -4.0, 1.0};
+      if (o.buff) val = val + wd * fb[k - 1];
+      if (dir == 2 && o.spg && k == 3) val = val + alfa * d * o.spg[p];
+    } else {
+      if (o.spg && k == 3) val = val + alfa * d * o.spg[(long long)(j - 1) + (long long)(i - 1) * g.ny];
+      if (o.buff && (j == 2 || j == g.ny - 1) && k >= 2 && k <= 4) val = val + wd * (k == 3 ? 2.0 : -1.0);
+    }
+  }
   mat[q] = val;
 }
 
@@ -597,6 +641,9 @@ struct lns_ctx2d {
   int res_cap = 0;
   int* status = nullptr;
   bool have_metrics = false, have_top = false;
+  bool have_sponge = false;  // ispg = 2: lns_upload_sponge2d called
+  double* spg = nullptr;     // spg + spg2
+  double* buff = nullptr;    // eps_e != 0: buff(nx,ny), ones until uploaded
 };
 
 namespace {
@@ -797,6 +844,12 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
     return fail2(LNS_ERR_ARG, "ctx2d_create: lhs_order must be 0 (fourth order), 2 or 4");
   if (p->lhs_order == 2 && p->ny < 8) return fail2(LNS_ERR_ARG, "ctx2d_create: the second-order LHS needs ny >= 8");
   if (p->impl < 0 || p->impl > 3) return fail2(LNS_ERR_ARG, "ctx2d_create: impl must be 0 or 1 (backward Euler), 2 or 3");
+  if (p->ispg != 0 && p->ispg != 2)
+    return fail2(LNS_ERR_ARG, "ctx2d_create: ispg must be 0 or 2 (the reference's nonlinear sponge)");
+  if (!(p->eps_e >= 0.0) || !std::isfinite(p->eps_e))
+    return fail2(LNS_ERR_ARG, "ctx2d_create: eps_e must be finite and >= 0");
+  if (p->lhs_order == 2 && (p->ispg != 0 || p->eps_e != 0.0))
+    return fail2(LNS_ERR_ARG, "ctx2d_create: the sponge and smoother are supported with the fourth-order LHS");
   lns_ctx2d* c = new lns_ctx2d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);
@@ -839,6 +892,8 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   A(sizeof(double) * 64, &q); c->res_dev = (double*)q;
   if (p->impl == 2) { A(sizeof(double) * 5 * np, &q); c->v2old = (double*)q; }
   if (p->impl == 3) { A(sizeof(double) * 5 * np, &q); c->wavg = (double*)q; }
+  if (p->ispg != 0) { A(sizeof(double) * np, &q); c->spg = (double*)q; }
+  if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (!rc) {
     c->res_cap = 64;
     e = cudaMemset(c->dscal, 0, sizeof(double) * 3);
@@ -856,6 +911,18 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   c->ops.V11 = o + 75 * np; c->ops.V12 = o + 81 * np; c->ops.V22 = o + 87 * np;
   c->ops.AB = nullptr;
   c->ops.dtl = o + 93 * np;
+  if (c->buff) {
+    // the reference's default buffer (ibuff = 0, src/buffer.f90): ones
+    std::vector<double> ones((size_t)np, 1.0);
+    e = cudaMemcpy(c->buff, ones.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      free2(c);
+      delete c;
+      return cuda2(e, "buffer init");
+    }
+    c->ops.buff = c->buff;
+    c->ops.eps_e = p->eps_e;
+  }
   *out = c;
   return LNS_OK;
 }
@@ -890,9 +957,37 @@ int lns_upload_top2d(lns_ctx2d* c, const double* bnt, const double* pot) {
   return LNS_OK;
 }
 
+int lns_upload_sponge2d(lns_ctx2d* c, const double* spg, const double* spg2) {
+  if (!c || !spg || !spg2) return fail2(LNS_ERR_ARG, "upload_sponge2d: null argument");
+  if (!c->spg) return fail2(LNS_ERR_ARG, "upload_sponge2d: the context was created with ispg = 0");
+  int rc = check_dev2(c);
+  if (rc) return rc;
+  // the sponge enters the RHS and the LHS only as spg + spg2 (src/genmtrx.f90:
+  // 440-444, src/lhsf.f90:307-312, src/lhsbt2f.f90:102-108): add once here
+  std::vector<double> h((size_t)c->np);
+  for (long long k = 0; k < c->np; ++k) h[k] = spg[k] + spg2[k];
+  cudaError_t e = cudaMemcpy(c->spg, h.data(), sizeof(double) * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda2(e, "upload sponge");
+  c->ops.spg = c->spg;
+  c->have_sponge = true;
+  return LNS_OK;
+}
+
+int lns_upload_buffer2d(lns_ctx2d* c, const double* buff) {
+  if (!c || !buff) return fail2(LNS_ERR_ARG, "upload_buffer2d: null argument");
+  if (!c->buff) return fail2(LNS_ERR_ARG, "upload_buffer2d: the context was created with eps_e = 0");
+  int rc = check_dev2(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->buff, buff, sizeof(double) * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda2(e, "upload buffer");
+  return LNS_OK;
+}
+
 static int ready2(lns_ctx2d* c, const char* who) {
   if (!c->have_metrics || !c->have_top)
     return fail2(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the far field first");
+  if (c->prm.ispg != 0 && !c->have_sponge)
+    return fail2(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
   return check_dev2(c);
 }
 

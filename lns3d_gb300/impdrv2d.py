@@ -37,11 +37,14 @@ class ImpDrv2D:
     """
 
     def __init__(self, params, metrics, bnt, pot, cflmax=1.0, dtmax=1e30, loctime=0, theta=0.0, res_compat=False,
-                 ilhs=1, impl=1):
+                 ilhs=1, impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None):
         """ilhs: the reference's iLHS switch, 1 = fourth-order LHS with
         pentadiagonal solves, 0 = second-order LHS with block-tridiagonal
         solves (src/impdrv.f90:307-344).  impl: time scheme, 1 backward
-        Euler, 2 two-step backward, 3 midpoint (src/impdrv.f90:186-279)."""
+        Euler, 2 two-step backward, 3 midpoint (src/impdrv.f90:186-279).
+        ispg (0 or 2), spg, spg2: the sponge towards the free stream; eps_e,
+        buff: the explicit smoother and implicit damping (buff ones when
+        None); both with ilhs = 1."""
         if ilhs not in (0, 1):
             raise ValueError("ilhs must be 0 or 1")
         if impl not in (1, 2, 3):
@@ -52,7 +55,7 @@ class ImpDrv2D:
                        gamma=p["gamma"], alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax, theta=theta, loctime=loctime,
                        xper=p["xper"], yper=p["yper"], navier=p["navier"], wall=p["wall"], wallt=p["wallt"],
                        top=p["top"], optx=p["optx"], opty=p["opty"], res_compat=1 if res_compat else 0,
-                       lhs_order=2 if ilhs == 0 else 4, impl=impl)
+                       lhs_order=2 if ilhs == 0 else 4, impl=impl, ispg=ispg, eps_e=eps_e)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx2d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx2d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")
@@ -64,6 +67,14 @@ class ImpDrv2D:
         assert b.shape == (self.nx, 2) and q.shape == (5, self.nx)
         check(lib().lns_upload_top2d(self._ctx, ctypes.c_void_p(b.ctypes.data), ctypes.c_void_p(q.ctypes.data)),
               "lns_upload_top2d")
+        if ispg:
+            s1 = np.asfortranarray(spg, dtype=np.float64)
+            s2 = np.asfortranarray(spg2, dtype=np.float64)
+            check(lib().lns_upload_sponge2d(self._ctx, ctypes.c_void_p(s1.ctypes.data),
+                                            ctypes.c_void_p(s2.ctypes.data)), "lns_upload_sponge2d")
+        if eps_e and buff is not None:
+            bb = np.asfortranarray(buff, dtype=np.float64)
+            check(lib().lns_upload_buffer2d(self._ctx, ctypes.c_void_p(bb.ctypes.data)), "lns_upload_buffer2d")
 
     @property
     def device_bytes(self):

@@ -159,7 +159,8 @@ def _params2d(**kw):
 @pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=2), dict(wallt=2),
                                  dict(top=1), dict(nx=7), dict(ny=6), dict(Ma=1.0), dict(deta=0.0),
                                  dict(res_compat=3), dict(lhs_order=3), dict(lhs_order=2, ny=7), dict(impl=4),
-                                 dict(impl=-1)])
+                                 dict(impl=-1), dict(ispg=1), dict(eps_e=-0.5),
+                                 dict(lhs_order=2, eps_e=0.01), dict(lhs_order=2, ispg=2)])
 def test_ctx2d_rejects_unsupported_options(lib, bad):
     ctx = ctypes.c_void_p()
     rc = lib.lns_ctx2d_create(ctypes.byref(_params2d(**bad)), ctypes.byref(ctx))
@@ -179,6 +180,8 @@ def test_ctx2d_null_arguments(lib):
     assert lib.lns_get_field2d(None, 0, None) == 1
     assert lib.lns_ctx2d_destroy(None) == 0
     assert lib.lns_ctx2d_bytes(None) == 0
+    assert lib.lns_upload_sponge2d(None, None, None) == 1
+    assert lib.lns_upload_buffer2d(None, None) == 1
 
 
 def test_batch3d_argument_errors(lib):
