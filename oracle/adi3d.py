@@ -17,7 +17,8 @@ class A3Grid(ctypes.Structure):
                 ("loctime", I), ("xper", I), ("yper", I), ("navier", I), ("wall", I), ("wallt", I), ("top", I),
                 ("optx", I), ("opty", I)] + [(k, P) for k in
                                              ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")] + \
-        [("resacc", P), ("ispg", I), ("spg", P), ("spg2", P), ("eps_e", D), ("buff", P)]
+        [("resacc", P), ("ispg", I), ("spg", P), ("spg2", P), ("eps_e", D), ("buff", P), ("vm", P), ("xc", P),
+         ("wamp", P), ("x0", D), ("cvic", P)]
 
 
 class A3Ops(ctypes.Structure):
@@ -57,11 +58,13 @@ class Oracle3D:
     """Holds the oracle's grid struct, operators and factor arrays for one case."""
 
     def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, res_compat=False, ispg=0, spg=None,
-                 spg2=None, eps_e=0.0, buff=None):
+                 spg2=None, eps_e=0.0, buff=None, x0=0.0, wamp=None, cvic=None):
         """ispg, spg, spg2: the sponge (0 none, 1 spg, > 4 spg + spg2), spg
         and spg2 (nx, ny) as the reference's sponge setup leaves them.
         eps_e, buff: the explicit smoother and implicit damping, buff (nx, ny)
-        (ones, the reference's ibuff = 0, when None)."""
+        (ones, the reference's ibuff = 0, when None).  The inflow sponges
+        (ispg 2, 3) use the case's x coordinates, x0 and (ispg 3) wamp (nx);
+        the eigenfunction sponge (ispg 4) its target cvic, complex (5, nx, ny)."""
         self.L = _lib(lib)
         self.case = case
         p = case["params"]
@@ -82,6 +85,12 @@ class Oracle3D:
             self.spg2 = np.asfortranarray(spg2 if spg2 is not None else np.zeros((nx, ny)),
                                           dtype=np.float64).reshape((nx, ny), order="F")
             self.g.ispg, self.g.spg, self.g.spg2 = ispg, ptr(self.spg).value, ptr(self.spg2).value
+            self._vm = np.asfortranarray(case["vm"], dtype=np.float64)
+            self._xc = np.asfortranarray(case["x"], dtype=np.float64)
+            self._wamp = np.ascontiguousarray(wamp if wamp is not None else np.ones(nx), dtype=np.float64)
+            self._cvic = np.asfortranarray(cvic if cvic is not None else np.zeros((5, nx, ny)), dtype=np.complex128)
+            self.g.vm, self.g.xc, self.g.wamp = ptr(self._vm).value, ptr(self._xc).value, ptr(self._wamp).value
+            self.g.x0, self.g.cvic = x0, ptr(self._cvic).value
         if eps_e:
             self.buff = np.asfortranarray(buff if buff is not None else np.ones((nx, ny)),
                                           dtype=np.float64).reshape((nx, ny), order="F")

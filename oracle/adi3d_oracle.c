@@ -435,6 +435,35 @@ double a3_set_time_step(const A3Grid* g, const double* vl, double* dtl) {
 #define CIM(a, k, g, i, j) (a)[2 * ((long)(k) + 5 * IX(g, i, j)) + 1]
 
 /* src/lrhs3d.f90:33-218 (ispg 0, eps_e 0) */
+/* The target of the inflow sponge at point (i, j), complex (5): with
+   cm = sqrt(T)/Ma, um = U of the mean flow, d = (4/3 + (gamma-1)/Pr)/(2 Re),
+   kk = omega/(cm + um), a = omega^2 d/(cm + um)^3 and
+   c3 = [wamp(i)] exp(-a (x - x0)) exp(i kk x) (wamp for ispg 3 only):
+   (c3/(2 cm^2), c3/(2 rho cm), 0, 0,
+    (gamma Ma^2 c3/2 - T c3/(2 cm^2))/rho), src/lrhs3d.f90:248-278, in the
+   reference's order of operations. */
+void a3_inflow_target(const A3Grid* g, int i, int j, double t[10]) {
+  const long p = IX(g, i, j);
+  const double* vm = g->vm + 5 * p;
+  const double onept33 = 1.3333333333333333333e+0;
+  const double cm = sqrt(vm[4]) / g->Ma, um = vm[1];
+  const double d = pt5 * (onept33 + g->gamma1 / g->Pr) / g->Re;
+  const double kk = g->omega / (cm + um);
+  const double cu = cm + um;
+  const double a = g->omega * g->omega * d / (cu * cu * cu);
+  const double xl = g->xc[p];
+  const double e = exp(-a * (xl - g->x0));
+  const double w = g->ispg == 3 ? g->wamp[i - 1] * e : e;
+  const double c3r = w * cos(kk * xl), c3i = w * sin(kk * xl);
+  const double cm2 = cm * cm;
+  t[0] = pt5 * c3r / cm2, t[1] = pt5 * c3i / cm2;
+  t[2] = c3r * pt5 / (vm[0] * cm), t[3] = c3i * pt5 / (vm[0] * cm);
+  t[4] = t[5] = t[6] = t[7] = zero;
+  const double gm2 = g->gamma * (g->Ma * g->Ma);
+  t[8] = (gm2 * c3r * pt5 - vm[4] * pt5 * c3r / cm2) / vm[0];
+  t[9] = (gm2 * c3i * pt5 - vm[4] * pt5 * c3i / cm2) / vm[0];
+}
+
 /* smoother3D, src/smoother3d.f90:1-200 without symmetry planes (lsym and
    rsym false): rl += eps_e buff D(vl), the eta pass first (rows 2 and ny-1
    second order, 3 and ny-2 fourth order, 4..ny-3 sixth order), then the xi
@@ -470,7 +499,6 @@ static void a3_smoother(const A3Grid* g, double* rl, const double* vl) {
 int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
   const int nx = g->nx, ny = g->ny;
   const long n10 = 10L * nx * ny;
-  if (g->ispg >= 2 && g->ispg <= 4) return 1; /* inflow sponges and cspg_it: not restated */
   double* c1v = (double*)calloc(n10, sizeof(double));
   double* c2v = (double*)calloc(n10, sizeof(double));
   double* c11v = (double*)calloc(n10, sizeof(double));
@@ -556,6 +584,13 @@ int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
       if (g->ispg == 1 || g->ispg > 4) {
         const double sp = g->ispg == 1 ? g->spg[p] : g->spg[p] + g->spg2[p];
         for (int k = 0; k < 10; ++k) rl[k + 10 * p] = rl[k + 10 * p] + sp * vl[k + 10 * p];
+      } else if (g->ispg == 2 || g->ispg == 3) {
+        /* the outflow sponge spg on v, then the inflow sponge spg2 towards
+           the decaying wave c3 (src/lrhs3d.f90:242-280) */
+        for (int k = 0; k < 10; ++k) rl[k + 10 * p] = rl[k + 10 * p] + g->spg[p] * vl[k + 10 * p];
+        double t[10];
+        a3_inflow_target(g, i, j, t);
+        for (int k = 0; k < 10; ++k) rl[k + 10 * p] = rl[k + 10 * p] + g->spg2[p] * (vl[k + 10 * p] - t[k]);
       }
 #undef C1
 #undef C2
@@ -563,6 +598,11 @@ int a3_lrhs(const A3Grid* g, const A3Ops* o, const double* vl, double* rl) {
 #undef R
     }
   free(c1v); free(c2v); free(c11v); free(c12v); free(c22v);
+  if (g->ispg == 4) /* cspg_it, src/sponge.f90:596-604 */
+    for (long p = 0; p < (long)nx * ny; ++p) {
+      const double sp = g->spg[p] + g->spg2[p];
+      for (int k = 0; k < 10; ++k) rl[k + 10 * p] = rl[k + 10 * p] + sp * (vl[k + 10 * p] - g->cvic[k + 10 * p]);
+    }
   if (g->eps_e != zero) a3_smoother(g, rl, vl); /* src/lrhs3d.f90:294 */
   return 0;
 }

@@ -55,6 +55,13 @@ typedef struct {
      277-298, 431-452): eps_e and buff(nx,ny); eps_e = 0 turns both off */
   double eps_e;
   const double* buff;
+  /* inflow sponges (src/lrhs3d.f90:242-280): the mean flow vm(5,nx,ny), the
+     x coordinates x(nx,ny), x0 and (ispg 3) wamp(nx); the eigenfunction
+     sponge (ispg 4, src/sponge.f90:536-607): its target cvic, complex
+     (5,nx,ny) */
+  const double *vm, *xc, *wamp;
+  double x0;
+  const double* cvic;
 } A3Grid;
 
 /* Frozen operators of the linear step (outputs of genmtrx(vm, kz, vm)). */
@@ -74,6 +81,8 @@ int a3_genmtrx(const A3Grid* g, const double* vm, A3Ops* ops);
 double a3_set_time_step(const A3Grid* g, const double* vm, double* dtl);
 /* r = L(v) (lrhs3D), then r = vold - v - dtl r (rbe3D) */
 int a3_lrhs(const A3Grid* g, const A3Ops* ops, const double* v, double* r);
+/* the inflow sponge's target at (i, j), complex (5) as 10 doubles */
+void a3_inflow_target(const A3Grid* g, int i, int j, double t[10]);
 void a3_rbe(const A3Grid* g, double* r, const double* v, const double* vold, const double* dtl);
 void a3_rhsbc(const A3Grid* g, double* r, const double* v);
 double a3_resstat(const A3Grid* g, const double* r, const double* dtl);

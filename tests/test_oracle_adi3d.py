@@ -249,3 +249,49 @@ def test_smoother_keeps_steps_stable():
     v = case["v"].copy(order="F")
     res = [o.step(v) for _ in range(6)]
     assert np.isfinite(v).all() and all(np.isfinite(res))
+
+
+@pytest.mark.parametrize("ispg", [2, 3, 4])
+def test_target_sponges_known_answer(ispg):
+    """The inflow sponges (ispg 2, 3; src/lrhs3d.f90:242-280): r += spg v +
+    spg2 (v - t) with t the decaying wave c3 = [wamp] exp(-a (x - x0))
+    exp(i kk x) mapped to (rho, u, v, w, T); the eigenfunction sponge (ispg 4,
+    src/sponge.f90:596-604): r += (spg + spg2)(v - cvic).  The eta LHS gains
+    alfa dtl (spg + spg2) on its diagonal for all three."""
+    from adi3dcase import sponge
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 24, 20
+    case = shear_layer(nx=nx, ny=ny, seed=1)
+    spg, spg2 = sponge(nx, ny)
+    rng = np.random.default_rng(9)
+    wamp = rng.uniform(0.5, 1.5, nx)
+    cvic = np.asfortranarray(rng.standard_normal((5, nx, ny)) + 1j * rng.standard_normal((5, nx, ny)))
+    plain = Oracle3D(case, cflmax=20.0, loctime=1)
+    o = Oracle3D(case, cflmax=20.0, loctime=1, ispg=ispg, spg=spg, spg2=spg2, x0=-1.0, wamp=wamp, cvic=cvic)
+    v = np.asfortranarray(rng.standard_normal((5, nx, ny)) + 1j * rng.standard_normal((5, nx, ny)))
+    if ispg == 4:
+        want = plain.lrhs(v) + (spg + spg2)[None] * (v - cvic)
+    else:
+        p = case["params"]
+        vm, x = case["vm"], case["x"]
+        cm = np.sqrt(vm[4]) / p["Ma"]
+        um = vm[1]
+        d = 0.5 * (1.3333333333333333333 + p["gamma1"] / p["Pr"]) / p["Re"]
+        kk = p["omega"] / (cm + um)
+        a = p["omega"] ** 2 * d / (cm + um) ** 3
+        c3 = np.exp(-a * (x + 1.0)) * np.exp(1j * kk * x)
+        if ispg == 3:
+            c3 = wamp[:, None] * c3
+        t = np.zeros_like(v)
+        t[0] = 0.5 * c3 / cm ** 2
+        t[1] = c3 * 0.5 / (vm[0] * cm)
+        t[4] = (p["gamma"] * p["Ma"] ** 2 * c3 * 0.5 - vm[4] * 0.5 * c3 / cm ** 2) / vm[0]
+        want = (plain.lrhs(v) + spg[None] * v) + spg2[None] * (v - t)
+    got = o.lrhs(v)
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+    dm = o.lhs(2) - plain.lhs(2)
+    w = case["params"]["alfa"] * o.dtl * (spg + spg2)
+    for a_ in range(5):
+        assert np.abs(dm[2, a_, a_, :, 1:-1] - w[:, 1:-1]).max() <= 4e-16 * np.abs(plain.lhs(2)).max()
+    assert np.array_equal(o.lhs(1), plain.lhs(1))
