@@ -339,12 +339,14 @@ typedef struct {
                                 operator at (v + vold)/2 with alfa = 1/2.  Steps
                                 are counted from the context's creation (a fresh
                                 run, lstep = 0).  Batches and servers take 1. */
-  int32_t ispg;              /* sponge (src/lrhs3d.f90:220-240, src/lhs2f3d.f90:207-224,
-                                src/lhsbt2f3d.f90:147-167): 0 none; 1 r += spg v and
-                                alfa dtl spg on the diagonal of the eta LHS; > 4 the same
-                                with spg + spg2.  The inflow sponges 2, 3 and the
-                                iterated sponge 4 are not supported.  Batches and servers
-                                take 0. */
+  int32_t ispg;              /* sponge (src/lrhs3d.f90:220-280, src/sponge.f90:536-607,
+                                src/lhs2f3d.f90:207-224, src/lhsbt2f3d.f90:147-167): 0 none;
+                                1 r += spg v and alfa dtl spg on the diagonal of the eta LHS;
+                                > 4 the same with spg + spg2; 2, 3 r += spg v + spg2 (v - t)
+                                towards the decaying inflow wave t (lns_upload_inflow3d; 3
+                                scales it by wamp(i)); 4 r += (spg + spg2)(v - cvic)
+                                (lns_upload_sponge_target3d).  2-4 put alfa dtl (spg + spg2)
+                                on the LHS diagonal.  Batches and servers take 0. */
   double eps_e;              /* explicit smoother (src/smoother3d.f90, at the end of lrhs3D)
                                 and implicit damping of both LHS (src/lhs1f3d.f90:168-200,
                                 src/lhs2f3d.f90:171-203, src/lhsbt2f3d.f90:277-298,
@@ -369,6 +371,13 @@ int lns_upload_metrics3d(lns_ctx3d* ctx, const double* metrics);
  * host's sponge setup (src/sponge.f90) leaves them; needed before the first
  * step when ispg != 0; invalidates the factored LHS. */
 int lns_upload_sponge3d(lns_ctx3d* ctx, const double* spg, const double* spg2);
+/* ispg 2, 3: the x coordinates x(nx,ny), the inflow station x0 and (ispg 3)
+ * the amplitudes wamp(nx) of the inflow sponge's wave (src/lrhs3d.f90:242-
+ * 268); its target is formed on the device from these and the mean flow. */
+int lns_upload_inflow3d(lns_ctx3d* ctx, const double* x, const double* wamp, double x0);
+/* ispg 4: the eigenfunction target cvic, complex (5,nx,ny) as interleaved
+ * doubles (src/sponge.f90:558-579). */
+int lns_upload_sponge_target3d(lns_ctx3d* ctx, const double* cvic);
 /* The smoother weight buff(nx,ny) of the host's buffer setup (src/buffer.f90,
  * ibuff > 0); only for eps_e != 0; invalidates the factored LHS. */
 int lns_upload_buffer3d(lns_ctx3d* ctx, const double* buff);

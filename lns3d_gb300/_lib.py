@@ -66,6 +66,8 @@ SIGNATURES = {
     "lns_ctx3d_destroy": [P],
     "lns_upload_metrics3d": [P, DP],
     "lns_upload_sponge3d": [P, DP, DP],
+    "lns_upload_inflow3d": [P, DP, DP, ctypes.c_double],
+    "lns_upload_sponge_target3d": [P, DP],
     "lns_upload_buffer3d": [P, DP],
     "lns_upload_sponge2d": [P, DP, DP],
     "lns_upload_buffer2d": [P, DP],

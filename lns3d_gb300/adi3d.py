@@ -48,11 +48,14 @@ class ImpDrv3D:
     corrector's own.  ispg, spg, spg2: the sponge (0 none, 1 spg, > 4
     spg + spg2; src/lrhs3d.f90:220-240), spg and spg2 (nx, ny) arrays.
     eps_e, buff: explicit smoother and implicit damping (src/smoother3d.f90),
-    buff (nx, ny) or None for the reference's default of ones.
+    buff (nx, ny) or None for the reference's default of ones.  ispg 2, 3
+    take the x coordinates x (nx, ny), x0 and (3) wamp (nx); ispg 4 the
+    complex target cvic (5, nx, ny).
     """
 
     def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False,
-                 impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None):
+                 impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None, x=None, x0=0.0, wamp=None,
+                 cvic=None):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -74,6 +77,16 @@ class ImpDrv3D:
             check(lib().lns_upload_sponge3d(self._ctx, ctypes.c_void_p(s1.ctypes.data),
                                             ctypes.c_void_p(s2.ctypes.data) if s2 is not None else None),
                   "lns_upload_sponge3d")
+        if ispg in (2, 3):
+            xx = np.asfortranarray(x, dtype=np.float64)
+            wa = np.ascontiguousarray(wamp, dtype=np.float64) if wamp is not None else None
+            check(lib().lns_upload_inflow3d(self._ctx, ctypes.c_void_p(xx.ctypes.data),
+                                            ctypes.c_void_p(wa.ctypes.data) if wa is not None else None, x0),
+                  "lns_upload_inflow3d")
+        if ispg == 4:
+            cv = np.asfortranarray(cvic, dtype=np.complex128)
+            check(lib().lns_upload_sponge_target3d(self._ctx, ctypes.c_void_p(cv.ctypes.data)),
+                  "lns_upload_sponge_target3d")
         if eps_e and buff is not None:
             b = np.asfortranarray(buff, dtype=np.float64)
             check(lib().lns_upload_buffer3d(self._ctx, ctypes.c_void_p(b.ctypes.data)), "lns_upload_buffer3d")

@@ -363,6 +363,36 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
   store_el(mat, q, lhs_entry(g, o, dir, p, k, a, b, ak, bk, combined, damp));
 }
 
+// The inflow sponge's target (ispg 2, 3; src/lrhs3d.f90:242-280) at every
+// point from the mean flow vm, the x coordinates and x0, wamp (ispg 3):
+// c3 = [wamp(i)] exp(-a (x - x0)) exp(i kk x), cm = sqrt(T)/Ma,
+// kk = omega/(cm + u), a = omega^2 d/(cm + u)^3, d = (4/3 + (gamma-1)/Pr)/(2 Re);
+// t = (c3/(2 cm^2), c3/(2 rho cm), 0, 0, (gamma Ma^2 c3/2 - T c3/(2 cm^2))/rho)
+__global__ void inflow_target_kernel(Grid g, int ispg, const double* __restrict__ vm, const double* __restrict__ xc,
+                                     const double* __restrict__ wamp, double x0, cd* __restrict__ vt) {
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= (long long)g.nx * g.ny) return;
+  const int i = (int)(p % g.nx) + 1;
+  const double* m = vm + 5 * p;
+  const double cm = sqrt(m[4]) / g.Ma, um = m[1];
+  const double d = 0.5 * (1.3333333333333333333e+0 + g.gamma1 / g.Pr) / g.Re;
+  const double cu = cm + um;
+  const double kk = g.omega / cu;
+  const double a = g.omega * g.omega * d / (cu * cu * cu);
+  const double xl = xc[p];
+  const double e = exp(-a * (xl - x0));
+  const double w = ispg == 3 ? wamp[i - 1] * e : e;
+  double sn, cs;
+  sincos(kk * xl, &sn, &cs);
+  const double c3r = w * cs, c3i = w * sn;
+  const double cm2 = cm * cm, gm2 = g.gamma * (g.Ma * g.Ma);
+  vt[5 * p + 0] = cd{0.5 * c3r / cm2, 0.5 * c3i / cm2};
+  vt[5 * p + 1] = cd{c3r * 0.5 / (m[0] * cm), c3i * 0.5 / (m[0] * cm)};
+  vt[5 * p + 2] = cd{0.0, 0.0};
+  vt[5 * p + 3] = cd{0.0, 0.0};
+  vt[5 * p + 4] = cd{(gm2 * c3r * 0.5 - m[4] * 0.5 * c3r / cm2) / m[0], (gm2 * c3i * 0.5 - m[4] * 0.5 * c3i / cm2) / m[0]};
+}
+
 // -------------------------------------------------------------------- RHS
 // c1v = d v / d xi (complex); (bx, by) is the block within the problem
 __device__ __forceinline__ void grad1_body(const Grid& g, const cd* __restrict__ v, cd* __restrict__ c1v, int bx,
@@ -451,8 +481,18 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
         subi(r[2], a2 * c1b.x + a4 * c2b.x, a2 * c1b.y + a4 * c2b.y);
       }
     }
-    // sponge, src/lrhs3d.f90:222-240: r = r + spg v on the operator's field
-    if (o.spg) {
+    // sponge, src/lrhs3d.f90:222-280 and src/sponge.f90:596-604: r = r +
+    // spg v, or the target sponges, on the operator's field
+    if (o.spg_b) {
+      const double sa = o.spg_a ? o.spg_a[p] : 0.0, sb = o.spg_b[p];
+      const cd* T = reinterpret_cast<const cd*>(o.vt) + 5 * p;
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const cd vm = v[m + 5 * p], tm = T[m];
+        if (o.spg_a) r[m] = cd{r[m].x + sa * vm.x, r[m].y + sa * vm.y};
+        r[m] = cd{r[m].x + sb * (vm.x - tm.x), r[m].y + sb * (vm.y - tm.y)};
+      }
+    } else if (o.spg) {
       const double sp = o.spg[p];
       #pragma unroll
       for (int m = 0; m < 5; ++m) {
@@ -725,7 +765,11 @@ struct lns_ctx3d {
   int* status = nullptr;
   bool have_metrics = false, have_mean = false, factored = false;
   bool have_sponge = false;   // ispg != 0: lns_upload_sponge3d called
-  double* spg = nullptr;      // spg, or spg + spg2 (ispg > 4)
+  double* spg = nullptr;      // spg (ispg 1), else spg + spg2
+  double *spg_a = nullptr, *spg_b = nullptr, *vt = nullptr;  // the target sponges (ispg 2-4)
+  double *xc = nullptr, *wamp = nullptr;  // ispg 2, 3: x(nx,ny), wamp(nx)
+  double x0 = 0.0;
+  bool have_inflow = false, have_target = false;
   double* buff = nullptr;     // eps_e != 0: buff(nx,ny), ones until uploaded
   // time scheme (src/impdrv3d.f90:130-199): the previous-previous state
   // (impl 2), the averaged field (impl 3), steps taken, alfa of the factors
@@ -1046,8 +1090,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->impl < 0 || p->impl > 3) return fail3(LNS_ERR_ARG, "ctx3d_create: impl must be 1, 2 or 3 (0 means 1)");
   if (!(p->eps_e >= 0.0) || !std::isfinite(p->eps_e))
     return fail3(LNS_ERR_ARG, "ctx3d_create: eps_e must be finite and >= 0");
-  if (p->ispg < 0 || (p->ispg >= 2 && p->ispg <= 4))
-    return fail3(LNS_ERR_ARG, "ctx3d_create: ispg must be 0, 1 or > 4 (the inflow sponges 2-4 are not supported)");
+  if (p->ispg < 0) return fail3(LNS_ERR_ARG, "ctx3d_create: ispg must be >= 0");
   lns_ctx3d* c = new lns_ctx3d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);
@@ -1085,6 +1128,15 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->impl == 2) { A(sizeof(cd) * 5 * np, &q); c->v2old = (cd*)q; }
   if (p->impl == 3) { A(sizeof(cd) * 5 * np, &q); c->wavg = (cd*)q; }
   if (p->ispg != 0) { A(sizeof(double) * np, &q); c->spg = (double*)q; }
+  if (p->ispg >= 2 && p->ispg <= 4) {
+    A(sizeof(double) * np, &q); c->spg_b = (double*)q;
+    A(sizeof(double) * 10 * np, &q); c->vt = (double*)q;
+  }
+  if (p->ispg == 2 || p->ispg == 3) {
+    A(sizeof(double) * np, &q); c->spg_a = (double*)q;
+    A(sizeof(double) * np, &q); c->xc = (double*)q;
+    A(sizeof(double) * p->nx, &q); c->wamp = (double*)q;
+  }
   if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
@@ -1154,7 +1206,22 @@ int need_data(const lns_ctx3d* c, const char* who) {
   if (!c->have_mean) return fail3(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the mean flow first");
   if (c->prm.ispg != 0 && !c->have_sponge)
     return fail3(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
+  if ((c->prm.ispg == 2 || c->prm.ispg == 3) && !c->have_inflow)
+    return fail3(LNS_ERR_ARG, std::string(who) + ": ispg 2, 3: upload the inflow data (lns_upload_inflow3d) first");
+  if (c->prm.ispg == 4 && !c->have_target)
+    return fail3(LNS_ERR_ARG, std::string(who) + ": ispg 4: upload the sponge target (lns_upload_sponge_target3d) first");
   return LNS_OK;
+}
+
+// the inflow sponge's target, once the mean flow and the inflow data are in
+int make_inflow_target(lns_ctx3d* c) {
+  if (!(c->prm.ispg == 2 || c->prm.ispg == 3) || !c->have_inflow || !c->have_mean) return LNS_OK;
+  const long long np = c->np;
+  lns::a3::inflow_target_kernel<<<(unsigned)((np + 255) / 256), 256>>>(c->g, c->prm.ispg, c->vm, c->xc, c->wamp,
+                                                                       c->x0, reinterpret_cast<cd*>(c->vt));
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "inflow_target_kernel");
 }
 }  // namespace
 
@@ -1163,19 +1230,52 @@ extern "C" {
 int lns_upload_sponge3d(lns_ctx3d* c, const double* spg, const double* spg2) {
   if (!c || !spg) return fail3(LNS_ERR_ARG, "upload_sponge3d: null argument");
   if (c->prm.ispg == 0) return fail3(LNS_ERR_ARG, "upload_sponge3d: the context was created with ispg = 0");
-  if (c->prm.ispg > 4 && !spg2) return fail3(LNS_ERR_ARG, "upload_sponge3d: ispg > 4 needs spg2");
+  if (c->prm.ispg > 1 && !spg2) return fail3(LNS_ERR_ARG, "upload_sponge3d: ispg > 1 needs spg2");
   int rc = check_device(c);
   if (rc) return rc;
-  // the double sponge enters the RHS and the LHS only as spg + spg2
-  // (src/lrhs3d.f90:232-240, src/lhs2f3d.f90:217-224): add once here
+  // the LHS (src/lhs2f3d.f90:207-224) and the double sponge's RHS
+  // (src/lrhs3d.f90:232-240) use spg + spg2, the eigenfunction sponge's RHS
+  // too (src/sponge.f90:600): add once here
   std::vector<double> h(spg, spg + c->np);
-  if (c->prm.ispg > 4)
+  if (c->prm.ispg > 1)
     for (long long k = 0; k < c->np; ++k) h[k] = spg[k] + spg2[k];
   cudaError_t e = cudaMemcpy(c->spg, h.data(), sizeof(double) * c->np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && c->spg_a) e = cudaMemcpy(c->spg_a, spg, sizeof(double) * c->np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && c->spg_b)
+    e = cudaMemcpy(c->spg_b, c->spg_a ? spg2 : h.data(), sizeof(double) * c->np, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda3(e, "upload sponge");
   c->ops.spg = c->spg;
+  c->ops.spg_a = c->spg_a;
+  c->ops.spg_b = c->spg_b;
+  c->ops.vt = c->vt;
   c->have_sponge = true;
   c->factored = false;
+  return LNS_OK;
+}
+
+int lns_upload_inflow3d(lns_ctx3d* c, const double* x, const double* wamp, double x0) {
+  if (!c || !x) return fail3(LNS_ERR_ARG, "upload_inflow3d: null argument");
+  if (c->prm.ispg != 2 && c->prm.ispg != 3) return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3");
+  if (c->prm.ispg == 3 && !wamp) return fail3(LNS_ERR_ARG, "upload_inflow3d: ispg 3 needs wamp");
+  if (!std::isfinite(x0)) return fail3(LNS_ERR_ARG, "upload_inflow3d: x0 must be finite");
+  int rc = check_device(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->xc, x, sizeof(double) * c->np, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && wamp) e = cudaMemcpy(c->wamp, wamp, sizeof(double) * c->g.nx, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload inflow data");
+  c->x0 = x0;
+  c->have_inflow = true;
+  return make_inflow_target(c);
+}
+
+int lns_upload_sponge_target3d(lns_ctx3d* c, const double* cvic) {
+  if (!c || !cvic) return fail3(LNS_ERR_ARG, "upload_sponge_target3d: null argument");
+  if (c->prm.ispg != 4) return fail3(LNS_ERR_ARG, "upload_sponge_target3d: needs ispg 4");
+  int rc = check_device(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->vt, cvic, sizeof(double) * 10 * c->np, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload sponge target");
+  c->have_target = true;
   return LNS_OK;
 }
 
@@ -1224,7 +1324,7 @@ int lns_upload_mean3d(lns_ctx3d* c, const double* vm, double* cfl) {
   if (cfl) *cfl = h;
   c->have_mean = true;
   c->factored = false;
-  return LNS_OK;
+  return make_inflow_target(c);
 }
 
 int lns_step3d_dev(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream) {

@@ -60,6 +60,12 @@ struct Ops {
   // the sponge coefficient (nx,ny): spg, or spg + spg2 for the double
   // sponge; null without a sponge
   const double* spg = nullptr;
+  // the target sponges: ispg 2, 3 r += spg_a v + spg_b (v - vt) (spg_a = spg,
+  // spg_b = spg2); ispg 4 r += spg_b (v - vt) (spg_b = spg + spg2); vt is
+  // the complex target (5,nx,ny) as interleaved doubles
+  const double* spg_a = nullptr;
+  const double* spg_b = nullptr;
+  const double* vt = nullptr;
   // explicit smoother / implicit damping: eps_e buff(nx,ny); null when eps_e = 0
   const double* buff = nullptr;
   double eps_e = 0.0;

@@ -120,7 +120,7 @@ def _params3d(**kw):
 
 @pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=0), dict(wallt=2),
                                  dict(top=1), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
-                                 dict(loctime=2), dict(ispg=2), dict(ispg=4), dict(ispg=-1),
+                                 dict(loctime=2), dict(ispg=-1),
                                  dict(eps_e=-1.0), dict(eps_e=float("nan"))])
 def test_ctx3d_rejects_unsupported_options(lib, bad):
     ctx = ctypes.c_void_p()
@@ -144,6 +144,8 @@ def test_ctx3d_null_arguments(lib):
     assert lib.lns_ctx3d_profile_read(None, None, None) == 1
     assert lib.lns_upload_sponge3d(None, None, None) == 1
     assert lib.lns_upload_buffer3d(None, None) == 1
+    assert lib.lns_upload_inflow3d(None, None, None, 0.0) == 1
+    assert lib.lns_upload_sponge_target3d(None, None) == 1
 
 
 def _params2d(**kw):

@@ -461,3 +461,54 @@ def test_smoother_default_buffer_is_ones(cuda):
     a.step(va, nsteps=3)
     b.step(vb, nsteps=3)
     assert np.array_equal(va, vb)
+
+
+@pytest.mark.parametrize("ispg", [2, 3, 4])
+def test_target_sponges_match_oracle(cuda, ispg):
+    """The inflow sponges (ispg 2, 3: the target wave formed on the device
+    from the mean flow, x, x0 and wamp; src/lrhs3d.f90:242-280) and the
+    eigenfunction sponge (ispg 4, src/sponge.f90:596-604): RHS, eta LHS and
+    steps against the oracle."""
+    import ctypes
+
+    import torch
+    from adi3dcase import _lib, ptr, sponge
+
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 40, 33
+    case = shear_layer(nx=nx, ny=ny, seed=11)
+    spg, spg2 = sponge(nx, ny, amp=1.0)
+    rng = np.random.default_rng(14)
+    wamp = rng.uniform(0.5, 1.5, nx)
+    cvic = np.asfortranarray(1e-3 * (rng.standard_normal((5, nx, ny)) + 1j * rng.standard_normal((5, nx, ny))))
+    kw = dict(ispg=ispg, spg=spg, spg2=spg2, x0=-1.0, wamp=wamp, cvic=cvic)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1, **kw)
+    mk = lambda: ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, x=case["x"], **kw)
+    drv = mk()
+    mat = torch.zeros(125 * nx * ny, dtype=torch.complex128, device="cuda")
+    drv.lhs(2, mat)
+    torch.cuda.synchronize()
+    assert rel(mat.cpu().numpy().reshape((5, 5, 5, nx, ny), order="F"), orc.lhs(2)) < OPS_TOL
+    shape = (5, nx, ny)
+    v = np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    vold = np.asfortranarray(v + 1e-3 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    L = _lib()
+    r = orc.lrhs(v)
+    L.a3_rbe(ctypes.byref(orc.g), ptr(r), ptr(v), ptr(vold), ptr(orc.dtl))
+    L.a3_rhsbc(ctypes.byref(orc.g), ptr(r), ptr(v))
+    dev = lambda a: torch.from_numpy(a.ravel(order="F")).cuda()
+    dv, dvo = dev(v), dev(vold)
+    dr = torch.zeros_like(dv)
+    drv.rhs(dv, dvo, dr, torch.zeros(1, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    assert rel(dr.cpu().numpy().reshape(shape, order="F"), r) < RHS_TOL
+    drv = mk()
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    for s in range(4):
+        res_ref = orc.step(v_ref)
+        res_gpu = drv.step(v_gpu, nsteps=1)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
