@@ -291,8 +291,7 @@ __device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, lo
   // src/lhs2f3d.f90:171-203), 2 the eta rows 2 and ny-1, (-1, 2, -1) in
   // slots 2..4 (src/lhsbt2f3d.f90:277-298, 431-452), 1 none (rows 1, ny)
   if (o.buff && a == b && damp != 1) {
-    const double fb[5] = {1.0, -4.0, 6.0, -4.0, 1.0}, sb[5] = {0.0, -1.0, 2.0, -1.0, 0.0};
-    const double c = damp == 0 ? fb[k - 1] : sb[k - 1];
+    const double c = damp == 0 ? pick5(k - 1, 1.0, -4.0, 6.0, -4.0, 1.0) : pick5(k - 1, 0.0, -1.0, 2.0, -1.0, 0.0);
     if (c != 0.0) re = re + g.alfa * d * o.eps_e * o.buff[p] * c;
   }
   // sponge of the eta LHS (src/lhs2f3d.f90:207-224, src/lhsbt2f3d.f90:147-167;
@@ -323,11 +322,10 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
   if (!g.yper && g.navier && j == 1) {
     if (dir == 1) return store_el(mat, q, ident);  // src/lhsbc1f3d.f90:24-45
     // src/lhsbc2f3d.f90:24-66: continuity / temperature rows in slots 3,4,5,1,2
-    const double gcs[5] = {gc1, gc2, gc3, gc4, gc5};
     const int tk = (k + 2) % 5;  // coefficient of slot k: slots 3,4,5,1,2 <-> 0..4
     if (a >= 2 && a <= 4) return store_el(mat, q, ident);
     if ((a == 1 && g.wall == 1) || (a == 5 && g.wallt == 1))
-      return store_el(mat, q, b == a ? cd{-gcs[tk], 0.0} : zero);
+      return store_el(mat, q, b == a ? cd{-pick5(tk, gc1, gc2, gc3, gc4, gc5), 0.0} : zero);
     if (a == 5 && g.wallt == 0) return store_el(mat, q, ident);
   }
   const double h = dir == 1 ? g.dxi : g.deta, alfa = g.alfa;
@@ -336,27 +334,28 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
   double ak, bk;
   bool combined = false;
   if (per || (pos > 2 && pos < n - 1)) {
-    const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
-    ak = alfa * gi[k - 1] / h;
-    bk = alfa * di[k - 1] / (h * h);
+    ak = alfa * pick5(k - 1, ga1, ga2, 0.0, ga3, ga4) / h;
+    bk = alfa * pick5(k - 1, da1, da2, da3, da4, da5) / (h * h);
   } else {
     // boundary rows j = 1, 2, ny-1, ny (src/lhsbt2f3d.f90:36-600): coefficient t of slot k
     const double hinv = 1.0 / h, hsinv = 1.0 / (h * h);
-    const double g1[5] = {gc1, gc2, gc3, gc4, gc5}, d1[5] = {dd1, dd2, dd3, dd4, dd5};
-    const double g2[5] = {gb1, gb2, gb3, gb4, gb5}, d2[5] = {db1, db2, db3, db4, db5};
+    auto g1 = [](int t) { return pick5(t, gc1, gc2, gc3, gc4, gc5); };
+    auto d1 = [](int t) { return pick5(t, dd1, dd2, dd3, dd4, dd5); };
+    auto g2 = [](int t) { return pick5(t, gb1, gb2, gb3, gb4, gb5); };
+    auto d2 = [](int t) { return pick5(t, db1, db2, db3, db4, db5); };
     combined = true;
     if (pos == 1) {  // slots 3,4,5,1,2
       const int t = (k + 2) % 5;
-      ak = alfa * g1[t] * hinv, bk = alfa * d1[t] * hsinv;
+      ak = alfa * g1(t) * hinv, bk = alfa * d1(t) * hsinv;
     } else if (pos == 2) {  // slots 2,3,4,5,1
       const int t = (k + 3) % 5;
-      ak = alfa * g2[t] * hinv, bk = alfa * d2[t] * hsinv;
+      ak = alfa * g2(t) * hinv, bk = alfa * d2(t) * hsinv;
     } else if (pos == n - 1) {  // slots 4,3,2,1,5
       const int t = k == 5 ? 4 : 4 - k;
-      ak = -(alfa * g2[t] * hinv), bk = alfa * d2[t] * hsinv;
+      ak = -(alfa * g2(t) * hinv), bk = alfa * d2(t) * hsinv;
     } else {  // slots 3,2,1,5,4
       const int t = k <= 3 ? 3 - k : 8 - k;
-      ak = -(alfa * g1[t] * hinv), bk = alfa * d1[t] * hsinv;
+      ak = -(alfa * g1(t) * hinv), bk = alfa * d1(t) * hsinv;
     }
   }
   const int damp = !combined ? 0 : (pos == 2 || pos == n - 1) ? 2 : 1;

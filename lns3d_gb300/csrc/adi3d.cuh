@@ -36,6 +36,12 @@ constexpr double dd1 = 2.916666666666666666667E+00, dd2 = -8.6666666666666666666
                  dd5 = 9.166666666666666666667E-01;
 constexpr double pt5 = 0.5, pt66 = 6.6666666666666666666e-1, two = 2.0, four = 4.0;
 
+// Entry t (0..4) of a five-coefficient stencil, as register selects: a
+// local array indexed by a thread-dependent t would live in local memory.
+__host__ __device__ __forceinline__ double pick5(int t, double a0, double a1, double a2, double a3, double a4) {
+  return t == 0 ? a0 : t == 1 ? a1 : t == 2 ? a2 : t == 3 ? a3 : a4;
+}
+
 struct Grid {
   int nx, ny;
   double dxi, deta;

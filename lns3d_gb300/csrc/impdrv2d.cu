@@ -462,18 +462,18 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
       if (a == 5 && (g.wallt == 0 || g.wallt == 1)) { mat[q] = ident; return; }
     } else {
       const int tk = (k + 2) % 5;  // coefficient of slot k: slots 3,4,5,1,2 <-> 0..4
-      const double gcs[5] = {gc1, gc2, gc3, gc4, gc5}, ex3[5] = {-1.0, 4.0, -6.0, 4.0, -1.0};
+      const double gct = pick5(tk, gc1, gc2, gc3, gc4, gc5), ext = pick5(tk, -1.0, 4.0, -6.0, 4.0, -1.0);
       if (a >= 2 && a <= 4) { mat[q] = ident; return; }
       // the second-order wall-3 row clears only mat(:,1,:,:,1) (columns 1
       // and 2): the blocks of columns 3..5 keep their closure entries off
       // the first column (src/lhsbc2.f90, wall = 3)
       const bool keep = order2 && g.wall == 3 && b != 1 && (k == 5 || k == 1 || k == 2);
       if (a == 1 && (g.wall == 1 || g.wall == 3) && !keep) {
-        mat[q] = b == 1 ? (g.wall == 1 ? -gcs[tk] : ex3[tk]) : 0.0;
+        mat[q] = b == 1 ? (g.wall == 1 ? -gct : ext) : 0.0;
         return;
       }
       if (a == 5 && g.wallt == 0) { mat[q] = -ident; return; }
-      if (a == 5 && g.wallt == 1) { mat[q] = b == 5 ? -gcs[tk] : 0.0; return; }
+      if (a == 5 && g.wallt == 1) { mat[q] = b == 5 ? -gct : 0.0; return; }
     }
   }
   // the far-field row j = ny
@@ -514,28 +514,30 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   } else if (order2 && !edge) {
     // rows 3 and ny-2: the central five-point stencil of lhsbt2 with a
     // literal zero diagonal block (src/lhsbt2.f90, rows 3 and ny-2)
-    const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
+    const double gik = pick5(k - 1, ga1, ga2, 0.0, ga3, ga4), dik = pick5(k - 1, da1, da2, da3, da4, da5);
     const double detainv = 1.0 / g.deta, detasinv = 1.0 / (g.deta * g.deta);
-    val = k == 3 ? 0.0 : alfa * d * gi[k - 1] * detainv * o.Bh[eab];
-    if (vk >= 0) val = val - alfa * d * di[k - 1] * detasinv * V[vk * np + p];
+    val = k == 3 ? 0.0 : alfa * d * gik * detainv * o.Bh[eab];
+    if (vk >= 0) val = val - alfa * d * dik * detasinv * V[vk * np + p];
   } else if (!edge) {
     const double h = dir == 1 ? g.dxi : g.deta;
-    const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
-    const double ak = alfa * gi[k - 1] / h, bk = alfa * di[k - 1] / (h * h);
+    const double ak = alfa * pick5(k - 1, ga1, ga2, 0.0, ga3, ga4) / h;
+    const double bk = alfa * pick5(k - 1, da1, da2, da3, da4, da5) / (h * h);
     val = ak * d * (dir == 1 ? o.Ah : o.Bh)[eab];
     if (dir == 1 && k == 3) val = val + alfa * d * o.Dh[eab];
     if (vk >= 0) val = val - bk * d * V[vk * np + p];
   } else {
     // rows 1, 2, ny-1, ny: coefficient t of slot k (src/lhsbt2f.f90)
     const double detainv = 1.0 / g.deta, detasinv = 1.0 / (g.deta * g.deta);
-    const double g1[5] = {gc1, gc2, gc3, gc4, gc5}, d1[5] = {dd1, dd2, dd3, dd4, dd5};
-    const double g2[5] = {gb1, gb2, gb3, gb4, gb5}, d2[5] = {db1, db2, db3, db4, db5};
+    auto g1 = [](int t) { return pick5(t, gc1, gc2, gc3, gc4, gc5); };
+    auto d1 = [](int t) { return pick5(t, dd1, dd2, dd3, dd4, dd5); };
+    auto g2 = [](int t) { return pick5(t, gb1, gb2, gb3, gb4, gb5); };
+    auto d2 = [](int t) { return pick5(t, db1, db2, db3, db4, db5); };
     double gcf, dcf;
     bool neg = false;
-    if (j == 1) { const int t = (k + 2) % 5; gcf = g1[t]; dcf = d1[t]; }
-    else if (j == 2) { const int t = (k + 3) % 5; gcf = g2[t]; dcf = d2[t]; }
-    else if (j == g.ny - 1) { const int t = k == 5 ? 4 : 4 - k; gcf = g2[t]; dcf = d2[t]; neg = true; }
-    else { const int t = k <= 3 ? 3 - k : 8 - k; gcf = g1[t]; dcf = d1[t]; neg = true; }
+    if (j == 1) { const int t = (k + 2) % 5; gcf = g1(t); dcf = d1(t); }
+    else if (j == 2) { const int t = (k + 3) % 5; gcf = g2(t); dcf = d2(t); }
+    else if (j == g.ny - 1) { const int t = k == 5 ? 4 : 4 - k; gcf = g2(t); dcf = d2(t); neg = true; }
+    else { const int t = k <= 3 ? 3 - k : 8 - k; gcf = g1(t); dcf = d1(t); neg = true; }
     val = alfa * d * gcf * detainv * o.Bh[eab];
     if (neg) val = -val;
     if (vk >= 0) val = val - alfa * d * dcf * detasinv * V[vk * np + p];
@@ -549,8 +551,7 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   if (!order2 && a == b && (o.buff || o.spg)) {
     const double wd = o.buff ? alfa * d * o.eps_e * o.buff[p] : 0.0;
     if (!edge) {
-      const double fb[5] = {1.0, -4.0, 6.0, -4.0, 1.0};
-      if (o.buff) val = val + wd * fb[k - 1];
+      if (o.buff) val = val + wd * pick5(k - 1, 1.0, -4.0, 6.0, -4.0, 1.0);
       if (dir == 2 && o.spg && k == 3) val = val + alfa * d * o.spg[p];
     } else {
       if (o.spg && k == 3) val = val + alfa * d * o.spg[(long long)(j - 1) + (long long)(i - 1) * g.ny];
