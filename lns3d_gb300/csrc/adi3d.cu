@@ -308,7 +308,7 @@ __device__ __forceinline__ void store_el(cf* m, long long q, cd v) { m[q] = cf{(
 // mat(5,5,5,nx,ny).  One thread per entry, so consecutive threads store
 // consecutive entries; T = cf rounds the FP64 entry to FP32.
 template <typename T>
-__global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
+__global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ mat) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 125 * o.np) return;
   const long long p = q / 125;
@@ -334,11 +334,11 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, T* __restrict__ mat) {
   double ak, bk;
   bool combined = false;
   if (per || (pos > 2 && pos < n - 1)) {
-    ak = alfa * pick5(k - 1, ga1, ga2, 0.0, ga3, ga4) / h;
-    bk = alfa * pick5(k - 1, da1, da2, da3, da4, da5) / (h * h);
+    ak = lc.ak[k - 1];
+    bk = lc.bk[k - 1];
   } else {
     // boundary rows j = 1, 2, ny-1, ny (src/lhsbt2f3d.f90:36-600): coefficient t of slot k
-    const double hinv = 1.0 / h, hsinv = 1.0 / (h * h);
+    const double hinv = lc.hinv, hsinv = lc.hsinv;
     auto g1 = [](int t) { return pick5(t, gc1, gc2, gc3, gc4, gc5); };
     auto d1 = [](int t) { return pick5(t, dd1, dd2, dd3, dd4, dd5); };
     auto g2 = [](int t) { return pick5(t, gb1, gb2, gb3, gb4, gb5); };
@@ -897,7 +897,8 @@ int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vs, const cd* vold, const cd
 template <typename T>
 int launch_lhs(lns_ctx3d* c, int dir, T* mat, cudaStream_t st) {
   const long long nq = 125 * c->np;
-  lns::a3::lhs_kernel<T><<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->g, c->ops, dir, mat);
+  const lns::a3::LhsCoef lc = lns::a3::lhs_coef(c->g.alfa, dir == 1 ? c->g.dxi : c->g.deta);
+  lns::a3::lhs_kernel<T><<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->g, c->ops, dir, lc, mat);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "lhs_kernel launch");
 }

@@ -36,6 +36,25 @@ constexpr double dd1 = 2.916666666666666666667E+00, dd2 = -8.6666666666666666666
                  dd5 = 9.166666666666666666667E-01;
 constexpr double pt5 = 0.5, pt66 = 6.6666666666666666666e-1, two = 2.0, four = 4.0;
 
+// The scalar coefficients of one LHS launch (direction and alfa fixed),
+// formed on the host with the reference's expressions (src/lhs1f3d.f90:40-52,
+// src/lhsf.f90:25-40, src/lhs.f90:25-33): FP64 division is slow on this part
+// and correctly rounded on both sides, so no thread divides.
+struct LhsCoef {
+  double ak[5], bk[5];  // fourth-order band: alfa g_k / h, alfa d_k / h^2
+  double ak2[3], bk2[3];  // second-order band: -alfa/2h, alfa 0, alfa/2h; alfa/h^2, -2 alfa/h^2, alfa/h^2
+  double hinv, hsinv;   // 1/h, 1/h^2 (boundary rows)
+};
+inline LhsCoef lhs_coef(double alfa, double h) {
+  LhsCoef c;
+  const double gi[5] = {ga1, ga2, 0.0, ga3, ga4}, di[5] = {da1, da2, da3, da4, da5};
+  for (int k = 0; k < 5; ++k) c.ak[k] = alfa * gi[k] / h, c.bk[k] = alfa * di[k] / (h * h);
+  c.ak2[0] = -alfa * 0.5 / h, c.ak2[1] = alfa * 0.0, c.ak2[2] = alfa * 0.5 / h;
+  c.bk2[0] = alfa / (h * h), c.bk2[1] = -alfa * 2.0 / (h * h), c.bk2[2] = alfa / (h * h);
+  c.hinv = 1.0 / h, c.hsinv = 1.0 / (h * h);
+  return c;
+}
+
 // Entry t (0..4) of a five-coefficient stencil, as register selects: a
 // local array indexed by a thread-dependent t would live in local memory.
 __host__ __device__ __forceinline__ double pick5(int t, double a0, double a1, double a2, double a3, double a4) {

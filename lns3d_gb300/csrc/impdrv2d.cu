@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
 // slots of a band row hold zero blocks, the boundary rows' bc(1..14)
 // blocks sit in the slots of their columns), so one set of line solvers
 // serves both orders: zero blocks add exact zeros to the elimination.
-__global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v, int dir, int order2,
+__global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v, int dir, int order2, LhsCoef lc,
                              double* __restrict__ mat) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 125 * o.np) return;
@@ -505,9 +505,7 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   if (order2 && !edge && (dir == 1 || j > 3 && j < g.ny - 2)) {
     // three-point band in slots 2..4 (src/lhs.f90:28-104, 176-240)
     if (k == 1 || k == 5) { mat[q] = 0.0; return; }
-    const double h = dir == 1 ? g.dxi : g.deta;
-    const double ak = k == 2 ? -alfa * 0.5 / h : k == 3 ? alfa * 0.0 : alfa * 0.5 / h;
-    const double bk = k == 3 ? -alfa * 2.0 / (h * h) : alfa / (h * h);
+    const double ak = lc.ak2[k - 2], bk = lc.bk2[k - 2];
     val = ak * d * (dir == 1 ? o.Ah : o.Bh)[eab];
     if (dir == 1 && k == 3) val = val + alfa * d * o.Dh[eab];
     if (vk >= 0) val = val - bk * d * V[vk * np + p];
@@ -515,19 +513,17 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
     // rows 3 and ny-2: the central five-point stencil of lhsbt2 with a
     // literal zero diagonal block (src/lhsbt2.f90, rows 3 and ny-2)
     const double gik = pick5(k - 1, ga1, ga2, 0.0, ga3, ga4), dik = pick5(k - 1, da1, da2, da3, da4, da5);
-    const double detainv = 1.0 / g.deta, detasinv = 1.0 / (g.deta * g.deta);
+    const double detainv = lc.hinv, detasinv = lc.hsinv;  // dir 2: h = deta
     val = k == 3 ? 0.0 : alfa * d * gik * detainv * o.Bh[eab];
     if (vk >= 0) val = val - alfa * d * dik * detasinv * V[vk * np + p];
   } else if (!edge) {
-    const double h = dir == 1 ? g.dxi : g.deta;
-    const double ak = alfa * pick5(k - 1, ga1, ga2, 0.0, ga3, ga4) / h;
-    const double bk = alfa * pick5(k - 1, da1, da2, da3, da4, da5) / (h * h);
+    const double ak = lc.ak[k - 1], bk = lc.bk[k - 1];
     val = ak * d * (dir == 1 ? o.Ah : o.Bh)[eab];
     if (dir == 1 && k == 3) val = val + alfa * d * o.Dh[eab];
     if (vk >= 0) val = val - bk * d * V[vk * np + p];
   } else {
     // rows 1, 2, ny-1, ny: coefficient t of slot k (src/lhsbt2f.f90)
-    const double detainv = 1.0 / g.deta, detasinv = 1.0 / (g.deta * g.deta);
+    const double detainv = lc.hinv, detasinv = lc.hsinv;  // dir 2: h = deta
     auto g1 = [](int t) { return pick5(t, gc1, gc2, gc3, gc4, gc5); };
     auto d1 = [](int t) { return pick5(t, dd1, dd2, dd3, dd4, dd5); };
     auto g2 = [](int t) { return pick5(t, gb1, gb2, gb3, gb4, gb5); };
@@ -742,7 +738,8 @@ int lhs2(lns_ctx2d* c, const double* v, int dir, double* mat, double alfa, cudaS
   const int order2 = c->prm.lhs_order == 2 ? 1 : 0;
   Grid g = c->g;
   g.alfa = alfa;
-  lns::a2::lhs2d_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(g, c->ops, top2(c), v, dir, order2, mat);
+  const lns::a3::LhsCoef lc = lns::a3::lhs_coef(alfa, dir == 1 ? g.dxi : g.deta);
+  lns::a2::lhs2d_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(g, c->ops, top2(c), v, dir, order2, lc, mat);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda2(e, "lhs2d_kernel launch");
 }
