@@ -85,6 +85,7 @@ class Oracle3D:
             self.spg2 = np.asfortranarray(spg2 if spg2 is not None else np.zeros((nx, ny)),
                                           dtype=np.float64).reshape((nx, ny), order="F")
             self.g.ispg, self.g.spg, self.g.spg2 = ispg, ptr(self.spg).value, ptr(self.spg2).value
+        if ispg or p["top"] == 1:
             self._vm = np.asfortranarray(case["vm"], dtype=np.float64)
             self._xc = np.asfortranarray(case["x"], dtype=np.float64)
             self._wamp = np.ascontiguousarray(wamp if wamp is not None else np.ones(nx), dtype=np.float64)

@@ -442,7 +442,15 @@ double a3_set_time_step(const A3Grid* g, const double* vl, double* dtl) {
    (c3/(2 cm^2), c3/(2 rho cm), 0, 0,
     (gamma Ma^2 c3/2 - T c3/(2 cm^2))/rho), src/lrhs3d.f90:248-278, in the
    reference's order of operations. */
-void a3_inflow_target(const A3Grid* g, int i, int j, double t[10]) {
+static void a3_wave(const A3Grid* g, int i, int j, int with_wamp, double t[10]);
+void a3_inflow_target(const A3Grid* g, int i, int j, double t[10]) { a3_wave(g, i, j, g->ispg == 3, t); }
+
+/* The same wave with wamp(i) always applied: the incoming acoustic wave of
+   the forced top boundary (top = 1, src/rhsbc3d.f90:129-160,
+   src/itrbc3d.f90:145-196) at j = ny. */
+void a3_top_target(const A3Grid* g, int i, double t[10]) { a3_wave(g, i, g->ny, 1, t); }
+
+static void a3_wave(const A3Grid* g, int i, int j, int with_wamp, double t[10]) {
   const long p = IX(g, i, j);
   const double* vm = g->vm + 5 * p;
   const double onept33 = 1.3333333333333333333e+0;
@@ -453,7 +461,7 @@ void a3_inflow_target(const A3Grid* g, int i, int j, double t[10]) {
   const double a = g->omega * g->omega * d / (cu * cu * cu);
   const double xl = g->xc[p];
   const double e = exp(-a * (xl - g->x0));
-  const double w = g->ispg == 3 ? g->wamp[i - 1] * e : e;
+  const double w = with_wamp ? g->wamp[i - 1] * e : e;
   const double c3r = w * cos(kk * xl), c3i = w * sin(kk * xl);
   const double cm2 = cm * cm;
   t[0] = pt5 * c3r / cm2, t[1] = pt5 * c3i / cm2;
@@ -642,6 +650,12 @@ void a3_rhsbc(const A3Grid* g, double* rl, const double* vl) {
     if (g->top == 0)
       for (int i = 1; i <= nx; ++i)
         for (int k = 0; k < 5; ++k) CRE(rl, k, g, i, ny) = zero, CIM(rl, k, g, i, ny) = zero;
+    if (g->top == 1) /* src/rhsbc3d.f90:129-160: r = -(v - t) */
+      for (int i = 1; i <= nx; ++i) {
+        double t[10];
+        a3_top_target(g, i, t);
+        for (int k = 0; k < 10; ++k) rl[k + 10 * IX(g, i, ny)] = -(vl[k + 10 * IX(g, i, ny)] - t[k]);
+      }
   }
   if (g->xper)
     for (int j = 1; j <= ny; ++j)
@@ -688,6 +702,8 @@ void a3_itrbc(const A3Grid* g, double* vl) {
     if (g->top == 0)
       for (int i = 1; i <= nx; ++i)
         for (int k = 0; k < 10; ++k) vl[k + 10 * IX(g, i, ny)] = zero;
+    if (g->top == 1) /* src/itrbc3d.f90:145-196: v = t */
+      for (int i = 1; i <= nx; ++i) a3_top_target(g, i, vl + 10 * IX(g, i, ny));
   }
   if (g->xper)
     for (int j = 1; j <= ny; ++j)

@@ -83,6 +83,8 @@ double a3_set_time_step(const A3Grid* g, const double* vm, double* dtl);
 int a3_lrhs(const A3Grid* g, const A3Ops* ops, const double* v, double* r);
 /* the inflow sponge's target at (i, j), complex (5) as 10 doubles */
 void a3_inflow_target(const A3Grid* g, int i, int j, double t[10]);
+/* the forced top boundary's wave at (i, ny) (top = 1) */
+void a3_top_target(const A3Grid* g, int i, double t[10]);
 void a3_rbe(const A3Grid* g, double* r, const double* v, const double* vold, const double* dtl);
 void a3_rhsbc(const A3Grid* g, double* r, const double* v);
 double a3_resstat(const A3Grid* g, const double* r, const double* dtl);

@@ -295,3 +295,54 @@ def test_target_sponges_known_answer(ispg):
     for a_ in range(5):
         assert np.abs(dm[2, a_, a_, :, 1:-1] - w[:, 1:-1]).max() <= 4e-16 * np.abs(plain.lhs(2)).max()
     assert np.array_equal(o.lhs(1), plain.lhs(1))
+
+
+def _wave(case, x0, wamp, j):
+    """The reference's forced wave at row j (src/itrbc3d.f90:166-196)."""
+    p = case["params"]
+    vm, x = case["vm"][:, :, j], case["x"][:, j]
+    cm = np.sqrt(vm[4]) / p["Ma"]
+    um = vm[1]
+    d = 0.5 * (1.3333333333333333333 + p["gamma1"] / p["Pr"]) / p["Re"]
+    kk = p["omega"] / (cm + um)
+    a = p["omega"] ** 2 * d / (cm + um) ** 3
+    c3 = wamp * np.exp(-a * (x - x0)) * np.exp(1j * kk * x)
+    t = np.zeros((5, len(x)), np.complex128)
+    t[0] = 0.5 * c3 / cm ** 2
+    t[1] = c3 * 0.5 / (vm[0] * cm)
+    t[4] = (p["gamma"] * p["Ma"] ** 2 * c3 * 0.5 - vm[4] * 0.5 * c3 / cm ** 2) / vm[0]
+    return t
+
+
+def test_forced_top_boundary_known_answer():
+    """top = 1 (src/itrbc3d.f90:145-196, src/rhsbc3d.f90:129-160): itrBC3D
+    puts the incoming acoustic wave on row ny, rhsBC3D sets r = -(v - t)
+    there, and the LHS row is the identity; steps keep the wave on the top
+    row."""
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 24, 20
+    case = shear_layer(nx=nx, ny=ny, seed=1)
+    case = dict(case, params=dict(case["params"], top=1))
+    rng = np.random.default_rng(3)
+    wamp = rng.uniform(0.5, 1.5, nx)
+    o = Oracle3D(case, cflmax=20.0, loctime=1, x0=-2.0, wamp=wamp)
+    t = _wave(case, -2.0, wamp, ny - 1)
+    v = np.asfortranarray(rng.standard_normal((5, nx, ny)) + 1j * rng.standard_normal((5, nx, ny)))
+    w = v.copy(order="F")
+    L = _lib()
+    L.a3_itrbc(ctypes.byref(o.g), ptr(w))
+    assert np.abs(w[:, :-1, -1] - t[:, :-1]).max() <= 1e-13 * np.abs(t).max()
+    assert np.array_equal(w[:, -1, :], w[:, 0, :])
+    r = np.asfortranarray(rng.standard_normal((5, nx, ny)) + 0j)
+    L.a3_rhsbc(ctypes.byref(o.g), ptr(r), ptr(v))
+    assert np.abs(r[:, :-1, -1] + (v[:, :-1, -1] - t[:, :-1])).max() <= 1e-13 * np.abs(t).max()
+    m = o.lhs(2)
+    eye = np.zeros((5, 5, 5), np.complex128)
+    eye[2] = np.eye(5)
+    assert all(np.array_equal(m[:, :, :, i, -1], eye) for i in range(nx))
+    v = case["v"].copy(order="F")
+    for _ in range(3):
+        o.step(v)
+    assert np.isfinite(v).all()
+    assert np.abs(v[:, :-1, -1] - t[:, :-1]).max() <= 1e-13 * np.abs(t).max()
