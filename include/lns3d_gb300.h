@@ -299,9 +299,10 @@ int lns_cpenta2bc_mixed_static_dev(int32_t n, int32_t nsys, int32_t nblk, const 
  *   lns_step3d / _dev       nsteps implicit steps of niter correctors
  * Supported options: xper = 1 (periodic xi sweep, cpenta2p), yper = 0 with a
  * viscous wall at j = 1 (navier = 1, wall 1 or 2, wallt 0 or 1) and a
- * zero-disturbance top (top = 0); optx, opty any; constant viscosity
- * (mattyp 0); no sponge, smoother, damper or filter.  Other options return
- * LNS_ERR_ARG.
+ * zero-disturbance top (top = 0) or a top forced by an incoming acoustic
+ * wave (top = 1, lns_upload_inflow3d); optx, opty any; constant viscosity
+ * (mattyp 0); the sponges (ispg) and the smoother (eps_e) below; no damper
+ * and no filter.  Other options return LNS_ERR_ARG.
  *
  * precision LNS_FP64 follows the reference arithmetic (complex*16
  * throughout).  LNS_MIXED keeps the RHS, the residual and the update in
@@ -371,9 +372,12 @@ int lns_upload_metrics3d(lns_ctx3d* ctx, const double* metrics);
  * host's sponge setup (src/sponge.f90) leaves them; needed before the first
  * step when ispg != 0; invalidates the factored LHS. */
 int lns_upload_sponge3d(lns_ctx3d* ctx, const double* spg, const double* spg2);
-/* ispg 2, 3: the x coordinates x(nx,ny), the inflow station x0 and (ispg 3)
- * the amplitudes wamp(nx) of the inflow sponge's wave (src/lrhs3d.f90:242-
- * 268); its target is formed on the device from these and the mean flow. */
+/* ispg 2, 3 or top 1: the x coordinates x(nx,ny), the station x0 and the
+ * amplitudes wamp(nx) (NULL: ones, the reference's default; ispg 3 needs
+ * them) of the inflow sponge's wave (src/lrhs3d.f90:242-268) and of the
+ * forced top boundary's incoming acoustic wave (top 1: v = t and r = -(v - t)
+ * on row ny, src/itrbc3d.f90:145-196, src/rhsbc3d.f90:129-160); the waves
+ * are formed on the device from these and the mean flow. */
 int lns_upload_inflow3d(lns_ctx3d* ctx, const double* x, const double* wamp, double x0);
 /* ispg 4: the eigenfunction target cvic, complex (5,nx,ny) as interleaved
  * doubles (src/sponge.f90:558-579). */

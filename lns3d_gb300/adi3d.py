@@ -49,8 +49,8 @@ class ImpDrv3D:
     spg + spg2; src/lrhs3d.f90:220-240), spg and spg2 (nx, ny) arrays.
     eps_e, buff: explicit smoother and implicit damping (src/smoother3d.f90),
     buff (nx, ny) or None for the reference's default of ones.  ispg 2, 3
-    take the x coordinates x (nx, ny), x0 and (3) wamp (nx); ispg 4 the
-    complex target cvic (5, nx, ny).
+    and the forced top (params top = 1) take the x coordinates x (nx, ny),
+    x0 and wamp (nx; None: ones); ispg 4 the complex target cvic (5, nx, ny).
     """
 
     def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False,
@@ -77,7 +77,7 @@ class ImpDrv3D:
             check(lib().lns_upload_sponge3d(self._ctx, ctypes.c_void_p(s1.ctypes.data),
                                             ctypes.c_void_p(s2.ctypes.data) if s2 is not None else None),
                   "lns_upload_sponge3d")
-        if ispg in (2, 3):
+        if ispg in (2, 3) or int(p["top"]) == 1:
             xx = np.asfortranarray(x, dtype=np.float64)
             wa = np.ascontiguousarray(wamp, dtype=np.float64) if wamp is not None else None
             check(lib().lns_upload_inflow3d(self._ctx, ctypes.c_void_p(xx.ctypes.data),

@@ -367,10 +367,15 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
 // c3 = [wamp(i)] exp(-a (x - x0)) exp(i kk x), cm = sqrt(T)/Ma,
 // kk = omega/(cm + u), a = omega^2 d/(cm + u)^3, d = (4/3 + (gamma-1)/Pr)/(2 Re);
 // t = (c3/(2 cm^2), c3/(2 rho cm), 0, 0, (gamma Ma^2 c3/2 - T c3/(2 cm^2))/rho)
-__global__ void inflow_target_kernel(Grid g, int ispg, const double* __restrict__ vm, const double* __restrict__ xc,
-                                     const double* __restrict__ wamp, double x0, cd* __restrict__ vt) {
-  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (p >= (long long)g.nx * g.ny) return;
+// With row0 > 0 the kernel forms only row row0 (the forced top boundary's
+// wave, src/itrbc3d.f90:166-196, wamp always applied) into vt(5,nx).
+__global__ void inflow_target_kernel(Grid g, int with_wamp, int row0, const double* __restrict__ vm,
+                                     const double* __restrict__ xc, const double* __restrict__ wamp, double x0,
+                                     cd* __restrict__ vt) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (row0 > 0 ? (long long)g.nx : (long long)g.nx * g.ny)) return;
+  const long long p = row0 > 0 ? (long long)(row0 - 1) * g.nx + t : t;
+  const long long o = row0 > 0 ? t : p;  // output record
   const int i = (int)(p % g.nx) + 1;
   const double* m = vm + 5 * p;
   const double cm = sqrt(m[4]) / g.Ma, um = m[1];
@@ -380,16 +385,16 @@ __global__ void inflow_target_kernel(Grid g, int ispg, const double* __restrict_
   const double a = g.omega * g.omega * d / (cu * cu * cu);
   const double xl = xc[p];
   const double e = exp(-a * (xl - x0));
-  const double w = ispg == 3 ? wamp[i - 1] * e : e;
+  const double w = with_wamp ? wamp[i - 1] * e : e;
   double sn, cs;
   sincos(kk * xl, &sn, &cs);
   const double c3r = w * cs, c3i = w * sn;
   const double cm2 = cm * cm, gm2 = g.gamma * (g.Ma * g.Ma);
-  vt[5 * p + 0] = cd{0.5 * c3r / cm2, 0.5 * c3i / cm2};
-  vt[5 * p + 1] = cd{c3r * 0.5 / (m[0] * cm), c3i * 0.5 / (m[0] * cm)};
-  vt[5 * p + 2] = cd{0.0, 0.0};
-  vt[5 * p + 3] = cd{0.0, 0.0};
-  vt[5 * p + 4] = cd{(gm2 * c3r * 0.5 - m[4] * 0.5 * c3r / cm2) / m[0], (gm2 * c3i * 0.5 - m[4] * 0.5 * c3i / cm2) / m[0]};
+  vt[5 * o + 0] = cd{0.5 * c3r / cm2, 0.5 * c3i / cm2};
+  vt[5 * o + 1] = cd{c3r * 0.5 / (m[0] * cm), c3i * 0.5 / (m[0] * cm)};
+  vt[5 * o + 2] = cd{0.0, 0.0};
+  vt[5 * o + 3] = cd{0.0, 0.0};
+  vt[5 * o + 4] = cd{(gm2 * c3r * 0.5 - m[4] * 0.5 * c3r / cm2) / m[0], (gm2 * c3i * 0.5 - m[4] * 0.5 * c3i / cm2) / m[0]};
 }
 
 // -------------------------------------------------------------------- RHS
@@ -567,6 +572,14 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
       if (g.top == 0 && j == g.ny)
         #pragma unroll
         for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
+      if (g.top == 1 && j == g.ny) {  // src/rhsbc3d.f90:129-160: r = -(v - t)
+        const cd* T = reinterpret_cast<const cd*>(o.ttop) + 5 * (i - 1);
+        #pragma unroll
+        for (int m = 0; m < 5; ++m) {
+          const cd w = vs[m + 5 * p];
+          r[m] = cd{-(w.x - T[m].x), -(w.y - T[m].y)};
+        }
+      }
     } else if (j == g.ny) {
       #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
@@ -603,7 +616,7 @@ __global__ void __launch_bounds__(128, 4) rhs_kernel(Grid g, Ops o, const cd* __
 // column i (wall row j = 1 from rows 2..5, top row j = ny); with a periodic
 // x direction the remaining threads copy the interior rows of column 1 to
 // column nx, and the thread of column 1 copies its boundary rows.
-__device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, int bx) {
+__device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const double* __restrict__ ttop, int bx) {
   const int t = bx * blockDim.x + threadIdx.x;
   const int ncol = g.xper ? g.nx - 1 : g.nx;
   if (t < ncol) {
@@ -623,6 +636,8 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, int b
       }
       if (g.top == 0)
         for (int m = 0; m < 5; ++m) W(m, g.ny) = cd{0.0, 0.0};
+      if (g.top == 1)  // src/itrbc3d.f90:145-196: the incoming wave
+        for (int m = 0; m < 5; ++m) W(m, g.ny) = reinterpret_cast<const cd*>(ttop)[m + 5 * (i - 1)];
     } else {
       for (int m = 0; m < 5; ++m) W(m, g.ny) = W(m, 1);
     }
@@ -638,7 +653,9 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, int b
   }
 }
 
-__global__ void bc_kernel(Grid g, cd* __restrict__ v) { bc_body(g, v, blockIdx.x); }
+__global__ void bc_kernel(Grid g, cd* __restrict__ v, const double* __restrict__ ttop) {
+  bc_body(g, v, ttop, blockIdx.x);
+}
 
 // ------------------------------------------------------------- batching
 // Per-problem arguments of the per-step kernels of a batch (lns_batch3d):
@@ -668,7 +685,7 @@ __global__ void bc_batch_kernel(const StepArgs* __restrict__ list, const int2* _
                                 const int* __restrict__ active) {
   const int2 w = table[blockIdx.x];
   if (!active[w.x]) return;
-  bc_body(list[w.x].g, list[w.x].v, w.y);
+  bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, w.y);
 }
 __global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4* __restrict__ table,
                                    const int* __restrict__ active) {
@@ -766,7 +783,8 @@ struct lns_ctx3d {
   bool have_sponge = false;   // ispg != 0: lns_upload_sponge3d called
   double* spg = nullptr;      // spg (ispg 1), else spg + spg2
   double *spg_a = nullptr, *spg_b = nullptr, *vt = nullptr;  // the target sponges (ispg 2-4)
-  double *xc = nullptr, *wamp = nullptr;  // ispg 2, 3: x(nx,ny), wamp(nx)
+  double *xc = nullptr, *wamp = nullptr;  // ispg 2, 3 or top 1: x(nx,ny), wamp(nx) (ones until uploaded)
+  double* ttop = nullptr;                 // top 1: the wave of row ny, complex (5,nx)
   double x0 = 0.0;
   bool have_inflow = false, have_target = false;
   double* buff = nullptr;     // eps_e != 0: buff(nx,ny), ones until uploaded
@@ -995,7 +1013,7 @@ int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
   const long long n = 5 * c->np;
   if (add) lns::a3::add_kernel<cd, RT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, r);
   const int nt = g.nx + g.ny;
-  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v);
+  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v, c->ops.ttop);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "update kernels launch");
 }
@@ -1082,7 +1100,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->yper != 0 || p->navier != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: need yper = 0 and navier = 1");
   if (p->wall != 1 && p->wall != 2) return fail3(LNS_ERR_ARG, "ctx3d_create: wall must be 1 or 2");
   if (p->wallt != 0 && p->wallt != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: wallt must be 0 or 1");
-  if (p->top != 0) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0");
+  if (p->top != 0 && p->top != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0 or 1");
   if (p->loctime != 0 && p->loctime != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: loctime must be 0 or 1");
   if (p->res_compat != 0 && p->res_compat != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: res_compat must be 0 or 1");
   if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
@@ -1132,11 +1150,12 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
     A(sizeof(double) * np, &q); c->spg_b = (double*)q;
     A(sizeof(double) * 10 * np, &q); c->vt = (double*)q;
   }
-  if (p->ispg == 2 || p->ispg == 3) {
-    A(sizeof(double) * np, &q); c->spg_a = (double*)q;
+  if (p->ispg == 2 || p->ispg == 3) { A(sizeof(double) * np, &q); c->spg_a = (double*)q; }
+  if (p->ispg == 2 || p->ispg == 3 || p->top == 1) {
     A(sizeof(double) * np, &q); c->xc = (double*)q;
     A(sizeof(double) * p->nx, &q); c->wamp = (double*)q;
   }
+  if (p->top == 1) { A(sizeof(double) * 10 * p->nx, &q); c->ttop = (double*)q; }
   if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
@@ -1174,6 +1193,15 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   c->ops.Ah = o; c->ops.Bh = o + 25 * np; c->ops.Dh = o + 50 * np; c->ops.Dhi = o + 75 * np;
   c->ops.V11 = o + 100 * np; c->ops.V12 = o + 106 * np; c->ops.V22 = o + 112 * np; c->ops.AB = o + 118 * np;
   c->ops.dtl = o + 124 * np;
+  if (c->wamp) {  // the reference's default amplitudes (useAmp false): ones
+    std::vector<double> ones((size_t)p->nx, 1.0);
+    ez = cudaMemcpy(c->wamp, ones.data(), sizeof(double) * p->nx, cudaMemcpyHostToDevice);
+    if (ez != cudaSuccess) {
+      free_all(c);
+      delete c;
+      return cuda3(ez, "wamp init");
+    }
+  }
   if (c->buff) {
     // the reference's default buffer (ibuff = 0, src/buffer.f90): ones
     std::vector<double> ones((size_t)np, 1.0);
@@ -1206,8 +1234,9 @@ int need_data(const lns_ctx3d* c, const char* who) {
   if (!c->have_mean) return fail3(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the mean flow first");
   if (c->prm.ispg != 0 && !c->have_sponge)
     return fail3(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
-  if ((c->prm.ispg == 2 || c->prm.ispg == 3) && !c->have_inflow)
-    return fail3(LNS_ERR_ARG, std::string(who) + ": ispg 2, 3: upload the inflow data (lns_upload_inflow3d) first");
+  if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1) && !c->have_inflow)
+    return fail3(LNS_ERR_ARG,
+                 std::string(who) + ": ispg 2, 3 or top 1: upload the wave data (lns_upload_inflow3d) first");
   if (c->prm.ispg == 4 && !c->have_target)
     return fail3(LNS_ERR_ARG, std::string(who) + ": ispg 4: upload the sponge target (lns_upload_sponge_target3d) first");
   return LNS_OK;
@@ -1215,10 +1244,16 @@ int need_data(const lns_ctx3d* c, const char* who) {
 
 // the inflow sponge's target, once the mean flow and the inflow data are in
 int make_inflow_target(lns_ctx3d* c) {
-  if (!(c->prm.ispg == 2 || c->prm.ispg == 3) || !c->have_inflow || !c->have_mean) return LNS_OK;
+  if (!c->have_inflow || !c->have_mean) return LNS_OK;
   const long long np = c->np;
-  lns::a3::inflow_target_kernel<<<(unsigned)((np + 255) / 256), 256>>>(c->g, c->prm.ispg, c->vm, c->xc, c->wamp,
-                                                                       c->x0, reinterpret_cast<cd*>(c->vt));
+  if (c->prm.ispg == 2 || c->prm.ispg == 3)
+    lns::a3::inflow_target_kernel<<<(unsigned)((np + 255) / 256), 256>>>(
+        c->g, c->prm.ispg == 3, 0, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->vt));
+  if (c->prm.top == 1) {
+    lns::a3::inflow_target_kernel<<<(unsigned)((c->g.nx + 127) / 128), 128>>>(
+        c->g, 1, c->g.ny, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->ttop));
+    c->ops.ttop = c->ttop;
+  }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "inflow_target_kernel");
@@ -1255,7 +1290,8 @@ int lns_upload_sponge3d(lns_ctx3d* c, const double* spg, const double* spg2) {
 
 int lns_upload_inflow3d(lns_ctx3d* c, const double* x, const double* wamp, double x0) {
   if (!c || !x) return fail3(LNS_ERR_ARG, "upload_inflow3d: null argument");
-  if (c->prm.ispg != 2 && c->prm.ispg != 3) return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3");
+  if (c->prm.ispg != 2 && c->prm.ispg != 3 && c->prm.top != 1)
+    return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3, or top 1");
   if (c->prm.ispg == 3 && !wamp) return fail3(LNS_ERR_ARG, "upload_inflow3d: ispg 3 needs wamp");
   if (!std::isfinite(x0)) return fail3(LNS_ERR_ARG, "upload_inflow3d: x0 must be finite");
   int rc = check_device(c);
@@ -1696,8 +1732,9 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
   for (int p = 0; p < nprob; ++p)
     if (params[p].impl > 1) return fail3(LNS_ERR_ARG, "batch3d_create: batches run impl = 1 (backward Euler)");
   for (int p = 0; p < nprob; ++p)
-    if (params[p].ispg != 0 || params[p].eps_e != 0.0)
-      return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge or smoother (ispg = 0, eps_e = 0)");
+    if (params[p].ispg != 0 || params[p].eps_e != 0.0 || params[p].top != 0)
+      return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge, smoother or forced top (ispg = 0, "
+                                "eps_e = 0, top = 0)");
   lns_batch3d* b = new lns_batch3d();
   b->P = nprob;
   b->mixed = params[0].precision == LNS_MIXED;
@@ -2066,8 +2103,9 @@ int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* 
   if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
   if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
   if (prm->impl > 1) return fail3(LNS_ERR_ARG, "server3d_submit: servers run impl = 1 (backward Euler)");
-  if (prm->ispg != 0 || prm->eps_e != 0.0)
-    return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge or smoother (ispg = 0, eps_e = 0)");
+  if (prm->ispg != 0 || prm->eps_e != 0.0 || prm->top != 0)
+    return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge, smoother or forced top (ispg = 0, "
+                              "eps_e = 0, top = 0)");
   if (!(tol > 0.0) || max_steps < 1) return fail3(LNS_ERR_ARG, "server3d_submit: need tol > 0 and max_steps >= 1");
   if (ctx_bytes_for(*prm) > s->budget) return fail3(LNS_ERR_ARG, "server3d_submit: request larger than the budget");
   SrvReq* r = new SrvReq();

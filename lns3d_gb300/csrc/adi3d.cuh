@@ -91,6 +91,8 @@ struct Ops {
   const double* spg_a = nullptr;
   const double* spg_b = nullptr;
   const double* vt = nullptr;
+  // the forced top boundary (top = 1): its wave at row ny, complex (5,nx)
+  const double* ttop = nullptr;
   // explicit smoother / implicit damping: eps_e buff(nx,ny); null when eps_e = 0
   const double* buff = nullptr;
   double eps_e = 0.0;

@@ -119,7 +119,7 @@ def _params3d(**kw):
 
 
 @pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=0), dict(wallt=2),
-                                 dict(top=1), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
+                                 dict(top=2), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
                                  dict(loctime=2), dict(ispg=-1),
                                  dict(eps_e=-1.0), dict(eps_e=float("nan"))])
 def test_ctx3d_rejects_unsupported_options(lib, bad):

@@ -524,3 +524,60 @@ def test_target_sponges_match_oracle(cuda, ispg):
         err = np.abs(v_gpu - v_ref).max() / max(np.abs(v_ref).max(), scale_t)
         assert err < STEP_TOL, s
         assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+
+
+def test_forced_top_boundary_matches_oracle(cuda):
+    """top = 1 (src/itrbc3d.f90:145-196, src/rhsbc3d.f90:129-160): the
+    incoming acoustic wave on row ny, formed on the device from the mean flow,
+    x, x0 and wamp; RHS, LHS and steps against the oracle, to 1e-12 of the
+    larger of the state and the wave (the device forms the wave with its own
+    exp, sin and cos)."""
+    import ctypes
+
+    import torch
+    from adi3dcase import _lib, ptr
+
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 40, 33
+    case = shear_layer(nx=nx, ny=ny, seed=12)
+    case = dict(case, params=dict(case["params"], top=1))
+    rng = np.random.default_rng(15)
+    wamp = rng.uniform(0.5, 1.5, nx)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1, x0=-2.0, wamp=wamp)
+    mk = lambda: ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, x=case["x"], x0=-2.0,
+                          wamp=wamp)
+    L = _lib()
+    L.a3_top_target.argtypes = [ctypes.POINTER(type(orc.g)), ctypes.c_int, ctypes.c_void_p]
+    t = np.zeros(10)
+    scale_t = 0.0
+    for i in range(1, nx + 1):
+        L.a3_top_target(ctypes.byref(orc.g), i, t.ctypes.data)
+        scale_t = max(scale_t, np.abs(t).max())
+    drv = mk()
+    mat = torch.zeros(125 * nx * ny, dtype=torch.complex128, device="cuda")
+    drv.lhs(2, mat)
+    torch.cuda.synchronize()
+    assert rel(mat.cpu().numpy().reshape((5, 5, 5, nx, ny), order="F"), orc.lhs(2)) < OPS_TOL
+    shape = (5, nx, ny)
+    v = np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    vold = np.asfortranarray(v + 1e-3 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    r = orc.lrhs(v)
+    L.a3_rbe(ctypes.byref(orc.g), ptr(r), ptr(v), ptr(vold), ptr(orc.dtl))
+    L.a3_rhsbc(ctypes.byref(orc.g), ptr(r), ptr(v))
+    dev = lambda a: torch.from_numpy(a.ravel(order="F")).cuda()
+    dv, dvo = dev(v), dev(vold)
+    dr = torch.zeros_like(dv)
+    drv.rhs(dv, dvo, dr, torch.zeros(1, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    got = dr.cpu().numpy().reshape(shape, order="F")
+    assert np.abs(got - r).max() / max(np.abs(r).max(), scale_t) < RHS_TOL
+    drv = mk()
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    for s in range(4):
+        res_ref = orc.step(v_ref)
+        res_gpu = drv.step(v_gpu, nsteps=1)[0]
+        assert np.abs(v_gpu - v_ref).max() / max(np.abs(v_ref).max(), scale_t) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
