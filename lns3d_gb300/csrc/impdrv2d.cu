@@ -479,6 +479,8 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   // the far-field row j = ny
   if (!g.yper && j == g.ny) {
     if (dir == 1 && g.top == 0) { mat[q] = ident; return; }
+    // the held quiescent top (top 3): identity eta row, src/lhsbc2f.f90:332-339
+    if (dir == 2 && g.Ma < 1.0 && g.top == 3) { mat[q] = ident; return; }
     if (dir == 2 && g.Ma < 1.0 && g.top == 0) {
       const RmState s = rm_state(g, tp, i, v + 5 * pix(g, i, g.ny), v + 5 * pix(g, i, g.ny - 1),
                                  v + 5 * pix(g, i, g.ny - 2));
@@ -586,6 +588,8 @@ __global__ void bc2d_kernel(Grid g, Top tp, double* __restrict__ v) {
         double b[5];
         rm_values(g, tp, i, s, b);
         for (int m = 0; m < 5; ++m) W(m, g.ny) = b[m];
+      } else if (g.top == 3) {  // the held quiescent top, src/itrbc.f90 (nonlinear)
+        W(0, g.ny) = 1.0; W(1, g.ny) = 0.0; W(2, g.ny) = 0.0; W(3, g.ny) = 0.0; W(4, g.ny) = 1.0;
       }
     }
     if (g.xper && i == 1)
@@ -834,7 +838,9 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   if (p->yper != 0 || p->navier != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: need yper = 0 and navier = 1");
   if (p->wall != 0 && p->wall != 1 && p->wall != 3) return fail2(LNS_ERR_ARG, "ctx2d_create: wall must be 0, 1 or 3");
   if (p->wallt != 0 && p->wallt != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: wallt must be 0 or 1");
-  if (p->top != 0) return fail2(LNS_ERR_ARG, "ctx2d_create: top must be 0");
+  if (p->top != 0 && p->top != 3) return fail2(LNS_ERR_ARG, "ctx2d_create: top must be 0 or 3");
+  if (p->top == 3 && p->lhs_order == 2)
+    return fail2(LNS_ERR_ARG, "ctx2d_create: the held top (top 3) is supported with the fourth-order LHS");
   if (!(p->Ma > 0.0) || p->Ma == 1.0) return fail2(LNS_ERR_ARG, "ctx2d_create: need Ma > 0 and Ma != 1");
   if (p->loctime != 0 && p->loctime != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: loctime must be 0 or 1");
   if (p->res_compat != 0 && p->res_compat != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: res_compat must be 0 or 1");
@@ -982,7 +988,7 @@ int lns_upload_buffer2d(lns_ctx2d* c, const double* buff) {
 }
 
 static int ready2(lns_ctx2d* c, const char* who) {
-  if (!c->have_metrics || !c->have_top)
+  if (!c->have_metrics || (!c->have_top && c->prm.top == 0 && c->prm.Ma < 1.0))
     return fail2(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the far field first");
   if (c->prm.ispg != 0 && !c->have_sponge)
     return fail2(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");

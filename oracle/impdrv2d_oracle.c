@@ -437,6 +437,11 @@ void a2_itrbc(const A2Grid* a2, double* vl) {
         rm_values(a2, i, &s, b);
         for (int k = 0; k < 5; ++k) VR(k, i, ny) = b[k];
       }
+    } else if (g->top == 3) {
+      /* the held quiescent top, src/itrbc.f90 (nonlinear, top = 3) */
+      for (int i = 1; i <= nx; ++i) {
+        VR(0, i, ny) = one; VR(1, i, ny) = zero; VR(2, i, ny) = zero; VR(3, i, ny) = zero; VR(4, i, ny) = one;
+      }
     }
   }
   if (g->xper)
@@ -707,6 +712,14 @@ int a2_lhs(const A2Grid* a2, const A3Ops* o, const double* dtl, const double* vl
         for (int k = 1; k <= 5; ++k)
           for (int b = 1; b <= 5; ++b) MT(k, a, b, p) = zero;
       rm_lhs(a2, i, vl + 5 * IX(g, i, ny), vl + 5 * IX(g, i, ny - 1), vl + 5 * IX(g, i, ny - 2), mat, p);
+    } else if (g->Ma < one && g->top == 3) {
+      /* src/lhsbc2f.f90:332-339: identity row (the xi LHS keeps its band row,
+         src/lhsbc1f.f90:596 acts for top 0 only; the RHS row is left as rbe
+         gives it, src/rhsbc.f90:350-356) */
+      for (int a = 1; a <= 5; ++a)
+        for (int k = 1; k <= 5; ++k)
+          for (int b = 1; b <= 5; ++b) MT(k, a, b, p) = zero;
+      for (int a = 1; a <= 5; ++a) MT(3, a, a, p) = one;
     }
   }
   return 0;

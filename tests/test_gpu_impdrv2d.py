@@ -328,3 +328,34 @@ def test_sponge_and_smoother_match_oracle(cuda, small, kw):
         res_g = d2.step(v_gpu, nsteps=1)[0]
         assert rel(v_gpu, v_ref) < STEP_TOL, s
         assert abs(res_g - res_o) <= 1e-10 * res_o, s
+
+
+def test_held_top_matches_oracle(cuda):
+    """top = 3 (the held quiescent top, src/itrbc.f90 nonlinear branch,
+    src/lhsbc2f.f90:332-339): both LHS and steps against the oracle; the
+    far-field arrays are not needed for it."""
+    import torch
+
+    from lns3d_gb300.cases import vortex2d
+
+    c = vortex2d(nx=40, ny=33, seed=8)
+    c = dict(c, params=dict(c["params"], top=3))
+    o = Oracle2D(c, cflmax=1.0, loctime=0)
+    drv = make(c)
+    v_ref = c["v"].copy(order="F")
+    o.itrbc(v_ref)
+    v_gpu = v_ref.copy(order="F")
+    for s in range(4):
+        res_o = o.step(v_ref)
+        res_g = drv.step(v_gpu, nsteps=1)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_g - res_o) <= 1e-10 * res_o, s
+    nx, ny = 40, 33
+    for direction in (1, 2):
+        ref = o.lhs(v_ref, o.dtl, direction)
+        mat = torch.zeros(125 * nx * ny, dtype=torch.float64, device="cuda")
+        dv = dev(v_ref)
+        drv.rhs(dv, dv, torch.zeros_like(dv))
+        drv.lhs(direction, dv, mat)
+        torch.cuda.synchronize()
+        assert rel(host(mat, ref.shape), ref) < OPS_TOL, direction

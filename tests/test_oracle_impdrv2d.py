@@ -233,3 +233,33 @@ def test_sponge_and_smoother_steps():
     assert np.isfinite(v).all() and all(r > 0 for r in res)
     with pytest.raises(ValueError):
         Oracle2D(c, ilhs=0, eps_e=0.01)
+
+
+def test_held_top_boundary():
+    """top = 3 with Ma < 1 (src/itrbc.f90, nonlinear branch; src/lhsbc2f.f90:
+    332-339): itrBC holds row ny at (1, 0, 0, 0, 1), the eta LHS row is the
+    identity, the xi LHS and the RHS rows are left as the interior gives them."""
+    from lns3d_gb300.cases import vortex2d
+
+    nx, ny = 24, 20
+    c = vortex2d(nx=nx, ny=ny)
+    c3 = dict(c, params=dict(c["params"], top=3))
+    o = Oracle2D(c3)
+    v = c3["v"].copy(order="F")
+    o.itrbc(v)
+    held = np.array([1.0, 0.0, 0.0, 0.0, 1.0])
+    assert np.array_equal(v[:, :, -1], np.repeat(held[:, None], nx, axis=1))
+    import ctypes
+
+    o.L.a3_set_time_step(ctypes.byref(o.g.g), ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(o.dtl.ctypes.data))
+    o.genmtrx(v)
+    m2 = o.lhs(v, o.dtl, 2)
+    eye = np.zeros((5, 5, 5))
+    eye[2] = np.eye(5)
+    assert all(np.array_equal(m2[:, :, :, i, -1], eye) for i in range(nx))
+    m1 = o.lhs(v, o.dtl, 1)
+    assert not np.array_equal(m1[:, :, :, 0, -1], eye)
+    for _ in range(3):
+        o.step(v)
+    assert np.isfinite(v).all()
+    assert np.array_equal(v[:, :, -1], np.repeat(held[:, None], nx, axis=1))
