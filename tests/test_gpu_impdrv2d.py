@@ -350,12 +350,18 @@ def test_held_top_matches_oracle(cuda):
         res_g = drv.step(v_gpu, nsteps=1)[0]
         assert rel(v_gpu, v_ref) < STEP_TOL, s
         assert abs(res_g - res_o) <= 1e-10 * res_o, s
+    import ctypes
+
     nx, ny = 40, 33
+    # operators and time step of the current state on both sides
+    o.L.a3_set_time_step(ctypes.byref(o.g.g), ctypes.c_void_p(v_ref.ctypes.data),
+                         ctypes.c_void_p(o.dtl.ctypes.data))
+    o.rhs(v_ref, v_ref, o.dtl)
+    dv = dev(v_ref)
+    drv.rhs(dv, dv, torch.zeros_like(dv))
     for direction in (1, 2):
         ref = o.lhs(v_ref, o.dtl, direction)
         mat = torch.zeros(125 * nx * ny, dtype=torch.float64, device="cuda")
-        dv = dev(v_ref)
-        drv.rhs(dv, dv, torch.zeros_like(dv))
         drv.lhs(direction, dv, mat)
         torch.cuda.synchronize()
         assert rel(host(mat, ref.shape), ref) < OPS_TOL, direction
