@@ -191,7 +191,8 @@ int lns_solve1p_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, d
  * equations.
  * Supported options: xper = 1, yper = 0, a viscous wall at j = 1 (navier 1,
  * wall 0, 1 or 3, wallt 0 or 1) and the Riemann far field at j = ny (top 0;
- * held free stream when Ma > 1); constant viscosity; no sponge, damper or
+ * held free stream when Ma > 1) or the held quiescent top (top 3, row ny held
+ * at (1, 0, 0, 0, 1), fourth-order LHS only); constant viscosity; no sponge, damper or
  * smoother.  Arrays are Fortran-ordered: v(5,nx,ny), metrics(nx,ny,10),
  * bnt(nx,2) (src/gengrid.f90:141-142), pot(5,nx) = the rho u v w T rows of
  * top.pot (src/potential.f90:22-26).
