@@ -222,7 +222,8 @@ typedef struct {
   double eps_e;              /* explicit smoother at the end of genmtrx (src/smoother.f90) and
                                 implicit damping of both LHS (src/lhsf.f90:113-145, 262-294,
                                 src/lhsbt2f.f90:193-213) weighted by buff (ones until
-                                lns_upload_buffer2d).  ispg and eps_e need lhs_order 0 or 4. */
+                                lns_upload_buffer2d); with lhs_order 2 the second-order damping
+                                of src/lhs.f90 and src/lhsbt2.f90. */
 } lns_params2d;
 
 typedef struct lns_ctx2d lns_ctx2d;

@@ -546,6 +546,28 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   // boundary rows the sponge through lhsbt2f's transposed spgl(ny,nx) view
   // of the (nx,ny) array, then the damping of rows 2 and ny-1 in slots 2..4
   // (src/lhsbt2f.f90:18, 84-108, 163-213, 266-316)
+  // the second-order LHS: band rows damping c_k = alfa eps_i (-1, 2, -1),
+  // eps_i = 4 eps_e, then the eta sponge (src/lhs.f90:23-27, 89-103,
+  // 229-250); the lhsbt2 rows 1..3 and ny-2..ny the sponge through the
+  // transposed spgl view, then the damping of rows 2, ny-1 (-1, 2, -1) and
+  // 3, ny-2 (fb1..fb5) (src/lhsbt2.f90)
+  if (order2 && a == b && (o.buff || o.spg)) {
+    if (dir == 1 || (j > 3 && j < g.ny - 2)) {
+      if (o.buff && k >= 2 && k <= 4) {
+        const double eps_i = 4.0 * o.eps_e;
+        const double ck = k == 3 ? alfa * 2.0 * eps_i : -alfa * eps_i;
+        val = val + ck * d * o.buff[p];
+      }
+      if (dir == 2 && o.spg && k == 3) val = val + alfa * d * o.spg[p];
+    } else {
+      if (o.spg && k == 3) val = val + alfa * d * o.spg[(long long)(j - 1) + (long long)(i - 1) * g.ny];
+      if (o.buff) {
+        const double wd = alfa * d * o.eps_e * o.buff[p];
+        if ((j == 2 || j == g.ny - 1) && k >= 2 && k <= 4) val = val + wd * (k == 3 ? 2.0 : -1.0);
+        if (j == 3 || j == g.ny - 2) val = val + wd * pick5(k - 1, 1.0, -4.0, 6.0, -4.0, 1.0);
+      }
+    }
+  }
   if (!order2 && a == b && (o.buff || o.spg)) {
     const double wd = o.buff ? alfa * d * o.eps_e * o.buff[p] : 0.0;
     if (!edge) {
@@ -852,8 +874,6 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
     return fail2(LNS_ERR_ARG, "ctx2d_create: ispg must be 0 or 2 (the reference's nonlinear sponge)");
   if (!(p->eps_e >= 0.0) || !std::isfinite(p->eps_e))
     return fail2(LNS_ERR_ARG, "ctx2d_create: eps_e must be finite and >= 0");
-  if (p->lhs_order == 2 && (p->ispg != 0 || p->eps_e != 0.0))
-    return fail2(LNS_ERR_ARG, "ctx2d_create: the sponge and smoother are supported with the fourth-order LHS");
   lns_ctx2d* c = new lns_ctx2d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);

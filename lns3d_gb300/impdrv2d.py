@@ -44,7 +44,7 @@ class ImpDrv2D:
         Euler, 2 two-step backward, 3 midpoint (src/impdrv.f90:186-279).
         ispg (0 or 2), spg, spg2: the sponge towards the free stream; eps_e,
         buff: the explicit smoother and implicit damping (buff ones when
-        None); both with ilhs = 1."""
+        None)."""
         if ilhs not in (0, 1):
             raise ValueError("ilhs must be 0 or 1")
         if impl not in (1, 2, 3):

@@ -55,9 +55,7 @@ class Oracle2D:
         (midpoint), src/impdrv.f90:186-279; steps are counted from creation.
         ispg = 2, spg, spg2: the sponge towards the free stream
         (src/genmtrx.f90:436-446); eps_e, buff: the explicit smoother and
-        implicit damping (buff ones when None).  Both with ilhs = 1 only."""
-        if (ispg or eps_e) and ilhs == 0:
-            raise ValueError("the sponge and smoother are restated for ilhs = 1 only")
+        implicit damping (buff ones when None)."""
         if ispg not in (0, 2):
             raise ValueError("the nonlinear 2D step supports ispg 0 or 2")
         self.L = _lib(lib)

@@ -818,6 +818,16 @@ int a2_lhs2(const A2Grid* a2, const A3Ops* o, const double* dtl, const double* v
         M3(k, 5, 5) = M3(k, 5, 5) - bk[k - 1] * d * V[3];
       }
       for (int a = 1; a <= 5; ++a) M3(2, a, a) = M3(2, a, a) + one;
+      /* second-order damping (eps_i = 4 eps_e) and, in the eta LHS, the
+         sponge (src/lhs.f90:23-27,89-103 and 229-250) */
+      if (g->eps_e != zero) {
+        const double eps_i = 4.0 * g->eps_e;
+        const double ck[3] = {-alfa * eps_i, alfa * two * eps_i, -alfa * eps_i};
+        for (int k = 1; k <= 3; ++k)
+          for (int a = 1; a <= 5; ++a) M3(k, a, a) = M3(k, a, a) + ck[k - 1] * d * g->buff[p];
+      }
+      if (dir == 2 && g->ispg == 2)
+        for (int a = 1; a <= 5; ++a) M3(2, a, a) = M3(2, a, a) + alfa * d * (g->spg[p] + g->spg2[p]);
 #undef M3
     }
   if (dir == 2) {
@@ -874,6 +884,26 @@ int a2_lhs2(const A2Grid* a2, const A3Ops* o, const double* dtl, const double* v
           for (int a = 1; a <= 5; ++a)
             for (int b = 1; b <= 5; ++b) mat3[2 + 3 * (a - 1) + 15 * (b - 1) + 75 * rec] = zero;
         for (int a = 1; a <= 5; ++a) mat3[1 + 3 * (a - 1) + 15 * (a - 1) + 75 * rec] += one;
+        /* sponge through the transposed spgl(ny,nx) view, then the damping
+           of rows 2, ny-1 (-1, 2, -1) and 3, ny-2 (fb1..fb5)
+           (src/lhsbt2.f90:96-110,170-205,266-310,374-420,482-525,579-595) */
+        if (g->ispg == 2) {
+          const long q = (long)(j - 1) + (long)(i - 1) * ny;
+          for (int a = 1; a <= 5; ++a)
+            mat3[1 + 3 * (a - 1) + 15 * (a - 1) + 75 * rec] += alfa * d * (g->spg[q] + g->spg2[q]);
+        }
+        if (g->eps_e != zero && r >= 1 && r <= 4) {
+          const double fb[5] = {1.000000000000000E+00, -4.000000000000000E+00, 6.000000000000000E+00,
+                                -4.000000000000000E+00, 1.000000000000000E+00};
+          const double sb[3] = {-one, two, -one};
+          const int wide = r == 2 || r == 3;
+          for (int t = 0; t < (wide ? 5 : 3); ++t) {
+            const int c = wide ? j - 2 + t : j - 1 + t;
+            const Blk B = tri_blk(mat3, bc, rec, i - 1, j, c, ny);
+            const double cf = wide ? fb[t] : sb[t];
+            for (int a = 1; a <= 5; ++a) EB(B, a, a) = EB(B, a, a) + alfa * d * g->eps_e * g->buff[p] * cf;
+          }
+        }
       }
   }
   /* boundary conditions (nonlinear branches) */

@@ -162,7 +162,6 @@ def _params2d(**kw):
                                  dict(top=1), dict(nx=7), dict(ny=6), dict(Ma=1.0), dict(deta=0.0),
                                  dict(res_compat=3), dict(lhs_order=3), dict(lhs_order=2, ny=7), dict(impl=4),
                                  dict(impl=-1), dict(ispg=1), dict(eps_e=-0.5),
-                                 dict(lhs_order=2, eps_e=0.01), dict(lhs_order=2, ispg=2),
                                  dict(top=3, lhs_order=2)])
 def test_ctx2d_rejects_unsupported_options(lib, bad):
     ctx = ctypes.c_void_p()

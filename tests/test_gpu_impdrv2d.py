@@ -279,7 +279,8 @@ def test_time_scheme_argument_checks():
         make(c, impl=4)
 
 
-@pytest.mark.parametrize("kw", [dict(ispg=2), dict(eps_e=0.02), dict(ispg=2, eps_e=0.02)])
+@pytest.mark.parametrize("kw", [dict(ispg=2), dict(eps_e=0.02), dict(ispg=2, eps_e=0.02),
+                                dict(ispg=2, eps_e=0.02, ilhs=0)])
 def test_sponge_and_smoother_match_oracle(cuda, small, kw):
     """The nonlinear sponge (ispg 2, src/genmtrx.f90:436-446) and the
     explicit smoother / implicit damping (src/smoother.f90, src/lhsf.f90,
@@ -310,11 +311,16 @@ def test_sponge_and_smoother_match_oracle(cuda, small, kw):
     torch.cuda.synchronize()
     assert rel(host(dr, v.shape), r_ref) < RHS_TOL
     for direction in (1, 2):
-        ref = o.lhs(v, o.dtl, direction)
         mat = torch.zeros(125 * nx * ny, dtype=torch.float64, device="cuda")
         drv.lhs(direction, dv, mat)
         torch.cuda.synchronize()
-        assert rel(host(mat, ref.shape), ref) < OPS_TOL, direction
+        if kw.get("ilhs", 1) == 0:
+            ref = _dense_lines(direction, nx, ny, tri=o.lhs2(v, o.dtl, direction))
+            got = _dense_lines(direction, nx, ny, penta=host(mat, (5, 5, 5, nx, ny)))
+            assert rel(got, ref) < OPS_TOL, direction
+        else:
+            ref = o.lhs(v, o.dtl, direction)
+            assert rel(host(mat, ref.shape), ref) < OPS_TOL, direction
     from lns3d_gb300.cases import vortex2d
 
     c2 = vortex2d(nx=nx, ny=ny, seed=7)

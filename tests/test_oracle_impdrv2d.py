@@ -231,8 +231,11 @@ def test_sponge_and_smoother_steps():
     o.itrbc(v)
     res = [o.step(v) for _ in range(5)]
     assert np.isfinite(v).all() and all(r > 0 for r in res)
-    with pytest.raises(ValueError):
-        Oracle2D(c, ilhs=0, eps_e=0.01)
+    o2 = Oracle2D(c, ilhs=0, ispg=2, spg=spg, spg2=np.zeros((nx, ny)), eps_e=0.01)
+    v = c["v"].copy(order="F")
+    o2.itrbc(v)
+    res2 = [o2.step(v) for _ in range(5)]
+    assert np.isfinite(v).all() and all(r > 0 for r in res2)
 
 
 def test_held_top_boundary():
@@ -263,3 +266,52 @@ def test_held_top_boundary():
         o.step(v)
     assert np.isfinite(v).all()
     assert np.array_equal(v[:, :, -1], np.repeat(held[:, None], nx, axis=1))
+
+
+def test_second_order_damping_and_sponge_known_answer():
+    """iLHS = 0 (src/lhs.f90:23-27, 89-103, 229-250; src/lhsbt2.f90): the band
+    gains c_k dtl buff on its diagonals, c = alfa eps_i (-1, 2, -1) with
+    eps_i = 4 eps_e; the eta band diagonal gains alfa dtl (spg + spg2); the
+    boundary rows 2 and ny-1 gain alfa dtl eps_e buff (-1, 2, -1)."""
+    import ctypes
+
+    from lns3d_gb300.cases import vortex2d
+
+    nx, ny = 24, 20
+    c = vortex2d(nx=nx, ny=ny)
+    rng = np.random.default_rng(8)
+    spg = np.asfortranarray(rng.uniform(size=(nx, ny)))
+    spg2 = np.asfortranarray(0.5 * rng.uniform(size=(nx, ny)))
+    buff = np.asfortranarray(0.5 + rng.uniform(size=(nx, ny)))
+    plain = Oracle2D(c, ilhs=0)
+    o = Oracle2D(c, ilhs=0, ispg=2, spg=spg, spg2=spg2, eps_e=0.02, buff=buff)
+    v = c["v"].copy(order="F")
+    o.L.a3_set_time_step(ctypes.byref(o.g.g), ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(o.dtl.ctypes.data))
+    dtl = o.dtl.copy(order="F")
+    for orc in (plain, o):
+        orc.genmtrx(v)
+    alfa = c["params"]["alfa"]
+    eps_i = 4.0 * 0.02
+    ck = [-alfa * eps_i, alfa * 2.0 * eps_i, -alfa * eps_i]
+    m_p, _ = plain.lhs2(v, dtl, 1)
+    m_s, _ = o.lhs2(v, dtl, 1)
+    d = m_s - m_p
+    scale = np.abs(m_p).max()
+    for k in range(3):
+        for a in range(5):
+            assert np.abs(d[k, a, a, :, 1:-1] - ck[k] * dtl[:, 1:-1] * buff[:, 1:-1]).max() <= 1e-15 * scale
+    m_p, b_p = plain.lhs2(v, dtl, 2)
+    m_s, b_s = o.lhs2(v, dtl, 2)
+    d = m_s - m_p
+    scale = np.abs(m_p).max()
+    for a in range(5):
+        want = ck[1] * dtl[:, 4:-4] * buff[:, 4:-4] + alfa * dtl[:, 4:-4] * (spg + spg2)[:, 4:-4]
+        assert np.abs(d[1, a, a, :, 4:-4] - want).max() <= 1e-15 * scale
+    flat = (spg + spg2).ravel(order="F")
+    w = alfa * dtl * 0.02 * buff
+    for jj in (1, ny - 2):
+        quirk = np.array([flat[jj + iv * ny] for iv in range(nx)])
+        for k, cc in ((0, -1.0), (1, 2.0), (2, -1.0)):
+            want = w[:, jj] * cc + (alfa * dtl[:, jj] * quirk if k == 1 else 0.0)
+            for a in range(5):
+                assert np.abs(d[k, a, a, :, jj] - want).max() <= 1e-15 * scale
