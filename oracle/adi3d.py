@@ -18,7 +18,7 @@ class A3Grid(ctypes.Structure):
                 ("optx", I), ("opty", I)] + [(k, P) for k in
                                              ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")] + \
         [("resacc", P), ("ispg", I), ("spg", P), ("spg2", P), ("eps_e", D), ("buff", P), ("vm", P), ("xc", P),
-         ("wamp", P), ("x0", D), ("cvic", P)]
+         ("wamp", P), ("x0", D), ("cvic", P), ("bump", P)]
 
 
 class A3Ops(ctypes.Structure):
@@ -58,7 +58,7 @@ class Oracle3D:
     """Holds the oracle's grid struct, operators and factor arrays for one case."""
 
     def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, res_compat=False, ispg=0, spg=None,
-                 spg2=None, eps_e=0.0, buff=None, x0=0.0, wamp=None, cvic=None):
+                 spg2=None, eps_e=0.0, buff=None, x0=0.0, wamp=None, cvic=None, bump=None):
         """ispg, spg, spg2: the sponge (0 none, 1 spg, > 4 spg + spg2), spg
         and spg2 (nx, ny) as the reference's sponge setup leaves them.
         eps_e, buff: the explicit smoother and implicit damping, buff (nx, ny)
@@ -92,6 +92,9 @@ class Oracle3D:
             self._cvic = np.asfortranarray(cvic if cvic is not None else np.zeros((5, nx, ny)), dtype=np.complex128)
             self.g.vm, self.g.xc, self.g.wamp = ptr(self._vm).value, ptr(self._xc).value, ptr(self._wamp).value
             self.g.x0, self.g.cvic = x0, ptr(self._cvic).value
+        if p["wall"] == 3:  # the bump wall's u1w, u2w, u3w, tw, twp, complex (5, nx)
+            self._bump = np.asfortranarray(bump, dtype=np.complex128).reshape((5, nx), order="F")
+            self.g.bump = ptr(self._bump).value
         if eps_e:
             self.buff = np.asfortranarray(buff if buff is not None else np.ones((nx, ny)),
                                           dtype=np.float64).reshape((nx, ny), order="F")

@@ -638,13 +638,21 @@ void a3_rhsbc(const A3Grid* g, double* rl, const double* vl) {
         for (int pt = 0; pt < 2; ++pt) {
 #define VR(k, jj) vl[2 * ((k) + 5 * IX(g, i, jj)) + pt]
 #define RV(k, jj) rl[2 * ((k) + 5 * IX(g, i, jj)) + pt]
-          for (int k = 1; k <= 3; ++k) RV(k, 1) = -(VR(k, 1) - zero);
+#define BW(k) g->bump[10 * (i - 1) + 2 * (k) + pt] /* u1w u2w u3w tw twp */
+          if (g->wall == 3)
+            for (int k = 1; k <= 3; ++k) RV(k, 1) = -(VR(k, 1) - BW(k - 1));
+          else
+            for (int k = 1; k <= 3; ++k) RV(k, 1) = -(VR(k, 1) - zero);
           if (g->wall == 1)
             RV(0, 1) = gc1 * VR(0, 1) + gc2 * VR(0, 2) + gc3 * VR(0, 3) + gc4 * VR(0, 4) + gc5 * VR(0, 5);
           if (g->wall == 2) RV(0, 1) = VR(0, 1) - two * VR(0, 2) + VR(0, 3);
-          if (g->wallt == 0) RV(4, 1) = zero;
-          if (g->wallt == 1)
+          if (g->wall == 3) RV(0, 1) = VR(0, 1) - (4.0 * VR(0, 2) - 6.0 * VR(0, 3) + 4.0 * VR(0, 4) - VR(0, 5));
+          if (g->wallt == 0) RV(4, 1) = g->wall == 3 ? -(VR(4, 1) - BW(3)) : zero;
+          if (g->wallt == 1) {
             RV(4, 1) = gc1 * VR(4, 1) + gc2 * VR(4, 2) + gc3 * VR(4, 3) + gc4 * VR(4, 4) + gc5 * VR(4, 5);
+            if (g->wall == 3) RV(4, 1) = RV(4, 1) - BW(4);
+          }
+#undef BW
         }
     }
     if (g->top == 0)
@@ -692,11 +700,19 @@ void a3_itrbc(const A3Grid* g, double* vl) {
     if (g->navier) {
       for (int i = 1; i <= nx; ++i)
         for (int pt = 0; pt < 2; ++pt) {
-          for (int k = 1; k <= 3; ++k) VR(k, 1) = zero;
+#define BW(k) g->bump[10 * (i - 1) + 2 * (k) + pt] /* u1w u2w u3w tw twp */
+          for (int k = 1; k <= 3; ++k) VR(k, 1) = g->wall == 3 ? BW(k - 1) : zero;
           if (g->wall == 1) VR(0, 1) = -(gc2 * VR(0, 2) + gc3 * VR(0, 3) + gc4 * VR(0, 4) + gc5 * VR(0, 5)) / gc1;
           if (g->wall == 2) VR(0, 1) = two * VR(0, 2) - VR(0, 3);
-          if (g->wallt == 0) VR(4, 1) = zero;
-          if (g->wallt == 1) VR(4, 1) = -(gc2 * VR(4, 2) + gc3 * VR(4, 3) + gc4 * VR(4, 4) + gc5 * VR(4, 5)) / gc1;
+          if (g->wall == 3) VR(0, 1) = 4.0 * VR(0, 2) - 6.0 * VR(0, 3) + 4.0 * VR(0, 4) - VR(0, 5);
+          if (g->wallt == 0) VR(4, 1) = g->wall == 3 ? BW(3) : zero;
+          if (g->wallt == 1) {
+            if (g->wall == 3)
+              VR(4, 1) = (BW(4) - (gc2 * VR(4, 2) + gc3 * VR(4, 3) + gc4 * VR(4, 4) + gc5 * VR(4, 5))) / gc1;
+            else
+              VR(4, 1) = -(gc2 * VR(4, 2) + gc3 * VR(4, 3) + gc4 * VR(4, 4) + gc5 * VR(4, 5)) / gc1;
+          }
+#undef BW
         }
     }
     if (g->top == 0)
@@ -843,6 +859,12 @@ int a3_lhs(const A3Grid* g, const A3Ops* o, const double* dtl, int dir, double* 
           for (int k = 1; k <= 5; ++k)
             for (int b = 1; b <= 5; ++b) MRE(k, 1, b, p) = zero, MIM(k, 1, b, p) = zero;
           for (int t = 0; t < 5; ++t) MRE(sl[t], 1, 1, p) = -gcs[t];
+        }
+        if (g->wall == 3) { /* third-order extrapolation, src/lhsbc2f3d.f90:41-48 */
+          const double ex3[5] = {-one, 4.0, -6.0, 4.0, -one};
+          for (int k = 1; k <= 5; ++k)
+            for (int b = 1; b <= 5; ++b) MRE(k, 1, b, p) = zero, MIM(k, 1, b, p) = zero;
+          for (int t = 0; t < 5; ++t) MRE(sl[t], 1, 1, p) = ex3[t];
         }
         for (int a = 2; a <= 4; ++a)
           for (int k = 1; k <= 5; ++k)

@@ -62,6 +62,9 @@ typedef struct {
   const double *vm, *xc, *wamp;
   double x0;
   const double* cvic;
+  /* the bump wall (wall = 3, src/rhsbc3d.f90:45-104, src/itrbc3d.f90:46-121):
+     u1w, u2w, u3w, tw, twp of src/genbump.f90, complex (5,nx) */
+  const double* bump;
 } A3Grid;
 
 /* Frozen operators of the linear step (outputs of genmtrx(vm, kz, vm)). */

@@ -346,3 +346,45 @@ def test_forced_top_boundary_known_answer():
         o.step(v)
     assert np.isfinite(v).all()
     assert np.abs(v[:, :-1, -1] - t[:, :-1]).max() <= 1e-13 * np.abs(t).max()
+
+
+@pytest.mark.parametrize("wallt", [0, 1])
+def test_bump_wall_known_answer(wallt):
+    """wall = 3, the bump (src/itrbc3d.f90:46-121, src/rhsbc3d.f90:45-104,
+    src/lhsbc2f3d.f90:41-48): itrBC3D puts the bump's velocities u1w..u3w on
+    the wall, rho by third-order extrapolation, T = tw (isothermal) or from
+    the gc closure set to twp (adiabatic); rhsBC3D gives the matching
+    residual rows; the continuity row of the eta LHS is (-1, 4, -6, 4, -1)."""
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 24, 20
+    case = shear_layer(nx=nx, ny=ny, seed=1)
+    case = dict(case, params=dict(case["params"], wall=3, wallt=wallt))
+    rng = np.random.default_rng(6)
+    bump = 1e-3 * (rng.standard_normal((5, nx)) + 1j * rng.standard_normal((5, nx)))
+    o = Oracle3D(case, cflmax=20.0, loctime=1, bump=bump)
+    L = _lib()
+    v = np.asfortranarray(rng.standard_normal((5, nx, ny)) + 1j * rng.standard_normal((5, nx, ny)))
+    w = v.copy(order="F")
+    L.a3_itrbc(ctypes.byref(o.g), ptr(w))
+    assert np.array_equal(w[1:4, :-1, 0], bump[0:3, :-1])
+    assert np.allclose(w[0, :, 0], 4 * w[0, :, 1] - 6 * w[0, :, 2] + 4 * w[0, :, 3] - w[0, :, 4], rtol=0, atol=1e-13)
+    gc = [-2.083333333333333333333E+00, 4.0, -3.0, 1.333333333333333333333E+00, -2.5E-01]
+    if wallt == 0:
+        assert np.array_equal(w[4, :-1, 0], bump[3, :-1])
+    else:
+        s = sum(gc[k] * w[4, :, k] for k in range(5))
+        assert np.allclose(s[:-1], bump[4, :-1], rtol=0, atol=1e-12)
+    r = np.asfortranarray(rng.standard_normal((5, nx, ny)) + 0j)
+    L.a3_rhsbc(ctypes.byref(o.g), ptr(r), ptr(v))
+    assert np.allclose(r[1:4, :-1, 0], -(v[1:4, :-1, 0] - bump[0:3, :-1]), rtol=0, atol=1e-14)
+    want0 = v[0, :, 0] - (4.0 * v[0, :, 1] - 6.0 * v[0, :, 2] + 4.0 * v[0, :, 3] - v[0, :, 4])
+    assert np.allclose(r[0, :-1, 0], want0[:-1], rtol=0, atol=1e-13)
+    m = o.lhs(2)
+    for i, s_ in enumerate([3, 4, 5, 1, 2]):
+        assert m[s_ - 1, 0, 0, 0, 0] == [-1.0, 4.0, -6.0, 4.0, -1.0][i]
+    assert not m[:, 0, 1:, :, 0].any()
+    v = case["v"].copy(order="F")
+    for _ in range(3):
+        o.step(v)
+    assert np.isfinite(v).all() and np.array_equal(v[1:4, :-1, 0], bump[0:3, :-1])
