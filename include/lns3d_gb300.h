@@ -300,7 +300,7 @@ int lns_cpenta2bc_mixed_static_dev(int32_t n, int32_t nsys, int32_t nblk, const 
  *                           on the GPU; the next step factors the LHS again
  *   lns_step3d / _dev       nsteps implicit steps of niter correctors
  * Supported options: xper = 1 (periodic xi sweep, cpenta2p), yper = 0 with a
- * viscous wall at j = 1 (navier = 1, wall 1 or 2, wallt 0 or 1) and a
+ * viscous wall at j = 1 (navier = 1, wall 1, 2 or 3 (the bump), wallt 0 or 1) and a
  * zero-disturbance top (top = 0) or a top forced by an incoming acoustic
  * wave (top = 1, lns_upload_inflow3d); optx, opty any; constant viscosity
  * (mattyp 0); the sponges (ispg) and the smoother (eps_e) below; no damper
@@ -384,6 +384,12 @@ int lns_upload_inflow3d(lns_ctx3d* ctx, const double* x, const double* wamp, dou
 /* ispg 4: the eigenfunction target cvic, complex (5,nx,ny) as interleaved
  * doubles (src/sponge.f90:558-579). */
 int lns_upload_sponge_target3d(lns_ctx3d* ctx, const double* cvic);
+/* wall 3 (the bump, src/genbump.f90): u1w, u2w, u3w, tw, twp, complex (5,nx)
+ * as interleaved doubles; the wall row holds these velocities, rho by
+ * third-order extrapolation, T = tw (wallt 0) or the gc closure equal to twp
+ * (wallt 1) (src/itrbc3d.f90:46-121, src/rhsbc3d.f90:45-104,
+ * src/lhsbc2f3d.f90:41-48).  Needed before the first step. */
+int lns_upload_bump3d(lns_ctx3d* ctx, const double* bump);
 /* The smoother weight buff(nx,ny) of the host's buffer setup (src/buffer.f90,
  * ibuff > 0); only for eps_e != 0; invalidates the factored LHS. */
 int lns_upload_buffer3d(lns_ctx3d* ctx, const double* buff);

@@ -51,11 +51,12 @@ class ImpDrv3D:
     buff (nx, ny) or None for the reference's default of ones.  ispg 2, 3
     and the forced top (params top = 1) take the x coordinates x (nx, ny),
     x0 and wamp (nx; None: ones); ispg 4 the complex target cvic (5, nx, ny).
+    wall = 3 (the bump) takes u1w, u2w, u3w, tw, twp as bump, complex (5, nx).
     """
 
     def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False,
                  impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None, x=None, x0=0.0, wamp=None,
-                 cvic=None):
+                 cvic=None, bump=None):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -87,6 +88,9 @@ class ImpDrv3D:
             cv = np.asfortranarray(cvic, dtype=np.complex128)
             check(lib().lns_upload_sponge_target3d(self._ctx, ctypes.c_void_p(cv.ctypes.data)),
                   "lns_upload_sponge_target3d")
+        if int(p["wall"]) == 3:
+            bb = np.asfortranarray(bump, dtype=np.complex128)
+            check(lib().lns_upload_bump3d(self._ctx, ctypes.c_void_p(bb.ctypes.data)), "lns_upload_bump3d")
         if eps_e and buff is not None:
             b = np.asfortranarray(buff, dtype=np.float64)
             check(lib().lns_upload_buffer3d(self._ctx, ctypes.c_void_p(b.ctypes.data)), "lns_upload_buffer3d")

@@ -326,6 +326,8 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
     if (a >= 2 && a <= 4) return store_el(mat, q, ident);
     if ((a == 1 && g.wall == 1) || (a == 5 && g.wallt == 1))
       return store_el(mat, q, b == a ? cd{-pick5(tk, gc1, gc2, gc3, gc4, gc5), 0.0} : zero);
+    if (a == 1 && g.wall == 3)  // third-order extrapolation, src/lhsbc2f3d.f90:41-48
+      return store_el(mat, q, b == 1 ? cd{pick5(tk, -1.0, 4.0, -6.0, 4.0, -1.0), 0.0} : zero);
     if (a == 5 && g.wallt == 0) return store_el(mat, q, ident);
   }
   const double h = dir == 1 ? g.dxi : g.deta, alfa = g.alfa;
@@ -558,16 +560,26 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
     if (!g.yper) {
       if (g.navier && j == 1) {
         auto W = [&](int k, int jj) -> const cd& { return vs[k + 5 * pix(g, i, jj)]; };
-        for (int m = 1; m <= 3; ++m) r[m] = cd{-(W(m, 1).x - 0.0), -(W(m, 1).y - 0.0)};
+        // the bump wall (wall 3, src/rhsbc3d.f90:45-104): u1w..u3w, tw, twp
+        const cd* BW = g.wall == 3 ? reinterpret_cast<const cd*>(o.bump) + 5 * (i - 1) : nullptr;
+        for (int m = 1; m <= 3; ++m) {
+          const cd u = BW ? BW[m - 1] : cd{0.0, 0.0};
+          r[m] = cd{-(W(m, 1).x - u.x), -(W(m, 1).y - u.y)};
+        }
         if (g.wall == 1)
           r[0] = cd{gc1 * W(0, 1).x + gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x,
                     gc1 * W(0, 1).y + gc2 * W(0, 2).y + gc3 * W(0, 3).y + gc4 * W(0, 4).y + gc5 * W(0, 5).y};
         if (g.wall == 2)
           r[0] = cd{W(0, 1).x - two * W(0, 2).x + W(0, 3).x, W(0, 1).y - two * W(0, 2).y + W(0, 3).y};
-        if (g.wallt == 0) r[4] = cd{0.0, 0.0};
-        if (g.wallt == 1)
+        if (g.wall == 3)
+          r[0] = cd{W(0, 1).x - (4.0 * W(0, 2).x - 6.0 * W(0, 3).x + 4.0 * W(0, 4).x - W(0, 5).x),
+                    W(0, 1).y - (4.0 * W(0, 2).y - 6.0 * W(0, 3).y + 4.0 * W(0, 4).y - W(0, 5).y)};
+        if (g.wallt == 0) r[4] = BW ? cd{-(W(4, 1).x - BW[3].x), -(W(4, 1).y - BW[3].y)} : cd{0.0, 0.0};
+        if (g.wallt == 1) {
           r[4] = cd{gc1 * W(4, 1).x + gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x,
                     gc1 * W(4, 1).y + gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y};
+          if (BW) r[4] = cd{r[4].x - BW[4].x, r[4].y - BW[4].y};
+        }
       }
       if (g.top == 0 && j == g.ny)
         #pragma unroll
@@ -616,7 +628,8 @@ __global__ void __launch_bounds__(128, 4) rhs_kernel(Grid g, Ops o, const cd* __
 // column i (wall row j = 1 from rows 2..5, top row j = ny); with a periodic
 // x direction the remaining threads copy the interior rows of column 1 to
 // column nx, and the thread of column 1 copies its boundary rows.
-__device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const double* __restrict__ ttop, int bx) {
+__device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const double* __restrict__ ttop,
+                                        const double* __restrict__ bump, int bx) {
   const int t = bx * blockDim.x + threadIdx.x;
   const int ncol = g.xper ? g.nx - 1 : g.nx;
   if (t < ncol) {
@@ -624,15 +637,25 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
     auto W = [&](int k, int jj) -> cd& { return v[k + 5 * pix(g, i, jj)]; };
     if (!g.yper) {
       if (g.navier) {
-        for (int m = 1; m <= 3; ++m) W(m, 1) = cd{0.0, 0.0};
+        // the bump wall (wall 3, src/itrbc3d.f90:46-121): u1w..u3w, tw, twp
+        const cd* BW = g.wall == 3 ? reinterpret_cast<const cd*>(bump) + 5 * (i - 1) : nullptr;
+        for (int m = 1; m <= 3; ++m) W(m, 1) = BW ? BW[m - 1] : cd{0.0, 0.0};
         if (g.wall == 1)
           W(0, 1) = cd{-(gc2 * W(0, 2).x + gc3 * W(0, 3).x + gc4 * W(0, 4).x + gc5 * W(0, 5).x) / gc1,
                        -(gc2 * W(0, 2).y + gc3 * W(0, 3).y + gc4 * W(0, 4).y + gc5 * W(0, 5).y) / gc1};
         if (g.wall == 2) W(0, 1) = cd{two * W(0, 2).x - W(0, 3).x, two * W(0, 2).y - W(0, 3).y};
-        if (g.wallt == 0) W(4, 1) = cd{0.0, 0.0};
-        if (g.wallt == 1)
-          W(4, 1) = cd{-(gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x) / gc1,
-                       -(gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y) / gc1};
+        if (g.wall == 3)
+          W(0, 1) = cd{4.0 * W(0, 2).x - 6.0 * W(0, 3).x + 4.0 * W(0, 4).x - W(0, 5).x,
+                       4.0 * W(0, 2).y - 6.0 * W(0, 3).y + 4.0 * W(0, 4).y - W(0, 5).y};
+        if (g.wallt == 0) W(4, 1) = BW ? BW[3] : cd{0.0, 0.0};
+        if (g.wallt == 1) {
+          if (BW)
+            W(4, 1) = cd{(BW[4].x - (gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x)) / gc1,
+                         (BW[4].y - (gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y)) / gc1};
+          else
+            W(4, 1) = cd{-(gc2 * W(4, 2).x + gc3 * W(4, 3).x + gc4 * W(4, 4).x + gc5 * W(4, 5).x) / gc1,
+                         -(gc2 * W(4, 2).y + gc3 * W(4, 3).y + gc4 * W(4, 4).y + gc5 * W(4, 5).y) / gc1};
+        }
       }
       if (g.top == 0)
         for (int m = 0; m < 5; ++m) W(m, g.ny) = cd{0.0, 0.0};
@@ -653,8 +676,9 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
   }
 }
 
-__global__ void bc_kernel(Grid g, cd* __restrict__ v, const double* __restrict__ ttop) {
-  bc_body(g, v, ttop, blockIdx.x);
+__global__ void bc_kernel(Grid g, cd* __restrict__ v, const double* __restrict__ ttop,
+                          const double* __restrict__ bump) {
+  bc_body(g, v, ttop, bump, blockIdx.x);
 }
 
 // ------------------------------------------------------------- batching
@@ -685,7 +709,7 @@ __global__ void bc_batch_kernel(const StepArgs* __restrict__ list, const int2* _
                                 const int* __restrict__ active) {
   const int2 w = table[blockIdx.x];
   if (!active[w.x]) return;
-  bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, w.y);
+  bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, list[w.x].o.bump, w.y);
 }
 __global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4* __restrict__ table,
                                    const int* __restrict__ active) {
@@ -785,6 +809,8 @@ struct lns_ctx3d {
   double *spg_a = nullptr, *spg_b = nullptr, *vt = nullptr;  // the target sponges (ispg 2-4)
   double *xc = nullptr, *wamp = nullptr;  // ispg 2, 3 or top 1: x(nx,ny), wamp(nx) (ones until uploaded)
   double* ttop = nullptr;                 // top 1: the wave of row ny, complex (5,nx)
+  double* bump = nullptr;                 // wall 3: u1w, u2w, u3w, tw, twp, complex (5,nx)
+  bool have_bump = false;
   double x0 = 0.0;
   bool have_inflow = false, have_target = false;
   double* buff = nullptr;     // eps_e != 0: buff(nx,ny), ones until uploaded
@@ -1013,7 +1039,7 @@ int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
   const long long n = 5 * c->np;
   if (add) lns::a3::add_kernel<cd, RT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, r);
   const int nt = g.nx + g.ny;
-  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v, c->ops.ttop);
+  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v, c->ops.ttop, c->ops.bump);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "update kernels launch");
 }
@@ -1098,7 +1124,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
   if (p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: only a periodic xi direction (xper = 1) is supported");
   if (p->yper != 0 || p->navier != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: need yper = 0 and navier = 1");
-  if (p->wall != 1 && p->wall != 2) return fail3(LNS_ERR_ARG, "ctx3d_create: wall must be 1 or 2");
+  if (p->wall != 1 && p->wall != 2 && p->wall != 3) return fail3(LNS_ERR_ARG, "ctx3d_create: wall must be 1, 2 or 3");
   if (p->wallt != 0 && p->wallt != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: wallt must be 0 or 1");
   if (p->top != 0 && p->top != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0 or 1");
   if (p->loctime != 0 && p->loctime != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: loctime must be 0 or 1");
@@ -1156,6 +1182,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
     A(sizeof(double) * p->nx, &q); c->wamp = (double*)q;
   }
   if (p->top == 1) { A(sizeof(double) * 10 * p->nx, &q); c->ttop = (double*)q; }
+  if (p->wall == 3) { A(sizeof(double) * 10 * p->nx, &q); c->bump = (double*)q; }
   if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
@@ -1237,6 +1264,8 @@ int need_data(const lns_ctx3d* c, const char* who) {
   if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1) && !c->have_inflow)
     return fail3(LNS_ERR_ARG,
                  std::string(who) + ": ispg 2, 3 or top 1: upload the wave data (lns_upload_inflow3d) first");
+  if (c->prm.wall == 3 && !c->have_bump)
+    return fail3(LNS_ERR_ARG, std::string(who) + ": wall 3: upload the bump (lns_upload_bump3d) first");
   if (c->prm.ispg == 4 && !c->have_target)
     return fail3(LNS_ERR_ARG, std::string(who) + ": ispg 4: upload the sponge target (lns_upload_sponge_target3d) first");
   return LNS_OK;
@@ -1302,6 +1331,18 @@ int lns_upload_inflow3d(lns_ctx3d* c, const double* x, const double* wamp, doubl
   c->x0 = x0;
   c->have_inflow = true;
   return make_inflow_target(c);
+}
+
+int lns_upload_bump3d(lns_ctx3d* c, const double* bump) {
+  if (!c || !bump) return fail3(LNS_ERR_ARG, "upload_bump3d: null argument");
+  if (c->prm.wall != 3) return fail3(LNS_ERR_ARG, "upload_bump3d: needs wall 3");
+  int rc = check_device(c);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(c->bump, bump, sizeof(double) * 10 * c->g.nx, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda3(e, "upload bump");
+  c->ops.bump = c->bump;
+  c->have_bump = true;
+  return LNS_OK;
 }
 
 int lns_upload_sponge_target3d(lns_ctx3d* c, const double* cvic) {
@@ -1732,7 +1773,7 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
   for (int p = 0; p < nprob; ++p)
     if (params[p].impl > 1) return fail3(LNS_ERR_ARG, "batch3d_create: batches run impl = 1 (backward Euler)");
   for (int p = 0; p < nprob; ++p)
-    if (params[p].ispg != 0 || params[p].eps_e != 0.0 || params[p].top != 0)
+    if (params[p].ispg != 0 || params[p].eps_e != 0.0 || params[p].top != 0 || params[p].wall == 3)
       return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge, smoother or forced top (ispg = 0, "
                                 "eps_e = 0, top = 0)");
   lns_batch3d* b = new lns_batch3d();
@@ -2103,7 +2144,7 @@ int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* 
   if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
   if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
   if (prm->impl > 1) return fail3(LNS_ERR_ARG, "server3d_submit: servers run impl = 1 (backward Euler)");
-  if (prm->ispg != 0 || prm->eps_e != 0.0 || prm->top != 0)
+  if (prm->ispg != 0 || prm->eps_e != 0.0 || prm->top != 0 || prm->wall == 3)
     return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge, smoother or forced top (ispg = 0, "
                               "eps_e = 0, top = 0)");
   if (!(tol > 0.0) || max_steps < 1) return fail3(LNS_ERR_ARG, "server3d_submit: need tol > 0 and max_steps >= 1");

@@ -93,6 +93,8 @@ struct Ops {
   const double* vt = nullptr;
   // the forced top boundary (top = 1): its wave at row ny, complex (5,nx)
   const double* ttop = nullptr;
+  // the bump wall (wall = 3): u1w, u2w, u3w, tw, twp, complex (5,nx)
+  const double* bump = nullptr;
   // explicit smoother / implicit damping: eps_e buff(nx,ny); null when eps_e = 0
   const double* buff = nullptr;
   double eps_e = 0.0;

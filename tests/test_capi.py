@@ -146,6 +146,7 @@ def test_ctx3d_null_arguments(lib):
     assert lib.lns_upload_buffer3d(None, None) == 1
     assert lib.lns_upload_inflow3d(None, None, None, 0.0) == 1
     assert lib.lns_upload_sponge_target3d(None, None) == 1
+    assert lib.lns_upload_bump3d(None, None) == 1
 
 
 def _params2d(**kw):

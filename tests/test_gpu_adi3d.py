@@ -581,3 +581,50 @@ def test_forced_top_boundary_matches_oracle(cuda):
         res_gpu = drv.step(v_gpu, nsteps=1)[0]
         assert np.abs(v_gpu - v_ref).max() / max(np.abs(v_ref).max(), scale_t) < STEP_TOL, s
         assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
+
+
+@pytest.mark.parametrize("wallt", [0, 1])
+def test_bump_wall_matches_oracle(cuda, wallt):
+    """wall = 3, the bump (src/itrbc3d.f90:46-121, src/rhsbc3d.f90:45-104,
+    src/lhsbc2f3d.f90:41-48): eta LHS, RHS and steps against the oracle."""
+    import ctypes
+
+    import torch
+    from adi3dcase import _lib, ptr
+
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    nx, ny = 40, 33
+    case = shear_layer(nx=nx, ny=ny, seed=13)
+    case = dict(case, params=dict(case["params"], wall=3, wallt=wallt))
+    rng = np.random.default_rng(16)
+    bump = np.asfortranarray(1e-3 * (rng.standard_normal((5, nx)) + 1j * rng.standard_normal((5, nx))))
+    orc = Oracle3D(case, cflmax=20.0, loctime=1, bump=bump)
+    mk = lambda: ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, bump=bump)
+    drv = mk()
+    mat = torch.zeros(125 * nx * ny, dtype=torch.complex128, device="cuda")
+    drv.lhs(2, mat)
+    torch.cuda.synchronize()
+    assert rel(mat.cpu().numpy().reshape((5, 5, 5, nx, ny), order="F"), orc.lhs(2)) < OPS_TOL
+    shape = (5, nx, ny)
+    v = np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+    vold = np.asfortranarray(v + 1e-3 * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)))
+    L = _lib()
+    r = orc.lrhs(v)
+    L.a3_rbe(ctypes.byref(orc.g), ptr(r), ptr(v), ptr(vold), ptr(orc.dtl))
+    L.a3_rhsbc(ctypes.byref(orc.g), ptr(r), ptr(v))
+    dev = lambda a: torch.from_numpy(a.ravel(order="F")).cuda()
+    dv, dvo = dev(v), dev(vold)
+    dr = torch.zeros_like(dv)
+    drv.rhs(dv, dvo, dr, torch.zeros(1, dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    assert rel(dr.cpu().numpy().reshape(shape, order="F"), r) < RHS_TOL
+    drv = mk()
+    v_ref = case["v"].copy(order="F")
+    v_gpu = case["v"].copy(order="F")
+    for s in range(4):
+        res_ref = orc.step(v_ref)
+        res_gpu = drv.step(v_gpu, nsteps=1)[0]
+        assert rel(v_gpu, v_ref) < STEP_TOL, s
+        assert abs(res_gpu - res_ref) <= 1e-10 * res_ref, s
