@@ -201,6 +201,17 @@ def time_reference_cpu(sample_reps=3):
                       % (sample_reps, t * 1e3)}
 
 
+def max_over_ranks(torch, x, dev, world):
+    """The largest x over the replicas (the timing rule of a multi-GPU run:
+    each rank times its own replica, the job takes as long as the slowest);
+    x itself on one rank."""
+    if world <= 1:
+        return x
+    t = torch.tensor([float(x)], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_mixed(torch, dev, L, sp, stream, rank, world, W, K, fp64_x, refine=2):
     """Times the mixed-precision solve (lns_cpenta2bc_mixed_dev, code 2) and
     checks the first timed step's solution against the FP64 direct one."""
@@ -228,10 +239,7 @@ def run_mixed(torch, dev, L, sp, stream, rank, world, W, K, fp64_x, refine=2):
     torch.cuda.synchronize()
     per_step = sorted(a.elapsed_time(b) for a, b in ev)
     total_ms = sum(per_step)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(torch, total_ms, dev, world)
     x = batches[W][1]
     err = float((x - fp64_x).abs().max() / fp64_x.abs().max())
     return {"value": world * PTS * K / (total_ms / 1e3), "ms_per_step": total_ms / K,
@@ -266,9 +274,7 @@ def run_e2e(torch, dev, L, rank, world, K):
     e2e_step(0)
     t = [e2e_step(s) for s in range(ke)]
     if world > 1:
-        tt = torch.tensor([max(t)], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        return world * PTS / float(tt.item())
+        return world * PTS / max_over_ranks(torch, max(t), dev, world)
     return PTS / statistics.mean(t)
 
 
@@ -661,10 +667,8 @@ def main():
     clk = Clocks(local)
     total_ms, per_step = time_steps(torch, d64, v64, K, stream)
     clocks = clk.stop()
+    total_ms = max_over_ranks(torch, total_ms, dev, world)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
         torch.distributed.barrier()
     value = world * PTS3 * K / (total_ms / 1e3)
 
@@ -688,10 +692,7 @@ def main():
     d32.profile(False)
     ph32 = {k: v / n32 for k, v in phases32.items()}
     kern32 = {k: v / n32 for k, v in seg32.items()}
-    if world > 1:
-        t = torch.tensor([total32], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total32 = float(t.item())
+    total32 = max_over_ranks(torch, total32, dev, world)
     mixed = {"value": world * PTS3 * K / (total32 / 1e3), "ms_per_step": total32 / K,
              "latency_ms": {"p50": percentile(per32, 0.5), "p99": percentile(per32, 0.99)},
              "phase_ms": ph32, "kernel_ms": kern32, "setup": setup32, "device_bytes": int(d32.device_bytes)}
@@ -727,10 +728,7 @@ def main():
             d64.step(hv, nsteps=1)
             t.append(time.perf_counter() - t0)
         tm = statistics.mean(t)
-        if world > 1:
-            tt = torch.tensor([tm], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            tm = float(tt.item())
+        tm = max_over_ranks(torch, tm, dev, world)
         e2e = {"value": world * PTS3 / tm, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": 5 * PTS3 * 16,
                "d2h_bytes_per_step": 5 * PTS3 * 16 + 8, "ms_per_step": tm * 1e3}
 
