@@ -15,6 +15,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIBNAME = "liblns3d_gb300.so"
+PROBE_NAME = "liblns3d_probe.so"
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -40,28 +41,52 @@ def build_library(verbose=False):
     srcs = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
     nvcc = _nvcc()
 
+    # an object newer than its source, every header and these flags is reused
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    deps += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    deps.append(os.path.abspath(__file__))
+    newest_dep = max(os.path.getmtime(d) for d in deps)
+
     def compile_one(src):
         obj = os.path.join(objdir, src[:-3] + ".o")
-        out = _run([nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
+        srcp = os.path.join(CSRC, src)
+        if os.path.exists(obj) and os.path.getmtime(obj) > max(newest_dep, os.path.getmtime(srcp)):
+            return obj
+        out = _run([nvcc] + NVCC_FLAGS + ["-c", srcp, "-o", obj])
         if verbose and out.strip():
             sys.stdout.write(out)
         return obj
 
-    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, min(8, len(srcs)))) as ex:
+    with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, min(8, len(srcs) + 1))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    target = os.path.join(LIBDIR, LIBNAME)
-    tmp = target + ".tmp"
-    _run([nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-lcudart"])
-    os.replace(tmp, target)
+        probe = ex.submit(build_probe)
+        target = os.path.join(LIBDIR, LIBNAME)
+        tmp = target + ".tmp"
+        _run([nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-lcudart"])
+        os.replace(tmp, target)
+        probe.result()
     return target
 
 
-def build_oracle():
-    _run(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+def build_probe():
+    """The benchmark's FP64 peak probe, outside the product library."""
+    out = os.path.join(LIBDIR, PROBE_NAME)
+    _run([_nvcc()] + NVCC_FLAGS + ["-shared", "-o", out + ".tmp", os.path.join(CSRC, "bench", "fp64_probe.cu")])
+    os.replace(out + ".tmp", out)
+    return out
 
 
-def build_all(verbose=False):
-    build_oracle()
+def build_oracle(refsrc=None):
+    """The checker libraries; with refsrc (the reference's src/ directory)
+    the reference's own sources are translated under oracle/_ref first."""
+    cmd = ["make", "-s", "-j4", "-C", os.path.join(ROOT, "oracle")]
+    if refsrc:
+        cmd.append("REFSRC=" + refsrc)
+    _run(cmd)
+
+
+def build_all(verbose=False, refsrc=None):
+    build_oracle(refsrc)
     return build_library(verbose=verbose)
 
 

@@ -26,10 +26,28 @@ grows, in the reference algorithm as here.
 
 Arrays are numpy, Fortran-ordered, with the reference shapes: metrics
 (nx, ny), vm (5, nx, ny), v (5, nx, ny) complex.
+
+The deck values carry the reference's own constants: gamma1 = 0.4 as
+src/init.f90:28 sets it (not gamma - 1, which differs in the last bit), and
+the spanwise wavenumber as src/input.f90 forms it from the deck's span,
+kz = 2 pi / Lz with Lz = 2 pi / beta.
 """
+import math
+
 import numpy as np
 
 GAMMA = 1.4
+GAMMA1 = 0.4
+
+
+def span_of(beta):
+    """The deck's Lz for a spanwise wavenumber beta (0: a 2D run)."""
+    return 2.0 * math.pi / beta if beta else 0.0
+
+
+def kz_of(Lz):
+    """kz as src/input.f90 forms it from the deck's Lz."""
+    return 2.0 * math.pi / Lz if Lz else 0.0
 
 
 def shear_layer(nx=512, ny=256, Lx=5.5, Ly=10.0, stretch=3.0, delta=1.0, Ma=0.8, Re=500.0, Pr=0.72,
@@ -67,7 +85,7 @@ def shear_layer(nx=512, ny=256, Lx=5.5, Ly=10.0, stretch=3.0, delta=1.0, Ma=0.8,
     pert *= amp / np.abs(pert).max()
     v = np.asfortranarray(pert.astype(np.complex128))
     params = dict(nx=nx, ny=ny, dxi=1.0 / (nx - 1), deta=1.0 / (ny - 1), Ma=Ma, Re=Re, Pr=Pr, gamma=GAMMA,
-                  gamma1=GAMMA - 1.0, omega=omega, kz=beta, alfa=1.0, xper=1, yper=0, navier=1, wall=1, wallt=1,
+                  gamma1=GAMMA1, omega=omega, kz=kz_of(span_of(beta)), alfa=1.0, xper=1, yper=0, navier=1, wall=1, wallt=1,
                   top=0, optx=-1, opty=-1)
     return dict(params=params, x=x, y=y, metrics=metrics, vm=vm, v=v)
 
@@ -144,7 +162,7 @@ def vortex2d(nx=128, ny=128, L=10.0, stretch=2.0, Ma=0.5, Re=1000.0, Pr=0.72, ci
     v[:, -1, :] = v[:, 0, :]        # periodic point
     pot = np.asfortranarray(v[:, :, -1].copy())   # rho, u, v, w, T on the top row
     params = dict(nx=nx, ny=ny, dxi=1.0 / (nx - 1), deta=1.0 / (ny - 1), Ma=Ma, Re=Re, Pr=Pr, gamma=GAMMA,
-                  gamma1=GAMMA - 1.0, omega=0.0, kz=0.0, alfa=1.0, xper=1, yper=0, navier=1, wall=0, wallt=1,
+                  gamma1=GAMMA1, omega=0.0, kz=0.0, alfa=1.0, xper=1, yper=0, navier=1, wall=0, wallt=1,
                   top=0, optx=-1, opty=-1)
     bnt = np.zeros((nx, 2), order="F")
     bnt[:, 1] = 1.0        # (n1, n2) / |n| at j = ny (src/gengrid.f90:141-142)

@@ -17,7 +17,7 @@ class A3Grid(ctypes.Structure):
                 ("loctime", I), ("xper", I), ("yper", I), ("navier", I), ("wall", I), ("wallt", I), ("top", I),
                 ("optx", I), ("opty", I)] + [(k, P) for k in
                                              ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")] + \
-        [("resacc", P), ("ispg", I), ("spg", P), ("spg2", P), ("eps_e", D), ("buff", P), ("vm", P), ("xc", P),
+        [("ispg", I), ("spg", P), ("spg2", P), ("eps_e", D), ("buff", P), ("vm", P), ("xc", P),
          ("wamp", P), ("x0", D), ("cvic", P), ("bump", P)]
 
 
@@ -57,7 +57,7 @@ def ptr(a):
 class Oracle3D:
     """Holds the oracle's grid struct, operators and factor arrays for one case."""
 
-    def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, res_compat=False, ispg=0, spg=None,
+    def __init__(self, case, cflmax=1.0, loctime=1, dtmax=1e30, lib=None, ispg=0, spg=None,
                  spg2=None, eps_e=0.0, buff=None, x0=0.0, wamp=None, cvic=None, bump=None):
         """ispg, spg, spg2: the sponge (0 none, 1 spg, > 4 spg + spg2), spg
         and spg2 (nx, ny) as the reference's sponge setup leaves them.
@@ -75,10 +75,6 @@ class Oracle3D:
                                              "omega", "kz", "alfa", "xper", "yper", "navier", "wall", "wallt",
                                              "top", "optx", "opty")},
                         **{k: ptr(v).value for k, v in self.keep.items()})
-        # the reference's running residual sum (its saved totres), when asked for
-        self.resacc = ctypes.c_double(0.0)
-        if res_compat:
-            self.g.resacc = ctypes.cast(ctypes.byref(self.resacc), P).value
         nx, ny = self.nx, self.ny
         if ispg:
             self.spg = np.asfortranarray(spg, dtype=np.float64).reshape((nx, ny), order="F")
@@ -113,6 +109,10 @@ class Oracle3D:
         self.per2x = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
         self.r = np.zeros((5, nx, ny), np.complex128, order="F")
         self.factored = I(0)
+
+    def itrbc(self, v):
+        """itrBC3D on v in place (src/itrbc3d.f90)."""
+        self.L.a3_itrbc(ctypes.byref(self.g), ptr(v))
 
     def step_impl(self, v, impl, niter=1):
         """One step of time scheme impl (1, 2, 3) on v in place; vold,

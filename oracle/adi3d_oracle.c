@@ -670,11 +670,11 @@ void a3_rhsbc(const A3Grid* g, double* rl, const double* vl) {
       for (int k = 0; k < 5; ++k) CRE(rl, k, g, nx, j) = zero, CIM(rl, k, g, nx, j) = zero;
 }
 
-/* src/resstat3d.f90:37-60: sqrt(sum |r|^2 / dtl^2 / (nx ny)); with
-   g->resacc the sum starts from the previous result, as the reference's
-   saved totres does (src/resstat3d.f90:18) */
+/* src/resstat3d.f90:37-60: sqrt(sum |r|^2 / dtl^2 / (nx ny)); the saved
+   totres of the reference is reset to zero at the end of each call
+   (src/resstat3d.f90:98), so each call's sum starts from zero */
 double a3_resstat(const A3Grid* g, const double* res, const double* dtl) {
-  double totres = g->resacc ? *g->resacc : 0.0;
+  double totres = 0.0;
   for (int j = 1; j <= g->ny; ++j)
     for (int i = 1; i <= g->nx; ++i) {
       double s = 0.0;
@@ -686,7 +686,6 @@ double a3_resstat(const A3Grid* g, const double* res, const double* dtl) {
       totres = totres + s / (d * d);
     }
   totres = sqrt(totres / (double)((long)g->nx * g->ny));
-  if (g->resacc) *g->resacc = totres;
   return totres;
 }
 

@@ -41,11 +41,6 @@ typedef struct {
   int xper, yper, navier, wall, wallt, top, optx, opty;
   /* metrics (nx,ny): m1 m2 n1 n2 m11 m12 m22 n11 n12 n22 */
   const double *m1, *m2, *n1, *n2, *m11, *m12, *m22, *n11, *n12, *n22;
-  /* NULL: resstat3D returns the residual of its own call.  Otherwise the
-     running sum of the reference (its totres keeps its value between calls,
-     src/resstat3d.f90:18): the sum starts from *resacc, and the result is
-     stored back into it. */
-  double* resacc;
   /* sponge (src/lrhs3d.f90:220-240, src/lhs2f3d.f90:207-224): ispg 0 none,
      1 spg, > 4 spg + spg2 (2..4 not restated); spg, spg2 (nx,ny) */
   int ispg;

@@ -47,7 +47,7 @@ def ptr(a):
 class Oracle2D:
     """Grid struct, operator storage and scratch of the oracle for one case."""
 
-    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, res_compat=False, ilhs=1, impl=1,
+    def __init__(self, case, cflmax=1.0, loctime=0, dtmax=1e30, lib=None, ilhs=1, impl=1,
                  ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None):
         """ilhs = 1: fourth-order LHS, pentadiagonal solves; ilhs = 0:
         second-order LHS, block-tridiagonal solves (src/impdrv.f90:307-344).
@@ -71,9 +71,6 @@ class Oracle2D:
                                          "kz", "alfa", "xper", "yper", "navier", "wall", "wallt", "top", "optx",
                                          "opty")},
                     **{k: ptr(v).value for k, v in self.keep.items()})
-        self.resacc = ctypes.c_double(0.0)
-        if res_compat:
-            g3.resacc = ctypes.cast(ctypes.byref(self.resacc), P).value
         if ispg:
             self.spg = np.asfortranarray(spg, dtype=np.float64).reshape((nx, ny), order="F")
             self.spg2 = np.asfortranarray(spg2, dtype=np.float64).reshape((nx, ny), order="F")

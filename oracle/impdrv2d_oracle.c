@@ -451,11 +451,10 @@ void a2_itrbc(const A2Grid* a2, double* vl) {
 #undef RV
 }
 
-/* src/resstat.f90:37-60; with g->resacc the sum starts from the previous
-   result (the reference's totres keeps its value, src/resstat.f90:17) */
+/* src/resstat.f90:37-60 (its saved totres is reset at the end of each call) */
 double a2_resstat(const A2Grid* a2, const double* res, const double* dtl) {
   const A3Grid* g = G(a2);
-  double totres = g->resacc ? *g->resacc : 0.0;
+  double totres = 0.0;
   for (int j = 1; j <= g->ny; ++j)
     for (int i = 1; i <= g->nx; ++i) {
       const double* r = res + 5 * IX(g, i, j);
@@ -464,7 +463,6 @@ double a2_resstat(const A2Grid* a2, const double* res, const double* dtl) {
       totres = totres + resnod;
     }
   totres = sqrt(totres / (double)((long)g->nx * g->ny));
-  if (g->resacc) *g->resacc = totres;
   return totres;
 }
 
