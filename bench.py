@@ -100,6 +100,17 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def fp64_probe():
+    """Live FP64 FMA rate of this GPU (TFLOP/s) from the probe library that
+    lns3d_gb300/_build.py builds beside the product library."""
+    from lns3d_gb300 import _build
+
+    L = ctypes.CDLL(os.path.join(_build.LIBDIR, _build.PROBE_NAME))
+    L.lns_probe_fp64_tflops.restype = ctypes.c_double
+    L.lns_probe_fp64_tflops.argtypes = []
+    return L.lns_probe_fp64_tflops()
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -751,7 +762,7 @@ def main():
         leg2d = run_impdrv2d(torch, dev, max(10, K), rank == 0 and not args.no_cpu_baseline)
 
     hbm_peak, peak_kind = peaks()
-    fp64_peak = L.lns_probe_fp64_tflops()
+    fp64_peak = fp64_probe()
     # the dominant kernel: the xi forward recurrence (chain_fwd_kernel<cd, 1>)
     dom = max(kern64, key=lambda k: kern64[k])
     achieved = KERNEL_BYTES[dom] * PTS3 / (kern64[dom] / 1e3) / 1e9

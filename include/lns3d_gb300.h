@@ -42,11 +42,6 @@ extern "C" {
 const char* lns_last_error(void);
 /* Library version string. */
 const char* lns_version(void);
-/* Measured FP64 fused multiply-add rate of the current device in TFLOP/s
- * (a short DFMA stream on every SM); the denominator of the FP64 roofline
- * that the line solvers are reported against.  No reference counterpart.
- * Returns a negative value on failure. */
-double lns_probe_fp64_tflops(void);
 
 /* ---------------------------------------------------------------------------
  * Real block-pentadiagonal solves with the 4th-order boundary-closure rows,
@@ -201,10 +196,12 @@ typedef struct {
   int32_t nx, ny;
   double dxi, deta;
   double Ma, Re, Pr, gamma;
+  double gamma1;             /* the reference's gamma1 module variable: 0.4 as src/init.f90:28
+                                sets it (not gamma - 1, which differs in the last bit); 0 means
+                                gamma - 1 */
   double alfa, cflmax, dtmax;
   double theta;              /* isothermal-wall recovery angle (wallt 0, src/itrbc.f90:683-686) */
   int32_t loctime, xper, yper, navier, wall, wallt, top, optx, opty;
-  int32_t res_compat;        /* as in lns_params3d (src/resstat.f90:17) */
   int32_t lhs_order;         /* 0 or 4: the fourth-order LHS with pentadiagonal solves (iLHS = 1);
                                 2: the second-order LHS (src/lhs.f90, src/lhsbt2.f90, src/lhsbc1.f90,
                                 src/lhsbc2.f90) with the block-tridiagonal solves solve2p (xi) and
@@ -322,19 +319,14 @@ int lns_cpenta2bc_mixed_static_dev(int32_t n, int32_t nsys, int32_t nblk, const 
 typedef struct {
   int32_t nx, ny;            /* grid points; with xper, point nx repeats point 1 */
   double dxi, deta;          /* computational spacings (src/gengrid.f90: 1/(nx-1), 1/(ny-1)) */
-  double Ma, Re, Pr, gamma;  /* src/input.f90 namelist values; gamma1 = gamma - 1 */
+  double Ma, Re, Pr, gamma;  /* src/input.f90 deck values */
+  double gamma1;             /* the reference's gamma1 (0.4, src/init.f90:28); 0 means gamma - 1 */
   double omega, beta;        /* temporal frequency and spanwise wavenumber kz = 2 pi / Lz */
   double alfa;               /* implicitness, 1 for backward Euler (impl = 1) */
   double cflmax, dtmax;      /* src/temporal.f90 time-step control */
   int32_t loctime;           /* 0 global time step, 1 local time step */
   int32_t xper, yper, navier, wall, wallt, top, optx, opty;
   int32_t precision;         /* LNS_FP64 or LNS_MIXED */
-  int32_t res_compat;        /* 0: totres of each corrector is the residual of
-                                that corrector.  1: the reference's reported
-                                value, whose sum keeps the previous result
-                                (its totres is saved between calls,
-                                src/resstat3d.f90:18), so that it levels off
-                                near 1/(nx*ny).  The step itself is the same. */
   int32_t impl;              /* time scheme (src/impdrv3d.f90:130-199): 1 (or 0)
                                 backward Euler with alfa; 2 two-step backward,
                                 backward Euler for the context's first step and
@@ -411,6 +403,8 @@ int lns_step3d(lns_ctx3d* ctx, double* v, int32_t nsteps, int32_t niter, double*
  * of nsteps doubles; enqueued on `stream`.  The first call after
  * lns_upload_mean3d factors the LHS and waits for the pivot check. */
 int lns_step3d_dev(lns_ctx3d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream);
+/* itrBC3D on a device state: the call before the step loop (src/impdrv3d.f90:125-126) */
+int lns_itrbc3d_dev(lns_ctx3d* ctx, double* v, void* stream);
 
 /* Inspection (device arrays, enqueued on `stream`), for parity checks.
  * r = rhsBC3D(rbe3D(lrhs3D(v), v, vold)) (src/lrhs3d.f90:2,
@@ -483,7 +477,8 @@ int lns_batch3d_get_state(lns_batch3d* batch, int32_t prob, double* v);
 #define LNS_REQ_RUNNING 2
 #define LNS_REQ_DONE 3      /* converged: residual <= tol */
 #define LNS_REQ_STOPPED 4   /* max_steps reached first */
-#define LNS_REQ_FAILED 5    /* could not be admitted (allocation or upload failed) */
+#define LNS_REQ_FAILED 5    /* could not be admitted (allocation or upload failed), or its
+                               result could not be read back */
 typedef struct lns_server3d lns_server3d;
 int lns_server3d_create(size_t budget_bytes, int32_t max_slots, int32_t precision, int32_t niter,
                         lns_server3d** server);
@@ -491,13 +486,16 @@ int lns_server3d_destroy(lns_server3d* server);
 /* copies the request's host arrays (as lns_batch3d_upload); *id names it */
 int lns_server3d_submit(lns_server3d* server, const lns_params3d* params, const double* metrics, const double* vm,
                         const double* v, double tol, int32_t max_steps, int64_t* id);
-/* admits what fits, runs nsteps batched steps, retires finished requests */
+/* admits what fits, runs up to nsteps batched steps (fewer when a running
+ * request has fewer left before its max_steps, so that none runs past it),
+ * retires finished requests */
 int lns_server3d_tick(lns_server3d* server, int32_t nsteps, int32_t* running, int32_t* queued);
 /* state LNS_REQ_*, the step that met tol (or steps run), the last residual,
  * and the seconds from submission to completion (-1 while unfinished) */
 int lns_server3d_poll(lns_server3d* server, int64_t id, int32_t* state, int32_t* steps, double* res,
                       double* latency_s);
-/* the finished request's state v(5,nx,ny) complex; forgets the request */
+/* the finished request's state v(5,nx,ny) complex; forgets the request.  A
+ * failed request returns LNS_ERR_ARG and is forgotten too. */
 int lns_server3d_fetch(lns_server3d* server, int64_t id, double* v);
 size_t lns_server3d_bytes_in_use(const lns_server3d* server);
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "lns_upload_mean3d": [P, DP, DP],
     "lns_step3d": [P, DP, I32, I32, DP],
     "lns_step3d_dev": [P, DP, I32, I32, DP, P],
+    "lns_itrbc3d_dev": [P, DP, P],
     "lns_rhs3d_dev": [P, DP, DP, DP, DP, P],
     "lns_lhs3d_dev": [P, I32, DP, P],
     "lns_get_field3d": [P, I32, DP],
@@ -109,10 +110,10 @@ class Params2D(ctypes.Structure):
     """lns_params2d of include/lns3d_gb300.h."""
     _fields_ = [("nx", I32), ("ny", I32), ("dxi", ctypes.c_double), ("deta", ctypes.c_double),
                 ("Ma", ctypes.c_double), ("Re", ctypes.c_double), ("Pr", ctypes.c_double),
-                ("gamma", ctypes.c_double), ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double),
-                ("dtmax", ctypes.c_double), ("theta", ctypes.c_double), ("loctime", I32), ("xper", I32),
+                ("gamma", ctypes.c_double), ("gamma1", ctypes.c_double), ("alfa", ctypes.c_double),
+                ("cflmax", ctypes.c_double), ("dtmax", ctypes.c_double), ("theta", ctypes.c_double), ("loctime", I32), ("xper", I32),
                 ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32), ("top", I32), ("optx", I32),
-                ("opty", I32), ("res_compat", I32), ("lhs_order", I32), ("impl", I32), ("ispg", I32),
+                ("opty", I32), ("lhs_order", I32), ("impl", I32), ("ispg", I32),
                 ("eps_e", ctypes.c_double)]
 
 
@@ -120,10 +121,11 @@ class Params3D(ctypes.Structure):
     """lns_params3d of include/lns3d_gb300.h."""
     _fields_ = [("nx", I32), ("ny", I32), ("dxi", ctypes.c_double), ("deta", ctypes.c_double),
                 ("Ma", ctypes.c_double), ("Re", ctypes.c_double), ("Pr", ctypes.c_double),
-                ("gamma", ctypes.c_double), ("omega", ctypes.c_double), ("beta", ctypes.c_double),
+                ("gamma", ctypes.c_double), ("gamma1", ctypes.c_double), ("omega", ctypes.c_double),
+                ("beta", ctypes.c_double),
                 ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double), ("dtmax", ctypes.c_double),
                 ("loctime", I32), ("xper", I32), ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32),
-                ("top", I32), ("optx", I32), ("opty", I32), ("precision", I32), ("res_compat", I32),
+                ("top", I32), ("optx", I32), ("opty", I32), ("precision", I32),
                 ("impl", I32), ("ispg", I32), ("eps_e", ctypes.c_double)]
 
 
@@ -138,8 +140,6 @@ def lib():
         L = ctypes.CDLL(path)
         L.lns_last_error.restype = ctypes.c_char_p
         L.lns_version.restype = ctypes.c_char_p
-        L.lns_probe_fp64_tflops.restype = ctypes.c_double
-        L.lns_probe_fp64_tflops.argtypes = []
         L.lns_mixed_workspace_bytes.restype = ctypes.c_size_t
         L.lns_mixed_workspace_bytes.argtypes = [I32, I32, I32, I32]
         L.lns_tri_workspace_bytes.restype = ctypes.c_size_t

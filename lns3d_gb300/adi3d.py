@@ -43,9 +43,7 @@ class ImpDrv3D:
     MIXED (FP32 scaled LHS factors and sweeps, FP64 RHS, residual and
     update).  impl: time scheme, 1 backward Euler, 2 two-step backward
     (backward Euler for the context's first step), 3 midpoint
-    (src/impdrv3d.f90:130-199).  res_compat: report the reference's running residual
-    (src/resstat3d.f90:18 keeps totres between calls) instead of each
-    corrector's own.  ispg, spg, spg2: the sponge (0 none, 1 spg, > 4
+    (src/impdrv3d.f90:130-199).  ispg, spg, spg2: the sponge (0 none, 1 spg, > 4
     spg + spg2; src/lrhs3d.f90:220-240), spg and spg2 (nx, ny) arrays.
     eps_e, buff: explicit smoother and implicit damping (src/smoother3d.f90),
     buff (nx, ny) or None for the reference's default of ones.  ispg 2, 3
@@ -54,18 +52,17 @@ class ImpDrv3D:
     wall = 3 (the bump) takes u1w, u2w, u3w, tw, twp as bump, complex (5, nx).
     """
 
-    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False,
+    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64,
                  impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None, x=None, x0=0.0, wamp=None,
                  cvic=None, bump=None):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
         prm = Params3D(nx=self.nx, ny=self.ny, dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
-                       gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax,
-                       dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
-                       wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
-                       precision=precision, res_compat=1 if res_compat else 0, impl=impl, ispg=ispg,
-                       eps_e=eps_e)
+                       gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), omega=p["omega"], beta=p["kz"],
+                       alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"],
+                       navier=p["navier"], wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"],
+                       opty=p["opty"], precision=precision, impl=impl, ispg=ispg, eps_e=eps_e)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")
@@ -122,6 +119,20 @@ class ImpDrv3D:
         if not v.flags.f_contiguous:
             raise ValueError("%s must be Fortran-ordered (5, nx, ny)" % name)
         return ctypes.c_void_p(v.ctypes.data), False
+
+    def itrbc(self, v):
+        """itrBC3D on v in place: the reference applies it once before the
+        step loop (src/impdrv3d.f90:125-126).  A host v is staged through
+        the device."""
+        pv, dev = self._check_v(v)
+        if dev:
+            check(lib().lns_itrbc3d_dev(self._ctx, pv, _stream()), "lns_itrbc3d_dev")
+            return
+        import torch
+
+        t = torch.from_numpy(v.ravel(order="F")).cuda()
+        check(lib().lns_itrbc3d_dev(self._ctx, ctypes.c_void_p(t.data_ptr()), _stream()), "lns_itrbc3d_dev")
+        v[...] = t.cpu().numpy().reshape(v.shape, order="F")
 
     def step(self, v, nsteps=1, niter=1, totres=None):
         """Advance v in place by nsteps implicit steps of niter correctors.
@@ -199,17 +210,17 @@ class Batch3D:
     problem's result equals its own ImpDrv3D run.
     """
 
-    def __init__(self, problems, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64, res_compat=False):
+    def __init__(self, problems, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64):
         self.P = len(problems)
         self.shapes = []
         arr = (Params3D * self.P)()
         for k, pr in enumerate(problems):
             p = pr["params"]
             arr[k] = Params3D(nx=p["nx"], ny=p["ny"], dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"],
-                              Pr=p["Pr"], gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"],
-                              cflmax=cflmax, dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"],
-                              navier=p["navier"], wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"],
-                              opty=p["opty"], precision=precision, res_compat=1 if res_compat else 0)
+                              Pr=p["Pr"], gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), omega=p["omega"],
+                              beta=p["kz"], alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax, loctime=loctime,
+                              xper=p["xper"], yper=p["yper"], navier=p["navier"], wall=p["wall"], wallt=p["wallt"],
+                              top=p["top"], optx=p["optx"], opty=p["opty"], precision=precision)
             self.shapes.append((5, int(p["nx"]), int(p["ny"])))
         self._b = ctypes.c_void_p()
         check(lib().lns_batch3d_create(self.P, arr, ctypes.byref(self._b)), "lns_batch3d_create")
@@ -278,13 +289,13 @@ class Server3D:
                                         ctypes.byref(self._s)), "lns_server3d_create")
         self._shape = {}
 
-    def submit(self, problem, tol=1e-10, max_steps=2000, cflmax=1.0, dtmax=1e30, loctime=1, res_compat=False):
+    def submit(self, problem, tol=1e-10, max_steps=2000, cflmax=1.0, dtmax=1e30, loctime=1):
         p = problem["params"]
         prm = Params3D(nx=p["nx"], ny=p["ny"], dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
-                       gamma=p["gamma"], omega=p["omega"], beta=p["kz"], alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax,
-                       loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"], wall=p["wall"],
-                       wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"], precision=self.precision,
-                       res_compat=1 if res_compat else 0)
+                       gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), omega=p["omega"], beta=p["kz"],
+                       alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"],
+                       navier=p["navier"], wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"],
+                       opty=p["opty"], precision=self.precision)
         nx, ny = int(p["nx"]), int(p["ny"])
         m = np.empty((nx, ny, 10), order="F")
         for i, name in enumerate(METRICS):

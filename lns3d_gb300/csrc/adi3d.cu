@@ -693,7 +693,6 @@ struct StepArgs {
   cf* r32;
   double* part;  // RHS block partials
   int nbx, nrhs;  // RHS blocks along x, partial count
-  double* acc;   // running residual of the reference mode, or null
   double tol;    // the problem stops (active = 0) at the first residual <= tol; 0: never
 };
 
@@ -747,10 +746,8 @@ __global__ void resid_batch_kernel(const StepArgs* __restrict__ list, int* activ
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double tot = a.acc ? *a.acc + red[0] : red[0];
-    const double r = sqrt(tot / (double)a.o.np);
+    const double r = sqrt(red[0] / (double)a.o.np);
     hist[(long long)(*step) * P + p] = r;
-    if (a.acc) *a.acc = r;
     if (a.tol > 0.0 && r <= a.tol) active[p] = 0;
   }
 }
@@ -924,7 +921,7 @@ int res_reserve(lns_ctx3d* c, int n) {
 // The operator acts on the field v; vs is the state (rbe3D / rtb3D and the
 // boundary rows); v2old selects rtb3D.
 int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vs, const cd* vold, const cd* v2old, cd* r64, cf* r32,
-               double* res, double* acc, cudaStream_t st) {
+               double* res, cudaStream_t st) {
   const Grid& g = c->g;
   lns::a3::grad1_kernel<<<pt_grid(g), 128, 0, st>>>(g, v, c->c1v);
   if (lns::a3::narrow_stencils(g))
@@ -933,7 +930,7 @@ int launch_rhs(lns_ctx3d* c, const cd* v, const cd* vs, const cd* vold, const cd
     lns::a3::rhs_kernel<false><<<pt_grid(g), 128, 0, st>>>(g, c->ops, v, vs, vold, v2old, c->c1v, r64, r32,
                                                            c->part);
   const int nrhs = (int)(pt_grid(g).x * pt_grid(g).y);  // rhs_kernel block partials
-  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res, acc);
+  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "rhs kernels launch");
 }
@@ -1060,7 +1057,6 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
   const int impl = c->prm.impl == 0 ? 1 : c->prm.impl;
   int rc;
   const size_t vbytes = sizeof(cd) * 5 * (size_t)c->np;
-  double* acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
   for (int s = 0; s < nsteps; ++s) {
     const bool rtb = impl == 2 && c->lstep > 0;
     const double alfa = impl == 3 ? 0.5 : rtb ? 6.6666666666666666666e-1 : (impl == 2 ? 1.0 : c->prm.alfa);
@@ -1087,7 +1083,7 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
       }
       const cd* v2 = rtb ? c->v2old : nullptr;
       if (mixed) {
-        if (!rc) rc = launch_rhs(c, field, v, c->vold, v2, nullptr, c->r32, res, acc, st);
+        if (!rc) rc = launch_rhs(c, field, v, c->vold, v2, nullptr, c->r32, res, st);
         if (!rc) rc = mark(c, st);
         if (!rc) rc = sweep_x<cf>(c, c->r32, st);
         if (!rc) rc = mark(c, st);
@@ -1095,7 +1091,7 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
         if (!rc) rc = mark(c, st);
         if (!rc) rc = launch_update<cf>(c, v, c->r32, 1, st);
       } else {
-        if (!rc) rc = launch_rhs(c, field, v, c->vold, v2, c->r64, nullptr, res, acc, st);
+        if (!rc) rc = launch_rhs(c, field, v, c->vold, v2, c->r64, nullptr, res, st);
         if (!rc) rc = mark(c, st);
         if (!rc) rc = sweep_x<cd>(c, c->r64, st);
         if (!rc) rc = mark(c, st);
@@ -1128,7 +1124,6 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (p->wallt != 0 && p->wallt != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: wallt must be 0 or 1");
   if (p->top != 0 && p->top != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0 or 1");
   if (p->loctime != 0 && p->loctime != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: loctime must be 0 or 1");
-  if (p->res_compat != 0 && p->res_compat != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: res_compat must be 0 or 1");
   if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
     return fail3(LNS_ERR_ARG, "ctx3d_create: precision must be LNS_FP64 or LNS_MIXED");
   if (p->impl < 0 || p->impl > 3) return fail3(LNS_ERR_ARG, "ctx3d_create: impl must be 1, 2 or 3 (0 means 1)");
@@ -1144,7 +1139,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   }
   Grid& g = c->g;
   g.nx = p->nx; g.ny = p->ny; g.dxi = p->dxi; g.deta = p->deta;
-  g.Ma = p->Ma; g.Re = p->Re; g.Pr = p->Pr; g.gamma = p->gamma; g.gamma1 = p->gamma - 1.0;
+  g.Ma = p->Ma; g.Re = p->Re; g.Pr = p->Pr; g.gamma = p->gamma;
+  g.gamma1 = p->gamma1 != 0.0 ? p->gamma1 : p->gamma - 1.0;
   g.omega = p->omega; g.kz = p->beta; g.alfa = p->alfa;
   g.xper = p->xper; g.yper = p->yper; g.navier = p->navier; g.wall = p->wall; g.wallt = p->wallt; g.top = p->top;
   g.dxinv = 1.0 / p->dxi; g.dyinv = 1.0 / p->deta;
@@ -1404,6 +1400,14 @@ int lns_upload_mean3d(lns_ctx3d* c, const double* vm, double* cfl) {
   return make_inflow_target(c);
 }
 
+int lns_itrbc3d_dev(lns_ctx3d* c, double* v, void* stream) {
+  if (!c || !v) return fail3(LNS_ERR_ARG, "itrbc3d: null argument");
+  if (int rn = need_data(c, "itrbc3d")) return rn;
+  int rc = check_device(c);
+  if (rc) return rc;
+  return launch_update<cd>(c, (cd*)v, nullptr, 0, (cudaStream_t)stream);
+}
+
 int lns_step3d_dev(lns_ctx3d* c, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream) {
   if (!c || !v) return fail3(LNS_ERR_ARG, "step3d: null argument");
   if (nsteps < 0 || niter < 1) return fail3(LNS_ERR_ARG, "step3d: need nsteps >= 0 and niter >= 1");
@@ -1440,8 +1444,7 @@ int lns_rhs3d_dev(lns_ctx3d* c, const double* v, const double* vold, double* r, 
   int rc = check_device(c);
   if (rc) return rc;
   return launch_rhs(c, (const cd*)v, (const cd*)v, (const cd*)vold, nullptr, (cd*)r, nullptr,
-                    totres_dev ? totres_dev : c->dscal + 1,
-                    nullptr, (cudaStream_t)stream);
+                    totres_dev ? totres_dev : c->dscal + 1, (cudaStream_t)stream);
 }
 
 int lns_lhs3d_dev(lns_ctx3d* c, int32_t dir, double* mat, void* stream) {
@@ -1690,7 +1693,6 @@ int prepare(lns_batch3d* b, double tol) {
     a.part = c->part;
     a.nbx = (c->g.nx + 127) / 128;
     a.nrhs = a.nbx * c->g.ny;
-    a.acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
     a.tol = tol;
     void* r = b->mixed ? (void*)c->r32 : (void*)c->r64;
     ax[p] = xargs(c, r);
@@ -2081,7 +2083,9 @@ int admit(lns_server3d* s) {
 }
 
 void retire(lns_server3d* s, SrvReq* r, int state) {
-  cudaMemcpy(r->v.data(), r->ctx->v, sizeof(cd) * 5 * r->ctx->np, cudaMemcpyDeviceToHost);
+  // a result that cannot be read back is a failed request, not the input state
+  if (cudaMemcpy(r->v.data(), r->ctx->v, sizeof(cd) * 5 * r->ctx->np, cudaMemcpyDeviceToHost) != cudaSuccess)
+    state = LNS_REQ_FAILED;
   s->used -= lns_ctx3d_bytes(r->ctx);
   lns_ctx3d_destroy(r->ctx);
   r->ctx = nullptr;
@@ -2173,6 +2177,9 @@ int lns_server3d_tick(lns_server3d* s, int32_t nsteps, int32_t* running, int32_t
   if (rc) return rc;
   lns_batch3d* b = s->b;
   if (b->P) {
+    // no request runs past its step limit: the tick is cut to the fewest
+    // steps any running request has left
+    for (const SrvReq* r : s->running) nsteps = std::min(nsteps, r->max_steps - r->steps);
     rc = reserve_hist(b, nsteps);
     if (!rc) rc = capture(b, s->niter);
     if (rc) return rc;
@@ -2207,8 +2214,6 @@ int lns_server3d_tick(lns_server3d* s, int32_t nsteps, int32_t* running, int32_t
       if (st) retire(s, r, st);
       else keep.push_back(r);
     }
-    // a request that reached max_steps mid-tick ran past it; the ones kept
-    // continue in the next batch
     s->running.swap(keep);
   }
   if (running) *running = (int32_t)s->running.size();
@@ -2233,6 +2238,11 @@ int lns_server3d_fetch(lns_server3d* s, int64_t id, double* v) {
   auto it = s->all.find(id);
   if (it == s->all.end()) return fail3(LNS_ERR_ARG, "server3d_fetch: unknown request");
   SrvReq* r = it->second;
+  if (r->state == LNS_REQ_FAILED) {  // nothing to return; forget it and its host copies
+    s->all.erase(it);
+    delete r;
+    return fail3(LNS_ERR_ARG, "server3d_fetch: the request failed");
+  }
   if (r->state != LNS_REQ_DONE && r->state != LNS_REQ_STOPPED)
     return fail3(LNS_ERR_ARG, "server3d_fetch: request not finished");
   std::copy(r->v.begin(), r->v.end(), v);

@@ -205,10 +205,8 @@ static __global__ void dtl_kernel(long long np, int nparts, const double* part, 
   if (blockIdx.x == 0 && threadIdx.x == 0) *cfl_out = cfl * delt;
 }
 
-// totres = sqrt(sum / (nx ny)) in a fixed summation order; with acc the sum
-// starts from *acc and the result is stored back into it (the reference's
-// saved totres, src/resstat3d.f90:18)
-static __global__ void resid_kernel(int nparts, const double* part, long long npts, double* out, double* acc) {
+// totres = sqrt(sum / (nx ny)) in a fixed summation order (src/resstat3d.f90:37-60)
+static __global__ void resid_kernel(int nparts, const double* part, long long npts, double* out) {
   __shared__ double red[256];
   double s = 0.0;
   for (int k = threadIdx.x; k < nparts; k += blockDim.x) s += part[k];
@@ -219,10 +217,7 @@ static __global__ void resid_kernel(int nparts, const double* part, long long np
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double tot = acc ? *acc + red[0] : red[0];
-    const double r = sqrt(tot / (double)npts);
-    *out = r;
-    if (acc) *acc = r;
+    *out = sqrt(red[0] / (double)npts);
   }
 }
 

@@ -1,9 +1,9 @@
-// Peak-rate probe used by the benchmark's FP64 roofline: a dependent-free
-// DFMA stream (eight independent chains per thread, every lane active, 32
-// warps per SM) timed with CUDA events.  Not part of the solver path.
+// Peak-rate probe of the benchmark's FP64 roofline (measurement tooling,
+// built into its own library, lib/liblns3d_probe.so, that only bench.py
+// loads): a dependent-free DFMA stream (eight independent chains per thread,
+// every lane active, 32 warps per SM) timed with CUDA events.  Returns the
+// rate in TFLOP/s, or a negative value on failure.
 #include <cuda_runtime.h>
-
-#include "../../include/lns3d_gb300.h"
 
 namespace {
 __global__ void dfma_stream(double* out, int iters, double a, double b) {

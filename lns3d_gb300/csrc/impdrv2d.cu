@@ -750,11 +750,11 @@ int time_step(lns_ctx2d* c, const double* v, cudaStream_t st) {
 }
 
 int rhs2(lns_ctx2d* c, const double* vs, const double* v, const double* vold, const double* v2old, double* r,
-         double* res, double* acc, cudaStream_t st) {
+         double* res, cudaStream_t st) {
   const Grid& g = c->g;
   lns::a2::rhs2d_kernel<<<pgrid(g), 128, 0, st>>>(g, c->ops, metrics2(c), top2(c), vs, v, vold, v2old, r, c->part);
   const int nrhs = (int)(pgrid(g).x * pgrid(g).y);
-  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res, acc);
+  lns::a3::resid_kernel<<<1, 256, 0, st>>>(nrhs, c->part, c->np, res);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda2(e, "rhs kernels launch");
 }
@@ -787,7 +787,6 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
   const size_t vbytes = sizeof(double) * 5 * (size_t)c->np;
   const long long n5 = 5 * c->np;
   const int impl = c->prm.impl == 0 ? 1 : c->prm.impl;
-  double* acc = c->prm.res_compat ? c->dscal + 2 : nullptr;
   cudaError_t e = cudaMemsetAsync(c->status, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda2(e, "cudaMemsetAsync");
   int rc = LNS_OK;
@@ -813,7 +812,7 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
         if (e != cudaSuccess) rc = cuda2(e, "avg2d_kernel launch");
         vs = c->wavg;
       }
-      if (!rc) rc = rhs2(c, vs, v, c->vold, rtb ? c->v2old : nullptr, c->r, res, acc, st);
+      if (!rc) rc = rhs2(c, vs, v, c->vold, rtb ? c->v2old : nullptr, c->r, res, st);
       if (!rc) rc = lhs2(c, v, 1, c->mat, alfa, st);
       // the fourth-order path solves with penta2p (its periodic fill-slot
       // quirk kept unless the exact mode is on), the second-order path with
@@ -865,7 +864,6 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
     return fail2(LNS_ERR_ARG, "ctx2d_create: the held top (top 3) is supported with the fourth-order LHS");
   if (!(p->Ma > 0.0) || p->Ma == 1.0) return fail2(LNS_ERR_ARG, "ctx2d_create: need Ma > 0 and Ma != 1");
   if (p->loctime != 0 && p->loctime != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: loctime must be 0 or 1");
-  if (p->res_compat != 0 && p->res_compat != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: res_compat must be 0 or 1");
   if (p->lhs_order != 0 && p->lhs_order != 2 && p->lhs_order != 4)
     return fail2(LNS_ERR_ARG, "ctx2d_create: lhs_order must be 0 (fourth order), 2 or 4");
   if (p->lhs_order == 2 && p->ny < 8) return fail2(LNS_ERR_ARG, "ctx2d_create: the second-order LHS needs ny >= 8");
@@ -883,7 +881,8 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   }
   Grid& g = c->g;
   g.nx = p->nx; g.ny = p->ny; g.dxi = p->dxi; g.deta = p->deta;
-  g.Ma = p->Ma; g.Re = p->Re; g.Pr = p->Pr; g.gamma = p->gamma; g.gamma1 = p->gamma - 1.0;
+  g.Ma = p->Ma; g.Re = p->Re; g.Pr = p->Pr; g.gamma = p->gamma;
+  g.gamma1 = p->gamma1 != 0.0 ? p->gamma1 : p->gamma - 1.0;
   g.omega = 0.0; g.kz = 0.0; g.alfa = p->alfa;
   g.xper = p->xper; g.yper = p->yper; g.navier = p->navier; g.wall = p->wall; g.wallt = p->wallt; g.top = p->top;
   g.dxinv = 1.0 / p->dxi; g.dyinv = 1.0 / p->deta;
@@ -1063,7 +1062,7 @@ int lns_rhs2d_dev(lns_ctx2d* c, const double* v, const double* vold, double* r, 
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   rc = time_step(c, v, st);
-  if (!rc) rc = rhs2(c, v, v, vold, nullptr, r, totres_dev ? totres_dev : c->dscal + 1, nullptr, st);
+  if (!rc) rc = rhs2(c, v, v, vold, nullptr, r, totres_dev ? totres_dev : c->dscal + 1, st);
   return rc;
 }
 

@@ -36,7 +36,7 @@ class ImpDrv2D:
     bnt: (nx, 2) unit normal of the top boundary; pot: (5, nx) top.pot rows.
     """
 
-    def __init__(self, params, metrics, bnt, pot, cflmax=1.0, dtmax=1e30, loctime=0, theta=0.0, res_compat=False,
+    def __init__(self, params, metrics, bnt, pot, cflmax=1.0, dtmax=1e30, loctime=0, theta=0.0,
                  ilhs=1, impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None):
         """ilhs: the reference's iLHS switch, 1 = fourth-order LHS with
         pentadiagonal solves, 0 = second-order LHS with block-tridiagonal
@@ -52,9 +52,9 @@ class ImpDrv2D:
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         prm = Params2D(nx=self.nx, ny=self.ny, dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
-                       gamma=p["gamma"], alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax, theta=theta, loctime=loctime,
-                       xper=p["xper"], yper=p["yper"], navier=p["navier"], wall=p["wall"], wallt=p["wallt"],
-                       top=p["top"], optx=p["optx"], opty=p["opty"], res_compat=1 if res_compat else 0,
+                       gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax,
+                       theta=theta, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
+                       wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
                        lhs_order=2 if ilhs == 0 else 4, impl=impl, ispg=ispg, eps_e=eps_e)
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx2d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx2d_create")
@@ -89,8 +89,17 @@ class ImpDrv2D:
         return ctypes.c_void_p(a.data_ptr())
 
     def itrbc(self, v):
-        """itrBC on a device state (src/itrbc.f90)."""
-        check(lib().lns_itrbc2d_dev(self._ctx, self._dev(v, "v"), _stream()), "lns_itrbc2d_dev")
+        """itrBC on v in place (src/itrbc.f90): the reference applies it once
+        before the step loop (src/impdrv.f90:160).  A host v is staged
+        through the device."""
+        if _is_torch(v):
+            check(lib().lns_itrbc2d_dev(self._ctx, self._dev(v, "v"), _stream()), "lns_itrbc2d_dev")
+            return
+        import torch
+
+        t = torch.from_numpy(np.asarray(v).ravel(order="F")).cuda()
+        check(lib().lns_itrbc2d_dev(self._ctx, self._dev(t, "v"), _stream()), "lns_itrbc2d_dev")
+        v[...] = t.cpu().numpy().reshape(v.shape, order="F")
 
     def step(self, v, nsteps=1, niter=1, totres=None):
         """Advance v in place by nsteps implicit steps of niter correctors;

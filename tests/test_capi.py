@@ -43,7 +43,7 @@ def test_python_signatures_cover_header():
     from lns3d_gb300._lib import SIGNATURES
 
     solver_syms = [n for n in declared_symbols()
-                   if n not in ("lns_last_error", "lns_version", "lns_probe_fp64_tflops",
+                   if n not in ("lns_last_error", "lns_version",
                                 "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes", "lns_batch3d_bytes",
                                 "lns_server3d_bytes_in_use", "lns_tri_workspace_bytes")]
     assert sorted(SIGNATURES) == solver_syms
@@ -153,15 +153,14 @@ def _params2d(**kw):
     from lns3d_gb300._lib import Params2D
 
     base = dict(nx=32, ny=24, dxi=1 / 31, deta=1 / 23, Ma=0.5, Re=1000.0, Pr=0.72, gamma=1.4, alfa=1.0, cflmax=1.0,
-                dtmax=1e30, theta=0.0, loctime=0, xper=1, yper=0, navier=1, wall=0, wallt=1, top=0, optx=-1, opty=-1,
-                res_compat=0)
+                dtmax=1e30, theta=0.0, loctime=0, xper=1, yper=0, navier=1, wall=0, wallt=1, top=0, optx=-1, opty=-1)
     base.update(kw)
     return Params2D(**base)
 
 
 @pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=2), dict(wallt=2),
                                  dict(top=1), dict(nx=7), dict(ny=6), dict(Ma=1.0), dict(deta=0.0),
-                                 dict(res_compat=3), dict(lhs_order=3), dict(lhs_order=2, ny=7), dict(impl=4),
+                                 dict(lhs_order=3), dict(lhs_order=2, ny=7), dict(impl=4),
                                  dict(impl=-1), dict(ispg=1), dict(eps_e=-0.5),
                                  dict(top=3, lhs_order=2)])
 def test_ctx2d_rejects_unsupported_options(lib, bad):

@@ -239,27 +239,6 @@ def test_full_size_step_is_linear(cuda, precision):
     assert err < (1e-12 if precision == 0 else 1e-4), err
 
 
-def test_reference_residual_history_mode(cuda):
-    # res_compat reproduces the reference's reported residual, whose sum keeps
-    # the previous result (src/resstat3d.f90:18); the states are unaffected
-    from lns3d_gb300.cases import shear_layer
-
-    case = shear_layer(nx=40, ny=33, seed=6)
-    orc = Oracle3D(case, cflmax=20.0, loctime=1, res_compat=True)
-    drv = make_drv(case)
-    from lns3d_gb300 import ImpDrv3D
-
-    drv_c = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1, res_compat=True)
-    v_ref, v_a, v_b = (case["v"].copy(order="F") for _ in range(3))
-    res_ref = np.array([orc.step(v_ref, niter=2) for _ in range(30)])
-    res_c = drv_c.step(v_a, nsteps=30, niter=2)
-    drv.step(v_b, nsteps=30, niter=2)
-    assert np.abs(res_c - res_ref).max() <= 1e-10 * res_ref.max()
-    assert np.array_equal(v_a, v_b)
-    # the reported value levels off near 1 / (nx ny)
-    assert abs(res_ref[-1] - 1.0 / (40 * 33)) < 0.05 / (40 * 33)
-
-
 @pytest.mark.parametrize("impl,niter", [(2, 1), (3, 1), (2, 2)])
 def test_time_schemes_match_oracle(cuda, impl, niter):
     """impl 2 (two-step backward: backward Euler, then rtb3D with the LHS

@@ -75,3 +75,25 @@ def test_admission_waits_for_memory(cuda):
     assert srv.bytes_in_use <= 2.5 * one
     drain(srv, ids, nsteps=10)
     assert all(srv.poll(i)["state"] == "stopped" for i in ids)
+
+
+def test_request_stops_exactly_at_max_steps(cuda):
+    """A step limit that is not a multiple of the tick length: the tick is cut
+    so that the request runs exactly max_steps steps, and the fetched state
+    is that of a lone run of max_steps steps."""
+    from lns3d_gb300 import ImpDrv3D, Server3D
+
+    x = case(40, 33, 0.3, 0.04, 11)
+    other = case(48, 24, 0.1, 0.02, 1)
+    srv = Server3D(1 << 33, max_slots=4)
+    i = srv.submit(x, tol=1e-30, max_steps=17, cflmax=20.0)
+    j = srv.submit(other, tol=1e-30, max_steps=40, cflmax=20.0)
+    drain(srv, [i, j], nsteps=10)
+    p = srv.poll(i)
+    assert p["state"] == "stopped" and p["steps"] == 17
+    drv = ImpDrv3D(x["params"], x["metrics"], x["vm"], cflmax=20.0, loctime=1, precision=1)
+    v = x["v"].copy(order="F")
+    hist = drv.step(v, nsteps=17)
+    assert np.array_equal(srv.fetch(i), v)
+    assert p["res"] == hist[-1]
+    assert srv.poll(j)["steps"] == 40
