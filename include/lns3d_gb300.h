@@ -431,6 +431,32 @@ int lns_ctx3d_profile_read(lns_ctx3d* ctx, double* ms, int32_t* ncorr);
 int lns_get_field3d(lns_ctx3d* ctx, int32_t which, double* out);
 
 /* ---------------------------------------------------------------------------
+ * The linearised two-dimensional implicit step (src/impdrv.f90:171-400 with
+ * linear = 1: src/lrhs.f90 about the frozen operators of genmtrx(vm, 0, vm),
+ * src/lns3d.f90:149; rbe/rtb, rhsBC, resstat, lhs1f/lhs2f with their
+ * boundary rows, penta2p or penta2bc, penta1p or penta1bc, v += r, itrBC).
+ * With the spanwise wavenumber and the frequency zero these are the
+ * single-mode step's routines on real fields, so the context runs a
+ * single-mode context at beta = omega = 0 (the options it supports, FP64)
+ * and converts the state: v(5,nx,ny) is real here.  Sequence:
+ *   lns_lin2d_create(params with beta = omega = 0)   deck values
+ *   lns_upload_metrics_lin2d, lns_upload_mean_lin2d  metric.dat, mean.dat
+ *   lns_itrbc_lin2d_dev                              the itrBC before the loop (src/impdrv.f90:160)
+ *   lns_step_lin2d / _dev                            nsteps steps of niter correctors
+ */
+typedef struct lns_lin2d lns_lin2d;
+int lns_lin2d_create(const lns_params3d* params, lns_lin2d** ctx);
+int lns_lin2d_destroy(lns_lin2d* ctx);
+size_t lns_lin2d_bytes(const lns_lin2d* ctx);
+int lns_upload_metrics_lin2d(lns_lin2d* ctx, const double* metrics);
+int lns_upload_mean_lin2d(lns_lin2d* ctx, const double* vm, double* cfl);
+int lns_itrbc_lin2d_dev(lns_lin2d* ctx, double* v, void* stream);
+/* v(5,nx,ny) real on the host, in place; totres[nsteps] (may be NULL) gets
+ * resstat's value of the last corrector of each step */
+int lns_step_lin2d(lns_lin2d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres);
+int lns_step_lin2d_dev(lns_lin2d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres_dev, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Batches of linearised problems (no reference counterpart: the reference
  * runs one problem per process).  A batch holds nprob independent problems
  * -- each with its own deck (grid size, beta, omega, ...), metrics, mean

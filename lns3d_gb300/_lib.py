@@ -79,6 +79,13 @@ SIGNATURES = {
     "lns_rhs3d_dev": [P, DP, DP, DP, DP, P],
     "lns_lhs3d_dev": [P, I32, DP, P],
     "lns_get_field3d": [P, I32, DP],
+    "lns_lin2d_create": [P, P],
+    "lns_lin2d_destroy": [P],
+    "lns_upload_metrics_lin2d": [P, DP],
+    "lns_upload_mean_lin2d": [P, DP, DP],
+    "lns_itrbc_lin2d_dev": [P, DP, P],
+    "lns_step_lin2d": [P, DP, I32, I32, DP],
+    "lns_step_lin2d_dev": [P, DP, I32, I32, DP, P],
     "lns_ctx3d_profile": [P, I32],
     "lns_ctx3d_profile_read": [P, DP, P],
     "lns_batch3d_create": [I32, P, P],
@@ -146,6 +153,8 @@ def lib():
         L.lns_tri_workspace_bytes.argtypes = [I32, I32, I32]
         L.lns_ctx3d_bytes.restype = ctypes.c_size_t
         L.lns_ctx3d_bytes.argtypes = [P]
+        L.lns_lin2d_bytes.restype = ctypes.c_size_t
+        L.lns_lin2d_bytes.argtypes = [P]
         L.lns_server3d_bytes_in_use.restype = ctypes.c_size_t
         L.lns_server3d_bytes_in_use.argtypes = [P]
         L.lns_batch3d_bytes.restype = ctypes.c_size_t

@@ -340,3 +340,61 @@ class Server3D:
             self.close()
         except Exception:
             pass
+
+
+class ImpDrvLin2D:
+    """The linearised 2D implicit step (src/impdrv.f90 with linear = 1,
+    src/lrhs.f90) on the current GPU: real fields v (5, nx, ny).
+
+    params: as ImpDrv3D's, with kz = 0 and omega = 0 (a deck with Lz = 0);
+    metrics: the ten (nx, ny) arrays; vm: (5, nx, ny) mean flow.  The
+    context runs the single-mode machinery at kz = omega = 0."""
+
+    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, impl=1, ispg=0, eps_e=0.0):
+        p = params
+        if p.get("kz", 0.0) != 0.0 or p.get("omega", 0.0) != 0.0:
+            raise ValueError("a 2D linear run has kz = 0 and omega = 0")
+        self.nx, self.ny = int(p["nx"]), int(p["ny"])
+        prm = Params3D(nx=self.nx, ny=self.ny, dxi=p["dxi"], deta=p["deta"], Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"],
+                       gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), omega=0.0, beta=0.0, alfa=p["alfa"],
+                       cflmax=cflmax, dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"],
+                       navier=p["navier"], wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"],
+                       opty=p["opty"], precision=FP64, impl=impl, ispg=ispg, eps_e=eps_e)
+        self._ctx = ctypes.c_void_p()
+        check(lib().lns_lin2d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_lin2d_create")
+        m = np.empty((self.nx, self.ny, 10), order="F")
+        for k, name in enumerate(METRICS):
+            m[:, :, k] = metrics[name]
+        check(lib().lns_upload_metrics_lin2d(self._ctx, ctypes.c_void_p(m.ctypes.data)), "lns_upload_metrics_lin2d")
+        vm = np.asfortranarray(vm, dtype=np.float64)
+        cfl = ctypes.c_double()
+        check(lib().lns_upload_mean_lin2d(self._ctx, ctypes.c_void_p(vm.ctypes.data), ctypes.byref(cfl)),
+              "lns_upload_mean_lin2d")
+        self.cfl = cfl.value
+
+    def _check(self, v):
+        if not isinstance(v, np.ndarray) or v.dtype != np.float64 or v.shape != (5, self.nx, self.ny) \
+                or not v.flags.f_contiguous:
+            raise ValueError("v must be a Fortran-ordered float64 array of shape (5, nx, ny)")
+
+    def itrbc(self, v):
+        """itrBC on v in place (the call before the step loop, src/impdrv.f90:160)."""
+        import torch
+
+        self._check(v)
+        t = torch.from_numpy(v.ravel(order="F")).cuda()
+        check(lib().lns_itrbc_lin2d_dev(self._ctx, ctypes.c_void_p(t.data_ptr()), _stream()), "lns_itrbc_lin2d_dev")
+        v[...] = t.cpu().numpy().reshape(v.shape, order="F")
+
+    def step(self, v, nsteps=1, niter=1):
+        """nsteps steps of niter correctors on host v in place; the per-step residuals."""
+        self._check(v)
+        res = np.zeros(max(nsteps, 1))
+        check(lib().lns_step_lin2d(self._ctx, ctypes.c_void_p(v.ctypes.data), nsteps, niter,
+                                   ctypes.c_void_p(res.ctypes.data)), "lns_step_lin2d")
+        return res[:nsteps]
+
+    def __del__(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            lib().lns_lin2d_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()

@@ -167,3 +167,44 @@ def vortex2d(nx=128, ny=128, L=10.0, stretch=2.0, Ma=0.5, Re=1000.0, Pr=0.72, ci
     bnt = np.zeros((nx, 2), order="F")
     bnt[:, 1] = 1.0        # (n1, n2) / |n| at j = ny (src/gengrid.f90:141-142)
     return dict(params=params, x=x, y=y, metrics=metrics, v=np.asfortranarray(v), pot=pot, bnt=bnt, theta=0.0)
+
+
+def acoustic_box(nx=64, ny=63, Lx=1.0, Ly=1.0, Lz=1.0, Ma=1.0, Pr=1.0):
+    """The reference's test/3d case: an inviscid oblique acoustic wave in a
+    square box periodic in both directions (test/3d/README.md).
+
+    * grid: uniform on [0, Lx] x [0, Ly] (test/3d/grid.inp), metrics exact;
+    * mean flow: fluid at rest, rho = T = 1 (util/mkmean.f90, "no flow");
+    * disturbance: the wave of util/mkdist3d.f90:155-215 with kx = 2 pi/Lx,
+      ky = 2 pi/Ly: c3 = exp(i (kx x + ky y)), rho = c3 / (2 cm^2),
+      u = c3 / (2 rho_m cm), v = w = 0, p = c3 / 2,
+      T = (gamma Ma^2 p - T_m rho) / rho_m, cm = sqrt(T_m) / Ma;
+    * deck (test/3d/cfl.inp): Ma 1, Re 0 (inviscid: Navier false and Re =
+      1e99, src/input.f90:40-44), Pr 1, xper and yper, the span Lz.
+    """
+    x1 = np.linspace(0.0, Lx, nx)
+    y1 = np.linspace(0.0, Ly, ny)
+    x = np.asfortranarray(np.repeat(x1[:, None], ny, axis=1))
+    y = np.asfortranarray(np.repeat(y1[None, :], nx, axis=0))
+    ones = np.ones((nx, ny))
+    zeros = np.zeros((nx, ny))
+    metrics = {"m1": ones / Lx, "m2": zeros.copy(), "n1": zeros.copy(), "n2": ones / Ly,
+               "m11": zeros.copy(), "m12": zeros.copy(), "m22": zeros.copy(),
+               "n11": zeros.copy(), "n12": zeros.copy(), "n22": zeros.copy()}
+    metrics = {k: np.asfortranarray(v) for k, v in metrics.items()}
+    vm = np.zeros((5, nx, ny), order="F")
+    vm[0] = 1.0
+    vm[4] = 1.0
+    kx, ky = 2.0 * math.pi / Lx, 2.0 * math.pi / Ly
+    cm = np.sqrt(vm[4]) / Ma
+    c3 = (np.cos(kx * x) * np.cos(ky * y) - np.sin(kx * x) * np.sin(ky * y)
+          + 1j * (np.cos(kx * x) * np.sin(ky * y) + np.sin(kx * x) * np.cos(ky * y)))
+    v = np.zeros((5, nx, ny), np.complex128, order="F")
+    v[0] = 0.5 * c3 / cm ** 2
+    v[1] = c3 * 0.5 / (vm[0] * cm)
+    p = c3 * 0.5
+    v[4] = (GAMMA * Ma ** 2 * p - vm[4] * v[0]) / vm[0]
+    params = dict(nx=nx, ny=ny, dxi=1.0 / (nx - 1), deta=1.0 / (ny - 1), Ma=Ma, Re=1e99, Pr=Pr, gamma=GAMMA,
+                  gamma1=GAMMA1, omega=0.0, kz=kz_of(Lz), alfa=1.0, xper=1, yper=1, navier=0, wall=-1, wallt=-1,
+                  top=-1, optx=-1, opty=-1)
+    return dict(params=params, x=x, y=y, metrics=metrics, vm=vm, v=v, span=Lz)

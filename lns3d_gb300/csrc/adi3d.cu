@@ -794,6 +794,9 @@ struct lns_ctx3d {
   // the sweeps (fillE/fillK alias perx/per2x in the FP64 mode)
   void *matx = nullptr, *maty = nullptr, *perx = nullptr, *per2x = nullptr;
   void *chnx = nullptr, *chny = nullptr, *fillE = nullptr, *fillK = nullptr;
+  // a periodic eta direction (yper): its fill in the reference storage and
+  // in the internal form (aliases in the FP64 mode)
+  void *pery = nullptr, *per2y = nullptr, *fillEy = nullptr, *fillKy = nullptr;
   double* part = nullptr;  // block partials (residual, CFL)
   int nparts = 0;
   double* dscal = nullptr;  // [0] cfl, [1..] residual of the inspection call
@@ -945,43 +948,56 @@ int launch_lhs(lns_ctx3d* c, int dir, T* mat, cudaStream_t st) {
 }
 
 // Arguments of the xi sweep (periodic lines along i, one per j: np = nx,
-// n = nx - 1 unknowns) and of the eta sweep (lines along j, one per i).
+// n = nx - 1 unknowns) and of the eta sweep (lines along j, one per i;
+// periodic lines with yper: n = ny - 1 unknowns).
 lns::chain::Args xargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
   return lns::chain::Args{c->matx, c->chnx, c->perx, c->per2x, c->fillE, c->fillK, rhs, g.nx - 1, g.ny, 1, g.nx};
 }
 lns::chain::Args yargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
+  if (g.yper) return lns::chain::Args{c->maty, c->chny, c->pery, c->per2y, c->fillEy, c->fillKy, rhs, g.ny - 1, g.nx,
+                                      g.nx, 1};
   return lns::chain::Args{c->maty, c->chny, nullptr, nullptr, nullptr, nullptr, rhs, g.ny, g.nx, g.nx, 1};
 }
 
-// The xi sweep: s = D^-1 r, forward recurrence, rows n-1 and n with the
-// periodic fill, the fill correction, backward recurrence.
+// A periodic sweep (xi, or eta with yper): s = D^-1 r, forward recurrence,
+// rows n-1 and n with the periodic fill, the fill correction, backward
+// recurrence.
+// xi_marks: the profiling marks of the xi sweep (after the scaling, the
+// forward recurrence and the fill); an eta sweep marks as a non-periodic one
+// (after the scaling and the forward recurrence with its fill).
 template <typename T>
-int sweep_x(lns_ctx3d* c, T* r, cudaStream_t st) {
+int sweep_periodic(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaStream_t st) {
   namespace ch = lns::chain;
-  const ch::Args a = xargs(c, r);
   const long long pts = (long long)a.n * a.nsys, fill = (long long)(a.n - 3) * a.nsys;
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
   ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
   int rc = mark(c, st);
   ch::chain_fwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
-  if (!rc) rc = mark(c, st);
+  if (!rc && xi_marks) rc = mark(c, st);
   ch::tail_kernel<T><<<a.nsys, 32 * ch::kTailWarps, 0, st>>>(a);
   ch::fill_kernel<T><<<(unsigned)ch::fill_blocks(fill), 256, 0, st>>>(a);
   if (!rc) rc = mark(c, st);
   ch::chain_bwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (rc) return rc;
   cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? LNS_OK : cuda3(e, "xi sweep launch");
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "periodic sweep launch");
 }
 
-// The eta sweep: s = D^-1 r, forward and backward recurrences.
+template <typename T>
+int sweep_x(lns_ctx3d* c, T* r, cudaStream_t st) {
+  return sweep_periodic<T>(c, xargs(c, r), true, st);
+}
+
+// The eta sweep: s = D^-1 r, forward and backward recurrences (periodic
+// lines as the xi sweep).
 template <typename T>
 int sweep_y(lns_ctx3d* c, T* r, cudaStream_t st) {
   namespace ch = lns::chain;
   const ch::Args a = yargs(c, r);
+  if (c->g.yper) return sweep_periodic<T>(c, a, false, st);
   const long long pts = (long long)a.n * a.nsys;
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
@@ -1008,7 +1024,8 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   int rc = launch_lhs<cd>(c, 1, mx, st);
   if (!rc) rc = lns::host::launch_p<cd>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status);
   if (!rc) rc = launch_lhs<cd>(c, 2, my, st);
-  if (!rc) rc = lns::host::launch_bc<cd>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
+  if (!rc && g.yper) rc = lns::host::launch_p<cd>(my, rr, c->pery, c->per2y, g.ny, g.nx, g.nx, 1, 0, st, c->status);
+  else if (!rc) rc = lns::host::launch_bc<cd>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
   if (rc) return rc;
   namespace ch = lns::chain;
   const ch::Args ax = xargs(c, nullptr), ay = yargs(c, nullptr);
@@ -1017,7 +1034,12 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   const unsigned by = (unsigned)((ty + ch::kPrepWarps - 1) / ch::kPrepWarps);
   ch::prep_kernel<cd, TC, true><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
   ch::prep_fill_kernel<cd, TC><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
-  ch::prep_kernel<cd, TC, false><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
+  if (g.yper) {
+    ch::prep_kernel<cd, TC, true><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
+    ch::prep_fill_kernel<cd, TC><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
+  } else {
+    ch::prep_kernel<cd, TC, false><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda3(e, "prep kernels launch");
   int status = 0;
@@ -1119,10 +1141,18 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
     return fail3(LNS_ERR_ARG, "ctx3d_create: nx*ny too large for 32-bit launch indexing");
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
   if (p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: only a periodic xi direction (xper = 1) is supported");
-  if (p->yper != 0 || p->navier != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: need yper = 0 and navier = 1");
-  if (p->wall != 1 && p->wall != 2 && p->wall != 3) return fail3(LNS_ERR_ARG, "ctx3d_create: wall must be 1, 2 or 3");
-  if (p->wallt != 0 && p->wallt != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: wallt must be 0 or 1");
-  if (p->top != 0 && p->top != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0 or 1");
+  if (p->yper != 0 && p->yper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: yper must be 0 or 1");
+  if (p->navier != 0 && p->navier != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: navier must be 0 or 1");
+  if (p->yper == 1 && p->ny < 8) return fail3(LNS_ERR_ARG, "ctx3d_create: a periodic eta direction needs ny >= 8");
+  if (!p->yper) {  // the wall and top rows (a periodic eta direction has neither, src/input.f90:126-132)
+    if (p->navier != 1)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: an inviscid run (navier = 0) needs a periodic eta direction");
+    if (p->wall != 1 && p->wall != 2 && p->wall != 3) return fail3(LNS_ERR_ARG, "ctx3d_create: wall must be 1, 2 or 3");
+    if (p->wallt != 0 && p->wallt != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: wallt must be 0 or 1");
+    if (p->top != 0 && p->top != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: top must be 0 or 1");
+  } else if (p->top == 1 || p->wall == 3) {
+    return fail3(LNS_ERR_ARG, "ctx3d_create: a periodic eta direction has no forced top or bump wall");
+  }
   if (p->loctime != 0 && p->loctime != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: loctime must be 0 or 1");
   if (p->precision != LNS_FP64 && p->precision != LNS_MIXED)
     return fail3(LNS_ERR_ARG, "ctx3d_create: precision must be LNS_FP64 or LNS_MIXED");
@@ -1194,6 +1224,17 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   } else {
     c->fillE = c->perx;
     c->fillK = c->per2x;
+  }
+  if (p->yper) {
+    A(sizeof(cd) * 50 * np, &c->pery);
+    A(sizeof(cd) * 50 * np, &c->per2y);
+    if (mixed) {
+      A(el * 50 * np, &c->fillEy);
+      A(el * 50 * np, &c->fillKy);
+    } else {
+      c->fillEy = c->pery;
+      c->fillKy = c->per2y;
+    }
   }
   A(sizeof(double) * c->nparts, &q); c->part = (double*)q;
   A(sizeof(double) * 3, &q); c->dscal = (double*)q;  // cfl, scratch residual, running residual
@@ -1775,6 +1816,9 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
   for (int p = 0; p < nprob; ++p)
     if (params[p].impl > 1) return fail3(LNS_ERR_ARG, "batch3d_create: batches run impl = 1 (backward Euler)");
   for (int p = 0; p < nprob; ++p)
+    if (params[p].yper != 0 || params[p].navier != 1)
+      return fail3(LNS_ERR_ARG, "batch3d_create: batches run a viscous wall-bounded eta direction (yper = 0)");
+  for (int p = 0; p < nprob; ++p)
     if (params[p].ispg != 0 || params[p].eps_e != 0.0 || params[p].top != 0 || params[p].wall == 3)
       return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge, smoother or forced top (ispg = 0, "
                                 "eps_e = 0, top = 0)");
@@ -2148,6 +2192,8 @@ int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* 
   if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
   if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
   if (prm->impl > 1) return fail3(LNS_ERR_ARG, "server3d_submit: servers run impl = 1 (backward Euler)");
+  if (prm->yper != 0 || prm->navier != 1)
+    return fail3(LNS_ERR_ARG, "server3d_submit: servers run a viscous wall-bounded eta direction (yper = 0)");
   if (prm->ispg != 0 || prm->eps_e != 0.0 || prm->top != 0 || prm->wall == 3)
     return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge, smoother or forced top (ispg = 0, "
                               "eps_e = 0, top = 0)");

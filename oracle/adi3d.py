@@ -40,11 +40,11 @@ def _lib(L=None):
         L.a3_resstat.restype = D
         L.a3_itrbc.argtypes = [ctypes.POINTER(A3Grid), P]
         L.a3_lhs.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, P]
-        L.a3_step.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, P, P, P, P, P, P, P,
+        L.a3_step.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, P, P, P, P, P, P, P, P, P,
                               ctypes.POINTER(I)]
         L.a3_step.restype = D
         L.a3_step_impl.argtypes = [ctypes.POINTER(A3Grid), ctypes.POINTER(A3Ops), P, I, I, I, P, P, P, P, P, P, P, P,
-                                   P, ctypes.POINTER(D)]
+                                   P, P, P, ctypes.POINTER(D)]
         L.a3_step_impl.restype = D
         L._a3_setup = True
     return L
@@ -107,6 +107,8 @@ class Oracle3D:
         self.maty = np.zeros((5, 5, 5, nx, ny), np.complex128, order="F")
         self.perx = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
         self.per2x = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
+        self.pery = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
+        self.per2y = np.zeros((2, 5, 5, nx, ny), np.complex128, order="F")
         self.r = np.zeros((5, nx, ny), np.complex128, order="F")
         self.factored = I(0)
 
@@ -126,7 +128,7 @@ class Oracle3D:
         res = self.L.a3_step_impl(ctypes.byref(self.g), ctypes.byref(self.o), ptr(self.dtl), niter, impl,
                                   self._lstep, ptr(v), ptr(self._vold), ptr(self._v2old), ptr(self._w), ptr(self.r),
                                   ptr(self.matx), ptr(self.maty), ptr(self.perx), ptr(self.per2x),
-                                  ctypes.byref(self._alfa_fac))
+                                  ptr(self.pery), ptr(self.per2y), ctypes.byref(self._alfa_fac))
         self._lstep += 1
         return res
 
@@ -134,7 +136,7 @@ class Oracle3D:
         vold = np.zeros_like(v)
         return self.L.a3_step(ctypes.byref(self.g), ctypes.byref(self.o), ptr(self.dtl), niter, ptr(v), ptr(vold),
                               ptr(self.r), ptr(self.matx), ptr(self.maty), ptr(self.perx), ptr(self.per2x),
-                              ctypes.byref(self.factored))
+                              ptr(self.pery), ptr(self.per2y), ctypes.byref(self.factored))
 
     def lrhs(self, v):
         r = np.zeros_like(v)

@@ -908,7 +908,8 @@ void a3_rtb(const A3Grid* g, double* r, const double* v, const double* vold, con
 /* src/impdrv3d.f90:130-356 with impl = 1, iLHS = 1, USE_CPENTA1BC semantics
    for the xi sweep (the corrected boundary solve) */
 double a3_step(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, double* v, double* vold, double* r,
-               double* matx, double* maty, double* perx, double* per2x, int* factored) {
+               double* matx, double* maty, double* perx, double* per2x, double* pery, double* per2y,
+               int* factored) {
   const int nx = g->nx, ny = g->ny;
   const long n10 = 10L * nx * ny;
   double totres = 0.0;
@@ -924,12 +925,14 @@ double a3_step(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, do
       if (g->xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 0, ORC_COMPAT_PERIODIC_SLOT);
       else orc_cpenta_bc(2, nx, ny, matx, r, 0, 0);
       a3_lhs(g, o, dtl, 2, maty);
-      orc_cpenta_bc(1, ny, nx, maty, r, 0, 0);
+      if (g->yper) orc_cpenta_p(1, ny, nx, maty, r, pery, per2y, 0, ORC_COMPAT_PERIODIC_SLOT);
+      else orc_cpenta_bc(1, ny, nx, maty, r, 0, 0);
       *factored = 1;
     }
     if (g->xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 1, ORC_COMPAT_PERIODIC_SLOT);
     else orc_cpenta_bc(2, nx, ny, matx, r, 1, 0);
-    orc_cpenta_bc(1, ny, nx, maty, r, 1, 0);
+    if (g->yper) orc_cpenta_p(1, ny, nx, maty, r, pery, per2y, 1, ORC_COMPAT_PERIODIC_SLOT);
+    else orc_cpenta_bc(1, ny, nx, maty, r, 1, 0);
     OMP_FOR
     for (long e = 0; e < n10; ++e) v[e] = v[e] + r[e];
     a3_itrbc(g, v);
@@ -947,7 +950,7 @@ double a3_step(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, do
    {1, 2/3, 1/2, g->alfa} before the first step). */
 double a3_step_impl(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, int impl, int lstep, double* v,
                     double* vold, double* v2old, double* w, double* r, double* matx, double* maty, double* perx,
-                    double* per2x, double* alfa_fac) {
+                    double* per2x, double* pery, double* per2y, double* alfa_fac) {
   const int nx = g->nx, ny = g->ny;
   const long n10 = 10L * nx * ny;
   const double pt66 = 6.6666666666666666666e-1, pt5 = 0.5;
@@ -975,12 +978,14 @@ double a3_step_impl(const A3Grid* g, const A3Ops* o, const double* dtl, int nite
       if (gl.xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 0, ORC_COMPAT_PERIODIC_SLOT);
       else orc_cpenta_bc(2, nx, ny, matx, r, 0, 0);
       a3_lhs(&gl, o, dtl, 2, maty);
-      orc_cpenta_bc(1, ny, nx, maty, r, 0, 0);
+      if (gl.yper) orc_cpenta_p(1, ny, nx, maty, r, pery, per2y, 0, ORC_COMPAT_PERIODIC_SLOT);
+      else orc_cpenta_bc(1, ny, nx, maty, r, 0, 0);
       *alfa_fac = gl.alfa;
     }
     if (gl.xper) orc_cpenta_p(2, nx, ny, matx, r, perx, per2x, 1, ORC_COMPAT_PERIODIC_SLOT);
     else orc_cpenta_bc(2, nx, ny, matx, r, 1, 0);
-    orc_cpenta_bc(1, ny, nx, maty, r, 1, 0);
+    if (gl.yper) orc_cpenta_p(1, ny, nx, maty, r, pery, per2y, 1, ORC_COMPAT_PERIODIC_SLOT);
+    else orc_cpenta_bc(1, ny, nx, maty, r, 1, 0);
     OMP_FOR
     for (long e = 0; e < n10; ++e) v[e] = v[e] + r[e];
     a3_itrbc(g, v);

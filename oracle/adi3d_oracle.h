@@ -94,13 +94,14 @@ int a3_lhs(const A3Grid* g, const A3Ops* ops, const double* dtl, int dir, double
    and factored when *factored == 0, and reused afterwards.  r is scratch.
    Returns totres of the last corrector. */
 double a3_step(const A3Grid* g, const A3Ops* ops, const double* dtl, int niter, double* v, double* vold,
-               double* r, double* matx, double* maty, double* perx, double* per2x, int* factored);
+               double* r, double* matx, double* maty, double* perx, double* per2x, double* pery, double* per2y,
+               int* factored);
 /* rtb3D (src/impdrv3d.f90:471-501) and one step of the time schemes impl
    1, 2, 3 (see adi3d_oracle.c); vold, v2old persist across steps */
 void a3_rtb(const A3Grid* g, double* r, const double* v, const double* vold, const double* v2old, const double* dtl);
 double a3_step_impl(const A3Grid* g, const A3Ops* o, const double* dtl, int niter, int impl, int lstep, double* v,
                     double* vold, double* v2old, double* w, double* r, double* matx, double* maty, double* perx,
-                    double* per2x, double* alfa_fac);
+                    double* per2x, double* pery, double* per2y, double* alfa_fac);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
 import refcase  # noqa: E402
-from lns3d_gb300.cases import shear_layer, vortex2d  # noqa: E402
+from lns3d_gb300.cases import acoustic_box, shear_layer, vortex2d  # noqa: E402
 
 # name -> (kind, case arguments, run arguments)
 GOLDEN = {
@@ -32,15 +32,64 @@ GOLDEN = {
     "step3d_shear": ("3d", dict(nx=96, ny=64, seed=0), dict(nsteps=30, cflmax=20.0, loctime=1)),
     "step3d_shear_two_step": ("3d", dict(nx=40, ny=33, seed=1), dict(nsteps=10, cflmax=20.0, loctime=1, impl=2)),
     "step3d_shear_midpoint": ("3d", dict(nx=40, ny=33, seed=1), dict(nsteps=10, cflmax=20.0, loctime=1, impl=3)),
+    # the reference's test/3d case (test/3d/cfl.inp): an inviscid oblique acoustic
+    # wave in a box periodic in both directions, two correctors per step
+    "step3d_box": ("3dbox", dict(nx=64, ny=63), dict(nsteps=20, Re=0.0, Pr=1.0, dtmax=0.0070710678e10,
+                                                     cflmax=0.1, niter=2, loctime=0, Lz=1.0)),
+    # the linear 2D step (src/impdrv.f90 with linear = 1) on the wall-bounded
+    # shear layer at beta = omega = 0
+    "step2d_lin_shear": ("2dlin", dict(nx=48, ny=33, seed=3, beta=0.0, omega=0.0),
+                         dict(nsteps=10, cflmax=20.0, loctime=1)),
 }
 
 
+# the reference's own linear 2D fixture (test/2d: a linear wave on a fluid at
+# rest, Euler, periodic in both directions, big-endian SGI files), run as its
+# run.sh does: ic.dat copied to output.R.0, lns3d < lns3d.inp with byte swap
+TEST2D_DIR = "/root/reference/test/2d"
+
+
+def generate_test2d():
+    import shutil
+
+    from lns3d_gb300 import refio
+
+    r = refcase.Run()
+    try:
+        for f in ("grid.dat", "metric.dat", "mean.dat"):
+            shutil.copy(os.path.join(TEST2D_DIR, f), r.path(f))
+        shutil.copy(os.path.join(TEST2D_DIR, "ic.dat"), r.path("output.R.0"))
+        deck = open(os.path.join(TEST2D_DIR, "lns3d.inp")).read()
+        r.run(deck, swap=True)
+        assert r.prog.oob() == 0
+        x, y = refio.read_grid(r.path("grid.dat"), endian=">")
+        nx, ny = x.shape
+        met = refio.read_metrics(r.path("metric.dat"), nx, ny, endian=">")
+        _, vm, _ = refio.read_field(r.path("mean.dat"), endian=">")
+        _, v0, _ = refio.read_field(r.path("output.R.0"), endian=">")
+        outs = {}
+        for k in (1, 2, 3):
+            h, v, _ = refio.read_field(r.path("output.R.%d" % k), endian=">")
+            outs["v_step%d" % h["lstep"]] = v
+        np.savez_compressed(os.path.join(HERE, "step2d_test2d.npz"), x=x, y=y, vm=vm, v0=v0,
+                            hist=refcase.history(r.path("output.h.1")), deck=deck,
+                            **{"m_" + k: a for k, a in met.items()}, **outs)
+    finally:
+        r.close()
+
+
 def generate(name):
+    if name == "step2d_test2d":
+        return generate_test2d()
     kind, cargs, rargs = GOLDEN[name]
     rargs = dict(rargs)
     nsteps = rargs.pop("nsteps")
     if kind == "2d":
         v, hist, run = refcase.run2d(vortex2d(**cargs), nsteps, **rargs)
+    elif kind == "3dbox":
+        v, hist, run = refcase.run3d(acoustic_box(**cargs), nsteps, **rargs)
+    elif kind == "2dlin":
+        v, hist, run = refcase.run2dlin(shear_layer(**cargs), nsteps, **rargs)
     else:
         v, hist, run = refcase.run3d(shear_layer(**cargs), nsteps, **rargs)
     try:
@@ -51,6 +100,6 @@ def generate(name):
 
 
 if __name__ == "__main__":
-    for name in (sys.argv[1:] or GOLDEN):
+    for name in (sys.argv[1:] or list(GOLDEN) + ["step2d_test2d"]):
         generate(name)
         print("wrote", name)

@@ -98,3 +98,20 @@ def run2d(case, nsteps, **kw):
     r.run(deck2d(case, nsteps, **kw))
     _, v, _ = refio.read_field(r.last_restart())
     return v, history(r.path("output.h.1")), r
+
+
+def run2dlin(case, nsteps, **kw):
+    """The reference's linear impdrv (linear = 1, Lz = 0: src/lrhs.f90) on
+    the real part of the case's state: (final v, totres history, Run)."""
+    p = case["params"]
+    r = Run()
+    refio.write_grid(r.path("grid.dat"), case["x"], case["y"])
+    refio.write_metrics(r.path("metric.dat"), case["metrics"])
+    refio.write_field(r.path("mean.dat"), case["vm"], Re=p["Re"], Ma=p["Ma"], Pr=p["Pr"])
+    refio.write_field(r.path("output.R.0"), np.asfortranarray(np.real(case["v"])), Re=p["Re"], Ma=p["Ma"],
+                      Pr=p["Pr"])
+    d = dict(omega=0.0, Lz=0.0)
+    d.update(kw)
+    r.run(deck3d(case, nsteps, **d))
+    _, v, _ = refio.read_field(r.last_restart())
+    return v, history(r.path("output.h.1")), r

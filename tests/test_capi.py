@@ -44,7 +44,7 @@ def test_python_signatures_cover_header():
 
     solver_syms = [n for n in declared_symbols()
                    if n not in ("lns_last_error", "lns_version",
-                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes", "lns_batch3d_bytes",
+                                "lns_mixed_workspace_bytes", "lns_ctx3d_bytes", "lns_ctx2d_bytes", "lns_lin2d_bytes", "lns_batch3d_bytes",
                                 "lns_server3d_bytes_in_use", "lns_tri_workspace_bytes")]
     assert sorted(SIGNATURES) == solver_syms
 
@@ -118,10 +118,10 @@ def _params3d(**kw):
     return Params3D(**base)
 
 
-@pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=0), dict(wallt=2),
+@pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=2), dict(navier=0), dict(wall=0), dict(wallt=2),
                                  dict(top=2), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
-                                 dict(loctime=2), dict(ispg=-1),
-                                 dict(eps_e=-1.0), dict(eps_e=float("nan"))])
+                                 dict(loctime=2), dict(ispg=-1), dict(yper=1, ny=7), dict(yper=1, top=1),
+                                 dict(navier=2, yper=1), dict(eps_e=-1.0), dict(eps_e=float("nan"))])
 def test_ctx3d_rejects_unsupported_options(lib, bad):
     ctx = ctypes.c_void_p()
     rc = lib.lns_ctx3d_create(ctypes.byref(_params3d(**bad)), ctypes.byref(ctx))
@@ -209,3 +209,14 @@ def test_server3d_argument_errors(lib):
     assert lib.lns_server3d_fetch(None, 1, None) == 1
     assert lib.lns_server3d_destroy(None) == 0
     assert lib.lns_server3d_bytes_in_use(None) == 0
+
+
+@pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1)])
+def test_lin2d_rejects_single_mode_options(lib, bad):
+    """The linear 2D context takes beta = omega = 0 and FP64."""
+    ctx = ctypes.c_void_p()
+    base = dict(beta=0.0, omega=0.0)
+    base.update(bad)
+    rc = lib.lns_lin2d_create(ctypes.byref(_params3d(**base)), ctypes.byref(ctx))
+    assert rc == 1 and not ctx.value
+    assert lib.lns_last_error()

@@ -88,6 +88,28 @@ def test_step3d_restatement_equals_reference(cfg):
         run.close()
 
 
+def test_periodic_inviscid_box_equals_reference():
+    """The reference's test/3d case (test/3d/cfl.inp): periodic in both
+    directions (cpenta1p for the eta sweep), inviscid (Re = 0 in the deck),
+    two correctors per step, global time step."""
+    from lns3d_gb300.cases import acoustic_box
+
+    case = acoustic_box(nx=24, ny=21)
+    nsteps = 3
+    v_ref, hist, run = refcase.run3d(case, nsteps, Re=0.0, Pr=1.0, dtmax=0.0070710678e10, cflmax=0.1, niter=2,
+                                     loctime=0, Lz=case["span"])
+    try:
+        assert run.prog.oob() == 0 and run.prog.get("navier") == 0
+        orc = Oracle3D(case, cflmax=0.1, loctime=0, dtmax=0.0070710678e10)
+        v = case["v"].copy(order="F")
+        orc.itrbc(v)
+        res = [orc.step(v, niter=2) for _ in range(nsteps)]
+        assert np.array_equal(v, v_ref), rel(v, v_ref)
+        assert np.array_equal(np.array(res), hist[1::2])
+    finally:
+        run.close()
+
+
 def test_operators_equal_reference():
     """genmtrx(vm, kz, vm) of the linear run (src/lns3d.f90:149): every
     frozen operator array bit for bit."""
