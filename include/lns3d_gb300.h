@@ -451,6 +451,8 @@ size_t lns_lin2d_bytes(const lns_lin2d* ctx);
 int lns_upload_metrics_lin2d(lns_lin2d* ctx, const double* metrics);
 int lns_upload_mean_lin2d(lns_lin2d* ctx, const double* vm, double* cfl);
 int lns_itrbc_lin2d_dev(lns_lin2d* ctx, double* v, void* stream);
+/* host copy of the frozen time step dtl(nx,ny) (set_time_step on the mean flow) */
+int lns_get_dtl_lin2d(lns_lin2d* ctx, double* dtl);
 /* v(5,nx,ny) real on the host, in place; totres[nsteps] (may be NULL) gets
  * resstat's value of the last corrector of each step */
 int lns_step_lin2d(lns_lin2d* ctx, double* v, int32_t nsteps, int32_t niter, double* totres);

@@ -16,6 +16,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIBNAME = "liblns3d_gb300.so"
 PROBE_NAME = "liblns3d_probe.so"
+DRIVER_NAME = "lns3d_gpu"
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -64,8 +65,20 @@ def build_library(verbose=False):
         tmp = target + ".tmp"
         _run([nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + objs + ["-lcudart"])
         os.replace(tmp, target)
+        driver = ex.submit(build_driver)
         probe.result()
+        driver.result()
     return target
+
+
+def build_driver():
+    """The host program lns3d_gpu (csrc/host/lns3d_gpu.cpp): the reference's
+    implicit run over the C ABI, linked to the library beside it."""
+    out = os.path.join(LIBDIR, DRIVER_NAME)
+    _run([_nvcc(), "-O2", "-std=c++17", "-o", out + ".tmp", os.path.join(CSRC, "host", "lns3d_gpu.cpp"),
+          "-L" + LIBDIR, "-llns3d_gb300", "-Xlinker", "-rpath,$ORIGIN"])
+    os.replace(out + ".tmp", out)
+    return out
 
 
 def build_probe():

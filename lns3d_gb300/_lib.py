@@ -84,6 +84,7 @@ SIGNATURES = {
     "lns_upload_metrics_lin2d": [P, DP],
     "lns_upload_mean_lin2d": [P, DP, DP],
     "lns_itrbc_lin2d_dev": [P, DP, P],
+    "lns_get_dtl_lin2d": [P, DP],
     "lns_step_lin2d": [P, DP, I32, I32, DP],
     "lns_step_lin2d_dev": [P, DP, I32, I32, DP, P],
     "lns_ctx3d_profile": [P, I32],

@@ -111,6 +111,11 @@ int lns_upload_mean_lin2d(lns_lin2d* c, const double* vm, double* cfl) {
   return lns_upload_mean3d(c->ctx, vm, cfl);
 }
 
+int lns_get_dtl_lin2d(lns_lin2d* c, double* dtl) {
+  if (!c || !dtl) return lns_fail(LNS_ERR_ARG, "get_dtl_lin2d: null argument");
+  return lns_get_field3d(c->ctx, 8, dtl);
+}
+
 int lns_itrbc_lin2d_dev(lns_lin2d* c, double* v, void* stream) {
   if (!c || !v) return lns_fail(LNS_ERR_ARG, "itrbc_lin2d: null argument");
   cudaStream_t st = (cudaStream_t)stream;
