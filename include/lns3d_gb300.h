@@ -274,7 +274,10 @@ int lns_get_field2d(lns_ctx2d* ctx, int32_t which, double* out);
  * 1, 0), exceeds it (about 29 900 rows x lines) are rejected with
  * LNS_ERR_ARG and a message giving both sizes.  Nothing in the scratch needs
  * to start at zero.  The first call on a device looks up the array's address
- * (once per device); make that first call before any stream capture.  All
+ * (once per device); make that first call before any stream capture.  The
+ * address is kept for the rest of the process: after cudaDeviceReset (or
+ * anything else that destroys the device's primary context) this entry
+ * point must not be called again in that process.  All
  * calls on a device share the one array, so calls that overlap in time -- on
  * different streams or from different host threads -- race and corrupt each
  * other's results: keep them ordered (one stream, or events). */
@@ -349,6 +352,12 @@ typedef struct {
                                 ibuff = 0) until lns_upload_buffer3d.  0 turns both off.
                                 Symmetry planes (lsym, rsym) are not supported.  Batches and
                                 servers take 0. */
+  int32_t left, right;       /* the xi boundaries when xper = 0 (src/itrbc3d.f90:203-414,
+                                src/rhsbc3d.f90:167-324, src/lhsbc1f3d.f90:412-448,
+                                src/lhsbc2f3d.f90:146-174): left 0 zero disturbance, 1 an
+                                incoming acoustic wave exp(-a (x - x0)) exp(i kk x) formed from
+                                the mean flow (lns_upload_inflow3d); right 0 zero disturbance.
+                                Ignored with xper = 1.  Batches and servers take xper = 1. */
 } lns_params3d;
 
 typedef struct lns_ctx3d lns_ctx3d;

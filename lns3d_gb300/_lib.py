@@ -134,7 +134,7 @@ class Params3D(ctypes.Structure):
                 ("alfa", ctypes.c_double), ("cflmax", ctypes.c_double), ("dtmax", ctypes.c_double),
                 ("loctime", I32), ("xper", I32), ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32),
                 ("top", I32), ("optx", I32), ("opty", I32), ("precision", I32),
-                ("impl", I32), ("ispg", I32), ("eps_e", ctypes.c_double)]
+                ("impl", I32), ("ispg", I32), ("eps_e", ctypes.c_double), ("left", I32), ("right", I32)]
 
 
 def lib():

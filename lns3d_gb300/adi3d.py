@@ -62,7 +62,8 @@ class ImpDrv3D:
                        gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), omega=p["omega"], beta=p["kz"],
                        alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"],
                        navier=p["navier"], wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"],
-                       opty=p["opty"], precision=precision, impl=impl, ispg=ispg, eps_e=eps_e)
+                       opty=p["opty"], precision=precision, impl=impl, ispg=ispg, eps_e=eps_e,
+                       left=p.get("left", -1), right=p.get("right", -1))
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")
@@ -75,7 +76,7 @@ class ImpDrv3D:
             check(lib().lns_upload_sponge3d(self._ctx, ctypes.c_void_p(s1.ctypes.data),
                                             ctypes.c_void_p(s2.ctypes.data) if s2 is not None else None),
                   "lns_upload_sponge3d")
-        if ispg in (2, 3) or int(p["top"]) == 1:
+        if ispg in (2, 3) or int(p["top"]) == 1 or (not int(p["xper"]) and int(p.get("left", -1)) == 1):
             xx = np.asfortranarray(x, dtype=np.float64)
             wa = np.ascontiguousarray(wamp, dtype=np.float64) if wamp is not None else None
             check(lib().lns_upload_inflow3d(self._ctx, ctypes.c_void_p(xx.ctypes.data),
@@ -359,7 +360,8 @@ class ImpDrvLin2D:
                        gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), omega=0.0, beta=0.0, alfa=p["alfa"],
                        cflmax=cflmax, dtmax=dtmax, loctime=loctime, xper=p["xper"], yper=p["yper"],
                        navier=p["navier"], wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"],
-                       opty=p["opty"], precision=FP64, impl=impl, ispg=ispg, eps_e=eps_e)
+                       opty=p["opty"], precision=FP64, impl=impl, ispg=ispg, eps_e=eps_e,
+                       left=p.get("left", -1), right=p.get("right", -1))
         self._ctx = ctypes.c_void_p()
         check(lib().lns_lin2d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_lin2d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")

@@ -317,6 +317,10 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
   const int i = (int)(p % g.nx) + 1, j = (int)(p / g.nx) + 1;
   const cd one{1.0, 0.0}, zero{0.0, 0.0};
   const cd ident = (k == 3 && a == b) ? one : zero;
+  // the xi boundaries of a non-periodic xi direction (src/lhsbc1f3d.f90:412-448,
+  // src/lhsbc2f3d.f90:146-174); they follow the wall and top rows, so the
+  // corners take them
+  if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && g.right == 0))) return store_el(mat, q, ident);
   // boundary conditions of the wall (j = 1) and top (j = ny) rows
   if (!g.yper && (g.top == 0 || g.top == 1) && j == g.ny) return store_el(mat, q, ident);
   if (!g.yper && g.navier && j == 1) {
@@ -371,13 +375,16 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
 // t = (c3/(2 cm^2), c3/(2 rho cm), 0, 0, (gamma Ma^2 c3/2 - T c3/(2 cm^2))/rho)
 // With row0 > 0 the kernel forms only row row0 (the forced top boundary's
 // wave, src/itrbc3d.f90:166-196, wamp always applied) into vt(5,nx).
-__global__ void inflow_target_kernel(Grid g, int with_wamp, int row0, const double* __restrict__ vm,
+// With col0 > 0 it forms column col0 (the left boundary's wave,
+// src/itrbc3d.f90:221-247, no wamp) into vt(5,ny).
+__global__ void inflow_target_kernel(Grid g, int with_wamp, int row0, int col0, const double* __restrict__ vm,
                                      const double* __restrict__ xc, const double* __restrict__ wamp, double x0,
                                      cd* __restrict__ vt) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (row0 > 0 ? (long long)g.nx : (long long)g.nx * g.ny)) return;
-  const long long p = row0 > 0 ? (long long)(row0 - 1) * g.nx + t : t;
-  const long long o = row0 > 0 ? t : p;  // output record
+  const long long nt = row0 > 0 ? (long long)g.nx : col0 > 0 ? (long long)g.ny : (long long)g.nx * g.ny;
+  if (t >= nt) return;
+  const long long p = row0 > 0 ? (long long)(row0 - 1) * g.nx + t : col0 > 0 ? t * g.nx + (col0 - 1) : t;
+  const long long o = row0 > 0 || col0 > 0 ? t : p;  // output record
   const int i = (int)(p % g.nx) + 1;
   const double* m = vm + 5 * p;
   const double cm = sqrt(m[4]) / g.Ma, um = m[1];
@@ -596,6 +603,18 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
       #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
     }
+    // the xi boundaries (src/rhsbc3d.f90:167-324), after the wall and top rows
+    if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && g.right == 0)))
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
+    if (!g.xper && i == 1 && g.left == 1) {  // src/rhsbc3d.f90:178-206: r = -(v - t)
+      const cd* T = reinterpret_cast<const cd*>(o.tleft) + 5 * (j - 1);
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const cd w = vs[m + 5 * p];
+        r[m] = cd{-(w.x - T[m].x), -(w.y - T[m].y)};
+      }
+    }
     if (g.xper && i == g.nx)
       #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
@@ -629,7 +648,8 @@ __global__ void __launch_bounds__(128, 4) rhs_kernel(Grid g, Ops o, const cd* __
 // x direction the remaining threads copy the interior rows of column 1 to
 // column nx, and the thread of column 1 copies its boundary rows.
 __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const double* __restrict__ ttop,
-                                        const double* __restrict__ bump, int bx) {
+                                        const double* __restrict__ bump, const double* __restrict__ tleft,
+                                        int bx) {
   const int t = bx * blockDim.x + threadIdx.x;
   const int ncol = g.xper ? g.nx - 1 : g.nx;
   if (t < ncol) {
@@ -669,6 +689,13 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
         v[m + 5 * pix(g, g.nx, 1)] = W(m, 1);
         v[m + 5 * pix(g, g.nx, g.ny)] = W(m, g.ny);
       }
+    // the xi boundaries (src/itrbc3d.f90:203-414), after the wall and top rows
+    if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && g.right == 0)))
+      for (int jj = 1; jj <= g.ny; ++jj)
+        for (int m = 0; m < 5; ++m) W(m, jj) = cd{0.0, 0.0};
+    if (!g.xper && i == 1 && g.left == 1)
+      for (int jj = 1; jj <= g.ny; ++jj)
+        for (int m = 0; m < 5; ++m) W(m, jj) = reinterpret_cast<const cd*>(tleft)[m + 5 * (jj - 1)];
   } else if (g.xper) {
     const int j = t - ncol + 2;
     if (j <= g.ny - 1)
@@ -677,8 +704,8 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
 }
 
 __global__ void bc_kernel(Grid g, cd* __restrict__ v, const double* __restrict__ ttop,
-                          const double* __restrict__ bump) {
-  bc_body(g, v, ttop, bump, blockIdx.x);
+                          const double* __restrict__ bump, const double* __restrict__ tleft) {
+  bc_body(g, v, ttop, bump, tleft, blockIdx.x);
 }
 
 // ------------------------------------------------------------- batching
@@ -708,7 +735,7 @@ __global__ void bc_batch_kernel(const StepArgs* __restrict__ list, const int2* _
                                 const int* __restrict__ active) {
   const int2 w = table[blockIdx.x];
   if (!active[w.x]) return;
-  bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, list[w.x].o.bump, w.y);
+  bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, list[w.x].o.bump, list[w.x].o.tleft, w.y);
 }
 __global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4* __restrict__ table,
                                    const int* __restrict__ active) {
@@ -809,6 +836,7 @@ struct lns_ctx3d {
   double *spg_a = nullptr, *spg_b = nullptr, *vt = nullptr;  // the target sponges (ispg 2-4)
   double *xc = nullptr, *wamp = nullptr;  // ispg 2, 3 or top 1: x(nx,ny), wamp(nx) (ones until uploaded)
   double* ttop = nullptr;                 // top 1: the wave of row ny, complex (5,nx)
+  double* tleft = nullptr;                // left 1: the wave of column 1, complex (5,ny)
   double* bump = nullptr;                 // wall 3: u1w, u2w, u3w, tw, twp, complex (5,nx)
   bool have_bump = false;
   double x0 = 0.0;
@@ -952,6 +980,7 @@ int launch_lhs(lns_ctx3d* c, int dir, T* mat, cudaStream_t st) {
 // periodic lines with yper: n = ny - 1 unknowns).
 lns::chain::Args xargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
+  if (!g.xper) return lns::chain::Args{c->matx, c->chnx, nullptr, nullptr, nullptr, nullptr, rhs, g.nx, g.ny, 1, g.nx};
   return lns::chain::Args{c->matx, c->chnx, c->perx, c->per2x, c->fillE, c->fillK, rhs, g.nx - 1, g.ny, 1, g.nx};
 }
 lns::chain::Args yargs(lns_ctx3d* c, void* rhs) {
@@ -986,8 +1015,30 @@ int sweep_periodic(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaS
   return e == cudaSuccess ? LNS_OK : cuda3(e, "periodic sweep launch");
 }
 
+// A sweep of lines with boundary-closure rows: s = D^-1 r, forward and
+// backward recurrences.  xi_marks: the profiling marks of the xi sweep
+// (after the scaling, the forward recurrence and a third, empty fill
+// segment).
+template <typename T>
+int sweep_bc(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaStream_t st) {
+  namespace ch = lns::chain;
+  const long long pts = (long long)a.n * a.nsys;
+  const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
+  const size_t sm = ch::chain_smem_bytes<T>();
+  ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
+  int rc = mark(c, st);
+  ch::chain_fwd_kernel<T, false><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
+  if (!rc) rc = mark(c, st);
+  if (!rc && xi_marks) rc = mark(c, st);
+  ch::chain_bwd_kernel<T, false><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
+  if (rc) return rc;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "sweep launch");
+}
+
 template <typename T>
 int sweep_x(lns_ctx3d* c, T* r, cudaStream_t st) {
+  if (!c->g.xper) return sweep_bc<T>(c, xargs(c, r), true, st);
   return sweep_periodic<T>(c, xargs(c, r), true, st);
 }
 
@@ -1022,7 +1073,8 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(c->status, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda3(e, "cudaMemsetAsync");
   int rc = launch_lhs<cd>(c, 1, mx, st);
-  if (!rc) rc = lns::host::launch_p<cd>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status);
+  if (!rc && g.xper) rc = lns::host::launch_p<cd>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status);
+  else if (!rc) rc = lns::host::launch_bc<cd>(mx, rr, g.nx, g.ny, 1, g.nx, 0, st, c->status);
   if (!rc) rc = launch_lhs<cd>(c, 2, my, st);
   if (!rc && g.yper) rc = lns::host::launch_p<cd>(my, rr, c->pery, c->per2y, g.ny, g.nx, g.nx, 1, 0, st, c->status);
   else if (!rc) rc = lns::host::launch_bc<cd>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
@@ -1032,8 +1084,12 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   const long long tx = (long long)ax.n * ax.nsys, ty = (long long)ay.n * ay.nsys;
   const unsigned bx = (unsigned)((tx + ch::kPrepWarps - 1) / ch::kPrepWarps);
   const unsigned by = (unsigned)((ty + ch::kPrepWarps - 1) / ch::kPrepWarps);
-  ch::prep_kernel<cd, TC, true><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
-  ch::prep_fill_kernel<cd, TC><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+  if (g.xper) {
+    ch::prep_kernel<cd, TC, true><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+    ch::prep_fill_kernel<cd, TC><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+  } else {
+    ch::prep_kernel<cd, TC, false><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+  }
   if (g.yper) {
     ch::prep_kernel<cd, TC, true><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
     ch::prep_fill_kernel<cd, TC><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
@@ -1058,7 +1114,7 @@ int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
   const long long n = 5 * c->np;
   if (add) lns::a3::add_kernel<cd, RT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, r);
   const int nt = g.nx + g.ny;
-  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v, c->ops.ttop, c->ops.bump);
+  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v, c->ops.ttop, c->ops.bump, c->ops.tleft);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "update kernels launch");
 }
@@ -1140,7 +1196,11 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if ((long long)p->nx * p->ny > (1LL << 31) / 125)
     return fail3(LNS_ERR_ARG, "ctx3d_create: nx*ny too large for 32-bit launch indexing");
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
-  if (p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: only a periodic xi direction (xper = 1) is supported");
+  if (p->xper != 0 && p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: xper must be 0 or 1");
+  if (!p->xper) {
+    if (p->left != 0 && p->left != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0 or 1 (xper = 0)");
+    if (p->right != 0) return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0 (xper = 0)");
+  }
   if (p->yper != 0 && p->yper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: yper must be 0 or 1");
   if (p->navier != 0 && p->navier != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: navier must be 0 or 1");
   if (p->yper == 1 && p->ny < 8) return fail3(LNS_ERR_ARG, "ctx3d_create: a periodic eta direction needs ny >= 8");
@@ -1173,6 +1233,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   g.gamma1 = p->gamma1 != 0.0 ? p->gamma1 : p->gamma - 1.0;
   g.omega = p->omega; g.kz = p->beta; g.alfa = p->alfa;
   g.xper = p->xper; g.yper = p->yper; g.navier = p->navier; g.wall = p->wall; g.wallt = p->wallt; g.top = p->top;
+  g.left = p->xper ? -1 : p->left;
+  g.right = p->xper ? -1 : p->right;
   g.dxinv = 1.0 / p->dxi; g.dyinv = 1.0 / p->deta;
   g.dxsinv = 1.0 / (p->dxi * p->dxi); g.dysinv = 1.0 / (p->deta * p->deta);
   coef1(p->optx, g.dxinv, g.gx);
@@ -1203,25 +1265,29 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
     A(sizeof(double) * 10 * np, &q); c->vt = (double*)q;
   }
   if (p->ispg == 2 || p->ispg == 3) { A(sizeof(double) * np, &q); c->spg_a = (double*)q; }
-  if (p->ispg == 2 || p->ispg == 3 || p->top == 1) {
+  const bool left_wave = !p->xper && p->left == 1;
+  if (p->ispg == 2 || p->ispg == 3 || p->top == 1 || left_wave) {
     A(sizeof(double) * np, &q); c->xc = (double*)q;
     A(sizeof(double) * p->nx, &q); c->wamp = (double*)q;
   }
   if (p->top == 1) { A(sizeof(double) * 10 * p->nx, &q); c->ttop = (double*)q; }
+  if (left_wave) { A(sizeof(double) * 10 * p->ny, &q); c->tleft = (double*)q; }
   if (p->wall == 3) { A(sizeof(double) * 10 * p->nx, &q); c->bump = (double*)q; }
   if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
   else { A(sizeof(cd) * 5 * np, &q); c->r64 = (cd*)q; }
   A(sizeof(cd) * 125 * np, &c->matx);
   A(sizeof(cd) * 125 * np, &c->maty);
-  A(sizeof(cd) * 50 * np, &c->perx);
-  A(sizeof(cd) * 50 * np, &c->per2x);
+  if (p->xper) {
+    A(sizeof(cd) * 50 * np, &c->perx);
+    A(sizeof(cd) * 50 * np, &c->per2x);
+  }
   A(el * 125 * np, &c->chnx);
   A(el * 125 * np, &c->chny);
-  if (mixed) {
+  if (p->xper && mixed) {
     A(el * 50 * np, &c->fillE);
     A(el * 50 * np, &c->fillK);
-  } else {
+  } else if (p->xper) {
     c->fillE = c->perx;
     c->fillK = c->per2x;
   }
@@ -1298,9 +1364,9 @@ int need_data(const lns_ctx3d* c, const char* who) {
   if (!c->have_mean) return fail3(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the mean flow first");
   if (c->prm.ispg != 0 && !c->have_sponge)
     return fail3(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
-  if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1) && !c->have_inflow)
+  if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1 || c->tleft) && !c->have_inflow)
     return fail3(LNS_ERR_ARG,
-                 std::string(who) + ": ispg 2, 3 or top 1: upload the wave data (lns_upload_inflow3d) first");
+                 std::string(who) + ": ispg 2, 3, top 1 or left 1: upload the wave data (lns_upload_inflow3d) first");
   if (c->prm.wall == 3 && !c->have_bump)
     return fail3(LNS_ERR_ARG, std::string(who) + ": wall 3: upload the bump (lns_upload_bump3d) first");
   if (c->prm.ispg == 4 && !c->have_target)
@@ -1314,11 +1380,16 @@ int make_inflow_target(lns_ctx3d* c) {
   const long long np = c->np;
   if (c->prm.ispg == 2 || c->prm.ispg == 3)
     lns::a3::inflow_target_kernel<<<(unsigned)((np + 255) / 256), 256>>>(
-        c->g, c->prm.ispg == 3, 0, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->vt));
+        c->g, c->prm.ispg == 3, 0, 0, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->vt));
   if (c->prm.top == 1) {
     lns::a3::inflow_target_kernel<<<(unsigned)((c->g.nx + 127) / 128), 128>>>(
-        c->g, 1, c->g.ny, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->ttop));
+        c->g, 1, c->g.ny, 0, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->ttop));
     c->ops.ttop = c->ttop;
+  }
+  if (c->tleft) {
+    lns::a3::inflow_target_kernel<<<(unsigned)((c->g.ny + 127) / 128), 128>>>(
+        c->g, 0, 0, 1, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->tleft));
+    c->ops.tleft = c->tleft;
   }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -1356,8 +1427,8 @@ int lns_upload_sponge3d(lns_ctx3d* c, const double* spg, const double* spg2) {
 
 int lns_upload_inflow3d(lns_ctx3d* c, const double* x, const double* wamp, double x0) {
   if (!c || !x) return fail3(LNS_ERR_ARG, "upload_inflow3d: null argument");
-  if (c->prm.ispg != 2 && c->prm.ispg != 3 && c->prm.top != 1)
-    return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3, or top 1");
+  if (c->prm.ispg != 2 && c->prm.ispg != 3 && c->prm.top != 1 && !c->tleft)
+    return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3, top 1 or left 1");
   if (c->prm.ispg == 3 && !wamp) return fail3(LNS_ERR_ARG, "upload_inflow3d: ispg 3 needs wamp");
   if (!std::isfinite(x0)) return fail3(LNS_ERR_ARG, "upload_inflow3d: x0 must be finite");
   int rc = check_device(c);
@@ -1816,8 +1887,9 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
   for (int p = 0; p < nprob; ++p)
     if (params[p].impl > 1) return fail3(LNS_ERR_ARG, "batch3d_create: batches run impl = 1 (backward Euler)");
   for (int p = 0; p < nprob; ++p)
-    if (params[p].yper != 0 || params[p].navier != 1)
-      return fail3(LNS_ERR_ARG, "batch3d_create: batches run a viscous wall-bounded eta direction (yper = 0)");
+    if (params[p].yper != 0 || params[p].navier != 1 || params[p].xper != 1)
+      return fail3(LNS_ERR_ARG, "batch3d_create: batches run a periodic xi direction and a viscous wall-bounded eta "
+                                "direction (xper = 1, yper = 0)");
   for (int p = 0; p < nprob; ++p)
     if (params[p].ispg != 0 || params[p].eps_e != 0.0 || params[p].top != 0 || params[p].wall == 3)
       return fail3(LNS_ERR_ARG, "batch3d_create: batches run without a sponge, smoother or forced top (ispg = 0, "
@@ -2192,8 +2264,9 @@ int lns_server3d_submit(lns_server3d* s, const lns_params3d* prm, const double* 
   if (!s || !prm || !metrics || !vm || !v || !id) return fail3(LNS_ERR_ARG, "server3d_submit: null argument");
   if (prm->precision != s->precision) return fail3(LNS_ERR_ARG, "server3d_submit: precision differs from the server's");
   if (prm->impl > 1) return fail3(LNS_ERR_ARG, "server3d_submit: servers run impl = 1 (backward Euler)");
-  if (prm->yper != 0 || prm->navier != 1)
-    return fail3(LNS_ERR_ARG, "server3d_submit: servers run a viscous wall-bounded eta direction (yper = 0)");
+  if (prm->yper != 0 || prm->navier != 1 || prm->xper != 1)
+    return fail3(LNS_ERR_ARG, "server3d_submit: servers run a periodic xi direction and a viscous wall-bounded eta "
+                              "direction (xper = 1, yper = 0)");
   if (prm->ispg != 0 || prm->eps_e != 0.0 || prm->top != 0 || prm->wall == 3)
     return fail3(LNS_ERR_ARG, "server3d_submit: servers run without a sponge, smoother or forced top (ispg = 0, "
                               "eps_e = 0, top = 0)");

@@ -66,6 +66,7 @@ struct Grid {
   double dxi, deta;
   double Ma, Re, Pr, gamma, gamma1, omega, kz, alfa;
   int xper, yper, navier, wall, wallt, top;
+  int left = -1, right = -1;             // xi boundaries when xper = 0
   double gx[6], gy[6], dx2[7], dy2[7];   // interior first / second derivative stencils (src/cgrad*.f90)
   double dxinv, dyinv, dxsinv, dysinv;
 };
@@ -93,6 +94,8 @@ struct Ops {
   const double* vt = nullptr;
   // the forced top boundary (top = 1): its wave at row ny, complex (5,nx)
   const double* ttop = nullptr;
+  // the forced left boundary (left = 1, xper = 0): its wave at column 1, complex (5,ny)
+  const double* tleft = nullptr;
   // the bump wall (wall = 3): u1w, u2w, u3w, tw, twp, complex (5,nx)
   const double* bump = nullptr;
   // explicit smoother / implicit damping: eps_e buff(nx,ny); null when eps_e = 0

@@ -278,7 +278,7 @@ int check_p(int np, int nsys, int nblk, const char* who) {
 namespace {
 
 constexpr size_t kStaticWorkBytes = size_t(LNS_STATIC_WORKSPACE_BYTES);
-__device__ __align__(256) unsigned char g_static_work[kStaticWorkBytes];
+static __device__ __align__(256) unsigned char g_static_work[kStaticWorkBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_static_mu;

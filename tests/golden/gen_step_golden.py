@@ -40,7 +40,20 @@ GOLDEN = {
     # shear layer at beta = omega = 0
     "step2d_lin_shear": ("2dlin", dict(nx=48, ny=33, seed=3, beta=0.0, omega=0.0),
                          dict(nsteps=10, cflmax=20.0, loctime=1)),
+    # a non-periodic xi direction: zero-disturbance inflow and outflow planes,
+    # and an incoming acoustic wave at the inflow plane (with which the
+    # reference's iteration grows fast on this case: three steps)
+    "step3d_open": ("3dopen", dict(nx=48, ny=33, seed=4, left=0, right=0), dict(nsteps=10, cflmax=20.0, loctime=1)),
+    "step3d_open_wave": ("3dopen", dict(nx=48, ny=33, seed=4, left=1, right=0),
+                         dict(nsteps=3, cflmax=20.0, loctime=1, x0=0.5)),
 }
+
+
+def open_layer(left, right, **kw):
+    """The shear layer with a non-periodic xi direction (xper = 0)."""
+    case = shear_layer(**kw)
+    case["params"].update(xper=0, left=left, right=right)
+    return case
 
 
 # the reference's own linear 2D fixture (test/2d: a linear wave on a fluid at
@@ -90,6 +103,8 @@ def generate(name):
         v, hist, run = refcase.run3d(acoustic_box(**cargs), nsteps, **rargs)
     elif kind == "2dlin":
         v, hist, run = refcase.run2dlin(shear_layer(**cargs), nsteps, **rargs)
+    elif kind == "3dopen":
+        v, hist, run = refcase.run3d(open_layer(**cargs), nsteps, **rargs)
     else:
         v, hist, run = refcase.run3d(shear_layer(**cargs), nsteps, **rargs)
     try:

@@ -18,8 +18,8 @@ def deck3d(case, nsteps, cflmax=20.0, dtmax=1e30, loctime=1, impl=1, niter=1, **
     p = case["params"]
     d = dict(Ma=p["Ma"], Re=p["Re"], Pr=p["Pr"], cflmax=cflmax, dtmax=dtmax, nstep=nsteps, xper=bool(p["xper"]),
              yper=bool(p["yper"]), optx=p["optx"], opty=p["opty"], linear=1, impl=impl, iLHS=1, niter=niter,
-             loctime=loctime, top=p["top"], wall=p["wall"], left=-1, right=-1, wallt=p["wallt"],
-             omega=p["omega"], Lz=span_of_kz(p["kz"]), ires=0, ntout=1000000)
+             loctime=loctime, top=p["top"], wall=p["wall"], left=p.get("left", -1), right=p.get("right", -1),
+             wallt=p["wallt"], omega=p["omega"], Lz=span_of_kz(p["kz"]), ires=0, ntout=1000000)
     d.update(kw)
     return refio.write_deck(d)
 

@@ -133,3 +133,27 @@ def test_reference_test2d_fixture(cuda):
     # ires = 1: the reference also measures the residual after each update
     want = d["hist"][0::deck["niter"] + 1]
     assert np.abs(np.asarray(res) - want).max() <= RES_TOL * want.max()
+
+
+@pytest.mark.parametrize("name", ["step3d_open", "step3d_open_wave"])
+def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
+    """A non-periodic xi direction: the boundary-closure rows of the xi LHS
+    (src/lhsbt1f3d.f90), the zero-disturbance and incoming-wave planes
+    (src/itrbc3d.f90:203-414, src/rhsbc3d.f90:167-324,
+    src/lhsbc1f3d.f90:412-448) and the cpenta2bc-factored xi sweep."""
+    import sys
+
+    from lns3d_gb300 import ImpDrv3D
+
+    sys.path.insert(0, GOLDEN)
+    import gen_step_golden
+
+    kind, cargs, rargs, d = golden(name)
+    case = gen_step_golden.open_layer(**cargs)
+    drv = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=rargs["cflmax"], loctime=rargs["loctime"],
+                   x=case["x"], x0=rargs.get("x0", 0.0))
+    v = case["v"].copy(order="F")
+    drv.itrbc(v)
+    res = drv.step(v, nsteps=rargs["nsteps"])
+    assert rel(v, d["v"]) < STATE_TOL, rel(v, d["v"])
+    assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
