@@ -41,11 +41,13 @@ GOLDEN = {
     "step2d_lin_shear": ("2dlin", dict(nx=48, ny=33, seed=3, beta=0.0, omega=0.0),
                          dict(nsteps=10, cflmax=20.0, loctime=1)),
     # a non-periodic xi direction: zero-disturbance inflow and outflow planes,
-    # and an incoming acoustic wave at the inflow plane (with which the
-    # reference's iteration grows fast on this case: three steps)
+    # and an incoming acoustic wave at the inflow plane (the reference's
+    # iteration diverges with it on this case at every CFL tried, its LHS
+    # keeping the closure row where its RHS forces the wave, so one step,
+    # before the growth amplifies rounding differences)
     "step3d_open": ("3dopen", dict(nx=48, ny=33, seed=4, left=0, right=0), dict(nsteps=10, cflmax=20.0, loctime=1)),
     "step3d_open_wave": ("3dopen", dict(nx=48, ny=33, seed=4, left=1, right=0),
-                         dict(nsteps=3, cflmax=20.0, loctime=1, x0=0.5)),
+                         dict(nsteps=1, cflmax=20.0, loctime=1, x0=0.5)),
 }
 
 
