@@ -76,10 +76,11 @@ KERNEL_FLOPS = {"x_scale": 200, "x_fwd": 400, "x_fill": 800, "x_bwd": 400, "y_sc
 KERNEL_NAMES = {"x_fwd": "chain_fwd_kernel<cd, periodic> (xi forward recurrence)",
                 "x_bwd": "chain_bwd_kernel<cd, periodic> (xi backward recurrence)",
                 "rhs": "grad1_kernel + rhs_kernel + resid_kernel"}
-# DRAM bytes per launch from ncu captures on this workload: the forward
-# recurrence from profiles/chain_kernels_cd_xsweep_512x256.md, the backward
-# one from an earlier capture of the same records read by one warp per line
-KERNEL_TRAFFIC = {"x_fwd": 129.294080e6 + 5.967104e6, "x_bwd": 129.350144e6 + 6.129152e6}
+# DRAM bytes (read + write) per launch from ncu captures on this workload:
+# the forward recurrence from profiles/chain_kernels_cd_xsweep_512x256.md,
+# the backward ones from profiles/chain_bwd_kernel_cd_sweeps_512x256.md
+KERNEL_TRAFFIC = {"x_fwd": 129.294080e6 + 5.967104e6, "x_bwd": 129.434624e6 + 5.784832e6,
+                  "y_bwd": 130.674432e6 + 2.793728e6}
 KERNELS_PER_STEP = 14  # bc (predictor), grad1, rhs, resid, xi sweep (5), eta sweep (3), add, bc
 
 # ---- secondary: the isolated batched solve
@@ -495,31 +496,63 @@ def batch_problems(P=64, seed=4):
 
 
 def run_batch(torch, with_cpu, max_steps=2000, tol=1e-10):
-    """All 64 problems to a 1e-10 residual in one batch (mixed precision:
-    FP64 residual, FP32 scaled factors and sweeps), lines per CTA autotuned."""
+    """All 64 problems to a 1e-10 residual in one batch, lines per CTA
+    autotuned, twice: in FP64 (the drop-in arithmetic) and in the mixed mode
+    (FP64 residual, FP32 scaled factors and sweeps).  The headline of the leg
+    is the mixed run; the FP64 run of the same problems gives the mixed/FP64
+    ratio on equal work and the mixed results' distance from the FP64 ones."""
     import numpy as np
 
     import lns3d_gb300 as g
 
     probs = batch_problems()
     pts = np.array([c["params"]["nx"] * c["params"]["ny"] for c in probs])
-    t0 = time.perf_counter()
-    batch = g.Batch3D(probs, cflmax=CFL3, loctime=1, precision=g.adi3d.MIXED)
-    w = batch.tune()
-    setup = time.perf_counter() - t0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    steps, res = batch.run(max_steps=max_steps, tol=tol, check_every=25)
-    wall = time.perf_counter() - t0
-    conv = steps > 0
-    done_pts = float((pts * np.where(conv, steps, max_steps)).sum())
+
+    def one(precision):
+        t0 = time.perf_counter()
+        batch = g.Batch3D(probs, cflmax=CFL3, loctime=1, precision=precision)
+        w = batch.tune()
+        setup = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        steps, res = batch.run(max_steps=max_steps, tol=tol, check_every=25)
+        wall = time.perf_counter() - t0
+        states = [batch.state(k) for k in range(len(probs))]
+        nbytes = int(batch.device_bytes)
+        batch.close()
+        conv = steps > 0
+        done_pts = float((pts * np.where(conv, steps, max_steps)).sum())
+        return dict(steps=steps, conv=conv, states=states, wall=wall, setup=setup, w=w, bytes=nbytes,
+                    value=done_pts / wall)
+
+    f64 = one(g.adi3d.FP64)
+    mix = one(g.adi3d.MIXED)
+    both = f64["conv"] & mix["conv"]
+    # time to the tolerance on the problems that reach it in both modes: the
+    # wall time of each run scaled by that set's share of its point-steps
+    def share(r):
+        done = pts * np.where(r["conv"], r["steps"], max_steps)
+        return float((pts * r["steps"])[both].sum() / done.sum()) * r["wall"]
+
+    err = max((float(np.abs(mix["states"][k] - f64["states"][k]).max() / np.abs(f64["states"][k]).max())
+               for k in np.flatnonzero(both)), default=None)
+    conv = mix["conv"]
+    steps = mix["steps"]
     out = {"workload": "batch-64-shear-layers-beta0-0.4-omega0.01-0.1-uneven-grids-mixed-to-1e-10",
            "problems": len(probs), "grid_points": int(pts.sum()), "converged": int(conv.sum()),
            "steps_min": int(steps[conv].min()) if conv.any() else None,
            "steps_max": int(steps[conv].max()) if conv.any() else None,
-           "wall_s": wall, "setup_s": setup, "value": done_pts / wall, "unit": "grid-pt-steps/s",
-           "lines_per_cta": w, "device_bytes": int(batch.device_bytes), "cpu_baseline": None}
-    batch.close()
+           "wall_s": mix["wall"], "setup_s": mix["setup"], "value": mix["value"], "unit": "grid-pt-steps/s",
+           "lines_per_cta": mix["w"], "device_bytes": mix["bytes"],
+           "not_converged": [int(k) for k in np.flatnonzero(~conv)],
+           "fp64": {"value": f64["value"], "wall_s": f64["wall"], "converged": int(f64["conv"].sum()),
+                    "lines_per_cta": f64["w"], "device_bytes": f64["bytes"]},
+           "mixed_vs_fp64": {"throughput_ratio": mix["value"] / f64["value"],
+                             "converged_in_both": int(both.sum()),
+                             "same_steps_in_both": int((f64["steps"][both] == mix["steps"][both]).sum()),
+                             "time_to_tol_ratio": share(f64) / share(mix) if both.any() else None,
+                             "max_state_rel_diff": err},
+           "cpu_baseline": None}
     if with_cpu:
         import oracle
         from oracle.adi3d import Oracle3D

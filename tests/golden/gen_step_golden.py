@@ -41,13 +41,14 @@ GOLDEN = {
     "step2d_lin_shear": ("2dlin", dict(nx=48, ny=33, seed=3, beta=0.0, omega=0.0),
                          dict(nsteps=10, cflmax=20.0, loctime=1)),
     # a non-periodic xi direction: zero-disturbance inflow and outflow planes,
-    # and an incoming acoustic wave at the inflow plane (the reference's
-    # iteration diverges with it on this case at every CFL tried, its LHS
-    # keeping the closure row where its RHS forces the wave, so one step,
-    # before the growth amplifies rounding differences)
+    # and an incoming acoustic wave at the inflow plane.  With the wave the
+    # reference's step is ill-conditioned at CFL 20 on this case (one step
+    # takes the state from 0.4 to 2e4, and the reference built with FMA
+    # contraction differs from itself by 5e-10); at CFL 0.2 that difference
+    # is 3e-16 after five steps, which carry the wave into the interior
     "step3d_open": ("3dopen", dict(nx=48, ny=33, seed=4, left=0, right=0), dict(nsteps=10, cflmax=20.0, loctime=1)),
     "step3d_open_wave": ("3dopen", dict(nx=48, ny=33, seed=4, left=1, right=0),
-                         dict(nsteps=1, cflmax=20.0, loctime=1, x0=0.5)),
+                         dict(nsteps=5, cflmax=0.2, loctime=1, x0=0.5)),
 }
 
 
