@@ -63,6 +63,8 @@ PHASE_FLOPS = {"xsweep": 8 * 225, "ysweep": 8 * 125}
 # per kernel segment (lns_ctx3d_profile): algorithmic bytes and flops per
 # grid point of one launch, FP64
 #   rhs      grad1 + rhs + resid: v, vold, dv/dxi 240 B + operators 984 B + r 80 B
+#            (about 510 FMA: operator products 200, derivatives 240, viscous
+#            and 3D terms 50, rbe and residual 20)
 #   x_scale  D^-1 400 B + r read and write 160 B            (25 complex FMA)
 #   x_fwd    F1, F2 800 B + s read 80 B + yh write 80 B     (50 complex FMA)
 #   x_fill   K 800 B + E 800 B + yh read, write 160 B       (100 complex FMA)
@@ -71,8 +73,8 @@ PHASE_FLOPS = {"xsweep": 8 * 225, "ysweep": 8 * 125}
 #   update   v read, write 160 B + r 80 B
 KERNEL_BYTES = {"rhs": 1304, "x_scale": 560, "x_fwd": 960, "x_fill": 1760, "x_bwd": 960, "y_scale": 560,
                 "y_fwd": 960, "y_bwd": 960, "update": 240}
-KERNEL_FLOPS = {"x_scale": 200, "x_fwd": 400, "x_fill": 800, "x_bwd": 400, "y_scale": 200, "y_fwd": 400,
-                "y_bwd": 400}
+KERNEL_FLOPS = {"rhs": 1020, "x_scale": 200, "x_fwd": 400, "x_fill": 800, "x_bwd": 400, "y_scale": 200,
+                "y_fwd": 400, "y_bwd": 400}
 KERNEL_NAMES = {"x_fwd": "chain_fwd_kernel<cd, periodic> (xi forward recurrence)",
                 "x_bwd": "chain_bwd_kernel<cd, periodic> (xi backward recurrence)",
                 "rhs": "grad1_kernel + rhs_kernel + resid_kernel"}
@@ -82,6 +84,13 @@ KERNEL_NAMES = {"x_fwd": "chain_fwd_kernel<cd, periodic> (xi forward recurrence)
 KERNEL_TRAFFIC = {"x_fwd": 129.294080e6 + 5.967104e6, "x_bwd": 129.434624e6 + 5.784832e6,
                   "y_bwd": 130.674432e6 + 2.793728e6}
 KERNELS_PER_STEP = 14  # bc (predictor), grad1, rhs, resid, xi sweep (5), eta sweep (3), add, bc
+# whole-step model of the linearised step with stored factors, per grid point
+# and step: RHS 1224 B (v, vold 160 B, frozen operators 984 B, r 80 B), xi
+# sweep 2160 B (factors 2000 B, r read and write 160 B), eta sweep 2240 B
+# (factors 2000 B, r read 80 B, v read and write 160 B); about 1 kflop for
+# the RHS and 1 kflop for each directional solve.  The periodic fill of the
+# xi lines (1600 B and 800 flops more per point) is outside this model.
+STEP_BYTES, STEP_FLOPS = 5624, 3000
 
 # ---- secondary: the isolated batched solve
 N_ROWS, N_LINES = 256, 512
@@ -352,6 +361,9 @@ def config3(world):
     return {"workload": "impdrv3d-shear-layer-512x256-beta0.2-omega0.05-niter1", "nx": NX, "ny": NY,
             "beta": 0.2, "omega": 0.05, "cfl": CFL3, "loctime": 1, "niter": 1,
             "parallelism": "replicas" if world > 1 else "single",
+            "grid": "x uniform on [0, 5.5] (periodic); y = 10 sinh(3 (2 eta - 1)) / sinh(3), metrics exact "
+                    "for the mapping",
+            "timed": "K steps after warm-up from the seeded disturbance (the run to 1e-10 is the converge leg)",
             "l2": "working set larger than L2 (operators 131 MB + two factored LHS 262 MB each per step)"}
 
 
@@ -398,9 +410,11 @@ def percentile(xs, q):
     return xs[min(len(xs) - 1, int(round(q * (len(xs) - 1))))]
 
 
-def run_isolated(torch, dev, L, sp, stream, rank, world, W, K):
+def run_isolated(torch, dev, L, sp, stream, rank, world, W, K, with_cpu=False):
     """The isolated batched solve (cpenta2bc code 2, FP64) and its mixed
-    form; each step solves its own pristine batch resident in HBM."""
+    form; each step solves its own pristine batch resident in HBM.  With
+    with_cpu, the reference's own cpenta2bc (translated) on the host cores
+    beside it."""
     batches = [make_batch(torch, dev, 1000 * rank + s) for s in range(W + K)]
     torch.cuda.synchronize()
 
@@ -430,7 +444,8 @@ def run_isolated(torch, dev, L, sp, stream, rank, world, W, K):
             "latency_ms": {"p50": percentile(per_step, 0.5), "p99": percentile(per_step, 0.99)},
             "bytes_per_pt": BYTES_PER_PT, "flops_per_pt": FLOPS_PER_PT,
             "hbm_gbs": BYTES_PER_PT * PTS / (ms / 1e3) / 1e9,
-            "fp64_tflops": FLOPS_PER_PT * PTS / (ms / 1e3) / 1e12, "mixed": mixed}
+            "fp64_tflops": FLOPS_PER_PT * PTS / (ms / 1e3) / 1e12, "mixed": mixed,
+            "cpu_baseline": time_reference_cpu() if with_cpu else None}
 
 
 def run_impdrv2d(torch, dev, steps, with_cpu):
@@ -450,10 +465,25 @@ def run_impdrv2d(torch, dev, steps, with_cpu):
     stream = torch.cuda.current_stream()
     total, per = time_steps(torch, drv, v, steps, stream)
     pts = 128 * 128
-    out = {"workload": "impdrv-oseen-vortex-128x128-Ma0.5-Re1000-cfl1", "value": pts * steps / (total / 1e3),
+    out = {"workload": "impdrv-oseen-vortex-128x128-Ma0.5-Re1000-cfl1",
+           "grid": "[-10, 10]^2, x uniform (periodic), y = 10 tanh(2 (2 eta - 1)) / tanh(2); metrics by the "
+                   "reference pre-processor's differencing (lns3d_gb300.pre)",
+           "value": pts * steps / (total / 1e3),
            "unit": "grid-pt-steps/s", "ms_per_step": total / steps, "dtype": "f64",
            "latency_ms": {"p50": percentile(per, 0.5), "p99": percentile(per, 0.99)},
            "launches_per_step": 12, "cpu_baseline": None}
+    # the nonlinear 2D step's model per grid point and step: 1856 B (v, vold,
+    # metrics, the operator hand-off between phases, r) and 5.5 kflop (RHS
+    # and operators 2 kflop, two factor-and-solve passes of about 850 FMA
+    # per row each), against the measured copy bandwidth and the live FP64
+    # rate
+    rate = out["value"]
+    hbm_peak, peak_kind = peaks()
+    fp64_peak = fp64_probe()
+    out["roofline"] = {"bound": "fp64", "bytes_per_pt": 1856, "flops_per_pt": 5500,
+                       "hbm_gbs": rate * 1856 / 1e9, "hbm_frac": rate * 1856 / 1e9 / hbm_peak,
+                       "fp64_tflops": rate * 5500 / 1e12, "fp64_frac": rate * 5500 / 1e12 / fp64_peak,
+                       "peak_source": peak_kind + " HBM copy; live FP64 DFMA stream"}
     if with_cpu:
         from oracle.impdrv2d import Oracle2D
         import oracle
@@ -780,7 +810,8 @@ def main():
     iso = None
     if not args.no_isolated:
         del d32
-        iso = run_isolated(torch, dev, L, sp, stream, rank, world, 3, max(3, min(K, 10)))
+        iso = run_isolated(torch, dev, L, sp, stream, rank, world, 3, max(3, min(K, 10)),
+                           rank == 0 and not args.no_cpu_baseline)
 
     legb = None
     if not args.no_batch:
@@ -818,6 +849,12 @@ def main():
             "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                               "frac": fp64_achieved / fp64_peak, "flops_per_pt": KERNEL_FLOPS.get(dom, 0),
                               "peak_source": "measured live: DFMA stream on every SM (lns_probe_fp64_tflops)"},
+            "roofline_step": {"bytes_per_pt": STEP_BYTES, "flops_per_pt": STEP_FLOPS,
+                              "hbm_gbs": value * STEP_BYTES / 1e9, "hbm_frac": value * STEP_BYTES / 1e9 / hbm_peak,
+                              "fp64_tflops": value * STEP_FLOPS / 1e12,
+                              "fp64_frac": value * STEP_FLOPS / 1e12 / fp64_peak,
+                              "model": "whole step with stored factors (RHS 1224 B, xi sweep 2160 B, eta sweep "
+                                       "2240 B per pt-step; 3 kflop), at the device-resident step rate"},
             "cpu_baseline": cpu,
             "isolated_solve": iso,
             "impdrv2d": leg2d,

@@ -103,12 +103,29 @@ def _oseen_f(x):
     return out
 
 
+def vortex_grid(nx=128, ny=128, L=10.0, stretch=2.0):
+    """The grid of the two-dimensional case: [-L, L]^2, x uniform, y =
+    L tanh(s (2 eta - 1)) / tanh(s) on a uniform eta in [0, 1]."""
+    xi = np.linspace(0.0, 1.0, nx)
+    eta = np.linspace(0.0, 1.0, ny)
+    y1 = L * np.tanh(stretch * (2.0 * eta - 1.0)) / np.tanh(stretch)
+    x = np.asfortranarray(np.repeat((-L + 2.0 * L * xi)[:, None], ny, axis=1))
+    y = np.asfortranarray(np.repeat(y1[None, :], nx, axis=0))
+    return x, y
+
+
 def vortex2d(nx=128, ny=128, L=10.0, stretch=2.0, Ma=0.5, Re=1000.0, Pr=0.72, circulation=1.0, seed=0,
              jitter=0.1):
     """The nonlinear two-dimensional case: an Oseen vortex in a uniform stream.
 
-    * grid: [-L, L]^2, x uniform and periodic (point nx repeats point 1), y
-      = L tanh(s (2 eta - 1)) / tanh(s); metrics exact for the mapping;
+    * grid (vortex_grid): [-L, L]^2, x uniform and periodic (point nx is the
+      periodic image of point 1), y = L tanh(s (2 eta - 1)) / tanh(s);
+    * metrics as the reference's pre-processor forms them from the grid
+      (lns3d_gb300.pre, pinned to pre/src_ij/pre.f90), differenced without
+      its periodic option: that option wraps the coordinates themselves,
+      which suits grids periodic in both coordinates (O-grids), while x here
+      jumps by the period at the seam; the top boundary normal from the
+      metrics as src/gengrid.f90:139-143 forms it;
     * state: uniform flow rho = u = T = 1 plus an Oseen vortex of core radius 1
       (alpha = 1.2564312086261697, util/mkvortex.f90:36) with the given
       circulation, its centre jittered uniformly by +-jitter from the origin
@@ -120,25 +137,10 @@ def vortex2d(nx=128, ny=128, L=10.0, stretch=2.0, Ma=0.5, Re=1000.0, Pr=0.72, ci
       (wall 0, wallt 1), Riemann far field at j = ny (top 0), global time
       step at CFL 1.
     """
-    xi = np.linspace(0.0, 1.0, nx)
-    eta = np.linspace(0.0, 1.0, ny)
-    s = stretch
-    z = s * (2.0 * eta - 1.0)
-    y1 = L * np.tanh(z) / np.tanh(s)
-    dy = L * 2.0 * s / np.cosh(z) ** 2 / np.tanh(s)                      # dy/deta
-    d2y = -L * 8.0 * s * s * np.tanh(z) / np.cosh(z) ** 2 / np.tanh(s)  # d2y/deta2
-    x = np.asfortranarray(np.repeat((-L + 2.0 * L * xi)[:, None], ny, axis=1))
-    y = np.asfortranarray(np.repeat(y1[None, :], nx, axis=0))
-    ones = np.ones((nx, ny))
-    zeros = np.zeros((nx, ny))
-    metrics = {
-        "m1": ones / (2.0 * L), "m2": zeros.copy(), "n1": zeros.copy(),
-        "n2": np.repeat((1.0 / dy)[None, :], nx, axis=0),
-        "m11": zeros.copy(), "m12": zeros.copy(), "m22": zeros.copy(),
-        "n11": zeros.copy(), "n12": zeros.copy(),
-        "n22": np.repeat((-d2y / dy ** 3)[None, :], nx, axis=0),
-    }
-    metrics = {k: np.asfortranarray(v) for k, v in metrics.items()}
+    from lns3d_gb300 import pre
+
+    x, y = vortex_grid(nx, ny, L, stretch)
+    metrics = pre.metrics(x, y, xper=False)
     rng = np.random.default_rng(seed)
     x0, y0 = rng.uniform(-jitter, jitter, 2)
     alpha = 1.2564312086261697
@@ -164,8 +166,10 @@ def vortex2d(nx=128, ny=128, L=10.0, stretch=2.0, Ma=0.5, Re=1000.0, Pr=0.72, ci
     params = dict(nx=nx, ny=ny, dxi=1.0 / (nx - 1), deta=1.0 / (ny - 1), Ma=Ma, Re=Re, Pr=Pr, gamma=GAMMA,
                   gamma1=GAMMA1, omega=0.0, kz=0.0, alfa=1.0, xper=1, yper=0, navier=1, wall=0, wallt=1,
                   top=0, optx=-1, opty=-1)
-    bnt = np.zeros((nx, 2), order="F")
-    bnt[:, 1] = 1.0        # (n1, n2) / |n| at j = ny (src/gengrid.f90:141-142)
+    n1, n2 = metrics["n1"][:, -1], metrics["n2"][:, -1]
+    bnt = np.zeros((nx, 2), order="F")     # (n1, n2) / |n| at j = ny (src/gengrid.f90:139-143)
+    bnt[:, 0] = n1 / np.sqrt(n1 * n1 + n2 * n2)
+    bnt[:, 1] = n2 / np.sqrt(n1 * n1 + n2 * n2)
     return dict(params=params, x=x, y=y, metrics=metrics, v=np.asfortranarray(v), pot=pot, bnt=bnt, theta=0.0)
 
 

@@ -2182,6 +2182,10 @@ int admit(lns_server3d* s) {
       if (c) lns_ctx3d_destroy(c);
       r->state = LNS_REQ_FAILED;
       r->t_done = now_s();
+      // a failed request returns nothing: drop its host copies now
+      std::vector<double>().swap(r->metrics);
+      std::vector<double>().swap(r->vm);
+      std::vector<double>().swap(r->v);
       continue;
     }
     r->ctx = c;

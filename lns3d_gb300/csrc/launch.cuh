@@ -92,14 +92,19 @@ template <typename T>
 int launch_bc(void* mat, void* rhs, int n, int nsys, long long row_stride, long long line_stride, int code,
               cudaStream_t st, int* status) {
   if (nsys == 0) return LNS_OK;
+  // With CTA teams (few lines) the right-hand side is eliminated in the
+  // factoring pass (code 2), which measured faster there than a separate
+  // solve kernel, with identical results; warp teams factor, then solve.
+  const bool cta_team = bc_team<T>(nsys) == 128;
   if (code != 1) {
-    lns::PentaArgs a{mat, rhs, n, nsys, row_stride, line_stride, 0, status};
-    if (bc_team<T>(nsys) == 128) launch_bc_team<T, 128>(a, st);
+    lns::PentaArgs a{mat, rhs, n, nsys, row_stride, line_stride, cta_team && code == 2 ? 2 : 0, status};
+    if (cta_team) launch_bc_team<T, 128>(a, st);
     else launch_bc_team<T, 32>(a, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return lns_cuda_fail(e, "penta_bc_kernel launch");
   }
-  if (code != 0) return launch_solve<T, false>(mat, rhs, nullptr, nullptr, n, nsys, row_stride, line_stride, st);
+  if (code == 1 || (code == 2 && !cta_team))
+    return launch_solve<T, false>(mat, rhs, nullptr, nullptr, n, nsys, row_stride, line_stride, st);
   return LNS_OK;
 }
 

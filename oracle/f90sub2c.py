@@ -2228,6 +2228,19 @@ class Gen:
         if fmt is not None or unit is None or unit.k == "star" or (unit.k == "num" and unit.a in ("6", "5")):
             # formatted or list-directed: numeric scalar items go to a hook, the rest is dropped
             if read:
+                # one character item under (aW) or (a): the record's first W
+                # characters (all of it for (a)), blank-padded
+                m = re.fullmatch(r"\(\s*a(\d*)\s*\)", fmt.a.strip().lower()) if fmt is not None and fmt.k == "str" \
+                    else None
+                if m and len(st.items) == 1 and st.items[0][0] == "e" and st.items[0][1].k == "name" \
+                        and self.type_of(c, st.items[0][1]) == "char":
+                    e = st.items[0][1]
+                    s_, _ = self.lookup(c.u, e.a)
+                    ucode = "5" if unit is None or unit.k == "star" else self.conv(*self.ex(c, unit), "int")
+                    code, _ = self.ex(c, e)
+                    lines.append(ind + "if (fio_aread(%s, %s, %d, %s) != 0) f_ioerror_();" % (
+                        ucode, code, s_.charlen or 1, m.group(1) or "-1"))
+                    return
                 lines.append(ind + "f_unsupported_(\"formatted read\");")
                 return
             ucode = "-1" if unit is None or unit.k == "star" else self.conv(*self.ex(c, unit), "int")
@@ -2296,7 +2309,28 @@ class Gen:
             lines.append(ind + "%sitem_es(%s.p, %d, %d * fsize(&%s));" % (fn, d, es, per, d))
             return
         if self.rank_of(c, e) > 0:
-            raise GenError("array expression in an I/O list")
+            # an array section or expression: its elements in array element
+            # order (the first index fastest)
+            sh = self.section_shape(c, e)
+            if sh is None:
+                raise GenError("array expression in an I/O list")
+            lv = [c.newtmp("i") for _ in sh]
+            ext = [c.newtmp("n") for _ in sh]
+            lines.append(ind + "{")
+            for j in range(len(sh)):
+                lines.append(ind + "  long %s = %s;" % (ext[j], sh[j]))
+            loops, close = self.loop_nest(lv, ext)
+            lines.extend(ind + "  " + x for x in loops)
+            code, tt = self.ex(c, e, lv)
+            if fn == "fio_r":
+                lines.append(ind + "  fio_ritem_es(&%s, %d, %d);" % (code, es, per))
+            else:
+                tmp = c.newtmp("w")
+                lines.append(ind + "  { %s %s = %s; fio_witem_es(&%s, %d, %d); }" % (
+                    CT[t], tmp, self.conv(code, tt, t), tmp, es, per))
+            lines.extend(ind + "  " + x for x in close)
+            lines.append(ind + "}")
+            return
         if fn == "fio_r":
             code, _ = self.ex(c, e)
             lines.append(ind + "fio_ritem_es(&%s, %d, %d);" % (code, es, per))
@@ -2613,6 +2647,7 @@ void fio_wbegin(int unit); void fio_witem_es(const void* p, unsigned long es, un
 void fio_fbegin(int unit); void fio_fnum(double v); void fio_fend(void);
 void fio_lbegin(int unit); void fio_lint(int* p); void fio_llog(int* p); void fio_lreal(double* p);
 void fio_lreal4(float* p); void fio_lcx(cx* p); void fio_lchar(char* p, int len); int fio_lend(void);
+int fio_aread(int unit, char* p, int len, int width);
 int fio_exists(const char* file);
 void f_stop_(void);
 void f_ioerror_(void);
@@ -2667,6 +2702,8 @@ def main():
         f.write(RT_HEADER)
         f.write("\n/* translated procedures */\n")
         f.write("\n".join(protos) + "\n")
+        # the harness leaves out its stand-ins of procedures translated here
+        f.write("".join("#define REF_HAVE_%s 1\n" % nm for nm in sorted(prog.procs)))
         f.write("\n/* procedures the harness provides */\n")
         f.write("\n".join(ext_protos) + "\n")
         f.write("extern const ref_sym ref_scalars[];\nextern const ref_sym ref_arrays[];\nvoid ref_init(void);\n")

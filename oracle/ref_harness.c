@@ -23,6 +23,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdint.h>
+#include <unistd.h>
 #ifndef REF_HDR
 #define REF_HDR "_ref/ref_step.h"
 #endif
@@ -200,6 +201,7 @@ typedef struct {
   unsigned char* buf; /* current record */
   size_t len, pos, cap;
   int bad;
+  int trunc; /* opened on an existing file: the first write ends the file there */
 } unit_t;
 static unit_t units[128];
 
@@ -219,11 +221,22 @@ int fio_open(int unit, const char* file, const char* form, const char* status) {
   int formatted = !(fm[0] == 'u' || fm[0] == 'U');
   const char* stt = fstr_trim(status);
   FILE* f;
-  if (stt[0] == 'o' || stt[0] == 'O') f = fopen(path, formatted ? "r" : "rb");
-  else f = fopen(path, formatted ? "w" : "wb");
+  int trunc = 0;
+  if (stt[0] == 'o' || stt[0] == 'O') {
+    f = fopen(path, formatted ? "r" : "rb");
+  } else if (stt[0] == 'n' || stt[0] == 'N' || stt[0] == 'r' || stt[0] == 'R' || stt[0] == 's' || stt[0] == 'S') {
+    f = fopen(path, formatted ? "w+" : "w+b");
+  } else {
+    /* unknown: an existing file is opened at its start for reading, and a
+     * sequential write there ends the file after the record written */
+    f = fopen(path, formatted ? "r+" : "r+b");
+    if (f) trunc = 1;
+    else f = fopen(path, formatted ? "w+" : "w+b");
+  }
   if (!f) return 1;
   units[unit].f = f;
   units[unit].formatted = formatted;
+  units[unit].trunc = trunc;
   return 0;
 }
 
@@ -337,6 +350,11 @@ void fio_witem(const void* p, unsigned long bytes) { fio_witem_es(p, bytes, 1); 
 int fio_wend(void) {
   if (wunit < 0 || wunit >= 128 || !units[wunit].f) return 1;
   FILE* f = units[wunit].f;
+  if (units[wunit].trunc) {
+    fflush(f);
+    if (ftruncate(fileno(f), ftell(f)) != 0) return 1;
+    units[wunit].trunc = 0;
+  }
   wr_marker(f, (uint32_t)wlen);
   fwrite(wbuf, 1, wlen, f);
   wr_marker(f, (uint32_t)wlen);
@@ -474,6 +492,22 @@ void fio_lchar(char* p, int len) {
 
 int fio_lend(void) { return lbad; }
 
+/* formatted read of one character item under (aW): the record's first W
+ * characters (the whole record for W < 0), blank-padded to len */
+int fio_aread(int unit, char* p, int len, int width) {
+  lunit = unit;
+  if (!next_record()) return 1;
+  char t[4096];
+  size_t k = 0;
+  while (lline[k] && lline[k] != '\r' && lline[k] != '\n' && (width < 0 || (int)k < width) && k < sizeof t - 1) {
+    t[k] = lline[k];
+    ++k;
+  }
+  t[k] = 0;
+  fstr_assign(p, len, t);
+  return 0;
+}
+
 int fio_exists(const char* file) {
   char path[2048];
   path_of(path, sizeof path, file);
@@ -488,7 +522,9 @@ int f_iargc(void) { return 0; }
 void f_getarg(int* i, char* arg) { (void)i; fstr_assign(arg, 1, " "); }
 
 /* diagnostics the benchmark decks never turn on */
+#ifndef REF_HAVE_wdata
 void f_wdata() { trap(4, "wdata is not translated"); }
+#endif
 void f_fstat3d() { trap(4, "fstat3d is not translated"); }
 void f_fstat2d() { trap(4, "fstat2d is not translated"); }
 void f_cfilter() { trap(4, "cfilter stops the reference on entry"); }

@@ -30,6 +30,10 @@ LIB = os.path.join(HERE, "_ref", "libref_step.so")
 # row n-3 index fault (src/cpenta1bc.f:675, src/cpenta2bc.f:676)
 LIB_ASIS = os.path.join(HERE, "_ref", "libref_step_asis.so")
 
+# the reference's metric pre-processor (pre/src_ij/pre.f90 and its grad,
+# grad2, stencil, wdata), translated the same way
+LIB_PRE = os.path.join(HERE, "_ref", "libref_pre.so")
+
 TYPES = {0: ctypes.c_int, 1: ctypes.c_double, 4: ctypes.c_float}
 
 
@@ -52,15 +56,17 @@ class RefError(RuntimeError):
 
 
 class RefProgram:
-    def __init__(self, asis=False):
+    def __init__(self, asis=False, lib=None):
         """asis: the reference exactly as written, without the correction of
-        the complex boundary solvers' row n-3 index fault."""
-        if not available(asis):
-            raise RefError("oracle/_ref/libref_step%s.so is not built (the reference sources are needed to "
-                           "translate it)" % ("_asis" if asis else ""))
+        the complex boundary solvers' row n-3 index fault.  lib: another
+        translated program (e.g. LIB_PRE) instead of the step program."""
+        src = lib or (LIB_ASIS if asis else LIB)
+        if not os.path.exists(src):
+            raise RefError("%s is not built (the reference sources are needed to translate it)"
+                           % os.path.relpath(src, os.path.dirname(HERE)))
         self._tmp = tempfile.mkdtemp(prefix="refstep_")
-        path = os.path.join(self._tmp, "libref_step.so")
-        shutil.copy(LIB_ASIS if asis else LIB, path)   # a private copy: its own module state
+        path = os.path.join(self._tmp, "libref.so")
+        shutil.copy(src, path)   # a private copy: its own module state
         self.L = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
         L = self.L
         L.ref_call.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
@@ -211,14 +217,14 @@ class RefProgram:
 
     # ---- the program -------------------------------------------------------
 
-    def run(self, rundir, deck, swap=False):
+    def run(self, rundir, deck, swap=False, program="lns3d"):
         """Run the reference program as ``lns3d < deck`` in rundir."""
         self.L.ref_set_dir(os.path.abspath(rundir).encode())
         self.L.ref_set_stdin(deck.encode())
         self.L.ref_set_swap(1 if swap else 0)
-        p = self.L.ref_proc_find(b"lns3d").contents
+        p = self.L.ref_proc_find(program.encode()).contents
         st = self.L.ref_call(p.fn, 0, (ctypes.c_void_p * 1)())
         msg = self.L.ref_last_message().decode()
         if st not in (0, 2):        # 2: the program's own STOP
-            raise RefError("lns3d: " + msg)
+            raise RefError(program + ": " + msg)
         return msg
