@@ -51,15 +51,14 @@ CFL3 = 20.0
 # algorithmic HBM bytes per grid point of each phase (FP64):
 #   RHS     v, vold 160 B + operators 984 B (Ah Bh Dh Dhi 100 doubles, V 18,
 #           the 4 used 3D terms, dtl) + r write 80 B            = 1224 B
-#   xi sweep (periodic) factors 2000 B + fill per, per2 1600 B + r read and
-#           write 160 B                                           = 3760 B
+#   xi sweep (periodic) factors 2000 B + border columns W 800 B + r read
+#           and write 160 B                                       = 2960 B
 #   eta sweep factors 2000 B + r read and write 160 B            = 2160 B
 #   update  v read and write 160 B + r read 80 B                 =  240 B
-PHASE_BYTES = {"rhs": 1224, "xsweep": 3760, "ysweep": 2160, "update": 240}
-# complex multiply-adds per point of a sweep (8 flops each): lower blocks 50,
-# in-block lower 10, upper blocks 50, in-block upper 10 and 5 divisions
-# (counted 5), periodic fill columns and rows +100
-PHASE_FLOPS = {"xsweep": 8 * 225, "ysweep": 8 * 125}
+PHASE_BYTES = {"rhs": 1224, "xsweep": 2960, "ysweep": 2160, "update": 240}
+# complex multiply-adds per point of a sweep (8 flops each): D^-1 25, lower
+# blocks 50, upper blocks 50; the periodic border correction +50
+PHASE_FLOPS = {"xsweep": 8 * 175, "ysweep": 8 * 125}
 # per kernel segment (lns_ctx3d_profile): algorithmic bytes and flops per
 # grid point of one launch, FP64
 #   rhs      grad1 + rhs + resid: v, vold, dv/dxi 240 B + operators 984 B + r 80 B
@@ -67,13 +66,14 @@ PHASE_FLOPS = {"xsweep": 8 * 225, "ysweep": 8 * 125}
 #            and 3D terms 50, rbe and residual 20)
 #   x_scale  D^-1 400 B + r read and write 160 B            (25 complex FMA)
 #   x_fwd    F1, F2 800 B + s read 80 B + yh write 80 B     (50 complex FMA)
-#   x_fill   K 800 B + E 800 B + yh read, write 160 B       (100 complex FMA)
 #   x_bwd    B1, B2 800 B + c read 80 B + x write 80 B      (50 complex FMA)
-#   y_*      as x without the fill
+#   x_fill   the periodic border: W 800 B + x read, write 160 B (50 complex
+#            FMA), and per line S^-1, A21 (the border unknowns)
+#   y_*      as x without the border
 #   update   v read, write 160 B + r 80 B
-KERNEL_BYTES = {"rhs": 1304, "x_scale": 560, "x_fwd": 960, "x_fill": 1760, "x_bwd": 960, "y_scale": 560,
+KERNEL_BYTES = {"rhs": 1304, "x_scale": 560, "x_fwd": 960, "x_fill": 960, "x_bwd": 960, "y_scale": 560,
                 "y_fwd": 960, "y_bwd": 960, "update": 240}
-KERNEL_FLOPS = {"rhs": 1020, "x_scale": 200, "x_fwd": 400, "x_fill": 800, "x_bwd": 400, "y_scale": 200,
+KERNEL_FLOPS = {"rhs": 1020, "x_scale": 200, "x_fwd": 400, "x_fill": 400, "x_bwd": 400, "y_scale": 200,
                 "y_fwd": 400, "y_bwd": 400}
 KERNEL_NAMES = {"x_fwd": "chain_fwd_kernel<cd, periodic> (xi forward recurrence)",
                 "x_bwd": "chain_bwd_kernel<cd, periodic> (xi backward recurrence)",

@@ -428,9 +428,11 @@ int lns_lhs3d_dev(lns_ctx3d* ctx, int32_t dir, double* mat, void* stream);
  * every later corrector record CUDA events on its stream (and resets the
  * record); lns_ctx3d_profile_read waits for them and returns the summed
  * milliseconds of LNS_PROFILE_SEGMENTS segments in ms[]: 0 RHS, 1 xi
- * scaling, 2 xi forward recurrence, 3 xi fill (tail and correction), 4 xi
- * backward recurrence, 5 eta scaling, 6 eta forward, 7 eta backward,
- * 8 update; and the number of correctors in *ncorr.  Clears the record. */
+ * scaling, 2 xi forward recurrence, 3 xi backward recurrence, 4 xi border
+ * (the periodic lines' border unknowns and correction; empty for a
+ * non-periodic xi), 5 eta scaling, 6 eta forward, 7 eta backward (with a
+ * periodic eta's border), 8 update; and the number of correctors in
+ * *ncorr.  Clears the record. */
 #define LNS_PROFILE_SEGMENTS 9
 int lns_ctx3d_profile(lns_ctx3d* ctx, int32_t on);
 int lns_ctx3d_profile_read(lns_ctx3d* ctx, double* ms, int32_t* ncorr);

@@ -175,7 +175,7 @@ class ImpDrv3D:
         """Start (or stop) recording per-phase CUDA events of every corrector."""
         check(lib().lns_ctx3d_profile(self._ctx, 1 if on else 0), "lns_ctx3d_profile")
 
-    SEGMENTS = ("rhs", "x_scale", "x_fwd", "x_fill", "x_bwd", "y_scale", "y_fwd", "y_bwd", "update")
+    SEGMENTS = ("rhs", "x_scale", "x_fwd", "x_bwd", "x_fill", "y_scale", "y_fwd", "y_bwd", "update")
 
     def profile_read(self):
         """Summed milliseconds per kernel segment (SEGMENTS) and per phase

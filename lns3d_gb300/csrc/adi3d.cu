@@ -818,12 +818,12 @@ struct lns_ctx3d {
   cf* r32 = nullptr;
   // FP64 factors in the reference storage (both modes), and the same
   // factors in the scaled block form of penta_chain.cuh in the precision of
-  // the sweeps (fillE/fillK alias perx/per2x in the FP64 mode)
+  // the sweeps; periodic lines add W (fillE, aliasing perx in the FP64 mode)
+  // and their border data (bordx: S^-1, A21)
   void *matx = nullptr, *maty = nullptr, *perx = nullptr, *per2x = nullptr;
-  void *chnx = nullptr, *chny = nullptr, *fillE = nullptr, *fillK = nullptr;
-  // a periodic eta direction (yper): its fill in the reference storage and
-  // in the internal form (aliases in the FP64 mode)
-  void *pery = nullptr, *per2y = nullptr, *fillEy = nullptr, *fillKy = nullptr;
+  void *chnx = nullptr, *chny = nullptr, *fillE = nullptr, *bordx = nullptr;
+  // a periodic eta direction (yper): the same for the eta lines
+  void *pery = nullptr, *per2y = nullptr, *fillEy = nullptr, *bordy = nullptr;
   double* part = nullptr;  // block partials (residual, CFL)
   int nparts = 0;
   double* dscal = nullptr;  // [0] cfl, [1..] residual of the inspection call
@@ -980,36 +980,37 @@ int launch_lhs(lns_ctx3d* c, int dir, T* mat, cudaStream_t st) {
 // periodic lines with yper: n = ny - 1 unknowns).
 lns::chain::Args xargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
-  if (!g.xper) return lns::chain::Args{c->matx, c->chnx, nullptr, nullptr, nullptr, nullptr, rhs, g.nx, g.ny, 1, g.nx};
-  return lns::chain::Args{c->matx, c->chnx, c->perx, c->per2x, c->fillE, c->fillK, rhs, g.nx - 1, g.ny, 1, g.nx};
+  if (!g.xper) return lns::chain::Args{c->matx, c->chnx, nullptr, nullptr, nullptr, rhs, g.nx, g.ny, 1, g.nx};
+  return lns::chain::Args{c->matx, c->chnx, c->perx, c->per2x, c->fillE, rhs, g.nx - 1, g.ny, 1, g.nx,
+                          c->bordx};
 }
 lns::chain::Args yargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
-  if (g.yper) return lns::chain::Args{c->maty, c->chny, c->pery, c->per2y, c->fillEy, c->fillKy, rhs, g.ny - 1, g.nx,
-                                      g.nx, 1};
-  return lns::chain::Args{c->maty, c->chny, nullptr, nullptr, nullptr, nullptr, rhs, g.ny, g.nx, g.nx, 1};
+  if (g.yper) return lns::chain::Args{c->maty, c->chny, c->pery, c->per2y, c->fillEy, rhs, g.ny - 1, g.nx,
+                                      g.nx, 1, c->bordy};
+  return lns::chain::Args{c->maty, c->chny, nullptr, nullptr, nullptr, rhs, g.ny, g.nx, g.nx, 1};
 }
 
-// A periodic sweep (xi, or eta with yper): s = D^-1 r, forward recurrence,
-// rows n-1 and n with the periodic fill, the fill correction, backward
-// recurrence.
-// xi_marks: the profiling marks of the xi sweep (after the scaling, the
-// forward recurrence and the fill); an eta sweep marks as a non-periodic one
-// (after the scaling and the forward recurrence with its fill).
+// A periodic sweep (xi, or eta with yper), bordered: s = D^-1 r on rows
+// 1..n-2, the two recurrences (z = A11^-1 b1), the border unknowns x2 =
+// S^-1 (b2 - A21 z) and the correction x1 = z - W x2.
+// xi_marks: the profiling marks of the xi sweep (after the scaling and each
+// recurrence; the border and correction close the segment); an eta sweep
+// marks as a non-periodic one (after the scaling and the forward recurrence).
 template <typename T>
 int sweep_periodic(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaStream_t st) {
   namespace ch = lns::chain;
-  const long long pts = (long long)a.n * a.nsys, fill = (long long)(a.n - 3) * a.nsys;
+  const long long pts = (long long)a.n * a.nsys, fill = (long long)(a.n - 2) * a.nsys;
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
   ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
   int rc = mark(c, st);
   ch::chain_fwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
-  if (!rc && xi_marks) rc = mark(c, st);
-  ch::tail_kernel<T><<<a.nsys, 32 * ch::kTailWarps, 0, st>>>(a);
-  ch::fill_kernel<T><<<(unsigned)ch::fill_blocks(fill), 256, 0, st>>>(a);
   if (!rc) rc = mark(c, st);
   ch::chain_bwd_kernel<T, true><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
+  if (!rc && xi_marks) rc = mark(c, st);
+  ch::btail_kernel<T><<<(a.nsys + ch::kBTailLines - 1) / ch::kBTailLines, 32 * ch::kBTailLines, 0, st>>>(a);
+  ch::fill_kernel<T><<<(unsigned)ch::fill_blocks(fill), 256, 0, st>>>(a);
   if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "periodic sweep launch");
@@ -1017,8 +1018,8 @@ int sweep_periodic(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaS
 
 // A sweep of lines with boundary-closure rows: s = D^-1 r, forward and
 // backward recurrences.  xi_marks: the profiling marks of the xi sweep
-// (after the scaling, the forward recurrence and a third, empty fill
-// segment).
+// (after the scaling, the forward and the backward recurrence, leaving the
+// border segment of the periodic xi sweep empty).
 template <typename T>
 int sweep_bc(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaStream_t st) {
   namespace ch = lns::chain;
@@ -1029,8 +1030,8 @@ int sweep_bc(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaStream_
   int rc = mark(c, st);
   ch::chain_fwd_kernel<T, false><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
   if (!rc) rc = mark(c, st);
-  if (!rc && xi_marks) rc = mark(c, st);
   ch::chain_bwd_kernel<T, false><<<cta, ch::chain_threads<T>(), sm, st>>>(a);
+  if (!rc && xi_marks) rc = mark(c, st);
   if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "sweep launch");
@@ -1062,6 +1063,30 @@ int sweep_y(lns_ctx3d* c, T* r, cudaStream_t st) {
   return e == cudaSuccess ? LNS_OK : cuda3(e, "eta sweep launch");
 }
 
+// W, S^-1 and A21 of the periodic lines of a (their border blocks copied by
+// bcopy_kernel before the factorisation, their records prepared): ten
+// solves z = A11^-1 (column j of A12) through the recurrences, then the
+// Schur complement.  a.rhs is a sweep-sized scratch buffer.
+template <typename TC>
+int form_border(lns_ctx3d* c, const lns::chain::Args& a, cudaStream_t st) {
+  namespace ch = lns::chain;
+  const long long pts = (long long)a.n * a.nsys;
+  const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
+  const size_t sm = ch::chain_smem_bytes<TC>();
+  for (int j = 0; j < 10; ++j) {
+    cudaError_t e = cudaMemsetAsync(a.rhs, 0, sizeof(TC) * 5 * (size_t)c->np, st);
+    if (e != cudaSuccess) return cuda3(e, "cudaMemsetAsync border");
+    ch::brhs_kernel<TC><<<(unsigned)((a.nsys * 30LL + 255) / 256), 256, 0, st>>>(a, j);
+    ch::scale_kernel<TC><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
+    ch::chain_fwd_kernel<TC, true><<<cta, ch::chain_threads<TC>(), sm, st>>>(a);
+    ch::chain_bwd_kernel<TC, true><<<cta, ch::chain_threads<TC>(), sm, st>>>(a);
+    ch::bw_kernel<TC><<<(unsigned)((a.nsys * (a.n - 2) * 5LL + 255) / 256), 256, 0, st>>>(a, j);
+  }
+  ch::bschur_kernel<TC><<<(a.nsys + 63) / 64, 64, 0, st>>>(a, c->status);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda3(e, "border kernels launch");
+}
+
 // Forms both LHS and factors them in FP64 (code 0), checks the pivots, and
 // writes the scaled block form in the precision TC of the sweeps.
 template <typename TC>
@@ -1072,32 +1097,44 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   cd* rr = c->c1v;  // a right-hand-side argument; code 0 does not touch it
   cudaError_t e = cudaMemsetAsync(c->status, 0, sizeof(int), st);
   if (e != cudaSuccess) return cuda3(e, "cudaMemsetAsync");
-  int rc = launch_lhs<cd>(c, 1, mx, st);
-  if (!rc && g.xper) rc = lns::host::launch_p<cd>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status);
-  else if (!rc) rc = lns::host::launch_bc<cd>(mx, rr, g.nx, g.ny, 1, g.nx, 0, st, c->status);
-  if (!rc) rc = launch_lhs<cd>(c, 2, my, st);
-  if (!rc && g.yper) rc = lns::host::launch_p<cd>(my, rr, c->pery, c->per2y, g.ny, g.nx, g.nx, 1, 0, st, c->status);
-  else if (!rc) rc = lns::host::launch_bc<cd>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
-  if (rc) return rc;
   namespace ch = lns::chain;
   const ch::Args ax = xargs(c, nullptr), ay = yargs(c, nullptr);
+  // the periodic factorisation mode, read once for both directions: the
+  // reference's (its row n-5 fill placement) unless the exact LU is chosen
+  const int exact = g_periodic_exact.load() ? 1 : 0;
+  int rc = launch_lhs<cd>(c, 1, mx, st);
+  if (!rc && g.xper) {
+    ch::bcopy_kernel<<<(unsigned)((ax.nsys * 400LL + 255) / 256), 256, 0, st>>>(ax);
+    rc = lns::host::launch_p<cd>(mx, rr, c->perx, c->per2x, g.nx, g.ny, 1, g.nx, 0, st, c->status, exact);
+    if (!rc && !exact) ch::bquirk_kernel<<<(unsigned)((ax.nsys * 25LL + 255) / 256), 256, 0, st>>>(ax);
+  } else if (!rc) {
+    rc = lns::host::launch_bc<cd>(mx, rr, g.nx, g.ny, 1, g.nx, 0, st, c->status);
+  }
+  if (!rc) rc = launch_lhs<cd>(c, 2, my, st);
+  if (!rc && g.yper) {
+    ch::bcopy_kernel<<<(unsigned)((ay.nsys * 400LL + 255) / 256), 256, 0, st>>>(ay);
+    rc = lns::host::launch_p<cd>(my, rr, c->pery, c->per2y, g.ny, g.nx, g.nx, 1, 0, st, c->status, exact);
+    if (!rc && !exact) ch::bquirk_kernel<<<(unsigned)((ay.nsys * 25LL + 255) / 256), 256, 0, st>>>(ay);
+  } else if (!rc) {
+    rc = lns::host::launch_bc<cd>(my, rr, g.ny, g.nx, g.nx, 1, 0, st, c->status);
+  }
+  if (rc) return rc;
   const long long tx = (long long)ax.n * ax.nsys, ty = (long long)ay.n * ay.nsys;
   const unsigned bx = (unsigned)((tx + ch::kPrepWarps - 1) / ch::kPrepWarps);
   const unsigned by = (unsigned)((ty + ch::kPrepWarps - 1) / ch::kPrepWarps);
-  if (g.xper) {
-    ch::prep_kernel<cd, TC, true><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
-    ch::prep_fill_kernel<cd, TC><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
-  } else {
-    ch::prep_kernel<cd, TC, false><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
-  }
-  if (g.yper) {
-    ch::prep_kernel<cd, TC, true><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
-    ch::prep_fill_kernel<cd, TC><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
-  } else {
-    ch::prep_kernel<cd, TC, false><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
-  }
+  if (g.xper) ch::prep_kernel<cd, TC, true><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+  else ch::prep_kernel<cd, TC, false><<<bx, 32 * ch::kPrepWarps, 0, st>>>(ax);
+  if (g.yper) ch::prep_kernel<cd, TC, true><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
+  else ch::prep_kernel<cd, TC, false><<<by, 32 * ch::kPrepWarps, 0, st>>>(ay);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda3(e, "prep kernels launch");
+  // periodic lines: W = A11^-1 A12 column by column through the sweeps'
+  // own recurrences (on the sweep buffer, free before the first RHS), then
+  // S^-1 and A21
+  TC* scratch = reinterpret_cast<TC*>(std::is_same<TC, cf>::value ? (void*)c->r32 : (void*)c->r64);
+  if (!rc && g.xper) rc = form_border<TC>(c, xargs(c, scratch), st);
+  if (!rc && g.yper) rc = form_border<TC>(c, yargs(c, scratch), st);
+  if (rc) return rc;
   int status = 0;
   e = cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1284,23 +1321,17 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   }
   A(el * 125 * np, &c->chnx);
   A(el * 125 * np, &c->chny);
-  if (p->xper && mixed) {
-    A(el * 50 * np, &c->fillE);
-    A(el * 50 * np, &c->fillK);
-  } else if (p->xper) {
-    c->fillE = c->perx;
-    c->fillK = c->per2x;
+  if (p->xper) {
+    if (mixed) A(el * 50 * np, &c->fillE);
+    else c->fillE = c->perx;  // W replaces the reference fill after the factorisation
+    A(sizeof(cd) * lns::chain::kBordCd * p->ny, &c->bordx);
   }
   if (p->yper) {
     A(sizeof(cd) * 50 * np, &c->pery);
     A(sizeof(cd) * 50 * np, &c->per2y);
-    if (mixed) {
-      A(el * 50 * np, &c->fillEy);
-      A(el * 50 * np, &c->fillKy);
-    } else {
-      c->fillEy = c->pery;
-      c->fillKy = c->per2y;
-    }
+    if (mixed) A(el * 50 * np, &c->fillEy);
+    else c->fillEy = c->pery;
+    A(sizeof(cd) * lns::chain::kBordCd * p->nx, &c->bordy);
   }
   A(sizeof(double) * c->nparts, &q); c->part = (double*)q;
   A(sizeof(double) * 3, &q); c->dscal = (double*)q;  // cfl, scratch residual, running residual
@@ -1696,8 +1727,9 @@ int build_tables(lns_batch3d* b) {
     const long long nxp = (long long)(g.nx - 1) * g.ny, nyp = (long long)g.ny * g.nx;
     for (long long k = 0; k < lns::chain::scale_blocks(nxp); ++k) tsx.push_back(make_int2(p, (int)k));
     for (int k = 0; k < (g.ny + b->W - 1) / b->W; ++k) tfx.push_back(make_int2(p, k));
-    for (int k = 0; k < g.ny; ++k) ttx.push_back(make_int2(p, k));
-    for (long long k = 0; k < lns::chain::fill_blocks((long long)(g.nx - 1 - 3) * g.ny); ++k) tlx.push_back(make_int2(p, (int)k));
+    for (int k = 0; k < (g.ny + lns::chain::kBTailLines - 1) / lns::chain::kBTailLines; ++k)
+      ttx.push_back(make_int2(p, k));
+    for (long long k = 0; k < lns::chain::fill_blocks((long long)(g.nx - 1 - 2) * g.ny); ++k) tlx.push_back(make_int2(p, (int)k));
     for (long long k = 0; k < lns::chain::scale_blocks(nyp); ++k) tsy.push_back(make_int2(p, (int)k));
     for (int k = 0; k < (g.nx + b->W - 1) / b->W; ++k) tfy.push_back(make_int2(p, k));
   }
@@ -1733,9 +1765,9 @@ int enqueue_step(lns_batch3d* b, int niter) {
     a3::resid_batch_kernel<<<b->P, 256, 0, st>>>(b->d_args, b->d_active, b->d_hist, b->d_step, b->P);
     ch::scale_batch_kernel<T><<<b->n_sx, 256, 0, st>>>(b->d_ax, b->t_sx, b->d_active);
     ch::chain_fwd_batch_kernel<T, true, W><<<b->n_fx, ch::chain_threads<T>(W), sm, st>>>(b->d_ax, b->t_fx, b->d_active);
-    ch::tail_batch_kernel<T><<<b->n_tx, 32 * ch::kTailWarps, 0, st>>>(b->d_ax, b->t_tx, b->d_active);
-    ch::fill_batch_kernel<T><<<b->n_lx, 256, 0, st>>>(b->d_ax, b->t_lx, b->d_active);
     ch::chain_bwd_batch_kernel<T, true, W><<<b->n_fx, ch::chain_threads<T>(W), sm, st>>>(b->d_ax, b->t_fx, b->d_active);
+    ch::btail_batch_kernel<T><<<b->n_tx, 32 * ch::kBTailLines, 0, st>>>(b->d_ax, b->t_tx, b->d_active);
+    ch::fill_batch_kernel<T><<<b->n_lx, 256, 0, st>>>(b->d_ax, b->t_lx, b->d_active);
     ch::scale_batch_kernel<T><<<b->n_sy, 256, 0, st>>>(b->d_ay, b->t_sy, b->d_active);
     ch::chain_fwd_batch_kernel<T, false, W><<<b->n_fy, ch::chain_threads<T>(W), sm, st>>>(b->d_ay, b->t_fy, b->d_active);
     ch::chain_bwd_batch_kernel<T, false, W><<<b->n_fy, ch::chain_threads<T>(W), sm, st>>>(b->d_ay, b->t_fy, b->d_active);

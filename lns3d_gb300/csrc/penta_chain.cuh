@@ -25,12 +25,16 @@
 //     row 2           F1 B3 B1 B2          row n-1  F1 F2 B1 F3
 //     row n           F1 F2 F3 F4          periodic lines: F1 F2 B1 B2 on
 //                                          every row, absent blocks zero
-// Periodic fill, 50 entries per record (may overwrite the per / per2
-// records they come from):
-//   E(i)   E1 = U_ii^-1 per(1,i) (column n-1, rows <= n-4) at [0,25),
-//          E0 = U_ii^-1 per(2,i) (column n,   rows <= n-3) at [25,50)
-//   K(c)   K1 = -D_{n-1}^-1 per2(n-1,c) U_cc (c <= n-4) at [0,25),
-//          K0 = -D_n^-1 per2(n,c) U_cc       (c <= n-3) at [25,50)
+// Periodic lines are solved bordered: with the unknowns split into the band
+// rows 1..n-2 (A11, whose factors are the records of those rows) and the
+// border rows n-1, n, [A11 A12; A21 A22] [x1; x2] = [b1; b2] gives
+//   z = A11^-1 b1 (the two recurrences, border terms left out),
+//   x2 = S^-1 (b2 - A21 z), S = A22 - A21 W, W = A11^-1 A12,
+//   x1 = z - W x2,
+// where W (ten columns, 50 entries per record, in the fill array), S^-1 and
+// the six non-zero blocks of A21 are formed once, at factoring time.  A21
+// reaches only rows 1, 2, n-3, n-2 of z, so the border needs no sum over the
+// line.
 // The prep kernels read the factors in one precision (TM) and write the
 // internal form in the precision of the sweeps (TC), computing in FP64.
 #pragma once
@@ -46,13 +50,21 @@ struct Args {
   void* chn;         // internal records
   const void* per;   // periodic fill in the reference storage (prep only)
   const void* per2;
-  void* fillE;       // periodic fill E, K in the internal form (may alias per, per2)
-  void* fillK;
+  void* fillE;       // periodic lines: W, 50 entries per record (may alias per)
   void* rhs;
   int n;             // unknowns per line (periodic: np - 1)
   int nsys;
   long long row_stride, line_stride;
+  // periodic lines: kBordCd complex doubles per line (see kBordCd)
+  void* bord = nullptr;
 };
+
+// Border data of a periodic line: S^-1 (row k, column j at k + 10 j; k, j =
+// m + 5 b for component m of border row n-1+b), the six blocks of A21 (rows
+// n-1: columns n-3, n-2, 1; row n: columns n-2, 1, 2; entry (m, q) at
+// m + 5 q), and the sixteen border blocks of the unfactored LHS, kept from
+// before the factorisation until W and S are formed.
+constexpr int kBordSinv = 0, kBordA21 = 100, kBordRaw = 250, kBordCd = 650;
 
 __device__ __forceinline__ long long rec_of(const Args& a, int r, int iv) {
   return a.row_stride * (r - 1) + a.line_stride * iv;
@@ -102,8 +114,7 @@ __device__ __forceinline__ bool has_p(int i, int n, int d) {
   return c >= 1 && c <= n && d >= -2 && d <= 2 && d != 0;
 }
 
-// One warp per record (row i of line iv): writes the internal record and,
-// for periodic lines, E into the per record.
+// One warp per record (row i of line iv): writes the internal record.
 template <typename TM, typename TC, bool PER>
 __global__ void __launch_bounds__(32 * kPrepWarps) prep_kernel(Args a) {
   __shared__ cd sm[kPrepWarps][kPrepSm];
@@ -184,77 +195,11 @@ __global__ void __launch_bounds__(32 * kPrepWarps) prep_kernel(Args a) {
   }
   for (int p = 1; p < 5; ++p)
     if (!written[p] && lane < 25) st_t(out + 25 * p + lane, cd{0.0, 0.0});
-  if (PER) {
-    // E1, E0 from per(1,i), per(2,i) (reference order j + 2m + 10q)
-    const TM* pr = reinterpret_cast<const TM*>(a.per) + 50 * rc;
-    TC* pe = reinterpret_cast<TC*>(a.fillE) + 50 * rc;
-    cd p1 = cd{0.0, 0.0}, p0 = cd{0.0, 0.0};
-    if (lane < 25) {
-      p1 = ld_cd(pr + 0 + 2 * m + 10 * q);
-      p0 = ld_cd(pr + 1 + 2 * m + 10 * q);
-    }
-    __syncwarp();
-    if (lane < 25) S[lane] = p1, Tm[lane] = p0;
-    __syncwarp();
-    const cd e1 = (act && i <= n - 4) ? mm5(Ui, S, m, q, false) : cd{0.0, 0.0};
-    const cd e0 = (act && i <= n - 3) ? mm5(Ui, Tm, m, q, false) : cd{0.0, 0.0};
-    if (lane < 25) {
-      st_t(pe + lane, e1);
-      st_t(pe + 25 + lane, e0);
-    }
-  }
-}
-
-// Periodic lines: K1, K0 of column c from its per2 record (one warp per
-// record; needs D_{n-1}^-1, D_n^-1 from prep_kernel).
-template <typename TM, typename TC>
-__global__ void __launch_bounds__(32 * kPrepWarps) prep_fill_kernel(Args a) {
-  __shared__ cd sm[kPrepWarps][4 * 25];
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const long long task = (long long)blockIdx.x * kPrepWarps + warp;
-  if (task >= (long long)a.n * a.nsys) return;
-  const int iv = (int)(task / a.n), c = (int)(task % a.n) + 1;
-  const int n = a.n;
-  const int m = lane % 5, q = lane / 5;
-  const TM* p2 = reinterpret_cast<const TM*>(a.per2) + 50 * rec_of(a, c, iv);
-  TC* pk = reinterpret_cast<TC*>(a.fillK) + 50 * rec_of(a, c, iv);
-  if (c > n - 3) {
-    if (lane < 25) st_t(pk + lane, cd{0.0, 0.0}), st_t(pk + 25 + lane, cd{0.0, 0.0});
-    return;
-  }
-  const TM* mat = reinterpret_cast<const TM*>(a.mat);
-  const TC* chn = reinterpret_cast<const TC*>(a.chn);
-  cd* Uc = sm[warp];
-  cd* P = Uc + 25;
-  cd* Tm = Uc + 50;
-  cd* Dn = Uc + 75;
-  if (lane < 25) Uc[lane] = m <= q ? ld_cd(mat + 125 * rec_of(a, c, iv) + 2 + 5 * m + 25 * q) : cd{0.0, 0.0};
-  cd k1 = cd{0.0, 0.0}, k0 = cd{0.0, 0.0};
-  for (int t = 0; t < 2; ++t) {
-    const int row = t == 0 ? n - 1 : n;
-    if (t == 0 && c > n - 4) continue;
-    __syncwarp();
-    if (lane < 25) {
-      P[lane] = ld_cd(p2 + t + 2 * m + 10 * q);
-      Dn[lane] = ld_cd(chn + 125 * rec_of(a, row, iv) + lane);
-    }
-    __syncwarp();
-    if (lane < 25) Tm[lane] = mm5(P, Uc, m, q, true);
-    __syncwarp();
-    cd v{0.0, 0.0};
-    if (lane < 25) v = mm5(Dn, Tm, m, q, false);
-    v = cd{-v.x, -v.y};
-    if (t == 0) k1 = v; else k0 = v;
-  }
-  __syncwarp();
-  if (lane < 25) {
-    st_t(pk + lane, k1);
-    st_t(pk + 25 + lane, k0);
-  }
 }
 
 // ------------------------------------------------------------ the sweeps
-// s = D^-1 r in place for the records of rows 1..n; bx is the block index
+// s = D^-1 r in place for the records of rows 1..n (periodic lines: rows
+// 1..n-2, the border rows keep their right-hand side); bx is the block index
 // within the problem.  Five lanes per record (lane m forms s_m), six records
 // per warp: a load instruction of the warp reads six 5-entry column runs of
 // D instead of 32 scattered records, and each output keeps the order of
@@ -268,14 +213,17 @@ template <typename T>
 __device__ __forceinline__ void scale_body(const Args& a, long long bx) {
   const int lane = threadIdx.x % 32, mm = lane % 5;
   const long long t = (bx * blockDim.x + threadIdx.x) / 32 * kScaleRecsPerWarp + lane / 5;
-  const bool on = lane < 5 * kScaleRecsPerWarp && t < (long long)a.n * a.nsys;
+  bool on = lane < 5 * kScaleRecsPerWarp && t < (long long)a.n * a.nsys;
   const T* D = nullptr;
   T* r = nullptr;
   T x[5];
+  int i = 0, iv = 0;
   if (on) {
-    int i, iv;
     if (a.row_stride == 1) i = (int)(t % a.n) + 1, iv = (int)(t / a.n);
     else iv = (int)(t % a.nsys), i = (int)(t / a.nsys) + 1;
+    on = !a.bord || i <= a.n - 2;  // a periodic line's border rows keep b2
+  }
+  if (on) {
     const long long rc = rec_of(a, i, iv);
     D = reinterpret_cast<const T*>(a.chn) + 125 * rc;
     r = reinterpret_cast<T*>(a.rhs) + 5 * rc;
@@ -347,7 +295,7 @@ __device__ __forceinline__ void chain_stage(T* slot, const T* src, const T* rhs,
 }
 
 // Forward recurrence yh_i = s_i - sum_c F_ic yh_c over rows 1..top (top = n,
-// or n-2 for periodic lines whose rows n-1, n follow in tail_kernel).  The
+// or n-2 for periodic lines, whose border rows follow in btail_kernel).  The
 // staging, ring and output positions advance by pointer increments.
 template <typename T, bool PER, int W>
 __device__ __forceinline__ void chain_fwd_body(const Args& a, int bx, unsigned char* smem_raw) {
@@ -409,8 +357,7 @@ __device__ __forceinline__ void chain_fwd_body(const Args& a, int bx, unsigned c
 }
 
 // Backward recurrence x_i = c_i - sum_c B_ic x_c from row top down to 1
-// (top = n; periodic: n-2, with x_{n-1}, x_n from tail_kernel and c_i from
-// fill_kernel; row np then repeats row 1).
+// (top = n; periodic: n-2, the border rows left out: z = A11^-1 b1).
 template <typename T, bool PER, int W>
 __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned char* smem_raw) {
   constexpr int kAhead = ChainCfg<T>::kAhead, kRing = kAhead + 1;
@@ -434,11 +381,9 @@ __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned c
   }
   const T* st = ring;
   T* out = grhs + 5 * rect + qq;
-  T x1 = zero<T>(), x2 = zero<T>(), x3 = zero<T>(), x4 = zero<T>();  // x of rows i+1..i+4, component qq
-  if (PER) {
-    x1 = grhs[5 * rec_of(a, n - 1, iv) + qq];
-    x2 = grhs[5 * rec_of(a, n, iv) + qq];
-  }
+  // x of rows i+1..i+4, component qq (periodic lines: z = A11^-1 b1, the
+  // border rows left out)
+  T x1 = zero<T>(), x2 = zero<T>(), x3 = zero<T>(), x4 = zero<T>();
   for (int k = 0; k < top; ++k) {
     __syncwarp();  // every lane is done with the slot about to be refilled
     const int i = top - k;
@@ -467,10 +412,7 @@ __device__ __forceinline__ void chain_bwd_body(const Args& a, int bx, unsigned c
     }
     const T xv = sub(st[50 + qq], gather5(p, qq));
     x4 = x3; x3 = x2; x2 = x1; x1 = xv;
-    if (lane < 25 && m == 0) {
-      *out = xv;
-      if (PER && i == 1) grhs[5 * rec_of(a, n + 1, iv) + qq] = xv;  // row np = row 1
-    }
+    if (lane < 25 && m == 0) *out = xv;
     out -= 5 * rs;
     st += kStage;
     if (st == rend) st = ring;
@@ -614,10 +556,6 @@ __device__ __forceinline__ void chain2_bwd_body(const Args& a, int bx, unsigned 
   const cd* st = ring;
   double* out = grhs + 2 * (5 * rect + qq) + C;
   cd x1{0.0, 0.0}, x2{0.0, 0.0}, x3{0.0, 0.0}, x4{0.0, 0.0};  // x of rows i+1..i+4, component qq
-  if (PER) {
-    x1 = grc[5 * rec_of(a, n - 1, iv) + qq];
-    x2 = grc[5 * rec_of(a, n, iv) + qq];
-  }
   cp_async_wait<kAhead - 1>();
   pair_sync(bar);
   for (int k = 0; k < top; ++k) {
@@ -649,7 +587,6 @@ __device__ __forceinline__ void chain2_bwd_body(const Args& a, int bx, unsigned 
     if (lane < 25 && m == 0) {
       xch[par * 10 + C * 5 + qq] = xc;
       *out = xc;
-      if (PER && i == 1) grhs[2 * (5 * rec_of(a, n + 1, iv) + qq) + C] = xc;  // row np = row 1
     }
     out -= 10 * rs;
     st += kStage;
@@ -712,77 +649,206 @@ __global__ void __launch_bounds__(chain_threads<T>(W)) chain_bwd_batch_kernel(co
   chain_bwd_any<T, PER, W>(list[w.x], w.y, smem_raw);
 }
 
-// Periodic lines, after the forward recurrence: the fill sums
-// t1 = sum_{c<=n-4} K1_c yh_c, t0 = sum_{c<=n-3} K0_c yh_c, rows n-1 and n of
-// both recurrences, and x_{n-1}, x_n into the right-hand side.  One CTA of
-// kTailWarps warps per line.
-constexpr int kTailWarps = 8;
-template <typename T>
-__device__ __forceinline__ void tail_body(const Args& a, int iv) {
-  __shared__ T red[2][kTailWarps][25];
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int n = a.n;
-  const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
-  T* grhs = reinterpret_cast<T*>(a.rhs);
-  const T* gchn = reinterpret_cast<const T*>(a.chn);
-  const T* gp2 = reinterpret_cast<const T*>(a.fillK);
-  T acc1 = zero<T>(), acc0 = zero<T>();
-  // unrolled so that several rows' loads are in flight per warp (the sums
-  // keep their order)
-#pragma unroll 4
-  for (int c = 1 + warp; c <= n - 3; c += kTailWarps) {
-    const long long rc = rec_of(a, c, iv);
-    const T y = grhs[5 * rc + qq];
-    acc1 = fmac(acc1, gp2[50 * rc + l], y);       // K1 (zero for c = n-3)
-    acc0 = fmac(acc0, gp2[50 * rc + 25 + l], y);  // K0
-  }
-  if (lane < 25) {
-    red[0][warp][lane] = acc1;
-    red[1][warp][lane] = acc0;
-  }
-  __syncthreads();
-  if (warp != 0) return;
-  T s1 = zero<T>(), s0 = zero<T>();
-#pragma unroll
-  for (int w = 0; w < kTailWarps; ++w) {
-    s1 = add(s1, red[0][w][l]);
-    s0 = add(s0, red[1][w][l]);
-  }
-  const T t1 = gather5(s1, qq), t0 = gather5(s0, qq);
-  const long long r1 = rec_of(a, n - 1, iv), r0 = rec_of(a, n, iv);
-  const T ym2 = grhs[5 * rec_of(a, n - 2, iv) + qq], ym3 = grhs[5 * rec_of(a, n - 3, iv) + qq];
-  // row n-1: band columns n-2 (F1), n-3 (F2)
-  const T* c1 = gchn + 125 * r1;
-  T p = fmac(mul(c1[25 + l], ym2), c1[50 + l], ym3);
-  const T yn1 = sub(sub(grhs[5 * r1 + qq], t1), gather5(p, qq));
-  // row n: band columns n-1 (F1), n-2 (F2)
-  const T* c0 = gchn + 125 * r0;
-  p = fmac(mul(c0[25 + l], yn1), c0[50 + l], ym2);
-  const T yn0 = sub(sub(grhs[5 * r0 + qq], t0), gather5(p, qq));
-  // backward: x_n = yh_n, x_{n-1} = yh_{n-1} - B1 x_n
-  p = mul(c1[75 + l], yn0);
-  const T xn1 = sub(yn1, gather5(p, qq));
-  if (lane < 25 && m == 0) {
-    grhs[5 * r1 + qq] = xn1;
-    grhs[5 * r0 + qq] = yn0;
+// ----------------------------------------------------- periodic border
+// The sixteen border blocks of a periodic line's LHS, before factoring: row,
+// reference slot (column i+slot-3, wrapped) and column.  0..5: A12 (rows 1,
+// 2, n-3, n-2 at columns n-1, n), 6..11: A21, 12..15: A22.
+struct BBlk {
+  int row, slot, col;
+};
+__host__ __device__ inline BBlk bblk(int k, int n) {
+  switch (k) {
+    case 0: return {1, 1, n - 1};
+    case 1: return {1, 2, n};
+    case 2: return {2, 1, n};
+    case 3: return {n - 3, 5, n - 1};
+    case 4: return {n - 2, 4, n - 1};
+    case 5: return {n - 2, 5, n};
+    case 6: return {n - 1, 1, n - 3};
+    case 7: return {n - 1, 2, n - 2};
+    case 8: return {n - 1, 5, 1};
+    case 9: return {n, 1, n - 2};
+    case 10: return {n, 4, 1};
+    case 11: return {n, 5, 2};
+    case 12: return {n - 1, 3, n - 1};
+    case 13: return {n - 1, 4, n};
+    case 14: return {n, 2, n - 1};
+    default: return {n, 3, n};
   }
 }
 
+// Copies the sixteen border blocks of every line from the unfactored LHS
+// (reference storage, entry (slot, m, q) at slot-1 + 5 m + 25 q) into the
+// raw part of the border data; one thread per entry.
+__global__ void bcopy_kernel(Args a) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)a.nsys * 400) return;
+  const int iv = (int)(t / 400), k = (int)(t / 25 % 16), e = (int)(t % 25);
+  const BBlk b = bblk(k, a.n);
+  const cd* mat = reinterpret_cast<const cd*>(a.mat) + 125 * rec_of(a, b.row, iv);
+  cd* out = reinterpret_cast<cd*>(a.bord) + (long long)kBordCd * iv + kBordRaw + 25 * k;
+  out[e] = mat[(b.slot - 1) + 5 * (e % 5) + 25 * (e / 5)];
+}
+
+// The reference's periodic factorisation adds, at pivot row n-5, row n-3's
+// update of column n-1 (M X: M its multiplier block at column n-5, X row
+// n-5's fill block at column n-1) to column n-2 instead (src/cpenta1p.f and
+// src/cpenta2p.f at i = n-5; penta_p_kernel keeps it unless the exact
+// factorisation is chosen).  Its factors are then those of the matrix whose
+// row n-3 has M X added at column n-2 and taken from column n-1; the band
+// records already hold the first, and this kernel makes the border block at
+// (n-3, n-1) the second, so that the bordered solve agrees with the
+// reference's.  One thread per entry (m, q); mat and per factored.
+__global__ void bquirk_kernel(Args a) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)a.nsys * 25) return;
+  const int iv = (int)(t / 25), e = (int)(t % 25), m = e % 5, q = e / 5;
+  const int n = a.n;
+  const cd* M = reinterpret_cast<const cd*>(a.mat) + 125 * rec_of(a, n - 3, iv);   // slot 1: column n-5
+  const cd* X = reinterpret_cast<const cd*>(a.per) + 50 * rec_of(a, n - 5, iv);    // per(1): column n-1
+  cd d{0.0, 0.0};
+#pragma unroll
+  for (int nc = 0; nc < 5; ++nc) d = fmac(d, M[5 * m + 25 * nc], X[2 * nc + 10 * q]);
+  cd* raw = reinterpret_cast<cd*>(a.bord) + (long long)kBordCd * iv + kBordRaw + 25 * 3;   // (n-3, n-1)
+  raw[m + 5 * q] = sub(raw[m + 5 * q], d);
+}
+
+// Column j of A12 (the coefficients of component j % 5 of border row
+// n-1 + j / 5) as a right-hand side: rows 1, 2, n-3, n-2 of rhs, which the
+// caller has cleared; one thread per (line, block, component).
+template <typename TC>
+__global__ void brhs_kernel(Args a, int j) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)a.nsys * 30) return;
+  const int iv = (int)(t / 30), k = (int)(t / 5 % 6), m = (int)(t % 5);
+  const BBlk b = bblk(k, a.n);
+  if ((b.col == a.n ? 1 : 0) != j / 5) return;
+  const cd* blk = reinterpret_cast<const cd*>(a.bord) + (long long)kBordCd * iv + kBordRaw + 25 * k;
+  st_t(reinterpret_cast<TC*>(a.rhs) + 5 * rec_of(a, b.row, iv) + m, blk[m + 5 * (j % 5)]);
+}
+
+// Column j of W = A11^-1 A12 from the solved rows 1..n-2 of rhs into the
+// fill array (entry (m, j) of a record's W at m + 5 j).
+template <typename TC>
+__global__ void bw_kernel(Args a, int j) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int rows = a.n - 2;
+  if (t >= (long long)a.nsys * rows * 5) return;
+  const int m = (int)(t % 5);
+  const long long r = t / 5;
+  const int iv = (int)(r / rows), i = (int)(r % rows) + 1;
+  const long long rc = rec_of(a, i, iv);
+  reinterpret_cast<TC*>(a.fillE)[50 * rc + m + 5 * j] = reinterpret_cast<const TC*>(a.rhs)[5 * rc + m];
+}
+
+// S = A22 - A21 W, inverted by Gauss-Jordan elimination with partial
+// pivoting, into the kept part of the border data with the A21 blocks; one
+// thread per line (formed once per factorisation, in FP64).
+template <typename TC>
+__global__ void bschur_kernel(Args a, int* status) {
+  const int iv = blockIdx.x * blockDim.x + threadIdx.x;
+  if (iv >= a.nsys) return;
+  const int n = a.n;
+  cd* bd = reinterpret_cast<cd*>(a.bord) + (long long)kBordCd * iv;
+  const cd* raw = bd + kBordRaw;
+  const TC* W = reinterpret_cast<const TC*>(a.fillE);
+  cd M[10][20];  // [S | I]
+  for (int k = 0; k < 10; ++k) {
+    const int bk = k / 5, m = k % 5;
+    for (int j = 0; j < 10; ++j) {
+      const int bj = j / 5, p = j % 5;
+      cd s = raw[25 * (12 + 2 * bk + bj) + m + 5 * p];   // A22 block (bk, bj)
+      for (int kk = 0; kk < 3; ++kk) {                 // A21 blocks of border row bk
+        const int blk = 6 + 3 * bk + kk;
+        const cd* A = raw + 25 * blk;
+        const TC* w = W + 50 * rec_of(a, bblk(blk, n).col, iv) + 5 * j;
+        for (int q = 0; q < 5; ++q) s = fmsc(s, A[m + 5 * q], ld_cd(w + q));
+      }
+      M[k][j] = s;
+      M[k][10 + j] = cd{k == j ? 1.0 : 0.0, 0.0};
+    }
+  }
+  bool ok = true;
+  for (int c = 0; c < 10; ++c) {
+    int piv = c;
+    double best = -1.0;
+    for (int r = c; r < 10; ++r) {
+      const double v = fabs(M[r][c].x) + fabs(M[r][c].y);
+      if (v > best) best = v, piv = r;
+    }
+    if (!(best > 0.0) || !isfinite(best)) {
+      ok = false;
+      break;
+    }
+    if (piv != c)
+      for (int j = 0; j < 20; ++j) {
+        const cd t = M[c][j];
+        M[c][j] = M[piv][j];
+        M[piv][j] = t;
+      }
+    const cd inv = rcp(M[c][c]);
+    for (int j = 0; j < 20; ++j) M[c][j] = mul(M[c][j], inv);
+    for (int r = 0; r < 10; ++r) {
+      if (r == c) continue;
+      const cd f = M[r][c];
+      for (int j = 0; j < 20; ++j) M[r][j] = fmsc(M[r][j], f, M[c][j]);
+    }
+  }
+  if (!ok) {
+    atomicExch(status, 1);
+    return;
+  }
+  for (int k = 0; k < 10; ++k)
+    for (int j = 0; j < 10; ++j) bd[kBordSinv + k + 10 * j] = M[k][10 + j];
+  for (int e = 0; e < 150; ++e) bd[kBordA21 + e] = raw[25 * 6 + e];
+}
+
+// Per step, after the recurrences gave z in rows 1..n-2: x2 = S^-1 (b2 -
+// A21 z) into rows n-1, n (which hold b2).  One warp per line, lane
+// k = m + 5 b < 10 forms entry k in FP64.
+constexpr int kBTailLines = 4;
 template <typename T>
-__global__ void __launch_bounds__(32 * kTailWarps) tail_kernel(Args a) { tail_body<T>(a, blockIdx.x); }
+__device__ __forceinline__ void btail_body(const Args& a, int iv) {
+  const int lane = threadIdx.x % 32;
+  if (iv >= a.nsys) return;
+  const int n = a.n;
+  const cd* bd = reinterpret_cast<const cd*>(a.bord) + (long long)kBordCd * iv;
+  T* grhs = reinterpret_cast<T*>(a.rhs);
+  const int k = min(lane, 9), b = k / 5, m = k % 5;
+  const long long rb = rec_of(a, n - 1 + b, iv);
+  cd t = ld_cd(grhs + 5 * rb + m);
+  for (int kk = 0; kk < 3; ++kk) {
+    const int blk = 6 + 3 * b + kk;
+    const cd* A = bd + kBordA21 + 25 * (3 * b + kk);
+    const T* z = grhs + 5 * rec_of(a, bblk(blk, n).col, iv);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) t = fmsc(t, A[m + 5 * q], ld_cd(z + q));
+  }
+  cd x{0.0, 0.0};
+#pragma unroll
+  for (int j = 0; j < 10; ++j) {
+    const cd tj{__shfl_sync(0xffffffffu, t.x, j), __shfl_sync(0xffffffffu, t.y, j)};
+    x = fmac(x, bd[kBordSinv + k + 10 * j], tj);
+  }
+  if (lane < 10) st_t(grhs + 5 * rb + m, x);
+}
 template <typename T>
-__global__ void __launch_bounds__(32 * kTailWarps) tail_batch_kernel(const Args* __restrict__ list,
-                                                                    const int2* __restrict__ table,
-                                                                    const int* __restrict__ active) {
+__global__ void __launch_bounds__(32 * kBTailLines) btail_kernel(Args a) {
+  btail_body<T>(a, blockIdx.x * kBTailLines + threadIdx.x / 32);
+}
+template <typename T>
+__global__ void __launch_bounds__(32 * kBTailLines) btail_batch_kernel(const Args* __restrict__ list,
+                                                                      const int2* __restrict__ table,
+                                                                      const int* __restrict__ active) {
   const int2 w = table[blockIdx.x];
   if (!active[w.x]) return;
-  tail_body<T>(list[w.x], w.y);
+  btail_body<T>(list[w.x], w.y * kBTailLines + threadIdx.x / 32);
 }
 
-// Periodic lines: c_i = yh_i - E1_i x_{n-1} - E0_i x_n for rows 1..n-3, one
-// thread per entry of c_i (thread 5 t + m forms entry m of record t), so a
-// warp's loads cover a few consecutive records' E runs; each entry keeps
-// the order of accumulation of a per-record loop (E1 columns, then E0).
+// Periodic lines, last: x_i = z_i - W_i x2 for rows 1..n-2 (and row np,
+// which repeats row 1), one thread per entry of x_i (thread 5 t + m forms
+// entry m of record t), so a warp's loads cover a few consecutive records'
+// W runs; each entry sums the columns of border row n-1, then of row n.
 __host__ __device__ constexpr long long fill_blocks(long long recs, int threads = 256) {
   return (5 * recs + threads - 1) / threads;
 }
@@ -791,7 +857,7 @@ __device__ __forceinline__ void fill_body(const Args& a, long long bx) {
   const long long t5 = bx * blockDim.x + threadIdx.x;
   const long long t = t5 / 5;
   const int mm = (int)(t5 - 5 * t);
-  const int rows = a.n - 3;
+  const int rows = a.n - 2;
   if (t >= (long long)rows * a.nsys) return;
   int i, iv;
   if (a.row_stride == 1) i = (int)(t % rows) + 1, iv = (int)(t / rows);
@@ -807,6 +873,7 @@ __device__ __forceinline__ void fill_body(const Args& a, long long bx) {
 #pragma unroll
   for (int k = 0; k < 5; ++k) acc = fmsc(acc, E[25 + 5 * k], xb[k]);
   grhs[5 * rc + mm] = acc;
+  if (i == 1) grhs[5 * rec_of(a, a.n + 1, iv) + mm] = acc;  // row np = row 1
 }
 
 template <typename T>
