@@ -424,6 +424,15 @@ int lns_rhs3d_dev(lns_ctx3d* ctx, const double* v, const double* vold, double* r
  * or eta sweep (dir 2: src/lhs2f3d.f90 + src/lhsbt2f3d.f90 +
  * src/lhsbc2f3d.f90) into the complex*16 device array mat(5,5,5,nx,ny). */
 int lns_lhs3d_dev(lns_ctx3d* ctx, int32_t dir, double* mat, void* stream);
+/* Line mode of the FP64 periodic sweeps, no reference counterpart.  With
+ * on = 1 (the default for a context used alone) periodic lines whose band
+ * has an odd number of rows (nx even for xi, ny even for a periodic eta)
+ * advance both recurrences two rows per step: the even rows' blocks are
+ * combined with their odd neighbours' once, at factoring time, which
+ * changes the solution by rounding only.  on = 0 keeps every line row by
+ * row, as the contexts of a batch or a server always are.  Takes effect at
+ * the next factorisation (the next step).  LNS_ERR_ARG for on not 0 or 1. */
+int lns_ctx3d_set_row_pairs(lns_ctx3d* ctx, int32_t on);
 /* Phase timing, no reference counterpart.  lns_ctx3d_profile(ctx, 1) makes
  * every later corrector record CUDA events on its stream (and resets the
  * record); lns_ctx3d_profile_read waits for them and returns the summed

@@ -50,11 +50,14 @@ class ImpDrv3D:
     and the forced top (params top = 1) take the x coordinates x (nx, ny),
     x0 and wamp (nx; None: ones); ispg 4 the complex target cvic (5, nx, ny).
     wall = 3 (the bump) takes u1w, u2w, u3w, tw, twp as bump, complex (5, nx).
+    row_pairs: FP64 periodic lines with an odd band advance their recurrences
+    two rows per step (lns_ctx3d_set_row_pairs); False keeps them row by
+    row, as a batch does.
     """
 
     def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64,
                  impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None, x=None, x0=0.0, wamp=None,
-                 cvic=None, bump=None):
+                 cvic=None, bump=None, row_pairs=True):
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -66,6 +69,8 @@ class ImpDrv3D:
                        left=p.get("left", -1), right=p.get("right", -1))
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx3d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx3d_create")
+        if not row_pairs:
+            check(lib().lns_ctx3d_set_row_pairs(self._ctx, 0), "lns_ctx3d_set_row_pairs")
         m = np.empty((self.nx, self.ny, 10), order="F")
         for k, name in enumerate(METRICS):
             m[:, :, k] = metrics[name]

@@ -824,6 +824,11 @@ struct lns_ctx3d {
   void *chnx = nullptr, *chny = nullptr, *fillE = nullptr, *bordx = nullptr;
   // a periodic eta direction (yper): the same for the eta lines
   void *pery = nullptr, *per2y = nullptr, *fillEy = nullptr, *bordy = nullptr;
+  // FP64 periodic lines with an odd band solved in row pairs (penta_chain.cuh):
+  // their pair arrays (allocated at the first factorisation), and whether the
+  // records are in the paired form; a batch's contexts stay row by row
+  void *pairx = nullptr, *pairy = nullptr;
+  bool pair_ok = true, paired_x = false, paired_y = false;
   double* part = nullptr;  // block partials (residual, CFL)
   int nparts = 0;
   double* dscal = nullptr;  // [0] cfl, [1..] residual of the inspection call
@@ -982,12 +987,12 @@ lns::chain::Args xargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
   if (!g.xper) return lns::chain::Args{c->matx, c->chnx, nullptr, nullptr, nullptr, rhs, g.nx, g.ny, 1, g.nx};
   return lns::chain::Args{c->matx, c->chnx, c->perx, c->per2x, c->fillE, rhs, g.nx - 1, g.ny, 1, g.nx,
-                          c->bordx};
+                          c->bordx, c->paired_x ? c->pairx : nullptr};
 }
 lns::chain::Args yargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
   if (g.yper) return lns::chain::Args{c->maty, c->chny, c->pery, c->per2y, c->fillEy, rhs, g.ny - 1, g.nx,
-                                      g.nx, 1, c->bordy};
+                                      g.nx, 1, c->bordy, c->paired_y ? c->pairy : nullptr};
   return lns::chain::Args{c->maty, c->chny, nullptr, nullptr, nullptr, rhs, g.ny, g.nx, g.nx, 1};
 }
 
@@ -997,10 +1002,35 @@ lns::chain::Args yargs(lns_ctx3d* c, void* rhs) {
 // xi_marks: the profiling marks of the xi sweep (after the scaling and each
 // recurrence; the border and correction close the segment); an eta sweep
 // marks as a non-periodic one (after the scaling and the forward recurrence).
+// FP64 lines in the paired form: the two recurrences advance two rows per
+// step (pair_chain_kernel), each after even_kernel has formed the even rows'
+// combined right-hand sides.
 template <typename T>
 int sweep_periodic(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaStream_t st) {
   namespace ch = lns::chain;
-  const long long pts = (long long)a.n * a.nsys, fill = (long long)(a.n - 2) * a.nsys;
+  const long long fill = (long long)(a.n - 2) * a.nsys;
+  if constexpr (std::is_same<T, cd>::value) {
+    if (a.pairs) {
+      const long long pts = (long long)a.n * a.nsys;
+      const int cta = (a.nsys + ch::kPairLines - 1) / ch::kPairLines;
+      const size_t sm = ch::pair_smem_bytes();
+      const unsigned eb = (unsigned)((5LL * ((a.n - 3) / 2) * a.nsys + 255) / 256);
+      ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
+      int rc = mark(c, st);
+      ch::even_kernel<false><<<eb, 256, 0, st>>>(a);
+      ch::pair_chain_kernel<false><<<cta, 128 * ch::kPairLines, sm, st>>>(a);
+      if (!rc) rc = mark(c, st);
+      ch::even_kernel<true><<<eb, 256, 0, st>>>(a);
+      ch::pair_chain_kernel<true><<<cta, 128 * ch::kPairLines, sm, st>>>(a);
+      if (!rc && xi_marks) rc = mark(c, st);
+      ch::btail_kernel<T><<<(a.nsys + ch::kBTailLines - 1) / ch::kBTailLines, 32 * ch::kBTailLines, 0, st>>>(a);
+      ch::fill_kernel<T><<<(unsigned)ch::fill_blocks(fill), 256, 0, st>>>(a);
+      if (rc) return rc;
+      cudaError_t e = cudaGetLastError();
+      return e == cudaSuccess ? LNS_OK : cuda3(e, "paired periodic sweep launch");
+    }
+  }
+  const long long pts = (long long)a.n * a.nsys;
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
   ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
@@ -1102,6 +1132,7 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   // the periodic factorisation mode, read once for both directions: the
   // reference's (its row n-5 fill placement) unless the exact LU is chosen
   const int exact = g_periodic_exact.load() ? 1 : 0;
+  c->paired_x = c->paired_y = false;  // the records are formed row by row again below
   int rc = launch_lhs<cd>(c, 1, mx, st);
   if (!rc && g.xper) {
     ch::bcopy_kernel<<<(unsigned)((ax.nsys * 400LL + 255) / 256), 256, 0, st>>>(ax);
@@ -1135,6 +1166,34 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   if (!rc && g.xper) rc = form_border<TC>(c, xargs(c, scratch), st);
   if (!rc && g.yper) rc = form_border<TC>(c, yargs(c, scratch), st);
   if (rc) return rc;
+  // FP64 periodic lines whose band has an odd number of rows: the paired form
+  if constexpr (std::is_same<TC, cd>::value) {
+    if (c->pair_ok && g.xper && (g.nx - 3) % 2 == 1) {
+      if (!c->pairx) rc = dalloc(c, sizeof(cd) * 50 * (size_t)c->np, &c->pairx);
+      if (!rc) {
+        ch::Args pa = xargs(c, nullptr);
+        pa.pairs = c->pairx;
+        const long long tasks = (long long)(pa.n - 3) / 2 * pa.nsys;
+        ch::pair_prep_kernel<<<(unsigned)((tasks + ch::kPrepWarps - 1) / ch::kPrepWarps), 32 * ch::kPrepWarps, 0,
+                               st>>>(pa);
+        c->paired_x = true;
+      }
+    }
+    if (!rc && c->pair_ok && g.yper && (g.ny - 3) % 2 == 1) {
+      if (!c->pairy) rc = dalloc(c, sizeof(cd) * 50 * (size_t)c->np, &c->pairy);
+      if (!rc) {
+        ch::Args pa = yargs(c, nullptr);
+        pa.pairs = c->pairy;
+        const long long tasks = (long long)(pa.n - 3) / 2 * pa.nsys;
+        ch::pair_prep_kernel<<<(unsigned)((tasks + ch::kPrepWarps - 1) / ch::kPrepWarps), 32 * ch::kPrepWarps, 0,
+                               st>>>(pa);
+        c->paired_y = true;
+      }
+    }
+    if (rc) return rc;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda3(e, "pair prep launch");
+  }
   int status = 0;
   e = cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1599,6 +1658,16 @@ int lns_lhs3d_dev(lns_ctx3d* c, int32_t dir, double* mat, void* stream) {
   return launch_lhs<cd>(c, dir, (cd*)mat, (cudaStream_t)stream);
 }
 
+int lns_ctx3d_set_row_pairs(lns_ctx3d* c, int32_t on) {
+  if (!c) return fail3(LNS_ERR_ARG, "ctx3d_set_row_pairs: null context");
+  if (on != 0 && on != 1) return fail3(LNS_ERR_ARG, "ctx3d_set_row_pairs: on must be 0 or 1");
+  if (c->pair_ok != (on == 1)) {
+    c->pair_ok = on == 1;
+    c->factored = false;  // the records are formed again in the chosen form
+  }
+  return LNS_OK;
+}
+
 int lns_ctx3d_profile(lns_ctx3d* c, int32_t on) {
   if (!c) return fail3(LNS_ERR_ARG, "ctx3d_profile: null context");
   c->profile = on != 0;
@@ -1939,6 +2008,7 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
     lns_ctx3d* c = nullptr;
     rc = lns_ctx3d_create(&params[p], &c);
     if (!rc) {
+      c->pair_ok = false;  // one launch per phase serves all problems row by row
       b->ctx.push_back(c);
       b->bytes += lns_ctx3d_bytes(c);
     }
@@ -2203,6 +2273,7 @@ int admit(lns_server3d* s) {
     if (s->used + need > s->budget && !s->running.empty()) break;  // wait for memory
     lns_ctx3d* c = nullptr;
     int rc = lns_ctx3d_create(&r->prm, &c);
+    if (!rc) c->pair_ok = false;  // served in a batch
     if (!rc) rc = lns_upload_metrics3d(c, r->metrics.data());
     if (!rc) rc = lns_upload_mean3d(c, r->vm.data(), nullptr);
     if (!rc) {

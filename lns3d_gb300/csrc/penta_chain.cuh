@@ -57,6 +57,9 @@ struct Args {
   long long row_stride, line_stride;
   // periodic lines: kBordCd complex doubles per line (see kBordCd)
   void* bord = nullptr;
+  // FP64 periodic lines solved in row pairs: 50 entries per record (see
+  // pair_prep_kernel); null for lines solved row by row
+  void* pairs = nullptr;
 };
 
 // Border data of a periodic line: S^-1 (row k, column j at k + 10 j; k, j =
@@ -617,6 +620,191 @@ __device__ __forceinline__ void chain_bwd_any(const Args& a, int bx, unsigned ch
   } else {
     chain_bwd_body<T, PER, W>(a, bx, smem_raw);
   }
+}
+
+// ------------------------------------ FP64 periodic lines, rows in pairs
+// The band rows of a periodic line all have the form
+//   yh_i = s_i - F1_i yh_{i-1} - F2_i yh_{i-2},  x_i = c_i - B1_i x_{i+1} - B2_i x_{i+2}
+// (the blocks of the first rows zero).  Substituting the odd row into the
+// even one,
+//   yh_{i+1} = s'_{i+1} - G yh_{i-1} - H yh_{i-2},
+//   G = F2_{i+1} - F1_{i+1} F1_i,  H = -F1_{i+1} F2_i,  s'_{i+1} = s_{i+1} - F1_{i+1} s_i,
+// so both rows of a pair (i, i+1), i odd, are two block products of the
+// same two rows of the previous pair, and a step of the recurrence covers
+// two rows.  Likewise downwards in pairs (i, i-1) from the top row (odd):
+//   x_{i-1} = c'_{i-1} - G' x_{i+1} - H' x_{i+2},
+//   G' = B2_{i-1} - B1_{i-1} B1_i,  H' = -B1_{i-1} B2_i,  c'_{i-1} = c_{i-1} - B1_{i-1} c_i.
+// The even rows' records hold G, H (blocks 1, 2) and G', H' (blocks 3, 4);
+// the pair array holds, per even record, its own F1 and B1, with which
+// even_kernel forms s' before the forward and c' before the backward pairs
+// (point-parallel, one thread per entry).  Used when the band has an odd
+// number of rows (top = n - 2 odd).
+constexpr int kPairAhead = 6;         // pairs staged ahead
+constexpr int kPStage = 2 * kStage;   // a pair's two staged rows
+constexpr int kPXchg = 40;            // 2 parities x 2 rows x 2 parts x 5 components (doubles)
+constexpr int kPairLines = 2;         // lines (four warps each) per CTA
+constexpr size_t pair_smem_bytes(int lines_per_cta = kPairLines) {
+  return (size_t)lines_per_cta * ((kPairAhead + 1) * kPStage * sizeof(cd) + kPXchg * sizeof(double));
+}
+
+// One warp per even record e of the band (2 <= e <= n-3): G, H, G', H' into
+// the record, its F1 and B1 into the pair array (formed in FP64 from the
+// FP64 records, after the border's W, which uses the records row by row).
+__global__ void __launch_bounds__(32 * kPrepWarps) pair_prep_kernel(Args a) {
+  __shared__ cd sm[kPrepWarps][8 * 25];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int rows = (a.n - 3) / 2;  // even rows 2..n-3
+  const long long task = (long long)blockIdx.x * kPrepWarps + warp;
+  if (task >= (long long)rows * a.nsys) return;
+  const int iv = (int)(task / rows), e = 2 * (int)(task % rows) + 2;
+  cd* chn = reinterpret_cast<cd*>(a.chn);
+  cd* re = chn + 125 * rec_of(a, e, iv);
+  const cd* rlo = chn + 125 * rec_of(a, e - 1, iv);
+  const cd* rhi = chn + 125 * rec_of(a, e + 1, iv);
+  cd* F1 = sm[warp];
+  cd *F2 = F1 + 25, *B1 = F1 + 50, *B2 = F1 + 75, *F1l = F1 + 100, *F2l = F1 + 125, *B1h = F1 + 150,
+     *B2h = F1 + 175;
+  const int m = lane % 5, q = lane / 5;
+  if (lane < 25) {
+    F1[lane] = re[25 + lane], F2[lane] = re[50 + lane], B1[lane] = re[75 + lane], B2[lane] = re[100 + lane];
+    F1l[lane] = rlo[25 + lane], F2l[lane] = rlo[50 + lane];
+    B1h[lane] = rhi[75 + lane], B2h[lane] = rhi[100 + lane];
+  }
+  __syncwarp();
+  if (lane < 25) {
+    const cd g = sub(F2[lane], mm5(F1, F1l, m, q, false));
+    const cd h = mm5(F1, F2l, m, q, false);
+    const cd g2 = sub(B2[lane], mm5(B1, B1h, m, q, false));
+    const cd h2 = mm5(B1, B2h, m, q, false);
+    re[25 + lane] = g;
+    re[50 + lane] = cd{-h.x, -h.y};
+    re[75 + lane] = g2;
+    re[100 + lane] = cd{-h2.x, -h2.y};
+    cd* pr = reinterpret_cast<cd*>(a.pairs) + 50 * rec_of(a, e, iv);
+    pr[lane] = F1[lane];
+    pr[25 + lane] = B1[lane];
+  }
+}
+
+// The even band rows' right-hand sides before a paired recurrence:
+// s'_j = s_j - F1_j s_{j-1} (UP = false) or c'_j = c_j - B1_j c_{j+1}
+// (UP = true), 2 <= j <= n-3; one thread per entry, only even rows written.
+template <bool UP>
+__global__ void even_kernel(Args a) {
+  const long long t5 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long t = t5 / 5;
+  const int mm = (int)(t5 - 5 * t);
+  const int rows = (a.n - 3) / 2;
+  if (t >= (long long)rows * a.nsys) return;
+  int k, iv;
+  if (a.row_stride == 1) k = (int)(t % rows), iv = (int)(t / rows);
+  else iv = (int)(t % a.nsys), k = (int)(t / a.nsys);
+  const long long rj = rec_of(a, 2 * k + 2, iv);
+  cd* grhs = reinterpret_cast<cd*>(a.rhs);
+  const cd* B = reinterpret_cast<const cd*>(a.pairs) + 50 * rj + (UP ? 25 : 0);
+  const cd* nb = grhs + 5 * (UP ? rj + a.row_stride : rj - a.row_stride);
+  cd acc = grhs[5 * rj + mm];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) acc = fmsc(acc, B[mm + 5 * q], nb[q]);
+  grhs[5 * rj + mm] = acc;
+}
+
+// Stage one pair (rows r0 and r1 = r0 +- 1; the second only when `two`):
+// each row's 50 block entries at its record plus off and its 5
+// right-hand-side entries; thread t < 110 of the line's team copies one.
+__device__ __forceinline__ void pair_stage(cd* slot, const cd* gchn, const cd* grc, long long rec0,
+                                           long long rec1, int off, bool two, int t) {
+  if (t >= 110) return;
+  const int r = t >= 55, e = r ? t - 55 : t;
+  if (r && !two) return;
+  const long long rc = r ? rec1 : rec0;
+  if (e < 50) cp_async_el(slot + t, gchn + 125 * rc + off + e);
+  else cp_async_el(slot + t, grc + 5 * rc + (e - 50));
+}
+
+__device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 128;\n" ::"r"(id) : "memory"); }
+
+// Both recurrences of a paired line: DOWN = false forward over pairs (2k+1,
+// 2k+2), DOWN = true backward over pairs (top-2k, top-2k-1).  Four warps per
+// line: warp 2P + C forms part C of row P of each pair (the split layout of
+// chain2: lane (m, q), a three-level tree of DADD), and the four post their
+// parts to a shared exchange slot and meet at the line's named barrier, which
+// also publishes the rows the team staged.
+template <int W, int P, int C, bool DOWN>
+__device__ __forceinline__ void pair_body(const Args& a, int bx, unsigned char* smem_raw) {
+  constexpr int kRing = kPairAhead + 1;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int ln = warp >> 2, t = (warp & 3) * 32 + lane;
+  const int iv = bx * W + ln;
+  if (iv >= a.nsys) return;  // the four warps of a line leave together
+  const int bar = 1 + ln;
+  cd* ring = reinterpret_cast<cd*>(smem_raw) + ln * kRing * kPStage;
+  double* xch = reinterpret_cast<double*>(reinterpret_cast<cd*>(smem_raw) + W * kRing * kPStage) + ln * kPXchg;
+  const int top = a.n - 2, npair = (top + 1) / 2;
+  const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
+  double* grhs = reinterpret_cast<double*>(a.rhs);
+  const cd* grc = reinterpret_cast<const cd*>(a.rhs);
+  const cd* gchn = reinterpret_cast<const cd*>(a.chn);
+  cd* const rend = ring + kRing * kPStage;
+  const long long rs = a.row_stride, base = a.line_stride * (long long)iv;
+  const long long step = DOWN ? -2 * rs : 2 * rs;              // records per pair
+  const long long dr = DOWN ? -rs : rs;                       // the pair's second row
+  const int off = DOWN ? 75 : 25;                             // the recurrence's two blocks
+  long long srec = base + rs * (DOWN ? top - 1 : 0);          // first row of the next pair to stage
+  cd* ws = ring;
+  for (int k = 0; k < kPairAhead; ++k) {
+    if (k < npair) pair_stage(ws, gchn, grc, srec, srec + dr, off, 2 * k + 2 <= top, t);
+    cp_async_commit();
+    srec += step, ws += kPStage;
+  }
+  cp_async_wait<kPairAhead - 1>();
+  team_sync(bar);
+  const cd* st = ring;
+  double* out = grhs + 2 * (5 * (base + rs * (DOWN ? top - 1 - P : P)) + qq) + C;
+  cd z1{0.0, 0.0}, z2{0.0, 0.0};  // the previous pair's rows: second, first (component qq)
+  for (int k = 0; k < npair; ++k) {
+    if (k + kPairAhead < npair) pair_stage(ws, gchn, grc, srec, srec + dr, off, 2 * (k + kPairAhead) + 2 <= top, t);
+    cp_async_commit();
+    srec += step, ws += kPStage;
+    if (ws == rend) ws = ring;
+    const bool live = P == 0 || 2 * k + 2 <= top;  // the last pair has its first row only
+    const cd* rw = st + P * kStage;
+    double p = 0.0;
+    if (lane < 5) p = C ? rw[50 + lane].y : rw[50 + lane].x;
+    p = part_msub<C>(p, rw[25 + l], z2);
+    p = part_msub<C>(p, rw[l], z1);
+    const double yc = tree5(p, qq);
+    const int par = k & 1;
+    if (live && lane < 25 && m == 0) {
+      xch[par * 20 + P * 10 + C * 5 + qq] = yc;
+      *out = yc;
+    }
+    out += DOWN ? -20 * rs : 20 * rs;
+    st += kPStage;
+    if (st == rend) st = ring;
+    cp_async_wait<kPairAhead - 1>();  // this thread's part of the next pair
+    team_sync(bar);
+    const double* x = xch + par * 20 + qq;
+    z2 = cd{x[0], x[5]};    // first row of the pair
+    z1 = cd{x[10], x[15]};  // second row
+  }
+  cp_async_wait<0>();
+}
+
+template <int W, bool DOWN>
+__device__ __forceinline__ void pair_any(const Args& a, int bx, unsigned char* smem_raw) {
+  switch ((threadIdx.x / 32) & 3) {
+    case 0: pair_body<W, 0, 0, DOWN>(a, bx, smem_raw); break;
+    case 1: pair_body<W, 0, 1, DOWN>(a, bx, smem_raw); break;
+    case 2: pair_body<W, 1, 0, DOWN>(a, bx, smem_raw); break;
+    default: pair_body<W, 1, 1, DOWN>(a, bx, smem_raw); break;
+  }
+}
+// Launch with 128 * W threads and pair_smem_bytes(W) bytes.
+template <bool DOWN, int W = kPairLines>
+__global__ void __launch_bounds__(128 * W) pair_chain_kernel(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pair_any<W, DOWN>(a, blockIdx.x, smem_raw);
 }
 
 // Launch with chain_threads<T>(W) threads and chain_smem_bytes<T>(W) bytes.

@@ -202,6 +202,42 @@ def test_rejects_bad_arguments(cuda, small):
         drv.lhs(3, torch.zeros(125 * 40 * 33, dtype=torch.complex128, device="cuda"))
 
 
+@pytest.mark.parametrize("nx", [40, 41])
+def test_row_pairs_agree_with_row_by_row(cuda, nx):
+    """Periodic xi lines advanced two rows per step (nx even: an odd band)
+    and row by row agree to rounding, and both with the oracle; nx odd has
+    an even band and stays row by row whatever the switch says."""
+    from lns3d_gb300 import ImpDrv3D
+    from lns3d_gb300.cases import shear_layer
+
+    case = shear_layer(nx=nx, ny=24, seed=9)
+    orc = Oracle3D(case, cflmax=20.0, loctime=1)
+    mk = lambda pairs: ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1,
+                                row_pairs=pairs)
+    vp, vr, vo = (case["v"].copy(order="F") for _ in range(3))
+    rp = mk(True).step(vp, nsteps=5)
+    rr = mk(False).step(vr, nsteps=5)
+    ro = [orc.step(vo) for _ in range(5)]
+    if nx % 2:
+        assert np.array_equal(vp, vr) and np.array_equal(rp, rr)
+    else:
+        assert 0.0 < rel(vp, vr) < 1e-13
+    for v in (vp, vr):
+        assert rel(v, vo) < STEP_TOL
+    assert np.abs(np.asarray(rp) - ro).max() <= 1e-10 * max(ro)
+
+
+def test_row_pairs_switch_rejects_bad_values(cuda, small):
+    from lns3d_gb300 import LnsError, lib
+
+    case, _ = small
+    drv = make_drv(case)
+    with pytest.raises(LnsError):
+        from lns3d_gb300._lib import check
+
+        check(lib().lns_ctx3d_set_row_pairs(drv._ctx, 2), "lns_ctx3d_set_row_pairs")
+
+
 def test_full_size_steps_match_oracle(cuda):
     # the 512 x 256 benchmark workload itself, three steps
     from lns3d_gb300.cases import shear_layer

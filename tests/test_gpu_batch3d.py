@@ -1,8 +1,9 @@
 """GPU tests of batched linearised problems (lns_batch3d_*, through the C
 ABI): every problem of a batch -- different grid sizes, beta and omega --
 must end with exactly the state and residuals of its own lns_ctx3d run (the
-same kernels on the same data), alone or in the mix; convergence steps and
-the autotuner must leave results unchanged."""
+same kernels on the same data: the context's periodic lines row by row, as
+a batch's), alone or in the mix; convergence steps and the autotuner must
+leave results unchanged."""
 import numpy as np
 import pytest
 
@@ -29,7 +30,8 @@ def test_batch_matches_individual_runs(cuda, precision):
     steps, res = batch.run(max_steps=12, tol=0.0, check_every=5)
     assert (steps == -1).all()
     for k, c in enumerate(probs):
-        drv = ImpDrv3D(c["params"], c["metrics"], c["vm"], cflmax=20.0, loctime=1, precision=precision)
+        drv = ImpDrv3D(c["params"], c["metrics"], c["vm"], cflmax=20.0, loctime=1, precision=precision,
+                       row_pairs=False)
         v = c["v"].copy(order="F")
         r = drv.step(v, nsteps=12)
         assert np.array_equal(batch.state(k), v), k
