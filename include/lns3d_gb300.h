@@ -425,11 +425,13 @@ int lns_rhs3d_dev(lns_ctx3d* ctx, const double* v, const double* vold, double* r
  * src/lhsbc2f3d.f90) into the complex*16 device array mat(5,5,5,nx,ny). */
 int lns_lhs3d_dev(lns_ctx3d* ctx, int32_t dir, double* mat, void* stream);
 /* Line mode of the FP64 periodic sweeps, no reference counterpart.  With
- * on = 1 (the default for a context used alone) periodic lines whose band
- * has an odd number of rows (nx even for xi, ny even for a periodic eta)
- * advance both recurrences two rows per step: the even rows' blocks are
- * combined with their odd neighbours' once, at factoring time, which
- * changes the solution by rounding only.  on = 0 keeps every line row by
+ * on = 1 (the default for a context used alone) the lines advance both
+ * recurrences two rows per step where their row count allows it (periodic
+ * lines with an odd band: nx even for xi, ny even for a periodic eta; eta
+ * lines with boundary-closure rows: ny even) and the direction has at most
+ * twice as many lines as the GPU has SMs (more lines fill the FP64 pipes
+ * row by row): one row of each pair is combined with its neighbour's blocks
+ * once, at factoring time, which changes the solution by rounding only.  on = 0 keeps every line row by
  * row, as the contexts of a batch or a server always are.  Takes effect at
  * the next factorisation (the next step).  LNS_ERR_ARG for on not 0 or 1. */
 int lns_ctx3d_set_row_pairs(lns_ctx3d* ctx, int32_t on);

@@ -829,6 +829,7 @@ struct lns_ctx3d {
   // records are in the paired form; a batch's contexts stay row by row
   void *pairx = nullptr, *pairy = nullptr;
   bool pair_ok = true, paired_x = false, paired_y = false;
+  int sms = 0;  // the device's SMs
   double* part = nullptr;  // block partials (residual, CFL)
   int nparts = 0;
   double* dscal = nullptr;  // [0] cfl, [1..] residual of the inspection call
@@ -993,7 +994,8 @@ lns::chain::Args yargs(lns_ctx3d* c, void* rhs) {
   const Grid& g = c->g;
   if (g.yper) return lns::chain::Args{c->maty, c->chny, c->pery, c->per2y, c->fillEy, rhs, g.ny - 1, g.nx,
                                       g.nx, 1, c->bordy, c->paired_y ? c->pairy : nullptr};
-  return lns::chain::Args{c->maty, c->chny, nullptr, nullptr, nullptr, rhs, g.ny, g.nx, g.nx, 1};
+  return lns::chain::Args{c->maty, c->chny, nullptr, nullptr, nullptr, rhs, g.ny, g.nx, g.nx, 1, nullptr,
+                          c->paired_y ? c->pairy : nullptr};
 }
 
 // A periodic sweep (xi, or eta with yper), bordered: s = D^-1 r on rows
@@ -1014,13 +1016,14 @@ int sweep_periodic(lns_ctx3d* c, const lns::chain::Args& a, bool xi_marks, cudaS
       const long long pts = (long long)a.n * a.nsys;
       const int cta = (a.nsys + ch::kPairLines - 1) / ch::kPairLines;
       const size_t sm = ch::pair_smem_bytes();
-      const unsigned eb = (unsigned)((5LL * ((a.n - 3) / 2) * a.nsys + 255) / 256);
+      const int rows = (a.n - 3) / 2;  // even band rows 2..n-3
+      const unsigned eb = (unsigned)((5LL * rows * a.nsys + 255) / 256);
       ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
       int rc = mark(c, st);
-      ch::even_kernel<false><<<eb, 256, 0, st>>>(a);
+      ch::even_kernel<false><<<eb, 256, 0, st>>>(a, 2, rows);
       ch::pair_chain_kernel<false><<<cta, 128 * ch::kPairLines, sm, st>>>(a);
       if (!rc) rc = mark(c, st);
-      ch::even_kernel<true><<<eb, 256, 0, st>>>(a);
+      ch::even_kernel<true><<<eb, 256, 0, st>>>(a, 2, rows);
       ch::pair_chain_kernel<true><<<cta, 128 * ch::kPairLines, sm, st>>>(a);
       if (!rc && xi_marks) rc = mark(c, st);
       ch::btail_kernel<T><<<(a.nsys + ch::kBTailLines - 1) / ch::kBTailLines, 32 * ch::kBTailLines, 0, st>>>(a);
@@ -1080,6 +1083,24 @@ int sweep_y(lns_ctx3d* c, T* r, cudaStream_t st) {
   namespace ch = lns::chain;
   const ch::Args a = yargs(c, r);
   if (c->g.yper) return sweep_periodic<T>(c, a, false, st);
+  if constexpr (std::is_same<T, cd>::value) {
+    if (a.pairs) {  // rows in pairs: forward second rows even, backward ones odd
+      const long long pts = (long long)a.n * a.nsys;
+      const int cta = (a.nsys + ch::kPairLines - 1) / ch::kPairLines, rows = a.n / 2;
+      const size_t sm = ch::pair_smem_bytes();
+      const unsigned eb = (unsigned)((5LL * rows * a.nsys + 255) / 256);
+      ch::scale_kernel<T><<<(unsigned)ch::scale_blocks(pts), 256, 0, st>>>(a);
+      int rc = mark(c, st);
+      ch::even_kernel<false><<<eb, 256, 0, st>>>(a, 2, rows);
+      ch::pair_chain_kernel<false, true><<<cta, 128 * ch::kPairLines, sm, st>>>(a);
+      if (!rc) rc = mark(c, st);
+      ch::even_kernel<true><<<eb, 256, 0, st>>>(a, 1, rows);
+      ch::pair_chain_kernel<true, true><<<cta, 128 * ch::kPairLines, sm, st>>>(a);
+      if (rc) return rc;
+      cudaError_t e = cudaGetLastError();
+      return e == cudaSuccess ? LNS_OK : cuda3(e, "paired eta sweep launch");
+    }
+  }
   const long long pts = (long long)a.n * a.nsys;
   const int cta = (a.nsys + ch::kChainWarps - 1) / ch::kChainWarps;
   const size_t sm = ch::chain_smem_bytes<T>();
@@ -1166,9 +1187,13 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
   if (!rc && g.xper) rc = form_border<TC>(c, xargs(c, scratch), st);
   if (!rc && g.yper) rc = form_border<TC>(c, yargs(c, scratch), st);
   if (rc) return rc;
-  // FP64 periodic lines whose band has an odd number of rows: the paired form
+  // FP64 lines in the paired form, where the row count allows it and the
+  // lines are few: with four warps a line the pairs pay while a direction's
+  // lines leave the SMs' sub-partitions at most two warps each (more lines
+  // already fill the FP64 pipes row by row, and pairs only add instructions)
   if constexpr (std::is_same<TC, cd>::value) {
-    if (c->pair_ok && g.xper && (g.nx - 3) % 2 == 1) {
+    const bool few_x = g.ny <= 2 * c->sms, few_y = g.nx <= 2 * c->sms;
+    if (c->pair_ok && few_x && g.xper && (g.nx - 3) % 2 == 1) {
       if (!c->pairx) rc = dalloc(c, sizeof(cd) * 50 * (size_t)c->np, &c->pairx);
       if (!rc) {
         ch::Args pa = xargs(c, nullptr);
@@ -1179,7 +1204,18 @@ int factor_all(lns_ctx3d* c, cudaStream_t st) {
         c->paired_x = true;
       }
     }
-    if (!rc && c->pair_ok && g.yper && (g.ny - 3) % 2 == 1) {
+    if (!rc && c->pair_ok && few_y && !g.yper && g.ny % 2 == 0) {  // eta lines with boundary-closure rows
+      if (!c->pairy) rc = dalloc(c, sizeof(cd) * 50 * (size_t)c->np, &c->pairy);
+      if (!rc) {
+        ch::Args pa = yargs(c, nullptr);
+        pa.pairs = c->pairy;
+        const long long tasks = (long long)pa.n * pa.nsys;
+        ch::pair_prep_bc_kernel<<<(unsigned)((tasks + ch::kPrepWarps - 1) / ch::kPrepWarps), 32 * ch::kPrepWarps, 0,
+                                  st>>>(pa);
+        c->paired_y = true;
+      }
+    }
+    if (!rc && c->pair_ok && few_y && g.yper && (g.ny - 3) % 2 == 1) {
       if (!c->pairy) rc = dalloc(c, sizeof(cd) * 50 * (size_t)c->np, &c->pairy);
       if (!rc) {
         ch::Args pa = yargs(c, nullptr);
@@ -1319,6 +1355,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   lns_ctx3d* c = new lns_ctx3d();
   c->prm = *p;
   cudaError_t e = cudaGetDevice(&c->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
   if (e != cudaSuccess) {
     delete c;
     return cuda3(e, "cudaGetDevice");

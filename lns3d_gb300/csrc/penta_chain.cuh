@@ -639,6 +639,14 @@ __device__ __forceinline__ void chain_bwd_any(const Args& a, int bx, unsigned ch
 // even_kernel forms s' before the forward and c' before the backward pairs
 // (point-parallel, one thread per entry).  Used when the band has an odd
 // number of rows (top = n - 2 odd).
+//
+// Lines with boundary-closure rows (top = n even) pair the same way, upwards
+// (1, 2) ... (n-1, n) and downwards (n, n-1) ... (2, 1), so the forward
+// second rows are even and the backward ones odd.  Their end rows reach one
+// row further: row n-1 has F3 and row n becomes G, H and J = F4 - F1 F3'
+// (block 3) on the rows of the previous pair and of the one before; row 2
+// has B3 and row 1 becomes G', H' and J' = B4 - B1 B3' (block 1).  Rows 2
+// and n-1 keep their blocks (their products meet zero rows only).
 constexpr int kPairAhead = 6;         // pairs staged ahead
 constexpr int kPStage = 2 * kStage;   // a pair's two staged rows
 constexpr int kPXchg = 40;            // 2 parities x 2 rows x 2 parts x 5 components (doubles)
@@ -686,20 +694,81 @@ __global__ void __launch_bounds__(32 * kPrepWarps) pair_prep_kernel(Args a) {
   }
 }
 
-// The even band rows' right-hand sides before a paired recurrence:
+// Lines with boundary-closure rows (n even): one warp per record, the even
+// rows' forward and the odd rows' backward blocks combined (above), each
+// row's own F1 (even) or B1 (odd) into the pair array.  A row writes only
+// blocks its neighbours' combinations do not read.
+__global__ void __launch_bounds__(32 * kPrepWarps) pair_prep_bc_kernel(Args a) {
+  __shared__ cd sm[kPrepWarps][6 * 25];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int n = a.n;
+  const long long task = (long long)blockIdx.x * kPrepWarps + warp;
+  if (task >= (long long)n * a.nsys) return;
+  const int iv = (int)(task / n), r = (int)(task % n) + 1;
+  cd* chn = reinterpret_cast<cd*>(a.chn);
+  cd* rr = chn + 125 * rec_of(a, r, iv);
+  cd* pr = reinterpret_cast<cd*>(a.pairs) + 50 * rec_of(a, r, iv);
+  const int m = lane % 5, q = lane / 5;
+  cd* A = sm[warp];  // own first block (F1 or B1)
+  cd *X = A + 25, *Y = A + 50, *Z = A + 75, *U = A + 100, *V = A + 125;
+  const bool act = lane < 25;
+  if (r % 2 == 0) {
+    // forward: own F1 at block 1; the odd row below: F1 (25), F2 (50), F3 (100 on row n-1)
+    if (act) pr[lane] = rr[25 + lane];
+    if (r == 2) return;
+    const cd* lo = chn + 125 * rec_of(a, r - 1, iv);
+    if (act) {
+      A[lane] = rr[25 + lane];
+      X[lane] = lo[25 + lane], Y[lane] = lo[50 + lane], Z[lane] = r == n ? lo[100 + lane] : cd{0.0, 0.0};
+      U[lane] = rr[50 + lane];                                  // F2
+      V[lane] = r == n ? rr[75 + lane] : cd{0.0, 0.0};          // F3 of row n
+    }
+    const cd F4 = (act && r == n) ? rr[100 + lane] : cd{0.0, 0.0};
+    __syncwarp();
+    if (act) {
+      const cd g = sub(U[lane], mm5(A, X, m, q, false));
+      const cd h = sub(V[lane], mm5(A, Y, m, q, false));      // row n: F3 - F1 F2'; else -F1 F2'
+      rr[25 + lane] = g;
+      rr[50 + lane] = h;
+      if (r == n) rr[75 + lane] = sub(F4, mm5(A, Z, m, q, false));  // J
+    }
+  } else {
+    // backward: own B1 at block 3; the even row above: B1 (75), B2 (100), B3 (50 on row 2)
+    if (act) pr[25 + lane] = rr[75 + lane];
+    if (r == n - 1) return;
+    const cd* hi = chn + 125 * rec_of(a, r + 1, iv);
+    if (act) {
+      A[lane] = rr[75 + lane];
+      X[lane] = hi[75 + lane], Y[lane] = hi[100 + lane], Z[lane] = r == 1 ? hi[50 + lane] : cd{0.0, 0.0};
+      U[lane] = rr[100 + lane];                                 // B2
+      V[lane] = r == 1 ? rr[25 + lane] : cd{0.0, 0.0};          // B3 of row 1
+    }
+    const cd B4 = (act && r == 1) ? rr[50 + lane] : cd{0.0, 0.0};
+    __syncwarp();
+    if (act) {
+      const cd g = sub(U[lane], mm5(A, X, m, q, false));
+      const cd h = sub(V[lane], mm5(A, Y, m, q, false));      // row 1: B3 - B1 B2'; else -B1 B2'
+      rr[75 + lane] = g;
+      rr[100 + lane] = h;
+      if (r == 1) rr[25 + lane] = sub(B4, mm5(A, Z, m, q, false));  // J'
+    }
+  }
+}
+
+// The second rows' right-hand sides before a paired recurrence:
 // s'_j = s_j - F1_j s_{j-1} (UP = false) or c'_j = c_j - B1_j c_{j+1}
-// (UP = true), 2 <= j <= n-3; one thread per entry, only even rows written.
+// (UP = true) on rows j = first, first + 2, ... (rows per line); one thread
+// per entry, only those rows written.
 template <bool UP>
-__global__ void even_kernel(Args a) {
+__global__ void even_kernel(Args a, int first, int rows) {
   const long long t5 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long t = t5 / 5;
   const int mm = (int)(t5 - 5 * t);
-  const int rows = (a.n - 3) / 2;
   if (t >= (long long)rows * a.nsys) return;
   int k, iv;
   if (a.row_stride == 1) k = (int)(t % rows), iv = (int)(t / rows);
   else iv = (int)(t % a.nsys), k = (int)(t / a.nsys);
-  const long long rj = rec_of(a, 2 * k + 2, iv);
+  const long long rj = rec_of(a, first + 2 * k, iv);
   cd* grhs = reinterpret_cast<cd*>(a.rhs);
   const cd* B = reinterpret_cast<const cd*>(a.pairs) + 50 * rj + (UP ? 25 : 0);
   const cd* nb = grhs + 5 * (UP ? rj + a.row_stride : rj - a.row_stride);
@@ -730,7 +799,7 @@ __device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 1
 // chain2: lane (m, q), a three-level tree of DADD), and the four post their
 // parts to a shared exchange slot and meet at the line's named barrier, which
 // also publishes the rows the team staged.
-template <int W, int P, int C, bool DOWN>
+template <int W, int P, int C, bool DOWN, bool BC>
 __device__ __forceinline__ void pair_body(const Args& a, int bx, unsigned char* smem_raw) {
   constexpr int kRing = kPairAhead + 1;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -740,12 +809,20 @@ __device__ __forceinline__ void pair_body(const Args& a, int bx, unsigned char* 
   const int bar = 1 + ln;
   cd* ring = reinterpret_cast<cd*>(smem_raw) + ln * kRing * kPStage;
   double* xch = reinterpret_cast<double*>(reinterpret_cast<cd*>(smem_raw) + W * kRing * kPStage) + ln * kPXchg;
-  const int top = a.n - 2, npair = (top + 1) / 2;
+  const int top = BC ? a.n : a.n - 2, npair = (top + 1) / 2;
   const int m = lane % 5, qq = min(lane / 5, 4), l = min(lane, 24);
   double* grhs = reinterpret_cast<double*>(a.rhs);
   const cd* grc = reinterpret_cast<const cd*>(a.rhs);
   const cd* gchn = reinterpret_cast<const cd*>(a.chn);
   cd* const rend = ring + kRing * kPStage;
+  // the end pair's third block (BC): forward rows n-1 (F3, block 4) and n
+  // (J, block 3); backward rows 2 (B3, block 2) and 1 (J', block 1)
+  const cd* g3 = nullptr;
+  if (BC) {
+    const int r3 = DOWN ? 2 - P : a.n - 1 + P;
+    const int b3 = DOWN ? (P ? 25 : 50) : (P ? 75 : 100);
+    g3 = gchn + 125 * rec_of(a, r3, iv) + b3;
+  }
   const long long rs = a.row_stride, base = a.line_stride * (long long)iv;
   const long long step = DOWN ? -2 * rs : 2 * rs;              // records per pair
   const long long dr = DOWN ? -rs : rs;                       // the pair's second row
@@ -762,6 +839,7 @@ __device__ __forceinline__ void pair_body(const Args& a, int bx, unsigned char* 
   const cd* st = ring;
   double* out = grhs + 2 * (5 * (base + rs * (DOWN ? top - 1 - P : P)) + qq) + C;
   cd z1{0.0, 0.0}, z2{0.0, 0.0};  // the previous pair's rows: second, first (component qq)
+  cd z3{0.0, 0.0};                // the second row of the pair before (BC end rows)
   for (int k = 0; k < npair; ++k) {
     if (k + kPairAhead < npair) pair_stage(ws, gchn, grc, srec, srec + dr, off, 2 * (k + kPairAhead) + 2 <= top, t);
     cp_async_commit();
@@ -771,6 +849,7 @@ __device__ __forceinline__ void pair_body(const Args& a, int bx, unsigned char* 
     const cd* rw = st + P * kStage;
     double p = 0.0;
     if (lane < 5) p = C ? rw[50 + lane].y : rw[50 + lane].x;
+    if (BC && k == npair - 1) p = part_msub<C>(p, g3[l], z3);
     p = part_msub<C>(p, rw[25 + l], z2);
     p = part_msub<C>(p, rw[l], z1);
     const double yc = tree5(p, qq);
@@ -785,26 +864,28 @@ __device__ __forceinline__ void pair_body(const Args& a, int bx, unsigned char* 
     cp_async_wait<kPairAhead - 1>();  // this thread's part of the next pair
     team_sync(bar);
     const double* x = xch + par * 20 + qq;
+    z3 = z1;
     z2 = cd{x[0], x[5]};    // first row of the pair
     z1 = cd{x[10], x[15]};  // second row
   }
   cp_async_wait<0>();
 }
 
-template <int W, bool DOWN>
+template <int W, bool DOWN, bool BC>
 __device__ __forceinline__ void pair_any(const Args& a, int bx, unsigned char* smem_raw) {
   switch ((threadIdx.x / 32) & 3) {
-    case 0: pair_body<W, 0, 0, DOWN>(a, bx, smem_raw); break;
-    case 1: pair_body<W, 0, 1, DOWN>(a, bx, smem_raw); break;
-    case 2: pair_body<W, 1, 0, DOWN>(a, bx, smem_raw); break;
-    default: pair_body<W, 1, 1, DOWN>(a, bx, smem_raw); break;
+    case 0: pair_body<W, 0, 0, DOWN, BC>(a, bx, smem_raw); break;
+    case 1: pair_body<W, 0, 1, DOWN, BC>(a, bx, smem_raw); break;
+    case 2: pair_body<W, 1, 0, DOWN, BC>(a, bx, smem_raw); break;
+    default: pair_body<W, 1, 1, DOWN, BC>(a, bx, smem_raw); break;
   }
 }
-// Launch with 128 * W threads and pair_smem_bytes(W) bytes.
-template <bool DOWN, int W = kPairLines>
+// Launch with 128 * W threads and pair_smem_bytes(W) bytes.  BC: lines with
+// boundary-closure rows (n even) instead of periodic ones.
+template <bool DOWN, bool BC = false, int W = kPairLines>
 __global__ void __launch_bounds__(128 * W) pair_chain_kernel(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  pair_any<W, DOWN>(a, blockIdx.x, smem_raw);
+  pair_any<W, DOWN, BC>(a, blockIdx.x, smem_raw);
 }
 
 // Launch with chain_threads<T>(W) threads and chain_smem_bytes<T>(W) bytes.

@@ -202,15 +202,16 @@ def test_rejects_bad_arguments(cuda, small):
         drv.lhs(3, torch.zeros(125 * 40 * 33, dtype=torch.complex128, device="cuda"))
 
 
-@pytest.mark.parametrize("nx", [40, 41])
-def test_row_pairs_agree_with_row_by_row(cuda, nx):
-    """Periodic xi lines advanced two rows per step (nx even: an odd band)
-    and row by row agree to rounding, and both with the oracle; nx odd has
-    an even band and stays row by row whatever the switch says."""
+@pytest.mark.parametrize("nx,ny", [(40, 24), (41, 24), (40, 25), (41, 25)])
+def test_row_pairs_agree_with_row_by_row(cuda, nx, ny):
+    """Lines advanced two rows per step -- periodic xi lines when nx is even
+    (an odd band), eta lines with boundary-closure rows when ny is even --
+    and row by row agree to rounding, and both with the oracle; with nx and
+    ny odd every line stays row by row whatever the switch says."""
     from lns3d_gb300 import ImpDrv3D
     from lns3d_gb300.cases import shear_layer
 
-    case = shear_layer(nx=nx, ny=24, seed=9)
+    case = shear_layer(nx=nx, ny=ny, seed=9)
     orc = Oracle3D(case, cflmax=20.0, loctime=1)
     mk = lambda pairs: ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=20.0, loctime=1,
                                 row_pairs=pairs)
@@ -218,7 +219,7 @@ def test_row_pairs_agree_with_row_by_row(cuda, nx):
     rp = mk(True).step(vp, nsteps=5)
     rr = mk(False).step(vr, nsteps=5)
     ro = [orc.step(vo) for _ in range(5)]
-    if nx % 2:
+    if nx % 2 and ny % 2:
         assert np.array_equal(vp, vr) and np.array_equal(rp, rr)
     else:
         assert 0.0 < rel(vp, vr) < 1e-13
