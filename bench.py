@@ -65,25 +65,34 @@ PHASE_FLOPS = {"xsweep": 8 * 175, "ysweep": 8 * 125}
 #            (about 510 FMA: operator products 200, derivatives 240, viscous
 #            and 3D terms 50, rbe and residual 20)
 #   x_scale  D^-1 400 B + r read and write 160 B            (25 complex FMA)
-#   x_fwd    F1, F2 800 B + s read 80 B + yh write 80 B     (50 complex FMA)
-#   x_bwd    B1, B2 800 B + c read 80 B + x write 80 B      (50 complex FMA)
+#   x_fwd    the xi lines in row pairs: the even rows' pass (F1 400 B, two
+#            right-hand sides read and one written, on half the rows: 320 B,
+#            12.5 complex FMA) + the paired recurrence (two blocks 800 B + s
+#            read 80 B + yh write 80 B, 50 complex FMA)
+#   x_bwd    as x_fwd with B1 and the backward blocks
 #   x_fill   the periodic border: W 800 B + x read, write 160 B (50 complex
 #            FMA), and per line S^-1, A21 (the border unknowns)
-#   y_*      as x without the border
+#   y_*      row by row: two blocks 800 B + 160 B (50 complex FMA); the
+#            scaling as x_scale
 #   update   v read, write 160 B + r 80 B
-KERNEL_BYTES = {"rhs": 1304, "x_scale": 560, "x_fwd": 960, "x_fill": 960, "x_bwd": 960, "y_scale": 560,
+KERNEL_BYTES = {"rhs": 1304, "x_scale": 560, "x_fwd": 1280, "x_fill": 960, "x_bwd": 1280, "y_scale": 560,
                 "y_fwd": 960, "y_bwd": 960, "update": 240}
-KERNEL_FLOPS = {"rhs": 1020, "x_scale": 200, "x_fwd": 400, "x_fill": 400, "x_bwd": 400, "y_scale": 200,
+KERNEL_FLOPS = {"rhs": 1020, "x_scale": 200, "x_fwd": 500, "x_fill": 400, "x_bwd": 500, "y_scale": 200,
                 "y_fwd": 400, "y_bwd": 400}
-KERNEL_NAMES = {"x_fwd": "chain_fwd_kernel<cd, periodic> (xi forward recurrence)",
-                "x_bwd": "chain_bwd_kernel<cd, periodic> (xi backward recurrence)",
+KERNEL_NAMES = {"x_fwd": "even_kernel<0> + pair_chain_kernel<0, 0> (xi forward recurrence in row pairs)",
+                "x_bwd": "even_kernel<1> + pair_chain_kernel<1, 0> (xi backward recurrence in row pairs)",
+                "y_fwd": "chain_fwd_kernel<cd, 0> (eta forward recurrence)",
+                "y_bwd": "chain_bwd_kernel<cd, 0> (eta backward recurrence)",
                 "rhs": "grad1_kernel + rhs_kernel + resid_kernel"}
 # DRAM bytes (read + write) per launch from ncu captures on this workload:
-# the forward recurrence from profiles/chain_kernels_cd_xsweep_512x256.md,
-# the backward ones from profiles/chain_bwd_kernel_cd_sweeps_512x256.md
-KERNEL_TRAFFIC = {"x_fwd": 129.294080e6 + 5.967104e6, "x_bwd": 129.434624e6 + 5.784832e6,
+# the xi segments (even pass + paired recurrence) from
+# profiles/pair_chain_kernel_cd_xsweep_512x256.md, the eta backward
+# recurrence from profiles/chain_bwd_kernel_cd_sweeps_512x256.md
+KERNEL_TRAFFIC = {"x_fwd": 43.721984e6 + 6912 + 129.308928e6 + 2.872320e6,
+                  "x_bwd": 43.753728e6 + 1536 + 129.341696e6 + 2.977024e6,
                   "y_bwd": 130.674432e6 + 2.793728e6}
-KERNELS_PER_STEP = 14  # bc (predictor), grad1, rhs, resid, xi sweep (5), eta sweep (3), add, bc
+KERNELS_PER_STEP = 16  # bc (predictor), grad1, rhs, resid, xi sweep (7: scale, two even passes, two paired
+#                       recurrences, border, correction), eta sweep (3), add, bc
 # whole-step model of the linearised step with stored factors, per grid point
 # and step: RHS 1224 B (v, vold 160 B, frozen operators 984 B, r 80 B), xi
 # sweep 2160 B (factors 2000 B, r read and write 160 B), eta sweep 2240 B
