@@ -548,6 +548,13 @@ int lns_server3d_poll(lns_server3d* server, int64_t id, int32_t* state, int32_t*
  * failed request returns LNS_ERR_ARG and is forgotten too. */
 int lns_server3d_fetch(lns_server3d* server, int64_t id, double* v);
 size_t lns_server3d_bytes_in_use(const lns_server3d* server);
+/* How many times the server has captured its step as a CUDA graph (a
+ * diagnostic, no reference counterpart).  The batched kernels are
+ * persistent grids over work tables in device memory, so requests joining
+ * and leaving rewrite the tables and leave the captured step in place; it is
+ * captured again only when a table outgrows its buffer or the stencil width
+ * of the running requests changes. */
+int32_t lns_server3d_graph_captures(const lns_server3d* server);
 
 #ifdef __cplusplus
 }

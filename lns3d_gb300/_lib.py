@@ -89,6 +89,7 @@ SIGNATURES = {
     "lns_step_lin2d_dev": [P, DP, I32, I32, DP, P],
     "lns_ctx3d_profile": [P, I32],
     "lns_ctx3d_set_row_pairs": [P, I32],
+    "lns_server3d_graph_captures": [P],
     "lns_ctx3d_profile_read": [P, DP, P],
     "lns_batch3d_create": [I32, P, P],
     "lns_batch3d_destroy": [P],

@@ -336,6 +336,10 @@ class Server3D:
     def bytes_in_use(self):
         return lib().lns_server3d_bytes_in_use(self._s)
 
+    @property
+    def graph_captures(self):
+        return lib().lns_server3d_graph_captures(self._s)
+
     def close(self):
         if self._s:
             lib().lns_server3d_destroy(self._s)

@@ -14,6 +14,7 @@
 // RHS, residual and update stay FP64.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <deque>
@@ -723,71 +724,89 @@ struct StepArgs {
   double tol;    // the problem stops (active = 0) at the first residual <= tol; 0: never
 };
 
+// The batched kernels are persistent: a fixed grid strides over the phase's
+// work table, whose length (and the problem count) the kernels read from
+// device memory, so a captured step stays valid when the batch's problems
+// change and only the tables are rewritten.
 __global__ void copy_batch_kernel(const StepArgs* __restrict__ list, const int2* __restrict__ table,
-                                  const int* __restrict__ active) {
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  const StepArgs& a = list[w.x];
-  const long long e = (long long)w.y * blockDim.x + threadIdx.x;
-  if (e < 5 * a.o.np) a.vold[e] = a.v[e];
+                                  const int* __restrict__ active, const int* __restrict__ cnt) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int2 w = table[k];
+    if (!active[w.x]) continue;
+    const StepArgs& a = list[w.x];
+    const long long e = (long long)w.y * blockDim.x + threadIdx.x;
+    if (e < 5 * a.o.np) a.vold[e] = a.v[e];
+  }
 }
 __global__ void bc_batch_kernel(const StepArgs* __restrict__ list, const int2* __restrict__ table,
-                                const int* __restrict__ active) {
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, list[w.x].o.bump, list[w.x].o.tleft, w.y);
+                                const int* __restrict__ active, const int* __restrict__ cnt) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int2 w = table[k];
+    if (!active[w.x]) continue;
+    bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, list[w.x].o.bump, list[w.x].o.tleft, w.y);
+  }
 }
 __global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4* __restrict__ table,
-                                   const int* __restrict__ active) {
-  const int4 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  const StepArgs& a = list[w.x];
-  grad1_body(a.g, a.v, a.c1v, w.y, w.z);
+                                   const int* __restrict__ active, const int* __restrict__ cnt) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int4 w = table[k];
+    if (!active[w.x]) continue;
+    const StepArgs& a = list[w.x];
+    grad1_body(a.g, a.v, a.c1v, w.y, w.z);
+  }
 }
 template <bool NARROW>
 __global__ void __launch_bounds__(128, 4) rhs_batch_kernel(const StepArgs* __restrict__ list,
                                                         const int4* __restrict__ table,
-                                                        const int* __restrict__ active, int mixed) {
-  const int4 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  const StepArgs& a = list[w.x];
-  rhs_body<NARROW>(a.g, a.o, a.v, a.v, a.vold, nullptr, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr,
-                   a.part, w.y, w.z, a.nbx);
-}
-// residual of each problem into hist[step * P + p] (src/resstat3d.f90:37-60)
-// A problem whose residual reaches its tolerance is switched off here, so
-// the rest of this step and later steps leave its state as it was when the
-// residual was measured.
-__global__ void resid_batch_kernel(const StepArgs* __restrict__ list, int* active, double* __restrict__ hist,
-                                   const int* __restrict__ step, int P) {
-  __shared__ double red[256];
-  const int p = blockIdx.x;
-  if (!active[p]) return;
-  const StepArgs& a = list[p];
-  double s = 0.0;
-  for (int k = threadIdx.x; k < a.nrhs; k += blockDim.x) s += a.part[k];
-  red[threadIdx.x] = s;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
+                                                        const int* __restrict__ active, const int* __restrict__ cnt,
+                                                        int mixed) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int4 w = table[k];
+    if (!active[w.x]) continue;
+    const StepArgs& a = list[w.x];
+    rhs_body<NARROW>(a.g, a.o, a.v, a.v, a.vold, nullptr, a.c1v, mixed ? nullptr : a.r64, mixed ? a.r32 : nullptr,
+                     a.part, w.y, w.z, a.nbx);
   }
-  if (threadIdx.x == 0) {
-    const double r = sqrt(red[0] / (double)a.o.np);
-    hist[(long long)(*step) * P + p] = r;
-    if (a.tol > 0.0 && r <= a.tol) active[p] = 0;
+}
+// residual of each problem into hist[step * P + p] (src/resstat3d.f90:37-60),
+// P = *nprob.  A problem whose residual reaches its tolerance is switched off
+// here, so the rest of this step and later steps leave its state as it was
+// when the residual was measured.
+__global__ void resid_batch_kernel(const StepArgs* __restrict__ list, int* active, double* __restrict__ hist,
+                                   const int* __restrict__ step, const int* __restrict__ nprob) {
+  __shared__ double red[256];
+  const int P = *nprob;
+  for (int p = blockIdx.x; p < P; p += gridDim.x) {
+    if (!active[p]) continue;
+    const StepArgs& a = list[p];
+    double s = 0.0;
+    for (int k = threadIdx.x; k < a.nrhs; k += blockDim.x) s += a.part[k];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double r = sqrt(red[0] / (double)a.o.np);
+      hist[(long long)(*step) * P + p] = r;
+      if (a.tol > 0.0 && r <= a.tol) active[p] = 0;
+    }
+    __syncthreads();  // red is refilled for the next problem
   }
 }
 template <typename RT>
 __global__ void add_batch_kernel(const StepArgs* __restrict__ list, const int2* __restrict__ table,
-                                 const int* __restrict__ active) {
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  const StepArgs& a = list[w.x];
-  const long long e = (long long)w.y * blockDim.x + threadIdx.x;
-  if (e >= 5 * a.o.np) return;
-  const RT* r = reinterpret_cast<const RT*>(std::is_same<RT, cd>::value ? (const void*)a.r64 : (const void*)a.r32);
-  a.v[e] = add(a.v[e], to_hi(r[e]));
+                                 const int* __restrict__ active, const int* __restrict__ cnt) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int2 w = table[k];
+    if (!active[w.x]) continue;
+    const StepArgs& a = list[w.x];
+    const long long e = (long long)w.y * blockDim.x + threadIdx.x;
+    if (e >= 5 * a.o.np) continue;
+    const RT* r = reinterpret_cast<const RT*>(std::is_same<RT, cd>::value ? (const void*)a.r64 : (const void*)a.r32);
+    a.v[e] = add(a.v[e], to_hi(r[e]));
+  }
 }
 __global__ void step_incr_kernel(int* step) { *step += 1; }
 
@@ -1774,13 +1793,24 @@ struct lns_batch3d {
   int* d_step = nullptr;
   double* d_hist = nullptr;
   long long hist_cap = 0;  // entries (steps x problems)
+  // the work tables of the phases (kTables of them), each in a buffer that
+  // only grows; their lengths and the problem count in d_cnt
   int2 *t_elem = nullptr, *t_col = nullptr, *t_sx = nullptr, *t_fx = nullptr, *t_tx = nullptr, *t_lx = nullptr,
        *t_sy = nullptr, *t_fy = nullptr;
   int4* t_pts = nullptr;
-  int n_elem = 0, n_col = 0, n_sx = 0, n_fx = 0, n_tx = 0, n_lx = 0, n_sy = 0, n_fy = 0, n_pts = 0;
+  int t_cap[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // entries each table buffer holds
+  int* d_cnt = nullptr;  // [0..8] table lengths (kCnt*), [9] problems
+  int* d_next = nullptr;  // the recurrences' entry counters, four per corrector
+  int next_cap = 0;
+  int sms = 0;           // the device's SMs
+  // persistent grids (CTAs) of the batched kernels, as many as stay resident
+  unsigned g_elem = 0, g_col = 0, g_pts = 0, g_rhs = 0, g_res = 0, g_scale = 0, g_chain = 0, g_tail = 0,
+           g_fill = 0;
   cudaGraphExec_t exec = nullptr;
   int exec_W = 0, exec_niter = 0;
-  std::vector<void*> table_allocs;  // freed when the tables are rebuilt
+  bool exec_narrow = true;
+  int captures = 0;      // step graphs captured so far
+  std::vector<void*> table_allocs;  // the table buffers
   std::vector<int> active;
   std::vector<bool> uploaded;
 };
@@ -1798,28 +1828,51 @@ int balloc(lns_batch3d* b, size_t bytes, void** out) {
   return LNS_OK;
 }
 
+// slots of the table lengths in lns_batch3d::d_cnt
+enum { kCntElem, kCntCol, kCntPts, kCntSx, kCntFx, kCntTx, kCntLx, kCntSy, kCntFy, kCntProb, kCnt };
+
+void drop_exec(lns_batch3d* b) {
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+}
+
+// Writes table `slot` into its buffer, growing the buffer (and dropping the
+// captured step, which holds the old address) when it is too small.
 template <typename E>
-int upload_table(lns_batch3d* b, const std::vector<E>& h, E** d, int* n) {
-  void* q = nullptr;
-  cudaError_t ea = cudaMalloc(&q, sizeof(E) * std::max<size_t>(h.size(), 1));
-  if (ea != cudaSuccess) return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(ea));
-  b->table_allocs.push_back(q);
-  cudaError_t e = cudaMemcpy(q, h.data(), sizeof(E) * h.size(), cudaMemcpyHostToDevice);
+int upload_table(lns_batch3d* b, const std::vector<E>& h, E** d, int slot, std::vector<int>& len) {
+  if ((int)h.size() > b->t_cap[slot] || !*d) {
+    const int cap = std::max(std::max((int)h.size(), 2 * b->t_cap[slot]), 1);
+    void* q = nullptr;
+    cudaError_t ea = cudaMalloc(&q, sizeof(E) * (size_t)cap);
+    if (ea != cudaSuccess) return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(ea));
+    if (*d) {
+      cudaFree(*d);
+      b->table_allocs.erase(std::find(b->table_allocs.begin(), b->table_allocs.end(), (void*)*d));
+    }
+    b->table_allocs.push_back(q);
+    *d = (E*)q;
+    b->t_cap[slot] = cap;
+    drop_exec(b);
+  }
+  cudaError_t e = cudaMemcpy(*d, h.data(), sizeof(E) * h.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda3(e, "upload work table");
-  *d = (E*)q;
-  *n = (int)h.size();
+  len[slot] = (int)h.size();
   return LNS_OK;
 }
 
 // The work tables of every phase, from the problems' sizes and the
-// recurrences' lines per CTA W.
+// recurrences' lines per CTA W, and their lengths; a captured step stays
+// valid unless a table buffer had to grow.
 int build_tables(lns_batch3d* b) {
-  if (b->exec) {  // the captured step refers to the tables being replaced
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
+  if (!b->d_cnt) {
+    cudaError_t e = cudaMalloc(&b->d_cnt, sizeof(int) * kCnt);
+    if (e != cudaSuccess) return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    b->table_allocs.push_back(b->d_cnt);
   }
-  for (void* q : b->table_allocs) cudaFree(q);
-  b->table_allocs.clear();
+  std::vector<int> len(kCnt, 0);
+  len[kCntProb] = b->P;
   std::vector<int2> te, tc, tsx, tfx, ttx, tlx, tsy, tfy;
   std::vector<int4> tp;
   for (int p = 0; p < b->P; ++p) {
@@ -1839,15 +1892,19 @@ int build_tables(lns_batch3d* b) {
     for (long long k = 0; k < lns::chain::scale_blocks(nyp); ++k) tsy.push_back(make_int2(p, (int)k));
     for (int k = 0; k < (g.nx + b->W - 1) / b->W; ++k) tfy.push_back(make_int2(p, k));
   }
-  int rc = upload_table(b, te, &b->t_elem, &b->n_elem);
-  if (!rc) rc = upload_table(b, tc, &b->t_col, &b->n_col);
-  if (!rc) rc = upload_table(b, tp, &b->t_pts, &b->n_pts);
-  if (!rc) rc = upload_table(b, tsx, &b->t_sx, &b->n_sx);
-  if (!rc) rc = upload_table(b, tfx, &b->t_fx, &b->n_fx);
-  if (!rc) rc = upload_table(b, ttx, &b->t_tx, &b->n_tx);
-  if (!rc) rc = upload_table(b, tlx, &b->t_lx, &b->n_lx);
-  if (!rc) rc = upload_table(b, tsy, &b->t_sy, &b->n_sy);
-  if (!rc) rc = upload_table(b, tfy, &b->t_fy, &b->n_fy);
+  int rc = upload_table(b, te, &b->t_elem, kCntElem, len);
+  if (!rc) rc = upload_table(b, tc, &b->t_col, kCntCol, len);
+  if (!rc) rc = upload_table(b, tp, &b->t_pts, kCntPts, len);
+  if (!rc) rc = upload_table(b, tsx, &b->t_sx, kCntSx, len);
+  if (!rc) rc = upload_table(b, tfx, &b->t_fx, kCntFx, len);
+  if (!rc) rc = upload_table(b, ttx, &b->t_tx, kCntTx, len);
+  if (!rc) rc = upload_table(b, tlx, &b->t_lx, kCntLx, len);
+  if (!rc) rc = upload_table(b, tsy, &b->t_sy, kCntSy, len);
+  if (!rc) rc = upload_table(b, tfy, &b->t_fy, kCntFy, len);
+  if (!rc) {
+    cudaError_t e = cudaMemcpy(b->d_cnt, len.data(), sizeof(int) * kCnt, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda3(e, "upload table lengths");
+  }
   return rc;
 }
 
@@ -1858,27 +1915,38 @@ int enqueue_step(lns_batch3d* b, int niter) {
   namespace ch = lns::chain;
   cudaStream_t st = b->st;
   const size_t sm = ch::chain_smem_bytes<T>(W);
-  bool narrow = true;  // every problem's stencils are five-point
-  for (int p = 0; p < b->P; ++p) narrow = narrow && a3::narrow_stencils(b->ctx[p]->g);
-  a3::copy_batch_kernel<<<b->n_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active);
-  a3::bc_batch_kernel<<<b->n_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active);
+  const bool narrow = b->exec_narrow;  // every problem's stencils are five-point
+  // persistent grids (set_grids), the tables' lengths in d_cnt, and the
+  // recurrences' entry counters cleared at the start of the step
+  const int* n = b->d_cnt;
+  cudaError_t em = cudaMemsetAsync(b->d_next, 0, sizeof(int) * 4 * niter, st);
+  if (em != cudaSuccess) return cuda3(em, "clear entry counters");
+  a3::copy_batch_kernel<<<b->g_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active, n + kCntElem);
+  a3::bc_batch_kernel<<<b->g_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active, n + kCntCol);
   for (int it = 0; it < niter; ++it) {
-    a3::grad1_batch_kernel<<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active);
+    int* next = b->d_next + 4 * it;
+    a3::grad1_batch_kernel<<<b->g_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, n + kCntPts);
     if (narrow)
-      a3::rhs_batch_kernel<true><<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, b->mixed ? 1 : 0);
+      a3::rhs_batch_kernel<true><<<b->g_rhs, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, n + kCntPts,
+                                                           b->mixed ? 1 : 0);
     else
-      a3::rhs_batch_kernel<false><<<b->n_pts, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, b->mixed ? 1 : 0);
-    a3::resid_batch_kernel<<<b->P, 256, 0, st>>>(b->d_args, b->d_active, b->d_hist, b->d_step, b->P);
-    ch::scale_batch_kernel<T><<<b->n_sx, 256, 0, st>>>(b->d_ax, b->t_sx, b->d_active);
-    ch::chain_fwd_batch_kernel<T, true, W><<<b->n_fx, ch::chain_threads<T>(W), sm, st>>>(b->d_ax, b->t_fx, b->d_active);
-    ch::chain_bwd_batch_kernel<T, true, W><<<b->n_fx, ch::chain_threads<T>(W), sm, st>>>(b->d_ax, b->t_fx, b->d_active);
-    ch::btail_batch_kernel<T><<<b->n_tx, 32 * ch::kBTailLines, 0, st>>>(b->d_ax, b->t_tx, b->d_active);
-    ch::fill_batch_kernel<T><<<b->n_lx, 256, 0, st>>>(b->d_ax, b->t_lx, b->d_active);
-    ch::scale_batch_kernel<T><<<b->n_sy, 256, 0, st>>>(b->d_ay, b->t_sy, b->d_active);
-    ch::chain_fwd_batch_kernel<T, false, W><<<b->n_fy, ch::chain_threads<T>(W), sm, st>>>(b->d_ay, b->t_fy, b->d_active);
-    ch::chain_bwd_batch_kernel<T, false, W><<<b->n_fy, ch::chain_threads<T>(W), sm, st>>>(b->d_ay, b->t_fy, b->d_active);
-    a3::add_batch_kernel<T><<<b->n_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active);
-    a3::bc_batch_kernel<<<b->n_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active);
+      a3::rhs_batch_kernel<false><<<b->g_rhs, 128, 0, st>>>(b->d_args, b->t_pts, b->d_active, n + kCntPts,
+                                                            b->mixed ? 1 : 0);
+    a3::resid_batch_kernel<<<b->g_res, 256, 0, st>>>(b->d_args, b->d_active, b->d_hist, b->d_step, n + kCntProb);
+    ch::scale_batch_kernel<T><<<b->g_scale, 256, 0, st>>>(b->d_ax, b->t_sx, b->d_active, n + kCntSx);
+    ch::chain_fwd_batch_kernel<T, true, W><<<b->g_chain, ch::chain_threads<T>(W), sm, st>>>(
+        b->d_ax, b->t_fx, b->d_active, n + kCntFx, next + 0);
+    ch::chain_bwd_batch_kernel<T, true, W><<<b->g_chain, ch::chain_threads<T>(W), sm, st>>>(
+        b->d_ax, b->t_fx, b->d_active, n + kCntFx, next + 1);
+    ch::btail_batch_kernel<T><<<b->g_tail, 32 * ch::kBTailLines, 0, st>>>(b->d_ax, b->t_tx, b->d_active, n + kCntTx);
+    ch::fill_batch_kernel<T><<<b->g_fill, 256, 0, st>>>(b->d_ax, b->t_lx, b->d_active, n + kCntLx);
+    ch::scale_batch_kernel<T><<<b->g_scale, 256, 0, st>>>(b->d_ay, b->t_sy, b->d_active, n + kCntSy);
+    ch::chain_fwd_batch_kernel<T, false, W><<<b->g_chain, ch::chain_threads<T>(W), sm, st>>>(
+        b->d_ay, b->t_fy, b->d_active, n + kCntFy, next + 2);
+    ch::chain_bwd_batch_kernel<T, false, W><<<b->g_chain, ch::chain_threads<T>(W), sm, st>>>(
+        b->d_ay, b->t_fy, b->d_active, n + kCntFy, next + 3);
+    a3::add_batch_kernel<T><<<b->g_elem, 256, 0, st>>>(b->d_args, b->t_elem, b->d_active, n + kCntElem);
+    a3::bc_batch_kernel<<<b->g_col, 128, 0, st>>>(b->d_args, b->t_col, b->d_active, n + kCntCol);
   }
   a3::step_incr_kernel<<<1, 1, 0, st>>>(b->d_step);
   cudaError_t e = cudaGetLastError();
@@ -1895,9 +1963,60 @@ int enqueue_step_w(lns_batch3d* b, int niter) {
   }
 }
 
-// (Re)captures the step as a graph for the current W and niter.
+// CTAs of kernel k with `threads` threads and `smem` dynamic bytes that stay
+// resident on the device at once (at least one per SM).
+template <typename K>
+unsigned resident(const lns_batch3d* b, K k, int threads, size_t smem) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, threads, smem) != cudaSuccess || nb < 1) nb = 1;
+  return (unsigned)(nb * b->sms);
+}
+
+// The persistent grids of the batched kernels for the precision T and lines
+// per CTA W, and room for the recurrences' entry counters.
+template <typename T, int W>
+int set_grids(lns_batch3d* b, int niter) {
+  namespace a3 = lns::a3;
+  namespace ch = lns::chain;
+  b->g_elem = resident(b, a3::add_batch_kernel<T>, 256, 0);
+  b->g_col = resident(b, a3::bc_batch_kernel, 128, 0);
+  b->g_pts = resident(b, a3::grad1_batch_kernel, 128, 0);
+  b->g_rhs = b->exec_narrow ? resident(b, a3::rhs_batch_kernel<true>, 128, 0)
+                            : resident(b, a3::rhs_batch_kernel<false>, 128, 0);
+  b->g_res = resident(b, a3::resid_batch_kernel, 256, 0);
+  b->g_scale = resident(b, ch::scale_batch_kernel<T>, 256, 0);
+  b->g_chain = resident(b, ch::chain_fwd_batch_kernel<T, true, W>, ch::chain_threads<T>(W), ch::chain_smem_bytes<T>(W));
+  b->g_tail = resident(b, ch::btail_batch_kernel<T>, 32 * ch::kBTailLines, 0);
+  b->g_fill = resident(b, ch::fill_batch_kernel<T>, 256, 0);
+  cudaGetLastError();  // an occupancy query that failed leaves no error behind
+  if (4 * niter > b->next_cap) {
+    if (b->d_next) cudaFree(b->d_next);
+    b->d_next = nullptr;
+    cudaError_t e = cudaMalloc(&b->d_next, sizeof(int) * 4 * niter);
+    if (e != cudaSuccess) return fail3(LNS_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    b->next_cap = 4 * niter;
+  }
+  return LNS_OK;
+}
+template <typename T>
+int set_grids_w(lns_batch3d* b, int niter) {
+  switch (b->W) {
+    case 1: return set_grids<T, 1>(b, niter);
+    case 2: return set_grids<T, 2>(b, niter);
+    case 4: return set_grids<T, 4>(b, niter);
+    default: return fail3(LNS_ERR_ARG, "batch: lines per CTA must be 1, 2 or 4");
+  }
+}
+
+// (Re)captures the step as a graph for the current W, niter and stencil
+// width; problems joining or leaving need none (the tables are rewritten).
 int capture(lns_batch3d* b, int niter) {
-  if (b->exec && b->exec_W == b->W && b->exec_niter == niter) return LNS_OK;
+  bool narrow = true;  // every problem's stencils are five-point
+  for (int p = 0; p < b->P; ++p) narrow = narrow && lns::a3::narrow_stencils(b->ctx[p]->g);
+  if (b->exec && b->exec_W == b->W && b->exec_niter == niter && b->exec_narrow == narrow) return LNS_OK;
+  b->exec_narrow = narrow;
+  int rg = b->mixed ? set_grids_w<cf>(b, niter) : set_grids_w<cd>(b, niter);
+  if (rg) return rg;
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
@@ -1915,6 +2034,7 @@ int capture(lns_batch3d* b, int niter) {
   e = cudaGraphInstantiate(&b->exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda3(e, "cudaGraphInstantiate");
+  ++b->captures;
   b->exec_W = b->W;
   b->exec_niter = niter;
   return LNS_OK;
@@ -1976,11 +2096,12 @@ int set_active(lns_batch3d* b) {
   return e == cudaSuccess ? LNS_OK : cuda3(e, "upload active flags");
 }
 
-// Residual history for `steps` steps of the current problems: the step
-// kernels write hist[step * P + p], so the capacity is counted in entries and
-// grows with the number of problems as well as with the steps.
-int reserve_hist(lns_batch3d* b, long long steps) {
-  const long long need = steps * (long long)b->P;
+// Residual history for `steps` steps of `probs` problems (default: the
+// current ones): the step kernels write hist[step * P + p], so the capacity
+// is counted in entries and grows with the number of problems as well as
+// with the steps.
+int reserve_hist(lns_batch3d* b, long long steps, int probs = -1) {
+  const long long need = steps * (long long)(probs < 0 ? b->P : probs);
   if (need <= b->hist_cap) return LNS_OK;
   void* q = nullptr;
   cudaError_t e = cudaStreamSynchronize(b->st);  // no step in flight writes the old buffer
@@ -2004,6 +2125,7 @@ int reserve_hist(lns_batch3d* b, long long steps) {
 void destroy_batch(lns_batch3d* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->d_hist) cudaFree(b->d_hist);
+  if (b->d_next) cudaFree(b->d_next);
   for (void* p : b->allocs) cudaFree(p);
   for (void* p : b->table_allocs) cudaFree(p);
   if (b->owns_ctx)
@@ -2036,6 +2158,7 @@ int lns_batch3d_create(int32_t nprob, const lns_params3d* params, lns_batch3d** 
   b->P = nprob;
   b->mixed = params[0].precision == LNS_MIXED;
   cudaError_t e = cudaGetDevice(&b->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
   if (e != cudaSuccess) {
     delete b;
     return cuda3(e, "cudaGetDevice");
@@ -2293,11 +2416,7 @@ int reform(lns_server3d* s) {
   for (int p = 0; p < b->P; ++p) args[p].tol = s->running[p]->tol;
   e = cudaMemcpy(b->d_args, args.data(), sizeof(args[0]) * b->P, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda3(e, "upload batch arguments");
-  rc = build_tables(b);
-  if (!rc && b->exec) {
-    cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-  }
+  rc = build_tables(b);  // keeps the captured step unless a table buffer grew
   if (!rc) rc = set_active(b);
   s->dirty = false;
   return rc;
@@ -2374,13 +2493,16 @@ int lns_server3d_create(size_t budget_bytes, int32_t max_slots, int32_t precisio
   b->mixed = precision == LNS_MIXED;
   int rc = LNS_OK;
   cudaError_t e = cudaGetDevice(&b->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
   if (e != cudaSuccess) rc = cuda3(e, "cudaGetDevice");
   void* q = nullptr;
   if (!rc) {
     e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) rc = cuda3(e, "cudaStreamCreate");
   }
-  if (!rc) rc = reserve_problems(b, std::min(max_slots, 64));
+  // the per-problem arrays for every slot at once, so that requests joining
+  // never move them (and the captured step stays valid)
+  if (!rc) rc = reserve_problems(b, max_slots);
   if (!rc) rc = balloc(b, sizeof(int), &q), b->d_step = (int*)q;
   if (rc) {
     destroy_batch(b);
@@ -2442,8 +2564,8 @@ int lns_server3d_tick(lns_server3d* s, int32_t nsteps, int32_t* running, int32_t
   if (b->P) {
     // no request runs past its step limit: the tick is cut to the fewest
     // steps any running request has left
+    rc = reserve_hist(b, nsteps, s->max_slots);  // sized for every slot: joins keep it
     for (const SrvReq* r : s->running) nsteps = std::min(nsteps, r->max_steps - r->steps);
-    rc = reserve_hist(b, nsteps);
     if (!rc) rc = capture(b, s->niter);
     if (rc) return rc;
     if ((long long)nsteps * b->P > b->hist_cap) return fail3(LNS_ERR_ARG, "server3d_tick: residual history too small");
@@ -2515,5 +2637,7 @@ int lns_server3d_fetch(lns_server3d* s, int64_t id, double* v) {
 }
 
 size_t lns_server3d_bytes_in_use(const lns_server3d* s) { return s ? s->used : 0; }
+
+int32_t lns_server3d_graph_captures(const lns_server3d* s) { return s && s->b ? s->b->captures : 0; }
 
 }  // extern "C"

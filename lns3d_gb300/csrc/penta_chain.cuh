@@ -244,14 +244,17 @@ __device__ __forceinline__ void scale_body(const Args& a, long long bx) {
 template <typename T>
 __global__ void scale_kernel(Args a) { scale_body<T>(a, blockIdx.x); }
 
-// Work tables of the batched launches: block b of a batched launch runs
-// block y of problem x (several problems in one launch, one ADI phase).
+// Work tables of the batched launches: entry k of a phase's table runs block
+// y of problem x (several problems in one launch, one ADI phase).  The
+// batched kernels are persistent: a fixed grid strides over the table, whose
+// length *cnt they read from device memory.
 template <typename T>
 __global__ void scale_batch_kernel(const Args* __restrict__ list, const int2* __restrict__ table,
-                                   const int* __restrict__ active) {
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  scale_body<T>(list[w.x], w.y);
+                                   const int* __restrict__ active, const int* __restrict__ cnt) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int2 w = table[k];
+    if (active[w.x]) scale_body<T>(list[w.x], w.y);
+  }
 }
 
 // kAhead: rows staged ahead of the recurrence.  kSplit: warps per line; the
@@ -899,23 +902,45 @@ __global__ void __launch_bounds__(chain_threads<T>(W)) chain_bwd_kernel(Args a) 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   chain_bwd_any<T, PER, W>(a, blockIdx.x, smem_raw);
 }
+// The recurrences' entries are lines of problems of different lengths, so
+// their CTAs take the next entry from a counter (*next, cleared before the
+// launch) rather than a fixed stride.  Each line's warps reuse their own
+// ring and exchange slots from entry to entry; the first barrier of an entry
+// orders them after the last reads of the previous one.
+__device__ __forceinline__ int next_entry(int* next, int* slot) {
+  if (threadIdx.x == 0) *slot = atomicAdd(next, 1);
+  __syncthreads();
+  const int k = *slot;
+  __syncthreads();  // every thread has read the slot before it is refilled
+  return k;
+}
 template <typename T, bool PER, int W>
 __global__ void __launch_bounds__(chain_threads<T>(W)) chain_fwd_batch_kernel(const Args* __restrict__ list,
                                                                              const int2* __restrict__ table,
-                                                                             const int* __restrict__ active) {
+                                                                             const int* __restrict__ active,
+                                                                             const int* __restrict__ cnt,
+                                                                             int* next) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  chain_fwd_any<T, PER, W>(list[w.x], w.y, smem_raw);
+  __shared__ int slot;
+  const int n = *cnt;
+  for (int k = next_entry(next, &slot); k < n; k = next_entry(next, &slot)) {
+    const int2 w = table[k];
+    if (active[w.x]) chain_fwd_any<T, PER, W>(list[w.x], w.y, smem_raw);
+  }
 }
 template <typename T, bool PER, int W>
 __global__ void __launch_bounds__(chain_threads<T>(W)) chain_bwd_batch_kernel(const Args* __restrict__ list,
                                                                              const int2* __restrict__ table,
-                                                                             const int* __restrict__ active) {
+                                                                             const int* __restrict__ active,
+                                                                             const int* __restrict__ cnt,
+                                                                             int* next) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  chain_bwd_any<T, PER, W>(list[w.x], w.y, smem_raw);
+  __shared__ int slot;
+  const int n = *cnt;
+  for (int k = next_entry(next, &slot); k < n; k = next_entry(next, &slot)) {
+    const int2 w = table[k];
+    if (active[w.x]) chain_bwd_any<T, PER, W>(list[w.x], w.y, smem_raw);
+  }
 }
 
 // ----------------------------------------------------- periodic border
@@ -1108,10 +1133,12 @@ __global__ void __launch_bounds__(32 * kBTailLines) btail_kernel(Args a) {
 template <typename T>
 __global__ void __launch_bounds__(32 * kBTailLines) btail_batch_kernel(const Args* __restrict__ list,
                                                                       const int2* __restrict__ table,
-                                                                      const int* __restrict__ active) {
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  btail_body<T>(list[w.x], w.y * kBTailLines + threadIdx.x / 32);
+                                                                      const int* __restrict__ active,
+                                                                      const int* __restrict__ cnt) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int2 w = table[k];
+    if (active[w.x]) btail_body<T>(list[w.x], w.y * kBTailLines + threadIdx.x / 32);
+  }
 }
 
 // Periodic lines, last: x_i = z_i - W_i x2 for rows 1..n-2 (and row np,
@@ -1149,10 +1176,11 @@ template <typename T>
 __global__ void fill_kernel(Args a) { fill_body<T>(a, blockIdx.x); }
 template <typename T>
 __global__ void fill_batch_kernel(const Args* __restrict__ list, const int2* __restrict__ table,
-                                  const int* __restrict__ active) {
-  const int2 w = table[blockIdx.x];
-  if (!active[w.x]) return;
-  fill_body<T>(list[w.x], w.y);
+                                  const int* __restrict__ active, const int* __restrict__ cnt) {
+  for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
+    const int2 w = table[k];
+    if (active[w.x]) fill_body<T>(list[w.x], w.y);
+  }
 }
 
 }  // namespace chain

@@ -97,3 +97,25 @@ def test_request_stops_exactly_at_max_steps(cuda):
     assert np.array_equal(srv.fetch(i), v)
     assert p["res"] == hist[-1]
     assert srv.poll(j)["steps"] == 40
+
+
+def test_joins_and_leaves_keep_the_captured_step(cuda):
+    """Eight same-size requests through four slots, leaving at different
+    steps: the ones queued join as slots free up, which rewrites the work
+    tables in place, so the step is captured once; each result equals a
+    lone run of the same request."""
+    from lns3d_gb300 import ImpDrv3D, Server3D
+
+    reqs = [case(40, 33, 0.05 * k, 0.02 + 0.01 * k, 20 + k) for k in range(8)]
+    limits = [12, 30, 18, 42, 24, 36, 6, 48]
+    srv = Server3D(1 << 33, max_slots=4)
+    ids = [srv.submit(c, tol=1e-30, max_steps=m, cflmax=20.0) for c, m in zip(reqs, limits)]
+    drain(srv, ids, nsteps=6)
+    assert srv.graph_captures == 1
+    for k in (0, 3, 7):
+        assert srv.poll(ids[k])["state"] == "stopped"
+        c = reqs[k]
+        drv = ImpDrv3D(c["params"], c["metrics"], c["vm"], cflmax=20.0, loctime=1, precision=1)
+        v = c["v"].copy(order="F")
+        drv.step(v, nsteps=limits[k])
+        assert np.array_equal(srv.fetch(ids[k]), v), k
