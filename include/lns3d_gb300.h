@@ -184,11 +184,18 @@ int lns_solve1p_dev(int32_t nsys, int32_t np, int32_t nblk, const double* mat, d
  * lhsbc2f and penta1bc (eta), v = v + r, itrBC.  The LHS is formed and
  * factored every corrector, as the reference does for the nonlinear
  * equations.
- * Supported options: xper = 1, yper = 0, a viscous wall at j = 1 (navier 1,
- * wall 0, 1 or 3, wallt 0 or 1) and the Riemann far field at j = ny (top 0;
- * held free stream when Ma > 1) or the held quiescent top (top 3, row ny held
- * at (1, 0, 0, 0, 1), fourth-order LHS only); constant viscosity; no sponge, damper or
- * smoother.  Arrays are Fortran-ordered: v(5,nx,ny), metrics(nx,ny,10),
+ * Supported options: a periodic xi direction (xper 1, penta2p), or a non-
+ * periodic one (xper 0, penta2bc along xi, the one-sided closure rows of
+ * src/lhsbt1f.f90) below Ma 1 with a Riemann far field (left 0, right 0;
+ * src/reimann.f90 on bnl / bnr and left.pot / right.pot) or a symmetry plane
+ * (left 2) on the left and first-order extrapolation of the right plane over
+ * the viscous layer (extrap, nbl, update_nbl: src/itrbc.f90:849-886,
+ * src/rhsbc.f90:461-476, src/lhsbc1f.f90:819-859); yper = 0, a viscous wall
+ * at j = 1 (navier 1, wall 0, 1 or 3, wallt 0 or 1) and the Riemann far
+ * field at j = ny (top 0; held free stream when Ma > 1) or the held
+ * quiescent top (top 3, row ny held at (1, 0, 0, 0, 1), fourth-order LHS
+ * only); constant viscosity; the sponge and the smoother as below; no
+ * damper.  Arrays are Fortran-ordered: v(5,nx,ny), metrics(nx,ny,10),
  * bnt(nx,2) (src/gengrid.f90:141-142), pot(5,nx) = the rho u v w T rows of
  * top.pot (src/potential.f90:22-26).
  */
@@ -221,6 +228,15 @@ typedef struct {
                                 src/lhsbt2f.f90:193-213) weighted by buff (ones until
                                 lns_upload_buffer2d); with lhs_order 2 the second-order damping
                                 of src/lhs.f90 and src/lhsbt2.f90. */
+  int32_t left, right;       /* xi planes when xper = 0: left 0 (Riemann) or 2 (symmetry plane),
+                                right 0 (Riemann); ignored when xper = 1 */
+  int32_t extrap;            /* -1 off, 0 or 1: the right plane extrapolated from its neighbours
+                                over rows 1..nbl (the viscous layer) */
+  int32_t nbl;               /* rows of the viscous layer before the first itrBC (the &extras
+                                namelist's nbl, default 0); 0 <= nbl <= ny */
+  int32_t update_nbl;        /* 1: every itrBC sets nbl to the first row whose u at column nx-1
+                                exceeds 0.99 (src/itrbc.f90:849-857); a state with no such row
+                                fails the step with LNS_ERR_ARG, where the reference stops */
 } lns_params2d;
 
 typedef struct lns_ctx2d lns_ctx2d;
@@ -233,6 +249,12 @@ size_t lns_ctx2d_bytes(const lns_ctx2d* ctx);
 int lns_upload_metrics2d(lns_ctx2d* ctx, const double* metrics);
 /* far field of the top boundary: unit normal bnt(nx,2) and top.pot (5,nx) */
 int lns_upload_top2d(lns_ctx2d* ctx, const double* bnt, const double* pot);
+/* far field of a xi plane (xper = 0): side 1 = left (bnl(ny,2), left.pot
+ * (5,ny)), 2 = right (bnr(ny,2), right.pot (5,ny)); the unit outward
+ * normals of src/gengrid.f90:145-155 and the rho u v w T rows of
+ * src/potential.f90:36-72.  Needed before the first step for a Riemann
+ * plane (left 0, right 0). */
+int lns_upload_side2d(lns_ctx2d* ctx, int32_t side, const double* bn, const double* pot);
 /* The sponge arrays spg(nx,ny), spg2(nx,ny) (src/sponge.f90) when ispg = 2;
  * needed before the first step. */
 int lns_upload_sponge2d(lns_ctx2d* ctx, const double* spg, const double* spg2);

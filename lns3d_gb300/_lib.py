@@ -107,6 +107,7 @@ SIGNATURES = {
     "lns_ctx2d_destroy": [P],
     "lns_upload_metrics2d": [P, DP],
     "lns_upload_top2d": [P, DP, DP],
+    "lns_upload_side2d": [P, I32, DP, DP],
     "lns_itrbc2d_dev": [P, DP, P],
     "lns_step2d": [P, DP, I32, I32, DP],
     "lns_step2d_dev": [P, DP, I32, I32, DP, P],
@@ -124,7 +125,8 @@ class Params2D(ctypes.Structure):
                 ("cflmax", ctypes.c_double), ("dtmax", ctypes.c_double), ("theta", ctypes.c_double), ("loctime", I32), ("xper", I32),
                 ("yper", I32), ("navier", I32), ("wall", I32), ("wallt", I32), ("top", I32), ("optx", I32),
                 ("opty", I32), ("lhs_order", I32), ("impl", I32), ("ispg", I32),
-                ("eps_e", ctypes.c_double)]
+                ("eps_e", ctypes.c_double), ("left", I32), ("right", I32), ("extrap", I32), ("nbl", I32),
+                ("update_nbl", I32)]
 
 
 class Params3D(ctypes.Structure):

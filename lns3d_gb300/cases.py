@@ -212,3 +212,45 @@ def acoustic_box(nx=64, ny=63, Lx=1.0, Ly=1.0, Lz=1.0, Ma=1.0, Pr=1.0):
                   gamma1=GAMMA1, omega=0.0, kz=kz_of(Lz), alfa=1.0, xper=1, yper=1, navier=0, wall=-1, wallt=-1,
                   top=-1, optx=-1, opty=-1)
     return dict(params=params, x=x, y=y, metrics=metrics, vm=vm, v=v, span=Lz)
+
+
+def boundary_normals(metrics):
+    """The unit outward normals of the four boundaries as src/gengrid.f90:
+    133-155 forms them from the metrics: bnb (nx, 2) at j = 1, bnt (nx, 2)
+    at j = ny, bnl (ny, 2) at i = 1 and bnr (ny, 2) at i = nx."""
+    out = {}
+    for name, (a, b, sel, sign) in {"bnb": ("n1", "n2", (slice(None), 0), -1.0),
+                                     "bnt": ("n1", "n2", (slice(None), -1), 1.0),
+                                     "bnl": ("m1", "m2", (0, slice(None)), -1.0),
+                                     "bnr": ("m1", "m2", (-1, slice(None)), 1.0)}.items():
+        p, q = metrics[a][sel], metrics[b][sel]
+        bn = np.zeros((p.size, 2), order="F")
+        bn[:, 0] = sign * p / np.sqrt(p * p + q * q)
+        bn[:, 1] = sign * q / np.sqrt(p * p + q * q)
+        out[name] = bn
+    return out
+
+
+def pcyl(fixture):
+    """The reference's swept parabolic-cylinder case (test/pcyl/sweep=35/
+    M=0.8/Re=1e5) from its stored fixture (tests/golden/pcyl_sweep35.npz:
+    the converged mean flow, metric.dat, top.pot and right.pot of the
+    reference's own run, 384 x 128): Ma 0.8, Re 1e5, Pr 0.7, fourth-order
+    stencils, xi non-periodic with the symmetry plane on the left (left 2)
+    and the Riemann outflow on the right (right 0) extrapolated over the
+    viscous layer (extrap 1, nbl 32 updated by itrBC), adiabatic no-slip
+    wall, Riemann top, one global time step at CFL 400 (dtmax 1), smoother
+    at eps_e 0.01 (the case's res.inp deck with the Pr and wall of the
+    stored solution)."""
+    names = ("m1", "m2", "n1", "n2", "m11", "m12", "m22", "n11", "n12", "n22")
+    metrics = {k: np.asfortranarray(fixture["m_" + k]) for k in names}
+    nx, ny = metrics["m1"].shape
+    bn = boundary_normals(metrics)
+    params = dict(nx=nx, ny=ny, dxi=1.0 / (nx - 1), deta=1.0 / (ny - 1), Ma=0.8, Re=1.0e5, Pr=0.7, gamma=GAMMA,
+                  gamma1=GAMMA1, omega=0.0, kz=0.0, alfa=float(fixture["alfa"]), xper=0, yper=0, navier=1, wall=0,
+                  wallt=1, top=0, optx=-1, opty=-1, left=2, right=0)
+    return dict(params=params, metrics=metrics, v=np.asfortranarray(fixture["v0"]),
+                bnt=bn["bnt"], pot=np.asfortranarray(np.asarray(fixture["top_pot"]).T),
+                right_far=(bn["bnr"], np.asfortranarray(np.asarray(fixture["right_pot"]).T)),
+                run=dict(cflmax=400.0, dtmax=1.0, loctime=0, theta=35.0, eps_e=0.01, extrap=1,
+                         nbl=int(fixture["nbl0"]), update_nbl=True))

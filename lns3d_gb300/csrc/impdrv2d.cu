@@ -31,25 +31,36 @@ using a3::Ops;
 using a3::pix;
 using namespace a3;  // stencil constants
 
-// Far field of the top boundary (src/gengrid.f90:141-142, src/potential.f90).
-struct Top {
-  const double* bnt;  // (nx,2)
-  const double* pot;  // (5,nx): rho, u, v, w, T of top.pot
-  double theta;       // wall recovery-temperature angle (wallt 0)
+// One far-field boundary: the unit outward normals bn(n,2) of its n nodes
+// (src/gengrid.f90:133-155) and the potential-flow values pot(5,n), the
+// rho u v w T rows of top.pot, left.pot or right.pot (src/potential.f90).
+struct Side {
+  const double* bn;
+  const double* pot;
+  int n;
+};
+
+// The boundaries of the step besides the wall: the top (j = ny) and, with
+// a non-periodic xi direction, the left (i = 1) and right (i = nx) planes.
+struct Far {
+  Side top, left, right;
+  double theta;     // wall recovery-temperature angle (wallt 0)
+  int extrap;       // extrapolation of the right plane over the viscous layer: -1 off, 0, 1, 2
+  const int* nbl;   // device: rows of the viscous layer (itrBC keeps it current)
 };
 
 // ------------------------------------------------------- Riemann far field
-// src/reimann.f90:60-72: invariants of top-boundary node i from the node and
-// the two nodes below it.
+// src/reimann.f90:60-72: invariants of boundary node k of a side from the
+// node and the two nodes inside it along the normal grid line.
 struct RmState {
   double vn, vint[5], R1, R2, rho, p, vt;
   bool inflow;
 };
 
-__device__ inline RmState rm_state(const Grid& g, const Top& tp, int i, const double* vb, const double* vb1,
+__device__ inline RmState rm_state(const Grid& g, const Side& sd, int k, const double* vb, const double* vb1,
                                    const double* vb2) {
-  const double bn1 = tp.bnt[i - 1], bn2 = tp.bnt[g.nx + i - 1];
-  const double* pt = tp.pot + 5 * (i - 1);
+  const double bn1 = sd.bn[k - 1], bn2 = sd.bn[sd.n + k - 1];
+  const double* pt = sd.pot + 5 * (k - 1);
   RmState s;
   s.vn = bn1 * vb[1] + bn2 * vb[2];
   for (int k = 0; k < 5; ++k) s.vint[k] = two * vb1[k] - vb2[k];
@@ -71,23 +82,25 @@ __device__ inline RmState rm_state(const Grid& g, const Top& tp, int i, const do
 }
 
 // the boundary state the invariants give, src/reimann.f90:104-150
-__device__ inline void rm_values(const Grid& g, const Top& tp, int i, const RmState& s, double out[5]) {
-  const double bn1 = tp.bnt[i - 1], bn2 = tp.bnt[g.nx + i - 1];
+__device__ inline void rm_values(const Grid& g, const Side& sd, int k, const RmState& s, double out[5]) {
+  const double bn1 = sd.bn[k - 1], bn2 = sd.bn[sd.n + k - 1];
   const double gamma = g.gamma, gamma1 = g.gamma1;
   const double vn = pt5 * (s.R1 + s.R2);
   const double gq = gamma1 / four, dR = s.R2 - s.R1;
   out[0] = pow(pow(s.rho, gamma) / (gamma * s.p) * (gq * gq) * (dR * dR), 1.0 / gamma1);
   out[1] = (-(bn1 * vn) - bn2 * s.vt) / (-(bn1 * bn1) - bn2 * bn2);
   out[2] = (-(bn2 * vn) + bn1 * s.vt) / (-(bn1 * bn1) - bn2 * bn2);
-  out[3] = s.inflow ? tp.pot[5 * (i - 1) + 3] : s.vint[3];
+  out[3] = s.inflow ? sd.pot[5 * (k - 1) + 3] : s.vint[3];
   const double q = g.Ma * gamma1 / four * dR;
   out[4] = q * q;
 }
 
-// Coefficient F(a,b) of ReimannLHS (src/reimann.f90:238-401): row ny holds
-// -I in slot 3, 2F in slot 2 and -F in slot 1.
-__device__ inline double rm_coef(const Grid& g, const Top& tp, int i, const RmState& s, int a, int b) {
-  const double bn1 = tp.bnt[i - 1], bn2 = tp.bnt[g.nx + i - 1];
+// Coefficient F(a,b) of ReimannLHS (src/reimann.f90:238-401): the boundary
+// row holds -I in the diagonal slot 3, 2F in the slot of the next node
+// inside and -F in the slot of the one after it (slots 2 and 1 at the top
+// and right planes, 4 and 5 at the left plane).
+__device__ inline double rm_coef(const Grid& g, const Side& sd, int k, const RmState& s, int a, int b) {
+  const double bn1 = sd.bn[k - 1], bn2 = sd.bn[sd.n + k - 1];
   const double gamma = g.gamma, gamma1 = g.gamma1, Ma = g.Ma;
   const double dR = s.R2 - s.R1, gq = gamma1 / four, sq = sqrt(s.vint[4]);
   const double bb = bn1 * bn1 + bn2 * bn2;
@@ -145,7 +158,7 @@ __device__ __forceinline__ double tw_wall(const Grid& g, double theta) {
 // pt5 (v + vold) for the midpoint rule, src/impdrv.f90:271-279); rbe and the
 // boundary rows use v; a non-null v2old selects rtb (src/impdrv.f90:511-539)
 // in place of rbe.
-__global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, Top tp, const double* __restrict__ vs,
+__global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, Far fr, const double* __restrict__ vs,
                                                     const double* __restrict__ v, const double* __restrict__ vold,
                                                     const double* __restrict__ v2old, double* __restrict__ r,
                                                     double* part) {
@@ -396,7 +409,7 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
             rr[0] = gc1 * VF(0, i, 1) + gc2 * VF(0, i, 2) + gc3 * VF(0, i, 3) + gc4 * VF(0, i, 4) + gc5 * VF(0, i, 5);
           if (g.wall == 3)
             rr[0] = VF(0, i, 1) - (4.0 * VF(0, i, 2) - 6.0 * VF(0, i, 3) + 4.0 * VF(0, i, 4) - VF(0, i, 5));
-          if (g.wallt == 0) rr[4] = VF(4, i, 1) - tw_wall(g, tp.theta);
+          if (g.wallt == 0) rr[4] = VF(4, i, 1) - tw_wall(g, fr.theta);
           if (g.wallt == 1)
             rr[4] = gc1 * VF(4, i, 1) + gc2 * VF(4, i, 2) + gc3 * VF(4, i, 3) + gc4 * VF(4, i, 4) + gc5 * VF(4, i, 5);
         }
@@ -404,15 +417,46 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
           if (g.Ma > 1.0) {
             for (int m = 0; m < 5; ++m) rr[m] = 0.0;
           } else if (g.top == 0) {
-            const RmState s = rm_state(g, tp, i, v + 5 * pix(g, i, g.ny), v + 5 * pix(g, i, g.ny - 1),
+            const RmState s = rm_state(g, fr.top, i, v + 5 * pix(g, i, g.ny), v + 5 * pix(g, i, g.ny - 1),
                                        v + 5 * pix(g, i, g.ny - 2));
             double b[5];
-            rm_values(g, tp, i, s, b);
+            rm_values(g, fr.top, i, s, b);
             for (int m = 0; m < 5; ++m) rr[m] = VF(m, i, j) - b[m];
           }
         }
       } else if (j == g.ny) {
         for (int m = 0; m < 5; ++m) rr[m] = 0.0;
+      }
+      // the xi boundary rows, src/rhsbc.f90:364-482, after the wall and top
+      // rows they overwrite at the corners: the Riemann far field (left 0,
+      // right 0) and the symmetry plane (left 2) below Ma 1; then, at any
+      // Ma, the extrapolation of the right plane over the viscous layer
+      // (rows 1..nbl) and the held right plane (right 8)
+      if (!g.xper && (i == 1 || i == g.nx)) {
+        const bool left = i == 1;
+        if (g.Ma < 1.0 && (left ? g.left : g.right) == 0) {
+          const Side& sd = left ? fr.left : fr.right;
+          const int i1 = left ? 2 : g.nx - 1, i2 = left ? 3 : g.nx - 2;
+          const RmState s = rm_state(g, sd, j, v + 5 * p, v + 5 * pix(g, i1, j), v + 5 * pix(g, i2, j));
+          double b[5];
+          rm_values(g, sd, j, s, b);
+          for (int m = 0; m < 5; ++m) rr[m] = VF(m, i, j) - b[m];
+        }
+        if (g.Ma < 1.0 && left && g.left == 2)
+          for (int m = 0; m < 5; ++m)
+            rr[m] = m == 2 ? 0.0
+                           : gc1 * VF(m, 1, j) + gc2 * VF(m, 2, j) + gc3 * VF(m, 3, j) + gc4 * VF(m, 4, j) +
+                                 gc5 * VF(m, 5, j);
+        if (!left && fr.extrap >= 0 && j <= *fr.nbl)
+          for (int m = 0; m < 5; ++m) {
+            const double e = fr.extrap == 0   ? VF(m, g.nx - 1, j)
+                             : fr.extrap == 1 ? two * VF(m, g.nx - 1, j) - VF(m, g.nx - 2, j)
+                                              : 3.0 * VF(m, g.nx - 1, j) - 3.0 * VF(m, g.nx - 2, j) +
+                                                    VF(m, g.nx - 3, j);
+            rr[m] = VF(m, g.nx, j) - e;
+          }
+        if (!left && g.right == 8)
+          for (int m = 0; m < 5; ++m) rr[m] = 0.0;
       }
       if (g.xper && i == g.nx)
         for (int m = 0; m < 5; ++m) rr[m] = 0.0;
@@ -443,7 +487,7 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, T
 // slots of a band row hold zero blocks, the boundary rows' bc(1..14)
 // blocks sit in the slots of their columns), so one set of line solvers
 // serves both orders: zero blocks add exact zeros to the elimination.
-__global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v, int dir, int order2, LhsCoef lc,
+__global__ void lhs2d_kernel(Grid g, Ops o, Far fr, const double* __restrict__ v, int dir, int order2, LhsCoef lc,
                              double* __restrict__ mat) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 125 * o.np) return;
@@ -454,6 +498,46 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   const double ident = (k == 3 && a == b) ? 1.0 : 0.0;
   const long long np = o.np;
   const double d = o.dtl[p], alfa = g.alfa;
+  // the rows of the xi boundary planes (non-periodic xi), which lhsbc1f
+  // and lhsbc2f set last and in full
+  if (!g.xper && (i == 1 || i == g.nx)) {
+    const bool left = i == 1;
+    if (dir == 2) {
+      // identity eta rows: below Ma 1 on the Riemann (left 0, right 0),
+      // symmetry (left 2) and held (right 8) planes, else over the viscous
+      // layer (src/lhsbc2f.f90:489-556)
+      const int bc = left ? g.left : g.right;
+      if (g.Ma < 1.0 ? (bc == 0 || (left ? bc == 2 : bc == 8)) : j <= *fr.nbl) {
+        mat[q] = ident;
+        return;
+      }
+    } else {
+      // src/lhsbc1f.f90:606-898: slot k holds the coefficient of node
+      // i + (k - 3) for rows inside the band; the boundary rows put the
+      // further nodes of their one-sided stencils in the free slots
+      double val = 0.0;
+      if (left && g.left == 2) {  // symmetry plane: -(gc1..gc5) on the diagonal of rows 1, 2, 4, 5
+        if (a == 3) val = ident;
+        else if (a == b) val = -pick5((k + 2) % 5, gc1, gc2, gc3, gc4, gc5);
+      } else if (g.Ma < 1.0 && (left ? g.left : g.right) == 0) {
+        const Side& sd = left ? fr.left : fr.right;
+        const int i1 = left ? 2 : g.nx - 1, i2 = left ? 3 : g.nx - 2;
+        const int s1 = left ? 4 : 2, s2 = left ? 5 : 1;
+        const RmState s = rm_state(g, sd, j, v + 5 * p, v + 5 * pix(g, i1, j), v + 5 * pix(g, i2, j));
+        if (k == 3) val = a == b ? -1.0 : 0.0;
+        else if (k == s1) val = two * rm_coef(g, sd, j, s, a, b);
+        else if (k == s2) val = -rm_coef(g, sd, j, s, a, b);
+        if (a == 4 && s.inflow && k != 3) val = 0.0;
+      }
+      if (!left && fr.extrap >= 0 && j <= *fr.nbl) {  // extrapolation of the viscous layer
+        const double c = a == b ? 1.0 : 0.0;
+        val = k == 3 ? -c : k == 2 ? (fr.extrap == 0 ? c : two * c) : (k == 1 && fr.extrap == 1 ? -c : 0.0);
+      }
+      if (!left && g.right == 8) val = k == 3 ? -(a == b ? 1.0 : 0.0) : 0.0;
+      mat[q] = val;
+      return;
+    }
+  }
   // boundary conditions of the wall row j = 1
   if (!g.yper && g.navier && j == 1) {
     if (dir == 1) {
@@ -482,12 +566,12 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
     // the held quiescent top (top 3): identity eta row, src/lhsbc2f.f90:332-339
     if (dir == 2 && g.Ma < 1.0 && g.top == 3) { mat[q] = ident; return; }
     if (dir == 2 && g.Ma < 1.0 && g.top == 0) {
-      const RmState s = rm_state(g, tp, i, v + 5 * pix(g, i, g.ny), v + 5 * pix(g, i, g.ny - 1),
+      const RmState s = rm_state(g, fr.top, i, v + 5 * pix(g, i, g.ny), v + 5 * pix(g, i, g.ny - 1),
                                  v + 5 * pix(g, i, g.ny - 2));
       double val = 0.0;
       if (k == 3) val = a == b ? -1.0 : 0.0;
-      else if (k == 2) val = two * rm_coef(g, tp, i, s, a, b);
-      else if (k == 1) val = -rm_coef(g, tp, i, s, a, b);
+      else if (k == 2) val = two * rm_coef(g, fr.top, i, s, a, b);
+      else if (k == 1) val = -rm_coef(g, fr.top, i, s, a, b);
       if (a == 4 && s.inflow && k != 3) val = 0.0;
       mat[q] = val;
       return;
@@ -503,7 +587,7 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
   else if (a == 4 && b == 4) vk = 2;
   else if (a == 5 && b == 5) vk = 3;
   double val;
-  const bool edge = dir == 2 && !g.yper && (j <= 2 || j >= g.ny - 1);
+  const bool edge = dir == 2 ? !g.yper && (j <= 2 || j >= g.ny - 1) : !g.xper && (i <= 2 || i >= g.nx - 1);
   if (order2 && !edge && (dir == 1 || j > 3 && j < g.ny - 2)) {
     // three-point band in slots 2..4 (src/lhs.f90:28-104, 176-240)
     if (k == 1 || k == 5) { mat[q] = 0.0; return; }
@@ -524,21 +608,25 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
     if (dir == 1 && k == 3) val = val + alfa * d * o.Dh[eab];
     if (vk >= 0) val = val - bk * d * V[vk * np + p];
   } else {
-    // rows 1, 2, ny-1, ny: coefficient t of slot k (src/lhsbt2f.f90)
-    const double detainv = lc.hinv, detasinv = lc.hsinv;  // dir 2: h = deta
+    // rows 1, 2, n-1, n of a line: coefficient t of slot k (eta:
+    // src/lhsbt2f.f90; xi: src/lhsbt1f.f90, whose rows also carry the D
+    // term in the diagonal slot)
+    const double hinv = lc.hinv, hsinv = lc.hsinv;  // h = dxi (dir 1) or deta (dir 2)
+    const int c = dir == 1 ? i : j, n = dir == 1 ? g.nx : g.ny;
     auto g1 = [](int t) { return pick5(t, gc1, gc2, gc3, gc4, gc5); };
     auto d1 = [](int t) { return pick5(t, dd1, dd2, dd3, dd4, dd5); };
     auto g2 = [](int t) { return pick5(t, gb1, gb2, gb3, gb4, gb5); };
     auto d2 = [](int t) { return pick5(t, db1, db2, db3, db4, db5); };
     double gcf, dcf;
     bool neg = false;
-    if (j == 1) { const int t = (k + 2) % 5; gcf = g1(t); dcf = d1(t); }
-    else if (j == 2) { const int t = (k + 3) % 5; gcf = g2(t); dcf = d2(t); }
-    else if (j == g.ny - 1) { const int t = k == 5 ? 4 : 4 - k; gcf = g2(t); dcf = d2(t); neg = true; }
+    if (c == 1) { const int t = (k + 2) % 5; gcf = g1(t); dcf = d1(t); }
+    else if (c == 2) { const int t = (k + 3) % 5; gcf = g2(t); dcf = d2(t); }
+    else if (c == n - 1) { const int t = k == 5 ? 4 : 4 - k; gcf = g2(t); dcf = d2(t); neg = true; }
     else { const int t = k <= 3 ? 3 - k : 8 - k; gcf = g1(t); dcf = d1(t); neg = true; }
-    val = alfa * d * gcf * detainv * o.Bh[eab];
+    val = alfa * d * gcf * hinv * (dir == 1 ? o.Ah : o.Bh)[eab];
     if (neg) val = -val;
-    if (vk >= 0) val = val - alfa * d * dcf * detasinv * V[vk * np + p];
+    if (dir == 1 && k == 3) val = val + alfa * d * o.Dh[eab];
+    if (vk >= 0) val = val - alfa * d * dcf * hsinv * V[vk * np + p];
   }
   val = val + ident;
   // implicit damping and sponge of the fourth-order LHS, after the I term:
@@ -574,8 +662,9 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
       if (o.buff) val = val + wd * pick5(k - 1, 1.0, -4.0, 6.0, -4.0, 1.0);
       if (dir == 2 && o.spg && k == 3) val = val + alfa * d * o.spg[p];
     } else {
-      if (o.spg && k == 3) val = val + alfa * d * o.spg[(long long)(j - 1) + (long long)(i - 1) * g.ny];
-      if (o.buff && (j == 2 || j == g.ny - 1) && k >= 2 && k <= 4) val = val + wd * (k == 3 ? 2.0 : -1.0);
+      const int c = dir == 1 ? i : j, n = dir == 1 ? g.nx : g.ny;
+      if (dir == 2 && o.spg && k == 3) val = val + alfa * d * o.spg[(long long)(j - 1) + (long long)(i - 1) * g.ny];
+      if (o.buff && (c == 2 || c == n - 1) && k >= 2 && k <= 4) val = val + wd * (k == 3 ? 2.0 : -1.0);
     }
   }
   mat[q] = val;
@@ -587,7 +676,7 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Top tp, const double* __restrict__ v
 // ny-1, ny-2); with a periodic x direction the remaining threads copy the
 // interior rows of column 1 to column nx, and the thread of column 1 copies
 // its boundary rows.
-__global__ void bc2d_kernel(Grid g, Top tp, double* __restrict__ v) {
+__global__ void bc2d_kernel(Grid g, Far fr, double* __restrict__ v) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int ncol = g.xper ? g.nx - 1 : g.nx;
   if (t < ncol) {
@@ -600,15 +689,15 @@ __global__ void bc2d_kernel(Grid g, Top tp, double* __restrict__ v) {
         for (int m = 1; m <= 3; ++m) W(m, 1) = 0.0;
         if (g.wall == 1) W(0, 1) = -(gc2 * W(0, 2) + gc3 * W(0, 3) + gc4 * W(0, 4) + gc5 * W(0, 5)) / gc1;
         if (g.wall == 3) W(0, 1) = 4.0 * W(0, 2) - 6.0 * W(0, 3) + 4.0 * W(0, 4) - W(0, 5);
-        if (g.wallt == 0) W(4, 1) = tw_wall(g, tp.theta);
+        if (g.wallt == 0) W(4, 1) = tw_wall(g, fr.theta);
         if (g.wallt == 1) W(4, 1) = -(gc2 * W(4, 2) + gc3 * W(4, 3) + gc4 * W(4, 4) + gc5 * W(4, 5)) / gc1;
       }
       if (g.Ma > 1.0) {
         W(0, g.ny) = 1.0; W(1, g.ny) = 1.0; W(2, g.ny) = 0.0; W(3, g.ny) = 0.0; W(4, g.ny) = 1.0;
       } else if (g.top == 0) {
-        const RmState s = rm_state(g, tp, i, &W(0, g.ny), &W(0, g.ny - 1), &W(0, g.ny - 2));
+        const RmState s = rm_state(g, fr.top, i, &W(0, g.ny), &W(0, g.ny - 1), &W(0, g.ny - 2));
         double b[5];
-        rm_values(g, tp, i, s, b);
+        rm_values(g, fr.top, i, s, b);
         for (int m = 0; m < 5; ++m) W(m, g.ny) = b[m];
       } else if (g.top == 3) {  // the held quiescent top, src/itrbc.f90 (nonlinear)
         W(0, g.ny) = 1.0; W(1, g.ny) = 0.0; W(2, g.ny) = 0.0; W(3, g.ny) = 0.0; W(4, g.ny) = 1.0;
@@ -624,6 +713,58 @@ __global__ void bc2d_kernel(Grid g, Top tp, double* __restrict__ v) {
     if (j <= g.ny - 1)
       for (int m = 0; m < 5; ++m) v[m + 5 * pix(g, g.nx, j)] = v[m + 5 * pix(g, 1, j)];
   }
+}
+
+// The xi boundary planes of itrBC (src/itrbc.f90:760-886, nonlinear), after
+// bc2d_kernel has set the wall and top rows they read and overwrite at the
+// corners.  One CTA in three phases separated by barriers: (1) on every row
+// the left plane (Riemann, left 0, from columns 2 and 3; symmetry plane,
+// left 2: rho, u, w and T extrapolated by the one-sided gc stencil from
+// columns 2..5, v = 0) and the right plane (Riemann, right 0, from columns
+// nx-1 and nx-2); (2) with update_nbl, the edge of the viscous layer: nbl =
+// the first row whose u at column nx-1 exceeds 0.99 (status bit 2 when no
+// row does: the reference stops there with "nbl > ny"); (3) the right plane
+// extrapolated from columns nx-1.. over rows 1..nbl.
+__global__ void __launch_bounds__(256) bcx2d_kernel(Grid g, Far fr, double* __restrict__ v, int* nbl,
+                                                    int update_nbl, int* status) {
+  __shared__ int first;
+  auto W = [&](int k, int ii, int jj) -> double& { return v[k + 5 * pix(g, ii, jj)]; };
+  for (int j = threadIdx.x + 1; j <= g.ny; j += blockDim.x) {
+    if (g.left == 0) {
+      const RmState s = rm_state(g, fr.left, j, &W(0, 1, j), &W(0, 2, j), &W(0, 3, j));
+      double b[5];
+      rm_values(g, fr.left, j, s, b);
+      for (int m = 0; m < 5; ++m) W(m, 1, j) = b[m];
+    } else if (g.left == 2) {
+      for (int m = 0; m < 5; ++m)
+        W(m, 1, j) = m == 2 ? 0.0 : -(gc2 * W(m, 2, j) + gc3 * W(m, 3, j) + gc4 * W(m, 4, j) + gc5 * W(m, 5, j)) / gc1;
+    }
+    if (g.right == 0) {
+      const RmState s = rm_state(g, fr.right, j, &W(0, g.nx, j), &W(0, g.nx - 1, j), &W(0, g.nx - 2, j));
+      double b[5];
+      rm_values(g, fr.right, j, s, b);
+      for (int m = 0; m < 5; ++m) W(m, g.nx, j) = b[m];
+    }
+  }
+  if (threadIdx.x == 0) first = g.ny + 1;
+  __syncthreads();
+  if (update_nbl) {
+    for (int j = threadIdx.x + 1; j <= g.ny; j += blockDim.x)
+      if (W(1, g.nx - 1, j) > 0.99) atomicMin(&first, j);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (first > g.ny) atomicOr(status, 2);
+      else *nbl = first;
+    }
+    __syncthreads();
+  }
+  const int n = *nbl;
+  if (fr.extrap >= 0)
+    for (int j = threadIdx.x + 1; j <= n; j += blockDim.x)
+      for (int m = 0; m < 5; ++m)
+        W(m, g.nx, j) = fr.extrap == 0   ? W(m, g.nx - 1, j)
+                        : fr.extrap == 1 ? two * W(m, g.nx - 1, j) - W(m, g.nx - 2, j)
+                                         : 3.0 * W(m, g.nx - 1, j) - 3.0 * W(m, g.nx - 2, j) + W(m, g.nx - 3, j);
 }
 
 // w = pt5 (v + vold), the midpoint state (src/impdrv.f90:273)
@@ -654,6 +795,9 @@ struct lns_ctx2d {
   double* opbuf = nullptr;    // Ah Bh Dh (25 np each), V11 V12 V22 (6 np each), dtl (np)
   Ops ops{};
   double *bnt = nullptr, *pot = nullptr;  // far field of the top boundary
+  // far fields of the xi planes (xper = 0 with left 0 / right 0): bn(ny,2), pot(5,ny)
+  double *bnl = nullptr, *potl = nullptr, *bnr = nullptr, *potr = nullptr;
+  int* nbl = nullptr;                     // device: itrBC's edge of the viscous layer
   double *v = nullptr, *vold = nullptr, *r = nullptr, *mat = nullptr, *per = nullptr, *per2 = nullptr;
   double *v2old = nullptr, *wavg = nullptr;  // impl 2 / impl 3 state
   long long lstep = 0;                       // steps taken since creation
@@ -663,7 +807,7 @@ struct lns_ctx2d {
   double* res_dev = nullptr;
   int res_cap = 0;
   int* status = nullptr;
-  bool have_metrics = false, have_top = false;
+  bool have_metrics = false, have_top = false, have_left = false, have_right = false;
   bool have_sponge = false;  // ispg = 2: lns_upload_sponge2d called
   double* spg = nullptr;     // spg + spg2
   double* buff = nullptr;    // eps_e != 0: buff(nx,ny), ones until uploaded
@@ -734,7 +878,16 @@ Metrics metrics2(const lns_ctx2d* c) {
                  m + 9 * np};
 }
 
-lns::a2::Top top2(const lns_ctx2d* c) { return lns::a2::Top{c->bnt, c->pot, c->prm.theta}; }
+lns::a2::Far top2(const lns_ctx2d* c) {
+  lns::a2::Far f;
+  f.top = lns::a2::Side{c->bnt, c->pot, c->g.nx};
+  f.left = lns::a2::Side{c->bnl, c->potl, c->g.ny};
+  f.right = lns::a2::Side{c->bnr, c->potr, c->g.ny};
+  f.theta = c->prm.theta;
+  f.extrap = c->g.xper ? -1 : c->prm.extrap;
+  f.nbl = c->nbl;
+  return f;
+}
 
 dim3 pgrid(const Grid& g) { return dim3((g.nx + 127) / 128, g.ny); }
 
@@ -773,8 +926,10 @@ int lhs2(lns_ctx2d* c, const double* v, int dir, double* mat, double alfa, cudaS
 int bc2(lns_ctx2d* c, double* v, cudaStream_t st) {
   const int nt = c->g.nx + c->g.ny;
   lns::a2::bc2d_kernel<<<(nt + 127) / 128, 128, 0, st>>>(c->g, top2(c), v);
+  if (!c->g.xper)
+    lns::a2::bcx2d_kernel<<<1, 256, 0, st>>>(c->g, top2(c), v, c->nbl, c->prm.update_nbl, c->status);
   cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? LNS_OK : cuda2(e, "bc2d_kernel launch");
+  return e == cudaSuccess ? LNS_OK : cuda2(e, "itrBC kernels launch");
 }
 
 // nsteps steps of niter correctors (src/impdrv.f90:171-400) with the time
@@ -817,9 +972,11 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
       // the fourth-order path solves with penta2p (its periodic fill-slot
       // quirk kept unless the exact mode is on), the second-order path with
       // solve2p, which has no such quirk (src/nsolve2p.f90)
-      if (!rc)
+      if (!rc && g.xper)
         rc = lns::host::launch_p<double>(c->mat, c->r, c->per, c->per2, g.nx, g.ny, 1, g.nx, 2, st, c->status,
                                          c->prm.lhs_order == 2 ? 1 : -1);
+      else if (!rc)  // penta2bc along xi (src/impdrv.f90:353-357)
+        rc = lns::host::launch_bc<double>(c->mat, c->r, g.nx, g.ny, 1, g.nx, 2, st, c->status);
       if (!rc) rc = lhs2(c, v, 2, c->mat, alfa, st);
       if (!rc) rc = lns::host::launch_bc<double>(c->mat, c->r, g.ny, g.nx, g.nx, 1, 2, st, c->status);
       if (!rc) {
@@ -840,6 +997,9 @@ int check_pivots2(lns_ctx2d* c, cudaStream_t st) {
   cudaError_t e = cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda2(e, "2D step");
+  if (status & 2)
+    return fail2(LNS_ERR_ARG, "itrBC: no row of column nx-1 has u > 0.99, so the viscous layer has no edge "
+                              "(the reference stops with nbl > ny)");
   if (status) return fail2(LNS_ERR_PIVOT, "zero or non-finite pivot in an LHS factorisation");
   return LNS_OK;
 }
@@ -855,7 +1015,22 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   if ((long long)p->nx * p->ny > (1LL << 31) / 125)
     return fail2(LNS_ERR_ARG, "ctx2d_create: nx*ny too large for 32-bit launch indexing");
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail2(LNS_ERR_ARG, "ctx2d_create: dxi and deta must be > 0");
-  if (p->xper != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: only a periodic xi direction (xper = 1) is supported");
+  if (p->xper != 0 && p->xper != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: xper must be 0 or 1");
+  if (p->xper == 0) {
+    // the non-periodic xi direction: the planes of src/rhsbc.f90:364-482,
+    // src/lhsbc1f.f90:606-898, src/lhsbc2f.f90:489-556, src/itrbc.f90:760-886
+    if (p->left != 0 && p->left != 2)
+      return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, left must be 0 (Riemann) or 2 (symmetry plane)");
+    if (p->right != 0) return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, right must be 0 (Riemann)");
+    if (!(p->Ma < 1.0)) return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, need Ma < 1");
+    if (p->extrap < -1 || p->extrap > 1)
+      return fail2(LNS_ERR_ARG, "ctx2d_create: extrap must be -1, 0 or 1 (the reference's xi LHS rejects 2)");
+    if (p->nbl < 0 || p->nbl > p->ny) return fail2(LNS_ERR_ARG, "ctx2d_create: need 0 <= nbl <= ny");
+    if (p->update_nbl != 0 && p->update_nbl != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: update_nbl must be 0 or 1");
+    if (p->lhs_order == 2)
+      return fail2(LNS_ERR_ARG, "ctx2d_create: a non-periodic xi direction is supported with the fourth-order LHS");
+    if (p->nx < 10) return fail2(LNS_ERR_ARG, "ctx2d_create: a non-periodic xi direction needs nx >= 10");
+  }
   if (p->yper != 0 || p->navier != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: need yper = 0 and navier = 1");
   if (p->wall != 0 && p->wall != 1 && p->wall != 3) return fail2(LNS_ERR_ARG, "ctx2d_create: wall must be 0, 1 or 3");
   if (p->wallt != 0 && p->wallt != 1) return fail2(LNS_ERR_ARG, "ctx2d_create: wallt must be 0 or 1");
@@ -885,6 +1060,7 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   g.gamma1 = p->gamma1 != 0.0 ? p->gamma1 : p->gamma - 1.0;
   g.omega = 0.0; g.kz = 0.0; g.alfa = p->alfa;
   g.xper = p->xper; g.yper = p->yper; g.navier = p->navier; g.wall = p->wall; g.wallt = p->wallt; g.top = p->top;
+  g.left = p->xper ? -1 : p->left; g.right = p->xper ? -1 : p->right;
   g.dxinv = 1.0 / p->dxi; g.dyinv = 1.0 / p->deta;
   g.dxsinv = 1.0 / (p->dxi * p->dxi); g.dysinv = 1.0 / (p->deta * p->deta);
   coef1(p->optx, g.dxinv, g.gx);
@@ -903,6 +1079,13 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   A(sizeof(double) * (3 * 25 + 3 * 6 + 1) * np, &q); c->opbuf = (double*)q;
   A(sizeof(double) * 2 * p->nx, &q); c->bnt = (double*)q;
   A(sizeof(double) * 5 * p->nx, &q); c->pot = (double*)q;
+  A(sizeof(int), &q); c->nbl = (int*)q;
+  if (p->xper == 0) {
+    A(sizeof(double) * 2 * p->ny, &q); c->bnl = (double*)q;
+    A(sizeof(double) * 5 * p->ny, &q); c->potl = (double*)q;
+    A(sizeof(double) * 2 * p->ny, &q); c->bnr = (double*)q;
+    A(sizeof(double) * 5 * p->ny, &q); c->potr = (double*)q;
+  }
   A(sizeof(double) * 5 * np, &q); c->v = (double*)q;
   A(sizeof(double) * 5 * np, &q); c->vold = (double*)q;
   A(sizeof(double) * 5 * np, &q); c->r = (double*)q;
@@ -920,7 +1103,9 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   if (!rc) {
     c->res_cap = 64;
     e = cudaMemset(c->dscal, 0, sizeof(double) * 3);
-    if (e != cudaSuccess) rc = cuda2(e, "cudaMemset");
+    const int nbl0 = p->xper ? 0 : p->nbl;
+    if (e == cudaSuccess) e = cudaMemcpy(c->nbl, &nbl0, sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda2(e, "context init");
   }
   if (rc) {
     free2(c);
@@ -980,6 +1165,21 @@ int lns_upload_top2d(lns_ctx2d* c, const double* bnt, const double* pot) {
   return LNS_OK;
 }
 
+int lns_upload_side2d(lns_ctx2d* c, int32_t side, const double* bn, const double* pot) {
+  if (!c || !bn || !pot) return fail2(LNS_ERR_ARG, "upload_side2d: null argument");
+  if (side != 1 && side != 2) return fail2(LNS_ERR_ARG, "upload_side2d: side must be 1 (left) or 2 (right)");
+  if (c->g.xper) return fail2(LNS_ERR_ARG, "upload_side2d: the context has a periodic xi direction");
+  int rc = check_dev2(c);
+  if (rc) return rc;
+  double* b = side == 1 ? c->bnl : c->bnr;
+  double* q = side == 1 ? c->potl : c->potr;
+  cudaError_t e = cudaMemcpy(b, bn, sizeof(double) * 2 * c->g.ny, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(q, pot, sizeof(double) * 5 * c->g.ny, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda2(e, "upload side far field");
+  (side == 1 ? c->have_left : c->have_right) = true;
+  return LNS_OK;
+}
+
 int lns_upload_sponge2d(lns_ctx2d* c, const double* spg, const double* spg2) {
   if (!c || !spg || !spg2) return fail2(LNS_ERR_ARG, "upload_sponge2d: null argument");
   if (!c->spg) return fail2(LNS_ERR_ARG, "upload_sponge2d: the context was created with ispg = 0");
@@ -1009,6 +1209,8 @@ int lns_upload_buffer2d(lns_ctx2d* c, const double* buff) {
 static int ready2(lns_ctx2d* c, const char* who) {
   if (!c->have_metrics || (!c->have_top && c->prm.top == 0 && c->prm.Ma < 1.0))
     return fail2(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the far field first");
+  if (!c->g.xper && ((c->prm.left == 0 && !c->have_left) || (c->prm.right == 0 && !c->have_right)))
+    return fail2(LNS_ERR_ARG, std::string(who) + ": upload the far field of the Riemann xi planes first");
   if (c->prm.ispg != 0 && !c->have_sponge)
     return fail2(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
   return check_dev2(c);

@@ -32,19 +32,25 @@ class ImpDrv2D:
     """One nonlinear 2D problem resident on the current GPU.
 
     params: dict with nx, ny, dxi, deta, Ma, Re, Pr, gamma, alfa, xper, yper,
-    navier, wall, wallt, top, optx, opty; metrics: the ten (nx, ny) arrays;
-    bnt: (nx, 2) unit normal of the top boundary; pot: (5, nx) top.pot rows.
+    navier, wall, wallt, top, optx, opty (and left, right with xper = 0);
+    metrics: the ten (nx, ny) arrays; bnt: (nx, 2) unit normal of the top
+    boundary; pot: (5, nx) top.pot rows.
     """
 
     def __init__(self, params, metrics, bnt, pot, cflmax=1.0, dtmax=1e30, loctime=0, theta=0.0,
-                 ilhs=1, impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None):
+                 ilhs=1, impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None, left_far=None,
+                 right_far=None, extrap=-1, nbl=0, update_nbl=False):
         """ilhs: the reference's iLHS switch, 1 = fourth-order LHS with
         pentadiagonal solves, 0 = second-order LHS with block-tridiagonal
         solves (src/impdrv.f90:307-344).  impl: time scheme, 1 backward
         Euler, 2 two-step backward, 3 midpoint (src/impdrv.f90:186-279).
         ispg (0 or 2), spg, spg2: the sponge towards the free stream; eps_e,
         buff: the explicit smoother and implicit damping (buff ones when
-        None)."""
+        None).  With a non-periodic xi direction: left_far, right_far the
+        (bn (ny, 2), pot (5, ny)) far fields of Riemann planes (bnl / bnr of
+        src/gengrid.f90, left.pot / right.pot); extrap, nbl, update_nbl the
+        extrapolation of the right plane over the viscous layer (the deck's
+        extrap and the &extras namelist's nbl and update_nbl)."""
         if ilhs not in (0, 1):
             raise ValueError("ilhs must be 0 or 1")
         if impl not in (1, 2, 3):
@@ -55,7 +61,9 @@ class ImpDrv2D:
                        gamma=p["gamma"], gamma1=p.get("gamma1", 0.0), alfa=p["alfa"], cflmax=cflmax, dtmax=dtmax,
                        theta=theta, loctime=loctime, xper=p["xper"], yper=p["yper"], navier=p["navier"],
                        wall=p["wall"], wallt=p["wallt"], top=p["top"], optx=p["optx"], opty=p["opty"],
-                       lhs_order=2 if ilhs == 0 else 4, impl=impl, ispg=ispg, eps_e=eps_e)
+                       lhs_order=2 if ilhs == 0 else 4, impl=impl, ispg=ispg, eps_e=eps_e,
+                       left=p.get("left", -1), right=p.get("right", -1), extrap=extrap, nbl=nbl,
+                       update_nbl=int(bool(update_nbl)))
         self._ctx = ctypes.c_void_p()
         check(lib().lns_ctx2d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_ctx2d_create")
         m = np.empty((self.nx, self.ny, 10), order="F")
@@ -67,6 +75,14 @@ class ImpDrv2D:
         assert b.shape == (self.nx, 2) and q.shape == (5, self.nx)
         check(lib().lns_upload_top2d(self._ctx, ctypes.c_void_p(b.ctypes.data), ctypes.c_void_p(q.ctypes.data)),
               "lns_upload_top2d")
+        for side, far in ((1, left_far), (2, right_far)):
+            if far is None:
+                continue
+            fb = np.asfortranarray(far[0], dtype=np.float64)
+            fq = np.asfortranarray(far[1], dtype=np.float64)
+            assert fb.shape == (self.ny, 2) and fq.shape == (5, self.ny)
+            check(lib().lns_upload_side2d(self._ctx, side, ctypes.c_void_p(fb.ctypes.data),
+                                          ctypes.c_void_p(fq.ctypes.data)), "lns_upload_side2d")
         if ispg:
             s1 = np.asfortranarray(spg, dtype=np.float64)
             s2 = np.asfortranarray(spg2, dtype=np.float64)

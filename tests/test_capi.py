@@ -158,7 +158,10 @@ def _params2d(**kw):
     return Params2D(**base)
 
 
-@pytest.mark.parametrize("bad", [dict(xper=0), dict(yper=1), dict(navier=0), dict(wall=2), dict(wallt=2),
+@pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=1), dict(xper=0, left=7), dict(xper=0, right=2),
+                                 dict(xper=0, Ma=1.2), dict(xper=0, extrap=2), dict(xper=0, extrap=-2),
+                                 dict(xper=0, nbl=25), dict(xper=0, nbl=-1), dict(xper=0, update_nbl=2),
+                                 dict(xper=0, lhs_order=2), dict(xper=0, nx=9), dict(yper=1), dict(navier=0), dict(wall=2), dict(wallt=2),
                                  dict(top=1), dict(nx=7), dict(ny=6), dict(Ma=1.0), dict(deta=0.0),
                                  dict(lhs_order=3), dict(lhs_order=2, ny=7), dict(impl=4),
                                  dict(impl=-1), dict(ispg=1), dict(eps_e=-0.5),
@@ -183,6 +186,7 @@ def test_ctx2d_null_arguments(lib):
     assert lib.lns_ctx2d_destroy(None) == 0
     assert lib.lns_ctx2d_bytes(None) == 0
     assert lib.lns_upload_sponge2d(None, None, None) == 1
+    assert lib.lns_upload_side2d(None, 1, None, None) == 1
     assert lib.lns_upload_buffer2d(None, None) == 1
 
 
