@@ -254,3 +254,20 @@ def pcyl(fixture):
                 right_far=(bn["bnr"], np.asfortranarray(np.asarray(fixture["right_pot"]).T)),
                 run=dict(cflmax=400.0, dtmax=1.0, loctime=0, theta=35.0, eps_e=0.01, extrap=1,
                          nbl=int(fixture["nbl0"]), update_nbl=True))
+
+
+def vortex2d_open(nx=48, ny=40, seed=1, left=0, right=0, extrap=-1, **kw):
+    """The two-dimensional vortex case (vortex2d) with a non-periodic xi
+    direction: Riemann planes (left 0, right 0) or a symmetry plane (left
+    2) at x = -L and x = L, their normals as src/gengrid.f90:145-155 forms
+    them and their left.pot / right.pot values the state's boundary
+    columns (as the top.pot values are its top row); extrap the deck's
+    extrapolation of the right plane over the viscous layer."""
+    case = vortex2d(nx=nx, ny=ny, seed=seed, **kw)
+    case["params"].update(xper=0, left=left, right=right)
+    bn = boundary_normals(case["metrics"])
+    v = case["v"]
+    case["left_far"] = (bn["bnl"], np.asfortranarray(v[:, 0, :].copy())) if left == 0 else None
+    case["right_far"] = (bn["bnr"], np.asfortranarray(v[:, -1, :].copy())) if right == 0 else None
+    case["extrap"] = extrap
+    return case

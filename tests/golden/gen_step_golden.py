@@ -20,7 +20,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
 import refcase  # noqa: E402
-from lns3d_gb300.cases import acoustic_box, shear_layer, vortex2d  # noqa: E402
+from lns3d_gb300.cases import acoustic_box, shear_layer, vortex2d, vortex2d_open  # noqa: E402
 
 # name -> (kind, case arguments, run arguments)
 GOLDEN = {
@@ -49,6 +49,14 @@ GOLDEN = {
     "step3d_open": ("3dopen", dict(nx=48, ny=33, seed=4, left=0, right=0), dict(nsteps=10, cflmax=20.0, loctime=1)),
     "step3d_open_wave": ("3dopen", dict(nx=48, ny=33, seed=4, left=1, right=0),
                          dict(nsteps=5, cflmax=0.2, loctime=1, x0=0.5)),
+    # the nonlinear 2D step with a non-periodic xi direction: Riemann planes
+    # on both sides; the symmetry plane on the left with the right plane
+    # extrapolated (zeroth order) over a viscous layer that itrBC moves
+    # (the &extras namelist's nbl and update_nbl)
+    "step2d_vortex_open": ("2dopen", dict(nx=48, ny=40, seed=1, left=0, right=0),
+                           dict(nsteps=10, cflmax=1.0, loctime=0)),
+    "step2d_vortex_open_sym": ("2dopen", dict(nx=48, ny=40, seed=2, left=2, right=0, extrap=0),
+                               dict(nsteps=10, cflmax=1.0, loctime=0, module=dict(nbl=6, update_nbl=1))),
 }
 
 
@@ -108,6 +116,8 @@ def generate(name):
         v, hist, run = refcase.run2dlin(shear_layer(**cargs), nsteps, **rargs)
     elif kind == "3dopen":
         v, hist, run = refcase.run3d(open_layer(**cargs), nsteps, **rargs)
+    elif kind == "2dopen":
+        v, hist, run = refcase.run2d(vortex2d_open(**cargs), nsteps, **rargs)
     else:
         v, hist, run = refcase.run3d(shear_layer(**cargs), nsteps, **rargs)
     try:

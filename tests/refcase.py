@@ -60,10 +60,15 @@ class Run:
     def path(self, name):
         return os.path.join(self.dir, name)
 
-    def run(self, deck, swap=False, asis=False):
+    def run(self, deck, swap=False, asis=False, module=None):
+        """module: values of module variables to set before the program
+        starts (the &extras namelist, which the translated program does not
+        read)."""
         from oracle.refstep import RefProgram
 
         self.prog = RefProgram(asis=asis)
+        for k, val in (module or {}).items():
+            self.prog.set(k, val)
         self.prog.run(self.dir, deck, swap=swap)
         return self.prog
 
@@ -87,15 +92,23 @@ def run3d(case, nsteps, asis=False, **kw):
     return v, history(r.path("output.h.1")), r
 
 
-def run2d(case, nsteps, **kw):
-    """The reference's nonlinear impdrv on the case: (final v, totres history, Run)."""
+def run2d(case, nsteps, module=None, **kw):
+    """The reference's nonlinear impdrv on the case: (final v, totres history,
+    Run).  A case with a non-periodic xi direction carries its deck's left,
+    right and extrap, and the far fields of its Riemann planes (left_far,
+    right_far: (bn, pot)), written as left.pot / right.pot."""
     p = case["params"]
     r = Run()
     refio.write_grid(r.path("grid.dat"), case["x"], case["y"])
     refio.write_metrics(r.path("metric.dat"), case["metrics"])
     refio.write_field(r.path("output.R.0"), case["v"], Re=p["Re"], Ma=p["Ma"], Pr=p["Pr"])
     refio.write_pot(r.path("top.pot"), np.asarray(case["pot"]).T)
-    r.run(deck2d(case, nsteps, **kw))
+    for name in ("left", "right"):
+        if case.get(name + "_far") is not None:
+            refio.write_pot(r.path(name + ".pot"), np.asarray(case[name + "_far"][1]).T)
+    if not p["xper"]:
+        kw = dict(dict(left=p["left"], right=p["right"], extrap=case.get("extrap", -1)), **kw)
+    r.run(deck2d(case, nsteps, **kw), module=module)
     _, v, _ = refio.read_field(r.last_restart())
     return v, history(r.path("output.h.1")), r
 

@@ -157,3 +157,25 @@ def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     res = drv.step(v, nsteps=rargs["nsteps"])
     assert rel(v, d["v"]) < STATE_TOL, rel(v, d["v"])
     assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
+
+
+@pytest.mark.parametrize("name", ["step2d_vortex_open", "step2d_vortex_open_sym"])
+def test_step2d_nonperiodic_xi_matches_reference_golden(cuda, name):
+    """The nonlinear 2D step with a non-periodic xi direction: Riemann planes
+    on both sides (left.pot / right.pot), and the symmetry plane with the
+    right plane extrapolated over a viscous layer that itrBC moves."""
+    from lns3d_gb300 import ImpDrv2D
+    from lns3d_gb300.cases import vortex2d_open
+
+    kind, cargs, rargs, d = golden(name)
+    case = vortex2d_open(**cargs)
+    nsteps = rargs.pop("nsteps")
+    module = rargs.pop("module", {})
+    drv = ImpDrv2D(case["params"], case["metrics"], case["bnt"], case["pot"], cflmax=rargs.get("cflmax", 1.0),
+                   loctime=rargs.get("loctime", 0), left_far=case["left_far"], right_far=case["right_far"],
+                   extrap=case["extrap"], nbl=module.get("nbl", 0), update_nbl=module.get("update_nbl", 0))
+    v = case["v"].copy(order="F")
+    drv.itrbc(v)
+    res = drv.step(v, nsteps=nsteps)
+    assert rel(v, d["v"]) < STATE_TOL, rel(v, d["v"])
+    assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
