@@ -378,7 +378,9 @@ typedef struct {
                                 src/rhsbc3d.f90:167-324, src/lhsbc1f3d.f90:412-448,
                                 src/lhsbc2f3d.f90:146-174): left 0 zero disturbance, 1 an
                                 incoming acoustic wave exp(-a (x - x0)) exp(i kk x) formed from
-                                the mean flow (lns_upload_inflow3d); right 0 zero disturbance.
+                                the mean flow (lns_upload_inflow3d), 4 the eigenfunction inflow
+                                (lns_upload_profile3d); right 0 zero disturbance, 4 the
+                                eigenfunction outflow (with left 4), 8 the held initial condition.
                                 Ignored with xper = 1.  Batches and servers take xper = 1. */
 } lns_params3d;
 
@@ -412,6 +414,14 @@ int lns_upload_sponge_target3d(lns_ctx3d* ctx, const double* cvic);
  * third-order extrapolation, T = tw (wallt 0) or the gc closure equal to twp
  * (wallt 1) (src/itrbc3d.f90:46-121, src/rhsbc3d.f90:45-104,
  * src/lhsbc2f3d.f90:41-48).  Needed before the first step. */
+/* The eigenfunction of the xi planes (left 4, and right 4), the inflow.dat
+ * profile that src/gendist.f90:40-47 reads: prof(10,ny) = rho, u, v, w, T as
+ * (re, im) pairs per row, held at column 1 (src/itrbc3d.f90:247-320,
+ * src/rhsbc3d.f90:207-243); with right 4, column nx holds
+ * prof * exp(i lalpha x(nx,j)) (src/itrbc3d.f90:357-381), xr(ny) = x(nx,:)
+ * and lalpha the inflow namelist's complex wavenumber (may be NULL / 0 with
+ * right != 4).  Needed before the first step with left 4. */
+int lns_upload_profile3d(lns_ctx3d* ctx, const double* prof, const double* xr, double lalpha_re, double lalpha_im);
 int lns_upload_bump3d(lns_ctx3d* ctx, const double* bump);
 /* The smoother weight buff(nx,ny) of the host's buffer setup (src/buffer.f90,
  * ibuff > 0); only for eps_e != 0; invalidates the factored LHS. */

@@ -69,6 +69,7 @@ SIGNATURES = {
     "lns_upload_inflow3d": [P, DP, DP, ctypes.c_double],
     "lns_upload_sponge_target3d": [P, DP],
     "lns_upload_bump3d": [P, DP],
+    "lns_upload_profile3d": [P, DP, DP, ctypes.c_double, ctypes.c_double],
     "lns_upload_buffer3d": [P, DP],
     "lns_upload_sponge2d": [P, DP, DP],
     "lns_upload_buffer2d": [P, DP],

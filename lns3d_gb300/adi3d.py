@@ -57,7 +57,11 @@ class ImpDrv3D:
 
     def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, precision=FP64,
                  impl=1, ispg=0, spg=None, spg2=None, eps_e=0.0, buff=None, x=None, x0=0.0, wamp=None,
-                 cvic=None, bump=None, row_pairs=True):
+                 cvic=None, bump=None, row_pairs=True, profile=None, lalpha=0j):
+        """profile: with xper = 0 and left 4, the eigenfunction of the xi
+        planes, complex (5, ny) (the inflow.dat columns); lalpha its complex
+        streamwise wavenumber for right 4, whose column nx holds profile *
+        exp(i lalpha x(nx, j)) (x needed)."""
         p = params
         self.nx, self.ny = int(p["nx"]), int(p["ny"])
         self.precision = precision
@@ -87,6 +91,13 @@ class ImpDrv3D:
             check(lib().lns_upload_inflow3d(self._ctx, ctypes.c_void_p(xx.ctypes.data),
                                             ctypes.c_void_p(wa.ctypes.data) if wa is not None else None, x0),
                   "lns_upload_inflow3d")
+        if not int(p["xper"]) and int(p.get("left", -1)) == 4:
+            pr = np.asfortranarray(profile, dtype=np.complex128)
+            assert pr.shape == (5, self.ny)
+            xr = np.ascontiguousarray(np.asarray(x)[-1, :], dtype=np.float64) if x is not None else None
+            check(lib().lns_upload_profile3d(self._ctx, ctypes.c_void_p(pr.ctypes.data),
+                                             ctypes.c_void_p(xr.ctypes.data) if xr is not None else None,
+                                             complex(lalpha).real, complex(lalpha).imag), "lns_upload_profile3d")
         if ispg == 4:
             cv = np.asfortranarray(cvic, dtype=np.complex128)
             check(lib().lns_upload_sponge_target3d(self._ctx, ctypes.c_void_p(cv.ctypes.data)),

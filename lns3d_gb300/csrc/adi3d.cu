@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <complex>
 #include <chrono>
 #include <cmath>
 #include <deque>
@@ -321,7 +322,10 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
   // the xi boundaries of a non-periodic xi direction (src/lhsbc1f3d.f90:412-448,
   // src/lhsbc2f3d.f90:146-174); they follow the wall and top rows, so the
   // corners take them
-  if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && g.right == 0))) return store_el(mat, q, ident);
+  if (!g.xper && ((i == 1 && (g.left == 0 || g.left == 4)) || (i == g.nx && (g.right == 0 || g.right == 4))))
+    return store_el(mat, q, ident);
+  // the held right plane (right 8): -I in the xi LHS only (src/lhsbc1f3d.f90:439-446)
+  if (!g.xper && dir == 1 && i == g.nx && g.right == 8) return store_el(mat, q, cd{-ident.x, -ident.y});
   // boundary conditions of the wall (j = 1) and top (j = ny) rows
   if (!g.yper && (g.top == 0 || g.top == 1) && j == g.ny) return store_el(mat, q, ident);
   if (!g.yper && g.navier && j == 1) {
@@ -605,10 +609,12 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
     }
     // the xi boundaries (src/rhsbc3d.f90:167-324), after the wall and top rows
-    if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && g.right == 0)))
+    if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && (g.right == 0 || g.right == 4 || g.right == 8))))
       #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
-    if (!g.xper && i == 1 && g.left == 1) {  // src/rhsbc3d.f90:178-206: r = -(v - t)
+    // the incoming wave (left 1, src/rhsbc3d.f90:178-206) and the eigenfunction
+    // inflow (left 4, :207-243): r = -(v - t)
+    if (!g.xper && i == 1 && (g.left == 1 || g.left == 4)) {
       const cd* T = reinterpret_cast<const cd*>(o.tleft) + 5 * (j - 1);
       #pragma unroll
       for (int m = 0; m < 5; ++m) {
@@ -650,7 +656,7 @@ __global__ void __launch_bounds__(128, 4) rhs_kernel(Grid g, Ops o, const cd* __
 // column nx, and the thread of column 1 copies its boundary rows.
 __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const double* __restrict__ ttop,
                                         const double* __restrict__ bump, const double* __restrict__ tleft,
-                                        int bx) {
+                                        const double* __restrict__ tright, int bx) {
   const int t = bx * blockDim.x + threadIdx.x;
   const int ncol = g.xper ? g.nx - 1 : g.nx;
   if (t < ncol) {
@@ -694,9 +700,15 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
     if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && g.right == 0)))
       for (int jj = 1; jj <= g.ny; ++jj)
         for (int m = 0; m < 5; ++m) W(m, jj) = cd{0.0, 0.0};
-    if (!g.xper && i == 1 && g.left == 1)
+    // the incoming wave (left 1) and the eigenfunction inflow (left 4,
+    // src/itrbc3d.f90:247-320) hold column 1 at t; the eigenfunction outflow
+    // (right 4, :357-381) holds column nx at its profile times exp(i lalpha x)
+    if (!g.xper && i == 1 && (g.left == 1 || g.left == 4))
       for (int jj = 1; jj <= g.ny; ++jj)
         for (int m = 0; m < 5; ++m) W(m, jj) = reinterpret_cast<const cd*>(tleft)[m + 5 * (jj - 1)];
+    if (!g.xper && i == g.nx && g.right == 4)
+      for (int jj = 1; jj <= g.ny; ++jj)
+        for (int m = 0; m < 5; ++m) W(m, jj) = reinterpret_cast<const cd*>(tright)[m + 5 * (jj - 1)];
   } else if (g.xper) {
     const int j = t - ncol + 2;
     if (j <= g.ny - 1)
@@ -705,8 +717,9 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
 }
 
 __global__ void bc_kernel(Grid g, cd* __restrict__ v, const double* __restrict__ ttop,
-                          const double* __restrict__ bump, const double* __restrict__ tleft) {
-  bc_body(g, v, ttop, bump, tleft, blockIdx.x);
+                          const double* __restrict__ bump, const double* __restrict__ tleft,
+                          const double* __restrict__ tright) {
+  bc_body(g, v, ttop, bump, tleft, tright, blockIdx.x);
 }
 
 // ------------------------------------------------------------- batching
@@ -743,7 +756,8 @@ __global__ void bc_batch_kernel(const StepArgs* __restrict__ list, const int2* _
   for (int k = blockIdx.x; k < *cnt; k += gridDim.x) {
     const int2 w = table[k];
     if (!active[w.x]) continue;
-    bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, list[w.x].o.bump, list[w.x].o.tleft, w.y);
+    bc_body(list[w.x].g, list[w.x].v, list[w.x].o.ttop, list[w.x].o.bump, list[w.x].o.tleft, list[w.x].o.tright,
+            w.y);
   }
 }
 __global__ void grad1_batch_kernel(const StepArgs* __restrict__ list, const int4* __restrict__ table,
@@ -861,7 +875,9 @@ struct lns_ctx3d {
   double *spg_a = nullptr, *spg_b = nullptr, *vt = nullptr;  // the target sponges (ispg 2-4)
   double *xc = nullptr, *wamp = nullptr;  // ispg 2, 3 or top 1: x(nx,ny), wamp(nx) (ones until uploaded)
   double* ttop = nullptr;                 // top 1: the wave of row ny, complex (5,nx)
-  double* tleft = nullptr;                // left 1: the wave of column 1, complex (5,ny)
+  double* tleft = nullptr;                // left 1: the wave of column 1; left 4: the eigenfunction; complex (5,ny)
+  double* tright = nullptr;               // right 4: the eigenfunction times exp(i lalpha x(nx,j)), complex (5,ny)
+  bool have_profile = false;              // left 4: lns_upload_profile3d called
   double* bump = nullptr;                 // wall 3: u1w, u2w, u3w, tw, twp, complex (5,nx)
   bool have_bump = false;
   double x0 = 0.0;
@@ -1265,7 +1281,8 @@ int launch_update(lns_ctx3d* c, cd* v, const RT* r, int add, cudaStream_t st) {
   const long long n = 5 * c->np;
   if (add) lns::a3::add_kernel<cd, RT><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, r);
   const int nt = g.nx + g.ny;
-  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v, c->ops.ttop, c->ops.bump, c->ops.tleft);
+  lns::a3::bc_kernel<<<(nt + 127) / 128, 128, 0, st>>>(g, v, c->ops.ttop, c->ops.bump, c->ops.tleft,
+                                                        c->ops.tright);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LNS_OK : cuda3(e, "update kernels launch");
 }
@@ -1349,8 +1366,12 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
   if (p->xper != 0 && p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: xper must be 0 or 1");
   if (!p->xper) {
-    if (p->left != 0 && p->left != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0 or 1 (xper = 0)");
-    if (p->right != 0) return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0 (xper = 0)");
+    if (p->left != 0 && p->left != 1 && p->left != 4)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1 or 4 (xper = 0)");
+    if (p->right != 0 && p->right != 4 && p->right != 8)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4 or 8 (xper = 0)");
+    // the reference reads the eigenfunction only for left 4 (src/gendist.f90:18)
+    if (p->right == 4 && p->left != 4) return fail3(LNS_ERR_ARG, "ctx3d_create: right 4 needs left 4");
   }
   if (p->yper != 0 && p->yper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: yper must be 0 or 1");
   if (p->navier != 0 && p->navier != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: navier must be 0 or 1");
@@ -1423,7 +1444,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
     A(sizeof(double) * p->nx, &q); c->wamp = (double*)q;
   }
   if (p->top == 1) { A(sizeof(double) * 10 * p->nx, &q); c->ttop = (double*)q; }
-  if (left_wave) { A(sizeof(double) * 10 * p->ny, &q); c->tleft = (double*)q; }
+  if (left_wave || (!p->xper && p->left == 4)) { A(sizeof(double) * 10 * p->ny, &q); c->tleft = (double*)q; }
+  if (!p->xper && p->right == 4) { A(sizeof(double) * 10 * p->ny, &q); c->tright = (double*)q; }
   if (p->wall == 3) { A(sizeof(double) * 10 * p->nx, &q); c->bump = (double*)q; }
   if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
@@ -1510,7 +1532,9 @@ int need_data(const lns_ctx3d* c, const char* who) {
   if (!c->have_mean) return fail3(LNS_ERR_ARG, std::string(who) + ": upload the metrics and the mean flow first");
   if (c->prm.ispg != 0 && !c->have_sponge)
     return fail3(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
-  if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1 || c->tleft) && !c->have_inflow)
+  if (!c->prm.xper && c->prm.left == 4 && !c->have_profile)
+    return fail3(LNS_ERR_ARG, std::string(who) + ": left 4: upload the eigenfunction (lns_upload_profile3d) first");
+  if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1 || (c->tleft && c->prm.left == 1)) && !c->have_inflow)
     return fail3(LNS_ERR_ARG,
                  std::string(who) + ": ispg 2, 3, top 1 or left 1: upload the wave data (lns_upload_inflow3d) first");
   if (c->prm.wall == 3 && !c->have_bump)
@@ -1532,7 +1556,7 @@ int make_inflow_target(lns_ctx3d* c) {
         c->g, 1, c->g.ny, 0, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->ttop));
     c->ops.ttop = c->ttop;
   }
-  if (c->tleft) {
+  if (c->tleft && c->prm.left == 1) {
     lns::a3::inflow_target_kernel<<<(unsigned)((c->g.ny + 127) / 128), 128>>>(
         c->g, 0, 0, 1, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->tleft));
     c->ops.tleft = c->tleft;
@@ -1573,7 +1597,7 @@ int lns_upload_sponge3d(lns_ctx3d* c, const double* spg, const double* spg2) {
 
 int lns_upload_inflow3d(lns_ctx3d* c, const double* x, const double* wamp, double x0) {
   if (!c || !x) return fail3(LNS_ERR_ARG, "upload_inflow3d: null argument");
-  if (c->prm.ispg != 2 && c->prm.ispg != 3 && c->prm.top != 1 && !c->tleft)
+  if (c->prm.ispg != 2 && c->prm.ispg != 3 && c->prm.top != 1 && !(c->tleft && c->prm.left == 1))
     return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3, top 1 or left 1");
   if (c->prm.ispg == 3 && !wamp) return fail3(LNS_ERR_ARG, "upload_inflow3d: ispg 3 needs wamp");
   if (!std::isfinite(x0)) return fail3(LNS_ERR_ARG, "upload_inflow3d: x0 must be finite");
@@ -1585,6 +1609,37 @@ int lns_upload_inflow3d(lns_ctx3d* c, const double* x, const double* wamp, doubl
   c->x0 = x0;
   c->have_inflow = true;
   return make_inflow_target(c);
+}
+
+int lns_upload_profile3d(lns_ctx3d* c, const double* prof, const double* xr, double lalpha_re, double lalpha_im) {
+  if (!c || !prof) return fail3(LNS_ERR_ARG, "upload_profile3d: null argument");
+  if (c->prm.xper || c->prm.left != 4) return fail3(LNS_ERR_ARG, "upload_profile3d: needs xper = 0 and left 4");
+  if (c->prm.right == 4 && !xr) return fail3(LNS_ERR_ARG, "upload_profile3d: right 4 needs x of column nx");
+  if (!std::isfinite(lalpha_re) || !std::isfinite(lalpha_im))
+    return fail3(LNS_ERR_ARG, "upload_profile3d: lalpha must be finite");
+  int rc = check_device(c);
+  if (rc) return rc;
+  const int ny = c->g.ny;
+  cudaError_t e = cudaMemcpy(c->tleft, prof, sizeof(double) * 10 * ny, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && c->tright) {
+    // src/itrbc3d.f90:357-381: cmplx(re, im) * exp(im * lalpha * x(nx,j))
+    std::vector<double> h((size_t)10 * ny);
+    const std::complex<double> ia(-lalpha_im, lalpha_re);
+    for (int j = 0; j < ny; ++j) {
+      const std::complex<double> f = std::exp(ia * xr[j]);
+      for (int m = 0; m < 5; ++m) {
+        const std::complex<double> z = std::complex<double>(prof[10 * j + 2 * m], prof[10 * j + 2 * m + 1]) * f;
+        h[10 * j + 2 * m] = z.real();
+        h[10 * j + 2 * m + 1] = z.imag();
+      }
+    }
+    e = cudaMemcpy(c->tright, h.data(), sizeof(double) * 10 * ny, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return cuda3(e, "upload profile");
+  c->ops.tleft = c->tleft;
+  c->ops.tright = c->tright;
+  c->have_profile = true;
+  return LNS_OK;
 }
 
 int lns_upload_bump3d(lns_ctx3d* c, const double* bump) {

@@ -96,6 +96,8 @@ struct Ops {
   const double* ttop = nullptr;
   // the forced left boundary (left = 1, xper = 0): its wave at column 1, complex (5,ny)
   const double* tleft = nullptr;
+  // the eigenfunction outflow (right = 4, xper = 0): its values at column nx, complex (5,ny)
+  const double* tright = nullptr;
   // the bump wall (wall = 3): u1w, u2w, u3w, tw, twp, complex (5,nx)
   const double* bump = nullptr;
   // explicit smoother / implicit damping: eps_e buff(nx,ny); null when eps_e = 0

@@ -49,6 +49,12 @@ GOLDEN = {
     "step3d_open": ("3dopen", dict(nx=48, ny=33, seed=4, left=0, right=0), dict(nsteps=10, cflmax=20.0, loctime=1)),
     "step3d_open_wave": ("3dopen", dict(nx=48, ny=33, seed=4, left=1, right=0),
                          dict(nsteps=5, cflmax=0.2, loctime=1, x0=0.5)),
+    # the eigenfunction planes (left 4 inflow, right 4 outflow with the
+    # inflow namelist's complex lalpha) and the held outflow (right 8)
+    "step3d_open_eig": ("3dopen", dict(nx=48, ny=33, seed=5, left=4, right=4, profile_seed=7),
+                        dict(nsteps=10, cflmax=20.0, loctime=1, module=dict(lalpha=0.3 + 0.05j))),
+    "step3d_open_hold": ("3dopen", dict(nx=48, ny=33, seed=6, left=0, right=8),
+                         dict(nsteps=10, cflmax=20.0, loctime=1)),
     # the nonlinear 2D step with a non-periodic xi direction: Riemann planes
     # on both sides; the symmetry plane on the left with the right plane
     # extrapolated (zeroth order) over a viscous layer that itrBC moves
@@ -60,10 +66,18 @@ GOLDEN = {
 }
 
 
-def open_layer(left, right, **kw):
-    """The shear layer with a non-periodic xi direction (xper = 0)."""
+def open_layer(left, right, profile_seed=None, **kw):
+    """The shear layer with a non-periodic xi direction (xper = 0); with
+    profile_seed, an eigenfunction for the planes left 4 / right 4: each
+    variable a seeded complex amplitude of the disturbance's size times a
+    Gaussian of the layer's width."""
     case = shear_layer(**kw)
     case["params"].update(xper=0, left=left, right=right)
+    if profile_seed is not None:
+        rng = np.random.default_rng(profile_seed)
+        y = case["y"][0, :]
+        amp = 1e-6 * (rng.standard_normal(5) + 1j * rng.standard_normal(5))
+        case["profile"] = np.asfortranarray(amp[:, None] * np.exp(-y[None, :] ** 2))
     return case
 
 

@@ -79,15 +79,26 @@ class Run:
         return self.path("output.R.%d" % n)
 
 
-def run3d(case, nsteps, asis=False, **kw):
-    """The reference's ImpDrv3D on the case: (final v, totres history, Run)."""
+def run3d(case, nsteps, asis=False, module=None, **kw):
+    """The reference's ImpDrv3D on the case: (final v, totres history, Run).
+    A case with an eigenfunction plane (left 4) carries its profile,
+    complex (5, ny), written as inflow.dat (src/gendist.f90:40-47) beside an
+    inflow.nml, whose namelist the translated program does not read (its
+    lalpha is set through module)."""
     p = case["params"]
     r = Run()
     refio.write_grid(r.path("grid.dat"), case["x"], case["y"])
     refio.write_metrics(r.path("metric.dat"), case["metrics"])
     refio.write_field(r.path("mean.dat"), case["vm"], Re=p["Re"], Ma=p["Ma"], Pr=p["Pr"])
     refio.write_field(r.path("output.R.0"), case["v"], Re=p["Re"], Ma=p["Ma"], Pr=p["Pr"])
-    r.run(deck3d(case, nsteps, **kw), asis=asis)
+    if case.get("profile") is not None:
+        with open(r.path("inflow.nml"), "w") as f:
+            f.write("&inflow\n/\n")
+        with open(r.path("inflow.dat"), "w") as f:
+            for j, col in enumerate(np.asarray(case["profile"]).T):
+                vals = [float(j + 1)] + [x for z in col for x in (z.real, z.imag)]
+                f.write(" ".join("%.17e" % x for x in vals) + "\n")
+    r.run(deck3d(case, nsteps, **kw), asis=asis, module=module)
     _, v, _ = refio.read_field(r.last_restart(), complex_=True)
     return v, history(r.path("output.h.1")), r
 

@@ -135,11 +135,12 @@ def test_reference_test2d_fixture(cuda):
     assert np.abs(np.asarray(res) - want).max() <= RES_TOL * want.max()
 
 
-@pytest.mark.parametrize("name", ["step3d_open", "step3d_open_wave"])
+@pytest.mark.parametrize("name", ["step3d_open", "step3d_open_wave", "step3d_open_eig", "step3d_open_hold"])
 def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     """A non-periodic xi direction: the boundary-closure rows of the xi LHS
-    (src/lhsbt1f3d.f90), the zero-disturbance and incoming-wave planes
-    (src/itrbc3d.f90:203-414, src/rhsbc3d.f90:167-324,
+    (src/lhsbt1f3d.f90), the zero-disturbance, incoming-wave and
+    eigenfunction inflow planes, the zero-disturbance, eigenfunction and
+    held outflow planes (src/itrbc3d.f90:203-414, src/rhsbc3d.f90:167-324,
     src/lhsbc1f3d.f90:412-448) and the cpenta2bc-factored xi sweep."""
     import sys
 
@@ -151,7 +152,8 @@ def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     kind, cargs, rargs, d = golden(name)
     case = gen_step_golden.open_layer(**cargs)
     drv = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=rargs["cflmax"], loctime=rargs["loctime"],
-                   x=case["x"], x0=rargs.get("x0", 0.0))
+                   x=case["x"], x0=rargs.get("x0", 0.0), profile=case.get("profile"),
+                   lalpha=rargs.get("module", {}).get("lalpha", 0j))
     v = case["v"].copy(order="F")
     drv.itrbc(v)
     res = drv.step(v, nsteps=rargs["nsteps"])
