@@ -311,12 +311,16 @@ __device__ __forceinline__ void store_el(cf* m, long long q, cd v) { m[q] = cf{(
 // consecutive entries; T = cf rounds the FP64 entry to FP32.
 template <typename T>
 __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ mat) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= 125 * o.np) return;
-  const long long p = q / 125;
-  const int e = (int)(q - 125 * p);
+  // 32-bit index arithmetic: creation bounds 125 nx ny below 2^31, and a
+  // 64-bit division by the run-time nx would be a long software sequence
+  const unsigned q32 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q32 >= 125u * (unsigned)o.np) return;
+  const unsigned p32 = q32 / 125u;
+  const long long q = q32, p = p32;
+  const int e = (int)(q32 - 125u * p32);
   const int k = e % 5 + 1, a = (e / 5) % 5 + 1, b = e / 25 + 1;
-  const int i = (int)(p % g.nx) + 1, j = (int)(p / g.nx) + 1;
+  const unsigned jm = p32 / (unsigned)g.nx;
+  const int i = (int)(p32 - jm * (unsigned)g.nx) + 1, j = (int)jm + 1;
   const cd one{1.0, 0.0}, zero{0.0, 0.0};
   const cd ident = (k == 3 && a == b) ? one : zero;
   // the xi boundaries of a non-periodic xi direction (src/lhsbc1f3d.f90:412-448,

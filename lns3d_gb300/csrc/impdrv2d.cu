@@ -489,12 +489,16 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, F
 // serves both orders: zero blocks add exact zeros to the elimination.
 __global__ void lhs2d_kernel(Grid g, Ops o, Far fr, const double* __restrict__ v, int dir, int order2, LhsCoef lc,
                              double* __restrict__ mat) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= 125 * o.np) return;
-  const long long p = q / 125;
-  const int e = (int)(q - 125 * p);
+  // 32-bit index arithmetic: creation bounds 125 nx ny below 2^31, and a
+  // 64-bit division by the run-time nx would be a long software sequence
+  const unsigned q32 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q32 >= 125u * (unsigned)o.np) return;
+  const unsigned p32 = q32 / 125u;
+  const long long q = q32, p = p32;
+  const int e = (int)(q32 - 125u * p32);
   const int k = e % 5 + 1, a = (e / 5) % 5 + 1, b = e / 25 + 1;
-  const int i = (int)(p % g.nx) + 1, j = (int)(p / g.nx) + 1;
+  const unsigned jm = p32 / (unsigned)g.nx;
+  const int i = (int)(p32 - jm * (unsigned)g.nx) + 1, j = (int)jm + 1;
   const double ident = (k == 3 && a == b) ? 1.0 : 0.0;
   const long long np = o.np;
   const double d = o.dtl[p], alfa = g.alfa;
