@@ -19,6 +19,7 @@
 #include "../../include/lns3d_gb300.h"
 #include "adi3d.cuh"
 #include "launch.cuh"
+#include "penta_rows.cuh"
 
 namespace lns {
 namespace a2 {
@@ -802,6 +803,7 @@ struct lns_ctx2d {
   // far fields of the xi planes (xper = 0 with left 0 / right 0): bn(ny,2), pot(5,ny)
   double *bnl = nullptr, *potl = nullptr, *bnr = nullptr, *potr = nullptr;
   int* nbl = nullptr;                     // device: itrBC's edge of the viscous layer
+  double* rowwork = nullptr;              // block-row solves: [U | z] records, 105 per point
   double *v = nullptr, *vold = nullptr, *r = nullptr, *mat = nullptr, *per = nullptr, *per2 = nullptr;
   double *v2old = nullptr, *wavg = nullptr;  // impl 2 / impl 3 state
   long long lstep = 0;                       // steps taken since creation
@@ -927,6 +929,16 @@ int lhs2(lns_ctx2d* c, const double* v, int dir, double* mat, double alfa, cudaS
   return e == cudaSuccess ? LNS_OK : cuda2(e, "lhs2d_kernel launch");
 }
 
+// A boundary-closure solve of the step's LHS in c->mat and right-hand side
+// in c->r (penta1bc / penta2bc semantics): lines of n rows, block-row
+// elimination (penta_rows.cuh)
+int rows2(lns_ctx2d* c, int n, int nsys, long long row_stride, long long line_stride, cudaStream_t st) {
+  const lns::rows::Args a{c->mat, c->r, c->rowwork, n, nsys, row_stride, line_stride, c->status};
+  lns::rows::rows_bc_kernel<<<nsys, lns::rows::kThreads, 0, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LNS_OK : cuda2(e, "rows_bc_kernel launch");
+}
+
 int bc2(lns_ctx2d* c, double* v, cudaStream_t st) {
   const int nt = c->g.nx + c->g.ny;
   lns::a2::bc2d_kernel<<<(nt + 127) / 128, 128, 0, st>>>(c->g, top2(c), v);
@@ -980,9 +992,9 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
         rc = lns::host::launch_p<double>(c->mat, c->r, c->per, c->per2, g.nx, g.ny, 1, g.nx, 2, st, c->status,
                                          c->prm.lhs_order == 2 ? 1 : -1);
       else if (!rc)  // penta2bc along xi (src/impdrv.f90:353-357)
-        rc = lns::host::launch_bc<double>(c->mat, c->r, g.nx, g.ny, 1, g.nx, 2, st, c->status);
+        rc = rows2(c, g.nx, g.ny, 1, g.nx, st);
       if (!rc) rc = lhs2(c, v, 2, c->mat, alfa, st);
-      if (!rc) rc = lns::host::launch_bc<double>(c->mat, c->r, g.ny, g.nx, g.nx, 1, 2, st, c->status);
+      if (!rc) rc = rows2(c, g.ny, g.nx, g.nx, 1, st);
       if (!rc) {
         const long long n = 5 * c->np;
         lns::a3::add_kernel<double, double><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, v, c->r);
@@ -1084,6 +1096,7 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   A(sizeof(double) * 2 * p->nx, &q); c->bnt = (double*)q;
   A(sizeof(double) * 5 * p->nx, &q); c->pot = (double*)q;
   A(sizeof(int), &q); c->nbl = (int*)q;
+  A(sizeof(double) * lns::rows::kRec * np, &q); c->rowwork = (double*)q;
   if (p->xper == 0) {
     A(sizeof(double) * 2 * p->ny, &q); c->bnl = (double*)q;
     A(sizeof(double) * 5 * p->ny, &q); c->potl = (double*)q;
