@@ -988,9 +988,14 @@ int run2(lns_ctx2d* c, double* v, int nsteps, int niter, double* totres_dev, cud
       // the fourth-order path solves with penta2p (its periodic fill-slot
       // quirk kept unless the exact mode is on), the second-order path with
       // solve2p, which has no such quirk (src/nsolve2p.f90)
-      if (!rc && g.xper)
-        rc = lns::host::launch_p<double>(c->mat, c->r, c->per, c->per2, g.nx, g.ny, 1, g.nx, 2, st, c->status,
-                                         c->prm.lhs_order == 2 ? 1 : -1);
+      if (!rc && g.xper) {
+        // penta2p (solve2p for the second-order LHS, which has no fill quirk)
+        const int quirk = c->prm.lhs_order == 2 ? 0 : (g_periodic_exact.load() ? 0 : 1);
+        const lns::rows::PArgs pa{c->mat, c->r, c->rowwork, g.nx - 1, g.ny, 1, g.nx, quirk, c->status};
+        lns::rows::rows_p_kernel<<<g.ny, lns::rows::kThreads, 0, st>>>(pa);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda2(e, "rows_p_kernel launch");
+      }
       else if (!rc)  // penta2bc along xi (src/impdrv.f90:353-357)
         rc = rows2(c, g.nx, g.ny, 1, g.nx, st);
       if (!rc) rc = lhs2(c, v, 2, c->mat, alfa, st);

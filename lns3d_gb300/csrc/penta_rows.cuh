@@ -210,5 +210,273 @@ __global__ void __launch_bounds__(kThreads) rows_bc_kernel(Args a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Periodic lines (penta2p / penta1p semantics, src/penta2p.f): n = np - 1
+// unknown rows; slot k of row t holds column t + k - 3, cyclically.  Rows
+// 1..n-2 run as above with their normalised records spanning the columns
+// [t+1, t+2, n-1, n] (merged where they meet), so row t's window holds
+// columns t-2..t+2 and the two border columns n-1, n.  Rows n-1 and n,
+// whose entries left of the band fill in column by column, are eliminated
+// right-looking: after row c's record is stored, column c leaves both
+// (their columns c..c+2 in a three-block ring, columns n-3..n fixed).
+// With quirk set, row n-3's update of column n-1 from pivot row n-5 lands in
+// column n-2, as the reference's factorisation places it (src/penta2p.f:278,
+// 339); the solution's row np repeats row 1.
+struct PArgs {
+  const double* mat;
+  double* rhs;
+  double* work;          // kRec doubles per row and line
+  int n, nsys;           // unknown rows (np - 1), lines
+  long long row_stride, line_stride;
+  int quirk;
+  int* status;
+};
+
+struct PSmem {
+  double raw[2][130];
+  // window blocks of columns t-2, t-1, t, t+1, t+2, n-1, n (W[25 w + 5 a + b],
+  // a column in two roles kept once: in block 5 or 6), r at 175
+  double W[180];
+  double G[180];
+  double ring[4][kRec];
+  double bot[2][7][25];  // rows n-1, n: columns c..c+2 at c % 3, columns n-3..n at 3..6
+  double brhs[2][5];
+  double xs[4][5];       // back substitution: rows t+1, t+2
+  double xf[2][5];       // x_{n-1}, x_n
+};
+
+__device__ __forceinline__ int gjp_at(int j, int col) {
+  return col < 25 ? 25 * (2 + col / 5) + 5 * j + col % 5 : 175 + j;
+}
+
+__global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
+  __shared__ PSmem S;
+  const int iv = blockIdx.x;
+  if (iv >= a.nsys) return;
+  const int tid = threadIdx.x, n = a.n;
+  auto rec = [&](int t) { return a.row_stride * (t - 1) + a.line_stride * iv; };
+  double* work = a.work + (long long)iv * n * kRec;
+  auto load_raw = [&](int t, int buf) {
+    const double* gm = a.mat + 125 * rec(t);
+    for (int e = tid; e < 125; e += kThreads) cp_async8(&S.raw[buf][e], gm + e);
+    if (tid < 5) cp_async8(&S.raw[buf][125 + tid], a.rhs + 5 * rec(t) + tid);
+    cp_commit();
+  };
+  // slot (1..5) of row t holding column col, or 0
+  auto slot_of = [&](int t, int col) {
+    int k = col - t + 3;
+    if (k < 1) k += n;
+    if (k > n) k -= n;
+    return k >= 1 && k <= 5 ? k : 0;
+  };
+  // the record's block s covers column target(c, s), or 0 when merged away
+  auto target = [&](int c, int s) {
+    if (s == 0) return c + 1 < n - 1 ? c + 1 : 0;
+    if (s == 1) return c + 2 < n - 1 ? c + 2 : 0;
+    return s == 2 ? n - 1 : n;
+  };
+  auto widx = [&](int t, int col) { return col == n - 1 ? 5 : col == n ? 6 : col - t + 2; };
+  auto bidx = [&](int col) { return col >= n - 3 ? 3 + col - (n - 3) : col % 3; };
+  // per-thread roles
+  const int d0 = tid / 25, ar = tid < 100 ? (tid % 25) / 5 : tid - 100, eb = tid % 5;
+  const int gj0 = tid / 26, gc0 = tid % 26, ga0 = gjp_at(gj0, gc0);
+  const int gj1 = 4, gc1 = 24 + tid, ga1 = tid < 2 ? gjp_at(gj1, gc1) : 0;
+  auto roff = [](int j, int col) { return col < 25 ? 25 * ((col - 5) / 5) + 5 * j + (col - 5) % 5 : 100 + j; };
+
+  // rows n-1 and n start in the bottom storage
+  for (int e = tid; e < 350; e += kThreads) (&S.bot[0][0][0])[e] = 0.0;
+  __syncthreads();
+  for (int e = tid; e < 260; e += kThreads) {
+    const int b = e / 130, x = e % 130, t = n - 1 + b;
+    const double val = a.mat[125 * rec(t) + (x < 125 ? x : 0)];
+    if (x < 125) {
+      const int k = x % 5 + 1, m = (x / 5) % 5, q = x / 25;
+      int col = t + k - 3;
+      if (col > n) col -= n;
+      S.bot[b][bidx(col)][5 * m + q] = val;
+    } else {
+      S.brhs[b][x - 125] = a.rhs[5 * rec(t) + x - 125];
+    }
+  }
+
+  // Gauss-Jordan of the prepared window, then [U_t | z_t] into the ring and work
+  auto normalise = [&](int t) {
+    double* cur = S.W;
+    double* nxt = S.G;
+#pragma unroll 1
+    for (int k = 0; k < 5; ++k) {
+      const double piv = cur[gjp_at(k, k)];
+      if (gc0 > k) {
+        const double g = cur[ga0];
+        nxt[ga0] = gj0 == k ? g : fma(-cur[gjp_at(gj0, k)], cur[gjp_at(k, gc0)], g * piv);
+      }
+      if (tid < 2) {
+        const double g = cur[ga1];
+        nxt[ga1] = k == 4 ? g : fma(-cur[gjp_at(gj1, k)], cur[gjp_at(k, gc1)], g * piv);
+      }
+      if (tid < k) nxt[gjp_at(tid, tid)] = cur[gjp_at(tid, tid)] * piv;
+      if (tid == k) nxt[gjp_at(k, k)] = piv;
+      double* sw = cur;
+      cur = nxt;
+      nxt = sw;
+      __syncthreads();
+    }
+    double* R = S.ring[(t - 1) & 3];
+    double* gw = work + (long long)(t - 1) * kRec;
+    if (gc0 >= 5) {
+      const double dj = cur[gjp_at(gj0, gj0)];
+      if (gc0 == 25 && !(fabs(dj) > 0.0 && isfinite(dj)) && a.status) atomicExch(a.status, 1);
+      const double val = cur[ga0] * recip(dj);
+      const int off = roff(gj0, gc0);
+      R[off] = val;
+      gw[off] = val;
+    }
+    if (tid < 2) {
+      const double dj = cur[gjp_at(gj1, gj1)];
+      if (tid == 1 && !(fabs(dj) > 0.0 && isfinite(dj)) && a.status) atomicExch(a.status, 1);
+      const double val = cur[ga1] * recip(dj);
+      const int off = roff(gj1, gc1);
+      R[off] = val;
+      gw[off] = val;
+    }
+    __syncthreads();
+  };
+
+  load_raw(1, 0);
+  for (int t = 1; t <= n - 2; ++t) {
+    const int buf = (t - 1) & 1;
+    cp_wait_all();
+    __syncthreads();
+    // the window: block w covers column t + w - 2 (w < 5, cyclically) or n-1, n
+    for (int e = tid; e < 180; e += kThreads) {
+      double val;
+      if (e < 175) {
+        const int w = e / 25, ab = e % 25;
+        int col = w == 5 ? n - 1 : w == 6 ? n : t + w - 2;
+        if (col < 1) col += n;
+        const bool own = w >= 5 || (col != n - 1 && col != n);
+        const int k = own ? slot_of(t, col) : 0;
+        val = k ? S.raw[buf][(k - 1) + 5 * (ab / 5) + 25 * (ab % 5)] : 0.0;
+      } else {
+        val = S.raw[buf][125 + e - 175];
+      }
+      S.W[e] = val;
+    }
+    __syncthreads();
+    if (t < n - 2) load_raw(t + 1, buf ^ 1);
+    // eliminate columns t-2, t-1
+    for (int c = t - 2; c < t; ++c) {
+      if (c < 1) continue;
+      const double* U = S.ring[(c - 1) & 3];
+      const double* L = S.W + 25 * (c - t + 2);
+      int col = tid < 100 ? target(c, d0) : 1;
+      if (tid < 100 && a.quirk && t == n - 3 && c == n - 5 && d0 == 2) col = n - 2;
+      if (tid < 100 ? col > 0 : tid < 105) {
+        const int at = tid < 100 ? 25 * widx(t, col) + 5 * ar + eb : 175 + ar;
+        const int ub = tid < 100 ? 25 * d0 + eb : 100;
+        const int us = tid < 100 ? 5 : 1;
+        double acc = S.W[at];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) acc = fma(-L[5 * ar + q], U[ub + us * q], acc);
+        S.W[at] = acc;
+      }
+      __syncthreads();
+    }
+    normalise(t);
+    // column t leaves rows n-1 and n
+    {
+      const double* R = S.ring[(t - 1) & 3];
+      for (int o = tid; o < 210; o += kThreads) {
+        const int b = o / 105, oo = o % 105;
+        const double* L = S.bot[b][bidx(t)];
+        if (oo < 100) {
+          const int s = oo / 25, r5 = (oo % 25) / 5, c5 = oo % 5, col = target(t, s);
+          if (col > 0) {
+            double* dst = &S.bot[b][bidx(col)][5 * r5 + c5];
+            double acc = *dst;
+#pragma unroll
+            for (int q = 0; q < 5; ++q) acc = fma(-L[5 * r5 + q], R[25 * s + 5 * q + c5], acc);
+            *dst = acc;
+          }
+        } else {
+          const int r5 = oo - 100;
+          double acc = S.brhs[b][r5];
+#pragma unroll
+          for (int q = 0; q < 5; ++q) acc = fma(-L[5 * r5 + q], R[100 + q], acc);
+          S.brhs[b][r5] = acc;
+        }
+      }
+      __syncthreads();
+      // column t's ring slot will hold column t + 3
+      if (t < n - 3 && tid < 50) S.bot[tid / 25][t % 3][tid % 25] = 0.0;
+    }
+  }
+  // row n-1: [C | block n | r] from the bottom storage
+  for (int e = tid; e < 180; e += kThreads) {
+    const int w = e / 25, ab = e % 25;
+    double val = 0.0;
+    if (e >= 175) val = S.brhs[0][e - 175];
+    else if (w == 2) val = S.bot[0][5][ab];
+    else if (w == 6) val = S.bot[0][6][ab];
+    S.W[e] = val;
+  }
+  __syncthreads();
+  normalise(n - 1);
+  // row n: column n-1 leaves it, then [C | r]
+  {
+    const double* R = S.ring[(n - 2) & 3];
+    const double* L = S.bot[1][5];
+    if (tid < 30) {
+      const int r5 = tid < 25 ? tid / 5 : tid - 25, c5 = tid % 5;
+      double acc = tid < 25 ? S.bot[1][6][5 * r5 + c5] : S.brhs[1][r5];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) acc = fma(-L[5 * r5 + q], tid < 25 ? R[75 + 5 * q + c5] : R[100 + q], acc);
+      if (tid < 25) S.bot[1][6][5 * r5 + c5] = acc;
+      else S.brhs[1][r5] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < 180; e += kThreads) {
+      const int w = e / 25, ab = e % 25;
+      double val = 0.0;
+      if (e >= 175) val = S.brhs[1][e - 175];
+      else if (w == 2) val = S.bot[1][6][ab];
+      S.W[e] = val;
+    }
+    __syncthreads();
+    normalise(n);
+  }
+  // back substitution, rows n..1
+  const int a5 = tid >> 4, p = tid & 15;
+  auto load_rec = [&](int t, int buf) {
+    const double* src = work + (long long)(t - 1) * kRec;
+    for (int e = tid; e < kRec; e += kThreads) cp_async8(&S.raw[buf][e], src + e);
+    cp_commit();
+  };
+  auto xat = [&](int col) -> double* { return col >= n - 1 ? S.xf[col - (n - 1)] : S.xs[(col - 1) & 3]; };
+  load_rec(n, 0);
+  for (int t = n; t >= 1; --t) {
+    const int buf = (n - t) & 1;
+    cp_wait_all();
+    __syncthreads();
+    if (t > 1) load_rec(t - 1, buf ^ 1);
+    double part = 0.0;
+    if (a5 < 5) {
+      for (int term = p; term < 20; term += 16) {
+        const int s = term / 5, q = term % 5;
+        const int col = t <= n - 2 ? target(t, s) : (t == n - 1 && s == 3 ? n : 0);
+        if (col > 0) part = fma(S.raw[buf][25 * s + 5 * a5 + q], xat(col)[q], part);
+      }
+    }
+    for (int sh = 8; sh > 0; sh >>= 1) part += __shfl_down_sync(0xffffffffu, part, sh, 16);
+    __syncthreads();
+    if (a5 < 5 && p == 0) {
+      const double x = S.raw[buf][100 + a5] - part;
+      xat(t)[a5] = x;
+      a.rhs[5 * rec(t) + a5] = x;
+      if (t == 1) a.rhs[5 * rec(n + 1) + a5] = x;  // the periodic image, row np
+    }
+  }
+}
+
 }  // namespace rows
 }  // namespace lns
