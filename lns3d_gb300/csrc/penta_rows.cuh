@@ -63,6 +63,58 @@ __device__ __forceinline__ void cp_async8(double* dst, const double* src) {
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
+// Gauss-Jordan on [C | four blocks | r] held in a window layout: block
+// column col / 5 of the right part at DB + 25 (col / 5), the right-hand side
+// at RB.  Thread roles: entry (tid / 26, tid % 26), and for threads 0 and 1
+// also (4, 24 + tid); addresses fixed for the line.
+template <int DB, int RB>
+struct GjRoles {
+  int j0, c0, a0, k0, p0, s0;  // own entry; (j0, 0); (0, c0); row stride of column c0
+  int a1, k1, p1, s1;
+  static __device__ __forceinline__ int at(int j, int col) {
+    return col < 25 ? DB + 25 * (col / 5) + 5 * j + col % 5 : RB + j;
+  }
+  __device__ explicit GjRoles(int tid) {
+    j0 = tid / 26;
+    c0 = tid % 26;
+    a0 = at(j0, c0);
+    k0 = DB + 5 * j0;
+    p0 = at(0, c0);
+    s0 = c0 < 25 ? 5 : 1;
+    const int c1 = 24 + tid;
+    a1 = tid < 2 ? at(4, c1) : 0;
+    k1 = DB + 20;
+    p1 = tid < 2 ? at(0, c1) : 0;
+    s1 = c1 < 25 ? 5 : 1;
+  }
+};
+
+// Five division-free steps: each scales the other rows by the pivot and
+// subtracts the pivot row; the rows already pivoted keep only their
+// diagonal, scaled too.  Returns the buffer holding the result.
+template <int DB, int RB>
+__device__ __forceinline__ double* gauss_jordan(double* cur, double* nxt, const GjRoles<DB, RB>& g, int tid) {
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const double piv = cur[DB + 6 * k];
+    if (g.c0 > k) {
+      const double x = cur[g.a0];
+      nxt[g.a0] = g.j0 == k ? x : fma(-cur[g.k0 + k], cur[g.p0 + g.s0 * k], x * piv);
+    }
+    if (tid < 2) {
+      const double x = cur[g.a1];
+      nxt[g.a1] = k == 4 ? x : fma(-cur[g.k1 + k], cur[g.p1 + g.s1 * k], x * piv);
+    }
+    if (tid < k) nxt[DB + 6 * tid] = cur[DB + 6 * tid] * piv;
+    if (tid == k) nxt[DB + 6 * k] = piv;
+    double* sw = cur;
+    cur = nxt;
+    nxt = sw;
+    __syncthreads();
+  }
+  return cur;
+}
+
 struct Smem {
   double raw[2][130];          // prefetched records: 125 matrix entries (reference order) and 5 rhs
   // the row's window of block columns, W[25 o + 5 a + b] (o = column - t + 4),
@@ -73,12 +125,6 @@ struct Smem {
   double ring[4][kRec];        // [U | z] of the last four rows
   double xs[4][5];             // back substitution: the last four solutions
 };
-
-// Gauss-Jordan entry (row j, column col) of [C | blocks t+1..t+4 | r] in
-// the window layout
-__device__ __forceinline__ int gj_at(int j, int col) {
-  return col < 25 ? 25 * (4 + col / 5) + 5 * j + col % 5 : 225 + j;
-}
 
 __global__ void __launch_bounds__(kThreads) rows_bc_kernel(Args a) {
   __shared__ Smem S;
@@ -103,9 +149,10 @@ __global__ void __launch_bounds__(kThreads) rows_bc_kernel(Args a) {
   // elimination output: block d0 (column c + d0 + 1), entry (ar, eb); r[ar] for threads 100..104
   const int d0 = tid / 25, ar = tid < 100 ? (tid % 25) / 5 : tid - 100, eb = tid % 5;
   // Gauss-Jordan entries e = tid (all threads) and tid + 128 (two threads)
-  const int gj0 = tid / 26, gc0 = tid % 26, ga0 = gj_at(gj0, gc0);
-  const int gj1 = 4, gc1 = 24 + tid, ga1 = tid < 2 ? gj_at(gj1, gc1) : 0;
+  const GjRoles<100, 225> gr(tid);
+  const int gj0 = gr.j0, gc0 = gr.c0, ga0 = gr.a0, gj1 = 4, gc1 = 24 + tid, ga1 = gr.a1;
   auto roff = [](int j, int col) { return col < 25 ? 25 * ((col - 5) / 5) + 5 * j + (col - 5) % 5 : 100 + j; };
+  const int off0 = roff(gj0, gc0 < 5 ? 5 : gc0), off1 = roff(gj1, gc1);
 
   load_raw(1, 0);
   for (int t = 1; t <= n; ++t) {
@@ -135,52 +182,29 @@ __global__ void __launch_bounds__(kThreads) rows_bc_kernel(Args a) {
     }
     // Gauss-Jordan on [C | blocks t+1..t+4 | r] (zero blocks past the row's
     // reach stay zero) without divisions, ping-pong between W and G
-    double* cur = S.W;
-    double* nxt = S.G;
-#pragma unroll 1
-    for (int k = 0; k < 5; ++k) {
-      const double piv = cur[gj_at(k, k)];
-      if (gc0 > k) {
-        const double g = cur[ga0];
-        nxt[ga0] = gj0 == k ? g : fma(-cur[gj_at(gj0, k)], cur[gj_at(k, gc0)], g * piv);
-      }
-      if (tid < 2) {
-        const double g = cur[ga1];
-        nxt[ga1] = k == 4 ? g : fma(-cur[gj_at(gj1, k)], cur[gj_at(k, gc1)], g * piv);
-      }
-      // the diagonals of the rows already pivoted, which the step scales by
-      // the pivot (their entry in the pivot row's column is zero), and the
-      // pivot row's own
-      if (tid < k) nxt[gj_at(tid, tid)] = cur[gj_at(tid, tid)] * piv;
-      if (tid == k) nxt[gj_at(k, k)] = piv;
-      double* sw = cur;
-      cur = nxt;
-      nxt = sw;
-      __syncthreads();
-    }
+    double* cur = gauss_jordan(S.W, S.G, gr, tid);
     // divide by the accumulated diagonals; store [U_t | z_t]
     double* R = S.ring[(t - 1) & 3];
     double* gw = work + (long long)(t - 1) * kRec;
     if (gc0 >= 5) {
-      const double dj = cur[gj_at(gj0, gj0)];
+      const double dj = cur[100 + 6 * gj0];
       if (gc0 == 25 && !(fabs(dj) > 0.0 && isfinite(dj)) && a.status) atomicExch(a.status, 1);
       const double val = cur[ga0] * recip(dj);
-      const int off = roff(gj0, gc0);
-      R[off] = val;
-      gw[off] = val;
+      R[off0] = val;
+      gw[off0] = val;
     }
     if (tid < 2) {
-      const double dj = cur[gj_at(gj1, gj1)];
+      const double dj = cur[100 + 6 * gj1];
       if (tid == 1 && !(fabs(dj) > 0.0 && isfinite(dj)) && a.status) atomicExch(a.status, 1);
       const double val = cur[ga1] * recip(dj);
-      const int off = roff(gj1, gc1);
-      R[off] = val;
-      gw[off] = val;
+      R[off1] = val;
+      gw[off1] = val;
     }
     __syncthreads();
   }
   // back substitution, rows n..1: the records of row t-1 prefetched during row t
   const int a5 = tid >> 4, p = tid & 15;  // unknown a5 (< 5), its 16-lane group
+  const int dA = p / 5 + 1, qA = p % 5, dB = (p + 16) / 5 + 1, qB = (p + 16) % 5;
   auto load_rec = [&](int t, int buf) {
     const double* src = work + (long long)(t - 1) * kRec;
     for (int e = tid; e < kRec; e += kThreads) cp_async8(&S.raw[buf][e], src + e);
@@ -194,11 +218,9 @@ __global__ void __launch_bounds__(kThreads) rows_bc_kernel(Args a) {
     if (t > 1) load_rec(t - 1, buf ^ 1);
     const int w = lo_col(t, n) + 4 - t;
     double part = 0.0;
-    if (a5 < 5) {
-      for (int term = p; term < 5 * w; term += 16) {
-        const int d = term / 5 + 1, q = term % 5;
-        part = fma(S.raw[buf][25 * (d - 1) + 5 * a5 + q], S.xs[(t + d - 1) & 3][q], part);
-      }
+    if (a5 < 5) {  // terms p and p + 16 of sum_d U_t[d] x_{t+d}: block dA / dB, entry qA / qB
+      if (p < 5 * w) part = S.raw[buf][25 * (dA - 1) + 5 * a5 + qA] * S.xs[(t + dA - 1) & 3][qA];
+      if (p + 16 < 5 * w) part = fma(S.raw[buf][25 * (dB - 1) + 5 * a5 + qB], S.xs[(t + dB - 1) & 3][qB], part);
     }
     for (int s = 8; s > 0; s >>= 1) part += __shfl_down_sync(0xffffffffu, part, s, 16);
     __syncthreads();  // every read of xs for row t is done before row t's value replaces row t+4's
@@ -245,10 +267,6 @@ struct PSmem {
   double xf[2][5];       // x_{n-1}, x_n
 };
 
-__device__ __forceinline__ int gjp_at(int j, int col) {
-  return col < 25 ? 25 * (2 + col / 5) + 5 * j + col % 5 : 175 + j;
-}
-
 __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
   __shared__ PSmem S;
   const int iv = blockIdx.x;
@@ -279,9 +297,10 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
   auto bidx = [&](int col) { return col >= n - 3 ? 3 + col - (n - 3) : col % 3; };
   // per-thread roles
   const int d0 = tid / 25, ar = tid < 100 ? (tid % 25) / 5 : tid - 100, eb = tid % 5;
-  const int gj0 = tid / 26, gc0 = tid % 26, ga0 = gjp_at(gj0, gc0);
-  const int gj1 = 4, gc1 = 24 + tid, ga1 = tid < 2 ? gjp_at(gj1, gc1) : 0;
+  const GjRoles<50, 175> gr(tid);
+  const int gj0 = gr.j0, gc0 = gr.c0, ga0 = gr.a0, gj1 = 4, gc1 = 24 + tid, ga1 = gr.a1;
   auto roff = [](int j, int col) { return col < 25 ? 25 * ((col - 5) / 5) + 5 * j + (col - 5) % 5 : 100 + j; };
+  const int off0 = roff(gj0, gc0 < 5 ? 5 : gc0), off1 = roff(gj1, gc1);
 
   // rows n-1 and n start in the bottom storage
   for (int e = tid; e < 350; e += kThreads) (&S.bot[0][0][0])[e] = 0.0;
@@ -301,43 +320,22 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
 
   // Gauss-Jordan of the prepared window, then [U_t | z_t] into the ring and work
   auto normalise = [&](int t) {
-    double* cur = S.W;
-    double* nxt = S.G;
-#pragma unroll 1
-    for (int k = 0; k < 5; ++k) {
-      const double piv = cur[gjp_at(k, k)];
-      if (gc0 > k) {
-        const double g = cur[ga0];
-        nxt[ga0] = gj0 == k ? g : fma(-cur[gjp_at(gj0, k)], cur[gjp_at(k, gc0)], g * piv);
-      }
-      if (tid < 2) {
-        const double g = cur[ga1];
-        nxt[ga1] = k == 4 ? g : fma(-cur[gjp_at(gj1, k)], cur[gjp_at(k, gc1)], g * piv);
-      }
-      if (tid < k) nxt[gjp_at(tid, tid)] = cur[gjp_at(tid, tid)] * piv;
-      if (tid == k) nxt[gjp_at(k, k)] = piv;
-      double* sw = cur;
-      cur = nxt;
-      nxt = sw;
-      __syncthreads();
-    }
+    double* cur = gauss_jordan(S.W, S.G, gr, tid);
     double* R = S.ring[(t - 1) & 3];
     double* gw = work + (long long)(t - 1) * kRec;
     if (gc0 >= 5) {
-      const double dj = cur[gjp_at(gj0, gj0)];
+      const double dj = cur[50 + 6 * gj0];
       if (gc0 == 25 && !(fabs(dj) > 0.0 && isfinite(dj)) && a.status) atomicExch(a.status, 1);
       const double val = cur[ga0] * recip(dj);
-      const int off = roff(gj0, gc0);
-      R[off] = val;
-      gw[off] = val;
+      R[off0] = val;
+      gw[off0] = val;
     }
     if (tid < 2) {
-      const double dj = cur[gjp_at(gj1, gj1)];
+      const double dj = cur[50 + 6 * gj1];
       if (tid == 1 && !(fabs(dj) > 0.0 && isfinite(dj)) && a.status) atomicExch(a.status, 1);
       const double val = cur[ga1] * recip(dj);
-      const int off = roff(gj1, gc1);
-      R[off] = val;
-      gw[off] = val;
+      R[off1] = val;
+      gw[off1] = val;
     }
     __syncthreads();
   };
@@ -447,6 +445,7 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
   }
   // back substitution, rows n..1
   const int a5 = tid >> 4, p = tid & 15;
+  const int sA = p / 5, qA = p % 5, qB = (p + 16) % 5;  // term p + 16 (p < 4) lies in block 3
   auto load_rec = [&](int t, int buf) {
     const double* src = work + (long long)(t - 1) * kRec;
     for (int e = tid; e < kRec; e += kThreads) cp_async8(&S.raw[buf][e], src + e);
@@ -460,11 +459,12 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
     __syncthreads();
     if (t > 1) load_rec(t - 1, buf ^ 1);
     double part = 0.0;
-    if (a5 < 5) {
-      for (int term = p; term < 20; term += 16) {
-        const int s = term / 5, q = term % 5;
-        const int col = t <= n - 2 ? target(t, s) : (t == n - 1 && s == 3 ? n : 0);
-        if (col > 0) part = fma(S.raw[buf][25 * s + 5 * a5 + q], xat(col)[q], part);
+    if (a5 < 5) {  // terms p and p + 16 of sum_s U_t[s] x_{target(s)}
+      const int colA = t <= n - 2 ? target(t, sA) : (t == n - 1 && sA == 3 ? n : 0);
+      if (colA > 0) part = S.raw[buf][25 * sA + 5 * a5 + qA] * xat(colA)[qA];
+      if (p < 4) {
+        const int colB = t <= n - 2 ? target(t, 3) : (t == n - 1 ? n : 0);
+        if (colB > 0) part = fma(S.raw[buf][75 + 5 * a5 + qB], xat(colB)[qB], part);
       }
     }
     for (int sh = 8; sh > 0; sh >>= 1) part += __shfl_down_sync(0xffffffffu, part, sh, 16);
