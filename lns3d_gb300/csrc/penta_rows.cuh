@@ -154,16 +154,25 @@ __global__ void __launch_bounds__(kThreads) rows_bc_kernel(Args a) {
   auto roff = [](int j, int col) { return col < 25 ? 25 * ((col - 5) / 5) + 5 * j + (col - 5) % 5 : 100 + j; };
   const int off0 = roff(gj0, gc0 < 5 ? 5 : gc0), off1 = roff(gj1, gc1);
 
-  load_raw(1, 0);
-  for (int t = 1; t <= n; ++t) {
+  // the window of row t from its record in raw buffer (t - 1) & 1
+  auto build_window = [&](int t) {
     const int buf = (t - 1) & 1;
-    cp_wait_all();
-    __syncthreads();
-    const int lo = lo_col(t, n), olo = lo - t + 4;  // the row holds block columns olo..olo+4
+    const int olo = lo_col(t, n) - t + 4;  // the row holds block columns olo..olo+4
     S.W[we0] = (wo0 >= olo && wo0 <= olo + 4) ? S.raw[buf][src0] : 0.0;
     if (we1 < 230) S.W[we1] = we1 >= 225 || (wo1 >= olo && wo1 <= olo + 4) ? S.raw[buf][src1] : 0.0;
-    __syncthreads();
-    if (t < n) load_raw(t + 1, buf ^ 1);
+  };
+
+  // Row t's window is built in row t-1's last segment, while row t+1's
+  // record is on its way: per row, the eliminations, five Gauss-Jordan
+  // steps and the store, each closed by one barrier.
+  load_raw(1, 0);
+  cp_wait_all();
+  __syncthreads();
+  build_window(1);
+  if (n > 1) load_raw(2, 1);
+  __syncthreads();
+  for (int t = 1; t <= n; ++t) {
+    const int lo = lo_col(t, n);
     // eliminate the columns left of the diagonal, ascending
     for (int c = lo; c < t; ++c) {
       const int wc = lo_col(c, n) + 4 - c;  // row c's normalised part spans c+1..c+wc
@@ -182,10 +191,16 @@ __global__ void __launch_bounds__(kThreads) rows_bc_kernel(Args a) {
     }
     // Gauss-Jordan on [C | blocks t+1..t+4 | r] (zero blocks past the row's
     // reach stay zero) without divisions, ping-pong between W and G
+    cp_wait_all();  // row t+1's record, visible after the Gauss-Jordan barriers
     double* cur = gauss_jordan(S.W, S.G, gr, tid);
-    // divide by the accumulated diagonals; store [U_t | z_t]
+    // divide by the accumulated diagonals; store [U_t | z_t]; the window of
+    // row t+1 (W is free: the result is in G)
     double* R = S.ring[(t - 1) & 3];
     double* gw = work + (long long)(t - 1) * kRec;
+    if (t < n) {
+      build_window(t + 1);
+      if (t + 1 < n) load_raw(t + 2, (t + 1) & 1);
+    }
     if (gc0 >= 5) {
       const double dj = cur[100 + 6 * gj0];
       if (gc0 == 25 && !(fabs(dj) > 0.0 && isfinite(dj)) && a.status) atomicExch(a.status, 1);
@@ -340,12 +355,10 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
     __syncthreads();
   };
 
-  load_raw(1, 0);
-  for (int t = 1; t <= n - 2; ++t) {
+  // the window of row t from raw buffer (t - 1) & 1: block w covers column
+  // t + w - 2 (w < 5, cyclically) or n-1, n
+  auto build_window = [&](int t) {
     const int buf = (t - 1) & 1;
-    cp_wait_all();
-    __syncthreads();
-    // the window: block w covers column t + w - 2 (w < 5, cyclically) or n-1, n
     for (int e = tid; e < 180; e += kThreads) {
       double val;
       if (e < 175) {
@@ -360,8 +373,19 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
       }
       S.W[e] = val;
     }
-    __syncthreads();
-    if (t < n - 2) load_raw(t + 1, buf ^ 1);
+  };
+
+  // as in rows_bc_kernel, row t's window is built in row t-1's last
+  // segment (here beside the elimination of column t-1 from the last rows)
+  load_raw(1, 0);
+  cp_wait_all();
+  __syncthreads();
+  build_window(1);
+  if (n - 2 > 1) load_raw(2, 1);
+  __syncthreads();
+  for (int t = 1; t <= n - 2; ++t) {
+    // column t-1's ring slot in the last rows will hold column t + 2
+    if (t - 1 >= 1 && t - 1 < n - 3 && tid < 50) S.bot[tid / 25][(t - 1) % 3][tid % 25] = 0.0;
     // eliminate columns t-2, t-1
     for (int c = t - 2; c < t; ++c) {
       if (c < 1) continue;
@@ -380,9 +404,14 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
       }
       __syncthreads();
     }
+    cp_wait_all();  // row t+1's record, visible after the Gauss-Jordan barriers
     normalise(t);
-    // column t leaves rows n-1 and n
+    // column t leaves rows n-1 and n; the window of row t+1 (W is free)
     {
+      if (t < n - 2) {
+        build_window(t + 1);
+        if (t + 1 < n - 2) load_raw(t + 2, (t + 1) & 1);
+      }
       const double* R = S.ring[(t - 1) & 3];
       for (int o = tid; o < 210; o += kThreads) {
         const int b = o / 105, oo = o % 105;
@@ -405,8 +434,6 @@ __global__ void __launch_bounds__(kThreads) rows_p_kernel(PArgs a) {
         }
       }
       __syncthreads();
-      // column t's ring slot will hold column t + 3
-      if (t < n - 3 && tid < 50) S.bot[tid / 25][t % 3][tid % 25] = 0.0;
     }
   }
   // row n-1: [C | block n | r] from the bottom storage
