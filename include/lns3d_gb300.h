@@ -379,8 +379,15 @@ typedef struct {
                                 src/lhsbc2f3d.f90:146-174): left 0 zero disturbance, 1 an
                                 incoming acoustic wave exp(-a (x - x0)) exp(i kk x) formed from
                                 the mean flow (lns_upload_inflow3d), 4 the eigenfunction inflow
-                                (lns_upload_profile3d); right 0 zero disturbance, 4 the
-                                eigenfunction outflow (with left 4), 8 the held initial condition.
+                                (lns_upload_profile3d), 7 a symmetry plane; right 0 zero
+                                disturbance, 4 the eigenfunction outflow (with left 4), 7 a
+                                symmetry plane, 8 the held initial condition.  A symmetry plane
+                                (src/cgrad.f90:193-266, src/lhsbs1f3d.f90) mirrors the field,
+                                v changing sign, into the stencils of its three nearest points
+                                and the xi LHS rows of its two; eps_e must then be 0, and
+                                ny <= nx (those rows read ABhi through the reference's
+                                (6,ny,nx) view of the (6,nx,ny) array, src/lhsbs1f3d.f90:17,
+                                which the GPU reproduces and which leaves the array when ny > nx).
                                 Ignored with xper = 1.  Batches and servers take xper = 1. */
 } lns_params3d;
 

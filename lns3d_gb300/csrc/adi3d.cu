@@ -256,7 +256,8 @@ __global__ void genmtrx_kernel(Grid g, const double* __restrict__ vm, Metrics mt
 // dtl (a X + rcalcd alfa (Dh + i Dhi)).  The operations run in the order of
 // the reference's loops.
 __device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, long long p, int k, int a, int b,
-                                        double ak, double bk, bool combined, int damp) {
+                                        double ak, double bk, bool combined, int damp, double dampc = 0.0,
+                                        long long pab = -1) {
   const long long np = o.np;
   const long long e = (long long)((a - 1) + 5 * (b - 1)) * np + p;
   const double x = (dir == 1 ? o.Ah : o.Bh)[e];
@@ -273,8 +274,9 @@ __device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, lo
   }
   // \hat{A}_i, \hat{B}_i: c_k = i a_k
   const double w = ak * d;
-  if ((a == 2 && b == 4) || (a == 4 && b == 2)) im = im - w * o.AB[(dir == 1 ? 0 : 2) * np + p];
-  if ((a == 3 && b == 4) || (a == 4 && b == 3)) im = im - w * o.AB[(dir == 1 ? 1 : 3) * np + p];
+  const long long pa = pab < 0 ? p : pab;
+  if ((a == 2 && b == 4) || (a == 4 && b == 2)) im = im - w * o.AB[(dir == 1 ? 0 : 2) * np + pa];
+  if ((a == 3 && b == 4) || (a == 4 && b == 3)) im = im - w * o.AB[(dir == 1 ? 1 : 3) * np + pa];
   if (calcd && !combined && k == 3) {
     re = re + alfa * d * o.Dh[e];
     im = im + alfa * d * o.Dhi[e];
@@ -293,7 +295,9 @@ __device__ __forceinline__ cd lhs_entry(const Grid& g, const Ops& o, int dir, lo
   // src/lhs2f3d.f90:171-203), 2 the eta rows 2 and ny-1, (-1, 2, -1) in
   // slots 2..4 (src/lhsbt2f3d.f90:277-298, 431-452), 1 none (rows 1, ny)
   if (o.buff && a == b && damp != 1) {
-    const double c = damp == 0 ? pick5(k - 1, 1.0, -4.0, 6.0, -4.0, 1.0) : pick5(k - 1, 0.0, -1.0, 2.0, -1.0, 0.0);
+    const double c = damp == 0   ? pick5(k - 1, 1.0, -4.0, 6.0, -4.0, 1.0)
+                     : damp == 3 ? dampc
+                                 : pick5(k - 1, 0.0, -1.0, 2.0, -1.0, 0.0);
     if (c != 0.0) re = re + g.alfa * d * o.eps_e * o.buff[p] * c;
   }
   // sponge of the eta LHS (src/lhs2f3d.f90:207-224, src/lhsbt2f3d.f90:147-167;
@@ -348,6 +352,30 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
   const int pos = dir == 1 ? i : j, n = dir == 1 ? g.nx : g.ny;
   double ak, bk;
   bool combined = false;
+  const int sym = dir == 1 ? xsym(g) : 0;
+  if (((sym & 1) && pos <= 2) || ((sym & 2) && pos >= n - 1)) {
+    // symmetry plane (src/lhsbs1f3d.f90): the band stencil with the nodes
+    // beyond the plane folded onto their mirror images, times -1 in the
+    // columns of the component that changes sign (b = 3)
+    const double sg = b == 3 ? -1.0 : 1.0;
+    double fa = 0.0, fb = 0.0;
+    for (int o5 = 0; o5 < 5; ++o5) {
+      int m = pos + o5 - 2;
+      bool mir = false;
+      if (m < 1) m = 2 - m, mir = true;
+      if (m > n) m = 2 * n - m, mir = true;
+      if (m - pos + 3 != k) continue;
+      fa = fa + (mir ? sg * lc.ak[o5] : lc.ak[o5]);
+      fb = fb + (mir ? sg * lc.bk[o5] : lc.bk[o5]);
+    }
+    // the reference declares this routine's ABhi dummy (6,ny,nx) for the
+    // (6,nx,ny) actual, so it reads entry (k, i, j) at point (i-1) + ny (j-1)
+    // (src/lhsbs1f3d.f90:17); creation requires ny <= nx, which keeps that
+    // point inside the array
+    const long long pab = (long long)(i - 1) + (long long)g.ny * (j - 1);
+    store_el(mat, q, lhs_entry(g, o, dir, p, k, a, b, fa, fb, true, 3, 0.0, pab));
+    return;
+  }
   if (per || (pos > 2 && pos < n - 1)) {
     ak = lc.ak[k - 1];
     bk = lc.bk[k - 1];
@@ -423,9 +451,13 @@ __device__ __forceinline__ void grad1_body(const Grid& g, const cd* __restrict__
   const int j = by + 1;
   if (i > g.nx) return;
   const long long p = pix(g, i, j);
+  const int sym = xsym(g);
   for (int k = 0; k < 5; ++k) {
-    const double re = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return v[k + 5 * pix(g, ii, j)].x; });
-    const double im = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return v[k + 5 * pix(g, ii, j)].y; });
+    const double sg = k == 2 ? -1.0 : 1.0;  // v changes sign across a symmetry plane
+    const double re =
+        d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return v[k + 5 * pix(g, ii, j)].x; }, sym, sg);
+    const double im =
+        d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return v[k + 5 * pix(g, ii, j)].y; }, sym, sg);
     c1v[k + 5 * p] = cd{re, im};
   }
 }
@@ -480,8 +512,10 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
         r[m].y += A * c1b.y + B * c2b.y + D * vb.y + Di * vb.x;
       }
       if (b == 0) continue;
-      const cd c11b{d2_at<NARROW>(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).x; }),
-                    d2_at<NARROW>(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).y; })};
+      const int sym = xsym(g);
+      const double sg = b == 2 ? -1.0 : 1.0;
+      const cd c11b{d2_at<NARROW>(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).x; }, sym, sg),
+                    d2_at<NARROW>(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return VX(ii).y; }, sym, sg)};
       const cd c22b{d2_at<NARROW>(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).x; }),
                     d2_at<NARROW>(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return VY(jj).y; })};
       const cd c12b{d1_at<NARROW>(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return CY(jj).x; }),
@@ -1370,10 +1404,17 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
   if (p->xper != 0 && p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: xper must be 0 or 1");
   if (!p->xper) {
-    if (p->left != 0 && p->left != 1 && p->left != 4)
-      return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1 or 4 (xper = 0)");
-    if (p->right != 0 && p->right != 4 && p->right != 8)
-      return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4 or 8 (xper = 0)");
+    if (p->left != 0 && p->left != 1 && p->left != 4 && p->left != 7)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1, 4 or 7 (xper = 0)");
+    if (p->right != 0 && p->right != 4 && p->right != 7 && p->right != 8)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4, 7 or 8 (xper = 0)");
+    // symmetry planes with the smoother would need its mirrored stencils (src/smoother3d.f90:89-250)
+    if ((p->left == 7 || p->right == 7) && p->eps_e != 0.0)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: symmetry planes (left or right 7) are supported with eps_e = 0");
+    // the symmetric xi LHS rows read ABhi through a (6,ny,nx) view of the (6,nx,ny) array
+    // (src/lhsbs1f3d.f90:17), which stays inside it only when ny <= nx
+    if ((p->left == 7 || p->right == 7) && p->ny > p->nx)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: symmetry planes (left or right 7) need ny <= nx");
     // the reference reads the eigenfunction only for left 4 (src/gendist.f90:18)
     if (p->right == 4 && p->left != 4) return fail3(LNS_ERR_ARG, "ctx3d_create: right 4 needs left 4");
   }

@@ -66,10 +66,15 @@ struct Grid {
   double dxi, deta;
   double Ma, Re, Pr, gamma, gamma1, omega, kz, alfa;
   int xper, yper, navier, wall, wallt, top;
-  int left = -1, right = -1;             // xi boundaries when xper = 0
+  int left = -1, right = -1;             // xi boundaries when xper = 0 (7: symmetry plane)
   double gx[6], gy[6], dx2[7], dy2[7];   // interior first / second derivative stencils (src/cgrad*.f90)
   double dxinv, dyinv, dxsinv, dysinv;
 };
+
+// symmetry planes of the xi lines (left / right 7), the d1_at / d2_at sym bits
+__host__ __device__ __forceinline__ int xsym(const Grid& g) {
+  return g.xper ? 0 : (g.left == 7 ? 1 : 0) | (g.right == 7 ? 2 : 0);
+}
 
 // true when every interior stencil of g has zero outermost coefficients
 inline bool narrow_stencils(const Grid& g) {
@@ -115,12 +120,23 @@ __device__ __forceinline__ long long pix(const Grid& g, int i, int j) {
 
 // First derivative along a line of n points at point i (1-based), from the
 // values u(k); periodic lines have period n-1 (point n repeats point 1).
+// sym: symmetry planes of a non-periodic line (bit 0 at point 1, bit 1 at
+// point n, the reference's lsym / rsym): the three points next to such a
+// plane take the interior stencil over the mirrored values u(2 - k),
+// u(2n - k), times sgn (-1 for the component that changes sign,
+// src/cgrad.f90:193-266, src/cgrad2.f90:232-307).
 // NARROW: the interior stencil's outermost coefficients (offsets +-3) are zero,
 // as for the fourth-order scheme (optx, opty = -1); their terms are skipped,
 // and the sum is an explicit left-to-right chain of fused multiply-adds so
 // that every kernel using it rounds the same way.
 template <bool NARROW = false, class U>
-__device__ __forceinline__ double d1_at(int i, int n, int periodic, const double* c, double dinv, U u) {
+__device__ __forceinline__ double d1_at(int i, int n, int periodic, const double* c, double dinv, U u, int sym = 0,
+                                        double sgn = 1.0) {
+  if (!periodic && (((sym & 1) && i <= 3) || ((sym & 2) && i >= n - 2))) {
+    auto w = [&](int k) { return k < 1 ? sgn * u(2 - k) : (k > n ? sgn * u(2 * n - k) : u(k)); };
+    if constexpr (NARROW) return fma(c[4], w(i + 2), fma(c[3], w(i + 1), fma(c[2], w(i - 1), c[1] * w(i - 2))));
+    return c[0] * w(i - 3) + c[1] * w(i - 2) + c[2] * w(i - 1) + c[3] * w(i + 1) + c[4] * w(i + 2) + c[5] * w(i + 3);
+  }
   if (periodic) {
     if (i == n) i = 1;
     auto w = [&](int k) { return k < 1 ? k + n - 1 : (k > n - 1 ? k - (n - 1) : k); };
@@ -139,7 +155,15 @@ __device__ __forceinline__ double d1_at(int i, int n, int periodic, const double
 }
 
 template <bool NARROW = false, class U>
-__device__ __forceinline__ double d2_at(int i, int n, int periodic, const double* c, double dsinv, U u) {
+__device__ __forceinline__ double d2_at(int i, int n, int periodic, const double* c, double dsinv, U u, int sym = 0,
+                                        double sgn = 1.0) {
+  if (!periodic && (((sym & 1) && i <= 3) || ((sym & 2) && i >= n - 2))) {
+    auto w = [&](int k) { return k < 1 ? sgn * u(2 - k) : (k > n ? sgn * u(2 * n - k) : u(k)); };
+    if constexpr (NARROW)
+      return fma(c[5], w(i + 2), fma(c[4], w(i + 1), fma(c[3], w(i), fma(c[2], w(i - 1), c[1] * w(i - 2)))));
+    return c[0] * w(i - 3) + c[1] * w(i - 2) + c[2] * w(i - 1) + c[3] * w(i) + c[4] * w(i + 1) + c[5] * w(i + 2) +
+           c[6] * w(i + 3);
+  }
   if (periodic) {
     if (i == n) i = 1;
     auto w = [&](int k) { return k < 1 ? k + n - 1 : (k > n - 1 ? k - (n - 1) : k); };

@@ -55,6 +55,11 @@ GOLDEN = {
                         dict(nsteps=10, cflmax=20.0, loctime=1, module=dict(lalpha=0.3 + 0.05j))),
     "step3d_open_hold": ("3dopen", dict(nx=48, ny=33, seed=6, left=0, right=8),
                          dict(nsteps=10, cflmax=20.0, loctime=1)),
+    # symmetry planes (left / right 7): mirrored stencils and xi LHS rows
+    "step3d_sym_left": ("3dopen", dict(nx=48, ny=33, seed=7, left=7, right=0),
+                        dict(nsteps=10, cflmax=20.0, loctime=1)),
+    "step3d_sym_both": ("3dopen", dict(nx=40, ny=33, seed=8, left=7, right=7),
+                        dict(nsteps=10, cflmax=20.0, loctime=1)),
     # the nonlinear 2D step with a non-periodic xi direction: Riemann planes
     # on both sides; the symmetry plane on the left with the right plane
     # extrapolated (zeroth order) over a viscous layer that itrBC moves
