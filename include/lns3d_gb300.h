@@ -372,8 +372,8 @@ typedef struct {
                                 src/lhs2f3d.f90:171-203, src/lhsbt2f3d.f90:277-298,
                                 431-452) with the weight buff(nx,ny): ones (the reference's
                                 ibuff = 0) until lns_upload_buffer3d.  0 turns both off.
-                                Symmetry planes (lsym, rsym) are not supported.  Batches and
-                                servers take 0. */
+                                Beside a symmetry plane (left or right 7) both take its
+                                mirrored stencils.  Batches and servers take 0. */
   int32_t left, right;       /* the xi boundaries when xper = 0 (src/itrbc3d.f90:203-414,
                                 src/rhsbc3d.f90:167-324, src/lhsbc1f3d.f90:412-448,
                                 src/lhsbc2f3d.f90:146-174): left 0 zero disturbance, 1 an
@@ -384,8 +384,9 @@ typedef struct {
                                 symmetry plane, 8 the held initial condition.  A symmetry plane
                                 (src/cgrad.f90:193-266, src/lhsbs1f3d.f90) mirrors the field,
                                 v changing sign, into the stencils of its three nearest points
-                                and the xi LHS rows of its two; eps_e must then be 0, and
-                                ny <= nx (those rows read ABhi through the reference's
+                                and the xi LHS rows of its two (the smoother and the implicit
+                                damping included); it needs ny <= nx (those rows read ABhi
+                                through the reference's
                                 (6,ny,nx) view of the (6,nx,ny) array, src/lhsbs1f3d.f90:17,
                                 which the GPU reproduces and which leaves the array when ny > nx).
                                 Ignored with xper = 1.  Batches and servers take xper = 1. */

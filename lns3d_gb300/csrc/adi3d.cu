@@ -358,22 +358,24 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
     // beyond the plane folded onto their mirror images, times -1 in the
     // columns of the component that changes sign (b = 3)
     const double sg = b == 3 ? -1.0 : 1.0;
-    double fa = 0.0, fb = 0.0;
+    double fa = 0.0, fb = 0.0, fd = 0.0;  // first-derivative, second-derivative and damping stencils
     for (int o5 = 0; o5 < 5; ++o5) {
       int m = pos + o5 - 2;
       bool mir = false;
       if (m < 1) m = 2 - m, mir = true;
       if (m > n) m = 2 * n - m, mir = true;
       if (m - pos + 3 != k) continue;
+      const double fbk = pick5(o5, 1.0, -4.0, 6.0, -4.0, 1.0);
       fa = fa + (mir ? sg * lc.ak[o5] : lc.ak[o5]);
       fb = fb + (mir ? sg * lc.bk[o5] : lc.bk[o5]);
+      fd = fd + (mir ? sg * fbk : fbk);
     }
     // the reference declares this routine's ABhi dummy (6,ny,nx) for the
     // (6,nx,ny) actual, so it reads entry (k, i, j) at point (i-1) + ny (j-1)
     // (src/lhsbs1f3d.f90:17); creation requires ny <= nx, which keeps that
     // point inside the array
     const long long pab = (long long)(i - 1) + (long long)g.ny * (j - 1);
-    store_el(mat, q, lhs_entry(g, o, dir, p, k, a, b, fa, fb, true, 3, 0.0, pab));
+    store_el(mat, q, lhs_entry(g, o, dir, p, k, a, b, fa, fb, true, 3, fd, pab));
     return;
   }
   if (per || (pos > 2 && pos < n - 1)) {
@@ -556,23 +558,41 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
         r[m] = cd{r[m].x + sp * vm.x, r[m].y + sp * vm.y};
       }
     }
-    // smoother3D (src/smoother3d.f90, lsym = rsym = false), the eta pass
-    // then the xi pass: rows/columns 2 and n-1 second order, 3 and n-2
-    // fourth order, the rest sixth order; no periodic wrap
+    // smoother3D (src/smoother3d.f90), the eta pass then the xi pass:
+    // rows/columns 2 and n-1 second order, 3 and n-2 fourth order, the rest
+    // sixth order; no periodic wrap.  Beside a symmetry plane the xi pass
+    // takes the sixth-order stencil at points 1..3 (n-2..n) over the
+    // mirrored values, v with its sign changed (src/smoother3d.f90:89-250).
     if (o.buff) {
       const double eb = o.eps_e * o.buff[p];
       const double fa[7] = {-1.666666666666667E-01, 2.0, -6.5, 9.333333333333333, -6.5, 2.0, -1.666666666666667E-01};
       #pragma unroll 1
       for (int pass = 0; pass < 2; ++pass) {
         const int c = pass == 0 ? j : i, n = pass == 0 ? g.ny : g.nx;
-        if (c < 2 || c > n - 1) continue;
+        const int sx_ = pass == 1 ? xsym(g) : 0;
+        const bool mirror = ((sx_ & 1) && c <= 3) || ((sx_ & 2) && c >= n - 2);
+        if (!mirror && (c < 2 || c > n - 1)) continue;
         const long long st = pass == 0 ? 5LL * g.nx : 5LL;
         #pragma unroll
         for (int m = 0; m < 5; ++m) {
           const cd* V = v + m + 5 * p;
           auto S = [&](int dd) -> const cd& { return V[dd * st]; };
           double sx, sy;
-          if (c == 2 || c == n - 1) {
+          if (mirror) {
+            const double sg = m == 2 ? -1.0 : 1.0;
+            auto M = [&](int dd) -> cd {
+              int kk = c + dd;
+              double f = 1.0;
+              if (kk < 1) kk = 2 - kk, f = sg;
+              else if (kk > n) kk = 2 * n - kk, f = sg;
+              const cd& x = V[(kk - c) * st];
+              return cd{f * x.x, f * x.y};
+            };
+            sx = fa[0] * M(-3).x + fa[1] * M(-2).x + fa[2] * M(-1).x + fa[3] * M(0).x + fa[4] * M(1).x +
+                 fa[5] * M(2).x + fa[6] * M(3).x;
+            sy = fa[0] * M(-3).y + fa[1] * M(-2).y + fa[2] * M(-1).y + fa[3] * M(0).y + fa[4] * M(1).y +
+                 fa[5] * M(2).y + fa[6] * M(3).y;
+          } else if (c == 2 || c == n - 1) {
             sx = -1.0 * S(-1).x + 2.0 * S(0).x - 1.0 * S(1).x;
             sy = -1.0 * S(-1).y + 2.0 * S(0).y - 1.0 * S(1).y;
           } else if (c == 3 || c == n - 2) {
@@ -1408,9 +1428,6 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
       return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1, 4 or 7 (xper = 0)");
     if (p->right != 0 && p->right != 4 && p->right != 7 && p->right != 8)
       return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4, 7 or 8 (xper = 0)");
-    // symmetry planes with the smoother would need its mirrored stencils (src/smoother3d.f90:89-250)
-    if ((p->left == 7 || p->right == 7) && p->eps_e != 0.0)
-      return fail3(LNS_ERR_ARG, "ctx3d_create: symmetry planes (left or right 7) are supported with eps_e = 0");
     // the symmetric xi LHS rows read ABhi through a (6,ny,nx) view of the (6,nx,ny) array
     // (src/lhsbs1f3d.f90:17), which stays inside it only when ny <= nx
     if ((p->left == 7 || p->right == 7) && p->ny > p->nx)

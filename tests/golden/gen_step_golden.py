@@ -60,6 +60,8 @@ GOLDEN = {
                         dict(nsteps=10, cflmax=20.0, loctime=1)),
     "step3d_sym_both": ("3dopen", dict(nx=40, ny=33, seed=8, left=7, right=7),
                         dict(nsteps=10, cflmax=20.0, loctime=1)),
+    "step3d_sym_smooth": ("3dopen", dict(nx=40, ny=33, seed=9, left=7, right=7),
+                          dict(nsteps=10, cflmax=20.0, loctime=1, eps_e=0.01)),
     # the nonlinear 2D step with a non-periodic xi direction: Riemann planes
     # on both sides; the symmetry plane on the left with the right plane
     # extrapolated (zeroth order) over a viscous layer that itrBC moves

@@ -120,7 +120,7 @@ def _params3d(**kw):
 
 @pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=2), dict(xper=0, left=5), dict(xper=0, right=1),
                                  dict(xper=0, right=5), dict(xper=0, right=9), dict(xper=0, left=0, right=4),
-                                 dict(xper=0, left=7, eps_e=0.01), dict(xper=0, right=7, nx=20, ny=24), dict(yper=2), dict(navier=0), dict(wall=0), dict(wallt=2),
+                                 dict(xper=0, right=7, nx=20, ny=24), dict(yper=2), dict(navier=0), dict(wall=0), dict(wallt=2),
                                  dict(top=2), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
                                  dict(loctime=2), dict(ispg=-1), dict(yper=1, ny=7), dict(yper=1, top=1),
                                  dict(navier=2, yper=1), dict(eps_e=-1.0), dict(eps_e=float("nan"))])

@@ -136,7 +136,7 @@ def test_reference_test2d_fixture(cuda):
 
 
 @pytest.mark.parametrize("name", ["step3d_open", "step3d_open_wave", "step3d_open_eig", "step3d_open_hold",
-                                  "step3d_sym_left", "step3d_sym_both"])
+                                  "step3d_sym_left", "step3d_sym_both", "step3d_sym_smooth"])
 def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     """A non-periodic xi direction: the boundary-closure rows of the xi LHS
     (src/lhsbt1f3d.f90), the zero-disturbance, incoming-wave and
@@ -154,7 +154,7 @@ def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     kind, cargs, rargs, d = golden(name)
     case = gen_step_golden.open_layer(**cargs)
     drv = ImpDrv3D(case["params"], case["metrics"], case["vm"], cflmax=rargs["cflmax"], loctime=rargs["loctime"],
-                   x=case["x"], x0=rargs.get("x0", 0.0), profile=case.get("profile"),
+                   x=case["x"], x0=rargs.get("x0", 0.0), profile=case.get("profile"), eps_e=rargs.get("eps_e", 0.0),
                    lalpha=rargs.get("module", {}).get("lalpha", 0j))
     v = case["v"].copy(order="F")
     drv.itrbc(v)
