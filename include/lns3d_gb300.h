@@ -228,8 +228,11 @@ typedef struct {
                                 src/lhsbt2f.f90:193-213) weighted by buff (ones until
                                 lns_upload_buffer2d); with lhs_order 2 the second-order damping
                                 of src/lhs.f90 and src/lhsbt2.f90. */
-  int32_t left, right;       /* xi planes when xper = 0: left 0 (Riemann) or 2 (symmetry plane),
-                                right 0 (Riemann); ignored when xper = 1 */
+  int32_t left, right;       /* xi planes when xper = 0: left 0 (Riemann), 2 (symmetry plane by
+                                extrapolation, src/itrbc.f90:776-798) or 7 (symmetry plane by
+                                mirrored stencils and LHS rows, src/grad.f90:155-250,
+                                src/lhsbs1f.f90, v = 0 on it); right 0 (Riemann) or 7;
+                                ignored when xper = 1 */
   int32_t extrap;            /* -1 off, 0 or 1: the right plane extrapolated from its neighbours
                                 over rows 1..nbl (the viscous layer) */
   int32_t nbl;               /* rows of the viscous layer before the first itrBC (the &extras

@@ -174,12 +174,14 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, F
     double g1v[5], g2v[5], g11v[5], g12v[5], g22v[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      g1v[k] = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, j); });
+      const int sym = xsym(g);
+      const double sg = k == 2 ? -1.0 : 1.0;  // v changes sign across a symmetry plane
+      g1v[k] = d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, j); }, sym, sg);
       g2v[k] = d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) { return V(k, i, jj); });
-      g11v[k] = d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return V(k, ii, j); });
+      g11v[k] = d2_at(i, g.nx, g.xper, g.dx2, g.dxsinv, [&](int ii) { return V(k, ii, j); }, sym, sg);
       g22v[k] = d2_at(j, g.ny, g.yper, g.dy2, g.dysinv, [&](int jj) { return V(k, i, jj); });
       g12v[k] = d1_at(j, g.ny, g.yper, g.gy, g.dyinv, [&](int jj) {
-        return d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, jj); });
+        return d1_at(i, g.nx, g.xper, g.gx, g.dxinv, [&](int ii) { return V(k, ii, jj); }, sym, sg);
       });
     }
     if (g.navier && (g.wallt == 1 || g.wallt == 2) && j == 1) g2v[4] = 0.0;  // src/gradbc.f90:15
@@ -379,11 +381,23 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, F
                               -1.666666666666667E-01};
         for (int pass = 0; pass < 2; ++pass) {
           const int c = pass == 0 ? j : i, n = pass == 0 ? g.ny : g.nx;
-          if (c < 2 || c > n - 1) continue;
+          // beside a symmetry plane the xi pass takes the sixth-order stencil
+          // at points 1..3 (n-2..n) over the mirrored values (src/smoother.f90:89-250)
+          const int sx_ = pass == 1 ? xsym(g) : 0;
+          const bool mirror = ((sx_ & 1) && c <= 3) || ((sx_ & 2) && c >= n - 2);
+          if (!mirror && (c < 2 || c > n - 1)) continue;
           for (int m = 0; m < 5; ++m) {
             auto S = [&](int dd) { return pass == 0 ? V(m, i, j + dd) : V(m, i + dd, j); };
             double sm;
-            if (c == 2 || c == n - 1) sm = -1.0 * S(-1) + 2.0 * S(0) - 1.0 * S(1);
+            if (mirror) {
+              const double sgm = m == 2 ? -1.0 : 1.0;
+              auto M = [&](int dd) {
+                const int kk = c + dd;
+                return kk < 1 ? sgm * V(m, 2 - kk, j) : kk > n ? sgm * V(m, 2 * n - kk, j) : V(m, kk, j);
+              };
+              sm = fa[0] * M(-3) + fa[1] * M(-2) + fa[2] * M(-1) + fa[3] * M(0) + fa[4] * M(1) + fa[5] * M(2) +
+                   fa[6] * M(3);
+            } else if (c == 2 || c == n - 1) sm = -1.0 * S(-1) + 2.0 * S(0) - 1.0 * S(1);
             else if (c == 3 || c == n - 2) sm = S(-2) - 4.0 * S(-1) + 6.0 * S(0) - 4.0 * S(1) + 1.0 * S(2);
             else
               sm = fa[0] * S(-3) + fa[1] * S(-2) + fa[2] * S(-1) + fa[3] * S(0) + fa[4] * S(1) + fa[5] * S(2) +
@@ -443,6 +457,7 @@ __global__ void __launch_bounds__(128) rhs2d_kernel(Grid g, Ops o, Metrics mt, F
           rm_values(g, sd, j, s, b);
           for (int m = 0; m < 5; ++m) rr[m] = VF(m, i, j) - b[m];
         }
+        if (g.Ma < 1.0 && (left ? g.left : g.right) == 7) rr[2] = 0.0;  // symmetry plane: v = 0
         if (g.Ma < 1.0 && left && g.left == 2)
           for (int m = 0; m < 5; ++m)
             rr[m] = m == 2 ? 0.0
@@ -505,7 +520,22 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Far fr, const double* __restrict__ v
   const double d = o.dtl[p], alfa = g.alfa;
   // the rows of the xi boundary planes (non-periodic xi), which lhsbc1f
   // and lhsbc2f set last and in full
-  if (!g.xper && (i == 1 || i == g.nx)) {
+  const bool symplane = !g.xper && ((i == 1 && g.left == 7) || (i == g.nx && g.right == 7));
+  if (symplane) {
+    // symmetry plane rows: the symmetric band row below, after the v row of
+    // the left plane (src/lhsbc1f.f90:652-655, src/lhsbc2f.f90:525-528) and
+    // the right plane's extrapolation rows, which lhsbc1f sets last
+    const bool left = i == 1;
+    if (left && a == 3 && (dir == 1 || g.Ma < 1.0)) {
+      mat[q] = ident;
+      return;
+    }
+    if (!left && dir == 1 && fr.extrap >= 0 && j <= *fr.nbl) {
+      const double c = a == b ? 1.0 : 0.0;
+      mat[q] = k == 3 ? -c : k == 2 ? (fr.extrap == 0 ? c : two * c) : (k == 1 && fr.extrap == 1 ? -c : 0.0);
+      return;
+    }
+  } else if (!g.xper && (i == 1 || i == g.nx)) {
     const bool left = i == 1;
     if (dir == 2) {
       // identity eta rows: below Ma 1 on the Riemann (left 0, right 0),
@@ -624,7 +654,24 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Far fr, const double* __restrict__ v
     auto d2 = [](int t) { return pick5(t, db1, db2, db3, db4, db5); };
     double gcf, dcf;
     bool neg = false;
-    if (c == 1) { const int t = (k + 2) % 5; gcf = g1(t); dcf = d1(t); }
+    const int sym = dir == 1 ? xsym(g) : 0;
+    if (((sym & 1) && c <= 2) || ((sym & 2) && c >= n - 1)) {
+      // symmetry plane (src/lhsbs1f.f90): the band stencil with the nodes
+      // beyond the plane folded onto their mirror images, times -1 in the
+      // columns of v (b = 3)
+      const double sg = b == 3 ? -1.0 : 1.0;
+      gcf = 0.0, dcf = 0.0;
+      for (int o5 = 0; o5 < 5; ++o5) {
+        int m = c + o5 - 2;
+        bool mir = false;
+        if (m < 1) m = 2 - m, mir = true;
+        if (m > n) m = 2 * n - m, mir = true;
+        if (m - c + 3 != k) continue;
+        const double gk = pick5(o5, ga1, ga2, 0.0, ga3, ga4), dk = pick5(o5, da1, da2, da3, da4, da5);
+        gcf = gcf + (mir ? sg * gk : gk);
+        dcf = dcf + (mir ? sg * dk : dk);
+      }
+    } else if (c == 1) { const int t = (k + 2) % 5; gcf = g1(t); dcf = d1(t); }
     else if (c == 2) { const int t = (k + 3) % 5; gcf = g2(t); dcf = d2(t); }
     else if (c == n - 1) { const int t = k == 5 ? 4 : 4 - k; gcf = g2(t); dcf = d2(t); neg = true; }
     else { const int t = k <= 3 ? 3 - k : 8 - k; gcf = g1(t); dcf = d1(t); neg = true; }
@@ -668,8 +715,27 @@ __global__ void lhs2d_kernel(Grid g, Ops o, Far fr, const double* __restrict__ v
       if (dir == 2 && o.spg && k == 3) val = val + alfa * d * o.spg[p];
     } else {
       const int c = dir == 1 ? i : j, n = dir == 1 ? g.nx : g.ny;
+      const int sym = dir == 1 ? xsym(g) : 0;
       if (dir == 2 && o.spg && k == 3) val = val + alfa * d * o.spg[(long long)(j - 1) + (long long)(i - 1) * g.ny];
-      if (o.buff && (c == 2 || c == n - 1) && k >= 2 && k <= 4) val = val + wd * (k == 3 ? 2.0 : -1.0);
+      if (((sym & 1) && c <= 2) || ((sym & 2) && c >= n - 1)) {
+        // the damping stencil folded like the band (src/lhsbs1f.f90)
+        if (o.buff) {
+          const double sg = a == 3 ? -1.0 : 1.0;
+          double fd = 0.0;
+          for (int o5 = 0; o5 < 5; ++o5) {
+            int m = c + o5 - 2;
+            bool mir = false;
+            if (m < 1) m = 2 - m, mir = true;
+            if (m > n) m = 2 * n - m, mir = true;
+            if (m - c + 3 != k) continue;
+            const double fk = pick5(o5, 1.0, -4.0, 6.0, -4.0, 1.0);
+            fd = fd + (mir ? sg * fk : fk);
+          }
+          if (fd != 0.0) val = val + wd * fd;
+        }
+      } else if (o.buff && (c == 2 || c == n - 1) && k >= 2 && k <= 4) {
+        val = val + wd * (k == 3 ? 2.0 : -1.0);
+      }
     }
   }
   mat[q] = val;
@@ -743,7 +809,10 @@ __global__ void __launch_bounds__(256) bcx2d_kernel(Grid g, Far fr, double* __re
     } else if (g.left == 2) {
       for (int m = 0; m < 5; ++m)
         W(m, 1, j) = m == 2 ? 0.0 : -(gc2 * W(m, 2, j) + gc3 * W(m, 3, j) + gc4 * W(m, 4, j) + gc5 * W(m, 5, j)) / gc1;
+    } else if (g.left == 7) {
+      W(2, 1, j) = 0.0;
     }
+    if (g.right == 7) W(2, g.nx, j) = 0.0;
     if (g.right == 0) {
       const RmState s = rm_state(g, fr.right, j, &W(0, g.nx, j), &W(0, g.nx - 1, j), &W(0, g.nx - 2, j));
       double b[5];
@@ -1040,9 +1109,12 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
   if (p->xper == 0) {
     // the non-periodic xi direction: the planes of src/rhsbc.f90:364-482,
     // src/lhsbc1f.f90:606-898, src/lhsbc2f.f90:489-556, src/itrbc.f90:760-886
-    if (p->left != 0 && p->left != 2)
-      return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, left must be 0 (Riemann) or 2 (symmetry plane)");
-    if (p->right != 0) return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, right must be 0 (Riemann)");
+    if (p->left != 0 && p->left != 2 && p->left != 7)
+      return fail2(LNS_ERR_ARG,
+                   "ctx2d_create: with xper = 0, left must be 0 (Riemann), 2 (extrapolated symmetry plane) or 7 "
+                   "(mirrored symmetry plane)");
+    if (p->right != 0 && p->right != 7)
+      return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, right must be 0 (Riemann) or 7 (symmetry plane)");
     if (!(p->Ma < 1.0)) return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, need Ma < 1");
     if (p->extrap < -1 || p->extrap > 1)
       return fail2(LNS_ERR_ARG, "ctx2d_create: extrap must be -1, 0 or 1 (the reference's xi LHS rejects 2)");

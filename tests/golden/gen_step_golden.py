@@ -70,6 +70,9 @@ GOLDEN = {
                            dict(nsteps=10, cflmax=1.0, loctime=0)),
     "step2d_vortex_open_sym": ("2dopen", dict(nx=48, ny=40, seed=2, left=2, right=0, extrap=0),
                                dict(nsteps=10, cflmax=1.0, loctime=0, module=dict(nbl=6, update_nbl=1))),
+    # mirrored symmetry planes (left / right 7), with the smoother
+    "step2d_vortex_mirror": ("2dopen", dict(nx=48, ny=40, seed=3, left=7, right=7),
+                             dict(nsteps=10, cflmax=1.0, loctime=0, eps_e=0.01)),
 }
 
 

@@ -163,11 +163,12 @@ def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
 
 
-@pytest.mark.parametrize("name", ["step2d_vortex_open", "step2d_vortex_open_sym"])
+@pytest.mark.parametrize("name", ["step2d_vortex_open", "step2d_vortex_open_sym", "step2d_vortex_mirror"])
 def test_step2d_nonperiodic_xi_matches_reference_golden(cuda, name):
     """The nonlinear 2D step with a non-periodic xi direction: Riemann planes
     on both sides (left.pot / right.pot), and the symmetry plane with the
-    right plane extrapolated over a viscous layer that itrBC moves."""
+    right plane extrapolated over a viscous layer that itrBC moves, and
+    mirrored symmetry planes on both sides with the smoother."""
     from lns3d_gb300 import ImpDrv2D
     from lns3d_gb300.cases import vortex2d_open
 
@@ -177,7 +178,8 @@ def test_step2d_nonperiodic_xi_matches_reference_golden(cuda, name):
     module = rargs.pop("module", {})
     drv = ImpDrv2D(case["params"], case["metrics"], case["bnt"], case["pot"], cflmax=rargs.get("cflmax", 1.0),
                    loctime=rargs.get("loctime", 0), left_far=case["left_far"], right_far=case["right_far"],
-                   extrap=case["extrap"], nbl=module.get("nbl", 0), update_nbl=module.get("update_nbl", 0))
+                   extrap=case["extrap"], nbl=module.get("nbl", 0), update_nbl=module.get("update_nbl", 0),
+                   eps_e=rargs.get("eps_e", 0.0))
     v = case["v"].copy(order="F")
     drv.itrbc(v)
     res = drv.step(v, nsteps=nsteps)
