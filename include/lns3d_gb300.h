@@ -231,7 +231,8 @@ typedef struct {
   int32_t left, right;       /* xi planes when xper = 0: left 0 (Riemann), 2 (symmetry plane by
                                 extrapolation, src/itrbc.f90:776-798) or 7 (symmetry plane by
                                 mirrored stencils and LHS rows, src/grad.f90:155-250,
-                                src/lhsbs1f.f90, v = 0 on it); right 0 (Riemann) or 7;
+                                src/lhsbs1f.f90, v = 0 on it); right 0 (Riemann), 7 or 8 (the
+                                initial condition held, src/rhsbc.f90:478-480);
                                 ignored when xper = 1 */
   int32_t extrap;            /* -1 off, 0 or 1: the right plane extrapolated from its neighbours
                                 over rows 1..nbl (the viscous layer) */

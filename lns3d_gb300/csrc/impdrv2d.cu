@@ -1113,8 +1113,9 @@ int lns_ctx2d_create(const lns_params2d* p, lns_ctx2d** out) {
       return fail2(LNS_ERR_ARG,
                    "ctx2d_create: with xper = 0, left must be 0 (Riemann), 2 (extrapolated symmetry plane) or 7 "
                    "(mirrored symmetry plane)");
-    if (p->right != 0 && p->right != 7)
-      return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, right must be 0 (Riemann) or 7 (symmetry plane)");
+    if (p->right != 0 && p->right != 7 && p->right != 8)
+      return fail2(LNS_ERR_ARG,
+                   "ctx2d_create: with xper = 0, right must be 0 (Riemann), 7 (symmetry plane) or 8 (held)");
     if (!(p->Ma < 1.0)) return fail2(LNS_ERR_ARG, "ctx2d_create: with xper = 0, need Ma < 1");
     if (p->extrap < -1 || p->extrap > 1)
       return fail2(LNS_ERR_ARG, "ctx2d_create: extrap must be -1, 0 or 1 (the reference's xi LHS rejects 2)");

@@ -73,6 +73,9 @@ int lns_lin2d_create(const lns_params3d* p, lns_lin2d** out) {
   if (p->beta != 0.0 || p->omega != 0.0)
     return lns_fail(LNS_ERR_ARG, "lin2d_create: a 2D linear run has beta = 0 and omega = 0 (Lz = 0 in the deck)");
   if (p->precision != LNS_FP64) return lns_fail(LNS_ERR_ARG, "lin2d_create: precision must be LNS_FP64");
+  // the linear 2D planes of a non-periodic xi direction (src/rhsbc.f90:182-253,
+  // src/itrbc.f90:300-620) differ from the 3D step's and are not built
+  if (p->xper != 1) return lns_fail(LNS_ERR_ARG, "lin2d_create: the linear 2D step needs xper = 1");
   lns_lin2d* c = new lns_lin2d();
   int rc = lns_ctx3d_create(p, &c->ctx);
   c->nx = p->nx;

@@ -73,6 +73,9 @@ GOLDEN = {
     # mirrored symmetry planes (left / right 7), with the smoother
     "step2d_vortex_mirror": ("2dopen", dict(nx=48, ny=40, seed=3, left=7, right=7),
                              dict(nsteps=10, cflmax=1.0, loctime=0, eps_e=0.01)),
+    # the held outflow plane (right 8)
+    "step2d_vortex_hold": ("2dopen", dict(nx=48, ny=40, seed=4, left=0, right=8),
+                           dict(nsteps=10, cflmax=1.0, loctime=0)),
 }
 
 

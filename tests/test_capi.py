@@ -161,7 +161,7 @@ def _params2d(**kw):
     return Params2D(**base)
 
 
-@pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=1), dict(xper=0, left=4), dict(xper=0, right=2),
+@pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=1), dict(xper=0, left=4), dict(xper=0, right=2), dict(xper=0, right=9),
                                  dict(xper=0, Ma=1.2), dict(xper=0, extrap=2), dict(xper=0, extrap=-2),
                                  dict(xper=0, nbl=25), dict(xper=0, nbl=-1), dict(xper=0, update_nbl=2),
                                  dict(xper=0, lhs_order=2), dict(xper=0, nx=9), dict(yper=1), dict(navier=0), dict(wall=2), dict(wallt=2),
@@ -218,9 +218,9 @@ def test_server3d_argument_errors(lib):
     assert lib.lns_server3d_bytes_in_use(None) == 0
 
 
-@pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1)])
+@pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1), dict(xper=0, left=0, right=0)])
 def test_lin2d_rejects_single_mode_options(lib, bad):
-    """The linear 2D context takes beta = omega = 0 and FP64."""
+    """The linear 2D context takes beta = omega = 0, FP64 and a periodic xi direction."""
     ctx = ctypes.c_void_p()
     base = dict(beta=0.0, omega=0.0)
     base.update(bad)

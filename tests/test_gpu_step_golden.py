@@ -163,7 +163,8 @@ def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
 
 
-@pytest.mark.parametrize("name", ["step2d_vortex_open", "step2d_vortex_open_sym", "step2d_vortex_mirror"])
+@pytest.mark.parametrize("name", ["step2d_vortex_open", "step2d_vortex_open_sym", "step2d_vortex_mirror",
+                                  "step2d_vortex_hold"])
 def test_step2d_nonperiodic_xi_matches_reference_golden(cuda, name):
     """The nonlinear 2D step with a non-periodic xi direction: Riemann planes
     on both sides (left.pot / right.pot), and the symmetry plane with the
