@@ -383,9 +383,14 @@ typedef struct {
                                 src/lhsbc2f3d.f90:146-174): left 0 zero disturbance, 1 an
                                 incoming acoustic wave exp(-a (x - x0)) exp(i kk x) formed from
                                 the mean flow (lns_upload_inflow3d), 4 the eigenfunction inflow
-                                (lns_upload_profile3d), 7 a symmetry plane; right 0 zero
-                                disturbance, 4 the eigenfunction outflow (with left 4), 7 a
-                                symmetry plane, 8 the held initial condition.  A symmetry plane
+                                (lns_upload_profile3d), 5 the undamped acoustic wave exp(i kk x)
+                                (lns_upload_inflow3d), 7 a symmetry plane; right 0 zero
+                                disturbance, 4 the eigenfunction outflow (with left 4), 5 the
+                                acoustic wave, 7 a symmetry plane, 8 the held initial
+                                condition.  The acoustic planes take x as the reference does,
+                                x(j,1) and x(j,nx) of the (nx,ny) grid, the point (j-1) and
+                                (j-1) + nx (nx-1) (src/itrbc3d.f90:331, 395); right 5 needs
+                                ny >= nx, which keeps that point inside the grid.  A symmetry plane
                                 (src/cgrad.f90:193-266, src/lhsbs1f3d.f90) mirrors the field,
                                 v changing sign, into the stencils of its three nearest points
                                 and the xi LHS rows of its two (the smoother and the implicit
@@ -411,7 +416,7 @@ int lns_upload_metrics3d(lns_ctx3d* ctx, const double* metrics);
  * host's sponge setup (src/sponge.f90) leaves them; needed before the first
  * step when ispg != 0; invalidates the factored LHS. */
 int lns_upload_sponge3d(lns_ctx3d* ctx, const double* spg, const double* spg2);
-/* ispg 2, 3 or top 1: the x coordinates x(nx,ny), the station x0 and the
+/* ispg 2, 3, top 1, left 1 or 5, right 5: the x coordinates x(nx,ny), the station x0 and the
  * amplitudes wamp(nx) (NULL: ones, the reference's default; ispg 3 needs
  * them) of the inflow sponge's wave (src/lrhs3d.f90:242-268) and of the
  * forced top boundary's incoming acoustic wave (top 1: v = t and r = -(v - t)

@@ -85,7 +85,8 @@ class ImpDrv3D:
             check(lib().lns_upload_sponge3d(self._ctx, ctypes.c_void_p(s1.ctypes.data),
                                             ctypes.c_void_p(s2.ctypes.data) if s2 is not None else None),
                   "lns_upload_sponge3d")
-        if ispg in (2, 3) or int(p["top"]) == 1 or (not int(p["xper"]) and int(p.get("left", -1)) == 1):
+        waves = not int(p["xper"]) and (int(p.get("left", -1)) in (1, 5) or int(p.get("right", -1)) == 5)
+        if ispg in (2, 3) or int(p["top"]) == 1 or waves:
             xx = np.asfortranarray(x, dtype=np.float64)
             wa = np.ascontiguousarray(wamp, dtype=np.float64) if wamp is not None else None
             check(lib().lns_upload_inflow3d(self._ctx, ctypes.c_void_p(xx.ctypes.data),

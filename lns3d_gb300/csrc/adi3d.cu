@@ -330,7 +330,8 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
   // the xi boundaries of a non-periodic xi direction (src/lhsbc1f3d.f90:412-448,
   // src/lhsbc2f3d.f90:146-174); they follow the wall and top rows, so the
   // corners take them
-  if (!g.xper && ((i == 1 && (g.left == 0 || g.left == 4)) || (i == g.nx && (g.right == 0 || g.right == 4))))
+  if (!g.xper && ((i == 1 && (g.left == 0 || g.left == 4 || g.left == 5)) ||
+                   (i == g.nx && (g.right == 0 || g.right == 4 || g.right == 5))))
     return store_el(mat, q, ident);
   // the held right plane (right 8): -I in the xi LHS only (src/lhsbc1f3d.f90:439-446)
   if (!g.xper && dir == 1 && i == g.nx && g.right == 8) return store_el(mat, q, cd{-ident.x, -ident.y});
@@ -443,6 +444,33 @@ __global__ void inflow_target_kernel(Grid g, int with_wamp, int row0, int col0, 
   vt[5 * o + 2] = cd{0.0, 0.0};
   vt[5 * o + 3] = cd{0.0, 0.0};
   vt[5 * o + 4] = cd{(gm2 * c3r * 0.5 - m[4] * 0.5 * c3r / cm2) / m[0], (gm2 * c3i * 0.5 - m[4] * 0.5 * c3i / cm2) / m[0]};
+}
+
+// The acoustic wave of a xi plane (left 5 at column 1, right 5 at column
+// nx; src/itrbc3d.f90:322-340, 382-405, src/rhsbc3d.f90:248-268, 286-308):
+// from the mean flow at (col, j), c3 = exp(i kk x) with kk = omega/(cm + u),
+// cm = sqrt(T)/Ma, and t = (c3/(2 cm^2), c3/(2 rho cm), 0, 0,
+// (gamma Ma^2 c3/2 - T c3/(2 cm^2))/rho).  The reference takes x as x(j,col)
+// of the (nx,ny) array, point (j-1) + nx (col-1), not (col, j): kept, as a
+// drop-in must (creation requires ny >= nx for right 5, which keeps that
+// point inside the array).
+__global__ void plane5_target_kernel(Grid g, int col, const double* __restrict__ vm, const double* __restrict__ xc,
+                                     cd* __restrict__ vt) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > g.ny) return;
+  const double* m = vm + 5 * pix(g, col, j);
+  const double cm = sqrt(m[4]) / g.Ma, um = m[1];
+  const double kk = g.omega / (cm + um);
+  const double xl = xc[(long long)(j - 1) + (long long)g.nx * (col - 1)];
+  double sn, cs;
+  sincos(kk * xl, &sn, &cs);
+  const double cm2 = cm * cm, gm2 = g.gamma * (g.Ma * g.Ma);
+  cd* o = vt + 5 * (j - 1);
+  o[0] = cd{0.5 * cs / cm2, 0.5 * sn / cm2};
+  o[1] = cd{cs * 0.5 / (m[0] * cm), sn * 0.5 / (m[0] * cm)};
+  o[2] = cd{0.0, 0.0};
+  o[3] = cd{0.0, 0.0};
+  o[4] = cd{(gm2 * cs * 0.5 - m[4] * 0.5 * cs / cm2) / m[0], (gm2 * sn * 0.5 - m[4] * 0.5 * sn / cm2) / m[0]};
 }
 
 // -------------------------------------------------------------------- RHS
@@ -670,9 +698,18 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
     if (!g.xper && ((i == 1 && g.left == 0) || (i == g.nx && (g.right == 0 || g.right == 4 || g.right == 8))))
       #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
-    // the incoming wave (left 1, src/rhsbc3d.f90:178-206) and the eigenfunction
-    // inflow (left 4, :207-243): r = -(v - t)
-    if (!g.xper && i == 1 && (g.left == 1 || g.left == 4)) {
+    // the incoming wave (left 1, src/rhsbc3d.f90:178-206), the eigenfunction
+    // inflow (left 4, :207-243), the acoustic planes (left 5, :248-268; right
+    // 5, :286-308): r = -(v - t)
+    if (!g.xper && i == g.nx && g.right == 5) {
+      const cd* T = reinterpret_cast<const cd*>(o.tright) + 5 * (j - 1);
+      #pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const cd w = vs[m + 5 * p];
+        r[m] = cd{-(w.x - T[m].x), -(w.y - T[m].y)};
+      }
+    }
+    if (!g.xper && i == 1 && (g.left == 1 || g.left == 4 || g.left == 5)) {
       const cd* T = reinterpret_cast<const cd*>(o.tleft) + 5 * (j - 1);
       #pragma unroll
       for (int m = 0; m < 5; ++m) {
@@ -761,10 +798,10 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
     // the incoming wave (left 1) and the eigenfunction inflow (left 4,
     // src/itrbc3d.f90:247-320) hold column 1 at t; the eigenfunction outflow
     // (right 4, :357-381) holds column nx at its profile times exp(i lalpha x)
-    if (!g.xper && i == 1 && (g.left == 1 || g.left == 4))
+    if (!g.xper && i == 1 && (g.left == 1 || g.left == 4 || g.left == 5))
       for (int jj = 1; jj <= g.ny; ++jj)
         for (int m = 0; m < 5; ++m) W(m, jj) = reinterpret_cast<const cd*>(tleft)[m + 5 * (jj - 1)];
-    if (!g.xper && i == g.nx && g.right == 4)
+    if (!g.xper && i == g.nx && (g.right == 4 || g.right == 5))
       for (int jj = 1; jj <= g.ny; ++jj)
         for (int m = 0; m < 5; ++m) W(m, jj) = reinterpret_cast<const cd*>(tright)[m + 5 * (jj - 1)];
   } else if (g.xper) {
@@ -1424,10 +1461,12 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
   if (p->xper != 0 && p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: xper must be 0 or 1");
   if (!p->xper) {
-    if (p->left != 0 && p->left != 1 && p->left != 4 && p->left != 7)
-      return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1, 4 or 7 (xper = 0)");
-    if (p->right != 0 && p->right != 4 && p->right != 7 && p->right != 8)
-      return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4, 7 or 8 (xper = 0)");
+    if (p->left != 0 && p->left != 1 && p->left != 4 && p->left != 5 && p->left != 7)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1, 4, 5 or 7 (xper = 0)");
+    if (p->right != 0 && p->right != 4 && p->right != 5 && p->right != 7 && p->right != 8)
+      return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4, 5, 7 or 8 (xper = 0)");
+    // right 5's wave reads x(j,nx) of the (nx,ny) array (src/rhsbc3d.f90:299), inside it only when ny >= nx
+    if (p->right == 5 && p->ny < p->nx) return fail3(LNS_ERR_ARG, "ctx3d_create: right 5 needs ny >= nx");
     // the symmetric xi LHS rows read ABhi through a (6,ny,nx) view of the (6,nx,ny) array
     // (src/lhsbs1f3d.f90:17), which stays inside it only when ny <= nx
     if ((p->left == 7 || p->right == 7) && p->ny > p->nx)
@@ -1501,13 +1540,17 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   }
   if (p->ispg == 2 || p->ispg == 3) { A(sizeof(double) * np, &q); c->spg_a = (double*)q; }
   const bool left_wave = !p->xper && p->left == 1;
-  if (p->ispg == 2 || p->ispg == 3 || p->top == 1 || left_wave) {
+  const bool plane5 = !p->xper && (p->left == 5 || p->right == 5);
+  if (p->ispg == 2 || p->ispg == 3 || p->top == 1 || left_wave || plane5) {
     A(sizeof(double) * np, &q); c->xc = (double*)q;
     A(sizeof(double) * p->nx, &q); c->wamp = (double*)q;
   }
   if (p->top == 1) { A(sizeof(double) * 10 * p->nx, &q); c->ttop = (double*)q; }
-  if (left_wave || (!p->xper && p->left == 4)) { A(sizeof(double) * 10 * p->ny, &q); c->tleft = (double*)q; }
-  if (!p->xper && p->right == 4) { A(sizeof(double) * 10 * p->ny, &q); c->tright = (double*)q; }
+  if (left_wave || (!p->xper && (p->left == 4 || p->left == 5))) {
+    A(sizeof(double) * 10 * p->ny, &q);
+    c->tleft = (double*)q;
+  }
+  if (!p->xper && (p->right == 4 || p->right == 5)) { A(sizeof(double) * 10 * p->ny, &q); c->tright = (double*)q; }
   if (p->wall == 3) { A(sizeof(double) * 10 * p->nx, &q); c->bump = (double*)q; }
   if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
@@ -1596,7 +1639,8 @@ int need_data(const lns_ctx3d* c, const char* who) {
     return fail3(LNS_ERR_ARG, std::string(who) + ": ispg != 0: upload the sponge first");
   if (!c->prm.xper && c->prm.left == 4 && !c->have_profile)
     return fail3(LNS_ERR_ARG, std::string(who) + ": left 4: upload the eigenfunction (lns_upload_profile3d) first");
-  if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1 || (c->tleft && c->prm.left == 1)) && !c->have_inflow)
+  const bool wave_planes = !c->prm.xper && (c->prm.left == 1 || c->prm.left == 5 || c->prm.right == 5);
+  if ((c->prm.ispg == 2 || c->prm.ispg == 3 || c->prm.top == 1 || wave_planes) && !c->have_inflow)
     return fail3(LNS_ERR_ARG,
                  std::string(who) + ": ispg 2, 3, top 1 or left 1: upload the wave data (lns_upload_inflow3d) first");
   if (c->prm.wall == 3 && !c->have_bump)
@@ -1617,6 +1661,16 @@ int make_inflow_target(lns_ctx3d* c) {
     lns::a3::inflow_target_kernel<<<(unsigned)((c->g.nx + 127) / 128), 128>>>(
         c->g, 1, c->g.ny, 0, c->vm, c->xc, c->wamp, c->x0, reinterpret_cast<cd*>(c->ttop));
     c->ops.ttop = c->ttop;
+  }
+  if (!c->prm.xper && c->prm.left == 5) {
+    lns::a3::plane5_target_kernel<<<(unsigned)((c->g.ny + 127) / 128), 128>>>(c->g, 1, c->vm, c->xc,
+                                                                             reinterpret_cast<cd*>(c->tleft));
+    c->ops.tleft = c->tleft;
+  }
+  if (!c->prm.xper && c->prm.right == 5) {
+    lns::a3::plane5_target_kernel<<<(unsigned)((c->g.ny + 127) / 128), 128>>>(c->g, c->g.nx, c->vm, c->xc,
+                                                                             reinterpret_cast<cd*>(c->tright));
+    c->ops.tright = c->tright;
   }
   if (c->tleft && c->prm.left == 1) {
     lns::a3::inflow_target_kernel<<<(unsigned)((c->g.ny + 127) / 128), 128>>>(
@@ -1659,8 +1713,9 @@ int lns_upload_sponge3d(lns_ctx3d* c, const double* spg, const double* spg2) {
 
 int lns_upload_inflow3d(lns_ctx3d* c, const double* x, const double* wamp, double x0) {
   if (!c || !x) return fail3(LNS_ERR_ARG, "upload_inflow3d: null argument");
-  if (c->prm.ispg != 2 && c->prm.ispg != 3 && c->prm.top != 1 && !(c->tleft && c->prm.left == 1))
-    return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3, top 1 or left 1");
+  if (c->prm.ispg != 2 && c->prm.ispg != 3 && c->prm.top != 1 &&
+      !(!c->prm.xper && (c->prm.left == 1 || c->prm.left == 5 || c->prm.right == 5)))
+    return fail3(LNS_ERR_ARG, "upload_inflow3d: needs ispg 2 or 3, top 1, left 1 or 5, or right 5");
   if (c->prm.ispg == 3 && !wamp) return fail3(LNS_ERR_ARG, "upload_inflow3d: ispg 3 needs wamp");
   if (!std::isfinite(x0)) return fail3(LNS_ERR_ARG, "upload_inflow3d: x0 must be finite");
   int rc = check_device(c);

@@ -55,6 +55,13 @@ GOLDEN = {
                         dict(nsteps=10, cflmax=20.0, loctime=1, module=dict(lalpha=0.3 + 0.05j))),
     "step3d_open_hold": ("3dopen", dict(nx=48, ny=33, seed=6, left=0, right=8),
                          dict(nsteps=10, cflmax=20.0, loctime=1)),
+    # the acoustic planes (left 5 inflow; right 5 outflow, which reads x at
+    # the (nx, ny) array's point (j, nx) and so needs ny >= nx), at the
+    # incoming wave's CFL 0.2
+    "step3d_open_acoustic": ("3dopen", dict(nx=48, ny=33, seed=10, left=5, right=0),
+                             dict(nsteps=5, cflmax=0.2, loctime=1)),
+    "step3d_open_acoustic_both": ("3dopen", dict(nx=32, ny=40, seed=11, left=5, right=5),
+                                  dict(nsteps=5, cflmax=0.2, loctime=1)),
     # symmetry planes (left / right 7): mirrored stencils and xi LHS rows
     "step3d_sym_left": ("3dopen", dict(nx=48, ny=33, seed=7, left=7, right=0),
                         dict(nsteps=10, cflmax=20.0, loctime=1)),

@@ -118,7 +118,8 @@ def _params3d(**kw):
     return Params3D(**base)
 
 
-@pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=2), dict(xper=0, left=5), dict(xper=0, right=1),
+# right 5 at nx 64 > ny 32: its wave reads x(j, nx) of the (nx, ny) grid
+@pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=2), dict(xper=0, left=6), dict(xper=0, right=1),
                                  dict(xper=0, right=5), dict(xper=0, right=9), dict(xper=0, left=0, right=4),
                                  dict(xper=0, right=7, nx=20, ny=24), dict(yper=2), dict(navier=0), dict(wall=0), dict(wallt=2),
                                  dict(top=2), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),

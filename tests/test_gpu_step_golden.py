@@ -136,12 +136,14 @@ def test_reference_test2d_fixture(cuda):
 
 
 @pytest.mark.parametrize("name", ["step3d_open", "step3d_open_wave", "step3d_open_eig", "step3d_open_hold",
+                                  "step3d_open_acoustic", "step3d_open_acoustic_both",
                                   "step3d_sym_left", "step3d_sym_both", "step3d_sym_smooth"])
 def test_step3d_nonperiodic_xi_matches_reference_golden(cuda, name):
     """A non-periodic xi direction: the boundary-closure rows of the xi LHS
-    (src/lhsbt1f3d.f90), the zero-disturbance, incoming-wave and
-    eigenfunction inflow planes, the zero-disturbance, eigenfunction and
-    held outflow planes (src/itrbc3d.f90:203-414, src/rhsbc3d.f90:167-324,
+    (src/lhsbt1f3d.f90), the zero-disturbance, incoming-wave,
+    eigenfunction and acoustic inflow planes, the zero-disturbance,
+    eigenfunction, acoustic and held outflow planes
+    (src/itrbc3d.f90:203-414, src/rhsbc3d.f90:167-324,
     src/lhsbc1f3d.f90:412-448), the symmetry planes (mirrored stencils,
     src/lhsbs1f3d.f90) and the cpenta2bc-factored xi sweep."""
     import sys
