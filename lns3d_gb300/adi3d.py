@@ -46,9 +46,10 @@ class ImpDrv3D:
     (src/impdrv3d.f90:130-199).  ispg, spg, spg2: the sponge (0 none, 1 spg, > 4
     spg + spg2; src/lrhs3d.f90:220-240), spg and spg2 (nx, ny) arrays.
     eps_e, buff: explicit smoother and implicit damping (src/smoother3d.f90),
-    buff (nx, ny) or None for the reference's default of ones.  ispg 2, 3
-    and the forced top (params top = 1) take the x coordinates x (nx, ny),
-    x0 and wamp (nx; None: ones); ispg 4 the complex target cvic (5, nx, ny).
+    buff (nx, ny) or None for the reference's default of ones.  ispg 2, 3,
+    the forced top (params top = 1) and, with xper = 0, the wave planes
+    (left 1 or 5, right 5) take the x coordinates x (nx, ny), x0 and wamp
+    (nx; None: ones); ispg 4 the complex target cvic (5, nx, ny).
     wall = 3 (the bump) takes u1w, u2w, u3w, tw, twp as bump, complex (5, nx).
     row_pairs: FP64 periodic lines with an odd band advance their recurrences
     two rows per step (lns_ctx3d_set_row_pairs); False keeps them row by
