@@ -73,9 +73,15 @@ int lns_lin2d_create(const lns_params3d* p, lns_lin2d** out) {
   if (p->beta != 0.0 || p->omega != 0.0)
     return lns_fail(LNS_ERR_ARG, "lin2d_create: a 2D linear run has beta = 0 and omega = 0 (Lz = 0 in the deck)");
   if (p->precision != LNS_FP64) return lns_fail(LNS_ERR_ARG, "lin2d_create: precision must be LNS_FP64");
-  // the linear 2D planes of a non-periodic xi direction (src/rhsbc.f90:182-253,
-  // src/itrbc.f90:300-620) differ from the 3D step's and are not built
-  if (p->xper != 1) return lns_fail(LNS_ERR_ARG, "lin2d_create: the linear 2D step needs xper = 1");
+  // a non-periodic xi direction: the zero-disturbance planes (left 0, right 0:
+  // v = 0, r = 0 and identity rows in both LHS, src/itrbc.f90:310-316,534-540,
+  // src/rhsbc.f90:189-191,238-240, src/lhsbc1f.f90:108-115,183-190,
+  // src/lhsbc2f.f90:124-131,164-171) are the single-mode step's.  The linear
+  // 2D branches' other planes (left 1-7, right 1 and 3) differ from it (the
+  // time-dependent characteristic inflows, no identity row for left 5, the
+  // unmirrored symmetry plane) and are not built.
+  if (p->xper != 1 && !(p->xper == 0 && p->left == 0 && p->right == 0))
+    return lns_fail(LNS_ERR_ARG, "lin2d_create: the linear 2D step needs xper = 1, or xper = 0 with left 0 and right 0");
   lns_lin2d* c = new lns_lin2d();
   int rc = lns_ctx3d_create(p, &c->ctx);
   c->nx = p->nx;

@@ -69,6 +69,12 @@ GOLDEN = {
                         dict(nsteps=10, cflmax=20.0, loctime=1)),
     "step3d_sym_smooth": ("3dopen", dict(nx=40, ny=33, seed=9, left=7, right=7),
                           dict(nsteps=10, cflmax=20.0, loctime=1, eps_e=0.01)),
+    # the linear 2D step with a non-periodic xi direction: the zero-
+    # disturbance planes (left 0, right 0), at CFL 2 (at CFL 20 the reference
+    # built with FMA contraction differs from itself by 1.2e-12 after ten
+    # steps, at CFL 2 by 5e-15)
+    "step2d_lin_open": ("2dlinopen", dict(nx=48, ny=33, seed=12, beta=0.0, omega=0.0, left=0, right=0),
+                        dict(nsteps=10, cflmax=2.0, loctime=1)),
     # the nonlinear 2D step with a non-periodic xi direction: Riemann planes
     # on both sides; the symmetry plane on the left with the right plane
     # extrapolated (zeroth order) over a viscous layer that itrBC moves
@@ -150,6 +156,8 @@ def generate(name):
         v, hist, run = refcase.run2dlin(shear_layer(**cargs), nsteps, **rargs)
     elif kind == "3dopen":
         v, hist, run = refcase.run3d(open_layer(**cargs), nsteps, **rargs)
+    elif kind == "2dlinopen":
+        v, hist, run = refcase.run2dlin(open_layer(**cargs), nsteps, **rargs)
     elif kind == "2dopen":
         v, hist, run = refcase.run2d(vortex2d_open(**cargs), nsteps, **rargs)
     else:

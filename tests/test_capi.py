@@ -219,9 +219,12 @@ def test_server3d_argument_errors(lib):
     assert lib.lns_server3d_bytes_in_use(None) == 0
 
 
-@pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1), dict(xper=0, left=0, right=0)])
+@pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1), dict(xper=0, left=7, right=0),
+                                 dict(xper=0, left=4, right=0), dict(xper=0, left=5, right=0),
+                                 dict(xper=0, left=0, right=1), dict(xper=0, left=0, right=7)])
 def test_lin2d_rejects_single_mode_options(lib, bad):
-    """The linear 2D context takes beta = omega = 0, FP64 and a periodic xi direction."""
+    """The linear 2D context takes beta = omega = 0, FP64 and a periodic xi
+    direction or the zero-disturbance planes (left 0, right 0)."""
     ctx = ctypes.c_void_p()
     base = dict(beta=0.0, omega=0.0)
     base.update(bad)

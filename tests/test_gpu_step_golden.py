@@ -103,6 +103,28 @@ def test_linear_2d_step_matches_reference_golden(cuda):
     assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
 
 
+def test_linear_2d_open_xi_matches_reference_golden(cuda):
+    """The linear 2D step with a non-periodic xi direction and its zero-
+    disturbance planes (left 0, right 0: src/itrbc.f90:310-316, 534-540,
+    src/rhsbc.f90:189-191, 238-240, src/lhsbc1f.f90:108-115, 183-190,
+    src/lhsbc2f.f90:124-131, 164-171) with the boundary-closure xi rows."""
+    import sys
+
+    from lns3d_gb300 import ImpDrvLin2D
+
+    sys.path.insert(0, GOLDEN)
+    import gen_step_golden
+
+    kind, cargs, rargs, d = golden("step2d_lin_open")
+    case = gen_step_golden.open_layer(**cargs)
+    drv = ImpDrvLin2D(case["params"], case["metrics"], case["vm"], cflmax=rargs["cflmax"], loctime=rargs["loctime"])
+    v = np.asfortranarray(case["v"].real)
+    drv.itrbc(v)
+    res = drv.step(v, nsteps=rargs["nsteps"])
+    assert rel(v, d["v"]) < STATE_TOL, rel(v, d["v"])
+    assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
+
+
 def test_reference_test2d_fixture(cuda):
     """The reference's own test/2d case (its grid, metric, mean and initial
     files, its deck lns3d.inp): 10 steps of the linear 2D step through the
