@@ -511,8 +511,10 @@ int lns_get_field3d(lns_ctx3d* ctx, int32_t which, double* out);
  * single-mode context at beta = omega = 0 (the options it supports, FP64)
  * and converts the state: v(5,nx,ny) is real here.  Sequence:
  *   lns_lin2d_create(params with beta = omega = 0)   deck values; xper = 1, or xper = 0 with
- *                                                    left 0 and right 0 (the zero-disturbance
- *                                                    planes, src/itrbc.f90:310-316, 534-540)
+ *                                                    left 0 (zero disturbance) or 7 (symmetry
+ *                                                    plane: the mirrored stencils, and v = 0 and
+ *                                                    r = 0 for the second velocity component,
+ *                                                    src/itrbc.f90:525-527) and right 0
  *   lns_upload_metrics_lin2d, lns_upload_mean_lin2d  metric.dat, mean.dat
  *   lns_itrbc_lin2d_dev                              the itrBC before the loop (src/impdrv.f90:160)
  *   lns_step_lin2d / _dev                            nsteps steps of niter correctors

@@ -717,6 +717,7 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
         r[m] = cd{-(w.x - T[m].x), -(w.y - T[m].y)};
       }
     }
+    if (!g.xper && i == 1 && g.left == kLinSymLeft) r[2] = cd{0.0, 0.0};
     if (g.xper && i == g.nx)
       #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
@@ -804,6 +805,8 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
     if (!g.xper && i == g.nx && (g.right == 4 || g.right == 5))
       for (int jj = 1; jj <= g.ny; ++jj)
         for (int m = 0; m < 5; ++m) W(m, jj) = reinterpret_cast<const cd*>(tright)[m + 5 * (jj - 1)];
+    if (!g.xper && i == 1 && g.left == kLinSymLeft)
+      for (int jj = 1; jj <= g.ny; ++jj) W(2, jj) = cd{0.0, 0.0};
   } else if (g.xper) {
     const int j = t - ncol + 2;
     if (j <= g.ny - 1)
@@ -1450,9 +1453,16 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
 
 }  // namespace
 
+int lns_ctx3d_create_planes(const lns_params3d* p, lns_ctx3d** out, bool lin2d_planes);
+
 extern "C" {
 
-int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
+int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) { return lns_ctx3d_create_planes(p, out, false); }
+
+}  // extern "C"
+
+// lin2d_planes: the linear 2D context's plane codes are accepted as well
+int lns_ctx3d_create_planes(const lns_params3d* p, lns_ctx3d** out, bool lin2d_planes) {
   if (!p || !out) return fail3(LNS_ERR_ARG, "ctx3d_create: null argument");
   *out = nullptr;
   if (p->nx < 8 || p->ny < 7) return fail3(LNS_ERR_ARG, "ctx3d_create: need nx >= 8 and ny >= 7");
@@ -1461,7 +1471,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   if (!(p->dxi > 0.0) || !(p->deta > 0.0)) return fail3(LNS_ERR_ARG, "ctx3d_create: dxi and deta must be > 0");
   if (p->xper != 0 && p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: xper must be 0 or 1");
   if (!p->xper) {
-    if (p->left != 0 && p->left != 1 && p->left != 4 && p->left != 5 && p->left != 7)
+    if (p->left != 0 && p->left != 1 && p->left != 4 && p->left != 5 && p->left != 7 &&
+        !(lin2d_planes && p->left == lns::a3::kLinSymLeft))
       return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1, 4, 5 or 7 (xper = 0)");
     if (p->right != 0 && p->right != 4 && p->right != 5 && p->right != 7 && p->right != 8)
       return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4, 5, 7 or 8 (xper = 0)");
@@ -1469,7 +1480,7 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
     if (p->right == 5 && p->ny < p->nx) return fail3(LNS_ERR_ARG, "ctx3d_create: right 5 needs ny >= nx");
     // the symmetric xi LHS rows read ABhi through a (6,ny,nx) view of the (6,nx,ny) array
     // (src/lhsbs1f3d.f90:17), which stays inside it only when ny <= nx
-    if ((p->left == 7 || p->right == 7) && p->ny > p->nx)
+    if ((p->left == 7 || p->left == lns::a3::kLinSymLeft || p->right == 7) && p->ny > p->nx)
       return fail3(LNS_ERR_ARG, "ctx3d_create: symmetry planes (left or right 7) need ny <= nx");
     // the reference reads the eigenfunction only for left 4 (src/gendist.f90:18)
     if (p->right == 4 && p->left != 4) return fail3(LNS_ERR_ARG, "ctx3d_create: right 4 needs left 4");
@@ -1620,6 +1631,8 @@ int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) {
   *out = c;
   return LNS_OK;
 }
+
+extern "C" {
 
 int lns_ctx3d_destroy(lns_ctx3d* c) {
   if (!c) return LNS_OK;

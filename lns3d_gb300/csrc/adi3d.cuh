@@ -71,9 +71,17 @@ struct Grid {
   double dxinv, dyinv, dxsinv, dysinv;
 };
 
+// The left plane code of the linear 2D step's symmetry plane (its left 7):
+// the mirrored stencils and symmetric xi LHS rows of left 7 (src/grad.f90:155
+// with lsym from src/input.f90:235, src/lhsbt1f.f90:30-32), and besides v = 0
+// and r = 0 for the second velocity component on column 1
+// (src/itrbc.f90:525-527, src/rhsbc.f90:229-231).  Only the linear 2D
+// context sets it.
+constexpr int kLinSymLeft = 17;
+
 // symmetry planes of the xi lines (left / right 7), the d1_at / d2_at sym bits
 __host__ __device__ __forceinline__ int xsym(const Grid& g) {
-  return g.xper ? 0 : (g.left == 7 ? 1 : 0) | (g.right == 7 ? 2 : 0);
+  return g.xper ? 0 : (g.left == 7 || g.left == kLinSymLeft ? 1 : 0) | (g.right == 7 ? 2 : 0);
 }
 
 // true when every interior stencil of g has zero outermost coefficients

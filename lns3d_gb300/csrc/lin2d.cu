@@ -18,10 +18,11 @@
 #include <string>
 
 #include "../../include/lns3d_gb300.h"
-#include "scalar.cuh"
+#include "adi3d.cuh"
 
 int lns_fail(int code, const std::string& msg);
 int lns_cuda_fail(cudaError_t e, const char* where);
+int lns_ctx3d_create_planes(const lns_params3d* p, lns_ctx3d** out, bool lin2d_planes);
 
 struct lns_lin2d {
   lns_ctx3d* ctx = nullptr;
@@ -76,14 +77,20 @@ int lns_lin2d_create(const lns_params3d* p, lns_lin2d** out) {
   // a non-periodic xi direction: the zero-disturbance planes (left 0, right 0:
   // v = 0, r = 0 and identity rows in both LHS, src/itrbc.f90:310-316,534-540,
   // src/rhsbc.f90:189-191,238-240, src/lhsbc1f.f90:108-115,183-190,
-  // src/lhsbc2f.f90:124-131,164-171) are the single-mode step's.  The linear
-  // 2D branches' other planes (left 1-7, right 1 and 3) differ from it (the
-  // time-dependent characteristic inflows, no identity row for left 5, the
-  // unmirrored symmetry plane) and are not built.
-  if (p->xper != 1 && !(p->xper == 0 && p->left == 0 && p->right == 0))
-    return lns_fail(LNS_ERR_ARG, "lin2d_create: the linear 2D step needs xper = 1, or xper = 0 with left 0 and right 0");
+  // src/lhsbc2f.f90:124-131,164-171) are the single-mode step's; the
+  // symmetry plane (left 7) is the single-mode step's left 7 with v = 0 and
+  // r = 0 for the second velocity component on the plane, the single-mode
+  // context's plane lns::a3::kLinSymLeft.  The linear 2D branches' other
+  // planes (left 1-6, right 1 and 3) differ from the single-mode step's (the
+  // time-dependent characteristic inflows, no identity row for left 5) and
+  // are not built.
+  if (p->xper != 1 && !(p->xper == 0 && (p->left == 0 || p->left == 7) && p->right == 0))
+    return lns_fail(LNS_ERR_ARG,
+                    "lin2d_create: the linear 2D step needs xper = 1, or xper = 0 with left 0 or 7 and right 0");
   lns_lin2d* c = new lns_lin2d();
-  int rc = lns_ctx3d_create(p, &c->ctx);
+  lns_params3d q3 = *p;
+  if (!p->xper && p->left == 7) q3.left = lns::a3::kLinSymLeft;
+  int rc = lns_ctx3d_create_planes(&q3, &c->ctx, true);
   c->nx = p->nx;
   c->ny = p->ny;
   void* q = nullptr;

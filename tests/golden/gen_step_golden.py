@@ -75,6 +75,9 @@ GOLDEN = {
     # steps, at CFL 2 by 5e-15)
     "step2d_lin_open": ("2dlinopen", dict(nx=48, ny=33, seed=12, beta=0.0, omega=0.0, left=0, right=0),
                         dict(nsteps=10, cflmax=2.0, loctime=1)),
+    # its symmetry plane (left 7: no mirrored stencils, v = 0 on the plane)
+    "step2d_lin_sym": ("2dlinopen", dict(nx=48, ny=33, seed=13, beta=0.0, omega=0.0, left=7, right=0),
+                       dict(nsteps=10, cflmax=2.0, loctime=1)),
     # the nonlinear 2D step with a non-periodic xi direction: Riemann planes
     # on both sides; the symmetry plane on the left with the right plane
     # extrapolated (zeroth order) over a viscous layer that itrBC moves

@@ -121,6 +121,7 @@ def _params3d(**kw):
 # right 5 at nx 64 > ny 32: its wave reads x(j, nx) of the (nx, ny) grid
 @pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=2), dict(xper=0, left=6), dict(xper=0, right=1),
                                  dict(xper=0, right=5), dict(xper=0, right=9), dict(xper=0, left=0, right=4),
+                                 dict(xper=0, left=17),
                                  dict(xper=0, right=7, nx=20, ny=24), dict(yper=2), dict(navier=0), dict(wall=0), dict(wallt=2),
                                  dict(top=2), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
                                  dict(loctime=2), dict(ispg=-1), dict(yper=1, ny=7), dict(yper=1, top=1),
@@ -219,12 +220,14 @@ def test_server3d_argument_errors(lib):
     assert lib.lns_server3d_bytes_in_use(None) == 0
 
 
-@pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1), dict(xper=0, left=7, right=0),
+@pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1), dict(xper=0, left=2, right=0),
                                  dict(xper=0, left=4, right=0), dict(xper=0, left=5, right=0),
-                                 dict(xper=0, left=0, right=1), dict(xper=0, left=0, right=7)])
+                                 dict(xper=0, left=17, right=0), dict(xper=0, left=0, right=1),
+                                 dict(xper=0, left=0, right=7)])
 def test_lin2d_rejects_single_mode_options(lib, bad):
     """The linear 2D context takes beta = omega = 0, FP64 and a periodic xi
-    direction or the zero-disturbance planes (left 0, right 0)."""
+    direction, or the zero-disturbance (left 0) or symmetry (left 7) plane
+    with the zero-disturbance right plane."""
     ctx = ctypes.c_void_p()
     base = dict(beta=0.0, omega=0.0)
     base.update(bad)

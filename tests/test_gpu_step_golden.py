@@ -103,11 +103,15 @@ def test_linear_2d_step_matches_reference_golden(cuda):
     assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
 
 
-def test_linear_2d_open_xi_matches_reference_golden(cuda):
-    """The linear 2D step with a non-periodic xi direction and its zero-
+@pytest.mark.parametrize("name", ["step2d_lin_open", "step2d_lin_sym"])
+def test_linear_2d_open_xi_matches_reference_golden(cuda, name):
+    """The linear 2D step with a non-periodic xi direction: the zero-
     disturbance planes (left 0, right 0: src/itrbc.f90:310-316, 534-540,
     src/rhsbc.f90:189-191, 238-240, src/lhsbc1f.f90:108-115, 183-190,
-    src/lhsbc2f.f90:124-131, 164-171) with the boundary-closure xi rows."""
+    src/lhsbc2f.f90:124-131, 164-171) with the boundary-closure xi rows, and
+    the symmetry plane (left 7: mirrored stencils, src/grad.f90:155-249, the
+    symmetric rows of src/lhsbs1f.f90, v = 0 and r = 0 for the second
+    velocity component, src/itrbc.f90:525-527, src/rhsbc.f90:229-231)."""
     import sys
 
     from lns3d_gb300 import ImpDrvLin2D
@@ -115,7 +119,7 @@ def test_linear_2d_open_xi_matches_reference_golden(cuda):
     sys.path.insert(0, GOLDEN)
     import gen_step_golden
 
-    kind, cargs, rargs, d = golden("step2d_lin_open")
+    kind, cargs, rargs, d = golden(name)
     case = gen_step_golden.open_layer(**cargs)
     drv = ImpDrvLin2D(case["params"], case["metrics"], case["vm"], cflmax=rargs["cflmax"], loctime=rargs["loctime"])
     v = np.asfortranarray(case["v"].real)
