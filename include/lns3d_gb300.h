@@ -511,10 +511,15 @@ int lns_get_field3d(lns_ctx3d* ctx, int32_t which, double* out);
  * single-mode context at beta = omega = 0 (the options it supports, FP64)
  * and converts the state: v(5,nx,ny) is real here.  Sequence:
  *   lns_lin2d_create(params with beta = omega = 0)   deck values; xper = 1, or xper = 0 with
- *                                                    left 0 (zero disturbance) or 7 (symmetry
- *                                                    plane: the mirrored stencils, and v = 0 and
- *                                                    r = 0 for the second velocity component,
- *                                                    src/itrbc.f90:525-527) and right 0
+ *                                                    left 0 (zero disturbance), 1 (nonreflecting)
+ *                                                    or 7 (symmetry plane: the mirrored stencils,
+ *                                                    and v = 0 and r = 0 for the second velocity
+ *                                                    component, src/itrbc.f90:525-527) and right
+ *                                                    0 or 1 (nonreflecting)
+ *   lns_lin2d_set_nbl                                the &extras namelist's nbl (default 0): the
+ *                                                    nonreflecting planes tie the density to the
+ *                                                    outgoing characteristic on rows j > nbl
+ *                                                    (src/itrbc.f90:340-342, src/rhsbc.f90:195)
  *   lns_upload_metrics_lin2d, lns_upload_mean_lin2d  metric.dat, mean.dat
  *   lns_itrbc_lin2d_dev                              the itrBC before the loop (src/impdrv.f90:160)
  *   lns_step_lin2d / _dev                            nsteps steps of niter correctors
@@ -523,6 +528,7 @@ typedef struct lns_lin2d lns_lin2d;
 int lns_lin2d_create(const lns_params3d* params, lns_lin2d** ctx);
 int lns_lin2d_destroy(lns_lin2d* ctx);
 size_t lns_lin2d_bytes(const lns_lin2d* ctx);
+int lns_lin2d_set_nbl(lns_lin2d* ctx, int32_t nbl);
 int lns_upload_metrics_lin2d(lns_lin2d* ctx, const double* metrics);
 int lns_upload_mean_lin2d(lns_lin2d* ctx, const double* vm, double* cfl);
 int lns_itrbc_lin2d_dev(lns_lin2d* ctx, double* v, void* stream);

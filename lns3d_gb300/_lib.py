@@ -82,6 +82,7 @@ SIGNATURES = {
     "lns_get_field3d": [P, I32, DP],
     "lns_lin2d_create": [P, P],
     "lns_lin2d_destroy": [P],
+    "lns_lin2d_set_nbl": [P, I32],
     "lns_upload_metrics_lin2d": [P, DP],
     "lns_upload_mean_lin2d": [P, DP, DP],
     "lns_itrbc_lin2d_dev": [P, DP, P],

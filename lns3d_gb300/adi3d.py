@@ -371,9 +371,11 @@ class ImpDrvLin2D:
 
     params: as ImpDrv3D's, with kz = 0 and omega = 0 (a deck with Lz = 0);
     metrics: the ten (nx, ny) arrays; vm: (5, nx, ny) mean flow.  The
-    context runs the single-mode machinery at kz = omega = 0."""
+    context runs the single-mode machinery at kz = omega = 0.  nbl: the
+    &extras namelist's nbl for the nonreflecting planes (left 1, right 1),
+    which act on rows j > nbl."""
 
-    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, impl=1, ispg=0, eps_e=0.0):
+    def __init__(self, params, metrics, vm, cflmax=1.0, dtmax=1e30, loctime=1, impl=1, ispg=0, eps_e=0.0, nbl=0):
         p = params
         if p.get("kz", 0.0) != 0.0 or p.get("omega", 0.0) != 0.0:
             raise ValueError("a 2D linear run has kz = 0 and omega = 0")
@@ -386,6 +388,8 @@ class ImpDrvLin2D:
                        left=p.get("left", -1), right=p.get("right", -1))
         self._ctx = ctypes.c_void_p()
         check(lib().lns_lin2d_create(ctypes.byref(prm), ctypes.byref(self._ctx)), "lns_lin2d_create")
+        if nbl:
+            check(lib().lns_lin2d_set_nbl(self._ctx, int(nbl)), "lns_lin2d_set_nbl")
         m = np.empty((self.nx, self.ny, 10), order="F")
         for k, name in enumerate(METRICS):
             m[:, :, k] = metrics[name]

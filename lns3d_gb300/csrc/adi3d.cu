@@ -327,6 +327,20 @@ __global__ void lhs_kernel(Grid g, Ops o, int dir, LhsCoef lc, T* __restrict__ m
   const int i = (int)(p32 - jm * (unsigned)g.nx) + 1, j = (int)jm + 1;
   const cd one{1.0, 0.0}, zero{0.0, 0.0};
   const cd ident = (k == 3 && a == b) ? one : zero;
+  // the linear 2D nonreflecting planes' density rows (j > nbl): in the xi LHS
+  // -rho + (gamma Ma rho_m sqrt(T_m) / T_m) u - (rho_m / T_m) T; right 1 writes
+  // that row into column 1 as well (src/lhsbc1f.f90:194-198, after the left
+  // plane, so it also replaces a zero-disturbance left plane's row there); in
+  // the eta LHS the identity row; these follow the wall and top rows and the
+  // other xi plane rows
+  if (!g.xper && a == 1 && j > g.nbl &&
+      ((i == 1 && (g.left == kLinNrLeft || (dir == 1 && g.right == kLinNrRight))) ||
+       (i == g.nx && g.right == kLinNrRight))) {
+    if (dir == 2) return store_el(mat, q, ident);
+    const double* F = (i == 1 ? o.tleft : o.tright) + 4 * (j - 1);
+    const double val = k != 3 ? 0.0 : b == 1 ? -1.0 : b == 2 ? F[0] / F[2] : b == 5 ? -F[1] / F[2] : 0.0;
+    return store_el(mat, q, cd{val, 0.0});
+  }
   // the xi boundaries of a non-periodic xi direction (src/lhsbc1f3d.f90:412-448,
   // src/lhsbc2f3d.f90:146-174); they follow the wall and top rows, so the
   // corners take them
@@ -471,6 +485,24 @@ __global__ void plane5_target_kernel(Grid g, int col, const double* __restrict__
   o[2] = cd{0.0, 0.0};
   o[3] = cd{0.0, 0.0};
   o[4] = cd{(gm2 * cs * 0.5 - m[4] * 0.5 * cs / cm2) / m[0], (gm2 * sn * 0.5 - m[4] * 0.5 * sn / cm2) / m[0]};
+}
+
+// The mean-flow factors of the linear 2D nonreflecting plane at column col
+// (kLinNrLeft / kLinNrRight), each formed as the reference's expressions
+// are: gamma Ma rho_m sqrt(T_m) (src/rhsbc.f90:195-197, src/lhsbc1f.f90:121),
+// rho_m, T_m, and gamma Ma^2 rho_m c_m with c_m = sqrt(T_m) / Ma on the left
+// and (1 / Ma) sqrt(T_m) on the right (src/itrbc.f90:322, 546, 340, 559).
+__global__ void nr_coef_kernel(Grid g, int col, const double* __restrict__ vm, double* __restrict__ f) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > g.ny) return;
+  const double* m = vm + 5 * pix(g, col, j);
+  const double rho = m[0], t = m[4];
+  const double cm = col == 1 ? sqrt(t) / g.Ma : 1.0 / g.Ma * sqrt(t);
+  double* o = f + 4 * (j - 1);
+  o[0] = g.gamma * g.Ma * rho * sqrt(t);
+  o[1] = rho;
+  o[2] = t;
+  o[3] = g.gamma * (g.Ma * g.Ma) * rho * cm;
 }
 
 // -------------------------------------------------------------------- RHS
@@ -718,6 +750,12 @@ __device__ __forceinline__ void rhs_body(const Grid& g, const Ops& o, const cd* 
       }
     }
     if (!g.xper && i == 1 && g.left == kLinSymLeft) r[2] = cd{0.0, 0.0};
+    // the linear 2D nonreflecting planes: r(1) = rho - (gamma Ma rho_m sqrt(T_m) u - rho_m T) / T_m
+    if (!g.xper && j > g.nbl && ((i == 1 && g.left == kLinNrLeft) || (i == g.nx && g.right == kLinNrRight))) {
+      const double* F = (i == 1 ? o.tleft : o.tright) + 4 * (j - 1);
+      const cd w1 = vs[0 + 5 * p], w2 = vs[1 + 5 * p], w5 = vs[4 + 5 * p];
+      r[0] = cd{w1.x - (F[0] * w2.x - F[1] * w5.x) / F[2], w1.y - (F[0] * w2.y - F[1] * w5.y) / F[2]};
+    }
     if (g.xper && i == g.nx)
       #pragma unroll
       for (int m = 0; m < 5; ++m) r[m] = cd{0.0, 0.0};
@@ -807,6 +845,15 @@ __device__ __forceinline__ void bc_body(const Grid& g, cd* __restrict__ v, const
         for (int m = 0; m < 5; ++m) W(m, jj) = reinterpret_cast<const cd*>(tright)[m + 5 * (jj - 1)];
     if (!g.xper && i == 1 && g.left == kLinSymLeft)
       for (int jj = 1; jj <= g.ny; ++jj) W(2, jj) = cd{0.0, 0.0};
+    // the linear 2D nonreflecting planes: rho = (gamma Ma^2 rho_m c_m u - rho_m T) / T_m on rows j > nbl
+    if (!g.xper && ((i == 1 && g.left == kLinNrLeft) || (i == g.nx && g.right == kLinNrRight))) {
+      const double* F = i == 1 ? tleft : tright;
+      for (int jj = g.nbl + 1; jj <= g.ny; ++jj) {
+        const double* f = F + 4 * (jj - 1);
+        const cd u = W(1, jj), t = W(4, jj);
+        W(0, jj) = cd{(f[3] * u.x - f[1] * t.x) / f[2], (f[3] * u.y - f[1] * t.y) / f[2]};
+      }
+    }
   } else if (g.xper) {
     const int j = t - ncol + 2;
     if (j <= g.ny - 1)
@@ -1455,6 +1502,15 @@ int run_steps(lns_ctx3d* c, cd* v, int nsteps, int niter, double* totres_dev, cu
 
 int lns_ctx3d_create_planes(const lns_params3d* p, lns_ctx3d** out, bool lin2d_planes);
 
+// the rows j <= nbl that the linear 2D nonreflecting planes leave alone
+int lns_ctx3d_set_nbl(lns_ctx3d* c, int nbl) {
+  if (!c) return fail3(LNS_ERR_ARG, "set_nbl: null context");
+  if (nbl < 0 || nbl > c->g.ny) return fail3(LNS_ERR_ARG, "set_nbl: nbl must be in 0..ny");
+  c->g.nbl = nbl;
+  c->factored = false;
+  return LNS_OK;
+}
+
 extern "C" {
 
 int lns_ctx3d_create(const lns_params3d* p, lns_ctx3d** out) { return lns_ctx3d_create_planes(p, out, false); }
@@ -1472,9 +1528,10 @@ int lns_ctx3d_create_planes(const lns_params3d* p, lns_ctx3d** out, bool lin2d_p
   if (p->xper != 0 && p->xper != 1) return fail3(LNS_ERR_ARG, "ctx3d_create: xper must be 0 or 1");
   if (!p->xper) {
     if (p->left != 0 && p->left != 1 && p->left != 4 && p->left != 5 && p->left != 7 &&
-        !(lin2d_planes && p->left == lns::a3::kLinSymLeft))
+        !(lin2d_planes && (p->left == lns::a3::kLinSymLeft || p->left == lns::a3::kLinNrLeft)))
       return fail3(LNS_ERR_ARG, "ctx3d_create: left must be 0, 1, 4, 5 or 7 (xper = 0)");
-    if (p->right != 0 && p->right != 4 && p->right != 5 && p->right != 7 && p->right != 8)
+    if (p->right != 0 && p->right != 4 && p->right != 5 && p->right != 7 && p->right != 8 &&
+        !(lin2d_planes && p->right == lns::a3::kLinNrRight))
       return fail3(LNS_ERR_ARG, "ctx3d_create: right must be 0, 4, 5, 7 or 8 (xper = 0)");
     // right 5's wave reads x(j,nx) of the (nx,ny) array (src/rhsbc3d.f90:299), inside it only when ny >= nx
     if (p->right == 5 && p->ny < p->nx) return fail3(LNS_ERR_ARG, "ctx3d_create: right 5 needs ny >= nx");
@@ -1562,6 +1619,12 @@ int lns_ctx3d_create_planes(const lns_params3d* p, lns_ctx3d** out, bool lin2d_p
     c->tleft = (double*)q;
   }
   if (!p->xper && (p->right == 4 || p->right == 5)) { A(sizeof(double) * 10 * p->ny, &q); c->tright = (double*)q; }
+  // the linear 2D nonreflecting planes' factors; right 1 also writes column 1's row
+  if (!p->xper && (p->left == lns::a3::kLinNrLeft || p->right == lns::a3::kLinNrRight)) {
+    A(sizeof(double) * 4 * p->ny, &q);
+    c->tleft = (double*)q;
+  }
+  if (!p->xper && p->right == lns::a3::kLinNrRight) { A(sizeof(double) * 4 * p->ny, &q); c->tright = (double*)q; }
   if (p->wall == 3) { A(sizeof(double) * 10 * p->nx, &q); c->bump = (double*)q; }
   if (p->eps_e != 0.0) { A(sizeof(double) * np, &q); c->buff = (double*)q; }
   if (mixed) { A(sizeof(cf) * 5 * np, &q); c->r32 = (cf*)q; }
@@ -1840,6 +1903,18 @@ int lns_upload_mean3d(lns_ctx3d* c, const double* vm, double* cfl) {
   if (cfl) *cfl = h;
   c->have_mean = true;
   c->factored = false;
+  if (!c->prm.xper && (c->prm.left == lns::a3::kLinNrLeft || c->prm.right == lns::a3::kLinNrRight)) {
+    const unsigned nbj = (unsigned)((g.ny + 127) / 128);
+    lns::a3::nr_coef_kernel<<<nbj, 128>>>(g, 1, c->vm, c->tleft);
+    c->ops.tleft = c->tleft;
+    if (c->prm.right == lns::a3::kLinNrRight) {
+      lns::a3::nr_coef_kernel<<<nbj, 128>>>(g, g.nx, c->vm, c->tright);
+      c->ops.tright = c->tright;
+    }
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda3(e, "nr_coef_kernel");
+  }
   return make_inflow_target(c);
 }
 

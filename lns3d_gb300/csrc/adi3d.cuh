@@ -67,6 +67,7 @@ struct Grid {
   double Ma, Re, Pr, gamma, gamma1, omega, kz, alfa;
   int xper, yper, navier, wall, wallt, top;
   int left = -1, right = -1;             // xi boundaries when xper = 0 (7: symmetry plane)
+  int nbl = 0;                           // the linear 2D nonreflecting planes act on rows j > nbl
   double gx[6], gy[6], dx2[7], dy2[7];   // interior first / second derivative stencils (src/cgrad*.f90)
   double dxinv, dyinv, dxsinv, dysinv;
 };
@@ -78,6 +79,16 @@ struct Grid {
 // (src/itrbc.f90:525-527, src/rhsbc.f90:229-231).  Only the linear 2D
 // context sets it.
 constexpr int kLinSymLeft = 17;
+// The plane codes of the linear 2D step's nonreflecting planes (its left 1
+// and right 1, src/itrbc.f90:318-346, 542-566, src/rhsbc.f90:193-201,
+// 242-250, src/lhsbc1f.f90:117-139, 192-221, src/lhsbc2f.f90:133-144,
+// 173-184): on rows j > nbl, the density row ties rho to the outgoing
+// characteristic, rho = (gamma Ma^2 rho_m c_m u - rho_m T) / T_m; the other
+// rows keep the one-sided stencils and closure rows.  The per-row mean-flow
+// factors are kept in tleft (column 1) and tright (column nx) as
+// (gamma Ma rho_m sqrt(T_m), rho_m, T_m, gamma Ma^2 rho_m c_m).  Only the
+// linear 2D context sets them.
+constexpr int kLinNrLeft = 11, kLinNrRight = 21;
 
 // symmetry planes of the xi lines (left / right 7), the d1_at / d2_at sym bits
 __host__ __device__ __forceinline__ int xsym(const Grid& g) {

@@ -23,6 +23,7 @@
 int lns_fail(int code, const std::string& msg);
 int lns_cuda_fail(cudaError_t e, const char* where);
 int lns_ctx3d_create_planes(const lns_params3d* p, lns_ctx3d** out, bool lin2d_planes);
+int lns_ctx3d_set_nbl(lns_ctx3d* c, int nbl);
 
 struct lns_lin2d {
   lns_ctx3d* ctx = nullptr;
@@ -80,16 +81,21 @@ int lns_lin2d_create(const lns_params3d* p, lns_lin2d** out) {
   // src/lhsbc2f.f90:124-131,164-171) are the single-mode step's; the
   // symmetry plane (left 7) is the single-mode step's left 7 with v = 0 and
   // r = 0 for the second velocity component on the plane, the single-mode
-  // context's plane lns::a3::kLinSymLeft.  The linear 2D branches' other
-  // planes (left 1-6, right 1 and 3) differ from the single-mode step's (the
-  // time-dependent characteristic inflows, no identity row for left 5) and
-  // are not built.
-  if (p->xper != 1 && !(p->xper == 0 && (p->left == 0 || p->left == 7) && p->right == 0))
+  // context's plane lns::a3::kLinSymLeft; the nonreflecting planes (left 1,
+  // right 1) are its planes kLinNrLeft and kLinNrRight.  The linear 2D
+  // branches' other planes (left 2-6, right 3) are not built: left 2
+  // extrapolates column 1 from columns 2-5 after their wall rows are set, left
+  // 3 and right 3 (Giles) and left 4 are time-dependent characteristic
+  // inflows, and left 5 keeps the interior LHS row.
+  if (p->xper != 1 && !(p->xper == 0 && (p->left == 0 || p->left == 1 || p->left == 7) &&
+                        (p->right == 0 || p->right == 1)))
     return lns_fail(LNS_ERR_ARG,
-                    "lin2d_create: the linear 2D step needs xper = 1, or xper = 0 with left 0 or 7 and right 0");
+                    "lin2d_create: the linear 2D step needs xper = 1, or xper = 0 with left 0, 1 or 7 and right 0 or 1");
   lns_lin2d* c = new lns_lin2d();
   lns_params3d q3 = *p;
   if (!p->xper && p->left == 7) q3.left = lns::a3::kLinSymLeft;
+  if (!p->xper && p->left == 1) q3.left = lns::a3::kLinNrLeft;
+  if (!p->xper && p->right == 1) q3.right = lns::a3::kLinNrRight;
   int rc = lns_ctx3d_create_planes(&q3, &c->ctx, true);
   c->nx = p->nx;
   c->ny = p->ny;
@@ -116,6 +122,11 @@ int lns_lin2d_destroy(lns_lin2d* c) {
 }
 
 size_t lns_lin2d_bytes(const lns_lin2d* c) { return c ? c->bytes + lns_ctx3d_bytes(c->ctx) : 0; }
+
+int lns_lin2d_set_nbl(lns_lin2d* c, int32_t nbl) {
+  if (!c) return lns_fail(LNS_ERR_ARG, "lin2d_set_nbl: null context");
+  return lns_ctx3d_set_nbl(c->ctx, nbl);
+}
 
 int lns_upload_metrics_lin2d(lns_lin2d* c, const double* metrics) {
   if (!c) return lns_fail(LNS_ERR_ARG, "upload_metrics_lin2d: null context");

@@ -78,6 +78,14 @@ GOLDEN = {
     # its symmetry plane (left 7: no mirrored stencils, v = 0 on the plane)
     "step2d_lin_sym": ("2dlinopen", dict(nx=48, ny=33, seed=13, beta=0.0, omega=0.0, left=7, right=0),
                        dict(nsteps=10, cflmax=2.0, loctime=1)),
+    # its nonreflecting planes (left 1, right 1) above the &extras nbl, at
+    # CFL 0.5 (with the left plane the reference's step grows the state by
+    # two orders a step at CFL 2); right 1 also writes column 1's density
+    # row, in the second case over a zero-disturbance left plane
+    "step2d_lin_nr": ("2dlinopen", dict(nx=48, ny=33, seed=14, beta=0.0, omega=0.0, left=1, right=1),
+                      dict(nsteps=10, cflmax=0.5, loctime=1, module=dict(nbl=4))),
+    "step2d_lin_nr_right": ("2dlinopen", dict(nx=48, ny=33, seed=15, beta=0.0, omega=0.0, left=0, right=1),
+                            dict(nsteps=10, cflmax=2.0, loctime=1)),
     # the nonlinear 2D step with a non-periodic xi direction: Riemann planes
     # on both sides; the symmetry plane on the left with the right plane
     # extrapolated (zeroth order) over a viscous layer that itrBC moves

@@ -124,9 +124,11 @@ def run2d(case, nsteps, module=None, **kw):
     return v, history(r.path("output.h.1")), r
 
 
-def run2dlin(case, nsteps, **kw):
+def run2dlin(case, nsteps, module=None, **kw):
     """The reference's linear impdrv (linear = 1, Lz = 0: src/lrhs.f90) on
-    the real part of the case's state: (final v, totres history, Run)."""
+    the real part of the case's state: (final v, totres history, Run);
+    module: variables of the program's modules set before the run (the
+    &extras namelist's nbl)."""
     p = case["params"]
     r = Run()
     refio.write_grid(r.path("grid.dat"), case["x"], case["y"])
@@ -136,6 +138,6 @@ def run2dlin(case, nsteps, **kw):
                       Pr=p["Pr"])
     d = dict(omega=0.0, Lz=0.0)
     d.update(kw)
-    r.run(deck3d(case, nsteps, **d))
+    r.run(deck3d(case, nsteps, **d), module=module)
     _, v, _ = refio.read_field(r.last_restart())
     return v, history(r.path("output.h.1")), r

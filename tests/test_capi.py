@@ -121,7 +121,7 @@ def _params3d(**kw):
 # right 5 at nx 64 > ny 32: its wave reads x(j, nx) of the (nx, ny) grid
 @pytest.mark.parametrize("bad", [dict(xper=2), dict(xper=0, left=2), dict(xper=0, left=6), dict(xper=0, right=1),
                                  dict(xper=0, right=5), dict(xper=0, right=9), dict(xper=0, left=0, right=4),
-                                 dict(xper=0, left=17),
+                                 dict(xper=0, left=17), dict(xper=0, left=11), dict(xper=0, right=21),
                                  dict(xper=0, right=7, nx=20, ny=24), dict(yper=2), dict(navier=0), dict(wall=0), dict(wallt=2),
                                  dict(top=2), dict(nx=7), dict(ny=6), dict(precision=2), dict(dxi=0.0),
                                  dict(loctime=2), dict(ispg=-1), dict(yper=1, ny=7), dict(yper=1, top=1),
@@ -152,6 +152,7 @@ def test_ctx3d_null_arguments(lib):
     assert lib.lns_upload_sponge_target3d(None, None) == 1
     assert lib.lns_upload_bump3d(None, None) == 1
     assert lib.lns_upload_profile3d(None, None, None, 0.0, 0.0) == 1
+    assert lib.lns_lin2d_set_nbl(None, 0) == 1
 
 
 def _params2d(**kw):
@@ -221,13 +222,15 @@ def test_server3d_argument_errors(lib):
 
 
 @pytest.mark.parametrize("bad", [dict(beta=0.2), dict(omega=0.05), dict(precision=1), dict(xper=0, left=2, right=0),
-                                 dict(xper=0, left=4, right=0), dict(xper=0, left=5, right=0),
-                                 dict(xper=0, left=17, right=0), dict(xper=0, left=0, right=1),
-                                 dict(xper=0, left=0, right=7)])
+                                 dict(xper=0, left=3, right=0), dict(xper=0, left=4, right=0),
+                                 dict(xper=0, left=5, right=0), dict(xper=0, left=11, right=0),
+                                 dict(xper=0, left=17, right=0), dict(xper=0, left=0, right=3),
+                                 dict(xper=0, left=0, right=7), dict(xper=0, left=0, right=21)])
 def test_lin2d_rejects_single_mode_options(lib, bad):
     """The linear 2D context takes beta = omega = 0, FP64 and a periodic xi
-    direction, or the zero-disturbance (left 0) or symmetry (left 7) plane
-    with the zero-disturbance right plane."""
+    direction, or the zero-disturbance (left 0), nonreflecting (left 1) or
+    symmetry (left 7) plane with the zero-disturbance or nonreflecting right
+    plane (right 0, 1)."""
     ctx = ctypes.c_void_p()
     base = dict(beta=0.0, omega=0.0)
     base.update(bad)

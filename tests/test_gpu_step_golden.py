@@ -103,7 +103,7 @@ def test_linear_2d_step_matches_reference_golden(cuda):
     assert np.abs(np.asarray(res) - d["hist"]).max() <= RES_TOL * d["hist"].max()
 
 
-@pytest.mark.parametrize("name", ["step2d_lin_open", "step2d_lin_sym"])
+@pytest.mark.parametrize("name", ["step2d_lin_open", "step2d_lin_sym", "step2d_lin_nr", "step2d_lin_nr_right"])
 def test_linear_2d_open_xi_matches_reference_golden(cuda, name):
     """The linear 2D step with a non-periodic xi direction: the zero-
     disturbance planes (left 0, right 0: src/itrbc.f90:310-316, 534-540,
@@ -111,7 +111,10 @@ def test_linear_2d_open_xi_matches_reference_golden(cuda, name):
     src/lhsbc2f.f90:124-131, 164-171) with the boundary-closure xi rows, and
     the symmetry plane (left 7: mirrored stencils, src/grad.f90:155-249, the
     symmetric rows of src/lhsbs1f.f90, v = 0 and r = 0 for the second
-    velocity component, src/itrbc.f90:525-527, src/rhsbc.f90:229-231)."""
+    velocity component, src/itrbc.f90:525-527, src/rhsbc.f90:229-231), and
+    the nonreflecting planes (left 1, right 1: the density row above nbl,
+    src/itrbc.f90:318-346, 542-566, src/rhsbc.f90:193-201, 242-250,
+    src/lhsbc1f.f90:117-139, 192-221, src/lhsbc2f.f90:133-144, 173-184)."""
     import sys
 
     from lns3d_gb300 import ImpDrvLin2D
@@ -121,7 +124,8 @@ def test_linear_2d_open_xi_matches_reference_golden(cuda, name):
 
     kind, cargs, rargs, d = golden(name)
     case = gen_step_golden.open_layer(**cargs)
-    drv = ImpDrvLin2D(case["params"], case["metrics"], case["vm"], cflmax=rargs["cflmax"], loctime=rargs["loctime"])
+    drv = ImpDrvLin2D(case["params"], case["metrics"], case["vm"], cflmax=rargs["cflmax"], loctime=rargs["loctime"],
+                      nbl=rargs.get("module", {}).get("nbl", 0))
     v = np.asfortranarray(case["v"].real)
     drv.itrbc(v)
     res = drv.step(v, nsteps=rargs["nsteps"])
