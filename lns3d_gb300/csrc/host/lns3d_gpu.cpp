@@ -386,12 +386,18 @@ int main(int argc, char** argv) {
     p.xper = in.xper; p.yper = in.yper; p.navier = in.navier;
     p.wall = in.wall; p.wallt = in.wallt; p.top = in.top; p.optx = in.optx; p.opty = in.opty;
     p.precision = LNS_FP64; p.impl = in.impl; p.ispg = 0; p.eps_e = in.eps_e;
+    p.left = in.left; p.right = in.right;
     double cfl = 0.0;
     std::vector<double> dtl(np);
     if (complex_run) {
+      // the eigenfunction planes read inflow.dat and the inflow namelist (src/gendist.f90)
+      if (!in.xper && in.left == 4) die("the eigenfunction planes (left 4) are not set up by this driver");
       lns_ctx3d* c = nullptr;
       check(lns_ctx3d_create(&p, &c), "lns_ctx3d_create");
       check(lns_upload_metrics3d(c, metrics.data()), "lns_upload_metrics3d");
+      // the forced top and the wave planes form their waves from x and x0 (wamp: ones)
+      if (in.top == 1 || (!in.xper && (in.left == 1 || in.left == 5 || in.right == 5)))
+        check(lns_upload_inflow3d(c, x.data(), nullptr, in.x0), "lns_upload_inflow3d");
       check(lns_upload_mean3d(c, vm.data(), &cfl), "lns_upload_mean3d");
       check(lns_get_field3d(c, 8, dtl.data()), "lns_get_field3d");
       const double delt = min_of(dtl);
@@ -427,6 +433,8 @@ int main(int argc, char** argv) {
     }
   } else {
     if (complex_run) die("3D code must be linear");  // src/lns3d.f90:173
+    // the Riemann planes read left.pot / right.pot and the &extras namelist's nbl
+    if (!in.xper) die("a non-periodic xi direction of the nonlinear 2D step is not set up by this driver");
     lns_params2d p{};
     p.nx = nx; p.ny = ny; p.dxi = dxi; p.deta = deta;
     p.Ma = in.Ma; p.Re = in.Re; p.Pr = in.Pr; p.gamma = gamma; p.gamma1 = gamma1;
